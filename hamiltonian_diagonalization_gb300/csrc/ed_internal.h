@@ -1,0 +1,163 @@
+// Internal declarations shared by the translation units of libedgb300.
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ed_capi.h"
+
+namespace edgb {
+
+// Largest orbital count of the device path: the two-table rank splits a word
+// into a low and a high half of at most 20 bits each, and the per-hop tables
+// must fit in shared memory.
+constexpr int kMaxOrbitals = 40;
+constexpr uint64_t kMiss = ~0ull;             // FindFockStateIndex miss code
+constexpr double kSparseZeroTol = 1e-14;      // hamiltonian_data.hpp:53
+constexpr double kCgEps = 1e-12;              // clebsch_gordan_coefficients.hpp:53
+
+struct Error : std::runtime_error {
+    ed_status code;
+    Error(ed_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& msg);
+// Number of kernels this library has launched (all devices, all threads).
+void count_launch();
+uint64_t launch_count();
+
+#define ED_CUDA(x)                                                                            \
+    do {                                                                                      \
+        cudaError_t _e = (x);                                                                 \
+        if (_e != cudaSuccess) {                                                              \
+            throw ::edgb::Error(_e == cudaErrorMemoryAllocation ? ED_ERR_OOM : ED_ERR_CUDA,     \
+                                std::string(#x) + ": " + cudaGetErrorString(_e));             \
+        }                                                                                     \
+    } while (0)
+
+#define ED_REQUIRE(cond, code, msg)                                                           \
+    do {                                                                                      \
+        if (!(cond)) throw ::edgb::Error((code), (msg));                                      \
+    } while (0)
+
+// Owning device buffer.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t count) { alloc(count); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count) {
+        release();
+        if (count) ED_CUDA(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)));
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// ------------------------------------------------------------ host tables
+
+// Quartic term tables as the reference keeps them (QuarticTermTables) plus
+// the derived per-hop table the device kernels read.
+struct HopTables {
+    int K = 0;
+    // pair sums s = a+b (a<b) run over 1..2K-3; pairs of sum s are
+    // (a, s-a) for a = lo(s) .. lo(s)+cnt(s)-1 with lo(s) = max(0, s-K+1).
+    std::vector<int> hop_off;     // size 2K: offset of the cnt(s)^2 block of sum s
+    std::vector<double> w;        // per (pair_in, pair_out) element value, 0 if dropped
+    std::vector<double> diag_a;   // K*K: first  diagonal term of ordered pair (k4,k3)
+    std::vector<double> diag_b;   // K*K: second diagonal term of ordered pair (k4,k3)
+};
+
+uint64_t binomial_u64(int n, int k);
+void coulomb_pseudopotentials(int norb, double* out);
+double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM);
+void quartic_tables(int norb, const double* pp, int npp, uint16_t* ktab, double* vtab);
+HopTables derive_hop_tables(int norb, const uint16_t* ktab, const double* vtab);
+
+// Symmetric eigen-decomposition of a dense m x m matrix (row-major, both
+// triangles filled).  evals ascending; evecs column-major (evecs[i + m*j] =
+// component i of eigenvector j).
+void sym_eigen(int m, const std::vector<double>& a, std::vector<double>& evals, std::vector<double>& evecs);
+
+// ------------------------------------------------------------- pair indexing
+
+// Helpers shared by host and device code for the per-hop table layout.
+#if defined(__CUDACC__)
+#define ED_HD __host__ __device__ __forceinline__
+#else
+#define ED_HD inline
+#endif
+
+ED_HD int pair_lo(int s, int K) { return s - (K - 1) > 0 ? s - (K - 1) : 0; }
+ED_HD int pair_cnt(int s, int K) {
+    int hi = (s - 1) / 2;                 // largest a with a < s-a
+    int lo = pair_lo(s, K);
+    return hi >= lo ? hi - lo + 1 : 0;
+}
+
+}  // namespace edgb
+
+// ------------------------------------------------------------ handle types
+
+struct ed_basis {
+    int N = 0, norb = 0, two_lz = 0;
+    int64_t sector_sum = -1;     // sum of occupied positions in the sector (-1: empty)
+    uint64_t dim = 0;
+    int low_bits = 0, high_bits = 0;
+    edgb::DevBuf<uint64_t> words;   // dim ascending words
+    edgb::DevBuf<uint64_t> hi;      // 2^high_bits: (class << 48) | offset
+    edgb::DevBuf<uint64_t> lo;      // 2^low_bits : (class << 32) | rank in class
+};
+
+struct ed_terms {
+    int norb = 0;
+    std::vector<uint16_t> ktab;
+    std::vector<double> vtab;
+    edgb::HopTables hop;
+    edgb::DevBuf<double> w_dev;       // hop.w
+    edgb::DevBuf<int> hop_off_dev;    // hop.hop_off
+    edgb::DevBuf<double> diag_a_dev;  // hop.diag_a
+    edgb::DevBuf<double> diag_b_dev;  // hop.diag_b
+};
+
+struct ed_crs {
+    int64_t n = 0, nnz = 0;
+    int upper = 0;
+    int max_row = 0;
+    edgb::DevBuf<int64_t> rowptr;
+    edgb::DevBuf<int32_t> col;
+    edgb::DevBuf<double> val;
+};
+
+// ----------------------------------------------------- device-side entry points
+namespace edgb {
+void basis_build(ed_basis& b, cudaStream_t st);
+void basis_rank(const ed_basis& b, const uint64_t* words, uint64_t* idx, uint64_t m, cudaStream_t st);
+void terms_upload(ed_terms& t);
+void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream_t st);
+void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, cudaStream_t st);
+void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st);
+void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const double* x, double* y,
+                cudaStream_t st);
+void exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);
+int64_t reduce_max_i64_host(const int64_t* in, int64_t n, cudaStream_t st);
+}  // namespace edgb

@@ -1,0 +1,665 @@
+// Thick-restart Lanczos with full FP64 reorthogonalisation on the device
+// (K7 vector kernels, K8 projected eigenproblem on the host, K9 residuals).
+//
+// Stands in for ArpackWrapper::DiagonalizeSymmetricMatrix<double>
+// (utilities/wrappers/arpack_wrapper.hpp:595-937), which runs ARPACK's
+// implicitly restarted Arnoldi (pdnaupd_/pdneupd_, WHICH="SR",
+// NCV = min(N, 2*NEV+21), 2000 iterations) with MatrixVectorFunction::Simple
+// as the reverse-communication product.  Here the Krylov basis lives in HBM,
+// every vector operation is a device kernel, and the host only sees the
+// small projected matrix once per restart cycle.
+//
+// One Lanczos step j (v_j = V[:,j], w written into V[:,j+1]):
+//   w = H v_j
+//   local three-term step  alpha = v_j.w ; w -= alpha v_j + beta_{j-1} v_{j-1}
+//   full Gram-Schmidt pass c = V[:,0..j]^T w ; w -= V c  (the projections are
+//   added to column j of the projected matrix), second pass when the norm
+//   dropped below 1/sqrt(2) of its value before the pass (DGKS test), and
+//   always on the first step of a cycle, where the thick-restart arrow makes
+//   the local step inapplicable;
+//   beta_j = ||w|| ; v_{j+1} = w / beta_j.
+// After m steps the m x m projected matrix is diagonalised on the host, the
+// residual of Ritz pair i is |beta_{m-1} y_{m-1,i}|, and the cycle restarts
+// from the k lowest Ritz vectors plus v_m (Wu & Simon's thick restart).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ed_lanczos.h"
+
+namespace edgb {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kJT = 8;               // columns per tile in the multi-dot
+constexpr double kDgksEta = 0.7071067811865476;
+
+int sm_count()
+{
+    int dev = 0, s = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return s;
+}
+
+// Block-wide sum of kThreads doubles held one per thread; result in thread 0.
+__device__ __forceinline__ double block_sum(double v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (warp == 0) {
+        t = lane < (kThreads / 32) ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 4; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    __syncthreads();
+    return t;
+}
+
+// Row range of block b when n rows are cut into nb contiguous chunks.
+__device__ __forceinline__ void chunk(int64_t n, int nb, int b, int64_t& r0, int64_t& r1)
+{
+    r0 = n * (int64_t)b / nb;
+    r1 = n * (int64_t)(b + 1) / nb;
+}
+
+// part[0*nb+b] = sum x.y, part[1*nb+b] = sum y.y over block b's rows.
+__global__ void __launch_bounds__(kThreads) k_dot2(const double* __restrict__ x, const double* __restrict__ y,
+                                                   int64_t n, double* __restrict__ part, const int* __restrict__ stop)
+{
+    if (stop && *stop) return;
+    __shared__ double red[kThreads / 32];
+    int64_t r0, r1;
+    chunk(n, gridDim.x, blockIdx.x, r0, r1);
+    double a = 0.0, b = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+        const double yr = y[r];
+        a = fma(x[r], yr, a);
+        b = fma(yr, yr, b);
+    }
+    a = block_sum(a, red);
+    b = block_sum(b, red);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = a;
+        part[gridDim.x + blockIdx.x] = b;
+    }
+}
+
+// Local step scalars: alpha = sum part[0..nb) (column j's diagonal),
+// ||H v_j||^2 = sum part[nb..2nb); beta_{j-1} enters column j at row j-1.
+__global__ void k_local_finalize(const double* __restrict__ part, int nb, double* __restrict__ coefcol, int j,
+                                 const double* __restrict__ beta_prev, double* __restrict__ hvnorm2,
+                                 const int* __restrict__ stop)
+{
+    if (stop && *stop) return;
+    __shared__ double red[kThreads / 32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < nb; i += kThreads) { a += part[i]; b += part[nb + i]; }
+    a = block_sum(a, red);
+    b = block_sum(b, red);
+    if (threadIdx.x == 0) {
+        coefcol[j] = a;
+        coefcol[j - 1] = *beta_prev;
+        *hvnorm2 = b;
+    }
+}
+
+// w -= alpha v_j + beta_{j-1} v_{j-1}
+__global__ void __launch_bounds__(kThreads) k_axpy2(double* __restrict__ w, const double* __restrict__ vj,
+                                                    const double* __restrict__ vjm1, int64_t n,
+                                                    const double* __restrict__ alpha, const double* __restrict__ beta,
+                                                    const int* __restrict__ stop)
+{
+    if (stop && *stop) return;
+    const double a = *alpha, b = *beta;
+    for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads)
+        w[r] = fma(-b, vjm1[r], fma(-a, vj[r], w[r]));
+}
+
+// Multi-dot: part[i*nb + b] = V[:,i].w over block b's rows for i < J, and
+// part[J*nb + b] = w.w.  run == nullptr or *run != 0 to execute.
+__global__ void __launch_bounds__(kThreads) k_mdot(const double* __restrict__ V, int64_t n, int J,
+                                                   const double* __restrict__ w, double* __restrict__ part,
+                                                   const int* __restrict__ run, const int* __restrict__ stop)
+{
+    if ((run && !*run) || (stop && *stop)) return;
+    __shared__ double red[kJT][kThreads + 1];
+    int64_t r0, r1;
+    chunk(n, gridDim.x, blockIdx.x, r0, r1);
+    const int nb = gridDim.x;
+    for (int j0 = 0; j0 <= J; j0 += kJT) {
+        double acc[kJT];
+#pragma unroll
+        for (int t = 0; t < kJT; ++t) acc[t] = 0.0;
+        const int jn = min(kJT, J + 1 - j0);
+        for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+            const double wr = w[r];
+#pragma unroll
+            for (int t = 0; t < kJT; ++t) {
+                const int i = j0 + t;
+                if (t < jn) {
+                    const double vv = (i < J) ? V[(int64_t)i * n + r] : wr;
+                    acc[t] = fma(vv, wr, acc[t]);
+                }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < kJT; ++t) red[t][threadIdx.x] = acc[t];
+        __syncthreads();
+        // warp t sums column t: 8 values per lane, then 5 shuffles
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (warp < jn) {
+            double s = 0.0;
+#pragma unroll
+            for (int q = 0; q < kThreads / 32; ++q) s += red[warp][q * 32 + lane];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) part[(int64_t)(j0 + warp) * nb + blockIdx.x] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// c[i] = sum_b part[i*nb+b] for i < J, coefcol[i] += c[i]; norm2 before the
+// pass (index J) to *before.
+__global__ void k_mdot_finalize(const double* __restrict__ part, int nb, int J, double* __restrict__ c,
+                                double* __restrict__ coefcol, double* __restrict__ before,
+                                const int* __restrict__ run, const int* __restrict__ stop)
+{
+    if ((run && !*run) || (stop && *stop)) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarp = blockDim.x >> 5;
+    for (int i = warp; i <= J; i += nwarp) {
+        double s = 0.0;
+        for (int b = lane; b < nb; b += 32) s += part[(int64_t)i * nb + b];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            if (i < J) {
+                c[i] = s;
+                coefcol[i] += s;
+            } else {
+                *before = s;
+            }
+        }
+    }
+}
+
+// w -= V[:,0..J) c ; npart[b] = ||w||^2 over block b's rows.
+__global__ void __launch_bounds__(kThreads) k_update(const double* __restrict__ V, int64_t n, int J,
+                                                     const double* __restrict__ c, double* __restrict__ w,
+                                                     double* __restrict__ npart, const int* __restrict__ run,
+                                                     const int* __restrict__ stop)
+{
+    if ((run && !*run) || (stop && *stop)) return;
+    extern __shared__ double sc[];
+    __shared__ double red[kThreads / 32];
+    for (int i = threadIdx.x; i < J; i += kThreads) sc[i] = -c[i];
+    __syncthreads();
+    int64_t r0, r1;
+    chunk(n, gridDim.x, blockIdx.x, r0, r1);
+    double nn = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+        double acc = w[r];
+        int i = 0;
+        for (; i + 4 <= J; i += 4) {
+            const double v0 = V[(int64_t)i * n + r], v1 = V[(int64_t)(i + 1) * n + r];
+            const double v2 = V[(int64_t)(i + 2) * n + r], v3 = V[(int64_t)(i + 3) * n + r];
+            acc = fma(sc[i], v0, acc);
+            acc = fma(sc[i + 1], v1, acc);
+            acc = fma(sc[i + 2], v2, acc);
+            acc = fma(sc[i + 3], v3, acc);
+        }
+        for (; i < J; ++i) acc = fma(sc[i], V[(int64_t)i * n + r], acc);
+        w[r] = acc;
+        nn = fma(acc, acc, nn);
+    }
+    nn = block_sum(nn, red);
+    if (threadIdx.x == 0) npart[blockIdx.x] = nn;
+}
+
+// beta = ||w|| after a pass.  With need2 != nullptr (first pass) also set
+// the second-pass flag: forced, or the DGKS test ||w_after|| < eta ||w_before||.
+__global__ void k_norm_finalize(const double* __restrict__ npart, int nb, const double* __restrict__ before,
+                                double* __restrict__ beta, int* __restrict__ need2, int force2,
+                                const int* __restrict__ run, const int* __restrict__ stop)
+{
+    if ((run && !*run) || (stop && *stop)) return;
+    __shared__ double red[kThreads / 32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += kThreads) s += npart[i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) {
+        *beta = sqrt(s);
+        if (need2) *need2 = (force2 || s < kDgksEta * kDgksEta * (*before)) ? 1 : 0;
+    }
+}
+
+// Invariant subspace: the new direction vanished relative to ||H v_j||.
+__global__ void k_break_test(const double* __restrict__ beta, const double* __restrict__ ref2,
+                             int* __restrict__ stop, int j)
+{
+    if (*stop) return;
+    const double ref = sqrt(fmax(*ref2, 0.0));
+    if (!(*beta > 1e-12 * ref)) *stop = j + 1;
+}
+
+__global__ void __launch_bounds__(kThreads) k_scale(double* __restrict__ w, int64_t n,
+                                                    const double* __restrict__ beta, const int* __restrict__ stop)
+{
+    if (stop && *stop) return;
+    const double inv = 1.0 / *beta;
+    for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads)
+        w[r] *= inv;
+}
+
+// out[:, t] = sum_{i<m} V[:, i] Y[i, t] for t < k (Y column-major, ld m).
+constexpr int kGT = 16;
+__global__ void __launch_bounds__(kThreads) k_gemm_vy(const double* __restrict__ V, int64_t n, int m,
+                                                      const double* __restrict__ Y, int ldy, int k,
+                                                      double* __restrict__ out)
+{
+    extern __shared__ double sy[];   // m * kGT
+    for (int t0 = 0; t0 < k; t0 += kGT) {
+        const int tn = min(kGT, k - t0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < m * kGT; q += kThreads) {
+            const int i = q / kGT, t = q % kGT;
+            sy[q] = (t < tn) ? Y[(int64_t)(t0 + t) * ldy + i] : 0.0;
+        }
+        __syncthreads();
+        for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads) {
+            double acc[kGT];
+#pragma unroll
+            for (int t = 0; t < kGT; ++t) acc[t] = 0.0;
+            for (int i = 0; i < m; ++i) {
+                const double v = V[(int64_t)i * n + r];
+#pragma unroll
+                for (int t = 0; t < kGT; ++t) acc[t] = fma(v, sy[i * kGT + t], acc[t]);
+            }
+            for (int t = 0; t < tn; ++t) out[(int64_t)(t0 + t) * n + r] = acc[t];
+        }
+    }
+}
+
+// Seeded uniform(-1,1) vector (splitmix64 of seed and index).
+__global__ void k_random(double* __restrict__ v, int64_t n, uint64_t seed)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(r + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        v[r] = 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+    }
+}
+
+// res[i] = || y_i - lambda_i x_i ||^2 partials -> host sums
+__global__ void __launch_bounds__(kThreads) k_resid_part(const double* __restrict__ y, const double* __restrict__ x,
+                                                         double lambda, int64_t n, double* __restrict__ part)
+{
+    __shared__ double red[kThreads / 32];
+    int64_t r0, r1;
+    chunk(n, gridDim.x, blockIdx.x, r0, r1);
+    double s = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+        const double d = fma(-lambda, x[r], y[r]);
+        s = fma(d, d, s);
+    }
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+}  // namespace
+
+// -------------------------------------------------------------- operator
+
+void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st)
+{
+    switch (op.kind) {
+    case ed_op::CRS:
+        spmv(*op.crs, x, y, st);
+        break;
+    case ed_op::MATFREE:
+        hv_matfree(*op.basis, *op.terms, op.diag.p, x, y, st);
+        break;
+    case ed_op::HOST: {
+        std::vector<double>& hx = const_cast<std::vector<double>&>(op.hx);
+        std::vector<double>& hy = const_cast<std::vector<double>&>(op.hy);
+        ED_CUDA(cudaMemcpyAsync(hx.data(), x, (size_t)op.n * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        op.fn(hx.data(), hy.data(), op.user);
+        ED_CUDA(cudaMemcpyAsync(y, hy.data(), (size_t)op.n * 8, cudaMemcpyHostToDevice, st));
+        break;
+    }
+    }
+}
+
+// --------------------------------------------------------------- solver
+
+namespace {
+
+struct Work {
+    int64_t n = 0;
+    int m = 0;
+    int nb = 0;                      // blocks of the row-chunked reductions
+    DevBuf<double> V, V2;            // n x (m+1), column-major
+    DevBuf<double> part;             // (m+2) * nb
+    DevBuf<double> npart;            // nb
+    DevBuf<double> coef;             // (m+1) x (m+1); column j holds step j's projections
+    DevBuf<double> beta;             // m+2
+    DevBuf<double> c;                // m+2
+    DevBuf<double> junk;             // m+2, coefficient sink for host-side orthonormalisation
+    DevBuf<double> scal;             // [0] ||w||^2 before pass 1, [1] ||H v_j||^2, [2] before pass 2
+    DevBuf<int> flags;               // [0] second pass wanted, [1] breakdown step + 1
+    DevBuf<double> Y;                // m x m Ritz coefficients
+};
+
+double host_sum_parts(Work& w, const double* dev, int count, cudaStream_t st)
+{
+    std::vector<double> h(count);
+    ED_CUDA(cudaMemcpyAsync(h.data(), dev, (size_t)count * 8, cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    double s = 0.0;
+    for (int i = 0; i < count; ++i) s += h[i];
+    (void)w;
+    return s;
+}
+
+// Orthogonalise column `col` of V against columns [0, col) twice, then
+// normalise it.  Returns the norm before normalisation.
+double orthonormalise_column(Work& w, double* Vbase, int col, cudaStream_t st)
+{
+    double* x = Vbase + (int64_t)col * w.n;
+    if (col > 0) {
+        for (int pass = 0; pass < 2; ++pass) {
+            k_mdot<<<w.nb, kThreads, 0, st>>>(Vbase, w.n, col, x, w.part.p, nullptr, nullptr); ::edgb::count_launch();
+            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nb, col, w.c.p, w.junk.p, w.scal.p + 3, nullptr, nullptr); ::edgb::count_launch();
+            k_update<<<w.nb, kThreads, (size_t)col * 8, st>>>(Vbase, w.n, col, w.c.p, x, w.npart.p, nullptr, nullptr); ::edgb::count_launch();
+            ED_CUDA(cudaGetLastError());
+        }
+    }
+    k_dot2<<<w.nb, kThreads, 0, st>>>(x, x, w.n, w.part.p, nullptr); ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    const double nrm = std::sqrt(host_sum_parts(w, w.part.p, w.nb, st));
+    ED_REQUIRE(nrm > 0.0 && std::isfinite(nrm), ED_ERR_ARG, "start vector is zero or not finite");
+    ED_CUDA(cudaMemcpyAsync(w.beta.p + w.m + 1, &nrm, 8, cudaMemcpyHostToDevice, st));
+    k_scale<<<w.nb, kThreads, 0, st>>>(x, w.n, w.beta.p + w.m + 1, nullptr); ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    ED_CUDA(cudaStreamSynchronize(st));
+    return nrm;
+}
+
+void gemm_vy(const double* V, int64_t n, int m, const double* Ydev, int ldy, int k, double* out, cudaStream_t st)
+{
+    const size_t smem = (size_t)m * kGT * 8;
+    if (smem > 48 * 1024) ED_CUDA(cudaFuncSetAttribute(k_gemm_vy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_gemm_vy<<<sm_count() * 4, kThreads, smem, st>>>(V, n, m, Ydev, ldy, k, out); ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+void dense_solve(const ed_op& op, int nev, double* evals_host, double* evecs_dev, ed_solve_info* info,
+                 cudaStream_t st)
+{
+    const int64_t n = op.n;
+    DevBuf<double> X((size_t)n * n), HX((size_t)n * n);
+    std::vector<double> id((size_t)n * n, 0.0);
+    for (int64_t i = 0; i < n; ++i) id[(size_t)i * n + i] = 1.0;
+    ED_CUDA(cudaMemcpyAsync(X.p, id.data(), id.size() * 8, cudaMemcpyHostToDevice, st));
+    for (int64_t i = 0; i < n; ++i) op_apply(op, X.p + i * n, HX.p + i * n, st);
+    std::vector<double> hx((size_t)n * n);
+    ED_CUDA(cudaMemcpyAsync(hx.data(), HX.p, hx.size() * 8, cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    // column i of HX is H e_i; symmetrise against round-off
+    std::vector<double> A((size_t)n * n);
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = 0; j < n; ++j) A[(size_t)i * n + j] = 0.5 * (hx[(size_t)j * n + i] + hx[(size_t)i * n + j]);
+    std::vector<double> ev, vec;
+    sym_eigen((int)n, A, ev, vec);
+    for (int i = 0; i < nev; ++i) evals_host[i] = ev[i];
+    if (evecs_dev)
+        ED_CUDA(cudaMemcpyAsync(evecs_dev, vec.data(), (size_t)n * nev * 8, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    if (info) {
+        info->converged = nev;
+        info->matvecs = n;
+        info->max_residual = 0.0;
+    }
+}
+
+}  // namespace
+
+void residual_norms(const ed_op& op, const double* x, const double* lambda, int k, double* res, cudaStream_t st)
+{
+    const int64_t n = op.n;
+    DevBuf<double> y(n);
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
+    DevBuf<double> part(nb);
+    for (int i = 0; i < k; ++i) {
+        op_apply(op, x + (int64_t)i * n, y.p, st);
+        k_resid_part<<<nb, kThreads, 0, st>>>(y.p, x + (int64_t)i * n, lambda[i], n, part.p); ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
+        std::vector<double> h(nb);
+        ED_CUDA(cudaMemcpyAsync(h.data(), part.p, (size_t)nb * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        double s = 0.0;
+        for (double v : h) s += v;
+        res[i] = std::sqrt(s);
+    }
+}
+
+void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
+                   double* evecs_dev, ed_solve_info* info, cudaStream_t st)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const int64_t n = op.n;
+    const int nev = p.nev;
+    ED_REQUIRE(n >= 1, ED_ERR_EMPTY, "operator has dimension 0");
+    ED_REQUIRE(nev >= 1 && nev <= n, ED_ERR_ARG, "need 1 <= nev <= n");
+    const double tol = p.tol > 0 ? p.tol : 1e-10;
+    const int max_restarts = p.max_restarts > 0 ? p.max_restarts : 2000;
+    ed_solve_info inf;
+    std::memset(&inf, 0, sizeof(inf));
+
+    // The reference switches to dense LAPACK below dimension 60
+    // (pseudopotential_model_base.hpp:244-251); so do we.
+    if (n < 60 || n <= (int64_t)nev + 2) {
+        dense_solve(op, nev, evals_host, evecs_dev, &inf, st);
+        inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (info) *info = inf;
+        return;
+    }
+    int64_t m64 = p.ncv > 0 ? p.ncv : std::min<int64_t>(n, 2 * (int64_t)nev + 21);
+    m64 = std::max<int64_t>(m64, nev + 2);
+    m64 = std::min<int64_t>(m64, n - 1);
+    m64 = std::min<int64_t>(m64, 1000);
+    const int m = (int)m64;
+    ED_REQUIRE(m > nev, ED_ERR_ARG, "Krylov subspace must exceed nev");
+
+    Work w;
+    w.n = n;
+    w.m = m;
+    w.nb = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
+    w.V.alloc((size_t)n * (m + 1));
+    w.V2.alloc((size_t)n * (m + 1));
+    w.part.alloc((size_t)(m + 2) * w.nb);
+    w.npart.alloc(w.nb);
+    w.coef.alloc((size_t)(m + 1) * (m + 1));
+    w.beta.alloc(m + 2);
+    w.c.alloc(m + 2);
+    w.junk.alloc(m + 2);
+    w.scal.alloc(4);
+    w.flags.alloc(2);
+    w.Y.alloc((size_t)m * m);
+    ED_CUDA(cudaMemsetAsync(w.beta.p, 0, (m + 2) * 8, st));
+    ED_CUDA(cudaMemsetAsync(w.junk.p, 0, (m + 2) * 8, st));
+
+    if (v0_dev) ED_CUDA(cudaMemcpyAsync(w.V.p, v0_dev, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    else {
+        k_random<<<sm_count() * 4, kThreads, 0, st>>>(w.V.p, n, p.seed); ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
+    }
+    orthonormalise_column(w, w.V.p, 0, st);
+
+    std::vector<cudaEvent_t> ev(2 * (m + 1), nullptr);
+    for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
+    struct EvGuard {
+        std::vector<cudaEvent_t>& v;
+        ~EvGuard() { for (auto e : v) if (e) cudaEventDestroy(e); }
+    } evguard{ev};
+
+    std::vector<double> T((size_t)m * m, 0.0), coef_h((size_t)(m + 1) * (m + 1)), beta_h(m + 1);
+    std::vector<double> theta, Y, prev_theta;
+    int k = 0, m_eff = m;
+    double beta_last = 0.0;
+    bool converged = false;
+    double spmv_ms = 0.0;
+    for (;;) {
+        ED_CUDA(cudaMemsetAsync(w.flags.p, 0, 2 * sizeof(int), st));
+        ED_CUDA(cudaMemsetAsync(w.coef.p + (size_t)k * (m + 1), 0, (size_t)(m - k) * (m + 1) * 8, st));
+        int* need2 = w.flags.p;
+        int* stop = w.flags.p + 1;
+        for (int j = k; j < m; ++j) {
+            double* vj = w.V.p + (int64_t)j * n;
+            double* wv = w.V.p + (int64_t)(j + 1) * n;
+            double* coefcol = w.coef.p + (size_t)j * (m + 1);
+            const bool first = (j == k);
+            ED_CUDA(cudaEventRecord(ev[2 * j], st));
+            op_apply(op, vj, wv, st);
+            ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
+            ++inf.matvecs;
+            if (!first) {
+                k_dot2<<<w.nb, kThreads, 0, st>>>(vj, wv, n, w.part.p, stop); ::edgb::count_launch();
+                k_local_finalize<<<1, kThreads, 0, st>>>(w.part.p, w.nb, coefcol, j, w.beta.p + (j - 1), w.scal.p + 1,
+                                                        stop); ::edgb::count_launch();
+                k_axpy2<<<w.nb, kThreads, 0, st>>>(wv, vj, w.V.p + (int64_t)(j - 1) * n, n, coefcol + j,
+                                                   w.beta.p + (j - 1), stop); ::edgb::count_launch();
+            }
+            const int J = j + 1;
+            k_mdot<<<w.nb, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, nullptr, stop); ::edgb::count_launch();
+            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nb, J, w.c.p, coefcol, w.scal.p, nullptr, stop); ::edgb::count_launch();
+            k_update<<<w.nb, kThreads, (size_t)J * 8, st>>>(w.V.p, n, J, w.c.p, wv, w.npart.p, nullptr, stop); ::edgb::count_launch();
+            k_norm_finalize<<<1, kThreads, 0, st>>>(w.npart.p, w.nb, w.scal.p, w.beta.p + j, need2, first ? 1 : 0,
+                                                    nullptr, stop); ::edgb::count_launch();
+            k_mdot<<<w.nb, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, need2, stop); ::edgb::count_launch();
+            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nb, J, w.c.p, coefcol, w.scal.p + 2, need2, stop); ::edgb::count_launch();
+            k_update<<<w.nb, kThreads, (size_t)J * 8, st>>>(w.V.p, n, J, w.c.p, wv, w.npart.p, need2, stop); ::edgb::count_launch();
+            k_norm_finalize<<<1, kThreads, 0, st>>>(w.npart.p, w.nb, w.scal.p + 2, w.beta.p + j, nullptr, 0, need2,
+                                                    stop); ::edgb::count_launch();
+            k_break_test<<<1, 1, 0, st>>>(w.beta.p + j, first ? w.scal.p : w.scal.p + 1, stop, j); ::edgb::count_launch();
+            k_scale<<<w.nb, kThreads, 0, st>>>(wv, n, w.beta.p + j, stop); ::edgb::count_launch();
+            ED_CUDA(cudaGetLastError());
+        }
+        int hstop = 0;
+        ED_CUDA(cudaMemcpyAsync(&hstop, stop, sizeof(int), cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaMemcpyAsync(coef_h.data(), w.coef.p, coef_h.size() * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaMemcpyAsync(beta_h.data(), w.beta.p, (size_t)(m + 1) * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        for (int j = k; j < m; ++j) {
+            float ms = 0.f;
+            ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * j], ev[2 * j + 1]));
+            spmv_ms += ms;
+        }
+        m_eff = hstop ? hstop : m;
+        if (hstop) ++inf.breakdowns;
+        for (int j = k; j < m_eff; ++j)
+            for (int i = 0; i <= j; ++i) {
+                const double v = coef_h[(size_t)j * (m + 1) + i];
+                T[(size_t)i * m + j] = v;
+                T[(size_t)j * m + i] = v;
+            }
+        std::vector<double> Tm((size_t)m_eff * m_eff);
+        for (int i = 0; i < m_eff; ++i)
+            for (int j = 0; j < m_eff; ++j) Tm[(size_t)i * m_eff + j] = T[(size_t)i * m + j];
+        sym_eigen(m_eff, Tm, theta, Y);
+        beta_last = hstop ? 0.0 : beta_h[m - 1];
+        int nconv = 0;
+        double maxres = 0.0;
+        const int want = std::min(nev, m_eff);
+        for (int i = 0; i < want; ++i) {
+            const double r = std::fabs(beta_last * Y[(size_t)(m_eff - 1) + (size_t)m_eff * i]);
+            maxres = std::max(maxres, r);
+            if (r <= tol) ++nconv;
+        }
+        inf.converged = nconv;
+        inf.max_residual = maxres;
+        // After a breakdown the Ritz pairs are exact but a fresh direction may
+        // still uncover more copies of a degenerate eigenvalue: accept only
+        // once a cycle leaves the nev lowest values unchanged, or when the
+        // whole space has been spanned.
+        bool stable = !hstop || (int64_t)m_eff >= n;
+        if (hstop && !stable && (int)prev_theta.size() >= nev && m_eff >= nev) {
+            stable = true;
+            for (int i = 0; i < nev; ++i)
+                if (std::fabs(theta[i] - prev_theta[i]) > tol * std::max(1.0, std::fabs(theta[i]))) stable = false;
+        }
+        prev_theta.assign(theta.begin(), theta.begin() + std::min<int>(nev, (int)theta.size()));
+        if (m_eff >= nev && nconv == nev && stable) {
+            converged = true;
+            break;
+        }
+        if (inf.restarts >= max_restarts) break;
+        ++inf.restarts;
+        // thick restart from the kk lowest Ritz vectors
+        int kk = std::min(m - 2, nev + std::max(1, (m - nev) / 2));
+        kk = std::max(kk, std::min(nev, m - 1));
+        if (hstop) kk = std::min(kk, m_eff);
+        ED_CUDA(cudaMemcpyAsync(w.Y.p, Y.data(), (size_t)m_eff * m_eff * 8, cudaMemcpyHostToDevice, st));
+        gemm_vy(w.V.p, n, m_eff, w.Y.p, m_eff, kk, w.V2.p, st);
+        if (!hstop) {
+            ED_CUDA(cudaMemcpyAsync(w.V2.p + (int64_t)kk * n, w.V.p + (int64_t)m * n, (size_t)n * 8,
+                                    cudaMemcpyDeviceToDevice, st));
+        } else {
+            k_random<<<sm_count() * 4, kThreads, 0, st>>>(w.V2.p + (int64_t)kk * n, n,
+                                                         p.seed + 0x51ED2701ull * (uint64_t)inf.restarts); ::edgb::count_launch();
+            ED_CUDA(cudaGetLastError());
+            orthonormalise_column(w, w.V2.p, kk, st);
+        }
+        std::swap(w.V, w.V2);
+        std::fill(T.begin(), T.end(), 0.0);
+        for (int i = 0; i < kk; ++i) {
+            T[(size_t)i * m + i] = theta[i];
+            if (!hstop) {
+                const double s = beta_last * Y[(size_t)(m_eff - 1) + (size_t)m_eff * i];
+                T[(size_t)i * m + kk] = s;
+                T[(size_t)kk * m + i] = s;
+            }
+        }
+        k = kk;
+        ED_CUDA(cudaStreamSynchronize(st));
+    }
+    for (int i = 0; i < nev; ++i) evals_host[i] = theta[i];
+    DevBuf<double> xtmp;
+    double* X = evecs_dev;
+    if (!X && p.verify) {
+        xtmp.alloc((size_t)n * nev);
+        X = xtmp.p;
+    }
+    if (X) {
+        ED_CUDA(cudaMemcpyAsync(w.Y.p, Y.data(), (size_t)m_eff * m_eff * 8, cudaMemcpyHostToDevice, st));
+        gemm_vy(w.V.p, n, m_eff, w.Y.p, m_eff, nev, X, st);
+    }
+    if (p.verify && X) {
+        std::vector<double> res(nev);
+        residual_norms(op, X, evals_host, nev, res.data(), st);
+        inf.matvecs += nev;
+        inf.max_residual = *std::max_element(res.begin(), res.end());
+        int nc = 0;
+        for (double r : res) nc += (r <= tol) ? 1 : 0;
+        inf.converged = nc;
+    }
+    ED_CUDA(cudaStreamSynchronize(st));
+    inf.spmv_seconds = spmv_ms * 1e-3;
+    inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (info) *info = inf;
+    ED_REQUIRE(converged, ED_ERR_NOCONV, "Lanczos did not converge within the restart cap");
+}
+
+}  // namespace edgb

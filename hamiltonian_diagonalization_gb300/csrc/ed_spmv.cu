@@ -1,0 +1,162 @@
+// Hamiltonian-vector products: stored CRS (K4) and matrix-free (K5).
+//
+// Reference: MatrixVectorFunction::Simple (hamiltonians/matrix_vector_routines.hpp:94-104)
+// -> SymmetricMatrixVectorMultiply (utilities/mathematics/sparse_linear_algebra.hpp:143-164):
+//   y[i] += a*x[c]; if (i != c) y[c] += a*x[i]   over the stored upper triangle.
+//
+// On GB300 FP64 FMA issues at about 0.6e12/s, which is what streaming the CRS
+// at HBM rate (12 bytes per nonzero) demands, so the kernels spend FP64
+// instructions only on the products: a row is owned by G lanes (G = 4 or 8
+// for the model's 200-350 nonzeros per row), each lane accumulates its share
+// serially into two chains, and only log2(G) shuffle additions per lane
+// remain.  Column and value streams are read once with evict-first loads so
+// that x stays resident in L2.
+#include "ed_hop.cuh"
+
+namespace edgb {
+
+namespace {
+
+__device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
+
+template <int G>
+__global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                   const double* __restrict__ val, const double* __restrict__ x,
+                                                   double* __restrict__ y, int64_t n)
+{
+    constexpr int RPW = 32 / G;   // rows per warp per step
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {   // warp-uniform loop
+        const int64_t r = rb + grp;
+        const bool valid = r < n;
+        const int64_t s = valid ? rowptr[r] : 0, e = valid ? rowptr[r + 1] : 0;
+        double acc0 = 0.0, acc1 = 0.0;
+        int64_t k = s + sub;
+        for (; k + G < e; k += 2 * G) {
+            const int c0 = ld_stream(col + k), c1 = ld_stream(col + k + G);
+            const double v0 = ld_stream(val + k), v1 = ld_stream(val + k + G);
+            acc0 = fma(v0, __ldg(x + c0), acc0);
+            acc1 = fma(v1, __ldg(x + c1), acc1);
+        }
+        if (k < e) acc0 = fma(ld_stream(val + k), __ldg(x + ld_stream(col + k)), acc0);
+        double acc = acc0 + acc1;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+        if (valid && sub == 0) y[r] = acc;
+    }
+}
+
+// Upper-triangle storage, the reference's layout: gather for the stored
+// part, scatter (atomic) for the transposed part.  y must be zero on entry.
+template <int G>
+__global__ void __launch_bounds__(256) k_spmv_upper(const int64_t* __restrict__ rowptr,
+                                                    const int32_t* __restrict__ col, const double* __restrict__ val,
+                                                    const double* __restrict__ x, double* __restrict__ y, int64_t n)
+{
+    constexpr int RPW = 32 / G;
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {
+        const int64_t r = rb + grp;
+        const bool valid = r < n;
+        const int64_t s = valid ? rowptr[r] : 0, e = valid ? rowptr[r + 1] : 0;
+        const double xr = valid ? __ldg(x + r) : 0.0;
+        double acc = 0.0;
+        for (int64_t k = s + sub; k < e; k += G) {
+            const int c = ld_stream(col + k);
+            const double v = ld_stream(val + k);
+            acc = fma(v, __ldg(x + c), acc);
+            if (c != r) atomicAdd(y + c, v * xr);
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+        if (valid && sub == 0) atomicAdd(y + r, acc);
+    }
+}
+
+// Matrix-free product: one thread per row regenerates the row's elements
+// (pair hops, parity sign, per-hop value from shared memory, two-table rank)
+// and accumulates them; the stored diagonal supplies y_i's own term.
+__global__ void __launch_bounds__(256) k_hv_matfree(const uint64_t* __restrict__ words, int64_t n,
+                                                    const double* __restrict__ diag, const double* __restrict__ w,
+                                                    int nw, const double* __restrict__ da,
+                                                    const double* __restrict__ db, const int* __restrict__ off, int K,
+                                                    const uint64_t* __restrict__ hi, const uint64_t* __restrict__ lo_tab,
+                                                    int L, const double* __restrict__ x, double* __restrict__ y)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const HopView hv = load_hop_smem(smem, w, nw, da, db, off, K);
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t in = words[r];
+        double acc = diag[r] * __ldg(x + r);
+        for (uint64_t ta = in; ta; ta &= ta - 1) {
+            const int a = __ffsll((long long)ta) - 1;
+            for (uint64_t tb = ta & (ta - 1); tb; tb &= tb - 1) {
+                const int b = __ffsll((long long)tb) - 1;
+                const int s = a + b;
+                const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
+                const int lo = pair_lo(s, K), pc = pair_cnt(s, K);
+                for (int ic = 0; ic < pc; ++ic) {
+                    const int c = lo + ic, d = s - c;
+                    if (c == a) continue;
+                    if ((rest >> c) & 1ull) continue;
+                    if ((rest >> d) & 1ull) continue;
+                    const uint64_t out = rest | (1ull << c) | (1ull << d);
+                    const double v = hop_element(hv, in, out, a, b, c, d);
+                    if (v == 0.0) continue;
+                    const uint64_t j = rank_in_sector(out, hi, lo_tab, L);
+                    acc = fma(v, __ldg(x + j), acc);
+                }
+            }
+        }
+        y[r] = acc;
+    }
+}
+
+int sms()
+{
+    int dev = 0, s = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return s;
+}
+
+}  // namespace
+
+void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
+{
+    if (a.n == 0) return;
+    const double avg = a.n ? (double)a.nnz / (double)a.n : 0.0;
+    const int threads = 256;
+    const int grid = sms() * 8;
+    if (!a.upper) {
+        if (avg >= 96) k_spmv_full<8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        else if (avg >= 24) k_spmv_full<4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        else k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+    } else {
+        ED_CUDA(cudaMemsetAsync(y, 0, (size_t)a.n * sizeof(double), st));
+        if (avg >= 48) k_spmv_upper<8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        else k_spmv_upper<4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+    }
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const double* x, double* y, cudaStream_t st)
+{
+    if (b.dim == 0) return;
+    const int K = t.norb;
+    const int nw = (int)t.hop.w.size();
+    const size_t smem = hop_smem_bytes(K, nw);
+    ED_CUDA(cudaFuncSetAttribute(k_hv_matfree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_hv_matfree<<<sms() * 4, 256, smem, st>>>(b.words.p, (int64_t)b.dim, diag, t.w_dev.p, nw, t.diag_a_dev.p,
+                                                t.diag_b_dev.p, t.hop_off_dev.p, K, b.hi.p, b.lo.p, b.low_bits, x, y);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+}  // namespace edgb

@@ -1,0 +1,423 @@
+"""Host-side mirror of the reference's C++ call surface for the hot path,
+over the C ABI of libedgb300.
+
+Classes keep the reference's names, method names and argument meaning so a
+caller of the reference finds the same entry points; the `mpi` arguments are
+accepted and ignored (one GPU, no ranks):
+
+  FermionFockBasis            basis/fermion_fock_basis.hpp:45
+  QuarticTermTables           fqhe_sphere/pseudopotential_model/term_tables.hpp
+  SpinlessFermionHamiltonian  hamiltonians/spinless_fermion_hamiltonian.hpp:52
+  MatrixVectorFunction        hamiltonians/matrix_vector_routines.hpp:41
+  ArpackWrapper               utilities/wrappers/arpack_wrapper.hpp:187
+  SpherePseudopotentialModel  fqhe_sphere/pseudopotential_model/pseudopotential_model.hpp
+Errors surface as EDError (status code + message), the counterpart of the
+reference's exit flag.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi as C
+from ._capi import EDError, LanczosParams, SolveInfo, check, lib
+
+SPARSE_MAPPED = 1   # utilities::_SPARSE_MAPPED_ (build-time storage of the reference)
+SPARSE_CRS = 2      # utilities::_SPARSE_CRS_
+
+
+class MpiWrapper:
+    """Stand-in for utilities::MpiWrapper: a single rank."""
+    m_id = 0
+    m_nbrProcs = 1
+    m_exitFlag = False
+
+    def ExitFlagTest(self):
+        if self.m_exitFlag:
+            raise EDError(C.ED_ERR_ARG, "exit flag set")
+
+
+def _dptr(t) -> int:
+    """Device pointer of a CUDA tensor-like object (torch.Tensor)."""
+    if hasattr(t, "data_ptr"):
+        if hasattr(t, "is_cuda") and not t.is_cuda:
+            raise EDError(C.ED_ERR_ARG, "expected a device (CUDA) tensor")
+        return int(t.data_ptr())
+    return int(t)
+
+
+def _f64p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def coulomb_pseudopotentials(norb: int) -> np.ndarray:
+    """LLL Coulomb V_m, m = 0..norb-1 (coulomb_pseudopotentials.cpp:40-69)."""
+    out = np.zeros(norb)
+    check(lib().ed_coulomb_pseudopotentials(norb, _f64p(out)))
+    return out
+
+
+def odd_coulomb_list(norb: int) -> np.ndarray:
+    """Coulomb V_m for odd m <= 2S-1, even m zero, length 2S: the list the
+    measured configurations pass as --two-body-pseudopotentials."""
+    v = coulomb_pseudopotentials(norb)[: norb - 1].copy()
+    v[0::2] = 0.0
+    return v
+
+
+def clebsch_gordan(tj1, tm1, tj2, tm2, tJ, tM) -> float:
+    return float(lib().ed_clebsch_gordan(tj1, tm1, tj2, tm2, tJ, tM))
+
+
+def dense_sym_eigen(a: np.ndarray):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    m = a.shape[0]
+    ev = np.empty(m)
+    vec = np.empty(m * m)
+    check(lib().ed_dense_sym_eigen(m, _f64p(a), _f64p(ev), _f64p(vec)))
+    return ev, vec.reshape(m, m).T.copy()
+
+
+class QuarticTermTables:
+    """k-table / V-table container (QuarticTermTables) plus its device image."""
+
+    def __init__(self, nbrOrbitals: int, pseudopotentials=None, ktable=None, vtable=None):
+        self.m_kMax = int(nbrOrbitals)
+        K = self.m_kMax
+        if ktable is None or vtable is None:
+            pp = np.ascontiguousarray(pseudopotentials if pseudopotentials is not None else [0.0, 1.0],
+                                      dtype=np.float64)
+            ktable = np.empty(K ** 3, dtype=np.uint16)
+            vtable = np.empty(K ** 3, dtype=np.float64)
+            check(lib().ed_quartic_tables(K, _f64p(pp), len(pp), ktable.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)),
+                                          _f64p(vtable)))
+        self.m_kTable = np.ascontiguousarray(ktable, dtype=np.uint16)
+        self.m_vTable = np.ascontiguousarray(vtable, dtype=np.float64)
+        self._h = None
+
+    # term_tables.cpp:109-124
+    def GetMaxKCount(self) -> int:
+        return 1
+
+    def GetK1(self, k2: int, k3: int, k4: int) -> list:
+        k1 = int(self.m_kTable[(k4 * self.m_kMax + k3) * self.m_kMax + k2])
+        return [k1] if k1 < self.m_kMax else []
+
+    # term_tables.cpp:144-156
+    def GetVkkkk(self, k1: int, k2: int, k3: int, k4: int) -> float:
+        return float(self.m_vTable[(k4 * self.m_kMax + k3) * self.m_kMax + k2])
+
+    def handle(self):
+        if self._h is None:
+            h = ctypes.c_void_p()
+            check(lib().ed_terms_set(self.m_kMax, self.m_kTable.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)),
+                                     _f64p(self.m_vTable), ctypes.byref(h)))
+            self._h = h
+        return self._h
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and C._LIB is not None:
+            C._LIB.ed_terms_free(self._h)
+            self._h = None
+
+
+class FermionFockBasis:
+    """Sector basis on the device (fermion_fock_basis.hpp:45)."""
+
+    def __init__(self):
+        self._h = None
+        self.m_basisStored = False
+
+    def GenerateFockSpace(self, nbrParticles: int, nbrOrbitals: int, twoLz: int, mpi=None, stream=None) -> bool:
+        """Build the fixed-Lz sector; returns True when its dimension is 0
+        (fermion_fock_basis.cpp:241-354).  The reference takes the Lz
+        predicate as a std::function; here the sector is named directly."""
+        self.free()
+        h = ctypes.c_void_p()
+        check(lib().ed_basis_build(int(nbrParticles), int(nbrOrbitals), int(twoLz), stream, ctypes.byref(h)))
+        self._h = h
+        self.m_basisStored = True
+        self.nbrParticles, self.nbrOrbitals, self.twoLz = int(nbrParticles), int(nbrOrbitals), int(twoLz)
+        return self.GetStoredDimension() == 0
+
+    def handle(self):
+        if self._h is None:
+            raise EDError(C.ED_ERR_ARG, "basis not generated")
+        return self._h
+
+    def GetStoredDimension(self) -> int:
+        d = ctypes.c_uint64()
+        check(lib().ed_basis_dim(self.handle(), ctypes.byref(d)))
+        return int(d.value)
+
+    def GetFockBasis(self, dim: int | None = None, mpi=None) -> np.ndarray:
+        n = self.GetStoredDimension() if dim is None else int(dim)
+        out = np.empty(n, dtype=np.uint64)
+        check(lib().ed_basis_get(self.handle(), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n))
+        return out
+
+    def FindFockStateIndices(self, states) -> np.ndarray:
+        w = np.ascontiguousarray(states, dtype=np.uint64)
+        out = np.empty(len(w), dtype=np.uint64)
+        check(lib().ed_basis_rank_host(self.handle(), w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), len(w)))
+        return out
+
+    def FindFockStateIndex(self, offset: int, state: int) -> int:
+        """Index of `state` (+offset), UINT64_MAX when absent (fermion_fock_basis.cpp:134-161)."""
+        i = int(self.FindFockStateIndices(np.array([state], dtype=np.uint64))[0])
+        return i if i == C.MISS else i + int(offset)
+
+    def words_device_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        check(lib().ed_basis_words(self.handle(), ctypes.byref(p)))
+        return int(p.value or 0)
+
+    def free(self):
+        if self._h is not None and C._LIB is not None:
+            C._LIB.ed_basis_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        self.free()
+
+
+class CrsSparseMatrix:
+    """Device CRS handle (crs_sparse_matrix.hpp:123) with int64 row pointers."""
+
+    def __init__(self, h):
+        self._h = h
+
+    def info(self):
+        n, nnz, up = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        check(lib().ed_crs_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(up)))
+        return int(n.value), int(nnz.value), bool(up.value)
+
+    def GetNbrRows(self) -> int:
+        return self.info()[0]
+
+    def GetNbrNonZeros(self) -> int:
+        return self.info()[1]
+
+    def to_host(self):
+        n, nnz, _ = self.info()
+        rp = np.empty(n + 1, dtype=np.int64)
+        col = np.empty(max(nnz, 0), dtype=np.int32)
+        val = np.empty(max(nnz, 0), dtype=np.float64)
+        check(lib().ed_crs_get(self._h, rp.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                               col.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _f64p(val)))
+        return rp, col, val
+
+    def device_arrays(self):
+        a, b, c = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        check(lib().ed_crs_arrays(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return int(a.value or 0), int(b.value or 0), int(c.value or 0)
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and C._LIB is not None:
+            C._LIB.ed_crs_free(self._h)
+            self._h = None
+
+
+class SpinlessFermionHamiltonian:
+    """spinless_fermion_hamiltonian.hpp:52 for T = double."""
+
+    def __init__(self):
+        self.m_fockBasis = FermionFockBasis()
+        self.m_crsSparseMatrix = None
+        self.m_matrixFree = False
+        self.m_terms = None
+        self.m_eigenvalues = None
+        self.m_eigenvectors = None
+        self.last_info = None
+
+    def Initialize(self, nbrParticles: int, nbrOrbitals: int, storageMethod=SPARSE_CRS, mpi=None,
+                   twoLz: int | None = None):
+        if nbrParticles <= 0 or nbrOrbitals <= 0:
+            raise EDError(C.ED_ERR_ARG, "MUST SPECIFY nbr particles > 0 and nbr orbitals > 0")
+        if nbrParticles >= 64:
+            raise EDError(C.ED_ERR_ARG, "CANNOT ADDRESS 64 PARTICLES OR MORE")
+        if nbrParticles > nbrOrbitals:
+            raise EDError(C.ED_ERR_ARG, "NBR PARTICLES > NBR ORBITALS - NOT ALLOWED")
+        self.m_nbrParticles, self.m_nbrOrbitals = int(nbrParticles), int(nbrOrbitals)
+        self.m_storageMethod = storageMethod
+        if twoLz is not None:
+            self.m_fockBasis.GenerateFockSpace(nbrParticles, nbrOrbitals, twoLz)
+
+    def Add_CdCdCC_Terms(self, termTables: QuarticTermTables, minRow: int = 0, maxRow: int | None = None, mpi=None,
+                         store_upper: bool = False, matrix_free: bool = False):
+        """Quartic terms into CRS on the device (spinless_fermion_hamiltonian.hpp:282-436).
+        The whole sector is built (row slicing was the reference's MPI split)."""
+        self.m_terms = termTables
+        if matrix_free:
+            self.m_matrixFree = True
+            self.m_crsSparseMatrix = None
+            return
+        h = ctypes.c_void_p()
+        check(lib().ed_ham_build_crs(self.m_fockBasis.handle(), termTables.handle(), int(bool(store_upper)), None,
+                                     ctypes.byref(h)))
+        self.m_crsSparseMatrix = CrsSparseMatrix(h)
+        self.m_matrixFree = False
+
+    def GetDimension(self) -> int:
+        return self.m_fockBasis.GetStoredDimension()
+
+    def operator_handle(self):
+        op = ctypes.c_void_p()
+        if self.m_matrixFree:
+            check(lib().ed_op_matfree(self.m_fockBasis.handle(), self.m_terms.handle(), ctypes.byref(op)))
+        else:
+            if self.m_crsSparseMatrix is None:
+                raise EDError(C.ED_ERR_ARG, "Hamiltonian not built")
+            check(lib().ed_op_from_crs(self.m_crsSparseMatrix._h, ctypes.byref(op)))
+        return op
+
+    def LanczosDiagonalize(self, nbrEigenvalues: int, tol: float = 1e-10, v0=None, seed: int = 0, ncv: int = 0,
+                           want_vectors: bool = True, verify: bool = True, max_restarts: int = 0):
+        """hamiltonian_base.hpp:770-931 with the device Lanczos; eigenvalues ascending."""
+        mv = MatrixVectorFunction(self)
+        arp = ArpackWrapper()
+        n = self.GetDimension()
+        evals = np.empty(nbrEigenvalues)
+        evecs = np.empty((nbrEigenvalues, n)) if want_vectors else None
+        ok = arp.DiagonalizeSymmetricMatrix(mv, evecs, evals, n, n, nbrEigenvalues, tol=tol, v0=v0, seed=seed,
+                                            ncv=ncv, verify=verify, max_restarts=max_restarts)
+        self.m_eigenvalues = evals
+        self.m_eigenvectors = evecs
+        self.last_info = arp.last_info
+        return ok
+
+
+class MatrixVectorFunction:
+    """H*v callback bound into the eigensolver (matrix_vector_routines.hpp:41)."""
+
+    def __init__(self, hamiltonian: SpinlessFermionHamiltonian, mpi=None):
+        self.hamiltonian = hamiltonian
+
+    def Simple(self, x, y, mpi=None, stream=None):
+        """y = H x on device vectors (torch CUDA tensors or raw pointers),
+        matrix_vector_routines.hpp:94-104."""
+        h = self.hamiltonian
+        if h.m_matrixFree:
+            check(lib().ed_hv_matfree(h.m_fockBasis.handle(), h.m_terms.handle(), _dptr(x), _dptr(y), stream))
+        else:
+            check(lib().ed_spmv(h.m_crsSparseMatrix._h, _dptr(x), _dptr(y), stream))
+
+
+class ArpackWrapper:
+    """Eigensolver front end (arpack_wrapper.hpp:187) over the device Lanczos."""
+
+    def __init__(self):
+        self.m_eigenvalueMagnitude = "S"
+        self.m_whatMagnitude = "R"
+        self.m_maxIterations = 2000
+        self.last_info = None
+        self.last_status = C.ED_OK
+
+    def DiagonalizeSymmetricMatrix(self, MatrixVectorMultiply, eigenvectors, eigenvalues, nodeDim: int, fullDim: int,
+                                   nbrEigenvalues: int, mpi=None, tol: float = 1e-10, v0=None, seed: int = 0,
+                                   ncv: int = 0, verify: bool = True, max_restarts: int = 0) -> bool:
+        """Lowest `nbrEigenvalues` eigenpairs.  MatrixVectorMultiply is either
+        a MatrixVectorFunction (device product) or a Python callable
+        f(x_host, y_host) on numpy arrays (the reference's std::function form).
+        eigenvalues: float64 array (filled ascending); eigenvectors: array of
+        shape (nbrEigenvalues, n) or None.  Returns False on failure, like the
+        reference, with the status in last_status."""
+        if nodeDim != fullDim:
+            raise EDError(C.ED_ERR_ARG, "one device holds the whole vector: nodeDim must equal fullDim")
+        n = int(fullDim)
+        cb = None
+        op = ctypes.c_void_p()
+        if isinstance(MatrixVectorMultiply, MatrixVectorFunction):
+            op = MatrixVectorMultiply.hamiltonian.operator_handle()
+        else:
+            fn = MatrixVectorMultiply
+
+            def _tramp(xp, yp, _user):
+                x = np.ctypeslib.as_array(xp, shape=(n,))
+                y = np.ctypeslib.as_array(yp, shape=(n,))
+                fn(x, y)
+
+            cb = C.HOST_MATVEC(_tramp)
+            check(lib().ed_op_host_callback(n, cb, None, ctypes.byref(op)))
+        try:
+            p = LanczosParams(nev=int(nbrEigenvalues), ncv=int(ncv), max_restarts=int(max_restarts or 0), tol=float(tol),
+                              seed=int(seed), want_vectors=int(eigenvectors is not None), verify=int(bool(verify)))
+            info = SolveInfo()
+            ev = np.empty(nbrEigenvalues)
+            vec = np.empty(n * nbrEigenvalues) if eigenvectors is not None else None
+            v0a = None if v0 is None else np.ascontiguousarray(v0, dtype=np.float64)
+            st = lib().ed_lanczos(op, ctypes.byref(p), _f64p(v0a) if v0a is not None else None, _f64p(ev),
+                                  _f64p(vec) if vec is not None else None, ctypes.byref(info))
+            self.last_info = info.as_dict()
+            self.last_status = st
+            eigenvalues[:nbrEigenvalues] = ev
+            if eigenvectors is not None:
+                eigenvectors[...] = vec.reshape(nbrEigenvalues, n)
+            if st != C.ED_OK:
+                self.last_error = lib().ed_last_error().decode(errors="replace")
+                return False
+            return True
+        finally:
+            lib().ed_op_free(op)
+            del cb
+
+
+class SpherePseudopotentialModel:
+    """One-sector driver: BuildTermTables / BuildFockBasis / BuildHamiltonian /
+    Diagonalize (pseudopotential_model.cpp:64-95, 160, 233, 264)."""
+
+    def __init__(self, nbrParticles: int, nbrOrbitals: int, pseudopotentials, nbrEigenvalues: int = 1):
+        self.N, self.norb = int(nbrParticles), int(nbrOrbitals)
+        self.pseudopotentials = np.ascontiguousarray(pseudopotentials, dtype=np.float64)
+        if len(self.pseudopotentials) > self.norb - 1:
+            raise EDError(C.ED_ERR_ARG, "TOO MANY 2-BODY PSEUDOPOTENTIAL COEFFICIENTS SPECIFIED")
+        self.nev = int(nbrEigenvalues)
+        self.twoLz = 0
+        self.tables = None
+        self.hamiltonian = None
+
+    def SetSector(self, twoLz: int):
+        self.twoLz = int(twoLz)
+
+    def BuildTermTables(self):
+        self.tables = QuarticTermTables(self.norb, self.pseudopotentials)
+
+    def BuildFockBasis(self) -> bool:
+        self.hamiltonian = SpinlessFermionHamiltonian()
+        self.hamiltonian.Initialize(self.N, self.norb, SPARSE_CRS)
+        return self.hamiltonian.m_fockBasis.GenerateFockSpace(self.N, self.norb, self.twoLz)
+
+    def BuildHamiltonian(self, matrix_free: bool = False, store_upper: bool = False):
+        self.hamiltonian.Add_CdCdCC_Terms(self.tables, store_upper=store_upper, matrix_free=matrix_free)
+
+    def Diagonalize(self, **kw):
+        return self.hamiltonian.LanczosDiagonalize(self.nev, **kw)
+
+
+def solve_sector(N: int, norb: int, twoLz: int, pseudopotentials, nev: int, tol: float = 1e-10, v0=None,
+                 seed: int = 0, ncv: int = 0, matrix_free: bool = False, want_vectors: bool = False,
+                 verify: bool = True):
+    """Whole-sector solve in one C-ABI call from host inputs (ed_solve_sector)."""
+    pp = np.ascontiguousarray(pseudopotentials, dtype=np.float64)
+    p = LanczosParams(nev=nev, ncv=ncv, max_restarts=0, tol=tol, seed=seed, want_vectors=int(want_vectors),
+                      verify=int(verify))
+    info = SolveInfo()
+    ev = np.empty(nev)
+    v0a = None if v0 is None else np.ascontiguousarray(v0, dtype=np.float64)
+    vec = None
+    if want_vectors:
+        n = int(np.asarray(v0a).shape[0]) if v0a is not None else None
+        if n is None:
+            b = FermionFockBasis()
+            b.GenerateFockSpace(N, norb, twoLz)
+            n = b.GetStoredDimension()
+        vec = np.empty(n * nev)
+    check(lib().ed_solve_sector(N, norb, twoLz, _f64p(pp), len(pp), int(matrix_free), ctypes.byref(p),
+                                _f64p(v0a) if v0a is not None else None, _f64p(ev),
+                                _f64p(vec) if vec is not None else None, ctypes.byref(info)))
+    out = {"eigenvalues": ev, "info": info.as_dict()}
+    if vec is not None:
+        out["eigenvectors"] = vec.reshape(nev, -1)
+    return out

@@ -1,0 +1,231 @@
+/*
+ * ed_capi.h - C ABI of the GB300-native exact-diagonalization engine for the
+ * lowest-Landau-level spinless-fermion model on the sphere.
+ *
+ * The engine replaces, on one GPU, the hot path of the reference
+ * (SimonDavenport/hamiltonian_diagonalization):
+ *   Fock basis of a fixed-Lz sector  -> quartic Hamiltonian build into CRS
+ *   -> Hamiltonian-vector product   -> Lanczos/ARPACK eigensolve.
+ * Each entry point below names the reference interface it stands in for.
+ *
+ * Conventions
+ *  - Every function returns ed_status (0 = ED_OK).  No C++ exception crosses
+ *    this boundary.  ed_last_error() gives the message of the last failure on
+ *    the calling thread.
+ *  - Handles are opaque, library-owned, released with the matching *_free.
+ *    A handle must not be used by two host threads at once.
+ *  - Pointers named *_dev are device pointers owned by the caller; pointers
+ *    named *_host (or plain arrays in host-side calls) are host memory.
+ *  - Streams are CUDA runtime streams (cudaStream_t is `struct CUstream_st*`);
+ *    NULL means the legacy default stream.
+ *  - Fock states are uint64 words, bit k = orbital k occupied, orbital k
+ *    carrying twice-angular-momentum m = 2k - (norb-1) in the Lz predicate
+ *    (angular_momentum_constraint.hpp:56).  The term tables use the
+ *    reference's k = (maxLz - m)/2 labels (pseudopotential_model_base.hpp:67).
+ *  - Indices and dimensions are uint64/int64; CRS column indices are int32
+ *    and row pointers int64 (the reference uses int32 for both; int64 row
+ *    pointers lift its 2^31-1 nonzero cap).
+ */
+#ifndef ED_CAPI_H
+#define ED_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* ed_stream;
+
+typedef enum {
+    ED_OK = 0,
+    ED_ERR_ARG = 1,          /* bad argument (null pointer, size, range)            */
+    ED_ERR_OOM = 2,          /* device or host allocation failed                    */
+    ED_ERR_CUDA = 3,         /* CUDA runtime error                                  */
+    ED_ERR_NOCONV = 4,       /* eigensolver hit its iteration cap                   */
+    ED_ERR_BREAKDOWN = 5,    /* Krylov breakdown that could not be recovered        */
+    ED_ERR_RANGE = 6,        /* problem outside the supported sizes                 */
+    ED_ERR_INTERNAL = 7,     /* a device-side consistency check failed              */
+    ED_ERR_EMPTY = 8         /* the requested sector has dimension 0                */
+} ed_status;
+
+typedef struct ed_basis ed_basis;   /* FermionFockBasis (basis/fermion_fock_basis.hpp:45)        */
+typedef struct ed_terms ed_terms;   /* QuarticTermTables (fqhe_sphere/.../term_tables.hpp)      */
+typedef struct ed_crs ed_crs;       /* CrsSparseMatrix<double> (utilities/data_structures/crs_sparse_matrix.hpp:123) */
+typedef struct ed_op ed_op;         /* the H*v operator bound into the eigensolver               */
+
+/* ------------------------------------------------------------------ misc */
+int ed_version(void);
+const char* ed_status_string(ed_status s);
+const char* ed_last_error(void);
+/* Kernels launched by this library since it was loaded (a counter kept on
+ * the host at every launch site). */
+uint64_t ed_kernel_launches(void);
+/* Number of visible CUDA devices (0 without a GPU); never fails. */
+int ed_device_count(void);
+
+/* ----------------------------------------------------- term tables (host) */
+
+/* LLL Coulomb pseudopotentials on the sphere, out[m] = V_m, m = 0..norb-1.
+ * Replaces GenCoulombPseudopotentials (fqhe_sphere/interaction_pseudopotentials/
+ * coulomb_pseudopotentials.cpp:40-69) with mulFactor 1. */
+ed_status ed_coulomb_pseudopotentials(int norb, double* out);
+
+/* Quartic term tables of the pseudopotential Hamiltonian, K = norb:
+ *   ktable[(k4*K+k3)*K+k2] = k1 with m1+m2 = m3+m4, 65535 if out of range
+ *   vtable[(k4*K+k3)*K+k2] = -sum_L V_L <S m1,S m2|J M><S m3,S m4|J M>,
+ *                            J = 2S - L (twice-units Lact = 2*maxLz - L)
+ * Host arrays of K^3 entries.  Replaces BaseGenerate4KTable and
+ * BaseTermsFromPseudopotentials (fqhe_sphere/pseudopotential_model/
+ * pseudopotential_model_base.hpp:97-139, 150-229).  npp may not exceed
+ * norb-1 (the reference's check, pseudopotential_model_data.cpp:285). */
+ed_status ed_quartic_tables(int norb, const double* pseudopotentials, int npp,
+                            uint16_t* ktable, double* vtable);
+
+/* Clebsch-Gordan coefficient <j1 m1; j2 m2 | J M>, all arguments twice the
+ * physical values; magnitudes at or below 1e-12 read as 0 like the
+ * reference's stored table (utilities/wrappers/clebsch_gordan_wrapper.hpp:160). */
+double ed_clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM);
+
+/* --------------------------------------------------------------- basis K1/K2 */
+
+/* Fock basis of the sector (N particles, norb orbitals, twice total Lz),
+ * ascending uint64 words, built on the device.  A sector of dimension 0 gives
+ * a valid handle with dim 0 (the reference's isZeroDim == true).
+ * Replaces FermionFockBasis::GenerateFockSpace (fermion_fock_basis.cpp:241-354)
+ * with the TestAngularMomentumSector constraint. */
+ed_status ed_basis_build(int N, int norb, int two_lz, ed_stream stream, ed_basis** out);
+ed_status ed_basis_free(ed_basis* b);
+ed_status ed_basis_dim(const ed_basis* b, uint64_t* dim);
+/* Device pointer to the n basis words (valid while the handle lives). */
+ed_status ed_basis_words(const ed_basis* b, const uint64_t** words_dev);
+/* Copy the first n words to host (GetFockBasis, fermion_fock_basis.cpp:359). */
+ed_status ed_basis_get(const ed_basis* b, uint64_t* host_words, uint64_t n);
+/* Index of each word in the basis, UINT64_MAX when absent.  Device arrays.
+ * Replaces FindFockStateIndex (fermion_fock_basis.cpp:134-161) with offset 0. */
+ed_status ed_basis_rank(const ed_basis* b, const uint64_t* words_dev, uint64_t* idx_dev,
+                        uint64_t m, ed_stream stream);
+/* Host-array convenience form of ed_basis_rank. */
+ed_status ed_basis_rank_host(const ed_basis* b, const uint64_t* words, uint64_t* idx, uint64_t m);
+
+/* ------------------------------------------------------------------- terms */
+
+/* Upload the quartic tables (host, K^3 entries each) and derive the per-hop
+ * matrix-element table used by the device build.  Stands in for the
+ * QuarticTermTables object handed to Add_CdCdCC_Terms
+ * (spinless_fermion_hamiltonian.hpp:263-282: GetK1/GetVkkkk). */
+ed_status ed_terms_set(int norb, const uint16_t* ktable, const double* vtable, ed_terms** out);
+ed_status ed_terms_free(ed_terms* t);
+
+/* -------------------------------------------------------- Hamiltonian K3 */
+
+/* Build H into CRS on the device: int64 row pointers, int32 columns
+ * ascending within each row, FP64 values.  store_upper = 1 keeps the upper
+ * triangle (col >= row) exactly as the reference stores it; 0 stores both
+ * triangles, the lower part being the bit-exact transpose of the upper.
+ * Same element set, signs, summation order and 1e-14 trims as
+ * SpinlessFermionHamiltonian::Add_CdCdCC_Terms + MappedSparseMatrix::Trim +
+ * CrsSparseMatrix::Initialize (spinless_fermion_hamiltonian.hpp:282-436,
+ * mapped_sparse_matrix.hpp:423-460, crs_sparse_matrix.hpp:193-254). */
+ed_status ed_ham_build_crs(const ed_basis* b, const ed_terms* t, int store_upper,
+                           ed_stream stream, ed_crs** out);
+ed_status ed_crs_free(ed_crs* a);
+ed_status ed_crs_info(const ed_crs* a, int64_t* n, int64_t* nnz, int* upper);
+ed_status ed_crs_arrays(const ed_crs* a, const int64_t** rowptr_dev, const int32_t** col_dev,
+                        const double** val_dev);
+/* Copy CRS to host arrays of n+1 / nnz / nnz entries. */
+ed_status ed_crs_get(const ed_crs* a, int64_t* rowptr, int32_t* col, double* val);
+/* Diagonal of H (n doubles, device), computed in the reference's term order. */
+ed_status ed_ham_diagonal(const ed_basis* b, const ed_terms* t, double* diag_dev, ed_stream stream);
+
+/* ------------------------------------------------------------ H*v K4 / K5 */
+
+/* y = H x from a stored CRS (either storage).  Device vectors of n doubles.
+ * Replaces MatrixVectorFunction::Simple (hamiltonians/matrix_vector_routines.hpp:94-104)
+ * -> SymmetricMatrixVectorMultiply (utilities/mathematics/sparse_linear_algebra.hpp:78-168). */
+ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream stream);
+
+/* y = H x with the matrix elements regenerated on the fly from the basis and
+ * the term tables (no stored matrix).  Stands in for the reference's
+ * unfinished MatrixVectorFunction::Recalculate (matrix_vector_routines.hpp:112-143). */
+ed_status ed_hv_matfree(const ed_basis* b, const ed_terms* t, const double* x_dev, double* y_dev,
+                        ed_stream stream);
+
+/* ------------------------------------------------------------ eigensolver */
+
+typedef void (*ed_host_matvec)(const double* x_host, double* y_host, void* user);
+
+/* Operators the eigensolver can drive. */
+ed_status ed_op_from_crs(const ed_crs* a, ed_op** out);
+ed_status ed_op_matfree(const ed_basis* b, const ed_terms* t, ed_op** out);
+/* A host callback y = A x on host arrays of n doubles: the generic
+ * std::function form of ArpackWrapper::DiagonalizeSymmetricMatrix
+ * (arpack_wrapper.hpp:595-606).  Vectors cross PCIe/NVLink-C2C per product. */
+ed_status ed_op_host_callback(int64_t n, ed_host_matvec fn, void* user, ed_op** out);
+ed_status ed_op_free(ed_op* op);
+ed_status ed_op_dim(const ed_op* op, int64_t* n);
+
+typedef struct {
+    int nev;            /* eigenpairs wanted (lowest algebraic)                      */
+    int ncv;            /* Krylov subspace size; 0 -> min(n, 2*nev+21) like ARPACK     */
+    int max_restarts;   /* 0 -> 2000 (the reference's ARPACK iteration cap)           */
+    double tol;         /* residual ||H x - theta x||_2 (x unit) required per pair     */
+    uint64_t seed;      /* start vector uniform(-1,1) from this seed if none is given  */
+    int want_vectors;   /* 1 -> return eigenvectors                                    */
+    int verify;         /* 1 -> recompute true residuals with extra products            */
+} ed_lanczos_params;
+
+typedef struct {
+    int converged;      /* number of converged pairs among the nev returned           */
+    int restarts;
+    int64_t matvecs;
+    double max_residual;    /* max over returned pairs of the residual (true one if verify) */
+    double seconds;         /* wall time of the solve                                  */
+    double spmv_seconds;    /* device time inside the H*v products                     */
+    int breakdowns;
+} ed_solve_info;
+
+/* Lowest nev eigenpairs of a real symmetric operator by thick-restart Lanczos
+ * with full FP64 reorthogonalisation on the device.  v0_host (n doubles) may
+ * be NULL (seeded random start).  evals_host receives nev values ascending;
+ * evecs_host (n*nev, column-major, may be NULL) the unit eigenvectors.
+ * Replaces ArpackWrapper::DiagonalizeSymmetricMatrix<double> (MPI form,
+ * arpack_wrapper.hpp:595-937) as driven by LanczosDiagonalize
+ * (hamiltonian_base.hpp:770-931); unlike the reference, which returns
+ * ARPACK's Ritz order, the values come sorted ascending. */
+ed_status ed_lanczos(const ed_op* op, const ed_lanczos_params* p, const double* v0_host,
+                     double* evals_host, double* evecs_host, ed_solve_info* info);
+
+/* Same solve with device-resident start vector and outputs (n doubles /
+ * n*nev doubles, column-major).  Either output may be NULL. */
+ed_status ed_lanczos_device(const ed_op* op, const ed_lanczos_params* p, const double* v0_dev,
+                            double* evals_host, double* evecs_dev, ed_solve_info* info);
+
+/* Dense symmetric eigen-decomposition on the host (FP64; Householder
+ * tridiagonalisation + implicit QR with Wilkinson shifts): a is m*m row-major,
+ * evals ascending, evecs column-major (may be NULL).  The projected-matrix
+ * solver of ed_lanczos, exposed for reuse; replaces the small dense problems
+ * the reference hands to LAPACK dsyevr_ (utilities/wrappers/lapack_wrapper.hpp:479-540,
+ * FullDiagonalize, hamiltonians/hamiltonian_base.hpp:634-758). */
+ed_status ed_dense_sym_eigen(int m, const double* a, double* evals, double* evecs);
+
+/* ||H x_i - lambda_i x_i||_2 for k device vectors (column-major n*k). */
+ed_status ed_residuals(const ed_op* op, const double* x_dev, const double* lambda_host, int k,
+                       double* res_host);
+
+/* ------------------------------------------------------- one-call driver */
+
+/* Whole sector solve from host inputs: basis -> tables -> CRS (or matrix-free
+ * when matfree != 0) -> Lanczos; eigenvalues and optional eigenvectors to host.
+ * The sequence SpherePseudopotentialModel::BuildTermTables / BuildFockBasis /
+ * BuildHamiltonian / Diagonalize performs (pseudopotential_model.cpp:64-95,
+ * 160, 233, 264) for one sector. */
+ed_status ed_solve_sector(int N, int norb, int two_lz, const double* pseudopotentials, int npp,
+                          int matfree, const ed_lanczos_params* p, const double* v0_host,
+                          double* evals_host, double* evecs_host, ed_solve_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ED_CAPI_H */

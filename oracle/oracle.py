@@ -1,0 +1,419 @@
+"""CPU oracle for the LLL spinless-fermion exact-diagonalization hot path.
+
+TEST INFRASTRUCTURE ONLY.  Only the tests, ``__graft_entry__.smoke()`` and the
+CPU legs of ``bench.py`` import this module, and only as the checker or as the
+timed CPU baseline.  The shipped library never calls into it.
+
+It restates the reference (SimonDavenport/hamiltonian_diagonalization):
+
+* ``oracle.c`` (loaded through ctypes): Fock-basis scan, binary-search rank,
+  ``Evaluate_CdCdCC``, the quartic build in the reference's loop order, and
+  the symmetric upper-triangle SpMV;
+* this file: the term tables (``BaseGenerate4KTable`` /
+  ``BaseTermsFromPseudopotentials``, pseudopotential_model_base.hpp:62-229)
+  with Clebsch-Gordan coefficients evaluated EXACTLY (rational Racah
+  formula), the LLL Coulomb pseudopotentials
+  (coulomb_pseudopotentials.cpp:40-69, exact integers), and the eigenvalue
+  oracle: SciPy's ARPACK, the same library family the reference drives
+  through ``pdnaupd_/pdneupd_`` (arpack_wrapper.hpp:595-937).
+
+``pin_against_reference()`` checks the bit-level restatement against the
+reference's own primitives compiled from its sources (oracle/_ref).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+from fractions import Fraction
+from functools import lru_cache
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+MISS = np.uint64(0xFFFFFFFFFFFFFFFF)
+SPARSE_ZERO_TOL = 1e-14          # hamiltonian_data.hpp:53
+CG_EPS = 1e-12                   # clebsch_gordan_coefficients.hpp:53 (values at or below are not stored)
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u16p = ctypes.POINTER(ctypes.c_uint16)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle/liboracle.so (and oracle/_ref when the reference tree is present)."""
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
+        os.path.join(HERE, "oracle.c")
+    ):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    return LIB_PATH
+
+
+def build_ref() -> str | None:
+    """Compile oracle/_ref/libref.so from the reference sources, if they are here."""
+    src = os.environ.get("REFSRC", "/root/reference/src")
+    if not os.path.isdir(src):
+        return None
+    subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFSRC={src}"])
+    return REF_PATH
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.or_binomial.restype = ctypes.c_uint64
+        L.or_binomial.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.or_next_hamming.restype = ctypes.c_uint64
+        L.or_next_hamming.argtypes = [ctypes.c_uint64]
+        L.or_unrank_hamming.restype = ctypes.c_uint64
+        L.or_unrank_hamming.argtypes = [ctypes.c_int, ctypes.c_uint64]
+        L.or_lz_ok.restype = ctypes.c_int
+        L.or_lz_ok.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+        L.or_basis_build.restype = ctypes.c_uint64
+        L.or_basis_build.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _u64p, ctypes.c_int]
+        L.or_find_index.restype = ctypes.c_uint64
+        L.or_find_index.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_uint64]
+        L.or_find_indices.restype = None
+        L.or_find_indices.argtypes = [_u64p, ctypes.c_uint64, _u64p, _u64p, ctypes.c_uint64]
+        L.or_evaluate_cdcdcc.restype = ctypes.c_uint64
+        L.or_evaluate_cdcdcc.argtypes = [ctypes.POINTER(ctypes.c_int)] + [ctypes.c_uint64] * 6
+        L.or_build_upper_count.restype = ctypes.c_int64
+        L.or_build_upper_count.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_int, _u16p, _f64p, ctypes.c_int,
+                                           ctypes.c_int64, ctypes.c_int64, _i64p, ctypes.c_int]
+        L.or_build_upper_fill.restype = None
+        L.or_build_upper_fill.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_int, _u16p, _f64p, ctypes.c_int,
+                                          ctypes.c_int64, ctypes.c_int64, _i64p, _i32p, _f64p, ctypes.c_int]
+        L.or_spmv_sym_upper.restype = None
+        L.or_spmv_sym_upper.argtypes = [_i64p, _i32p, _f64p, ctypes.c_int64, _f64p, _f64p]
+        L.or_spmv_sym_upper_mt.restype = None
+        L.or_spmv_sym_upper_mt.argtypes = [_i64p, _i32p, _f64p, ctypes.c_int64, _f64p, _f64p, _f64p, ctypes.c_int]
+        L.or_spmv_full.restype = None
+        L.or_spmv_full.argtypes = [_i64p, _i32p, _f64p, ctypes.c_int64, _f64p, _f64p, ctypes.c_int]
+        L.or_num_procs.restype = ctypes.c_int
+        _LIB = L
+    return _LIB
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def num_procs() -> int:
+    return int(lib().or_num_procs())
+
+
+# ------------------------------------------------------------------ bit tools
+
+def binomial(n: int, k: int) -> int:
+    return int(lib().or_binomial(n, k))
+
+
+def next_hamming(x: int) -> int:
+    return int(lib().or_next_hamming(x))
+
+
+def unrank_hamming(w: int, index: int) -> int:
+    return int(lib().or_unrank_hamming(w, index))
+
+
+def lz_ok(state: int, two_lz: int, max_lz: int) -> bool:
+    return bool(lib().or_lz_ok(state, two_lz, max_lz))
+
+
+def evaluate_cdcdcc(k1: int, k2: int, k3: int, k4: int, state: int, norb: int):
+    """(out_word, sign) of c+_k1 c+_k2 c_k3 c_k4 |state>  (fermions.hpp:52-144)."""
+    s = ctypes.c_int(0)
+    out = lib().or_evaluate_cdcdcc(ctypes.byref(s), 1 << k1, 1 << k2, 1 << k3, 1 << k4, state,
+                                   1 << (norb - 1))
+    return int(out), int(s.value)
+
+
+# ---------------------------------------------------------------- Fock basis
+
+def sector_sum(N: int, norb: int, two_lz: int):
+    """Sum of occupied bit positions of every state in the sector, or None if empty
+    (angular_momentum_constraint.hpp:41-62: sum(2k - maxLz) == 2Lz)."""
+    t = two_lz + N * (norb - 1)
+    if t % 2:
+        return None
+    return t // 2
+
+
+def basis(N: int, norb: int, two_lz: int, nthreads: int | None = None) -> np.ndarray:
+    """Ascending sector basis (fermion_fock_basis.cpp:241-354)."""
+    nt = nthreads or num_procs()
+    n = int(lib().or_basis_build(N, norb, two_lz, None, nt))
+    out = np.empty(n, dtype=np.uint64)
+    if n:
+        lib().or_basis_build(N, norb, two_lz, _p(out, _u64p), nt)
+    return out
+
+
+def find_indices(b: np.ndarray, words: np.ndarray) -> np.ndarray:
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    out = np.empty(len(w), dtype=np.uint64)
+    lib().or_find_indices(_p(b, _u64p), len(b), _p(w, _u64p), _p(out, _u64p), len(w))
+    return out
+
+
+# --------------------------------------------------------------- term tables
+
+def k_table(norb: int) -> np.ndarray:
+    """kTable[(k4*K+k3)*K+k2] = k1 with m1+m2 = m3+m4, 65535 when out of range.
+
+    pseudopotential_model_base.hpp:62-139 (ConvertStateLabel k=(maxLz-m)/2,
+    FindM1 with error code maxLz2+2 = maxLz+2 for one Landau level,
+    BaseGenerate4KTable loop order m4, m3, m2 from +maxLz down in steps of 2).
+    """
+    max_lz = norb - 1
+    K = norb
+    out = np.empty(K ** 3, dtype=np.uint16)
+    it = 0
+    for m4 in range(max_lz, -max_lz - 1, -2):
+        for m3 in range(max_lz, -max_lz - 1, -2):
+            for m2 in range(max_lz, -max_lz - 1, -2):
+                m1 = m3 + m4 - m2
+                if not (-max_lz <= m1 <= max_lz):
+                    m1 = max_lz + 2
+                out[it] = ((-m1 + max_lz) // 2) & 0xFFFF
+                it += 1
+    return out
+
+
+_FACT = [1]
+for _i in range(1, 400):
+    _FACT.append(_FACT[-1] * _i)
+
+
+@lru_cache(maxsize=None)
+def cg_exact(tj1: int, tm1: int, tj2: int, tm2: int, tJ: int, tM: int) -> float:
+    """<j1 m1; j2 m2 | J M> from the Racah closed form in exact rational
+    arithmetic; all arguments are twice the physical quantum numbers.
+    Magnitudes at or below 1e-12 are returned as 0, as the reference's table
+    does not store them (clebsch_gordan_wrapper.hpp:116-124)."""
+    if tm1 + tm2 != tM or abs(tm1) > tj1 or abs(tm2) > tj2 or abs(tM) > tJ:
+        return 0.0
+    if tJ > tj1 + tj2 or tJ < abs(tj1 - tj2) or (tj1 + tj2 + tJ) % 2:
+        return 0.0
+    if (tj1 + tm1) % 2 or (tj2 + tm2) % 2 or (tJ + tM) % 2:
+        return 0.0
+    j1p, j1m = (tj1 + tm1) // 2, (tj1 - tm1) // 2
+    j2p, j2m = (tj2 + tm2) // 2, (tj2 - tm2) // 2
+    Jp, Jm = (tJ + tM) // 2, (tJ - tM) // 2
+    a = (tj1 + tj2 - tJ) // 2
+    b = (tj1 - tj2 + tJ) // 2
+    c = (-tj1 + tj2 + tJ) // 2
+    s = (tj1 + tj2 + tJ) // 2
+    F = _FACT
+    pref2 = Fraction((tJ + 1) * F[a] * F[b] * F[c], F[s + 1]) * (F[j1p] * F[j1m] * F[j2p] * F[j2m] * F[Jp] * F[Jm])
+    e1 = (tJ - tj2 + tm1) // 2      # J - j2 + m1
+    e2 = (tJ - tj1 - tm2) // 2      # J - j1 - m2
+    kmin = max(0, -e1, -e2)
+    kmax = min(a, j1m, j2p)
+    tot = Fraction(0)
+    for k in range(kmin, kmax + 1):
+        d = F[k] * F[a - k] * F[j1m - k] * F[j2p - k] * F[e1 + k] * F[e2 + k]
+        tot += Fraction(-1 if k & 1 else 1, d)
+    if tot == 0:
+        return 0.0
+    val = math.sqrt(float(pref2 * tot * tot))
+    if tot < 0:
+        val = -val
+    if abs(val) <= CG_EPS:
+        return 0.0
+    return val
+
+
+def v_table(norb: int, pseudopotentials) -> np.ndarray:
+    """vTable[(k4*K+k3)*K+k2] = -sum_L V_L <S m1,S m2|Lact M><S m3,S m4|Lact M>.
+
+    pseudopotential_model_base.hpp:150-229 (BaseTermsFromPseudopotentials):
+    loop over m4,m3,m2 from +maxLz down; m1 = FindM1; for L = 0,2,..
+    < 2*len(V): Lact = 2*maxLz - L, M = m1+m2, the product of the two
+    coefficients when |M| <= Lact, subtracted with weight V[L/2]."""
+    max_lz = norb - 1
+    K = norb
+    pp = [float(v) for v in pseudopotentials]
+    out = np.zeros(K ** 3, dtype=np.float64)
+    it = 0
+    for m4 in range(max_lz, -max_lz - 1, -2):
+        for m3 in range(max_lz, -max_lz - 1, -2):
+            for m2 in range(max_lz, -max_lz - 1, -2):
+                total = 0.0
+                m1 = m3 + m4 - m2
+                if -max_lz <= m1 <= max_lz:
+                    M = m1 + m2
+                    for L in range(0, 2 * len(pp), 2):
+                        temp = 0.0
+                        lact = 2 * max_lz - L
+                        if -lact <= M <= lact:
+                            temp += cg_exact(max_lz, m1, max_lz, m2, lact, M) * cg_exact(max_lz, m3, max_lz, m4, lact, M)
+                        total -= pp[L // 2] * temp
+                out[it] = total
+                it += 1
+    return out
+
+
+def quartic_tables(norb: int, pseudopotentials):
+    return k_table(norb), v_table(norb, pseudopotentials)
+
+
+def coulomb_pseudopotentials(norb: int) -> np.ndarray:
+    """LLL Coulomb pseudopotentials on the sphere, V_m for m = 0..2S with
+    mulFactor 1 (coulomb_pseudopotentials.cpp:40-69):
+    p[2S-L] = 2/sqrt(S) C(4S-2L,2S-L) C(4S+2L+2,2S+L+1) / C(4S+2,2S+1)^2,
+    here with exact integer binomials."""
+    max_lz = norb - 1
+    p = np.zeros(max_lz + 1)
+    den = math.comb(2 * max_lz + 2, max_lz + 1) ** 2
+    for L in range(max_lz + 1):
+        r = Fraction(math.comb(2 * max_lz - 2 * L, max_lz - L) * math.comb(2 * max_lz + 2 * L + 2, max_lz + L + 1), den)
+        p[max_lz - L] = 2.0 / math.sqrt(max_lz / 2.0) * float(r)
+    return p
+
+
+def odd_coulomb_list(norb: int) -> np.ndarray:
+    """The pseudopotential list the measured configurations use: Coulomb V_m
+    for odd m with 1 <= m <= 2S-1, even m set to 0, length 2S (the longest
+    list the reference accepts, pseudopotential_model_data.cpp:285-290)."""
+    v = coulomb_pseudopotentials(norb)[: norb - 1].copy()
+    v[0::2] = 0.0
+    return v
+
+
+def sweep_list(norb: int, v1: float) -> np.ndarray:
+    """H(V1) = V1*P_1 + sum_{odd m>=3} V_m^Coulomb P_m as a pseudopotential list."""
+    v = odd_coulomb_list(norb)
+    v[1] = v1
+    return v
+
+
+# ------------------------------------------------------------- quartic build
+
+def build_upper(b: np.ndarray, norb: int, ktab: np.ndarray, vtab: np.ndarray,
+                nthreads: int | None = None, rows: tuple[int, int] | None = None):
+    """Upper-triangle CRS (int64 rowptr, int32 col, f64 val) in the
+    reference's loop and summation order (spinless_fermion_hamiltonian.hpp:282-436,
+    mapped_sparse_matrix.hpp:423-460, crs_sparse_matrix.hpp:193-254).
+    ``rows`` restricts the build to a row range [r0, r1)."""
+    nt = nthreads or num_procs()
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    kt = np.ascontiguousarray(ktab, dtype=np.uint16)
+    vt = np.ascontiguousarray(vtab, dtype=np.float64)
+    K = norb
+    r0, r1 = rows if rows is not None else (0, len(b))
+    rowlen = np.zeros(r1 - r0, dtype=np.int64)
+    L = lib()
+    L.or_build_upper_count(_p(b, _u64p), len(b), norb, _p(kt, _u16p), _p(vt, _f64p), K, r0, r1,
+                           _p(rowlen, _i64p), nt)
+    rowptr = np.zeros(r1 - r0 + 1, dtype=np.int64)
+    np.cumsum(rowlen, out=rowptr[1:])
+    nnz = int(rowptr[-1])
+    col = np.empty(nnz, dtype=np.int32)
+    val = np.empty(nnz, dtype=np.float64)
+    L.or_build_upper_fill(_p(b, _u64p), len(b), norb, _p(kt, _u16p), _p(vt, _f64p), K, r0, r1,
+                          _p(rowptr, _i64p), _p(col, _i32p), _p(val, _f64p), nt)
+    return rowptr, col, val
+
+
+def upper_to_full(rowptr, col, val, n):
+    """Both triangles of the symmetric matrix as CRS with ascending columns;
+    the lower entries are the exact transposes of the stored upper ones."""
+    import scipy.sparse as sp
+    U = sp.csr_matrix((val, col, rowptr), shape=(n, n))
+    D = sp.diags(U.diagonal())
+    A = (U + U.T - D).tocsr()
+    A.sort_indices()
+    # drop structural zeros that the sum above cannot create (kept explicit)
+    return A.indptr.astype(np.int64), A.indices.astype(np.int32), A.data.astype(np.float64)
+
+
+def spmv_sym_upper(rowptr, col, val, x, nthreads: int = 1):
+    """y = H x from the stored upper triangle (sparse_linear_algebra.hpp:143-164)."""
+    n = len(rowptr) - 1
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty(n, dtype=np.float64)
+    L = lib()
+    if nthreads <= 1:
+        L.or_spmv_sym_upper(_p(rowptr, _i64p), _p(col, _i32p), _p(val, _f64p), n, _p(x, _f64p), _p(y, _f64p))
+    else:
+        work = np.empty(n * nthreads, dtype=np.float64)
+        L.or_spmv_sym_upper_mt(_p(rowptr, _i64p), _p(col, _i32p), _p(val, _f64p), n, _p(x, _f64p),
+                               _p(y, _f64p), _p(work, _f64p), nthreads)
+    return y
+
+
+# -------------------------------------------------------------- eigen oracle
+
+def start_vector(n: int, seed: int) -> np.ndarray:
+    """Seeded uniform(-1,1) start vector, normalised."""
+    v = np.random.default_rng(seed).uniform(-1.0, 1.0, n)
+    return v / np.linalg.norm(v)
+
+
+def lowest_eigenpairs(rowptr, col, val, nev: int, tol: float = 1e-12, v0=None, upper: bool = True,
+                      nthreads: int = 1, driver: str = "eigs"):
+    """Lowest ``nev`` eigenpairs with SciPy's ARPACK.  ``driver='eigs'`` uses the
+    non-symmetric driver with which='SR', ncv = min(n, 2*nev+21) and maxiter
+    2000, the reference's settings (arpack_wrapper.hpp:702-708); ``'eigsh'``
+    uses the symmetric driver.  The matrix-vector product is the upper-
+    triangle loop of the reference when ``upper`` is set."""
+    import scipy.sparse.linalg as sla
+    n = len(rowptr) - 1
+    if upper:
+        op = sla.LinearOperator((n, n), matvec=lambda x: spmv_sym_upper(rowptr, col, val, x, nthreads),
+                                dtype=np.float64)
+    else:
+        import scipy.sparse as sp
+        op = sp.csr_matrix((val, col, rowptr), shape=(n, n))
+    ncv = min(n, 2 * nev + 21)
+    if driver == "eigs":
+        w, v = sla.eigs(op, k=nev, which="SR", tol=tol, v0=v0, ncv=ncv, maxiter=2000)
+        w, v = w.real, v.real
+    else:
+        w, v = sla.eigsh(op, k=nev, which="SA", tol=tol, v0=v0, ncv=ncv, maxiter=2000)
+    order = np.argsort(w)
+    w, v = w[order], v[:, order]
+    v = v / np.linalg.norm(v, axis=0)
+    return w, v
+
+
+# ----------------------------------------------- pin against the reference
+
+def ref_lib():
+    """The reference's own primitives (oracle/_ref/libref.so), or None."""
+    if not os.path.exists(REF_PATH):
+        try:
+            if build_ref() is None:
+                return None
+        except Exception:
+            return None
+    L = ctypes.CDLL(REF_PATH)
+    L.ref_evaluate_cdcdcc.restype = ctypes.c_uint64
+    L.ref_evaluate_cdcdcc.argtypes = [ctypes.POINTER(ctypes.c_int)] + [ctypes.c_uint64] * 6
+    L.ref_next_hamming.restype = ctypes.c_uint64
+    L.ref_next_hamming.argtypes = [ctypes.c_uint64]
+    L.ref_generate_hamming.restype = ctypes.c_uint64
+    L.ref_generate_hamming.argtypes = [ctypes.c_uint, ctypes.c_uint64]
+    L.ref_hamming_weight.restype = ctypes.c_int
+    L.ref_hamming_weight.argtypes = [ctypes.c_uint64]
+    L.ref_base2log.restype = ctypes.c_uint
+    L.ref_base2log.argtypes = [ctypes.c_uint64]
+    L.ref_binomial.restype = ctypes.c_long
+    L.ref_binomial.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.ref_binary_search.restype = ctypes.c_uint64
+    L.ref_binary_search.argtypes = [ctypes.c_uint64, _u64p, ctypes.c_uint64]
+    L.ref_lz_ok.restype = ctypes.c_int
+    L.ref_lz_ok.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+    return L

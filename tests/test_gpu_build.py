@@ -1,0 +1,85 @@
+"""Device Hamiltonian build (K3) against the oracle's restatement of
+Add_CdCdCC_Terms: row pointers, columns and values bit-exact."""
+import numpy as np
+import pytest
+
+import hamiltonian_diagonalization_gb300 as ed
+
+pytestmark = pytest.mark.gpu
+
+
+def build_gpu(N, norb, tlz, pp, upper):
+    H = ed.SpinlessFermionHamiltonian()
+    H.Initialize(N, norb, twoLz=tlz)
+    T = ed.QuarticTermTables(norb, pp)
+    H.Add_CdCdCC_Terms(T, store_upper=upper)
+    return H, T
+
+
+CASES = [(2, 8, 0), (4, 10, 0), (4, 10, -2), (5, 13, 3), (6, 16, 4), (8, 22, 0), (8, 22, 2), (3, 40, 0),
+         (7, 19, 1)]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_upper_crs_bit_exact(cuda, oracle, case):
+    N, norb, tlz = case
+    rng = np.random.default_rng(norb * 7 + N)
+    for pp in (oracle.odd_coulomb_list(norb), rng.uniform(-1, 2, size=norb - 1)):
+        H, T = build_gpu(N, norb, tlz, pp, upper=True)
+        rp, col, val = H.m_crsSparseMatrix.to_host()
+        b = oracle.basis(N, norb, tlz)
+        orp, ocol, oval = oracle.build_upper(b, norb, T.m_kTable, T.m_vTable)
+        assert np.array_equal(rp, orp)
+        assert np.array_equal(col, ocol)
+        assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+
+
+@pytest.mark.parametrize("case", [(4, 10, 0), (6, 16, 4), (8, 22, 0)])
+def test_full_crs_is_exact_symmetric_completion(cuda, oracle, case):
+    N, norb, tlz = case
+    pp = oracle.odd_coulomb_list(norb)
+    H, T = build_gpu(N, norb, tlz, pp, upper=False)
+    rp, col, val = H.m_crsSparseMatrix.to_host()
+    b = oracle.basis(N, norb, tlz)
+    orp, ocol, oval = oracle.upper_to_full(*oracle.build_upper(b, norb, T.m_kTable, T.m_vTable), len(b))
+    assert np.array_equal(rp, orp)
+    assert np.array_equal(col, ocol)
+    assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+
+
+def test_sector_of_batched_sweep_bit_exact(cuda, oracle):
+    # one Lz sector of the N=10, 2S=27 sweep (246,448 rows)
+    N, norb, tlz = 10, 28, 0
+    pp = oracle.sweep_list(norb, 1.7)
+    H, T = build_gpu(N, norb, tlz, pp, upper=True)
+    rp, col, val = H.m_crsSparseMatrix.to_host()
+    b = oracle.basis(N, norb, tlz)
+    orp, ocol, oval = oracle.build_upper(b, norb, T.m_kTable, T.m_vTable)
+    assert rp[-1] == orp[-1]
+    assert np.array_equal(rp, orp)
+    assert np.array_equal(col, ocol)
+    assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+
+
+def test_stored_crs_at_scale_row_samples(cuda, oracle):
+    # N=11, 2S=30 (1,371,535 rows): compare sampled row blocks with the oracle
+    N, norb, tlz = 11, 31, 0
+    pp = oracle.odd_coulomb_list(norb)
+    H, T = build_gpu(N, norb, tlz, pp, upper=True)
+    rp, col, val = H.m_crsSparseMatrix.to_host()
+    b = oracle.basis(N, norb, tlz)
+    n = len(b)
+    assert len(rp) == n + 1
+    for r0 in (0, 123457, n // 2, n - 700):
+        orp, ocol, oval = oracle.build_upper(b, norb, T.m_kTable, T.m_vTable, rows=(r0, r0 + 700))
+        s, e = rp[r0], rp[r0 + 700]
+        assert np.array_equal(rp[r0:r0 + 701] - s, orp)
+        assert np.array_equal(col[s:e], ocol)
+        assert np.array_equal(val[s:e].view(np.uint64), oval.view(np.uint64))
+    # full storage = 2*upper - diagonal
+    Hf, _ = build_gpu(N, norb, tlz, pp, upper=False)
+    nf = Hf.m_crsSparseMatrix.GetNbrNonZeros()
+    nonempty = rp[1:] > rp[:-1]
+    first = col[rp[:-1][nonempty]]
+    ndiag = int(np.sum(first == np.arange(n)[nonempty]))
+    assert nf == 2 * (len(col)) - ndiag

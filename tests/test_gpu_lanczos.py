@@ -1,0 +1,136 @@
+"""Device Lanczos against the eigenvalue oracle (SciPy's ARPACK on the
+oracle's matrix, dense LAPACK for small cases) and known answers.
+Eigenvalues to 1e-10 relative, residuals ||Hx - lambda x|| <= 1e-10."""
+import ctypes
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import hamiltonian_diagonalization_gb300 as ed
+
+pytestmark = pytest.mark.gpu
+
+
+def model(N, norb, tlz, pp, nev, **kw):
+    m = ed.SpherePseudopotentialModel(N, norb, pp, nev)
+    m.SetSector(tlz)
+    m.BuildTermTables()
+    assert m.BuildFockBasis() is False
+    m.BuildHamiltonian(matrix_free=kw.pop("matrix_free", False), store_upper=kw.pop("store_upper", False))
+    ok = m.Diagonalize(**kw)
+    return m, ok
+
+
+def test_small_config_matches_arpack(cuda, oracle):
+    # N=8, 2S=21, Lz=0: 8,512 states, lowest 5, tol 1e-12, seeded start
+    N, norb = 8, 22
+    pp = oracle.odd_coulomb_list(norb)
+    b = oracle.basis(N, norb, 0)
+    v0 = oracle.start_vector(len(b), 42)
+    kt, vt = oracle.quartic_tables(norb, pp)
+    rp, c, v = oracle.build_upper(b, norb, kt, vt)
+    wref, _ = oracle.lowest_eigenpairs(rp, c, v, 5, tol=1e-12, v0=v0)
+    for kw in ({}, {"store_upper": True}, {"matrix_free": True}):
+        m, ok = model(N, norb, 0, pp, 5, tol=1e-10, v0=v0, **kw)
+        assert ok, m.hamiltonian.last_info
+        w = m.hamiltonian.m_eigenvalues
+        assert np.max(np.abs(w - wref) / np.abs(wref)) <= 1e-10, (w, wref)
+        info = m.hamiltonian.last_info
+        assert info["max_residual"] <= 1e-10 and info["converged"] == 5
+        X = m.hamiltonian.m_eigenvectors
+        for i in range(5):
+            r = oracle.spmv_sym_upper(rp, c, v, X[i]) - w[i] * X[i]
+            assert np.linalg.norm(r) <= 1e-10
+        assert np.max(np.abs(X @ X.T - np.eye(5))) < 1e-10
+
+
+def test_sweep_sector_matches_arpack(cuda, oracle):
+    N, norb = 10, 28
+    pp = oracle.sweep_list(norb, 0.9)
+    b = oracle.basis(N, norb, 4)
+    kt, vt = oracle.quartic_tables(norb, pp)
+    rp, c, v = oracle.build_upper(b, norb, kt, vt)
+    fr, fc, fv = oracle.upper_to_full(rp, c, v, len(b))
+    A = sp.csr_matrix((fv, fc, fr), shape=(len(b), len(b)))
+    import scipy.sparse.linalg as sla
+    v0 = oracle.start_vector(len(b), 3)
+    wref = np.sort(sla.eigsh(A, k=4, which="SA", tol=1e-13, v0=v0)[0])
+    m, ok = model(N, norb, 4, pp, 4, tol=1e-10, v0=v0)
+    assert ok
+    w = m.hamiltonian.m_eigenvalues
+    assert np.max(np.abs(w - wref) / np.abs(wref)) <= 1e-10
+
+
+def test_two_particle_and_laughlin_known_answers(cuda):
+    # N=2: levels are 2*V_m (the reference's normalisation); 2S = 9 -> 10 orbitals
+    pp = [0.0, 1.3, 0.0, 0.7, 0.0, 0.25, 0.0, 0.1, 0.0]
+    m, ok = model(2, 10, 0, pp, 4, tol=1e-12)
+    assert ok
+    assert np.allclose(m.hamiltonian.m_eigenvalues, [0.0, 0.2, 0.5, 1.4], atol=1e-12)
+    # V1 only at 2S = 3(N-1): the Laughlin state has exactly zero energy
+    m, ok = model(6, 16, 0, [0.0, 1.0], 2, tol=1e-11)
+    assert ok
+    assert abs(m.hamiltonian.m_eigenvalues[0]) < 1e-10 and m.hamiltonian.m_eigenvalues[1] > 1e-3
+
+
+def test_host_callback_operator_and_dense_path(cuda, oracle):
+    # std::function form: a host matvec; n < 60 goes through the dense path
+    for n in (40, 300):
+        rng = np.random.default_rng(n)
+        Q = np.linalg.qr(rng.standard_normal((n, n)))[0]
+        d = np.sort(rng.uniform(-3, 5, n))
+        A = (Q * d) @ Q.T
+        arp = ed.ArpackWrapper()
+        ev = np.empty(3)
+        vec = np.empty((3, n))
+        ok = arp.DiagonalizeSymmetricMatrix(lambda x, y: np.copyto(y, A @ x), vec, ev, n, n, 3, tol=1e-11)
+        assert ok, arp.last_info
+        assert np.allclose(ev, d[:3], atol=1e-10)
+
+
+def test_breakdown_in_invariant_subspace(cuda):
+    # A diagonal operator with 4 distinct eigenvalues: the Krylov space is
+    # exhausted after 4 steps and the solver must restart with fresh vectors
+    n = 500
+    d = np.repeat([-2.0, -1.0, 0.5, 3.0], n // 4)
+    arp = ed.ArpackWrapper()
+    ev = np.empty(3)
+    ok = arp.DiagonalizeSymmetricMatrix(lambda x, y: np.multiply(d, x, out=y), None, ev, n, n, 3, tol=1e-10,
+                                        v0=np.ones(n))
+    assert ok, arp.last_info
+    assert arp.last_info["breakdowns"] >= 1
+    assert np.allclose(ev, [-2.0, -2.0, -2.0], atol=1e-10)
+
+
+def test_no_convergence_reported(cuda, oracle):
+    N, norb = 8, 22
+    H = ed.SpinlessFermionHamiltonian()
+    H.Initialize(N, norb, twoLz=0)
+    H.Add_CdCdCC_Terms(ed.QuarticTermTables(norb, oracle.odd_coulomb_list(norb)))
+    ok = H.LanczosDiagonalize(5, tol=1e-30, max_restarts=1)
+    assert ok is False
+    assert H.last_info["restarts"] == 1
+    # the best Ritz values so far are still returned and are close
+    assert np.all(np.isfinite(H.m_eigenvalues))
+
+
+def test_zero_start_vector_rejected(cuda):
+    H = ed.SpinlessFermionHamiltonian()
+    H.Initialize(4, 12, twoLz=0)
+    H.Add_CdCdCC_Terms(ed.QuarticTermTables(12, [0.0, 1.0]))
+    ok = H.LanczosDiagonalize(2, v0=np.zeros(H.GetDimension()))
+    assert ok is False
+
+
+def test_one_call_solve_matches_stepwise(cuda, oracle):
+    N, norb = 8, 22
+    pp = oracle.odd_coulomb_list(norb)
+    n = len(oracle.basis(N, norb, 0))
+    v0 = oracle.start_vector(n, 42)
+    out = ed.solve_sector(N, norb, 0, pp, 5, tol=1e-10, v0=v0, want_vectors=True)
+    m, ok = model(N, norb, 0, pp, 5, tol=1e-10, v0=v0)
+    assert np.max(np.abs(out["eigenvalues"] - m.hamiltonian.m_eigenvalues)) <= 1e-11
+    assert out["info"]["max_residual"] <= 1e-10
+    out2 = ed.solve_sector(N, norb, 0, pp, 5, tol=1e-10, v0=v0, matrix_free=True)
+    assert np.max(np.abs(out2["eigenvalues"] - out["eigenvalues"])) <= 1e-11
