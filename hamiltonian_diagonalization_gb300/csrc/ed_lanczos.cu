@@ -635,7 +635,10 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
         k = kk;
         ED_CUDA(cudaStreamSynchronize(st));
     }
-    for (int i = 0; i < nev; ++i) evals_host[i] = theta[i];
+    // an unconverged run can end inside a breakdown cycle with fewer Ritz
+    // pairs than requested: report the ones there are, NaN for the rest
+    const int nfound = std::min(nev, m_eff);
+    for (int i = 0; i < nev; ++i) evals_host[i] = i < nfound ? theta[i] : std::nan("");
     DevBuf<double> xtmp;
     double* X = evecs_dev;
     if (!X && p.verify) {
@@ -643,10 +646,11 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
         X = xtmp.p;
     }
     if (X) {
+        if (nfound < nev) ED_CUDA(cudaMemsetAsync(X, 0, (size_t)n * nev * 8, st));
         ED_CUDA(cudaMemcpyAsync(w.Y.p, Y.data(), (size_t)m_eff * m_eff * 8, cudaMemcpyHostToDevice, st));
-        gemm_vy(w.V.p, n, m_eff, w.Y.p, m_eff, nev, X, st);
+        gemm_vy(w.V.p, n, m_eff, w.Y.p, m_eff, nfound, X, st);
     }
-    if (p.verify && X) {
+    if (p.verify && X && nfound == nev) {
         std::vector<double> res(nev);
         residual_norms(op, X, evals_host, nev, res.data(), st);
         inf.matvecs += nev;

@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(256) k_hv_matfree(const uint64_t* __restrict__
                     const double v = hop_element(hv, in, out, a, b, c, d);
                     if (v == 0.0) continue;
                     const uint64_t j = rank_in_sector(out, hi, lo_tab, L);
+                    if (j >= (uint64_t)n) continue;   // cannot happen for a sector word; never read out of range
                     acc = fma(v, __ldg(x + j), acc);
                 }
             }
