@@ -468,6 +468,19 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     ed_solve_info inf;
     std::memset(&inf, 0, sizeof(inf));
 
+    if (v0_dev) {
+        // a start vector must be finite and nonzero on every path
+        const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
+        DevBuf<double> part(2 * (size_t)nb);
+        k_dot2<<<nb, kThreads, 0, st>>>(v0_dev, v0_dev, n, part.p, nullptr); ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
+        std::vector<double> h(2 * (size_t)nb);
+        ED_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        double nn = 0.0;
+        for (int i = 0; i < nb; ++i) nn += h[i];
+        ED_REQUIRE(nn > 0.0 && std::isfinite(nn), ED_ERR_ARG, "start vector is zero or not finite");
+    }
     // The reference switches to dense LAPACK below dimension 60
     // (pseudopotential_model_base.hpp:244-251); so do we.
     if (n < 60 || n <= (int64_t)nev + 2) {

@@ -1,0 +1,384 @@
+// ed_host.hpp - C++ host classes with the reference's call surface for the
+// exact-diagonalization hot path, implemented over the C ABI (ed_capi.h).
+//
+// Drop-in names and argument meaning of SimonDavenport/hamiltonian_diagonalization:
+//   diagonalization::FermionFockBasis            basis/fermion_fock_basis.hpp:45
+//   diagonalization::QuarticTermTables           fqhe_sphere/pseudopotential_model/term_tables.hpp
+//   diagonalization::SpinlessFermionHamiltonian  hamiltonians/spinless_fermion_hamiltonian.hpp:52
+//   diagonalization::MatrixVectorFunction        hamiltonians/matrix_vector_routines.hpp:41
+//   utilities::linearAlgebra::ArpackWrapper      utilities/wrappers/arpack_wrapper.hpp:187
+//   utilities::MpiWrapper                        a single-rank stand-in; accepted and ignored
+// Differences, all deliberate:
+//   - GenerateFockSpace takes the Lz sector (twice Lz) instead of a
+//     std::function predicate: the device enumerates the sector directly.
+//   - MatrixVectorFunction::Simple takes DEVICE vectors (the Krylov basis
+//     lives in HBM).  ArpackWrapper still accepts a host std::function
+//     product, called once per product with host vectors.
+//   - Failures set mpi.m_exitFlag and print to std::cerr like the reference,
+//     and also raise utilities::EdError from the call that failed.
+//   - Eigenvalues come back sorted ascending.
+// Link with -ledgb300 (hamiltonian_diagonalization_gb300/libedgb300.so).
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ed_capi.h"
+
+namespace utilities {
+
+typedef uint64_t fock_t;
+
+enum storageMethod_t { _DENSE_ = 0, _SPARSE_MAPPED_ = 1, _SPARSE_CRS_ = 2 };
+
+struct MpiWrapper {
+    int m_id = 0;
+    int m_nbrProcs = 1;
+    bool m_exitFlag = false;
+    void ExitFlagTest() const
+    {
+        if (m_exitFlag) throw std::runtime_error("exit flag set");
+    }
+};
+
+struct EdError : std::runtime_error {
+    ed_status status;
+    EdError(ed_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void EdCheck(ed_status s, MpiWrapper* mpi = nullptr)
+{
+    if (s != ED_OK) {
+        std::string msg = std::string(ed_status_string(s)) + ": " + ed_last_error();
+        std::cerr << "\n\tERROR: " << msg << std::endl;
+        if (mpi) mpi->m_exitFlag = true;
+        throw EdError(s, msg);
+    }
+}
+
+}  // namespace utilities
+
+namespace diagonalization {
+
+using utilities::fock_t;
+typedef uint32_t iSize_t;
+typedef uint16_t kState_t;
+typedef int16_t mState_t;
+
+// Quartic term tables: kTable[(k4*K+k3)*K+k2] = k1, vTable[...] = V_{k1k2k3k4}.
+class QuarticTermTables {
+  public:
+    QuarticTermTables() = default;
+    QuarticTermTables(const QuarticTermTables&) = delete;
+    QuarticTermTables& operator=(const QuarticTermTables&) = delete;
+    ~QuarticTermTables() { if (m_h) ed_terms_free(m_h); }
+
+    // BaseGenerate4KTable + BaseTermsFromPseudopotentials for one Landau level
+    void Initialize(iSize_t nbrOrbitals, const std::vector<double>& pseudopotentials)
+    {
+        m_kMax = nbrOrbitals;
+        const size_t K3 = (size_t)m_kMax * m_kMax * m_kMax;
+        m_kTable.assign(K3, 0);
+        m_vTable.assign(K3, 0.0);
+        utilities::EdCheck(ed_quartic_tables((int)m_kMax, pseudopotentials.data(), (int)pseudopotentials.size(),
+                                             m_kTable.data(), m_vTable.data()));
+        Reset();
+    }
+    // Tables supplied by the caller (e.g. read from a file)
+    void SetTables(iSize_t nbrOrbitals, const std::vector<kState_t>& kTable, const std::vector<double>& vTable)
+    {
+        m_kMax = nbrOrbitals;
+        m_kTable = kTable;
+        m_vTable = vTable;
+        Reset();
+    }
+    iSize_t GetMaxKCount() const { return 1; }
+    void GetK1(kState_t* buf, iSize_t& nbrK1, kState_t k2, kState_t k3, kState_t k4) const
+    {
+        nbrK1 = 1;
+        buf[0] = m_kTable[((size_t)k4 * m_kMax + k3) * m_kMax + k2];
+        if (buf[0] >= m_kMax) nbrK1 = 0;
+    }
+    double GetVkkkk(kState_t, kState_t k2, kState_t k3, kState_t k4) const
+    {
+        return m_vTable[((size_t)k4 * m_kMax + k3) * m_kMax + k2];
+    }
+    iSize_t GetKMax() const { return m_kMax; }
+    ed_terms* handle()
+    {
+        if (!m_h) utilities::EdCheck(ed_terms_set((int)m_kMax, m_kTable.data(), m_vTable.data(), &m_h));
+        return m_h;
+    }
+
+  private:
+    void Reset()
+    {
+        if (m_h) ed_terms_free(m_h);
+        m_h = nullptr;
+    }
+    iSize_t m_kMax = 0;
+    std::vector<kState_t> m_kTable;
+    std::vector<double> m_vTable;
+    ed_terms* m_h = nullptr;
+};
+
+class FermionFockBasis {
+  public:
+    FermionFockBasis() = default;
+    FermionFockBasis(const FermionFockBasis&) = delete;
+    FermionFockBasis& operator=(const FermionFockBasis&) = delete;
+    ~FermionFockBasis() { if (m_h) ed_basis_free(m_h); }
+
+    // fermion_fock_basis.cpp:241: returns true when the sector is empty
+    bool GenerateFockSpace(iSize_t nbrParticles, iSize_t nbrOrbitals, int twoLz, utilities::MpiWrapper& mpi)
+    {
+        if (m_h) ed_basis_free(m_h);
+        m_h = nullptr;
+        utilities::EdCheck(ed_basis_build((int)nbrParticles, (int)nbrOrbitals, twoLz, nullptr, &m_h), &mpi);
+        m_basisStored = true;
+        return GetStoredDimension() == 0;
+    }
+    fock_t GetStoredDimension() const
+    {
+        uint64_t d = 0;
+        if (m_h) utilities::EdCheck(ed_basis_dim(m_h, &d));
+        return d;
+    }
+    // fermion_fock_basis.cpp:134: UINT64_MAX when absent
+    fock_t FindFockStateIndex(fock_t offset, fock_t state) const
+    {
+        uint64_t idx = 0;
+        utilities::EdCheck(ed_basis_rank_host(m_h, &state, &idx, 1));
+        return idx == ~0ull ? idx : idx + offset;
+    }
+    void FindFockStateIndices(const fock_t* states, fock_t* idx, fock_t m) const
+    {
+        utilities::EdCheck(ed_basis_rank_host(m_h, states, idx, m));
+    }
+    // fermion_fock_basis.cpp:359
+    void GetFockBasis(fock_t* buffer, fock_t dim, utilities::MpiWrapper& mpi) const
+    {
+        utilities::EdCheck(ed_basis_get(m_h, buffer, dim), &mpi);
+    }
+    ed_basis* handle() const { return m_h; }
+    bool m_basisStored = false;
+
+  private:
+    ed_basis* m_h = nullptr;
+};
+
+template <typename T>
+class SpinlessFermionHamiltonian;
+
+template <typename T, class L1 = QuarticTermTables, class L2 = QuarticTermTables>
+class MatrixVectorFunction {
+  public:
+    MatrixVectorFunction(SpinlessFermionHamiltonian<T>& hamiltonian, const utilities::MpiWrapper&)
+        : hamiltonian(&hamiltonian) {}
+    // matrix_vector_routines.hpp:94: y = H x on device vectors of the sector dimension
+    void Simple(T* x, T* y, const utilities::MpiWrapper&) { hamiltonian->Apply(x, y); }
+    SpinlessFermionHamiltonian<T>* hamiltonian;
+};
+
+namespace detail {
+inline void host_trampoline(const double* x, double* y, void* user)
+{
+    auto* fn = static_cast<std::function<void(double*, double*, utilities::MpiWrapper&)>*>(user);
+    utilities::MpiWrapper mpi;
+    (*fn)(const_cast<double*>(x), y, mpi);
+}
+}  // namespace detail
+
+}  // namespace diagonalization
+
+namespace utilities {
+namespace linearAlgebra {
+
+class ArpackWrapper {
+  public:
+    ArpackWrapper() = default;
+    void SetMaxIterations(int maxIterations) { m_maxIterations = maxIterations; }
+    void SetTolerance(double tol) { m_tol = tol; }
+    void SetNcv(int ncv) { m_ncv = ncv; }
+    void SetSeed(uint64_t seed) { m_seed = seed; }
+    // start vector (host, nodeDim doubles) in place of --use-initial's file
+    void SetInitialVector(const std::vector<double>& v) { m_initial = v; }
+    const ed_solve_info& LastInfo() const { return m_info; }
+
+    // arpack_wrapper.hpp:595: generic host product (std::function form)
+    template <typename T>
+    bool DiagonalizeSymmetricMatrix(const std::function<void(T*, T*, MpiWrapper&)>& MatrixVectorMultiply,
+                                    T* eigenvectors, double* eigenvalues, int nodeDim, int fullDim, int nbrEigenvalues,
+                                    MpiWrapper& mpi)
+    {
+        static_assert(sizeof(T) == sizeof(double), "real FP64 only");
+        if (nodeDim != fullDim) return Fail(ED_ERR_ARG, "one device holds the whole vector", mpi);
+        std::function<void(double*, double*, MpiWrapper&)> fn = MatrixVectorMultiply;
+        ed_op* op = nullptr;
+        ed_status s = ed_op_host_callback(fullDim, &diagonalization::detail::host_trampoline, &fn, &op);
+        if (s != ED_OK) return Fail(s, ed_last_error(), mpi);
+        const bool ok = Run(op, eigenvectors, eigenvalues, fullDim, nbrEigenvalues, mpi);
+        ed_op_free(op);
+        return ok;
+    }
+
+    // the device product of a built Hamiltonian (the fast path)
+    template <typename T, class L1, class L2>
+    bool DiagonalizeSymmetricMatrix(diagonalization::MatrixVectorFunction<T, L1, L2>& mv, T* eigenvectors,
+                                    double* eigenvalues, int nodeDim, int fullDim, int nbrEigenvalues, MpiWrapper& mpi)
+    {
+        if (nodeDim != fullDim) return Fail(ED_ERR_ARG, "one device holds the whole vector", mpi);
+        ed_op* op = mv.hamiltonian->MakeOperator();
+        const bool ok = Run(op, eigenvectors, eigenvalues, fullDim, nbrEigenvalues, mpi);
+        ed_op_free(op);
+        return ok;
+    }
+
+  private:
+    bool Fail(ed_status s, const std::string& msg, MpiWrapper& mpi)
+    {
+        std::cerr << "\n\tERROR in DiagonalizeSymmetricMatrix: " << ed_status_string(s) << ": " << msg << std::endl;
+        mpi.m_exitFlag = true;
+        m_status = s;
+        return false;
+    }
+    bool Run(ed_op* op, double* eigenvectors, double* eigenvalues, int n, int nev, MpiWrapper& mpi)
+    {
+        ed_lanczos_params p{};
+        p.nev = nev;
+        p.ncv = m_ncv;
+        p.max_restarts = m_maxIterations;
+        p.tol = m_tol;
+        p.seed = m_seed;
+        p.want_vectors = eigenvectors != nullptr;
+        p.verify = 1;
+        const double* v0 = ((int)m_initial.size() == n) ? m_initial.data() : nullptr;
+        ed_status s = ed_lanczos(op, &p, v0, eigenvalues, eigenvectors, &m_info);
+        m_status = s;
+        if (s != ED_OK) return Fail(s, ed_last_error(), mpi);
+        return true;
+    }
+    int m_maxIterations = 2000;
+    int m_ncv = 0;
+    double m_tol = 1e-10;
+    uint64_t m_seed = 0;
+    std::vector<double> m_initial;
+    ed_solve_info m_info{};
+    ed_status m_status = ED_OK;
+};
+
+}  // namespace linearAlgebra
+}  // namespace utilities
+
+namespace diagonalization {
+
+template <typename T>
+class SpinlessFermionHamiltonian {
+    static_assert(sizeof(T) == sizeof(double), "the device path is real FP64");
+
+  public:
+    SpinlessFermionHamiltonian() = default;
+    SpinlessFermionHamiltonian(const SpinlessFermionHamiltonian&) = delete;
+    SpinlessFermionHamiltonian& operator=(const SpinlessFermionHamiltonian&) = delete;
+    ~SpinlessFermionHamiltonian() { Clear(); }
+
+    // spinless_fermion_hamiltonian.hpp:59 (+ the sector, which the reference
+    // passes to its basis separately)
+    void Initialize(iSize_t nbrParticles, iSize_t nbrOrbitals, utilities::storageMethod_t storageMethod,
+                    utilities::MpiWrapper& mpi, int twoLz = 0)
+    {
+        if (nbrParticles == 0 || nbrOrbitals == 0 || nbrParticles >= 64 || nbrParticles > nbrOrbitals) {
+            std::cerr << "\n\tERROR: bad particle/orbital numbers" << std::endl;
+            mpi.m_exitFlag = true;
+            throw utilities::EdError(ED_ERR_ARG, "bad particle/orbital numbers");
+        }
+        m_nbrParticles = nbrParticles;
+        m_nbrOrbitals = nbrOrbitals;
+        m_storageMethod = storageMethod;
+        m_fockBasis.GenerateFockSpace(nbrParticles, nbrOrbitals, twoLz, mpi);
+    }
+    // spinless_fermion_hamiltonian.hpp:282.  The whole sector is built in one
+    // device call; minRow/maxRow are accepted for signature compatibility.
+    template <class L>
+    void Add_CdCdCC_Terms(L* termTables, fock_t /*minRow*/, fock_t /*maxRow*/, utilities::MpiWrapper& mpi,
+                          bool storeUpper = false)
+    {
+        if (m_crs) ed_crs_free(m_crs);
+        m_crs = nullptr;
+        m_terms = termTables;
+        utilities::EdCheck(ed_ham_build_crs(m_fockBasis.handle(), termTables->handle(), storeUpper ? 1 : 0, nullptr,
+                                            &m_crs),
+                           &mpi);
+    }
+    // regenerate elements on the fly instead of storing them
+    template <class L>
+    void SetMatrixFree(L* termTables)
+    {
+        if (m_crs) ed_crs_free(m_crs);
+        m_crs = nullptr;
+        m_terms = termTables;
+    }
+    fock_t GetFockSpaceDimension() const { return m_fockBasis.GetStoredDimension(); }
+    int64_t GetNbrNonZeros() const
+    {
+        int64_t nnz = 0;
+        if (m_crs) utilities::EdCheck(ed_crs_info(m_crs, nullptr, &nnz, nullptr));
+        return nnz;
+    }
+    void GetCrs(std::vector<int64_t>& rowStarts, std::vector<int32_t>& cols, std::vector<double>& data) const
+    {
+        int64_t n = 0, nnz = 0;
+        utilities::EdCheck(ed_crs_info(m_crs, &n, &nnz, nullptr));
+        rowStarts.resize(n + 1);
+        cols.resize(nnz);
+        data.resize(nnz);
+        utilities::EdCheck(ed_crs_get(m_crs, rowStarts.data(), cols.data(), data.data()));
+    }
+    void Apply(const double* x_dev, double* y_dev)
+    {
+        if (m_crs) utilities::EdCheck(ed_spmv(m_crs, x_dev, y_dev, nullptr));
+        else utilities::EdCheck(ed_hv_matfree(m_fockBasis.handle(), m_terms->handle(), x_dev, y_dev, nullptr));
+    }
+    ed_op* MakeOperator()
+    {
+        ed_op* op = nullptr;
+        if (m_crs) utilities::EdCheck(ed_op_from_crs(m_crs, &op));
+        else utilities::EdCheck(ed_op_matfree(m_fockBasis.handle(), m_terms->handle(), &op));
+        return op;
+    }
+    // hamiltonian_base.hpp:770
+    bool LanczosDiagonalize(iSize_t nbrEigenvalues, utilities::MpiWrapper& mpi, double tol = 1e-10,
+                            bool wantVectors = true)
+    {
+        const fock_t n = GetFockSpaceDimension();
+        m_eigenvalues.assign(nbrEigenvalues, 0.0);
+        m_eigenvectors.assign(wantVectors ? (size_t)n * nbrEigenvalues : 0, 0.0);
+        MatrixVectorFunction<T> mv(*this, mpi);
+        m_arpackWrapper.SetTolerance(tol);
+        return m_arpackWrapper.DiagonalizeSymmetricMatrix(mv, wantVectors ? m_eigenvectors.data() : nullptr,
+                                                          m_eigenvalues.data(), (int)n, (int)n, (int)nbrEigenvalues,
+                                                          mpi);
+    }
+    void Clear()
+    {
+        if (m_crs) ed_crs_free(m_crs);
+        m_crs = nullptr;
+    }
+
+    FermionFockBasis m_fockBasis;
+    utilities::linearAlgebra::ArpackWrapper m_arpackWrapper;
+    std::vector<double> m_eigenvalues;
+    std::vector<double> m_eigenvectors;   // column-major n x nev
+
+  private:
+    iSize_t m_nbrParticles = 0, m_nbrOrbitals = 0;
+    utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
+    ed_crs* m_crs = nullptr;
+    QuarticTermTables* m_terms = nullptr;
+};
+
+}  // namespace diagonalization

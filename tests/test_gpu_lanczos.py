@@ -115,12 +115,17 @@ def test_no_convergence_reported(cuda, oracle):
     assert np.all(np.isfinite(H.m_eigenvalues))
 
 
-def test_zero_start_vector_rejected(cuda):
-    H = ed.SpinlessFermionHamiltonian()
-    H.Initialize(4, 12, twoLz=0)
-    H.Add_CdCdCC_Terms(ed.QuarticTermTables(12, [0.0, 1.0]))
-    ok = H.LanczosDiagonalize(2, v0=np.zeros(H.GetDimension()))
-    assert ok is False
+def test_bad_start_vector_rejected(cuda):
+    for (N, norb) in [(4, 12), (6, 16)]:      # dense path (dim < 60) and Lanczos path
+        H = ed.SpinlessFermionHamiltonian()
+        H.Initialize(N, norb, twoLz=0)
+        H.Add_CdCdCC_Terms(ed.QuarticTermTables(norb, [0.0, 1.0]))
+        n = H.GetDimension()
+        assert H.LanczosDiagonalize(2, v0=np.zeros(n)) is False
+        bad = np.ones(n)
+        bad[3] = np.nan
+        assert H.LanczosDiagonalize(2, v0=bad) is False
+        assert H.LanczosDiagonalize(2, v0=np.ones(n)) is True
 
 
 def test_one_call_solve_matches_stepwise(cuda, oracle):
@@ -134,3 +139,23 @@ def test_one_call_solve_matches_stepwise(cuda, oracle):
     assert out["info"]["max_residual"] <= 1e-10
     out2 = ed.solve_sector(N, norb, 0, pp, 5, tol=1e-10, v0=v0, matrix_free=True)
     assert np.max(np.abs(out2["eigenvalues"] - out["eigenvalues"])) <= 1e-11
+
+
+def test_stored_crs_config_matches_arpack_fixture(cuda):
+    # N=11, 2S=30, Lz=0 (1,371,535 states): the 10 lowest eigenvalues against
+    # the reference-family ARPACK run recorded in tests/golden
+    import json
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "arpack_n11_2s30_lz0.json")
+    if not os.path.exists(path):
+        pytest.skip("ARPACK fixture not generated yet (tests/golden/make_arpack_fixture.py)")
+    ref = json.load(open(path))
+    n = ref["n"]
+    v0 = np.random.default_rng(ref["seed"]).uniform(-1.0, 1.0, n)
+    v0 /= np.linalg.norm(v0)
+    out = ed.solve_sector(ref["N"], ref["norb"], ref["two_lz"], ed.odd_coulomb_list(ref["norb"]), ref["nev"],
+                          tol=1e-10, v0=v0)
+    w = out["eigenvalues"]
+    wref = np.array(ref["eigenvalues"])
+    assert np.max(np.abs(w - wref) / np.abs(wref)) <= 1e-10, (w, wref)
+    assert out["info"]["max_residual"] <= 1e-10
