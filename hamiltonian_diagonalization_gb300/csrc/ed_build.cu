@@ -217,8 +217,12 @@ void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, c
     const int64_t maxrow = reduce_max_i64_host(rowlen.p, n, st);
     ED_CUDA(cudaStreamSynchronize(st));
     a.max_row = (int)maxrow;
-    a.col.alloc(a.nnz > 0 ? (size_t)a.nnz : 1);
-    a.val.alloc(a.nnz > 0 ? (size_t)a.nnz : 1);
+    // kCrsPad zeroed elements past the end let the SpMV batches load
+    // without bounds tests (column 0, value 0)
+    a.col.alloc((size_t)a.nnz + kCrsPad);
+    a.val.alloc((size_t)a.nnz + kCrsPad);
+    ED_CUDA(cudaMemsetAsync(a.col.p + a.nnz, 0, kCrsPad * sizeof(int32_t), st));
+    ED_CUDA(cudaMemsetAsync(a.val.p + a.nnz, 0, kCrsPad * sizeof(double), st));
     int cap = 32;
     while (cap < maxrow) cap <<= 1;
     const size_t tbytes = (tsm + 15) & ~(size_t)15;

@@ -20,6 +20,7 @@ constexpr int kMaxOrbitals = 40;
 constexpr uint64_t kMiss = ~0ull;             // FindFockStateIndex miss code
 constexpr double kSparseZeroTol = 1e-14;      // hamiltonian_data.hpp:53
 constexpr double kCgEps = 1e-12;              // clebsch_gordan_coefficients.hpp:53
+constexpr int64_t kCrsPad = 256;              // zeroed CRS elements after the last row
 
 struct Error : std::runtime_error {
     ed_status code;
