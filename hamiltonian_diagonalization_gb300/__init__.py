@@ -7,6 +7,7 @@ from .host import (  # noqa: F401
     ArpackWrapper,
     CrsSparseMatrix,
     FermionFockBasis,
+    HamiltonianBatch,
     MatrixVectorFunction,
     MpiWrapper,
     QuarticTermTables,

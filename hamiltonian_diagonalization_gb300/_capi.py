@@ -50,6 +50,15 @@ class SolveInfo(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("converged", c_int), ("restarts", c_int), ("block_products", c_i64), ("max_residual", c_double),
+                ("seconds", c_double), ("spmm_seconds", c_double), ("breakdowns", c_int),
+                ("tile_hamiltonians", c_int), ("tile_unroll", c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 HOST_MATVEC = ctypes.CFUNCTYPE(None, P(c_double), P(c_double), c_void_p)
 
 _SIGS = {
@@ -85,9 +94,15 @@ _SIGS = {
     "ed_lanczos": (c_int, [c_void_p, P(LanczosParams), P(c_double), P(c_double), P(c_double), P(SolveInfo)]),
     "ed_lanczos_device": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(SolveInfo)]),
     "ed_residuals": (c_int, [c_void_p, c_void_p, P(c_double), c_int, P(c_double)]),
+    "ed_kernel_launches": (c_u64, []),
     "ed_dense_sym_eigen": (c_int, [c_int, P(c_double), P(c_double), P(c_double)]),
     "ed_solve_sector": (c_int, [c_int, c_int, c_int, P(c_double), c_int, c_int, P(LanczosParams), P(c_double),
                                 P(c_double), P(c_double), P(SolveInfo)]),
+    "ed_batch_create": (c_int, [c_void_p, c_int, P(ctypes.c_uint16), P(c_double), c_int, P(c_void_p)]),
+    "ed_batch_free": (c_int, [c_void_p]),
+    "ed_batch_dims": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
+    "ed_batch_spmm": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ed_batch_solve": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(BatchInfo)]),
 }
 
 _LIB = None

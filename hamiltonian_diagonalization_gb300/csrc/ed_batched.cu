@@ -1,0 +1,923 @@
+// Batched sweep (K6): many Hamiltonians of one Lz sector that differ only in
+// their pseudopotentials, solved together in lockstep.
+//
+// All of them share the sparsity pattern: an element of H(V) is
+// sign(state) * W_V[hop] for the pair hop it belongs to, and only the per-hop
+// table W_V depends on the pseudopotentials.  The pattern is built once per
+// sector as CRS with an int32 column and a uint16 code per element (bit 15 =
+// fermionic sign, bits 0..14 = hop index; diagonal elements live in a
+// separate n x B array).  The block product Y[:,b] = H_b X[:,b] stages the
+// per-Hamiltonian hop tables of a tile of TB Hamiltonians in shared memory and
+// gives each lane one (row, Hamiltonian) pair, so every element costs one FP64
+// FMA and no cross-lane reduction; the column and code of an element are
+// loaded once for the TB lanes that share the row.
+//
+// Vectors are stored [row][problem] (problem index fastest) so the gathers of
+// a tile of Hamiltonians read one contiguous segment.  The thick-restart
+// Lanczos of ed_lanczos.cu runs here for B problems at once: the same
+// recurrences, full FP64 reorthogonalisation and restarts, with every scalar
+// per problem and every kernel covering all problems.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ed_hop.cuh"
+#include "ed_lanczos.h"
+
+struct ed_batch {
+    int B = 0;                    // Hamiltonians
+    int K = 0, N = 0;
+    int64_t n = 0, nnz = 0;       // sector dimension, off-diagonal pattern entries
+    int nhop = 0;
+    edgb::DevBuf<int64_t> rowptr;
+    edgb::DevBuf<int32_t> col;    // nnz + pad
+    edgb::DevBuf<uint16_t> code;  // nnz + pad
+    edgb::DevBuf<double> w;       // [nhop][B] per-Hamiltonian hop values
+    edgb::DevBuf<double> diag;    // [n][B]
+    int tb = 8, unroll = 8;       // tuned tile of Hamiltonians per CTA, load batch
+};
+
+namespace edgb {
+
+namespace {
+
+constexpr uint16_t kCodeSign = 0x8000;
+
+int sms_b()
+{
+    int dev = 0, s = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return s;
+}
+
+// Element code for the pair hop (a,b)->(c,d) of `in` (canonical direction
+// as in hop_element); keep = the hop exists in at least one Hamiltonian.
+__device__ __forceinline__ uint16_t hop_code(const HopView& hv, uint64_t in, uint64_t out, int a, int b, int c, int d,
+                                             bool& keep)
+{
+    const int s = a + b;
+    const int lo = pair_lo(s, hv.K), cnt = pair_cnt(s, hv.K);
+    int h, par;
+    if (out > in) {
+        h = hv.off[s] + (a - lo) * cnt + (c - lo);
+        par = hop_parity(in, a, b, c, d);
+    } else {
+        h = hv.off[s] + (c - lo) * cnt + (a - lo);
+        par = hop_parity(out, c, d, a, b);
+    }
+    keep = hv.w[h] != 0.0;
+    return (uint16_t)((par ? kCodeSign : 0) | h);
+}
+
+// off-diagonal entries per row of the union pattern
+__global__ void k_pat_count(const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ wu, int nw,
+                            const int* __restrict__ off, int K, int64_t* __restrict__ rowlen)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* sw = reinterpret_cast<double*>(smem);
+    int* soff = reinterpret_cast<int*>(sw + nw);
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = wu[i];
+    for (int i = threadIdx.x; i < 2 * K; i += blockDim.x) soff[i] = off[i];
+    __syncthreads();
+    const HopView hv{sw, nullptr, nullptr, soff, K};
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t in = words[r];
+        int64_t cnt = 0;
+        for (uint64_t ta = in; ta; ta &= ta - 1) {
+            const int a = __ffsll((long long)ta) - 1;
+            for (uint64_t tb = ta & (ta - 1); tb; tb &= tb - 1) {
+                const int b = __ffsll((long long)tb) - 1;
+                const int s = a + b;
+                const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
+                const int lo = pair_lo(s, K), pc = pair_cnt(s, K);
+                for (int ic = 0; ic < pc; ++ic) {
+                    const int c = lo + ic, d = s - c;
+                    if (c == a || ((rest >> c) & 1ull) || ((rest >> d) & 1ull)) continue;
+                    bool keep;
+                    hop_code(hv, in, rest | (1ull << c) | (1ull << d), a, b, c, d, keep);
+                    cnt += keep ? 1 : 0;
+                }
+            }
+        }
+        rowlen[r] = cnt;
+    }
+}
+
+// One warp per row: (out word, code) pairs, sorted by word, ranked, stored.
+__global__ void k_pat_fill(const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ wu, int nw,
+                           const int* __restrict__ off, int K, int N, const int64_t* __restrict__ rowptr,
+                           const uint64_t* __restrict__ hi, const uint64_t* __restrict__ lo_tab, int L, int cap,
+                           int32_t* __restrict__ col, uint16_t* __restrict__ code, int* __restrict__ err)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* sw = reinterpret_cast<double*>(smem);
+    int* soff = reinterpret_cast<int*>(sw + nw);
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = wu[i];
+    for (int i = threadIdx.x; i < 2 * K; i += blockDim.x) soff[i] = off[i];
+    __syncthreads();
+    const HopView hv{sw, nullptr, nullptr, soff, K};
+    const size_t tbytes = ((size_t)nw * 8 + (size_t)2 * K * 4 + 15) & ~(size_t)15;
+    const int wic = threadIdx.x >> 5, lane = threadIdx.x & 31, wpc = blockDim.x >> 5;
+    uint64_t* keys = reinterpret_cast<uint64_t*>(smem + tbytes) + (size_t)wic * cap;
+    uint32_t* pay = reinterpret_cast<uint32_t*>(smem + tbytes + (size_t)wpc * cap * 8) + (size_t)wic * cap;
+    int* counter = reinterpret_cast<int*>(smem + tbytes + (size_t)wpc * cap * 12) + wic;
+    unsigned char* occ = reinterpret_cast<unsigned char*>(smem + tbytes + (size_t)wpc * cap * 12 + wpc * 4) +
+                         (size_t)wic * 64;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int npairs = N * (N - 1) / 2;
+    for (int64_t r = gw; r < n; r += nwarps) {
+        const uint64_t in = words[r];
+        const int64_t base = rowptr[r];
+        const int64_t want = rowptr[r + 1] - base;
+        for (int pos0 = 0; pos0 < K; pos0 += 32) {
+            const int pos = pos0 + lane;
+            const bool set = pos < K && ((in >> pos) & 1ull);
+            const unsigned m = __ballot_sync(0xffffffffu, set);
+            if (set) occ[__popc(m & ((1u << lane) - 1u)) + __popcll(in & ((1ull << pos0) - 1ull))] = (unsigned char)pos;
+        }
+        if (lane == 0) *counter = 0;
+        __syncwarp();
+        for (int p = lane; p < npairs; p += 32) {
+            int j = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)p)) * 0.5f);
+            while (j * (j - 1) / 2 > p) --j;
+            while ((j + 1) * j / 2 <= p) ++j;
+            const int i = p - j * (j - 1) / 2;
+            const int a = occ[i], b = occ[j];
+            const int s = a + b;
+            const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
+            const int lo = pair_lo(s, K), pc = pair_cnt(s, K);
+            for (int ic = 0; ic < pc; ++ic) {
+                const int c = lo + ic, d = s - c;
+                if (c == a || ((rest >> c) & 1ull) || ((rest >> d) & 1ull)) continue;
+                const uint64_t out = rest | (1ull << c) | (1ull << d);
+                bool keep;
+                const uint16_t cd = hop_code(hv, in, out, a, b, c, d, keep);
+                if (!keep) continue;
+                const int slot = atomicAdd(counter, 1);
+                if (slot < cap) { keys[slot] = out; pay[slot] = cd; }
+            }
+        }
+        __syncwarp();
+        const int cnt = *counter;
+        if (cnt != want || cnt > cap) {
+            if (lane == 0) atomicOr(err, 1);
+            __syncwarp();
+            continue;
+        }
+        int P = 1;
+        while (P < cnt) P <<= 1;
+        for (int t = cnt + lane; t < P; t += 32) keys[t] = ~0ull;
+        __syncwarp();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (int t = lane; t < (P >> 1); t += 32) {
+                    const int i0 = ((t & ~(jj - 1)) << 1) | (t & (jj - 1));
+                    const int i1 = i0 + jj;
+                    const bool up = (i0 & k) == 0;
+                    const uint64_t k0 = keys[i0], k1 = keys[i1];
+                    if ((k0 > k1) == up) {
+                        keys[i0] = k1;
+                        keys[i1] = k0;
+                        const uint32_t p0 = pay[i0];
+                        pay[i0] = pay[i1];
+                        pay[i1] = p0;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        for (int t = lane; t < cnt; t += 32) {
+            const uint64_t c = rank_in_sector(keys[t], hi, lo_tab, L);
+            if (c == kMiss) atomicOr(err, 2);
+            col[base + t] = (int32_t)c;
+            code[base + t] = (uint16_t)pay[t];
+        }
+        __syncwarp();
+    }
+}
+
+// diag[r*B + b] for every Hamiltonian: the reference's term order, per-b tables
+__global__ void k_bdiag(const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ da,
+                        const double* __restrict__ db, int K, int B, double* __restrict__ diag)
+{
+    const int64_t total = n * (int64_t)B;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / B;
+        const int b = (int)(t - r * B);
+        const uint64_t in = words[r];
+        const double* ta = da + (size_t)b * K * K;
+        const double* tb = db + (size_t)b * K * K;
+        double acc = 0.0;
+        for (uint64_t t4 = in; t4; t4 &= t4 - 1) {
+            const int k4 = __ffsll((long long)t4) - 1;
+            for (uint64_t t3 = in & ~(1ull << k4); t3; t3 &= t3 - 1) {
+                const int k3 = __ffsll((long long)t3) - 1;
+                acc = acc + ta[k4 * K + k3];
+                acc = acc + tb[k4 * K + k3];
+            }
+        }
+        diag[t] = acc;
+    }
+}
+
+// Y[r][b] = diag[r][b] X[r][b] + sum_k sign_k W_b[h_k] X[col_k][b] for b in
+// this CTA's tile [b0, b0+TB).  Lane = (row slot, b); U loads in flight.
+template <int TB, int U>
+__global__ void __launch_bounds__(256) k_bspmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                               const uint16_t* __restrict__ code, const double* __restrict__ w,
+                                               int nhop, const double* __restrict__ diag, const double* __restrict__ X,
+                                               double* __restrict__ Y, int64_t n, int B)
+{
+    extern __shared__ double sw[];   // [nhop][TB]
+    const int b0 = blockIdx.y * TB;
+    for (int i = threadIdx.x; i < nhop * TB; i += blockDim.x) {
+        const int h = i / TB, t = i - h * TB;
+        sw[i] = (b0 + t < B) ? w[(size_t)h * B + b0 + t] : 0.0;
+    }
+    __syncthreads();
+    constexpr int RPW = 32 / TB;
+    const int lane = threadIdx.x & 31, bl = lane % TB, grp = lane / TB;
+    const int b = b0 + bl;
+    const bool bvalid = b < B;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {
+        const int64_t r = rb + grp;
+        if (r >= n || !bvalid) continue;
+        const int64_t s = rowptr[r], e = rowptr[r + 1];
+        double acc0 = diag[r * B + b] * X[r * B + b], acc1 = 0.0;
+        for (int64_t k = s; k < e; k += U) {
+            int c[U];
+            uint16_t cd[U];
+            double xv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) { c[u] = __ldg(col + k + u); cd[u] = __ldg(code + k + u); }
+#pragma unroll
+            for (int u = 0; u < U; ++u) xv[u] = __ldg(X + (int64_t)c[u] * B + b);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < e) {
+                    double wv = sw[(cd[u] & 0x7FFF) * TB + bl];
+                    if (cd[u] & kCodeSign) wv = -wv;
+                    if (u & 1) acc1 = fma(wv, xv[u], acc1);
+                    else acc0 = fma(wv, xv[u], acc0);
+                }
+            }
+        }
+        Y[r * B + b] = acc0 + acc1;
+    }
+}
+
+// ------------------------------------------------------ batched Lanczos kernels
+// Vectors [n][B]; a block owns a row chunk, thread t handles problem t % BP
+// (BP = B rounded up to a power of two) on rows t / BP, t / BP + 256/BP, ...
+
+constexpr int kBT = 256;
+
+__device__ __forceinline__ void chunk_rows(int64_t n, int nb, int b, int64_t& r0, int64_t& r1)
+{
+    r0 = n * (int64_t)b / nb;
+    r1 = n * (int64_t)(b + 1) / nb;
+}
+
+// sum over the 256/BP threads of each problem, partial to part[(q*nb + blk)*B + p]
+__device__ __forceinline__ void reduce_per_problem(double v, double* red, int BP, int B, double* out_slot_base,
+                                                   int64_t stride_q, int q)
+{
+    red[threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.x < BP) {
+        double s = 0.0;
+        for (int t = threadIdx.x; t < kBT; t += BP) s += red[t];
+        if (threadIdx.x < B) out_slot_base[stride_q * q + threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+// part[0][blk][p] = v_p . w_p, part[1][blk][p] = w_p . w_p
+__global__ void __launch_bounds__(kBT) k_bdot2(const double* __restrict__ v, const double* __restrict__ w, int64_t n,
+                                               int B, int BP, double* __restrict__ part)
+{
+    __shared__ double red[kBT];
+    int64_t r0, r1;
+    chunk_rows(n, gridDim.x, blockIdx.x, r0, r1);
+    const int p = threadIdx.x % BP, rl = threadIdx.x / BP, nrl = kBT / BP;
+    double a = 0.0, c = 0.0;
+    if (p < B)
+        for (int64_t r = r0 + rl; r < r1; r += nrl) {
+            const double wv = w[r * B + p];
+            a = fma(v[r * B + p], wv, a);
+            c = fma(wv, wv, c);
+        }
+    const int64_t sq = (int64_t)gridDim.x * B;
+    reduce_per_problem(a, red, BP, B, part + (int64_t)blockIdx.x * B, sq, 0);
+    reduce_per_problem(c, red, BP, B, part + (int64_t)blockIdx.x * B, sq, 1);
+}
+
+// out[q][p] = sum over blocks of part[q][blk][p] for q < Q
+__global__ void k_bsum(const double* __restrict__ part, int nb, int B, int Q, double* __restrict__ out)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < Q * B; t += gridDim.x * blockDim.x) {
+        const int q = t / B, p = t - q * B;
+        double s = 0.0;
+        for (int blk = 0; blk < nb; ++blk) s += part[((int64_t)q * nb + blk) * B + p];
+        out[t] = s;
+    }
+}
+
+// w_p -= alpha_p v_p + beta_p u_p
+__global__ void k_baxpy2(double* __restrict__ w, const double* __restrict__ v, const double* __restrict__ u, int64_t n,
+                         int B, const double* __restrict__ alpha, const double* __restrict__ beta)
+{
+    const int64_t total = n * (int64_t)B;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(t % B);
+        w[t] = fma(-beta[p], u[t], fma(-alpha[p], v[t], w[t]));
+    }
+}
+
+// part[i][blk][p] = V_i,p . w_p for i < J; part[J][blk][p] = w_p . w_p.
+// Problems with need[p] == 0 (when need is given) contribute zeros.
+__global__ void __launch_bounds__(kBT) k_bmdot(const double* __restrict__ V, int64_t n, int B, int BP, int J,
+                                               const double* __restrict__ w, double* __restrict__ part,
+                                               const int* __restrict__ need)
+{
+    __shared__ double red[kBT];
+    int64_t r0, r1;
+    chunk_rows(n, gridDim.x, blockIdx.x, r0, r1);
+    const int p = threadIdx.x % BP, rl = threadIdx.x / BP, nrl = kBT / BP;
+    const int64_t vs = n * (int64_t)B;
+    const int64_t sq = (int64_t)gridDim.x * B;
+    const bool act = p < B && (!need || need[p]);
+    for (int i0 = 0; i0 <= J; i0 += 4) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        if (act)
+            for (int64_t r = r0 + rl; r < r1; r += nrl) {
+                const double wv = w[r * B + p];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int i = i0 + t;
+                    if (i < J) acc[t] = fma(V[i * vs + r * B + p], wv, acc[t]);
+                    else if (i == J) acc[t] = fma(wv, wv, acc[t]);
+                }
+            }
+        for (int t = 0; t < 4 && i0 + t <= J; ++t)
+            reduce_per_problem(acc[t], red, BP, B, part + (int64_t)blockIdx.x * B, sq, i0 + t);
+    }
+}
+
+// w_p -= sum_i c[i][p] V_i,p ; npart[blk][p] = |w_p|^2
+__global__ void __launch_bounds__(kBT) k_bupdate(const double* __restrict__ V, int64_t n, int B, int BP, int J,
+                                                 const double* __restrict__ c, double* __restrict__ w,
+                                                 double* __restrict__ npart, const int* __restrict__ need)
+{
+    __shared__ double red[kBT];
+    int64_t r0, r1;
+    chunk_rows(n, gridDim.x, blockIdx.x, r0, r1);
+    const int p = threadIdx.x % BP, rl = threadIdx.x / BP, nrl = kBT / BP;
+    const int64_t vs = n * (int64_t)B;
+    double nn = 0.0;
+    if (p < B) {
+        const bool act = !need || need[p];
+        for (int64_t r = r0 + rl; r < r1; r += nrl) {
+            double acc = w[r * B + p];
+            if (act)
+                for (int i = 0; i < J; ++i) acc = fma(-c[i * B + p], V[i * vs + r * B + p], acc);
+            w[r * B + p] = acc;
+            nn = fma(acc, acc, nn);
+        }
+    }
+    reduce_per_problem(nn, red, BP, B, npart + (int64_t)blockIdx.x * B, 0, 0);
+}
+
+// Local step bookkeeping: column j gets alpha at row j and beta_{j-1} at row j-1.
+__global__ void k_blocal(double* __restrict__ cj, const double* __restrict__ alpha, const double* __restrict__ beta_prev,
+                         int j, int B)
+{
+    for (int p = threadIdx.x; p < B; p += blockDim.x) {
+        cj[(size_t)j * B + p] = alpha[p];
+        cj[(size_t)(j - 1) * B + p] = beta_prev[p];
+    }
+}
+
+// cj[i][p] += c[i][p] for i < J where the pass ran for p
+__global__ void k_bacc(double* __restrict__ cj, const double* __restrict__ c, int J, int B,
+                       const int* __restrict__ need)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < J * B; t += gridDim.x * blockDim.x) {
+        const int p = t % B;
+        if (!need || need[p]) cj[t] += c[t];
+    }
+}
+
+// after pass 1: need2[p] = forced or ||w_after||^2 < eta^2 ||w_before||^2 (DGKS)
+__global__ void k_bneed(const double* __restrict__ after, const double* __restrict__ before, int B, int force,
+                        int* __restrict__ need2)
+{
+    for (int p = threadIdx.x; p < B; p += blockDim.x)
+        need2[p] = (force || after[p] < 0.5 * before[p]) ? 1 : 0;
+}
+
+// beta_j = ||w||; breakdown when it vanishes relative to ||H v_j||
+__global__ void k_bfinal(const double* __restrict__ norm2, const double* __restrict__ ref2, double* __restrict__ beta,
+                         int* __restrict__ brk, int B, int j)
+{
+    for (int p = threadIdx.x; p < B; p += blockDim.x) {
+        const double b = sqrt(norm2[p]);
+        const double ref = sqrt(fmax(ref2[p], 0.0));
+        if (!(b > 1e-12 * ref)) {
+            if (brk[p] == 0) brk[p] = j + 1;
+            beta[p] = 1.0;          // keeps the (abandoned) vector finite
+        } else {
+            beta[p] = b;
+        }
+    }
+}
+
+__global__ void k_bscale(double* __restrict__ w, int64_t n, int B, const double* __restrict__ beta)
+{
+    const int64_t total = n * (int64_t)B;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(t % B);
+        w[t] = w[t] / beta[p];
+    }
+}
+
+// out_i,p = sum_j V_j,p Y_p[j][i] for i < k (Y per problem, [p][i][j] = column i)
+__global__ void k_bgemm(const double* __restrict__ V, int64_t n, int B, int m, const double* __restrict__ Y, int k,
+                        double* __restrict__ out)
+{
+    const int64_t vs = n * (int64_t)B;
+    const int64_t total = n * (int64_t)B;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(t % B);
+        const double* Yp = Y + (size_t)p * m * m;
+        for (int i0 = 0; i0 < k; i0 += 8) {
+            double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int j = 0; j < m; ++j) {
+                const double v = V[j * vs + t];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (i0 + q < k) acc[q] = fma(v, Yp[(size_t)(i0 + q) * m + j], acc[q]);
+            }
+            for (int q = 0; q < 8 && i0 + q < k; ++q) out[(i0 + q) * vs + t] = acc[q];
+        }
+    }
+}
+
+__global__ void k_brandom(double* __restrict__ v, int64_t total, uint64_t seed)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(t + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        v[t] = 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+    }
+}
+
+// residual part: sum over rows of (y - lambda x)^2 per problem
+__global__ void __launch_bounds__(kBT) k_bresid(const double* __restrict__ y, const double* __restrict__ x, int64_t n,
+                                                int B, int BP, const double* __restrict__ lam, double* __restrict__ part)
+{
+    __shared__ double red[kBT];
+    int64_t r0, r1;
+    chunk_rows(n, gridDim.x, blockIdx.x, r0, r1);
+    const int p = threadIdx.x % BP, rl = threadIdx.x / BP, nrl = kBT / BP;
+    double s = 0.0;
+    if (p < B)
+        for (int64_t r = r0 + rl; r < r1; r += nrl) {
+            const double d = fma(-lam[p], x[r * B + p], y[r * B + p]);
+            s = fma(d, d, s);
+        }
+    reduce_per_problem(s, red, BP, B, part + (int64_t)blockIdx.x * B, 0, 0);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+
+void batch_create(ed_batch& bt, const ed_basis& basis, int K, int B, const uint16_t* ktab, const double* vtabs,
+                  cudaStream_t st)
+{
+    ED_REQUIRE(B >= 1 && B <= 256, ED_ERR_ARG, "1..256 Hamiltonians per batch");
+    ED_REQUIRE(basis.norb == K, ED_ERR_ARG, "tables and basis have different orbital counts");
+    ED_REQUIRE(basis.dim > 0, ED_ERR_EMPTY, "empty sector");
+    const size_t K3 = (size_t)K * K * K;
+    std::vector<HopTables> hops;
+    hops.reserve(B);
+    for (int b = 0; b < B; ++b) hops.push_back(derive_hop_tables(K, ktab, vtabs + (size_t)b * K3));
+    const int nhop = (int)hops[0].w.size();
+    ED_REQUIRE(nhop <= 0x7FFF, ED_ERR_RANGE, "too many hop types for 15-bit codes");
+    bt.B = B;
+    bt.K = K;
+    bt.N = basis.N;
+    bt.n = (int64_t)basis.dim;
+    bt.nhop = nhop;
+    std::vector<double> wu(nhop, 0.0), wall((size_t)nhop * B), da((size_t)B * K * K), db((size_t)B * K * K);
+    for (int b = 0; b < B; ++b) {
+        for (int h = 0; h < nhop; ++h) {
+            wall[(size_t)h * B + b] = hops[b].w[h];
+            if (hops[b].w[h] != 0.0) wu[h] = 1.0;
+        }
+        std::memcpy(&da[(size_t)b * K * K], hops[b].diag_a.data(), (size_t)K * K * 8);
+        std::memcpy(&db[(size_t)b * K * K], hops[b].diag_b.data(), (size_t)K * K * 8);
+    }
+    DevBuf<double> dwu(nhop), dda(da.size()), ddb(db.size());
+    DevBuf<int> doff(2 * K);
+    bt.w.alloc(wall.size());
+    ED_CUDA(cudaMemcpyAsync(dwu.p, wu.data(), wu.size() * 8, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(doff.p, hops[0].hop_off.data(), 2 * K * 4, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(bt.w.p, wall.data(), wall.size() * 8, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(dda.p, da.data(), da.size() * 8, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(ddb.p, db.data(), db.size() * 8, cudaMemcpyHostToDevice, st));
+    const int64_t n = bt.n;
+    bt.diag.alloc((size_t)n * B);
+    k_bdiag<<<sms_b() * 8, 256, 0, st>>>(basis.words.p, n, dda.p, ddb.p, K, B, bt.diag.p); count_launch();
+    ED_CUDA(cudaGetLastError());
+    // union pattern
+    const size_t tsm = (size_t)nhop * 8 + (size_t)2 * K * 4;
+    DevBuf<int64_t> rowlen(n);
+    bt.rowptr.alloc(n + 1);
+    ED_CUDA(cudaFuncSetAttribute(k_pat_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    k_pat_count<<<sms_b() * 4, 256, tsm, st>>>(basis.words.p, n, dwu.p, nhop, doff.p, K, rowlen.p); count_launch();
+    ED_CUDA(cudaGetLastError());
+    exclusive_scan_i64(rowlen.p, bt.rowptr.p, n, st);
+    ED_CUDA(cudaMemcpyAsync(&bt.nnz, bt.rowptr.p + n, 8, cudaMemcpyDeviceToHost, st));
+    const int64_t maxrow = reduce_max_i64_host(rowlen.p, n, st);
+    ED_CUDA(cudaStreamSynchronize(st));
+    bt.col.alloc((size_t)bt.nnz + kCrsPad);
+    bt.code.alloc((size_t)bt.nnz + kCrsPad);
+    ED_CUDA(cudaMemsetAsync(bt.col.p + bt.nnz, 0, kCrsPad * 4, st));
+    ED_CUDA(cudaMemsetAsync(bt.code.p + bt.nnz, 0, kCrsPad * 2, st));
+    int cap = 32;
+    while (cap < maxrow) cap <<= 1;
+    const size_t tbytes = (tsm + 15) & ~(size_t)15;
+    const size_t per_warp = (size_t)cap * 12 + 4 + 64;
+    const size_t budget = 200 * 1024;
+    ED_REQUIRE(tbytes + per_warp <= budget, ED_ERR_RANGE, "rows too long for the shared-memory sort");
+    int wpc = (int)std::min<size_t>(16, (budget - tbytes) / per_warp);
+    const size_t smem = tbytes + (size_t)wpc * per_warp;
+    ED_CUDA(cudaFuncSetAttribute(k_pat_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DevBuf<int> err(1);
+    ED_CUDA(cudaMemsetAsync(err.p, 0, 4, st));
+    k_pat_fill<<<sms_b(), wpc * 32, smem, st>>>(basis.words.p, n, dwu.p, nhop, doff.p, K, basis.N, bt.rowptr.p,
+                                                basis.hi.p, basis.lo.p, basis.low_bits, cap, bt.col.p, bt.code.p,
+                                                err.p); count_launch();
+    ED_CUDA(cudaGetLastError());
+    int herr = 0;
+    ED_CUDA(cudaMemcpyAsync(&herr, err.p, 4, cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    ED_REQUIRE(herr == 0, ED_ERR_INTERNAL, "batched pattern fill: row count or rank check failed on the device");
+}
+
+namespace {
+
+template <int TB, int U>
+void launch_bspmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
+{
+    const size_t smem = (size_t)bt.nhop * TB * 8;
+    static_assert(U <= kCrsPad, "batch overruns the padding");
+    if (smem > 48 * 1024) ED_CUDA(cudaFuncSetAttribute(k_bspmm<TB, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)(sms_b() * 2), (unsigned)((bt.B + TB - 1) / TB));
+    k_bspmm<TB, U><<<grid, 256, smem, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.nhop, bt.diag.p, X, Y, bt.n,
+                                            bt.B);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+void bspmm_variant(const ed_batch& bt, int tb, int u, const double* X, double* Y, cudaStream_t st)
+{
+    if (tb == 4 && u == 4) launch_bspmm<4, 4>(bt, X, Y, st);
+    else if (tb == 4 && u == 8) launch_bspmm<4, 8>(bt, X, Y, st);
+    else if (tb == 8 && u == 4) launch_bspmm<8, 4>(bt, X, Y, st);
+    else if (tb == 8 && u == 8) launch_bspmm<8, 8>(bt, X, Y, st);
+    else if (tb == 16 && u == 4) launch_bspmm<16, 4>(bt, X, Y, st);
+    else launch_bspmm<16, 8>(bt, X, Y, st);
+}
+
+}  // namespace
+
+void batch_spmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
+{
+    bspmm_variant(bt, bt.tb, bt.unroll, X, Y, st);
+}
+
+// Pick the (Hamiltonians per CTA, loads in flight) pair that runs the block
+// product fastest on this data; shared-memory capacity rules out tiles whose
+// hop tables do not fit.
+void batch_autotune(ed_batch& bt, cudaStream_t st)
+{
+    DevBuf<double> X((size_t)bt.n * bt.B), Y((size_t)bt.n * bt.B);
+    k_brandom<<<sms_b() * 4, 256, 0, st>>>(X.p, bt.n * bt.B, 7); count_launch();
+    cudaEvent_t a, b;
+    ED_CUDA(cudaEventCreate(&a));
+    ED_CUDA(cudaEventCreate(&b));
+    float best = 1e30f;
+    int btb = 8, bu = 8;
+    for (int tb : {4, 8, 16}) {
+        if ((size_t)bt.nhop * tb * 8 > 200 * 1024) continue;
+        if (tb > 4 && bt.B <= 4) continue;
+        for (int u : {4, 8}) {
+            bspmm_variant(bt, tb, u, X.p, Y.p, st);
+            ED_CUDA(cudaEventRecord(a, st));
+            for (int r = 0; r < 3; ++r) bspmm_variant(bt, tb, u, X.p, Y.p, st);
+            ED_CUDA(cudaEventRecord(b, st));
+            ED_CUDA(cudaEventSynchronize(b));
+            float ms = 0.f;
+            ED_CUDA(cudaEventElapsedTime(&ms, a, b));
+            if (ms < best) { best = ms; btb = tb; bu = u; }
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    bt.tb = btb;
+    bt.unroll = bu;
+}
+
+// Lockstep thick-restart Lanczos for the B problems of a batch: the
+// recurrences of lanczos_solve (local three-term step, full Gram-Schmidt pass
+// with a DGKS second pass, forced on the first step of a cycle), every scalar
+// per problem.  All problems restart together; converged ones keep iterating
+// (their pairs stay converged) until every problem has its nev pairs.  A
+// Krylov breakdown, which needs an exactly invariant subspace, is reported
+// as ED_ERR_BREAKDOWN for the batch; such a problem is solved with ed_lanczos.
+void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V0, double* evals, double* evecs,
+                 ed_batch_info* info, cudaStream_t st)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const int64_t n = bt.n;
+    const int B = bt.B;
+    const int nev = p.nev;
+    ED_REQUIRE(nev >= 1 && nev + 2 < n, ED_ERR_ARG, "need 1 <= nev < n - 2");
+    const double tol = p.tol > 0 ? p.tol : 1e-10;
+    const int max_restarts = p.max_restarts > 0 ? p.max_restarts : 2000;
+    int64_t m64 = p.ncv > 0 ? p.ncv : std::min<int64_t>(n - 1, 2 * (int64_t)nev + 21);
+    m64 = std::max<int64_t>(m64, nev + 2);
+    m64 = std::min<int64_t>(m64, std::min<int64_t>(n - 1, 200));
+    const int m = (int)m64;
+    int BP = 1;
+    while (BP < B) BP <<= 1;
+    ED_REQUIRE(BP <= kBT, ED_ERR_ARG, "at most 256 problems per batch");
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 2, n / 256));
+    const int64_t vs = n * (int64_t)B;
+    DevBuf<double> V((size_t)vs * (m + 1)), V2((size_t)vs * (m + 1));
+    DevBuf<double> part((size_t)(m + 2) * nb * B), npart((size_t)nb * B);
+    DevBuf<double> sc((size_t)(m + 2) * B);
+    DevBuf<double> s2((size_t)6 * B);   // [0] alpha [1] |Hv|^2 [2] scratch [3] |w|^2 after a pass
+    DevBuf<int> need2(B), brk(B);
+    DevBuf<double> coef((size_t)m * (m + 1) * B);
+    DevBuf<double> betas((size_t)(m + 1) * B);
+    DevBuf<double> Yd((size_t)B * m * m);
+    ED_CUDA(cudaMemsetAsync(betas.p, 0, betas.bytes(), st));
+    auto grid_for = [&](int64_t work) { return (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 8, (work + 255) / 256)); };
+    if (V0) ED_CUDA(cudaMemcpyAsync(V.p, V0, (size_t)vs * 8, cudaMemcpyDeviceToDevice, st));
+    else { k_brandom<<<grid_for(vs), 256, 0, st>>>(V.p, vs, p.seed); count_launch(); }
+    {   // normalise every start vector, rejecting zero or non-finite ones
+        k_bdot2<<<nb, kBT, 0, st>>>(V.p, V.p, n, B, BP, part.p); count_launch();
+        k_bsum<<<1, 256, 0, st>>>(part.p, nb, B, 1, s2.p); count_launch();
+        std::vector<double> nn(B);
+        ED_CUDA(cudaMemcpyAsync(nn.data(), s2.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        for (int b = 0; b < B; ++b) {
+            ED_REQUIRE(nn[b] > 0 && std::isfinite(nn[b]), ED_ERR_ARG, "a start vector is zero or not finite");
+            nn[b] = std::sqrt(nn[b]);
+        }
+        ED_CUDA(cudaMemcpyAsync(s2.p + 2 * B, nn.data(), (size_t)B * 8, cudaMemcpyHostToDevice, st));
+        k_bscale<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, s2.p + 2 * B); count_launch();
+    }
+    ed_batch_info inf;
+    std::memset(&inf, 0, sizeof(inf));
+    inf.tile_hamiltonians = bt.tb;
+    inf.tile_unroll = bt.unroll;
+    std::vector<std::vector<double>> T(B, std::vector<double>((size_t)m * m, 0.0)), theta(B), Y(B);
+    std::vector<double> coef_h((size_t)m * (m + 1) * B), beta_h((size_t)(m + 1) * B), Yall((size_t)B * m * m);
+    std::vector<int> brk_h(B);
+    std::vector<cudaEvent_t> ev(2 * (size_t)(m + 1), nullptr);
+    for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
+    struct EvG {
+        std::vector<cudaEvent_t>& v;
+        ~EvG() { for (auto e : v) if (e) cudaEventDestroy(e); }
+    } evg{ev};
+    double spmm_ms = 0.0;
+    bool converged = false;
+    int k = 0;
+    for (;;) {
+        ED_CUDA(cudaMemsetAsync(coef.p, 0, coef.bytes(), st));
+        ED_CUDA(cudaMemsetAsync(brk.p, 0, (size_t)B * 4, st));
+        float cycle_ms = 0.f;
+        for (int j = k; j < m; ++j) {
+            double* vj = V.p + (int64_t)j * vs;
+            double* w = V.p + (int64_t)(j + 1) * vs;
+            double* cj = coef.p + (size_t)j * (m + 1) * B;
+            const bool first = (j == k);
+            ED_CUDA(cudaEventRecord(ev[2 * j], st));
+            batch_spmm(bt, vj, w, st);
+            ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
+            ++inf.block_products;
+            if (!first) {
+                k_bdot2<<<nb, kBT, 0, st>>>(vj, w, n, B, BP, part.p); count_launch();
+                k_bsum<<<1, 256, 0, st>>>(part.p, nb, B, 2, s2.p); count_launch();
+                k_blocal<<<1, 256, 0, st>>>(cj, s2.p, betas.p + (size_t)(j - 1) * B, j, B); count_launch();
+                k_baxpy2<<<grid_for(vs), 256, 0, st>>>(w, vj, V.p + (int64_t)(j - 1) * vs, n, B, s2.p,
+                                                       betas.p + (size_t)(j - 1) * B); count_launch();
+            }
+            const int J = j + 1;
+            for (int pass = 0; pass < 2; ++pass) {
+                const int* mask = pass == 0 ? nullptr : need2.p;
+                k_bmdot<<<nb, kBT, 0, st>>>(V.p, n, B, BP, J, w, part.p, mask); count_launch();
+                k_bsum<<<grid_for((int64_t)(J + 1) * B), 256, 0, st>>>(part.p, nb, B, J + 1, sc.p); count_launch();
+                k_bupdate<<<nb, kBT, 0, st>>>(V.p, n, B, BP, J, sc.p, w, npart.p, mask); count_launch();
+                k_bacc<<<grid_for((int64_t)J * B), 256, 0, st>>>(cj, sc.p, J, B, mask); count_launch();
+                k_bsum<<<1, 256, 0, st>>>(npart.p, nb, B, 1, s2.p + 3 * B); count_launch();
+                if (pass == 0) {
+                    k_bneed<<<1, 256, 0, st>>>(s2.p + 3 * B, sc.p + (size_t)J * B, B, first ? 1 : 0, need2.p);
+                    count_launch();
+                    if (first)   // ||H v_j||^2 is the norm before the first pass
+                        ED_CUDA(cudaMemcpyAsync(s2.p + B, sc.p + (size_t)J * B, (size_t)B * 8, cudaMemcpyDeviceToDevice,
+                                                st));
+                }
+            }
+            k_bfinal<<<1, 256, 0, st>>>(s2.p + 3 * B, s2.p + B, betas.p + (size_t)j * B, brk.p, B, j); count_launch();
+            k_bscale<<<grid_for(vs), 256, 0, st>>>(w, n, B, betas.p + (size_t)j * B); count_launch();
+            ED_CUDA(cudaGetLastError());
+        }
+        ED_CUDA(cudaMemcpyAsync(coef_h.data(), coef.p, coef.bytes(), cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaMemcpyAsync(beta_h.data(), betas.p, beta_h.size() * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaMemcpyAsync(brk_h.data(), brk.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        for (int j = k; j < m; ++j) {
+            float ms = 0.f;
+            ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * j], ev[2 * j + 1]));
+            cycle_ms += ms;
+        }
+        spmm_ms += cycle_ms;
+        int nconv = 0;
+        double maxres = 0.0;
+        for (int b = 0; b < B; ++b) {
+            if (brk_h[b]) {
+                inf.breakdowns++;
+                continue;
+            }
+            std::vector<double>& Tb = T[b];
+            for (int j = k; j < m; ++j)
+                for (int i = 0; i <= j; ++i) {
+                    const double v = coef_h[((size_t)j * (m + 1) + i) * B + b];
+                    Tb[(size_t)i * m + j] = v;
+                    Tb[(size_t)j * m + i] = v;
+                }
+            sym_eigen(m, Tb, theta[b], Y[b]);
+            const double bl = beta_h[(size_t)(m - 1) * B + b];
+            bool ok = true;
+            for (int i = 0; i < nev; ++i) {
+                const double r = std::fabs(bl * Y[b][(size_t)(m - 1) + (size_t)m * i]);
+                maxres = std::max(maxres, r);
+                if (!(r <= tol)) ok = false;
+            }
+            nconv += ok ? 1 : 0;
+        }
+        ED_REQUIRE(inf.breakdowns == 0, ED_ERR_BREAKDOWN,
+                   "Krylov breakdown in a batched problem: solve it with ed_lanczos");
+        inf.converged = nconv;
+        inf.max_residual = maxres;
+        if (nconv == B) {
+            converged = true;
+            break;
+        }
+        if (inf.restarts >= max_restarts) break;
+        ++inf.restarts;
+        int kk = std::min(m - 2, nev + std::max(1, (m - nev) / 2));
+        kk = std::max(kk, std::min(nev, m - 1));
+        for (int b = 0; b < B; ++b) std::memcpy(&Yall[(size_t)b * m * m], Y[b].data(), (size_t)m * m * 8);
+        ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), Yall.size() * 8, cudaMemcpyHostToDevice, st));
+        k_bgemm<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, m, Yd.p, kk, V2.p); count_launch();
+        ED_CUDA(cudaMemcpyAsync(V2.p + (int64_t)kk * vs, V.p + (int64_t)m * vs, (size_t)vs * 8, cudaMemcpyDeviceToDevice,
+                                st));
+        std::swap(V, V2);
+        for (int b = 0; b < B; ++b) {
+            std::vector<double>& Tb = T[b];
+            std::fill(Tb.begin(), Tb.end(), 0.0);
+            const double bl = beta_h[(size_t)(m - 1) * B + b];
+            for (int i = 0; i < kk; ++i) {
+                Tb[(size_t)i * m + i] = theta[b][i];
+                const double s = bl * Y[b][(size_t)(m - 1) + (size_t)m * i];
+                Tb[(size_t)i * m + kk] = s;
+                Tb[(size_t)kk * m + i] = s;
+            }
+        }
+        k = kk;
+        ED_CUDA(cudaStreamSynchronize(st));
+    }
+    for (int b = 0; b < B; ++b)
+        for (int i = 0; i < nev; ++i) evals[(size_t)b * nev + i] = theta[b][i];
+    DevBuf<double> xtmp, ytmp;
+    double* X = evecs;
+    if (!X && p.verify) {
+        xtmp.alloc((size_t)vs * nev);
+        X = xtmp.p;
+    }
+    if (X) {
+        for (int b = 0; b < B; ++b) std::memcpy(&Yall[(size_t)b * m * m], Y[b].data(), (size_t)m * m * 8);
+        ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), Yall.size() * 8, cudaMemcpyHostToDevice, st));
+        k_bgemm<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, m, Yd.p, nev, X); count_launch();
+    }
+    if (p.verify && X) {
+        ytmp.alloc((size_t)vs);
+        std::vector<double> lam(B), res(B);
+        DevBuf<double> dl(B);
+        double worst = 0.0;
+        int ok_all = 0;
+        std::vector<char> okb(B, 1);
+        for (int i = 0; i < nev; ++i) {
+            for (int b = 0; b < B; ++b) lam[b] = evals[(size_t)b * nev + i];
+            ED_CUDA(cudaMemcpyAsync(dl.p, lam.data(), (size_t)B * 8, cudaMemcpyHostToDevice, st));
+            batch_spmm(bt, X + (int64_t)i * vs, ytmp.p, st);
+            ++inf.block_products;
+            k_bresid<<<nb, kBT, 0, st>>>(ytmp.p, X + (int64_t)i * vs, n, B, BP, dl.p, part.p); count_launch();
+            k_bsum<<<1, 256, 0, st>>>(part.p, nb, B, 1, s2.p); count_launch();
+            ED_CUDA(cudaMemcpyAsync(res.data(), s2.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+            ED_CUDA(cudaStreamSynchronize(st));
+            for (int b = 0; b < B; ++b) {
+                const double r = std::sqrt(res[b]);
+                worst = std::max(worst, r);
+                if (!(r <= tol)) okb[b] = 0;
+            }
+        }
+        for (int b = 0; b < B; ++b) ok_all += okb[b];
+        inf.max_residual = worst;
+        inf.converged = ok_all;
+    }
+    ED_CUDA(cudaStreamSynchronize(st));
+    inf.spmm_seconds = spmm_ms * 1e-3;
+    inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (info) *info = inf;
+    ED_REQUIRE(converged, ED_ERR_NOCONV, "batched Lanczos did not converge within the restart cap");
+}
+
+}  // namespace edgb
+
+using namespace edgb;
+
+extern "C" {
+
+ed_status ed_batch_create(const ed_basis* b, int nham, const uint16_t* ktable, const double* vtables, int autotune,
+                          ed_batch** out)
+{
+    return guard([&] {
+        ED_REQUIRE(b && ktable && vtables && out, ED_ERR_ARG, "NULL argument");
+        *out = nullptr;
+        ed_batch* bt = new ed_batch();
+        try {
+            batch_create(*bt, *b, b->norb, nham, ktable, vtables, nullptr);
+            if (autotune) batch_autotune(*bt, nullptr);
+        } catch (...) {
+            delete bt;
+            throw;
+        }
+        *out = bt;
+    });
+}
+
+ed_status ed_batch_free(ed_batch* bt)
+{
+    return guard([&] { delete bt; });
+}
+
+ed_status ed_batch_dims(const ed_batch* bt, int64_t* n, int64_t* nnz, int* nham)
+{
+    return guard([&] {
+        ED_REQUIRE(bt, ED_ERR_ARG, "NULL batch");
+        if (n) *n = bt->n;
+        if (nnz) *nnz = bt->nnz;
+        if (nham) *nham = bt->B;
+    });
+}
+
+ed_status ed_batch_spmm(const ed_batch* bt, const double* X, double* Y, ed_stream stream)
+{
+    return guard([&] {
+        ED_REQUIRE(bt && X && Y, ED_ERR_ARG, "NULL argument");
+        ED_REQUIRE(X != Y, ED_ERR_ARG, "X and Y must be distinct");
+        batch_spmm(*bt, X, Y, (cudaStream_t)stream);
+    });
+}
+
+ed_status ed_batch_solve(const ed_batch* bt, const ed_lanczos_params* p, const double* V0, double* evals,
+                         double* evecs, ed_batch_info* info)
+{
+    return guard([&] {
+        ED_REQUIRE(bt && p && evals, ED_ERR_ARG, "NULL argument");
+        if (info) std::memset(info, 0, sizeof(*info));
+        batch_solve(*bt, *p, V0, evals, evecs, info, nullptr);
+    });
+}
+
+}  // extern "C"
+
+namespace edgb {
+}  // namespace edgb
+

@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <cstddef>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -45,6 +46,29 @@ uint64_t launch_count();
     do {                                                                                      \
         if (!(cond)) throw ::edgb::Error((code), (msg));                                      \
     } while (0)
+
+// Run f, turning any exception into a status code and a last-error message
+// (no exception crosses the C ABI).
+template <class F>
+ed_status guard(F&& f)
+{
+    try {
+        f();
+        return ED_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return ED_ERR_OOM;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return ED_ERR_INTERNAL;
+    } catch (...) {
+        set_last_error("unknown error");
+        return ED_ERR_INTERNAL;
+    }
+}
 
 // Owning device buffer.
 template <class T>

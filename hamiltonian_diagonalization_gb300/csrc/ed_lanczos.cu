@@ -123,47 +123,44 @@ __global__ void __launch_bounds__(kThreads) k_axpy2(double* __restrict__ w, cons
         w[r] = fma(-b, vjm1[r], fma(-a, vj[r], w[r]));
 }
 
-// Multi-dot: part[i*nb + b] = V[:,i].w over block b's rows for i < J, and
-// part[J*nb + b] = w.w.  run == nullptr or *run != 0 to execute.
+// Multi-dot: part[i*nb + b] = V[:,i].w over rows [b*kMdotRows, ...) for
+// i < J, and part[J*nb + b] = w.w; nb = ceil(n / kMdotRows) blocks.  The
+// block's slice of w is staged in shared memory once; warps then take the
+// columns in turn, each streaming its column slice coalesced with four
+// independent FMA chains (one FP64 FMA per element plus a 5-step shuffle per
+// column and block).  run == nullptr or *run != 0 to execute.
+constexpr int kMdotRows = 4096;
 __global__ void __launch_bounds__(kThreads) k_mdot(const double* __restrict__ V, int64_t n, int J,
                                                    const double* __restrict__ w, double* __restrict__ part,
                                                    const int* __restrict__ run, const int* __restrict__ stop)
 {
     if ((run && !*run) || (stop && *stop)) return;
-    __shared__ double red[kJT][kThreads + 1];
-    int64_t r0, r1;
-    chunk(n, gridDim.x, blockIdx.x, r0, r1);
+    __shared__ double sw[kMdotRows];
+    const int64_t r0 = (int64_t)blockIdx.x * kMdotRows;
+    const int len = (int)min((int64_t)kMdotRows, n - r0);
+    for (int i = threadIdx.x; i < len; i += kThreads) sw[i] = w[r0 + i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nb = gridDim.x;
-    for (int j0 = 0; j0 <= J; j0 += kJT) {
-        double acc[kJT];
-#pragma unroll
-        for (int t = 0; t < kJT; ++t) acc[t] = 0.0;
-        const int jn = min(kJT, J + 1 - j0);
-        for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
-            const double wr = w[r];
-#pragma unroll
-            for (int t = 0; t < kJT; ++t) {
-                const int i = j0 + t;
-                if (t < jn) {
-                    const double vv = (i < J) ? V[(int64_t)i * n + r] : wr;
-                    acc[t] = fma(vv, wr, acc[t]);
-                }
+    for (int i = warp; i <= J; i += kThreads / 32) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        int r = lane;
+        if (i < J) {
+            const double* col = V + (int64_t)i * n + r0;
+            for (; r + 96 < len; r += 128) {
+                a0 = fma(col[r], sw[r], a0);
+                a1 = fma(col[r + 32], sw[r + 32], a1);
+                a2 = fma(col[r + 64], sw[r + 64], a2);
+                a3 = fma(col[r + 96], sw[r + 96], a3);
             }
+            for (; r < len; r += 32) a0 = fma(col[r], sw[r], a0);
+        } else {
+            for (; r < len; r += 32) a0 = fma(sw[r], sw[r], a0);
         }
+        double s = (a0 + a1) + (a2 + a3);
 #pragma unroll
-        for (int t = 0; t < kJT; ++t) red[t][threadIdx.x] = acc[t];
-        __syncthreads();
-        // warp t sums column t: 8 values per lane, then 5 shuffles
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        if (warp < jn) {
-            double s = 0.0;
-#pragma unroll
-            for (int q = 0; q < kThreads / 32; ++q) s += red[warp][q * 32 + lane];
-#pragma unroll
-            for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) part[(int64_t)(j0 + warp) * nb + blockIdx.x] = s;
-        }
-        __syncthreads();
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) part[(int64_t)i * nb + blockIdx.x] = s;
     }
 }
 
@@ -350,6 +347,7 @@ struct Work {
     int64_t n = 0;
     int m = 0;
     int nb = 0;                      // blocks of the row-chunked reductions
+    int nbm = 0;                     // blocks of the multi-dot (kMdotRows rows each)
     DevBuf<double> V, V2;            // n x (m+1), column-major
     DevBuf<double> part;             // (m+2) * nb
     DevBuf<double> npart;            // nb
@@ -380,8 +378,8 @@ double orthonormalise_column(Work& w, double* Vbase, int col, cudaStream_t st)
     double* x = Vbase + (int64_t)col * w.n;
     if (col > 0) {
         for (int pass = 0; pass < 2; ++pass) {
-            k_mdot<<<w.nb, kThreads, 0, st>>>(Vbase, w.n, col, x, w.part.p, nullptr, nullptr); ::edgb::count_launch();
-            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nb, col, w.c.p, w.junk.p, w.scal.p + 3, nullptr, nullptr); ::edgb::count_launch();
+            k_mdot<<<w.nbm, kThreads, 0, st>>>(Vbase, w.n, col, x, w.part.p, nullptr, nullptr); ::edgb::count_launch();
+            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nbm, col, w.c.p, w.junk.p, w.scal.p + 3, nullptr, nullptr); ::edgb::count_launch();
             k_update<<<w.nb, kThreads, (size_t)col * 8, st>>>(Vbase, w.n, col, w.c.p, x, w.npart.p, nullptr, nullptr); ::edgb::count_launch();
             ED_CUDA(cudaGetLastError());
         }
@@ -502,7 +500,8 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     w.nb = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
     w.V.alloc((size_t)n * (m + 1));
     w.V2.alloc((size_t)n * (m + 1));
-    w.part.alloc((size_t)(m + 2) * w.nb);
+    w.nbm = (int)((n + kMdotRows - 1) / kMdotRows);
+    w.part.alloc((size_t)(m + 2) * std::max(w.nb, w.nbm));
     w.npart.alloc(w.nb);
     w.coef.alloc((size_t)(m + 1) * (m + 1));
     w.beta.alloc(m + 2);
@@ -556,13 +555,13 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
                                                    w.beta.p + (j - 1), stop); ::edgb::count_launch();
             }
             const int J = j + 1;
-            k_mdot<<<w.nb, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, nullptr, stop); ::edgb::count_launch();
-            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nb, J, w.c.p, coefcol, w.scal.p, nullptr, stop); ::edgb::count_launch();
+            k_mdot<<<w.nbm, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, nullptr, stop); ::edgb::count_launch();
+            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nbm, J, w.c.p, coefcol, w.scal.p, nullptr, stop); ::edgb::count_launch();
             k_update<<<w.nb, kThreads, (size_t)J * 8, st>>>(w.V.p, n, J, w.c.p, wv, w.npart.p, nullptr, stop); ::edgb::count_launch();
             k_norm_finalize<<<1, kThreads, 0, st>>>(w.npart.p, w.nb, w.scal.p, w.beta.p + j, need2, first ? 1 : 0,
                                                     nullptr, stop); ::edgb::count_launch();
-            k_mdot<<<w.nb, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, need2, stop); ::edgb::count_launch();
-            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nb, J, w.c.p, coefcol, w.scal.p + 2, need2, stop); ::edgb::count_launch();
+            k_mdot<<<w.nbm, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, need2, stop); ::edgb::count_launch();
+            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nbm, J, w.c.p, coefcol, w.scal.p + 2, need2, stop); ::edgb::count_launch();
             k_update<<<w.nb, kThreads, (size_t)J * 8, st>>>(w.V.p, n, J, w.c.p, wv, w.npart.p, need2, stop); ::edgb::count_launch();
             k_norm_finalize<<<1, kThreads, 0, st>>>(w.npart.p, w.nb, w.scal.p + 2, w.beta.p + j, nullptr, 0, need2,
                                                     stop); ::edgb::count_launch();

@@ -421,3 +421,52 @@ def solve_sector(N: int, norb: int, twoLz: int, pseudopotentials, nev: int, tol:
     if vec is not None:
         out["eigenvectors"] = vec.reshape(nev, -1)
     return out
+
+
+class HamiltonianBatch:
+    """Many Hamiltonians of one sector differing only in their pseudopotential
+    lists, sharing one device pattern (ed_batch_create).  No reference
+    counterpart: the reference solves one Hamiltonian per run."""
+
+    def __init__(self, basis: FermionFockBasis, pseudopotential_lists, autotune: bool = True):
+        lists = [np.ascontiguousarray(v, dtype=np.float64) for v in pseudopotential_lists]
+        self.nham = len(lists)
+        K = basis.nbrOrbitals
+        self.K = K
+        tabs = [QuarticTermTables(K, v) for v in lists]
+        kt = tabs[0].m_kTable
+        vts = np.ascontiguousarray(np.concatenate([t.m_vTable for t in tabs]))
+        self.basis = basis
+        h = ctypes.c_void_p()
+        check(lib().ed_batch_create(basis.handle(), self.nham, kt.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)),
+                                    _f64p(vts), int(autotune), ctypes.byref(h)))
+        self._h = h
+        n, nnz, nh = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        check(lib().ed_batch_dims(h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(nh)))
+        self.n, self.nnz = int(n.value), int(nnz.value)
+
+    def spmm(self, X, Y, stream=None):
+        """Y[:, b] = H_b X[:, b] on device [n][nham] arrays (torch CUDA tensors)."""
+        check(lib().ed_batch_spmm(self._h, _dptr(X), _dptr(Y), stream))
+
+    def solve(self, nev: int, tol: float = 1e-10, V0=None, seed: int = 0, ncv: int = 0, want_vectors: bool = False,
+              verify: bool = True, max_restarts: int = 0):
+        """Lowest nev eigenpairs of every Hamiltonian.  V0: device [n][nham]
+        start vectors (torch tensor) or None.  Returns (evals [nham, nev],
+        evecs device tensor [nev, n, nham] or None, info dict)."""
+        p = C.LanczosParams(nev=nev, ncv=ncv, max_restarts=max_restarts, tol=tol, seed=seed,
+                            want_vectors=int(want_vectors), verify=int(verify))
+        info = C.BatchInfo()
+        ev = np.empty(self.nham * nev)
+        vec = None
+        if want_vectors:
+            import torch
+            vec = torch.empty((nev, self.n, self.nham), dtype=torch.float64, device="cuda")
+        check(lib().ed_batch_solve(self._h, ctypes.byref(p), None if V0 is None else _dptr(V0), _f64p(ev),
+                                   None if vec is None else _dptr(vec), ctypes.byref(info)))
+        return ev.reshape(self.nham, nev), vec, info.as_dict()
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and C._LIB is not None:
+            C._LIB.ed_batch_free(self._h)
+            self._h = None

@@ -214,6 +214,44 @@ ed_status ed_dense_sym_eigen(int m, const double* a, double* evals, double* evec
 ed_status ed_residuals(const ed_op* op, const double* x_dev, const double* lambda_host, int k,
                        double* res_host);
 
+/* ------------------------------------------------------ batched sweep K6 */
+
+/* Many Hamiltonians of one sector that differ only in their pseudopotentials
+ * (e.g. a V1 sweep), solved together.  No reference counterpart: the
+ * reference solves one Hamiltonian per run (pseudopotential_model.cpp:264).
+ * Vectors of a batch are [row][problem] arrays: element (r, b) at r*nham + b. */
+typedef struct ed_batch ed_batch;
+
+typedef struct {
+    int converged;            /* problems whose nev pairs all converged             */
+    int restarts;
+    int64_t block_products;   /* each applies every Hamiltonian of the batch once   */
+    double max_residual;
+    double seconds;
+    double spmm_seconds;      /* device time inside the block products               */
+    int breakdowns;
+    int tile_hamiltonians;    /* autotuned Hamiltonians per CTA of the block product */
+    int tile_unroll;          /* autotuned loads in flight per lane                  */
+} ed_batch_info;
+
+/* Shared pattern (int32 column + uint16 hop code per element) built once on
+ * the device, per-Hamiltonian hop tables and diagonals.  vtables holds nham
+ * V tables of K^3 entries each (ed_quartic_tables), all with the one
+ * momentum-conserving ktable.  autotune != 0 times the block-product
+ * variants on this data and keeps the fastest. */
+ed_status ed_batch_create(const ed_basis* b, int nham, const uint16_t* ktable, const double* vtables, int autotune,
+                          ed_batch** out);
+ed_status ed_batch_free(ed_batch* bt);
+ed_status ed_batch_dims(const ed_batch* bt, int64_t* n, int64_t* nnz_offdiag, int* nham);
+/* Y[:, b] = H_b X[:, b] for every Hamiltonian b (device [n][nham] arrays). */
+ed_status ed_batch_spmm(const ed_batch* bt, const double* X_dev, double* Y_dev, ed_stream stream);
+/* Lowest p->nev eigenpairs of every Hamiltonian, all in lockstep (the
+ * thick-restart Lanczos of ed_lanczos, batched).  V0_dev: [n][nham] start
+ * vectors or NULL (seeded random); evals_host: nham*nev values, ascending per
+ * Hamiltonian; evecs_dev (may be NULL): nev consecutive [n][nham] arrays. */
+ed_status ed_batch_solve(const ed_batch* bt, const ed_lanczos_params* p, const double* V0_dev, double* evals_host,
+                         double* evecs_dev, ed_batch_info* info);
+
 /* ------------------------------------------------------- one-call driver */
 
 /* Whole sector solve from host inputs: basis -> tables -> CRS (or matrix-free

@@ -1,0 +1,85 @@
+"""Batched sweep (K6): the shared-pattern block product and the lockstep
+Lanczos against the single-Hamiltonian path on the same inputs."""
+import numpy as np
+import pytest
+
+import hamiltonian_diagonalization_gb300 as ed
+
+pytestmark = pytest.mark.gpu
+
+
+def sweep_lists(norb, v1s):
+    base = ed.odd_coulomb_list(norb)
+    out = []
+    for v1 in v1s:
+        v = base.copy()
+        v[1] = v1
+        out.append(v)
+    return out
+
+
+def single_product(torch, N, norb, tlz, pp, x):
+    H = ed.SpinlessFermionHamiltonian()
+    H.Initialize(N, norb, twoLz=tlz)
+    H.Add_CdCdCC_Terms(ed.QuarticTermTables(norb, pp))
+    xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    yd = torch.empty_like(xd)
+    ed.MatrixVectorFunction(H).Simple(xd, yd)
+    torch.cuda.synchronize()
+    return yd.cpu().numpy()
+
+
+@pytest.mark.parametrize("case", [(6, 16, 4), (8, 22, 0)])
+def test_block_product_matches_single_products(cuda, case):
+    torch = cuda
+    N, norb, tlz = case
+    lists = sweep_lists(norb, [0.5, 1.1, 2.0, 3.0, 0.8])
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(N, norb, tlz)
+    batch = ed.HamiltonianBatch(b, lists)
+    n, B = batch.n, batch.nham
+    X = np.random.default_rng(2).uniform(-1, 1, (n, B))
+    Xd = torch.from_numpy(X).cuda()
+    Yd = torch.empty_like(Xd)
+    batch.spmm(Xd, Yd)
+    torch.cuda.synchronize()
+    Y = Yd.cpu().numpy()
+    for j, pp in enumerate(lists):
+        y = single_product(torch, N, norb, tlz, pp, X[:, j])
+        assert np.max(np.abs(Y[:, j] - y)) <= 1e-13 * np.max(np.abs(y)), j
+
+
+def test_batched_solve_matches_single_solves(cuda):
+    torch = cuda
+    N, norb, tlz, nev = 8, 22, 0, 4
+    v1s = [0.6, 1.4, 2.2, 2.9]
+    lists = sweep_lists(norb, v1s)
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(N, norb, tlz)
+    batch = ed.HamiltonianBatch(b, lists)
+    ev, vec, info = batch.solve(nev, tol=1e-10, seed=5, want_vectors=True)
+    assert info["converged"] == len(v1s), info
+    assert info["max_residual"] <= 1e-10
+    assert info["tile_hamiltonians"] in (4, 8, 16)
+    for j, pp in enumerate(lists):
+        out = ed.solve_sector(N, norb, tlz, pp, nev, tol=1e-10, seed=11)
+        assert np.max(np.abs(ev[j] - out["eigenvalues"]) / np.abs(out["eigenvalues"])) <= 1e-10, j
+    # eigenvectors: unit norm, orthogonal within each Hamiltonian
+    V = vec.cpu().numpy()          # [nev, n, nham]
+    for j in range(len(v1s)):
+        G = V[:, :, j] @ V[:, :, j].T
+        assert np.max(np.abs(G - np.eye(nev))) < 1e-9
+
+
+def test_batched_solve_from_given_starts(cuda):
+    torch = cuda
+    N, norb, tlz = 6, 16, 0
+    lists = sweep_lists(norb, [1.0, 2.0])
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(N, norb, tlz)
+    batch = ed.HamiltonianBatch(b, lists, autotune=False)
+    V0 = torch.from_numpy(np.random.default_rng(0).uniform(-1, 1, (batch.n, 2))).cuda()
+    ev, _, info = batch.solve(2, tol=1e-10, V0=V0)
+    assert info["converged"] == 2
+    with pytest.raises(ed.EDError):
+        batch.solve(2, V0=torch.zeros((batch.n, 2), dtype=torch.float64, device="cuda"))
