@@ -94,6 +94,7 @@ _SIGS = {
     "ed_lanczos": (c_int, [c_void_p, P(LanczosParams), P(c_double), P(c_double), P(c_double), P(SolveInfo)]),
     "ed_lanczos_device": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(SolveInfo)]),
     "ed_residuals": (c_int, [c_void_p, c_void_p, P(c_double), c_int, P(c_double)]),
+    "ed_residuals_noalloc": (c_int, [c_void_p, c_void_p, P(c_double), c_int, P(c_double)]),
     "ed_kernel_launches": (c_u64, []),
     "ed_dense_sym_eigen": (c_int, [c_int, P(c_double), P(c_double), P(c_double)]),
     "ed_solve_sector": (c_int, [c_int, c_int, c_int, P(c_double), c_int, c_int, P(LanczosParams), P(c_double),

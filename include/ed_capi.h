@@ -214,6 +214,21 @@ ed_status ed_dense_sym_eigen(int m, const double* a, double* evals, double* evec
 ed_status ed_residuals(const ed_op* op, const double* x_dev, const double* lambda_host, int k,
                        double* res_host);
 
+/* Allocation-free form of ed_residuals, for callers that cannot let the
+ * library call cudaMalloc (programs that give all device memory to their own
+ * pool allocator, and loops where cudaMalloc/cudaFree would synchronise the
+ * device).  Same inputs and outputs; no reference counterpart (the reference
+ * computes no residuals on a device).  The product is fused into the residual
+ * and the only scratch is one file-scope device array of 513 KiB per device,
+ * held until the process exits.  Limits: 1..64 vectors per call; a stored CRS
+ * with both triangles only (ED_ERR_ARG otherwise).  All calls on a device
+ * share that array, so calls that overlap on the GPU race: serialise them.
+ * The first call on a device looks up the array's address with that device
+ * current; make it before any stream capture.  Runs on the legacy default
+ * stream and returns when res_host is filled. */
+ed_status ed_residuals_noalloc(const ed_op* op, const double* x_dev, const double* lambda_host, int k,
+                               double* res_host);
+
 /* ------------------------------------------------------ batched sweep K6 */
 
 /* Many Hamiltonians of one sector that differ only in their pseudopotentials
