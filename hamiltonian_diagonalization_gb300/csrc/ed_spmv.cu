@@ -20,19 +20,15 @@ namespace {
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
 
-// G lanes per row; each lane takes every G-th element of its row in batches
-// of B: the B column loads, then the B gathers of x, then the B value loads
-// are all issued before the first FMA, so a warp keeps 3*B independent
-// memory requests in flight (the gathers hit L2, ~0.5 us away).  The loads
-// are unconditional: past a row's end they read the next row or the zeroed
-// padding after the last row (kCrsPad >= B*G), and only the FMAs are
-// predicated.  Four accumulation chains.
-template <int G, int B>
+// G lanes per row, each lane taking every G-th element in two independent
+// chains.  Measured on GB300 (N=11, 2S=30): G=8 keeps the FP64 pipe ~74%
+// busy at 1.14 ms per product; deeper unguarded batches (G=4, 8 loads in
+// flight) stalled on the dependent gathers and ran slower (1.31 ms).
+template <int G>
 __global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                    const double* __restrict__ val, const double* __restrict__ x,
                                                    double* __restrict__ y, int64_t n)
 {
-    static_assert(B * G <= kCrsPad, "batch overruns the CRS padding");
     constexpr int RPW = 32 / G;   // rows per warp per step
     const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -41,21 +37,16 @@ __global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ r
         const int64_t r = rb + grp;
         const bool valid = r < n;
         const int64_t s = valid ? rowptr[r] : 0, e = valid ? rowptr[r + 1] : 0;
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int64_t k = s + sub; k < e; k += (int64_t)B * G) {
-            int c[B];
-            double v[B], xv[B];
-#pragma unroll
-            for (int i = 0; i < B; ++i) c[i] = ld_stream(col + k + i * G);
-#pragma unroll
-            for (int i = 0; i < B; ++i) xv[i] = __ldg(x + c[i]);
-#pragma unroll
-            for (int i = 0; i < B; ++i) v[i] = ld_stream(val + k + i * G);
-#pragma unroll
-            for (int i = 0; i < B; ++i)
-                if (k + i * G < e) acc[i & 3] = fma(v[i], xv[i], acc[i & 3]);
+        double acc0 = 0.0, acc1 = 0.0;
+        int64_t k = s + sub;
+        for (; k + G < e; k += 2 * G) {
+            const int c0 = ld_stream(col + k), c1 = ld_stream(col + k + G);
+            const double v0 = ld_stream(val + k), v1 = ld_stream(val + k + G);
+            acc0 = fma(v0, __ldg(x + c0), acc0);
+            acc1 = fma(v1, __ldg(x + c1), acc1);
         }
-        double a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+        if (k < e) acc0 = fma(ld_stream(val + k), __ldg(x + ld_stream(col + k)), acc0);
+        double a = acc0 + acc1;
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
         if (valid && sub == 0) y[r] = a;
@@ -148,9 +139,9 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
     const int threads = 256;
     const int grid = sms() * 8;
     if (!a.upper) {
-        if (avg >= 48) k_spmv_full<4, 8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
-        else if (avg >= 12) k_spmv_full<2, 8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
-        else k_spmv_full<1, 8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        if (avg >= 96) k_spmv_full<8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        else if (avg >= 24) k_spmv_full<4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        else k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else {
         ED_CUDA(cudaMemsetAsync(y, 0, (size_t)a.n * sizeof(double), st));
         if (avg >= 48) k_spmv_upper<8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
