@@ -306,7 +306,7 @@ def load_peaks():
 
 
 def load_traffic():
-    p = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    p = os.path.join(ROOT, "profiles", "spmv_traffic.txt")
     if os.path.exists(p):
         try:
             return json.load(open(p))
