@@ -13,6 +13,7 @@ from .host import (  # noqa: F401
     QuarticTermTables,
     SpherePseudopotentialModel,
     SpinlessFermionHamiltonian,
+    WarmStartMLP,
     clebsch_gordan,
     coulomb_pseudopotentials,
     dense_sym_eigen,

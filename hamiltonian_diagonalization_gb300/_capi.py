@@ -104,6 +104,17 @@ _SIGS = {
     "ed_batch_dims": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
     "ed_batch_spmm": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "ed_batch_solve": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(BatchInfo)]),
+    "ed_mlp_create": (c_int, [c_int, c_int, c_u64, P(c_void_p)]),
+    "ed_mlp_free": (c_int, [c_void_p]),
+    "ed_mlp_num_params": (c_int, [c_void_p, P(c_i64)]),
+    "ed_mlp_get_params": (c_int, [c_void_p, P(ctypes.c_float), c_i64]),
+    "ed_mlp_set_params": (c_int, [c_void_p, P(ctypes.c_float), c_i64]),
+    "ed_mlp_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "ed_mlp_gradients": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_i64, P(ctypes.c_float), P(c_double)]),
+    "ed_mlp_train_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_i64, ctypes.c_float, P(c_double)]),
+    "ed_mlp_fit": (c_int, [c_void_p, c_void_p, P(c_double), c_int, c_void_p, c_int, c_int, ctypes.c_float, c_u64,
+                           P(c_double)]),
+    "ed_warm_start": (c_int, [c_void_p, c_void_p, P(c_double), c_int, c_void_p]),
 }
 
 _LIB = None

@@ -272,6 +272,50 @@ __global__ void __launch_bounds__(256) k_bspmm(const int64_t* __restrict__ rowpt
     }
 }
 
+// Warp per row, lanes = 32 consecutive Hamiltonians: the row's column and
+// code are loaded once (broadcast), the hop values W[h][b0..b0+31] and the
+// gathered X[c][b0..b0+31] are each one contiguous 256-byte read, and every
+// lane does one FMA per element with no reduction.  The [nhop][B] hop table
+// is read through L1 instead of being staged in shared memory, so all 32
+// Hamiltonians fit whatever the table size.
+template <int U>
+__global__ void __launch_bounds__(256) k_bspmm_warp(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                    const uint16_t* __restrict__ code, const double* __restrict__ w,
+                                                    const double* __restrict__ diag, const double* __restrict__ X,
+                                                    double* __restrict__ Y, int64_t n, int B)
+{
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.y * 32 + lane;
+    const bool bv = b < B;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < n; r += nwarps) {
+        const int64_t s = rowptr[r], e = rowptr[r + 1];
+        double acc0 = bv ? diag[r * B + b] * X[r * B + b] : 0.0, acc1 = 0.0;
+        for (int64_t k = s; k < e; k += U) {
+            int c[U];
+            uint16_t cd[U];
+            double xv[U], wv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) { c[u] = __ldg(col + k + u); cd[u] = __ldg(code + k + u); }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                xv[u] = bv ? __ldg(X + (int64_t)c[u] * B + b) : 0.0;
+                wv[u] = bv ? __ldg(w + (int64_t)(cd[u] & 0x7FFF) * B + b) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < e) {
+                    const double wu = (cd[u] & kCodeSign) ? -wv[u] : wv[u];
+                    if (u & 1) acc1 = fma(wu, xv[u], acc1);
+                    else acc0 = fma(wu, xv[u], acc0);
+                }
+            }
+        }
+        if (bv) Y[r * B + b] = acc0 + acc1;
+    }
+}
+
 // ------------------------------------------------------ batched Lanczos kernels
 // Vectors [n][B]; a block owns a row chunk, thread t handles problem t % BP
 // (BP = B rounded up to a power of two) on rows t / BP, t / BP + 256/BP, ...
@@ -590,9 +634,21 @@ void launch_bspmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t s
     ED_CUDA(cudaGetLastError());
 }
 
+template <int U>
+void launch_bspmm_warp(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
+{
+    static_assert(U <= kCrsPad, "batch overruns the padding");
+    dim3 grid((unsigned)(sms_b() * 8), (unsigned)((bt.B + 31) / 32));
+    k_bspmm_warp<U><<<grid, 256, 0, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.diag.p, X, Y, bt.n, bt.B);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
 void bspmm_variant(const ed_batch& bt, int tb, int u, const double* X, double* Y, cudaStream_t st)
 {
-    if (tb == 4 && u == 4) launch_bspmm<4, 4>(bt, X, Y, st);
+    if (tb == 32 && u == 4) launch_bspmm_warp<4>(bt, X, Y, st);
+    else if (tb == 32) launch_bspmm_warp<8>(bt, X, Y, st);
+    else if (tb == 4 && u == 4) launch_bspmm<4, 4>(bt, X, Y, st);
     else if (tb == 4 && u == 8) launch_bspmm<4, 8>(bt, X, Y, st);
     else if (tb == 8 && u == 4) launch_bspmm<8, 4>(bt, X, Y, st);
     else if (tb == 8 && u == 8) launch_bspmm<8, 8>(bt, X, Y, st);
@@ -619,9 +675,9 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
     ED_CUDA(cudaEventCreate(&b));
     float best = 1e30f;
     int btb = 8, bu = 8;
-    for (int tb : {4, 8, 16}) {
-        if ((size_t)bt.nhop * tb * 8 > 200 * 1024) continue;
-        if (tb > 4 && bt.B <= 4) continue;
+    for (int tb : {4, 8, 16, 32}) {
+        if (tb < 32 && (size_t)bt.nhop * tb * 8 > 200 * 1024) continue;
+        if (tb > 4 && tb < 32 && bt.B <= 4) continue;
         for (int u : {4, 8}) {
             bspmm_variant(bt, tb, u, X.p, Y.p, st);
             ED_CUDA(cudaEventRecord(a, st));

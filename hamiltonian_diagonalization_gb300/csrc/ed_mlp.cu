@@ -1,0 +1,621 @@
+// Learned warm start (K10/K11): a small MLP maps (occupation bitstring, V1)
+// to (log|psi|, sign logit) of the sector's ground state.  It is trained on
+// ground states the solver itself produced, with BF16 weights and
+// activations and FP32 accumulation on the tensor cores (warp-level
+// mma.sync m16n8k16), FP32 master weights and Adam.  Its prediction,
+// evaluated on every basis word of a held-out V1, normalised, seeds the
+// Lanczos solve.  No reference counterpart: the reference always starts ARPACK
+// from its own random vector or a file (arpack_wrapper.hpp:753-774).
+//
+// Layout: features x = (2*bit_k - 1 for k < norb, (V1 - 1.75)/1.25, zeros)
+// padded to 32; hidden width H (multiple of 64) for three SiLU layers; the
+// output layer is padded to 8 columns of which 0 = log|psi|, 1 = sign logit.
+// Weights are [in][out] row-major.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "ed_internal.h"
+
+namespace edgb {
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kIn = 32;
+constexpr int kOut = 8;
+constexpr int kLayers = 4;
+
+// ------------------------------------------------------------- GEMM core
+// C[M,N] = sum_k A(m,k) B(k,n) with A(m,k) = A[m*sam + k*sak] and
+// B(k,n) = Bm[k*sbk + n*sbn] (bf16), FP32 accumulation in mma.sync
+// m16n8k16; 64x64 block tile, BK 32, four warps of 32x32.  Tiles are staged
+// through shared memory with bounds checks, so any strides (transposes)
+// and any M, N, K work; the epilogue functor receives (row, col, value).
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(128) k_gemm(const bf16* __restrict__ A, int64_t sam, int64_t sak,
+                                              const bf16* __restrict__ Bm, int64_t sbk, int64_t sbn, int M, int N, int K,
+                                              Epi epi)
+{
+    __shared__ __align__(16) bf16 sA[64][40];   // [m][k]
+    __shared__ __align__(16) bf16 sB[64][40];   // [n][k]
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int g = lane >> 2, tq = lane & 3;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int k0 = 0; k0 < K; k0 += 32) {
+        for (int i = threadIdx.x; i < 64 * 32; i += 128) {
+            const int r = i >> 5, c = i & 31;
+            const int gm = m0 + r, gk = k0 + c;
+            sA[r][c] = (gm < M && gk < K) ? A[(int64_t)gm * sam + (int64_t)gk * sak] : zero;
+            const int gn = n0 + r;
+            sB[r][c] = (gn < N && gk < K) ? Bm[(int64_t)gk * sbk + (int64_t)gn * sbn] : zero;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 32; kk += 16) {
+            uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+            for (int mi = 0; mi < 2; ++mi) {
+                const int r = wm + mi * 16 + g;
+                af[mi][0] = *reinterpret_cast<const uint32_t*>(&sA[r][kk + tq * 2]);
+                af[mi][1] = *reinterpret_cast<const uint32_t*>(&sA[r + 8][kk + tq * 2]);
+                af[mi][2] = *reinterpret_cast<const uint32_t*>(&sA[r][kk + tq * 2 + 8]);
+                af[mi][3] = *reinterpret_cast<const uint32_t*>(&sA[r + 8][kk + tq * 2 + 8]);
+            }
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni) {
+                const int nn = wn + ni * 8 + g;
+                bfr[ni][0] = *reinterpret_cast<const uint32_t*>(&sB[nn][kk + tq * 2]);
+                bfr[ni][1] = *reinterpret_cast<const uint32_t*>(&sB[nn][kk + tq * 2 + 8]);
+            }
+#pragma unroll
+            for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+                for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], af[mi], bfr[ni]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int row = m0 + wm + mi * 16 + g + ((e >= 2) ? 8 : 0);
+                const int col = n0 + wn + ni * 8 + tq * 2 + (e & 1);
+                if (row < M && col < N) epi(row, col, acc[mi][ni][e]);
+            }
+}
+
+template <class Epi>
+void gemm(const bf16* A, int64_t sam, int64_t sak, const bf16* B, int64_t sbk, int64_t sbn, int M, int N, int K,
+          Epi epi, cudaStream_t st)
+{
+    dim3 grid((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64));
+    k_gemm<Epi><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, epi);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z)
+{
+    const float s = 1.f / (1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
+
+// Forward epilogue: Z = acc + bias (FP32, kept for the backward pass) and,
+// for hidden layers, H = bf16(SiLU(Z)).
+struct EpiForward {
+    const float* bias;
+    float* Z;
+    bf16* Hout;   // nullptr for the output layer
+    int ld;
+    __device__ void operator()(int r, int c, float v) const
+    {
+        const float z = v + bias[c];
+        Z[(int64_t)r * ld + c] = z;
+        if (Hout) Hout[(int64_t)r * ld + c] = __float2bfloat16(silu(z));
+    }
+};
+
+// Backward-data epilogue: dZ = acc * SiLU'(Z) in bf16 (input of the next GEMMs)
+// and FP32 (for the bias gradient).
+struct EpiBackData {
+    const float* Z;
+    bf16* dZ;
+    float* dZf;
+    int ld;
+    __device__ void operator()(int r, int c, float v) const
+    {
+        const float d = v * dsilu(Z[(int64_t)r * ld + c]);
+        dZ[(int64_t)r * ld + c] = __float2bfloat16(d);
+        dZf[(int64_t)r * ld + c] = d;
+    }
+};
+
+// Weight-gradient epilogue: plain FP32 store.
+struct EpiStore {
+    float* out;
+    int ld;
+    __device__ void operator()(int r, int c, float v) const { out[(int64_t)r * ld + c] = v; }
+};
+
+// features of sample i: word bits as +-1, scaled V1, zero padding
+__global__ void k_features(const uint64_t* __restrict__ words, const float* __restrict__ v1, int64_t m, int norb,
+                           bf16* __restrict__ X)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * kIn; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / kIn;
+        const int f = (int)(t - i * kIn);
+        float x = 0.f;
+        if (f < norb) x = ((words[i] >> f) & 1ull) ? 1.f : -1.f;
+        else if (f == norb) x = (v1[i] - 1.75f) / 1.25f;
+        X[t] = __float2bfloat16(x);
+    }
+}
+
+// loss and output gradient: L = mean[(y0-t0)^2 + softplus(y1) - t1*y1]
+__global__ void k_loss_grad(const float* __restrict__ Z4, const float* __restrict__ target, int64_t m,
+                            bf16* __restrict__ dZ4, float* __restrict__ dZ4f, double* __restrict__ loss)
+{
+    __shared__ double red[256];
+    double l = 0.0;
+    const float inv = 1.f / (float)m;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const float y0 = Z4[i * kOut], y1 = Z4[i * kOut + 1];
+        const float t0 = target[2 * i], t1 = target[2 * i + 1];
+        const float d0 = y0 - t0;
+        const float sp = y1 > 0 ? y1 + log1pf(__expf(-y1)) : log1pf(__expf(y1));
+        l += (double)(d0 * d0 + sp - t1 * y1);
+        const float g0 = 2.f * d0 * inv;
+        const float g1 = (1.f / (1.f + __expf(-y1)) - t1) * inv;
+        for (int c = 0; c < kOut; ++c) {
+            const float g = c == 0 ? g0 : (c == 1 ? g1 : 0.f);
+            dZ4[i * kOut + c] = __float2bfloat16(g);
+            dZ4f[i * kOut + c] = g;
+        }
+    }
+    red[threadIdx.x] = l;
+    __syncthreads();
+    for (int s = 128; s; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, red[0]);
+}
+
+// db[c] = sum_i dZ[i][c]  (one block per column tile, FP32)
+__global__ void k_colsum(const float* __restrict__ dZ, int64_t m, int n, float* __restrict__ db)
+{
+    const int c = blockIdx.x;
+    __shared__ float red[256];
+    float s = 0.f;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s += dZ[i * n + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = 128; k; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[c] = red[0];
+}
+
+// Adam on the FP32 masters, refreshing the bf16 copies of the weights.
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, bf16* __restrict__ pb, int64_t n, float lr, float b1, float b2,
+                       float c1, float c2, float eps)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float a = b1 * m1[i] + (1.f - b1) * gi;
+        const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+        m1[i] = a;
+        m2[i] = b;
+        const float v = p[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+        p[i] = v;
+        if (pb) pb[i] = __float2bfloat16(v);
+    }
+}
+
+__global__ void k_to_bf16(const float* __restrict__ x, bf16* __restrict__ y, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16(x[i]);
+}
+
+// training batch: sample s -> (state r, V1 index b) from a seeded hash; the
+// target is (log|psi_b(r)|, sign), log clipped at -40
+__global__ void k_make_batch(const uint64_t* __restrict__ basis, int64_t n, const double* __restrict__ psi, int nv,
+                             const float* __restrict__ v1s, int64_t m, uint64_t seed, uint64_t* __restrict__ words,
+                             float* __restrict__ v1, float* __restrict__ target)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(s + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const int64_t r = (int64_t)((z >> 20) % (uint64_t)n);
+        const int b = (int)((z & 0xFFFFF) % (uint64_t)nv);
+        const double a = psi[r * nv + b];
+        words[s] = basis[r];
+        v1[s] = v1s[b];
+        target[2 * s] = (float)fmax(log(fabs(a) + 1e-300), -40.0);
+        target[2 * s + 1] = a >= 0.0 ? 1.f : 0.f;
+    }
+}
+
+// warm start: V0[r][b] = sign * exp(logamp - shift_b); shift per problem
+// keeps exp in range, normalisation follows in the solver
+__global__ void k_psi_from_out(const float* __restrict__ out, int64_t n, int B, int b, const float* __restrict__ shift,
+                               double* __restrict__ V0)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const float y0 = out[r * kOut], y1 = out[r * kOut + 1];
+        const double a = exp((double)y0 - (double)shift[0]);
+        V0[r * B + b] = y1 >= 0.f ? a : -a;
+    }
+}
+
+__global__ void k_max_col0(const float* __restrict__ out, int64_t n, float* __restrict__ mx)
+{
+    __shared__ float red[256];
+    float m = -3.0e38f;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, out[r * kOut]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = 128; s; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        // float atomic max through the ordered-int trick (values may be negative)
+        int* addr = reinterpret_cast<int*>(mx);
+        float v = red[0];
+        int old = *addr;
+        while (true) {
+            const float cur = __int_as_float(old);
+            if (cur >= v) break;
+            const int prev = atomicCAS(addr, old, __float_as_int(v));
+            if (prev == old) break;
+            old = prev;
+        }
+    }
+}
+
+int grid_sz(int64_t work)
+{
+    int dev = 0, s = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)s * 8, (work + 255) / 256));
+}
+
+}  // namespace
+
+}  // namespace edgb
+
+struct ed_mlp {
+    int norb = 0, H = 0;
+    int dims[edgb::kLayers + 1];          // 32, H, H, H, 8
+    int64_t woff[edgb::kLayers], boff[edgb::kLayers], nparam = 0;
+    edgb::DevBuf<float> p, g, m1, m2;    // all parameters (weights then bias per layer)
+    edgb::DevBuf<__nv_bfloat16> pb;      // bf16 copies (weights only used)
+    int64_t step = 0;
+    // activations sized for the largest batch seen
+    int64_t cap = 0;
+    edgb::DevBuf<__nv_bfloat16> X, Hb[3], dZb[4];
+    edgb::DevBuf<float> Z[4], dZf[4];
+    edgb::DevBuf<uint64_t> words;
+    edgb::DevBuf<float> v1, target;
+    edgb::DevBuf<double> loss;
+};
+
+namespace edgb {
+
+namespace {
+
+void mlp_reserve(ed_mlp& net, int64_t m)
+{
+    if (m <= net.cap) return;
+    net.X.alloc((size_t)m * kIn);
+    for (int l = 0; l < 3; ++l) net.Hb[l].alloc((size_t)m * net.H);
+    for (int l = 0; l < 4; ++l) {
+        const int w = net.dims[l + 1];
+        net.Z[l].alloc((size_t)m * w);
+        net.dZf[l].alloc((size_t)m * w);
+        net.dZb[l].alloc((size_t)m * w);
+    }
+    net.words.alloc(m);
+    net.v1.alloc(m);
+    net.target.alloc((size_t)2 * m);
+    net.loss.alloc(1);
+    net.cap = m;
+}
+
+// forward for m samples whose features are already in net.X; Z[3] holds the outputs
+void mlp_forward(ed_mlp& net, int64_t m, cudaStream_t st)
+{
+    const bf16* in = net.X.p;
+    int ldin = kIn;
+    for (int l = 0; l < kLayers; ++l) {
+        const int K = net.dims[l], N = net.dims[l + 1];
+        EpiForward e{net.p.p + net.boff[l], net.Z[l].p, l < 3 ? net.Hb[l].p : nullptr, N};
+        gemm(in, ldin, 1, net.pb.p + net.woff[l], N, 1, (int)m, N, K, e, st);
+        if (l < 3) {
+            in = net.Hb[l].p;
+            ldin = N;
+        }
+    }
+}
+
+// backward from dZ[3] (set by the loss) into net.g
+void mlp_backward(ed_mlp& net, int64_t m, cudaStream_t st)
+{
+    for (int l = kLayers - 1; l >= 0; --l) {
+        const int K = net.dims[l], N = net.dims[l + 1];
+        // dW_l = in^T dZ_l  (K x N), reduction over the m samples
+        const bf16* in = l == 0 ? net.X.p : net.Hb[l - 1].p;
+        const int ldin = l == 0 ? kIn : net.dims[l];
+        EpiStore es{net.g.p + net.woff[l], N};
+        gemm(in, 1, ldin, net.dZb[l].p, N, 1, K, N, (int)m, es, st);
+        k_colsum<<<N, 256, 0, st>>>(net.dZf[l].p, m, N, net.g.p + net.boff[l]);
+        count_launch();
+        if (l > 0) {
+            // dZ_{l-1} = (dZ_l W_l^T) * SiLU'(Z_{l-1})
+            EpiBackData eb{net.Z[l - 1].p, net.dZb[l - 1].p, net.dZf[l - 1].p, K};
+            gemm(net.dZb[l].p, N, 1, net.pb.p + net.woff[l], 1, N, (int)m, K, N, eb, st);
+        }
+    }
+}
+
+void mlp_features(ed_mlp& net, const uint64_t* words, const float* v1, int64_t m, cudaStream_t st)
+{
+    k_features<<<grid_sz(m * kIn), 256, 0, st>>>(words, v1, m, net.norb, net.X.p);
+    count_launch();
+}
+
+double mlp_loss(ed_mlp& net, const float* target, int64_t m, cudaStream_t st)
+{
+    ED_CUDA(cudaMemsetAsync(net.loss.p, 0, 8, st));
+    k_loss_grad<<<grid_sz(m), 256, 0, st>>>(net.Z[3].p, target, m, net.dZb[3].p, net.dZf[3].p, net.loss.p);
+    count_launch();
+    double l = 0.0;
+    ED_CUDA(cudaMemcpyAsync(&l, net.loss.p, 8, cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    return l / (double)m;
+}
+
+void mlp_adam(ed_mlp& net, float lr, cudaStream_t st)
+{
+    net.step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)net.step), c2 = 1.f - std::pow(b2, (float)net.step);
+    k_adam<<<grid_sz(net.nparam), 256, 0, st>>>(net.p.p, net.g.p, net.m1.p, net.m2.p, net.pb.p, net.nparam, lr, b1, b2,
+                                                c1, c2, 1e-8f);
+    count_launch();
+}
+
+}  // namespace
+
+}  // namespace edgb
+
+using namespace edgb;
+
+extern "C" {
+
+ed_status ed_mlp_create(int norb, int hidden, uint64_t seed, ed_mlp** out)
+{
+    return guard([&] {
+        ED_REQUIRE(out, ED_ERR_ARG, "NULL output");
+        ED_REQUIRE(norb >= 2 && norb < kIn, ED_ERR_RANGE, "the network takes up to 31 orbitals");
+        ED_REQUIRE(hidden >= 64 && hidden % 64 == 0 && hidden <= 1024, ED_ERR_ARG, "hidden width: multiple of 64");
+        ed_mlp* net = new ed_mlp();
+        try {
+            net->norb = norb;
+            net->H = hidden;
+            const int d[kLayers + 1] = {kIn, hidden, hidden, hidden, kOut};
+            int64_t off = 0;
+            for (int l = 0; l <= kLayers; ++l) net->dims[l] = d[l];
+            for (int l = 0; l < kLayers; ++l) {
+                net->woff[l] = off;
+                off += (int64_t)d[l] * d[l + 1];
+                net->boff[l] = off;
+                off += d[l + 1];
+            }
+            net->nparam = off;
+            std::vector<float> h(off, 0.f);
+            std::mt19937_64 rng(seed);
+            for (int l = 0; l < kLayers; ++l) {
+                // He-style uniform initialisation for SiLU layers, small output layer
+                const float a = (l < 3 ? std::sqrt(6.f / d[l]) : 0.1f * std::sqrt(3.f / d[l]));
+                std::uniform_real_distribution<float> U(-a, a);
+                for (int64_t i = 0; i < (int64_t)d[l] * d[l + 1]; ++i) h[net->woff[l] + i] = U(rng);
+            }
+            net->p.alloc(off);
+            net->g.alloc(off);
+            net->m1.alloc(off);
+            net->m2.alloc(off);
+            net->pb.alloc(off);
+            ED_CUDA(cudaMemcpy(net->p.p, h.data(), off * 4, cudaMemcpyHostToDevice));
+            ED_CUDA(cudaMemset(net->m1.p, 0, off * 4));
+            ED_CUDA(cudaMemset(net->m2.p, 0, off * 4));
+            k_to_bf16<<<grid_sz(off), 256>>>(net->p.p, net->pb.p, off);
+            count_launch();
+            ED_CUDA(cudaDeviceSynchronize());
+        } catch (...) {
+            delete net;
+            throw;
+        }
+        *out = net;
+    });
+}
+
+ed_status ed_mlp_free(ed_mlp* net)
+{
+    return guard([&] { delete net; });
+}
+
+ed_status ed_mlp_num_params(const ed_mlp* net, int64_t* count)
+{
+    return guard([&] {
+        ED_REQUIRE(net && count, ED_ERR_ARG, "NULL argument");
+        *count = net->nparam;
+    });
+}
+
+ed_status ed_mlp_get_params(const ed_mlp* net, float* host, int64_t count)
+{
+    return guard([&] {
+        ED_REQUIRE(net && host && count == net->nparam, ED_ERR_ARG, "bad buffer");
+        ED_CUDA(cudaMemcpy(host, net->p.p, count * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+ed_status ed_mlp_set_params(ed_mlp* net, const float* host, int64_t count)
+{
+    return guard([&] {
+        ED_REQUIRE(net && host && count == net->nparam, ED_ERR_ARG, "bad buffer");
+        ED_CUDA(cudaMemcpy(net->p.p, host, count * 4, cudaMemcpyHostToDevice));
+        k_to_bf16<<<grid_sz(count), 256>>>(net->p.p, net->pb.p, count);
+        count_launch();
+        ED_CUDA(cudaDeviceSynchronize());
+    });
+}
+
+ed_status ed_mlp_forward(ed_mlp* net, const uint64_t* words_dev, const float* v1_dev, int64_t m, float* out_dev)
+{
+    return guard([&] {
+        ED_REQUIRE(net && words_dev && v1_dev && out_dev && m >= 1, ED_ERR_ARG, "bad argument");
+        mlp_reserve(*net, m);
+        mlp_features(*net, words_dev, v1_dev, m, nullptr);
+        mlp_forward(*net, m, nullptr);
+        ED_CUDA(cudaMemcpyAsync(out_dev, net->Z[3].p, (size_t)m * kOut * 4, cudaMemcpyDeviceToDevice, nullptr));
+        ED_CUDA(cudaStreamSynchronize(nullptr));
+    });
+}
+
+ed_status ed_mlp_gradients(ed_mlp* net, const uint64_t* words_dev, const float* v1_dev, const float* target_dev,
+                           int64_t m, float* grads_host, double* loss_host)
+{
+    return guard([&] {
+        ED_REQUIRE(net && words_dev && v1_dev && target_dev && m >= 1, ED_ERR_ARG, "bad argument");
+        mlp_reserve(*net, m);
+        mlp_features(*net, words_dev, v1_dev, m, nullptr);
+        mlp_forward(*net, m, nullptr);
+        const double l = mlp_loss(*net, target_dev, m, nullptr);
+        mlp_backward(*net, m, nullptr);
+        if (grads_host) ED_CUDA(cudaMemcpy(grads_host, net->g.p, net->nparam * 4, cudaMemcpyDeviceToHost));
+        if (loss_host) *loss_host = l;
+        ED_CUDA(cudaStreamSynchronize(nullptr));
+    });
+}
+
+ed_status ed_mlp_train_step(ed_mlp* net, const uint64_t* words_dev, const float* v1_dev, const float* target_dev,
+                            int64_t m, float lr, double* loss_host)
+{
+    return guard([&] {
+        ED_REQUIRE(net && words_dev && v1_dev && target_dev && m >= 1, ED_ERR_ARG, "bad argument");
+        mlp_reserve(*net, m);
+        mlp_features(*net, words_dev, v1_dev, m, nullptr);
+        mlp_forward(*net, m, nullptr);
+        const double l = mlp_loss(*net, target_dev, m, nullptr);
+        mlp_backward(*net, m, nullptr);
+        mlp_adam(*net, lr, nullptr);
+        if (loss_host) *loss_host = l;
+    });
+}
+
+ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* basis, const double* v1_host, int nv, const double* psi_dev,
+                     int steps, int batch, float lr, uint64_t seed, double* final_loss)
+{
+    return guard([&] {
+        ED_REQUIRE(net && basis && v1_host && psi_dev && nv >= 1 && steps >= 1 && batch >= 64, ED_ERR_ARG,
+                   "bad argument");
+        ED_REQUIRE(basis->norb == net->norb, ED_ERR_ARG, "basis and network have different orbital counts");
+        mlp_reserve(*net, batch);
+        std::vector<float> v1f(nv);
+        for (int i = 0; i < nv; ++i) v1f[i] = (float)v1_host[i];
+        DevBuf<float> dv1(nv);
+        ED_CUDA(cudaMemcpy(dv1.p, v1f.data(), nv * 4, cudaMemcpyHostToDevice));
+        double l = 0.0;
+        for (int s = 0; s < steps; ++s) {
+            k_make_batch<<<grid_sz(batch), 256>>>(basis->words.p, (int64_t)basis->dim, psi_dev, nv, dv1.p, batch,
+                                                   seed + 0x632BE59BD9B4E019ull * (uint64_t)(s + 1), net->words.p,
+                                                   net->v1.p, net->target.p);
+            count_launch();
+            mlp_features(*net, net->words.p, net->v1.p, batch, nullptr);
+            mlp_forward(*net, batch, nullptr);
+            const bool report = (s + 1 == steps) || ((s & 63) == 0);
+            if (report) l = mlp_loss(*net, net->target.p, batch, nullptr);
+            else {
+                k_loss_grad<<<grid_sz(batch), 256>>>(net->Z[3].p, net->target.p, batch, net->dZb[3].p,
+                                                     net->dZf[3].p, net->loss.p);
+                count_launch();
+            }
+            mlp_backward(*net, batch, nullptr);
+            mlp_adam(*net, lr, nullptr);
+        }
+        ED_CUDA(cudaStreamSynchronize(nullptr));
+        if (final_loss) *final_loss = l;
+    });
+}
+
+ed_status ed_warm_start(ed_mlp* net, const ed_basis* basis, const double* v1_host, int nham, double* V0_dev)
+{
+    return guard([&] {
+        ED_REQUIRE(net && basis && v1_host && V0_dev && nham >= 1, ED_ERR_ARG, "bad argument");
+        ED_REQUIRE(basis->norb == net->norb, ED_ERR_ARG, "basis and network have different orbital counts");
+        const int64_t n = (int64_t)basis->dim;
+        ED_REQUIRE(n >= 1, ED_ERR_EMPTY, "empty sector");
+        const int64_t chunk = std::min<int64_t>(n, 1 << 20);
+        mlp_reserve(*net, chunk);
+        DevBuf<float> v1c(chunk), out((size_t)n * kOut), mx(1);
+        for (int b = 0; b < nham; ++b) {
+            const float vf = (float)v1_host[b];
+            std::vector<float> fill(chunk, vf);
+            ED_CUDA(cudaMemcpy(v1c.p, fill.data(), chunk * 4, cudaMemcpyHostToDevice));
+            for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+                const int64_t m = std::min(chunk, n - r0);
+                mlp_features(*net, basis->words.p + r0, v1c.p, m, nullptr);
+                mlp_forward(*net, m, nullptr);
+                ED_CUDA(cudaMemcpyAsync(out.p + r0 * kOut, net->Z[3].p, (size_t)m * kOut * 4, cudaMemcpyDeviceToDevice,
+                                        nullptr));
+            }
+            const float neg = -3.0e38f;
+            ED_CUDA(cudaMemcpy(mx.p, &neg, 4, cudaMemcpyHostToDevice));
+            k_max_col0<<<grid_sz(n), 256>>>(out.p, n, mx.p);
+            count_launch();
+            k_psi_from_out<<<grid_sz(n), 256>>>(out.p, n, nham, b, mx.p, V0_dev);
+            count_launch();
+        }
+        ED_CUDA(cudaDeviceSynchronize());
+    });
+}
+
+}  // extern "C"

@@ -20,10 +20,13 @@ namespace {
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
 
-// G lanes per row, each lane taking every G-th element in two independent
-// chains.  Measured on GB300 (N=11, 2S=30): G=8 keeps the FP64 pipe ~74%
-// busy at 1.14 ms per product; deeper unguarded batches (G=4, 8 loads in
-// flight) stalled on the dependent gathers and ran slower (1.31 ms).
+// G lanes per row, each lane summing every G-th element of the row in one
+// FMA chain.  Measured on GB300 (N=11, 2S=30, same process, 20 products):
+// G=8 one chain 0.825 ms (5.1 TB/s, 75% of the measured copy peak); two
+// chains 0.885 ms, four chains 1.04 ms, G=4 or 16 >= 1.04 ms; deeper
+// unguarded batches (G=4, 8 loads in flight) 1.31 ms.  The extra chains cost
+// registers and FP64 additions without adding useful memory parallelism: the
+// warps of a full SM already keep the DRAM queue busy.
 template <int G>
 __global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                    const double* __restrict__ val, const double* __restrict__ x,
@@ -37,19 +40,11 @@ __global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ r
         const int64_t r = rb + grp;
         const bool valid = r < n;
         const int64_t s = valid ? rowptr[r] : 0, e = valid ? rowptr[r + 1] : 0;
-        double acc0 = 0.0, acc1 = 0.0;
-        int64_t k = s + sub;
-        for (; k + G < e; k += 2 * G) {
-            const int c0 = ld_stream(col + k), c1 = ld_stream(col + k + G);
-            const double v0 = ld_stream(val + k), v1 = ld_stream(val + k + G);
-            acc0 = fma(v0, __ldg(x + c0), acc0);
-            acc1 = fma(v1, __ldg(x + c1), acc1);
-        }
-        if (k < e) acc0 = fma(ld_stream(val + k), __ldg(x + ld_stream(col + k)), acc0);
-        double a = acc0 + acc1;
+        double acc = 0.0;
+        for (int64_t k = s + sub; k < e; k += G) acc = fma(ld_stream(val + k), __ldg(x + ld_stream(col + k)), acc);
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
-        if (valid && sub == 0) y[r] = a;
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+        if (valid && sub == 0) y[r] = acc;
     }
 }
 

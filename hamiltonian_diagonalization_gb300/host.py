@@ -470,3 +470,56 @@ class HamiltonianBatch:
         if getattr(self, "_h", None) is not None and C._LIB is not None:
             C._LIB.ed_batch_free(self._h)
             self._h = None
+
+
+class WarmStartMLP:
+    """Learned warm start (ed_mlp_*): an MLP from (occupation bits, V1) to
+    (log|psi|, sign logit), trained on ground states the solver produced and
+    evaluated on a sector to seed Lanczos."""
+
+    def __init__(self, norb: int, hidden: int = 256, seed: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().ed_mlp_create(norb, hidden, seed, ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_int64()
+        check(lib().ed_mlp_num_params(h, ctypes.byref(n)))
+        self.nparam = int(n.value)
+        self.norb, self.hidden = norb, hidden
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.nparam, dtype=np.float32)
+        check(lib().ed_mlp_get_params(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), self.nparam))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().ed_mlp_set_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), self.nparam))
+
+    def forward(self, words_dev, v1_dev, out_dev):
+        check(lib().ed_mlp_forward(self._h, _dptr(words_dev), _dptr(v1_dev), int(words_dev.numel()), _dptr(out_dev)))
+
+    def gradients(self, words_dev, v1_dev, target_dev):
+        g = np.empty(self.nparam, dtype=np.float32)
+        loss = ctypes.c_double()
+        check(lib().ed_mlp_gradients(self._h, _dptr(words_dev), _dptr(v1_dev), _dptr(target_dev),
+                                     int(words_dev.numel()), g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                     ctypes.byref(loss)))
+        return g, loss.value
+
+    def fit(self, basis: FermionFockBasis, v1s, psi_dev, steps: int = 2000, batch: int = 4096, lr: float = 1e-3,
+            seed: int = 0) -> float:
+        """psi_dev: device [n][len(v1s)] ground states (torch tensor)."""
+        v = np.ascontiguousarray(v1s, dtype=np.float64)
+        loss = ctypes.c_double()
+        check(lib().ed_mlp_fit(self._h, basis.handle(), _f64p(v), len(v), _dptr(psi_dev), steps, batch, lr, seed,
+                               ctypes.byref(loss)))
+        return loss.value
+
+    def warm_start(self, basis: FermionFockBasis, v1s, V0_dev):
+        v = np.ascontiguousarray(v1s, dtype=np.float64)
+        check(lib().ed_warm_start(self._h, basis.handle(), _f64p(v), len(v), _dptr(V0_dev)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and C._LIB is not None:
+            C._LIB.ed_mlp_free(self._h)
+            self._h = None

@@ -67,6 +67,65 @@ def run_batched(N, norb, sectors, v1s, nev, tol, seed):
     return time.perf_counter() - t0, evals, infos
 
 
+def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=2000, batch=4096, lr=1e-3,
+             hidden=256):
+    """Batched + learned warm start.  Per sector: solve the training V1 points
+    (a seeded random 3/4 of them) batched from random starts, fit the MLP on
+    their ground states, then solve the held-out points batched from the
+    network's prediction.  The held-out points are also solved from random
+    starts (untimed) to report what the warm start saves."""
+    import torch
+
+    import hamiltonian_diagonalization_gb300 as ed
+    rng = np.random.default_rng(seed)
+    idx = rng.permutation(len(v1s))
+    nheld = max(1, int(round(held_frac * len(v1s))))
+    held, train = np.sort(idx[:nheld]), np.sort(idx[nheld:])
+    lists = sweep_lists(norb, v1s)
+    evals = {}
+    rec = []
+    total = 0.0
+    for tlz in sectors:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b = ed.FermionFockBasis()
+        b.GenerateFockSpace(N, norb, tlz)
+        bt = ed.HamiltonianBatch(b, [lists[j] for j in train])
+        ev_t, vec_t, inf_t = bt.solve(nev, tol=tol, seed=seed, want_vectors=True)
+        t1 = time.perf_counter()
+        net = ed.WarmStartMLP(norb, hidden, seed=seed)
+        psi = vec_t[0].contiguous()
+        loss = net.fit(b, v1s[train], psi, steps=steps, batch=batch, lr=lr, seed=seed + 1)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        bh = ed.HamiltonianBatch(b, [lists[j] for j in held])
+        V0 = torch.empty((bh.n, len(held)), dtype=torch.float64, device="cuda")
+        net.warm_start(b, v1s[held], V0)
+        ev_w, vec_w, inf_w = bh.solve(nev, tol=tol, V0=V0, want_vectors=True)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        total += t3 - t0
+        # held-out from random starts, for the comparison only (not timed into the sweep)
+        t4 = time.perf_counter()
+        ev_r, _, inf_r = bh.solve(nev, tol=tol, seed=seed + 2)
+        t5 = time.perf_counter()
+        P = V0.cpu().numpy()
+        T = vec_w[0].cpu().numpy()
+        ov = np.abs(np.sum(P * T, axis=0)) / np.linalg.norm(P, axis=0)
+        for k, j in enumerate(train):
+            evals[(tlz, j)] = ev_t[k]
+        for k, j in enumerate(held):
+            evals[(tlz, j)] = ev_w[k]
+        rec.append({"two_lz": tlz, "train_seconds": t1 - t0, "fit_seconds": t2 - t1, "fit_loss": loss,
+                    "held_warm_seconds": t3 - t2, "held_random_seconds": t5 - t4,
+                    "held_warm_products": inf_w["block_products"], "held_random_products": inf_r["block_products"],
+                    "train_products": inf_t["block_products"], "overlap_min": float(ov.min()),
+                    "overlap_mean": float(ov.mean()),
+                    "ground_energy_warm_vs_random_max_rel": float(np.max(np.abs(ev_w[:, 0] - ev_r[:, 0]) /
+                                                                         np.abs(ev_r[:, 0])))})
+    return total, evals, rec
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--N", type=int, default=10)
@@ -76,14 +135,18 @@ def main():
     ap.add_argument("--nev", type=int, default=4)
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--mode", default="both", choices=["plain", "batched", "both"])
+    ap.add_argument("--mode", default="both", choices=["plain", "batched", "both", "warm", "all"])
+    ap.add_argument("--mlp-steps", type=int, default=2000)
     args = ap.parse_args()
     sectors = [int(s) for s in args.sectors.split(",")]
     v1s = np.linspace(0.5, 3.0, args.points)
     nsolve = len(sectors) * len(v1s)
     out = {"N": args.N, "norb": args.norb, "sectors": sectors, "points": args.points, "nev": args.nev,
            "tol": args.tol, "solves": nsolve}
-    if args.mode in ("batched", "both"):
+    if args.mode in ("warm", "all"):
+        tw, ew, rec = run_warm(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, steps=args.mlp_steps)
+        out["batched_warm"] = {"seconds": tw, "solves_per_s": nsolve / tw, "per_sector": rec}
+    if args.mode in ("batched", "both", "all"):
         # one untimed warm-up batch (module load, autotune code paths)
         run_batched(args.N, args.norb, sectors[:1], v1s[:2], args.nev, args.tol, args.seed)
         tb, eb, infos = run_batched(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed)
@@ -94,13 +157,16 @@ def main():
                           "max_residual": max(i["max_residual"] for i in infos),
                           "converged": sum(i["converged"] for i in infos),
                           "tile": [infos[0]["tile_hamiltonians"], infos[0]["tile_unroll"]]}
-    if args.mode in ("plain", "both"):
+    if args.mode in ("plain", "both", "all"):
         run_plain(args.N, args.norb, sectors[:1], v1s[:1], args.nev, args.tol, args.seed)
         tp, ep, products = run_plain(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed)
         out["plain"] = {"seconds": tp, "solves_per_s": nsolve / tp, "products": products}
-    if args.mode == "both":
+    if args.mode in ("both", "all"):
         out["speedup_batched_vs_plain"] = out["plain"]["seconds"] / out["batched"]["seconds"]
         out["max_rel_eigenvalue_diff"] = float(max(np.max(np.abs(eb[k] - ep[k]) / np.abs(ep[k])) for k in ep))
+    if args.mode == "all":
+        out["speedup_batched_warm_vs_plain"] = out["plain"]["seconds"] / out["batched_warm"]["seconds"]
+        out["max_rel_eigenvalue_diff_warm"] = float(max(np.max(np.abs(ew[k] - ep[k]) / np.abs(ep[k])) for k in ep))
     print(json.dumps(out))
 
 

@@ -267,6 +267,37 @@ ed_status ed_batch_spmm(const ed_batch* bt, const double* X_dev, double* Y_dev, 
 ed_status ed_batch_solve(const ed_batch* bt, const ed_lanczos_params* p, const double* V0_dev, double* evals_host,
                          double* evecs_dev, ed_batch_info* info);
 
+/* ------------------------------------------------- learned warm start K10/K11 */
+
+/* A small MLP (features: occupation bits as +-1 and the scaled V1, padded to
+ * 32; three SiLU hidden layers of `hidden` units; outputs log|psi| and a sign
+ * logit) trained with BF16 weights/activations and FP32 accumulation on the
+ * tensor cores, FP32 master weights and Adam.  No reference counterpart: the
+ * reference starts ARPACK from a random or file vector
+ * (arpack_wrapper.hpp:753-774).  Parameters are laid out layer by layer,
+ * weights [in][out] row-major then biases. */
+typedef struct ed_mlp ed_mlp;
+ed_status ed_mlp_create(int norb, int hidden, uint64_t seed, ed_mlp** out);
+ed_status ed_mlp_free(ed_mlp* net);
+ed_status ed_mlp_num_params(const ed_mlp* net, int64_t* count);
+ed_status ed_mlp_get_params(const ed_mlp* net, float* host, int64_t count);
+ed_status ed_mlp_set_params(ed_mlp* net, const float* host, int64_t count);
+/* out_dev: m x 8 floats, columns 0 (log|psi|) and 1 (sign logit) used. */
+ed_status ed_mlp_forward(ed_mlp* net, const uint64_t* words_dev, const float* v1_dev, int64_t m, float* out_dev);
+/* Loss (mean squared log-amplitude error + sign cross-entropy) and its
+ * gradient for one batch; target_dev: m x 2 (log|psi|, sign as 0/1). */
+ed_status ed_mlp_gradients(ed_mlp* net, const uint64_t* words_dev, const float* v1_dev, const float* target_dev,
+                           int64_t m, float* grads_host, double* loss_host);
+ed_status ed_mlp_train_step(ed_mlp* net, const uint64_t* words_dev, const float* v1_dev, const float* target_dev,
+                            int64_t m, float lr, double* loss_host);
+/* Train on ground states psi_dev ([n][nv], one column per V1 value) of the
+ * basis: `steps` Adam steps on seeded random batches of (state, V1). */
+ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* b, const double* v1_host, int nv, const double* psi_dev, int steps,
+                     int batch, float lr, uint64_t seed, double* final_loss);
+/* Start vectors for nham Hamiltonians: V0_dev[r*nham + j] = predicted psi of
+ * basis word r at v1_host[j] (unnormalised; the solvers normalise). */
+ed_status ed_warm_start(ed_mlp* net, const ed_basis* b, const double* v1_host, int nham, double* V0_dev);
+
 /* ------------------------------------------------------- one-call driver */
 
 /* Whole sector solve from host inputs: basis -> tables -> CRS (or matrix-free
