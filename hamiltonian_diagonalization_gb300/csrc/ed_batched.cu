@@ -21,6 +21,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "ed_hop.cuh"
@@ -272,24 +274,27 @@ __global__ void __launch_bounds__(256) k_bspmm(const int64_t* __restrict__ rowpt
     }
 }
 
-// Warp per row, lanes = 32 consecutive Hamiltonians: the row's column and
-// code are loaded once (broadcast), the hop values W[h][b0..b0+31] and the
-// gathered X[c][b0..b0+31] are each one contiguous 256-byte read, and every
-// lane does one FMA per element with no reduction.  The [nhop][B] hop table
-// is read through L1 instead of being staged in shared memory, so all 32
-// Hamiltonians fit whatever the table size.
-template <int U>
+// TB lanes per row (TB = 16 or 32), lanes = TB consecutive Hamiltonians:
+// the row's column and code are loaded once (broadcast), the hop values
+// W[h][b0..b0+TB) and the gathered X[c][b0..b0+TB) are each one contiguous
+// read, and every lane does one FMA per element with no reduction.  The
+// [nhop][B] hop table is read through L1 instead of being staged in shared
+// memory, so the tile fits whatever the table size.
+template <int U, int TB>
 __global__ void __launch_bounds__(256) k_bspmm_warp(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                     const uint16_t* __restrict__ code, const double* __restrict__ w,
                                                     const double* __restrict__ diag, const double* __restrict__ X,
                                                     double* __restrict__ Y, int64_t n, int B)
 {
+    constexpr int RPW = 32 / TB;
     const int lane = threadIdx.x & 31;
-    const int b = blockIdx.y * 32 + lane;
+    const int b = blockIdx.y * TB + (lane % TB);
     const bool bv = b < B;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = warp; r < n; r += nwarps) {
+    for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {
+        const int64_t r = rb + lane / TB;
+        if (r >= n) continue;
         const int64_t s = rowptr[r], e = rowptr[r + 1];
         double acc0 = bv ? diag[r * B + b] * X[r * B + b] : 0.0, acc1 = 0.0;
         for (int64_t k = s; k < e; k += U) {
@@ -634,20 +639,24 @@ void launch_bspmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t s
     ED_CUDA(cudaGetLastError());
 }
 
-template <int U>
+template <int U, int TB>
 void launch_bspmm_warp(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
 {
     static_assert(U <= kCrsPad, "batch overruns the padding");
-    dim3 grid((unsigned)(sms_b() * 8), (unsigned)((bt.B + 31) / 32));
-    k_bspmm_warp<U><<<grid, 256, 0, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.diag.p, X, Y, bt.n, bt.B);
+    dim3 grid((unsigned)(sms_b() * 8), (unsigned)((bt.B + TB - 1) / TB));
+    k_bspmm_warp<U, TB><<<grid, 256, 0, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.diag.p, X, Y, bt.n, bt.B);
     count_launch();
     ED_CUDA(cudaGetLastError());
 }
 
+// tb 4, 8: hop tables staged in shared memory; tb 16 (code 17), 32: read
+// through L1 by the TB-lanes-per-row kernel
 void bspmm_variant(const ed_batch& bt, int tb, int u, const double* X, double* Y, cudaStream_t st)
 {
-    if (tb == 32 && u == 4) launch_bspmm_warp<4>(bt, X, Y, st);
-    else if (tb == 32) launch_bspmm_warp<8>(bt, X, Y, st);
+    if (tb == 32 && u == 4) launch_bspmm_warp<4, 32>(bt, X, Y, st);
+    else if (tb == 32) launch_bspmm_warp<8, 32>(bt, X, Y, st);
+    else if (tb == 17 && u == 4) launch_bspmm_warp<4, 16>(bt, X, Y, st);
+    else if (tb == 17) launch_bspmm_warp<8, 16>(bt, X, Y, st);
     else if (tb == 4 && u == 4) launch_bspmm<4, 4>(bt, X, Y, st);
     else if (tb == 4 && u == 8) launch_bspmm<4, 8>(bt, X, Y, st);
     else if (tb == 8 && u == 4) launch_bspmm<8, 4>(bt, X, Y, st);
@@ -666,8 +675,27 @@ void batch_spmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
 // Pick the (Hamiltonians per CTA, loads in flight) pair that runs the block
 // product fastest on this data; shared-memory capacity rules out tiles whose
 // hop tables do not fit.
+// Choices are remembered per (device, Hamiltonians, hop types, rows/4096,
+// nonzeros/2^16) so that the sectors of one sweep are tuned once.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::vector<int64_t>, std::pair<int, int>> g_tune;
+}  // namespace
+
 void batch_autotune(ed_batch& bt, cudaStream_t st)
 {
+    int dev = 0;
+    ED_CUDA(cudaGetDevice(&dev));
+    const std::vector<int64_t> key{dev, bt.B, bt.nhop, bt.n >> 12, bt.nnz >> 16};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            bt.tb = it->second.first;
+            bt.unroll = it->second.second;
+            return;
+        }
+    }
     DevBuf<double> X((size_t)bt.n * bt.B), Y((size_t)bt.n * bt.B);
     k_brandom<<<sms_b() * 4, 256, 0, st>>>(X.p, bt.n * bt.B, 7); count_launch();
     cudaEvent_t a, b;
@@ -675,9 +703,9 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
     ED_CUDA(cudaEventCreate(&b));
     float best = 1e30f;
     int btb = 8, bu = 8;
-    for (int tb : {4, 8, 16, 32}) {
-        if (tb < 32 && (size_t)bt.nhop * tb * 8 > 200 * 1024) continue;
-        if (tb > 4 && tb < 32 && bt.B <= 4) continue;
+    for (int tb : {4, 8, 16, 17, 32}) {
+        if (tb <= 16 && (size_t)bt.nhop * tb * 8 > 200 * 1024) continue;
+        if (tb > 4 && bt.B <= tb / 2) continue;
         for (int u : {4, 8}) {
             bspmm_variant(bt, tb, u, X.p, Y.p, st);
             ED_CUDA(cudaEventRecord(a, st));
@@ -693,6 +721,8 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
     cudaEventDestroy(b);
     bt.tb = btb;
     bt.unroll = bu;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[key] = {btb, bu};
 }
 
 // Lockstep thick-restart Lanczos for the B problems of a batch: the
@@ -748,7 +778,8 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     }
     ed_batch_info inf;
     std::memset(&inf, 0, sizeof(inf));
-    inf.tile_hamiltonians = bt.tb;
+    inf.tile_hamiltonians = bt.tb == 17 ? 16 : bt.tb;
+    inf.tile_l1 = bt.tb >= 17 ? 1 : 0;
     inf.tile_unroll = bt.unroll;
     std::vector<std::vector<double>> T(B, std::vector<double>((size_t)m * m, 0.0)), theta(B), Y(B);
     std::vector<double> coef_h((size_t)m * (m + 1) * B), beta_h((size_t)(m + 1) * B), Yall((size_t)B * m * m);

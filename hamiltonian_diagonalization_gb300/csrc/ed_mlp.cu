@@ -249,18 +249,32 @@ __global__ void k_to_bf16(const float* __restrict__ x, bf16* __restrict__ y, int
 }
 
 // training batch: sample s -> (state r, V1 index b) from a seeded hash; the
-// target is (log|psi_b(r)|, sign), log clipped at -40
+// target is (log|psi_b(r)|, sign), log clipped at -40.  Even samples draw r
+// uniformly (the network must also learn where the state is small), odd
+// samples draw r with probability |psi_b(r)|^2 from the per-column
+// cumulative table cdf[b][r] (the configurations that carry the overlap).
 __global__ void k_make_batch(const uint64_t* __restrict__ basis, int64_t n, const double* __restrict__ psi, int nv,
-                             const float* __restrict__ v1s, int64_t m, uint64_t seed, uint64_t* __restrict__ words,
-                             float* __restrict__ v1, float* __restrict__ target)
+                             const float* __restrict__ v1s, const double* __restrict__ cdf, int64_t m, uint64_t seed,
+                             uint64_t* __restrict__ words, float* __restrict__ v1, float* __restrict__ target)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
         uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(s + 1);
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
         z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
         z ^= z >> 31;
-        const int64_t r = (int64_t)((z >> 20) % (uint64_t)n);
+        int64_t r = (int64_t)((z >> 20) % (uint64_t)n);
         const int b = (int)((z & 0xFFFFF) % (uint64_t)nv);
+        if ((s & 1) && cdf) {
+            const double* c = cdf + (int64_t)b * n;
+            const double u = (double)(r + 0.5) / (double)n * c[n - 1];
+            int64_t lo = 0, hi = n - 1;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (c[mid] > u) hi = mid;
+                else lo = mid + 1;
+            }
+            r = lo;
+        }
         const double a = psi[r * nv + b];
         words[s] = basis[r];
         v1[s] = v1s[b];
@@ -563,9 +577,25 @@ ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* basis, const double* v1_host, 
         for (int i = 0; i < nv; ++i) v1f[i] = (float)v1_host[i];
         DevBuf<float> dv1(nv);
         ED_CUDA(cudaMemcpy(dv1.p, v1f.data(), nv * 4, cudaMemcpyHostToDevice));
+        // per-column cumulative |psi|^2 for the importance-sampled half
+        const int64_t n = (int64_t)basis->dim;
+        std::vector<double> hp((size_t)n * nv), hc((size_t)n * nv);
+        ED_CUDA(cudaMemcpy(hp.data(), psi_dev, hp.size() * 8, cudaMemcpyDeviceToHost));
+        for (int b = 0; b < nv; ++b) {
+            double acc = 0.0;
+            for (int64_t r = 0; r < n; ++r) {
+                const double a = hp[(size_t)r * nv + b];
+                acc += a * a;
+                hc[(size_t)b * n + r] = acc;
+            }
+        }
+        DevBuf<double> cdf(hc.size());
+        ED_CUDA(cudaMemcpy(cdf.p, hc.data(), hc.size() * 8, cudaMemcpyHostToDevice));
         double l = 0.0;
         for (int s = 0; s < steps; ++s) {
-            k_make_batch<<<grid_sz(batch), 256>>>(basis->words.p, (int64_t)basis->dim, psi_dev, nv, dv1.p, batch,
+            // linear decay to a tenth of the rate over the run
+            const float lr_s = lr * (1.f - 0.9f * (float)s / (float)steps);
+            k_make_batch<<<grid_sz(batch), 256>>>(basis->words.p, n, psi_dev, nv, dv1.p, cdf.p, batch,
                                                    seed + 0x632BE59BD9B4E019ull * (uint64_t)(s + 1), net->words.p,
                                                    net->v1.p, net->target.p);
             count_launch();
@@ -579,7 +609,7 @@ ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* basis, const double* v1_host, 
                 count_launch();
             }
             mlp_backward(*net, batch, nullptr);
-            mlp_adam(*net, lr, nullptr);
+            mlp_adam(*net, lr_s, nullptr);
         }
         ED_CUDA(cudaStreamSynchronize(nullptr));
         if (final_loss) *final_loss = l;

@@ -46,11 +46,15 @@ def run_plain(N, norb, sectors, v1s, nev, tol, seed):
     return time.perf_counter() - t0, evals, products
 
 
-def run_batched(N, norb, sectors, v1s, nev, tol, seed):
+def run_batched(N, norb, sectors, v1s, nev, tol, seed, batch_size=0):
+    """Each sector's Hamiltonians in batches of batch_size (0: all at once);
+    a batch's [row][problem] vectors should stay within L2 for the block
+    product's gathers to hit it."""
     import torch
 
     import hamiltonian_diagonalization_gb300 as ed
     lists = sweep_lists(norb, v1s)
+    bs = batch_size or len(lists)
     evals = {}
     infos = []
     torch.cuda.synchronize()
@@ -58,11 +62,12 @@ def run_batched(N, norb, sectors, v1s, nev, tol, seed):
     for tlz in sectors:
         b = ed.FermionFockBasis()
         b.GenerateFockSpace(N, norb, tlz)
-        batch = ed.HamiltonianBatch(b, lists)
-        ev, _, info = batch.solve(nev, tol=tol, seed=seed)
-        infos.append(info)
-        for j in range(len(lists)):
-            evals[(tlz, j)] = ev[j]
+        for j0 in range(0, len(lists), bs):
+            batch = ed.HamiltonianBatch(b, lists[j0:j0 + bs])
+            ev, _, info = batch.solve(nev, tol=tol, seed=seed)
+            infos.append(info)
+            for j in range(len(lists[j0:j0 + bs])):
+                evals[(tlz, j0 + j)] = ev[j]
     torch.cuda.synchronize()
     return time.perf_counter() - t0, evals, infos
 
@@ -137,6 +142,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--mode", default="both", choices=["plain", "batched", "both", "warm", "all"])
     ap.add_argument("--mlp-steps", type=int, default=2000)
+    ap.add_argument("--batch-size", type=int, default=0, help="Hamiltonians per batch (0: all of a sector)")
     args = ap.parse_args()
     sectors = [int(s) for s in args.sectors.split(",")]
     v1s = np.linspace(0.5, 3.0, args.points)
@@ -149,7 +155,7 @@ def main():
     if args.mode in ("batched", "both", "all"):
         # one untimed warm-up batch (module load, autotune code paths)
         run_batched(args.N, args.norb, sectors[:1], v1s[:2], args.nev, args.tol, args.seed)
-        tb, eb, infos = run_batched(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed)
+        tb, eb, infos = run_batched(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, args.batch_size)
         out["batched"] = {"seconds": tb, "solves_per_s": nsolve / tb,
                           "block_products": [i["block_products"] for i in infos],
                           "restarts": [i["restarts"] for i in infos],

@@ -245,8 +245,9 @@ typedef struct {
     double seconds;
     double spmm_seconds;      /* device time inside the block products               */
     int breakdowns;
-    int tile_hamiltonians;    /* autotuned Hamiltonians per CTA of the block product */
+    int tile_hamiltonians;    /* autotuned Hamiltonians per row tile of the block product */
     int tile_unroll;          /* autotuned loads in flight per lane                  */
+    int tile_l1;              /* 1: hop values read through L1, 0: staged in shared memory */
 } ed_batch_info;
 
 /* Shared pattern (int32 column + uint16 hop code per element) built once on

@@ -81,7 +81,7 @@ def test_training_and_warm_start_gain(cuda):
     V0 = torch.empty((n, len(held)), dtype=torch.float64, device="cuda")
     net.warm_start(basis, held, V0)
     batch, ev_rand, vec_true, info_rand = ground_states(torch, basis, norb, held, seed=4)
-    _, ev_warm, info_warm = batch.solve(1, tol=1e-10, V0=V0)
+    ev_warm, _, info_warm = batch.solve(1, tol=1e-10, V0=V0)
     assert np.max(np.abs(ev_warm - ev_rand) / np.abs(ev_rand)) <= 1e-10
     # overlap of the predicted state with the converged ground state
     P = V0.cpu().numpy()
