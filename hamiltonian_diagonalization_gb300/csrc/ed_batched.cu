@@ -18,7 +18,10 @@
 // recurrences, full FP64 reorthogonalisation and restarts, with every scalar
 // per problem and every kernel covering all problems.
 #include <algorithm>
+#include <array>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -38,7 +41,9 @@ struct ed_batch {
     edgb::DevBuf<uint16_t> code;  // nnz + pad
     edgb::DevBuf<double> w;       // [nhop][B] per-Hamiltonian hop values
     edgb::DevBuf<double> diag;    // [n][B]
-    int tb = 8, unroll = 8;       // tuned tile of Hamiltonians per CTA, load batch
+    // tuned block-product tile: Hamiltonians per tile, loads in flight, threads
+    // per CTA, hop values through L1 (1) or staged in shared memory (0)
+    int tb = 32, unroll = 4, nt = 256, l1 = 1;
 };
 
 namespace edgb {
@@ -226,17 +231,25 @@ __global__ void k_bdiag(const uint64_t* __restrict__ words, int64_t n, const dou
     }
 }
 
+// W with the element's fermionic sign applied: bit 15 of the code moved to the
+// sign bit of the high word, an integer XOR that leaves the FP64 pipe to the FMAs.
+__device__ __forceinline__ double signed_w(double w, uint16_t code)
+{
+    return __hiloint2double(__double2hiint(w) ^ (int)((unsigned)(code & kCodeSign) << 16), __double2loint(w));
+}
+
 // Y[r][b] = diag[r][b] X[r][b] + sum_k sign_k W_b[h_k] X[col_k][b] for b in
-// this CTA's tile [b0, b0+TB).  Lane = (row slot, b); U loads in flight.
-template <int TB, int U>
-__global__ void __launch_bounds__(256) k_bspmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                                               const uint16_t* __restrict__ code, const double* __restrict__ w,
-                                               int nhop, const double* __restrict__ diag, const double* __restrict__ X,
-                                               double* __restrict__ Y, int64_t n, int B)
+// this CTA's tile [b0, b0+TB) (NT threads).  The tile's hop values
+// W[nhop][TB] sit in shared memory; lane = (row slot, b); U loads in flight.
+template <int TB, int U, int NT>
+__global__ void __launch_bounds__(NT) k_bspmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                              const uint16_t* __restrict__ code, const double* __restrict__ w,
+                                              int nhop, const double* __restrict__ diag, const double* __restrict__ X,
+                                              double* __restrict__ Y, int64_t n, int B)
 {
     extern __shared__ double sw[];   // [nhop][TB]
     const int b0 = blockIdx.y * TB;
-    for (int i = threadIdx.x; i < nhop * TB; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nhop * TB; i += NT) {
         const int h = i / TB, t = i - h * TB;
         sw[i] = (b0 + t < B) ? w[(size_t)h * B + b0 + t] : 0.0;
     }
@@ -245,8 +258,8 @@ __global__ void __launch_bounds__(256) k_bspmm(const int64_t* __restrict__ rowpt
     const int lane = threadIdx.x & 31, bl = lane % TB, grp = lane / TB;
     const int b = b0 + bl;
     const bool bvalid = b < B;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * NT) >> 5;
     for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {
         const int64_t r = rb + grp;
         if (r >= n || !bvalid) continue;
@@ -263,8 +276,7 @@ __global__ void __launch_bounds__(256) k_bspmm(const int64_t* __restrict__ rowpt
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < e) {
-                    double wv = sw[(cd[u] & 0x7FFF) * TB + bl];
-                    if (cd[u] & kCodeSign) wv = -wv;
+                    const double wv = signed_w(sw[(cd[u] & 0x7FFF) * TB + bl], cd[u]);
                     if (u & 1) acc1 = fma(wv, xv[u], acc1);
                     else acc0 = fma(wv, xv[u], acc0);
                 }
@@ -311,9 +323,8 @@ __global__ void __launch_bounds__(256) k_bspmm_warp(const int64_t* __restrict__ 
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < e) {
-                    const double wu = (cd[u] & kCodeSign) ? -wv[u] : wv[u];
-                    if (u & 1) acc1 = fma(wu, xv[u], acc1);
-                    else acc0 = fma(wu, xv[u], acc0);
+                    if (u & 1) acc1 = fma(signed_w(wv[u], cd[u]), xv[u], acc1);
+                    else acc0 = fma(signed_w(wv[u], cd[u]), xv[u], acc0);
                 }
             }
         }
@@ -367,14 +378,29 @@ __global__ void __launch_bounds__(kBT) k_bdot2(const double* __restrict__ v, con
     reduce_per_problem(c, red, BP, B, part + (int64_t)blockIdx.x * B, sq, 1);
 }
 
-// out[q][p] = sum over blocks of part[q][blk][p] for q < Q
-__global__ void k_bsum(const double* __restrict__ part, int nb, int B, int Q, double* __restrict__ out)
+// out[q][p] = sum over blocks of part[q][blk][p] for q < Q (t = q*B + p):
+// 32 consecutive t per CTA, its 8 warps split the block range, and the
+// partial sums are combined in a fixed order.  With mask given, out[t] is
+// written only where mask[p] != 0.
+__global__ void __launch_bounds__(256) k_bsum(const double* __restrict__ part, int nb, int B, int Q,
+                                              double* __restrict__ out, const int* __restrict__ mask)
 {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < Q * B; t += gridDim.x * blockDim.x) {
+    __shared__ double red[8][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int t = blockIdx.x * 32 + lane;
+    double s = 0.0;
+    if (t < Q * B) {
         const int q = t / B, p = t - q * B;
-        double s = 0.0;
-        for (int blk = 0; blk < nb; ++blk) s += part[((int64_t)q * nb + blk) * B + p];
-        out[t] = s;
+        const double* src = part + (int64_t)q * nb * B + p;
+        for (int blk = warp; blk < nb; blk += 8) s += src[(int64_t)blk * B];
+    }
+    red[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && t < Q * B) {
+        double tot = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) tot += red[w][lane];
+        if (!mask || mask[t % B]) out[t] = tot;
     }
 }
 
@@ -419,7 +445,8 @@ __global__ void __launch_bounds__(kBT) k_bmdot(const double* __restrict__ V, int
     }
 }
 
-// w_p -= sum_i c[i][p] V_i,p ; npart[blk][p] = |w_p|^2
+// w_p -= sum_i c[i][p] V_i,p ; npart[blk][p] = |w_p|^2.  Problems with
+// need[p] == 0 (when need is given) are left alone and contribute zeros.
 __global__ void __launch_bounds__(kBT) k_bupdate(const double* __restrict__ V, int64_t n, int B, int BP, int J,
                                                  const double* __restrict__ c, double* __restrict__ w,
                                                  double* __restrict__ npart, const int* __restrict__ need)
@@ -430,12 +457,10 @@ __global__ void __launch_bounds__(kBT) k_bupdate(const double* __restrict__ V, i
     const int p = threadIdx.x % BP, rl = threadIdx.x / BP, nrl = kBT / BP;
     const int64_t vs = n * (int64_t)B;
     double nn = 0.0;
-    if (p < B) {
-        const bool act = !need || need[p];
+    if (p < B && (!need || need[p])) {
         for (int64_t r = r0 + rl; r < r1; r += nrl) {
             double acc = w[r * B + p];
-            if (act)
-                for (int i = 0; i < J; ++i) acc = fma(-c[i * B + p], V[i * vs + r * B + p], acc);
+            for (int i = 0; i < J; ++i) acc = fma(-c[i * B + p], V[i * vs + r * B + p], acc);
             w[r * B + p] = acc;
             nn = fma(acc, acc, nn);
         }
@@ -496,22 +521,22 @@ __global__ void k_bscale(double* __restrict__ w, int64_t n, int B, const double*
     }
 }
 
-// out_i,p = sum_j V_j,p Y_p[j][i] for i < k (Y per problem, [p][i][j] = column i)
+// out_i,p = sum_j V_j,p Y[i][j][p] for i < k: Y holds the Ritz coefficients
+// with the problem index fastest, so a warp's lanes (consecutive problems)
+// read them coalesced.
 __global__ void k_bgemm(const double* __restrict__ V, int64_t n, int B, int m, const double* __restrict__ Y, int k,
                         double* __restrict__ out)
 {
     const int64_t vs = n * (int64_t)B;
-    const int64_t total = n * (int64_t)B;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < vs; t += (int64_t)gridDim.x * blockDim.x) {
         const int p = (int)(t % B);
-        const double* Yp = Y + (size_t)p * m * m;
         for (int i0 = 0; i0 < k; i0 += 8) {
             double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             for (int j = 0; j < m; ++j) {
                 const double v = V[j * vs + t];
 #pragma unroll
                 for (int q = 0; q < 8; ++q)
-                    if (i0 + q < k) acc[q] = fma(v, Yp[(size_t)(i0 + q) * m + j], acc[q]);
+                    if (i0 + q < k) acc[q] = fma(v, __ldg(Y + ((size_t)(i0 + q) * m + j) * B + p), acc[q]);
             }
             for (int q = 0; q < 8 && i0 + q < k; ++q) out[(i0 + q) * vs + t] = acc[q];
         }
@@ -626,103 +651,141 @@ void batch_create(ed_batch& bt, const ed_basis& basis, int K, int B, const uint1
 
 namespace {
 
-template <int TB, int U>
-void launch_bspmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
+constexpr size_t kSmemOptIn = 227 * 1024;   // dynamic shared memory per CTA on sm_103a
+
+template <int TB, int U, int NT>
+void launch_bspmm(const ed_batch& bt, const double* X, double* Y, int64_t rows, cudaStream_t st)
 {
     const size_t smem = (size_t)bt.nhop * TB * 8;
     static_assert(U <= kCrsPad, "batch overruns the padding");
-    if (smem > 48 * 1024) ED_CUDA(cudaFuncSetAttribute(k_bspmm<TB, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((unsigned)(sms_b() * 2), (unsigned)((bt.B + TB - 1) / TB));
-    k_bspmm<TB, U><<<grid, 256, smem, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.nhop, bt.diag.p, X, Y, bt.n,
-                                            bt.B);
+    ED_REQUIRE(smem <= kSmemOptIn, ED_ERR_RANGE, "hop table tile exceeds shared memory");
+    if (smem > 48 * 1024)
+        ED_CUDA(cudaFuncSetAttribute(k_bspmm<TB, U, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1;
+    ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bspmm<TB, U, NT>, NT, smem));
+    dim3 grid((unsigned)(sms_b() * std::max(1, per_sm)), (unsigned)((bt.B + TB - 1) / TB));
+    k_bspmm<TB, U, NT><<<grid, NT, smem, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.nhop, bt.diag.p, X, Y,
+                                                 rows, bt.B);
     count_launch();
     ED_CUDA(cudaGetLastError());
 }
 
 template <int U, int TB>
-void launch_bspmm_warp(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
+void launch_bspmm_warp(const ed_batch& bt, const double* X, double* Y, int64_t rows, cudaStream_t st)
 {
     static_assert(U <= kCrsPad, "batch overruns the padding");
     dim3 grid((unsigned)(sms_b() * 8), (unsigned)((bt.B + TB - 1) / TB));
-    k_bspmm_warp<U, TB><<<grid, 256, 0, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.diag.p, X, Y, bt.n, bt.B);
+    k_bspmm_warp<U, TB><<<grid, 256, 0, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.diag.p, X, Y, rows, bt.B);
     count_launch();
     ED_CUDA(cudaGetLastError());
 }
 
-// tb 4, 8: hop tables staged in shared memory; tb 16 (code 17), 32: read
-// through L1 by the TB-lanes-per-row kernel
-void bspmm_variant(const ed_batch& bt, int tb, int u, const double* X, double* Y, cudaStream_t st)
+// One block-product variant on rows [0, rows): l1 = 1 reads the hop values
+// through L1 (TB 16 or 32 lanes per row); l1 = 0 stages the tile's hop table
+// in shared memory (TB 4, 8 or 16 Hamiltonians, 256 or 1024 threads).
+void bspmm_variant(const ed_batch& bt, int tb, int u, int nt, int l1, const double* X, double* Y, int64_t rows,
+                   cudaStream_t st)
 {
-    if (tb == 32 && u == 4) launch_bspmm_warp<4, 32>(bt, X, Y, st);
-    else if (tb == 32) launch_bspmm_warp<8, 32>(bt, X, Y, st);
-    else if (tb == 17 && u == 4) launch_bspmm_warp<4, 16>(bt, X, Y, st);
-    else if (tb == 17) launch_bspmm_warp<8, 16>(bt, X, Y, st);
-    else if (tb == 4 && u == 4) launch_bspmm<4, 4>(bt, X, Y, st);
-    else if (tb == 4 && u == 8) launch_bspmm<4, 8>(bt, X, Y, st);
-    else if (tb == 8 && u == 4) launch_bspmm<8, 4>(bt, X, Y, st);
-    else if (tb == 8 && u == 8) launch_bspmm<8, 8>(bt, X, Y, st);
-    else if (tb == 16 && u == 4) launch_bspmm<16, 4>(bt, X, Y, st);
-    else launch_bspmm<16, 8>(bt, X, Y, st);
+    if (l1) {
+        if (tb == 32) u == 4 ? launch_bspmm_warp<4, 32>(bt, X, Y, rows, st) : launch_bspmm_warp<8, 32>(bt, X, Y, rows, st);
+        else u == 4 ? launch_bspmm_warp<4, 16>(bt, X, Y, rows, st) : launch_bspmm_warp<8, 16>(bt, X, Y, rows, st);
+        return;
+    }
+#define ED_BSPMM_CASE(TB_, U_, NT_)                                                   \
+    if (tb == TB_ && u == U_ && nt == NT_) {                                          \
+        launch_bspmm<TB_, U_, NT_>(bt, X, Y, rows, st);                               \
+        return;                                                                       \
+    }
+    ED_BSPMM_CASE(4, 4, 256) ED_BSPMM_CASE(4, 8, 256) ED_BSPMM_CASE(8, 4, 256) ED_BSPMM_CASE(8, 8, 256)
+    ED_BSPMM_CASE(16, 4, 256) ED_BSPMM_CASE(16, 8, 256)
+    ED_BSPMM_CASE(4, 4, 1024) ED_BSPMM_CASE(4, 8, 1024) ED_BSPMM_CASE(8, 4, 1024) ED_BSPMM_CASE(8, 8, 1024)
+    ED_BSPMM_CASE(16, 4, 1024) ED_BSPMM_CASE(16, 8, 1024)
+#undef ED_BSPMM_CASE
+    throw Error(ED_ERR_INTERNAL, "unknown block-product tile");
 }
 
 }  // namespace
 
 void batch_spmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
 {
-    bspmm_variant(bt, bt.tb, bt.unroll, X, Y, st);
+    bspmm_variant(bt, bt.tb, bt.unroll, bt.nt, bt.l1, X, Y, bt.n, st);
 }
 
-// Pick the (Hamiltonians per CTA, loads in flight) pair that runs the block
-// product fastest on this data; shared-memory capacity rules out tiles whose
-// hop tables do not fit.
-// Choices are remembered per (device, Hamiltonians, hop types, rows/4096,
-// nonzeros/2^16) so that the sectors of one sweep are tuned once.
+// Pick the block-product tile that runs fastest on this data, timed on the
+// first rows of the pattern (the rows of a sector are alike, and tuning stays
+// a small fraction of a solve); tiles whose hop tables do not fit in shared
+// memory are skipped.  Choices are remembered per (device, Hamiltonians, hop
+// types, mean row length) so that the sectors of one sweep are tuned once.
+// ED_TUNE_VERBOSE=1 prints every candidate's time to stderr.
 namespace {
 std::mutex g_tune_mu;
-std::map<std::vector<int64_t>, std::pair<int, int>> g_tune;
+std::map<std::vector<int64_t>, std::array<int, 4>> g_tune;
 }  // namespace
 
 void batch_autotune(ed_batch& bt, cudaStream_t st)
 {
     int dev = 0;
     ED_CUDA(cudaGetDevice(&dev));
-    const std::vector<int64_t> key{dev, bt.B, bt.nhop, bt.n >> 12, bt.nnz >> 16};
+    const int64_t mean_len = bt.n ? (bt.nnz + bt.n / 2) / bt.n : 0;
+    const std::vector<int64_t> key{dev, bt.B, bt.nhop, mean_len / 8};
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
-            bt.tb = it->second.first;
-            bt.unroll = it->second.second;
+            bt.tb = it->second[0];
+            bt.unroll = it->second[1];
+            bt.nt = it->second[2];
+            bt.l1 = it->second[3];
             return;
         }
     }
+    const char* verbose_env = std::getenv("ED_TUNE_VERBOSE");
+    const bool verbose = verbose_env && verbose_env[0] == '1';
+    const int64_t rows = std::min<int64_t>(bt.n, 65536);
     DevBuf<double> X((size_t)bt.n * bt.B), Y((size_t)bt.n * bt.B);
     k_brandom<<<sms_b() * 4, 256, 0, st>>>(X.p, bt.n * bt.B, 7); count_launch();
     cudaEvent_t a, b;
     ED_CUDA(cudaEventCreate(&a));
     ED_CUDA(cudaEventCreate(&b));
     float best = 1e30f;
-    int btb = 8, bu = 8;
-    for (int tb : {4, 8, 16, 17, 32}) {
-        if (tb <= 16 && (size_t)bt.nhop * tb * 8 > 200 * 1024) continue;
-        if (tb > 4 && bt.B <= tb / 2) continue;
+    std::array<int, 4> pick{32, 4, 256, 1};
+    std::vector<std::array<int, 4>> cands;
+    for (int tb : {4, 8, 16}) {
+        const size_t smem = (size_t)bt.nhop * tb * 8;
+        if (smem > kSmemOptIn || (tb > 4 && bt.B <= tb / 2)) continue;
         for (int u : {4, 8}) {
-            bspmm_variant(bt, tb, u, X.p, Y.p, st);
-            ED_CUDA(cudaEventRecord(a, st));
-            for (int r = 0; r < 3; ++r) bspmm_variant(bt, tb, u, X.p, Y.p, st);
-            ED_CUDA(cudaEventRecord(b, st));
-            ED_CUDA(cudaEventSynchronize(b));
-            float ms = 0.f;
-            ED_CUDA(cudaEventElapsedTime(&ms, a, b));
-            if (ms < best) { best = ms; btb = tb; bu = u; }
+            if (smem <= 110 * 1024) cands.push_back({tb, u, 256, 0});   // two or more CTAs per SM
+            if (smem > 56 * 1024) cands.push_back({tb, u, 1024, 0});    // one large CTA per SM
+        }
+    }
+    for (int tb : {16, 32}) {
+        if (bt.B <= tb / 2) continue;
+        for (int u : {4, 8}) cands.push_back({tb, u, 256, 1});
+    }
+    for (const auto& c : cands) {
+        bspmm_variant(bt, c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
+        ED_CUDA(cudaEventRecord(a, st));
+        for (int r = 0; r < 3; ++r) bspmm_variant(bt, c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
+        ED_CUDA(cudaEventRecord(b, st));
+        ED_CUDA(cudaEventSynchronize(b));
+        float ms = 0.f;
+        ED_CUDA(cudaEventElapsedTime(&ms, a, b));
+        if (verbose)
+            std::fprintf(stderr, "ed_batch tune: B=%d tb=%d unroll=%d threads=%d l1=%d rows=%lld  %.4f ms\n", bt.B, c[0],
+                         c[1], c[2], c[3], (long long)rows, ms / 3);
+        if (ms < best) {
+            best = ms;
+            pick = c;
         }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    bt.tb = btb;
-    bt.unroll = bu;
+    bt.tb = pick[0];
+    bt.unroll = pick[1];
+    bt.nt = pick[2];
+    bt.l1 = pick[3];
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tune[key] = {btb, bu};
+    g_tune[key] = pick;
 }
 
 // Lockstep thick-restart Lanczos for the B problems of a batch: the
@@ -732,8 +795,10 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
 // (their pairs stay converged) until every problem has its nev pairs.  A
 // Krylov breakdown, which needs an exactly invariant subspace, is reported
 // as ED_ERR_BREAKDOWN for the batch; such a problem is solved with ed_lanczos.
+// A restart cycle runs without host round trips and is replayed as a CUDA
+// graph on the solver's own stream.
 void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V0, double* evals, double* evecs,
-                 ed_batch_info* info, cudaStream_t st)
+                 ed_batch_info* info, cudaStream_t caller_stream)
 {
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t n = bt.n;
@@ -749,6 +814,8 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     int BP = 1;
     while (BP < B) BP <<= 1;
     ED_REQUIRE(BP <= kBT, ED_ERR_ARG, "at most 256 problems per batch");
+    SolveStream ss(caller_stream);
+    cudaStream_t st = ss.s;
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 2, n / 256));
     const int64_t vs = n * (int64_t)B;
     DevBuf<double> V((size_t)vs * (m + 1)), V2((size_t)vs * (m + 1));
@@ -761,11 +828,14 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     DevBuf<double> Yd((size_t)B * m * m);
     ED_CUDA(cudaMemsetAsync(betas.p, 0, betas.bytes(), st));
     auto grid_for = [&](int64_t work) { return (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 8, (work + 255) / 256)); };
+    auto bsum = [&](const double* src, int Q, double* out, const int* mask) {
+        k_bsum<<<(unsigned)((Q * B + 31) / 32), 256, 0, st>>>(src, nb, B, Q, out, mask); count_launch();
+    };
     if (V0) ED_CUDA(cudaMemcpyAsync(V.p, V0, (size_t)vs * 8, cudaMemcpyDeviceToDevice, st));
     else { k_brandom<<<grid_for(vs), 256, 0, st>>>(V.p, vs, p.seed); count_launch(); }
     {   // normalise every start vector, rejecting zero or non-finite ones
         k_bdot2<<<nb, kBT, 0, st>>>(V.p, V.p, n, B, BP, part.p); count_launch();
-        k_bsum<<<1, 256, 0, st>>>(part.p, nb, B, 1, s2.p); count_launch();
+        bsum(part.p, 1, s2.p, nullptr);
         std::vector<double> nn(B);
         ED_CUDA(cudaMemcpyAsync(nn.data(), s2.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
         ED_CUDA(cudaStreamSynchronize(st));
@@ -778,9 +848,10 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     }
     ed_batch_info inf;
     std::memset(&inf, 0, sizeof(inf));
-    inf.tile_hamiltonians = bt.tb == 17 ? 16 : bt.tb;
-    inf.tile_l1 = bt.tb >= 17 ? 1 : 0;
+    inf.tile_hamiltonians = bt.tb;
+    inf.tile_l1 = bt.l1;
     inf.tile_unroll = bt.unroll;
+    inf.tile_threads = bt.l1 ? 256 : bt.nt;
     std::vector<std::vector<double>> T(B, std::vector<double>((size_t)m * m, 0.0)), theta(B), Y(B);
     std::vector<double> coef_h((size_t)m * (m + 1) * B), beta_h((size_t)(m + 1) * B), Yall((size_t)B * m * m);
     std::vector<int> brk_h(B);
@@ -790,25 +861,30 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
         std::vector<cudaEvent_t>& v;
         ~EvG() { for (auto e : v) if (e) cudaEventDestroy(e); }
     } evg{ev};
-    double spmm_ms = 0.0;
-    bool converged = false;
-    int k = 0;
-    for (;;) {
+    // Ritz coefficients of every problem, [i][j][p] (problem fastest)
+    auto pack_Y = [&]() {
+        for (int b = 0; b < B; ++b)
+            for (int i = 0; i < m; ++i)
+                for (int j = 0; j < m; ++j) Yall[((size_t)i * m + j) * B + b] = Y[b][(size_t)j + (size_t)m * i];
+        ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), Yall.size() * 8, cudaMemcpyHostToDevice, st));
+    };
+
+    auto enqueue_cycle = [&](int k, bool capturing) {
         ED_CUDA(cudaMemsetAsync(coef.p, 0, coef.bytes(), st));
         ED_CUDA(cudaMemsetAsync(brk.p, 0, (size_t)B * 4, st));
-        float cycle_ms = 0.f;
         for (int j = k; j < m; ++j) {
             double* vj = V.p + (int64_t)j * vs;
             double* w = V.p + (int64_t)(j + 1) * vs;
             double* cj = coef.p + (size_t)j * (m + 1) * B;
             const bool first = (j == k);
-            ED_CUDA(cudaEventRecord(ev[2 * j], st));
+            if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j], st, cudaEventRecordExternal));
+            else ED_CUDA(cudaEventRecord(ev[2 * j], st));
             batch_spmm(bt, vj, w, st);
-            ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
-            ++inf.block_products;
+            if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j + 1], st, cudaEventRecordExternal));
+            else ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
             if (!first) {
                 k_bdot2<<<nb, kBT, 0, st>>>(vj, w, n, B, BP, part.p); count_launch();
-                k_bsum<<<1, 256, 0, st>>>(part.p, nb, B, 2, s2.p); count_launch();
+                bsum(part.p, 2, s2.p, nullptr);
                 k_blocal<<<1, 256, 0, st>>>(cj, s2.p, betas.p + (size_t)(j - 1) * B, j, B); count_launch();
                 k_baxpy2<<<grid_for(vs), 256, 0, st>>>(w, vj, V.p + (int64_t)(j - 1) * vs, n, B, s2.p,
                                                        betas.p + (size_t)(j - 1) * B); count_launch();
@@ -817,10 +893,11 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
             for (int pass = 0; pass < 2; ++pass) {
                 const int* mask = pass == 0 ? nullptr : need2.p;
                 k_bmdot<<<nb, kBT, 0, st>>>(V.p, n, B, BP, J, w, part.p, mask); count_launch();
-                k_bsum<<<grid_for((int64_t)(J + 1) * B), 256, 0, st>>>(part.p, nb, B, J + 1, sc.p); count_launch();
+                bsum(part.p, J + 1, sc.p, nullptr);
                 k_bupdate<<<nb, kBT, 0, st>>>(V.p, n, B, BP, J, sc.p, w, npart.p, mask); count_launch();
                 k_bacc<<<grid_for((int64_t)J * B), 256, 0, st>>>(cj, sc.p, J, B, mask); count_launch();
-                k_bsum<<<1, 256, 0, st>>>(npart.p, nb, B, 1, s2.p + 3 * B); count_launch();
+                // the norm after the pass, kept from pass 1 for problems that skip pass 2
+                bsum(npart.p, 1, s2.p + 3 * B, mask);
                 if (pass == 0) {
                     k_bneed<<<1, 256, 0, st>>>(s2.p + 3 * B, sc.p + (size_t)J * B, B, first ? 1 : 0, need2.p);
                     count_launch();
@@ -833,6 +910,42 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
             k_bscale<<<grid_for(vs), 256, 0, st>>>(w, n, B, betas.p + (size_t)j * B); count_launch();
             ED_CUDA(cudaGetLastError());
         }
+    };
+    CycleGraphs cache;
+    auto run_cycle = [&](int k) {
+        CycleGraphs::Entry* g = cache.find(k, V.p);
+        if (!g) {
+            const uint64_t c0 = launch_count();
+            ED_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            try {
+                enqueue_cycle(k, true);
+            } catch (...) {
+                cudaGraph_t broken = nullptr;
+                cudaStreamEndCapture(st, &broken);
+                if (broken) cudaGraphDestroy(broken);
+                throw;
+            }
+            cudaGraph_t graph = nullptr;
+            ED_CUDA(cudaStreamEndCapture(st, &graph));
+            const int64_t kernels = (int64_t)(launch_count() - c0);
+            count_launches(-kernels);
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            ED_CUDA(e);
+            cache.e.push_back({k, V.p, exec, kernels});
+            g = &cache.e.back();
+        }
+        ED_CUDA(cudaGraphLaunch(g->exec, st));
+        count_launches(g->kernels);
+    };
+
+    double spmm_ms = 0.0;
+    bool converged = false;
+    int k = 0;
+    for (;;) {
+        run_cycle(k);
+        inf.block_products += m - k;
         ED_CUDA(cudaMemcpyAsync(coef_h.data(), coef.p, coef.bytes(), cudaMemcpyDeviceToHost, st));
         ED_CUDA(cudaMemcpyAsync(beta_h.data(), betas.p, beta_h.size() * 8, cudaMemcpyDeviceToHost, st));
         ED_CUDA(cudaMemcpyAsync(brk_h.data(), brk.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
@@ -840,9 +953,8 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
         for (int j = k; j < m; ++j) {
             float ms = 0.f;
             ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * j], ev[2 * j + 1]));
-            cycle_ms += ms;
+            spmm_ms += ms;
         }
-        spmm_ms += cycle_ms;
         int nconv = 0;
         double maxres = 0.0;
         for (int b = 0; b < B; ++b) {
@@ -879,8 +991,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
         ++inf.restarts;
         int kk = std::min(m - 2, nev + std::max(1, (m - nev) / 2));
         kk = std::max(kk, std::min(nev, m - 1));
-        for (int b = 0; b < B; ++b) std::memcpy(&Yall[(size_t)b * m * m], Y[b].data(), (size_t)m * m * 8);
-        ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), Yall.size() * 8, cudaMemcpyHostToDevice, st));
+        pack_Y();
         k_bgemm<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, m, Yd.p, kk, V2.p); count_launch();
         ED_CUDA(cudaMemcpyAsync(V2.p + (int64_t)kk * vs, V.p + (int64_t)m * vs, (size_t)vs * 8, cudaMemcpyDeviceToDevice,
                                 st));
@@ -908,8 +1019,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
         X = xtmp.p;
     }
     if (X) {
-        for (int b = 0; b < B; ++b) std::memcpy(&Yall[(size_t)b * m * m], Y[b].data(), (size_t)m * m * 8);
-        ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), Yall.size() * 8, cudaMemcpyHostToDevice, st));
+        pack_Y();
         k_bgemm<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, m, Yd.p, nev, X); count_launch();
     }
     if (p.verify && X) {
@@ -925,7 +1035,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
             batch_spmm(bt, X + (int64_t)i * vs, ytmp.p, st);
             ++inf.block_products;
             k_bresid<<<nb, kBT, 0, st>>>(ytmp.p, X + (int64_t)i * vs, n, B, BP, dl.p, part.p); count_launch();
-            k_bsum<<<1, 256, 0, st>>>(part.p, nb, B, 1, s2.p); count_launch();
+            bsum(part.p, 1, s2.p, nullptr);
             ED_CUDA(cudaMemcpyAsync(res.data(), s2.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
             ED_CUDA(cudaStreamSynchronize(st));
             for (int b = 0; b < B; ++b) {

@@ -42,6 +42,7 @@ namespace {
 std::atomic<uint64_t> g_launches{0};
 }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(int64_t d) { g_launches.fetch_add((uint64_t)d, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 void terms_upload(ed_terms& t)

@@ -31,6 +31,9 @@ struct Error : std::runtime_error {
 void set_last_error(const std::string& msg);
 // Number of kernels this library has launched (all devices, all threads).
 void count_launch();
+// Adds d (may be negative): kernels recorded into a CUDA graph are counted
+// when the graph is launched, not when they are captured.
+void count_launches(int64_t d);
 uint64_t launch_count();
 
 #define ED_CUDA(x)                                                                            \

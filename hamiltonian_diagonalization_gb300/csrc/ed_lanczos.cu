@@ -18,6 +18,12 @@
 //   always on the first step of a cycle, where the thick-restart arrow makes
 //   the local step inapplicable;
 //   beta_j = ||w|| ; v_{j+1} = w / beta_j.
+// Kernels per step: the product, k_local_dot (alpha, ||H v_j||), k_mdot with
+// the three-term step folded into its staging, k_update, the gated second
+// k_mdot/k_update pair (an early return when the DGKS test passed) and
+// k_scale.  Each reduction is finished by the last block of its own launch.
+// Every decision (second pass, breakdown) is a device flag, so a whole cycle
+// is enqueued without host round trips and replayed as a CUDA graph.
 // After m steps the m x m projected matrix is diagonalised on the host, the
 // residual of Ritz pair i is |beta_{m-1} y_{m-1,i}|, and the cycle restarts
 // from the k lowest Ritz vectors plus v_m (Wu & Simon's thick restart).
@@ -34,7 +40,6 @@ namespace edgb {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kJT = 8;               // columns per tile in the multi-dot
 constexpr double kDgksEta = 0.7071067811865476;
 
 int sm_count()
@@ -70,11 +75,39 @@ __device__ __forceinline__ void chunk(int64_t n, int nb, int b, int64_t& r0, int
     r1 = n * (int64_t)(b + 1) / nb;
 }
 
+// Completion of a reduction launch without a second kernel: every block calls
+// this after writing its partials; it returns true in exactly one block, the
+// last one to arrive, which then sees every block's partials.  That block
+// resets the counter for the next launch.  Nothing waits, so no block can
+// stall on another.
+__device__ __forceinline__ bool last_block(unsigned int* counter)
+{
+    __shared__ unsigned int ticket;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
+    __syncthreads();
+    const bool last = ticket == gridDim.x - 1;
+    if (last) {
+        __threadfence();
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+    return last;
+}
+
+// Sum of nb partials in a fixed order (thread-strided, then block_sum), so
+// the result does not depend on which block finished last; in thread 0.
+__device__ __forceinline__ double sum_parts(const double* p, int nb, double* red)
+{
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += kThreads) s += __ldcg(p + i);
+    return block_sum(s, red);
+}
+
 // part[0*nb+b] = sum x.y, part[1*nb+b] = sum y.y over block b's rows.
 __global__ void __launch_bounds__(kThreads) k_dot2(const double* __restrict__ x, const double* __restrict__ y,
-                                                   int64_t n, double* __restrict__ part, const int* __restrict__ stop)
+                                                   int64_t n, double* __restrict__ part)
 {
-    if (stop && *stop) return;
     __shared__ double red[kThreads / 32];
     int64_t r0, r1;
     chunk(n, gridDim.x, blockIdx.x, r0, r1);
@@ -92,18 +125,34 @@ __global__ void __launch_bounds__(kThreads) k_dot2(const double* __restrict__ x,
     }
 }
 
-// Local step scalars: alpha = sum part[0..nb) (column j's diagonal),
-// ||H v_j||^2 = sum part[nb..2nb); beta_{j-1} enters column j at row j-1.
-__global__ void k_local_finalize(const double* __restrict__ part, int nb, double* __restrict__ coefcol, int j,
-                                 const double* __restrict__ beta_prev, double* __restrict__ hvnorm2,
-                                 const int* __restrict__ stop)
+// Local step scalars of step j (w = H v_j): alpha = v_j.w goes to column j's
+// diagonal, beta_{j-1} to row j-1 of column j, and ||H v_j||^2 to *hvnorm2,
+// all written by the last block from the per-block partials.
+__global__ void __launch_bounds__(kThreads) k_local_dot(const double* __restrict__ vj, const double* __restrict__ w,
+                                                        int64_t n, double* __restrict__ part,
+                                                        unsigned int* __restrict__ counter, double* __restrict__ coefcol,
+                                                        int j, const double* __restrict__ beta_prev,
+                                                        double* __restrict__ hvnorm2, const int* __restrict__ stop)
 {
-    if (stop && *stop) return;
+    if (*stop) return;
     __shared__ double red[kThreads / 32];
+    int64_t r0, r1;
+    chunk(n, gridDim.x, blockIdx.x, r0, r1);
     double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < nb; i += kThreads) { a += part[i]; b += part[nb + i]; }
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+        const double wr = w[r];
+        a = fma(vj[r], wr, a);
+        b = fma(wr, wr, b);
+    }
     a = block_sum(a, red);
     b = block_sum(b, red);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = a;
+        part[gridDim.x + blockIdx.x] = b;
+    }
+    if (!last_block(counter)) return;
+    a = sum_parts(part, gridDim.x, red);
+    b = sum_parts(part + gridDim.x, gridDim.x, red);
     if (threadIdx.x == 0) {
         coefcol[j] = a;
         coefcol[j - 1] = *beta_prev;
@@ -111,34 +160,38 @@ __global__ void k_local_finalize(const double* __restrict__ part, int nb, double
     }
 }
 
-// w -= alpha v_j + beta_{j-1} v_{j-1}
-__global__ void __launch_bounds__(kThreads) k_axpy2(double* __restrict__ w, const double* __restrict__ vj,
-                                                    const double* __restrict__ vjm1, int64_t n,
-                                                    const double* __restrict__ alpha, const double* __restrict__ beta,
-                                                    const int* __restrict__ stop)
-{
-    if (stop && *stop) return;
-    const double a = *alpha, b = *beta;
-    for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads)
-        w[r] = fma(-b, vjm1[r], fma(-a, vj[r], w[r]));
-}
-
-// Multi-dot: part[i*nb + b] = V[:,i].w over rows [b*kMdotRows, ...) for
-// i < J, and part[J*nb + b] = w.w; nb = ceil(n / kMdotRows) blocks.  The
-// block's slice of w is staged in shared memory once; warps then take the
-// columns in turn, each streaming its column slice coalesced with four
-// independent FMA chains (one FP64 FMA per element plus a 5-step shuffle per
-// column and block).  run == nullptr or *run != 0 to execute.
-constexpr int kMdotRows = 4096;
-__global__ void __launch_bounds__(kThreads) k_mdot(const double* __restrict__ V, int64_t n, int J,
-                                                   const double* __restrict__ w, double* __restrict__ part,
+// Multi-dot against the Krylov basis, R rows per block (R doubles of dynamic
+// shared memory hold the block's slice of w): part[i*nb + b] = V[:,i].w for
+// i < J and part[J*nb + b] = w.w.  With local != 0 the three-term step
+// w -= alpha v_{J-1} + beta v_{J-2} is applied to the slice while it is staged
+// and written back, so the pass sees the locally orthogonalised w.  Warps take
+// the columns in turn, each streaming its column slice coalesced with four
+// independent FMA chains.  The last block sums the partials column by column:
+// c[i] for i < J (also added to coefcol[i] when coefcol is given) and
+// *before = w.w.  Runs when run is null or *run != 0, and stop is clear.
+__global__ void __launch_bounds__(kThreads) k_mdot(const double* __restrict__ V, int64_t n, int R, int J,
+                                                   double* __restrict__ w, int local, const double* __restrict__ alpha,
+                                                   const double* __restrict__ beta_prev, double* __restrict__ part,
+                                                   unsigned int* __restrict__ counter, double* __restrict__ c,
+                                                   double* __restrict__ coefcol, double* __restrict__ before,
                                                    const int* __restrict__ run, const int* __restrict__ stop)
 {
     if ((run && !*run) || (stop && *stop)) return;
-    __shared__ double sw[kMdotRows];
-    const int64_t r0 = (int64_t)blockIdx.x * kMdotRows;
-    const int len = (int)min((int64_t)kMdotRows, n - r0);
-    for (int i = threadIdx.x; i < len; i += kThreads) sw[i] = w[r0 + i];
+    extern __shared__ double sw[];
+    const int64_t r0 = (int64_t)blockIdx.x * R;
+    const int len = (int)min((int64_t)R, n - r0);
+    if (local) {
+        const double a = *alpha, b = *beta_prev;
+        const double* vj = V + (int64_t)(J - 1) * n + r0;
+        const double* vjm1 = V + (int64_t)(J - 2) * n + r0;
+        for (int i = threadIdx.x; i < len; i += kThreads) {
+            const double x = fma(-b, vjm1[i], fma(-a, vj[i], w[r0 + i]));
+            w[r0 + i] = x;
+            sw[i] = x;
+        }
+    } else {
+        for (int i = threadIdx.x; i < len; i += kThreads) sw[i] = w[r0 + i];
+    }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nb = gridDim.x;
@@ -162,26 +215,16 @@ __global__ void __launch_bounds__(kThreads) k_mdot(const double* __restrict__ V,
         for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) part[(int64_t)i * nb + blockIdx.x] = s;
     }
-}
-
-// c[i] = sum_b part[i*nb+b] for i < J, coefcol[i] += c[i]; norm2 before the
-// pass (index J) to *before.
-__global__ void k_mdot_finalize(const double* __restrict__ part, int nb, int J, double* __restrict__ c,
-                                double* __restrict__ coefcol, double* __restrict__ before,
-                                const int* __restrict__ run, const int* __restrict__ stop)
-{
-    if ((run && !*run) || (stop && *stop)) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarp = blockDim.x >> 5;
-    for (int i = warp; i <= J; i += nwarp) {
+    if (!last_block(counter)) return;
+    for (int i = warp; i <= J; i += kThreads / 32) {
         double s = 0.0;
-        for (int b = lane; b < nb; b += 32) s += part[(int64_t)i * nb + b];
+        for (int b = lane; b < nb; b += 32) s += __ldcg(part + (int64_t)i * nb + b);
 #pragma unroll
         for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) {
             if (i < J) {
                 c[i] = s;
-                coefcol[i] += s;
+                if (coefcol) coefcol[i] += s;
             } else {
                 *before = s;
             }
@@ -189,11 +232,21 @@ __global__ void k_mdot_finalize(const double* __restrict__ part, int nb, int J, 
     }
 }
 
-// w -= V[:,0..J) c ; npart[b] = ||w||^2 over block b's rows.
+// w -= V[:,0..J) c and a per-block partial of ||w||^2.  The last block then
+// finishes the pass:
+//   mode 1 (first pass): *need2 = force2 or ||w||^2 < eta^2 *before (the
+//          DGKS test); without a second pass also beta and the breakdown test;
+//   mode 2 (second pass): beta and the breakdown test;
+//   mode 0: nothing (the counter is not touched).
+// beta = ||w||; breakdown (stop = j + 1) when beta <= 1e-12 sqrt(*ref2), the
+// new direction having vanished relative to ||H v_j||.
 __global__ void __launch_bounds__(kThreads) k_update(const double* __restrict__ V, int64_t n, int J,
                                                      const double* __restrict__ c, double* __restrict__ w,
-                                                     double* __restrict__ npart, const int* __restrict__ run,
-                                                     const int* __restrict__ stop)
+                                                     double* __restrict__ npart, unsigned int* __restrict__ counter,
+                                                     int mode, int force2, const double* __restrict__ before,
+                                                     int* __restrict__ need2, double* __restrict__ beta,
+                                                     const double* __restrict__ ref2, int j,
+                                                     const int* __restrict__ run, int* __restrict__ stop)
 {
     if ((run && !*run) || (stop && *stop)) return;
     extern __shared__ double sc[];
@@ -220,32 +273,21 @@ __global__ void __launch_bounds__(kThreads) k_update(const double* __restrict__ 
     }
     nn = block_sum(nn, red);
     if (threadIdx.x == 0) npart[blockIdx.x] = nn;
-}
-
-// beta = ||w|| after a pass.  With need2 != nullptr (first pass) also set
-// the second-pass flag: forced, or the DGKS test ||w_after|| < eta ||w_before||.
-__global__ void k_norm_finalize(const double* __restrict__ npart, int nb, const double* __restrict__ before,
-                                double* __restrict__ beta, int* __restrict__ need2, int force2,
-                                const int* __restrict__ run, const int* __restrict__ stop)
-{
-    if ((run && !*run) || (stop && *stop)) return;
-    __shared__ double red[kThreads / 32];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < nb; i += kThreads) s += npart[i];
-    s = block_sum(s, red);
+    if (mode == 0 || !last_block(counter)) return;
+    const double s = sum_parts(npart, gridDim.x, red);
     if (threadIdx.x == 0) {
-        *beta = sqrt(s);
-        if (need2) *need2 = (force2 || s < kDgksEta * kDgksEta * (*before)) ? 1 : 0;
+        bool finish = true;
+        if (mode == 1) {
+            const int again = (force2 || s < kDgksEta * kDgksEta * (*before)) ? 1 : 0;
+            *need2 = again;
+            finish = !again;
+        }
+        if (finish) {
+            const double b = sqrt(s);
+            *beta = b;
+            if (!(b > 1e-12 * sqrt(fmax(*ref2, 0.0)))) *stop = j + 1;
+        }
     }
-}
-
-// Invariant subspace: the new direction vanished relative to ||H v_j||.
-__global__ void k_break_test(const double* __restrict__ beta, const double* __restrict__ ref2,
-                             int* __restrict__ stop, int j)
-{
-    if (*stop) return;
-    const double ref = sqrt(fmax(*ref2, 0.0));
-    if (!(*beta > 1e-12 * ref)) *stop = j + 1;
 }
 
 __global__ void __launch_bounds__(kThreads) k_scale(double* __restrict__ w, int64_t n,
@@ -347,9 +389,10 @@ struct Work {
     int64_t n = 0;
     int m = 0;
     int nb = 0;                      // blocks of the row-chunked reductions
-    int nbm = 0;                     // blocks of the multi-dot (kMdotRows rows each)
+    int R = 0;                       // rows per multi-dot block
+    int nbm = 0;                     // blocks of the multi-dot
     DevBuf<double> V, V2;            // n x (m+1), column-major
-    DevBuf<double> part;             // (m+2) * nb
+    DevBuf<double> part;             // (m+2) * max(nb, nbm)
     DevBuf<double> npart;            // nb
     DevBuf<double> coef;             // (m+1) x (m+1); column j holds step j's projections
     DevBuf<double> beta;             // m+2
@@ -357,17 +400,32 @@ struct Work {
     DevBuf<double> junk;             // m+2, coefficient sink for host-side orthonormalisation
     DevBuf<double> scal;             // [0] ||w||^2 before pass 1, [1] ||H v_j||^2, [2] before pass 2
     DevBuf<int> flags;               // [0] second pass wanted, [1] breakdown step + 1
+    DevBuf<unsigned int> counters;   // last-block counters: [0] local dot, [1] multi-dot, [2] update
     DevBuf<double> Y;                // m x m Ritz coefficients
+
+    void mdot(const double* Vb, int J, double* x, int local, const double* alpha, const double* beta_prev,
+              double* coefcol, double* before, const int* run, const int* stop, cudaStream_t st)
+    {
+        k_mdot<<<nbm, kThreads, (size_t)R * 8, st>>>(Vb, n, R, J, x, local, alpha, beta_prev, part.p,
+                                                      counters.p + 1, c.p, coefcol, before, run, stop);
+        ::edgb::count_launch();
+    }
+    void update(const double* Vb, int J, double* x, int mode, int force2, const double* before, int* need2,
+                double* b, const double* ref2, int j, const int* run, int* stop, cudaStream_t st)
+    {
+        k_update<<<nb, kThreads, (size_t)J * 8, st>>>(Vb, n, J, c.p, x, npart.p, counters.p + 2, mode, force2,
+                                                       before, need2, b, ref2, j, run, stop);
+        ::edgb::count_launch();
+    }
 };
 
-double host_sum_parts(Work& w, const double* dev, int count, cudaStream_t st)
+double host_sum_parts(const double* dev, int count, cudaStream_t st)
 {
     std::vector<double> h(count);
     ED_CUDA(cudaMemcpyAsync(h.data(), dev, (size_t)count * 8, cudaMemcpyDeviceToHost, st));
     ED_CUDA(cudaStreamSynchronize(st));
     double s = 0.0;
     for (int i = 0; i < count; ++i) s += h[i];
-    (void)w;
     return s;
 }
 
@@ -378,15 +436,14 @@ double orthonormalise_column(Work& w, double* Vbase, int col, cudaStream_t st)
     double* x = Vbase + (int64_t)col * w.n;
     if (col > 0) {
         for (int pass = 0; pass < 2; ++pass) {
-            k_mdot<<<w.nbm, kThreads, 0, st>>>(Vbase, w.n, col, x, w.part.p, nullptr, nullptr); ::edgb::count_launch();
-            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nbm, col, w.c.p, w.junk.p, w.scal.p + 3, nullptr, nullptr); ::edgb::count_launch();
-            k_update<<<w.nb, kThreads, (size_t)col * 8, st>>>(Vbase, w.n, col, w.c.p, x, w.npart.p, nullptr, nullptr); ::edgb::count_launch();
+            w.mdot(Vbase, col, x, 0, nullptr, nullptr, w.junk.p, w.scal.p + 3, nullptr, nullptr, st);
+            w.update(Vbase, col, x, 0, 0, nullptr, nullptr, nullptr, nullptr, 0, nullptr, nullptr, st);
             ED_CUDA(cudaGetLastError());
         }
     }
-    k_dot2<<<w.nb, kThreads, 0, st>>>(x, x, w.n, w.part.p, nullptr); ::edgb::count_launch();
+    k_dot2<<<w.nb, kThreads, 0, st>>>(x, x, w.n, w.part.p); ::edgb::count_launch();
     ED_CUDA(cudaGetLastError());
-    const double nrm = std::sqrt(host_sum_parts(w, w.part.p, w.nb, st));
+    const double nrm = std::sqrt(host_sum_parts(w.part.p, w.nb, st));
     ED_REQUIRE(nrm > 0.0 && std::isfinite(nrm), ED_ERR_ARG, "start vector is zero or not finite");
     ED_CUDA(cudaMemcpyAsync(w.beta.p + w.m + 1, &nrm, 8, cudaMemcpyHostToDevice, st));
     k_scale<<<w.nb, kThreads, 0, st>>>(x, w.n, w.beta.p + w.m + 1, nullptr); ::edgb::count_launch();
@@ -454,7 +511,7 @@ void residual_norms(const ed_op& op, const double* x, const double* lambda, int 
 }
 
 void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
-                   double* evecs_dev, ed_solve_info* info, cudaStream_t st)
+                   double* evecs_dev, ed_solve_info* info, cudaStream_t caller_stream)
 {
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t n = op.n;
@@ -465,12 +522,15 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     const int max_restarts = p.max_restarts > 0 ? p.max_restarts : 2000;
     ed_solve_info inf;
     std::memset(&inf, 0, sizeof(inf));
+    SolveStream ss(caller_stream);
+    cudaStream_t st = ss.s;
+    const int nsm = sm_count();
 
     if (v0_dev) {
         // a start vector must be finite and nonzero on every path
-        const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
+        const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(nsm * 2, n / 2048));
         DevBuf<double> part(2 * (size_t)nb);
-        k_dot2<<<nb, kThreads, 0, st>>>(v0_dev, v0_dev, n, part.p, nullptr); ::edgb::count_launch();
+        k_dot2<<<nb, kThreads, 0, st>>>(v0_dev, v0_dev, n, part.p); ::edgb::count_launch();
         ED_CUDA(cudaGetLastError());
         std::vector<double> h(2 * (size_t)nb);
         ED_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -497,10 +557,12 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     Work w;
     w.n = n;
     w.m = m;
-    w.nb = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
+    w.nb = (int)std::max<int64_t>(1, std::min<int64_t>(nsm * 4, n / 1024));
+    // multi-dot slices: about two blocks per SM, 512..4096 rows (a multiple of 128)
+    w.R = (int)std::min<int64_t>(4096, std::max<int64_t>(512, ((n + 2 * nsm - 1) / (2 * nsm) + 127) / 128 * 128));
+    w.nbm = (int)((n + w.R - 1) / w.R);
     w.V.alloc((size_t)n * (m + 1));
     w.V2.alloc((size_t)n * (m + 1));
-    w.nbm = (int)((n + kMdotRows - 1) / kMdotRows);
     w.part.alloc((size_t)(m + 2) * std::max(w.nb, w.nbm));
     w.npart.alloc(w.nb);
     w.coef.alloc((size_t)(m + 1) * (m + 1));
@@ -509,13 +571,15 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     w.junk.alloc(m + 2);
     w.scal.alloc(4);
     w.flags.alloc(2);
+    w.counters.alloc(4);
     w.Y.alloc((size_t)m * m);
     ED_CUDA(cudaMemsetAsync(w.beta.p, 0, (m + 2) * 8, st));
     ED_CUDA(cudaMemsetAsync(w.junk.p, 0, (m + 2) * 8, st));
+    ED_CUDA(cudaMemsetAsync(w.counters.p, 0, 4 * sizeof(unsigned int), st));
 
     if (v0_dev) ED_CUDA(cudaMemcpyAsync(w.V.p, v0_dev, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
     else {
-        k_random<<<sm_count() * 4, kThreads, 0, st>>>(w.V.p, n, p.seed); ::edgb::count_launch();
+        k_random<<<nsm * 4, kThreads, 0, st>>>(w.V.p, n, p.seed); ::edgb::count_launch();
         ED_CUDA(cudaGetLastError());
     }
     orthonormalise_column(w, w.V.p, 0, st);
@@ -527,6 +591,76 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
         ~EvGuard() { for (auto e : v) if (e) cudaEventDestroy(e); }
     } evguard{ev};
 
+    // One restart cycle, steps k..m-1, all on the device: breakdown and the
+    // second Gram-Schmidt pass are flags that later kernels read, so the host
+    // enqueues a whole cycle without waiting, and (for device operators)
+    // replays it as one CUDA graph.
+    int* need2 = w.flags.p;
+    int* stop = w.flags.p + 1;
+    auto enqueue_cycle = [&](int k, bool capturing) {
+        ED_CUDA(cudaMemsetAsync(w.flags.p, 0, 2 * sizeof(int), st));
+        ED_CUDA(cudaMemsetAsync(w.coef.p + (size_t)k * (m + 1), 0, (size_t)(m - k) * (m + 1) * 8, st));
+        for (int j = k; j < m; ++j) {
+            double* vj = w.V.p + (int64_t)j * n;
+            double* wv = w.V.p + (int64_t)(j + 1) * n;
+            double* coefcol = w.coef.p + (size_t)j * (m + 1);
+            const bool first = (j == k);
+            if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j], st, cudaEventRecordExternal));
+            else ED_CUDA(cudaEventRecord(ev[2 * j], st));
+            op_apply(op, vj, wv, st);
+            if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j + 1], st, cudaEventRecordExternal));
+            else ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
+            if (!first) {
+                k_local_dot<<<w.nb, kThreads, 0, st>>>(vj, wv, n, w.part.p, w.counters.p, coefcol, j,
+                                                       w.beta.p + (j - 1), w.scal.p + 1, stop); ::edgb::count_launch();
+            }
+            const int J = j + 1;
+            // pass 1 (with the three-term step on non-first steps), then the
+            // DGKS-gated pass 2; breakdown is judged against ||H v_j||
+            w.mdot(w.V.p, J, wv, first ? 0 : 1, coefcol + j, w.beta.p + (j - 1), coefcol, w.scal.p, nullptr, stop, st);
+            w.update(w.V.p, J, wv, 1, first ? 1 : 0, w.scal.p, need2, w.beta.p + j,
+                     first ? w.scal.p : w.scal.p + 1, j, nullptr, stop, st);
+            w.mdot(w.V.p, J, wv, 0, nullptr, nullptr, coefcol, w.scal.p + 2, need2, stop, st);
+            w.update(w.V.p, J, wv, 2, 0, nullptr, nullptr, w.beta.p + j, first ? w.scal.p : w.scal.p + 1, j, need2,
+                     stop, st);
+            k_scale<<<w.nb, kThreads, 0, st>>>(wv, n, w.beta.p + j, stop); ::edgb::count_launch();
+            ED_CUDA(cudaGetLastError());
+        }
+    };
+    const bool graphs = op.kind != ed_op::HOST;
+    CycleGraphs cache;
+    auto run_cycle = [&](int k) {
+        if (!graphs) {
+            enqueue_cycle(k, false);
+            return;
+        }
+        CycleGraphs::Entry* g = cache.find(k, w.V.p);
+        if (!g) {
+            const uint64_t c0 = launch_count();
+            ED_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            try {
+                enqueue_cycle(k, true);
+            } catch (...) {
+                cudaGraph_t broken = nullptr;
+                cudaStreamEndCapture(st, &broken);
+                if (broken) cudaGraphDestroy(broken);
+                throw;
+            }
+            cudaGraph_t graph = nullptr;
+            ED_CUDA(cudaStreamEndCapture(st, &graph));
+            const int64_t kernels = (int64_t)(launch_count() - c0);
+            count_launches(-kernels);
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            ED_CUDA(e);
+            cache.e.push_back({k, w.V.p, exec, kernels});
+            g = &cache.e.back();
+        }
+        ED_CUDA(cudaGraphLaunch(g->exec, st));
+        count_launches(g->kernels);
+    };
+
     std::vector<double> T((size_t)m * m, 0.0), coef_h((size_t)(m + 1) * (m + 1)), beta_h(m + 1);
     std::vector<double> theta, Y, prev_theta;
     int k = 0, m_eff = m;
@@ -534,41 +668,8 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     bool converged = false;
     double spmv_ms = 0.0;
     for (;;) {
-        ED_CUDA(cudaMemsetAsync(w.flags.p, 0, 2 * sizeof(int), st));
-        ED_CUDA(cudaMemsetAsync(w.coef.p + (size_t)k * (m + 1), 0, (size_t)(m - k) * (m + 1) * 8, st));
-        int* need2 = w.flags.p;
-        int* stop = w.flags.p + 1;
-        for (int j = k; j < m; ++j) {
-            double* vj = w.V.p + (int64_t)j * n;
-            double* wv = w.V.p + (int64_t)(j + 1) * n;
-            double* coefcol = w.coef.p + (size_t)j * (m + 1);
-            const bool first = (j == k);
-            ED_CUDA(cudaEventRecord(ev[2 * j], st));
-            op_apply(op, vj, wv, st);
-            ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
-            ++inf.matvecs;
-            if (!first) {
-                k_dot2<<<w.nb, kThreads, 0, st>>>(vj, wv, n, w.part.p, stop); ::edgb::count_launch();
-                k_local_finalize<<<1, kThreads, 0, st>>>(w.part.p, w.nb, coefcol, j, w.beta.p + (j - 1), w.scal.p + 1,
-                                                        stop); ::edgb::count_launch();
-                k_axpy2<<<w.nb, kThreads, 0, st>>>(wv, vj, w.V.p + (int64_t)(j - 1) * n, n, coefcol + j,
-                                                   w.beta.p + (j - 1), stop); ::edgb::count_launch();
-            }
-            const int J = j + 1;
-            k_mdot<<<w.nbm, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, nullptr, stop); ::edgb::count_launch();
-            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nbm, J, w.c.p, coefcol, w.scal.p, nullptr, stop); ::edgb::count_launch();
-            k_update<<<w.nb, kThreads, (size_t)J * 8, st>>>(w.V.p, n, J, w.c.p, wv, w.npart.p, nullptr, stop); ::edgb::count_launch();
-            k_norm_finalize<<<1, kThreads, 0, st>>>(w.npart.p, w.nb, w.scal.p, w.beta.p + j, need2, first ? 1 : 0,
-                                                    nullptr, stop); ::edgb::count_launch();
-            k_mdot<<<w.nbm, kThreads, 0, st>>>(w.V.p, n, J, wv, w.part.p, need2, stop); ::edgb::count_launch();
-            k_mdot_finalize<<<1, 256, 0, st>>>(w.part.p, w.nbm, J, w.c.p, coefcol, w.scal.p + 2, need2, stop); ::edgb::count_launch();
-            k_update<<<w.nb, kThreads, (size_t)J * 8, st>>>(w.V.p, n, J, w.c.p, wv, w.npart.p, need2, stop); ::edgb::count_launch();
-            k_norm_finalize<<<1, kThreads, 0, st>>>(w.npart.p, w.nb, w.scal.p + 2, w.beta.p + j, nullptr, 0, need2,
-                                                    stop); ::edgb::count_launch();
-            k_break_test<<<1, 1, 0, st>>>(w.beta.p + j, first ? w.scal.p : w.scal.p + 1, stop, j); ::edgb::count_launch();
-            k_scale<<<w.nb, kThreads, 0, st>>>(wv, n, w.beta.p + j, stop); ::edgb::count_launch();
-            ED_CUDA(cudaGetLastError());
-        }
+        run_cycle(k);
+        inf.matvecs += m - k;
         int hstop = 0;
         ED_CUDA(cudaMemcpyAsync(&hstop, stop, sizeof(int), cudaMemcpyDeviceToHost, st));
         ED_CUDA(cudaMemcpyAsync(coef_h.data(), w.coef.p, coef_h.size() * 8, cudaMemcpyDeviceToHost, st));

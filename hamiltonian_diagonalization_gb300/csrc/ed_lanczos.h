@@ -19,6 +19,48 @@ struct ed_op {
 };
 
 namespace edgb {
+
+// Instantiated restart cycles, one per (first step, Krylov buffer), with the
+// number of kernels each launches.
+struct CycleGraphs {
+    struct Entry {
+        int k;
+        const double* V;
+        cudaGraphExec_t exec;
+        int64_t kernels;
+    };
+    std::vector<Entry> e;
+    ~CycleGraphs() { for (auto& x : e) cudaGraphExecDestroy(x.exec); }
+    Entry* find(int k, const double* V)
+    {
+        for (auto& x : e)
+            if (x.k == k && x.V == V) return &x;
+        return nullptr;
+    }
+};
+
+// The solver's own stream: stream capture is not available on the legacy
+// default stream, so the solve runs on a private non-blocking stream that
+// is ordered after the caller's stream on entry and before it on exit.
+struct SolveStream {
+    cudaStream_t s = nullptr;
+    cudaStream_t caller = nullptr;
+    cudaEvent_t e = nullptr;
+    explicit SolveStream(cudaStream_t c) : caller(c)
+    {
+        ED_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        ED_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ED_CUDA(cudaEventRecord(e, caller));
+        ED_CUDA(cudaStreamWaitEvent(s, e, 0));
+    }
+    ~SolveStream()
+    {
+        if (cudaEventRecord(e, s) == cudaSuccess) cudaStreamWaitEvent(caller, e, 0);
+        cudaEventDestroy(e);
+        cudaStreamDestroy(s);
+    }
+};
+
 void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st);
 // Lowest p.nev eigenpairs; v0_dev may be null; evecs_dev (n*nev) may be null.
 void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,

@@ -581,6 +581,34 @@ ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* basis, const double* v1_host, 
         const int64_t n = (int64_t)basis->dim;
         std::vector<double> hp((size_t)n * nv), hc((size_t)n * nv);
         ED_CUDA(cudaMemcpy(hp.data(), psi_dev, hp.size() * 8, cudaMemcpyDeviceToHost));
+        // Sign gauge: an eigensolver returns each ground state with an arbitrary
+        // overall sign, which would hand the sign output contradictory targets.
+        // Taking the columns in V1 order, the first gets its largest component
+        // positive and each later one the sign that overlaps its predecessor
+        // positively (neighbouring V1 points have strongly overlapping ground
+        // states away from level crossings).
+        std::vector<int> order(nv);
+        for (int b = 0; b < nv; ++b) order[b] = b;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return v1_host[x] < v1_host[y]; });
+        std::vector<double> flip(nv, 1.0);
+        for (int t = 0; t < nv; ++t) {
+            const int b = order[t];
+            double s = 0.0;
+            if (t == 0) {
+                int64_t arg = 0;
+                for (int64_t r = 1; r < n; ++r)
+                    if (std::fabs(hp[(size_t)r * nv + b]) > std::fabs(hp[(size_t)arg * nv + b])) arg = r;
+                s = hp[(size_t)arg * nv + b];
+            } else {
+                const int a = order[t - 1];
+                for (int64_t r = 0; r < n; ++r) s += flip[a] * hp[(size_t)r * nv + a] * hp[(size_t)r * nv + b];
+            }
+            flip[b] = s < 0.0 ? -1.0 : 1.0;
+        }
+        for (int64_t r = 0; r < n; ++r)
+            for (int b = 0; b < nv; ++b) hp[(size_t)r * nv + b] *= flip[b];
+        DevBuf<double> psi_g(hp.size());
+        ED_CUDA(cudaMemcpy(psi_g.p, hp.data(), hp.size() * 8, cudaMemcpyHostToDevice));
         for (int b = 0; b < nv; ++b) {
             double acc = 0.0;
             for (int64_t r = 0; r < n; ++r) {
@@ -595,7 +623,7 @@ ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* basis, const double* v1_host, 
         for (int s = 0; s < steps; ++s) {
             // linear decay to a tenth of the rate over the run
             const float lr_s = lr * (1.f - 0.9f * (float)s / (float)steps);
-            k_make_batch<<<grid_sz(batch), 256>>>(basis->words.p, n, psi_dev, nv, dv1.p, cdf.p, batch,
+            k_make_batch<<<grid_sz(batch), 256>>>(basis->words.p, n, psi_g.p, nv, dv1.p, cdf.p, batch,
                                                    seed + 0x632BE59BD9B4E019ull * (uint64_t)(s + 1), net->words.p,
                                                    net->v1.p, net->target.p);
             count_launch();

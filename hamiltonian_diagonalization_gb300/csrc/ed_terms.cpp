@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "ed_internal.h"
@@ -205,6 +207,36 @@ void coulomb_pseudopotentials(int norb, double* out)
     }
 }
 
+namespace {
+
+// CG(maxLz/2, m1; maxLz/2, m2 | Lact, m1+m2) for every (k1, k2) and every
+// l = 0..norb-2 (Lact = 2 maxLz - 2 l), indexed ((k1*K + k2)*(K-1) + l).  The
+// values depend only on the orbital count, so each table is computed once per
+// process and shared by every later call (sweeps build many V tables per K).
+const std::vector<double>& cg_table(int norb)
+{
+    static std::mutex mu;
+    static std::map<int, std::vector<double>> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(norb);
+    if (it != cache.end()) return it->second;
+    const int maxLz = norb - 1, K = norb, NL = std::max(norb - 1, 1);
+    std::vector<double> cg((size_t)K * K * NL, 0.0);
+    for (int k1 = 0; k1 < K; ++k1)
+        for (int k2 = 0; k2 < K; ++k2)
+            for (int l = 0; l < norb - 1; ++l) {
+                const int m1 = maxLz - 2 * k1, m2 = maxLz - 2 * k2;
+                const int lact = 2 * maxLz - 2 * l;
+                const int M = m1 + m2;
+                double v = 0.0;
+                if (-lact <= M && M <= lact) v = clebsch_gordan(maxLz, m1, maxLz, m2, lact, M);
+                cg[((size_t)k1 * K + k2) * NL + l] = v;
+            }
+    return cache.emplace(norb, std::move(cg)).first->second;
+}
+
+}  // namespace
+
 // pseudopotential_model_base.hpp:62-229 for one Landau level (maxLz2 =
 // maxLz, so FindM1's error code maxLz+2 converts to k = 65535).
 void quartic_tables(int norb, const double* pp, int npp, uint16_t* ktab, double* vtab)
@@ -214,18 +246,8 @@ void quartic_tables(int norb, const double* pp, int npp, uint16_t* ktab, double*
                "too many two-body pseudopotential coefficients (at most 2S = norb-1)");
     const int maxLz = norb - 1;
     const int K = norb;
-    // CG table for j1 = j2 = maxLz/2, indexed by (k1, k2, L/2): m = maxLz - 2k
-    std::vector<double> cg((size_t)K * K * std::max(npp, 1), 0.0);
-    for (int k1 = 0; k1 < K; ++k1)
-        for (int k2 = 0; k2 < K; ++k2)
-            for (int l = 0; l < npp; ++l) {
-                const int m1 = maxLz - 2 * k1, m2 = maxLz - 2 * k2;
-                const int lact = 2 * maxLz - 2 * l;
-                const int M = m1 + m2;
-                double v = 0.0;
-                if (-lact <= M && M <= lact) v = clebsch_gordan(maxLz, m1, maxLz, m2, lact, M);
-                cg[((size_t)k1 * K + k2) * std::max(npp, 1) + l] = v;
-            }
+    const std::vector<double>& cg = cg_table(norb);
+    const int NL = std::max(norb - 1, 1);
     size_t it = 0;
     for (int m4 = maxLz; m4 >= -maxLz; m4 -= 2) {
         for (int m3 = maxLz; m3 >= -maxLz; m3 -= 2) {
@@ -243,7 +265,7 @@ void quartic_tables(int norb, const double* pp, int npp, uint16_t* ktab, double*
                         double temp = 0.0;
                         const int lact = 2 * maxLz - 2 * l;
                         if (-lact <= M && M <= lact) {
-                            temp += cg[((size_t)k1 * K + k2) * npp + l] * cg[((size_t)k3 * K + k4) * npp + l];
+                            temp += cg[((size_t)k1 * K + k2) * NL + l] * cg[((size_t)k3 * K + k4) * NL + l];
                         }
                         total -= pp[l] * temp;
                     }

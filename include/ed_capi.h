@@ -248,6 +248,7 @@ typedef struct {
     int tile_hamiltonians;    /* autotuned Hamiltonians per row tile of the block product */
     int tile_unroll;          /* autotuned loads in flight per lane                  */
     int tile_l1;              /* 1: hop values read through L1, 0: staged in shared memory */
+    int tile_threads;         /* threads per CTA of the block product                */
 } ed_batch_info;
 
 /* Shared pattern (int32 column + uint16 hop code per element) built once on
@@ -292,7 +293,9 @@ ed_status ed_mlp_gradients(ed_mlp* net, const uint64_t* words_dev, const float* 
 ed_status ed_mlp_train_step(ed_mlp* net, const uint64_t* words_dev, const float* v1_dev, const float* target_dev,
                             int64_t m, float lr, double* loss_host);
 /* Train on ground states psi_dev ([n][nv], one column per V1 value) of the
- * basis: `steps` Adam steps on seeded random batches of (state, V1). */
+ * basis: `steps` Adam steps on seeded random batches of (state, V1).  The
+ * columns' overall signs are first made consistent (V1 order, each overlapping
+ * its predecessor positively); psi_dev itself is not changed. */
 ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* b, const double* v1_host, int nv, const double* psi_dev, int steps,
                      int batch, float lr, uint64_t seed, double* final_loss);
 /* Start vectors for nham Hamiltonians: V0_dev[r*nham + j] = predicted psi of
