@@ -54,7 +54,7 @@ class BatchInfo(ctypes.Structure):
     _fields_ = [("converged", c_int), ("restarts", c_int), ("block_products", c_i64), ("max_residual", c_double),
                 ("seconds", c_double), ("spmm_seconds", c_double), ("breakdowns", c_int),
                 ("tile_hamiltonians", c_int), ("tile_unroll", c_int), ("tile_l1", c_int),
-                ("tile_threads", c_int)]
+                ("tile_threads", c_int), ("problem_products", c_i64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

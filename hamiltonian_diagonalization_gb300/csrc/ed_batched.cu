@@ -415,38 +415,60 @@ __global__ void k_baxpy2(double* __restrict__ w, const double* __restrict__ v, c
     }
 }
 
+// Eight per-problem sums at once: acc[t] of every thread to
+// part[(q0+t)*stride_q + p] summed over the block's row lanes, for t < cnt.
+__device__ __forceinline__ void reduce8_per_problem(const double (&acc)[8], int cnt, double* red, int BP, int B,
+                                                    double* out_slot_base, int64_t stride_q, int q0)
+{
+#pragma unroll
+    for (int t = 0; t < 8; ++t) red[t * kBT + threadIdx.x] = acc[t];
+    __syncthreads();
+    const int nrl = kBT / BP;
+    for (int q = threadIdx.x; q < cnt * BP; q += kBT) {
+        const int t = q / BP, pp = q - t * BP;
+        double s = 0.0;
+        for (int l = 0; l < nrl; ++l) s += red[t * kBT + l * BP + pp];
+        if (pp < B) out_slot_base[stride_q * (q0 + t) + pp] = s;
+    }
+    __syncthreads();
+}
+
 // part[i][blk][p] = V_i,p . w_p for i < J; part[J][blk][p] = w_p . w_p.
-// Problems with need[p] == 0 (when need is given) contribute zeros.
+// Columns in groups of eight: one w load and eight independent V loads per
+// row in flight.  Problems with need[p] == 0 (when need is given) contribute
+// zeros.
 __global__ void __launch_bounds__(kBT) k_bmdot(const double* __restrict__ V, int64_t n, int B, int BP, int J,
                                                const double* __restrict__ w, double* __restrict__ part,
                                                const int* __restrict__ need)
 {
-    __shared__ double red[kBT];
+    __shared__ double red[8 * kBT];
     int64_t r0, r1;
     chunk_rows(n, gridDim.x, blockIdx.x, r0, r1);
     const int p = threadIdx.x % BP, rl = threadIdx.x / BP, nrl = kBT / BP;
     const int64_t vs = n * (int64_t)B;
     const int64_t sq = (int64_t)gridDim.x * B;
     const bool act = p < B && (!need || need[p]);
-    for (int i0 = 0; i0 <= J; i0 += 4) {
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i0 = 0; i0 <= J; i0 += 8) {
+        double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         if (act)
             for (int64_t r = r0 + rl; r < r1; r += nrl) {
                 const double wv = w[r * B + p];
+                double v[8];
 #pragma unroll
-                for (int t = 0; t < 4; ++t) {
+                for (int t = 0; t < 8; ++t) {
                     const int i = i0 + t;
-                    if (i < J) acc[t] = fma(V[i * vs + r * B + p], wv, acc[t]);
-                    else if (i == J) acc[t] = fma(wv, wv, acc[t]);
+                    v[t] = i < J ? V[i * vs + r * B + p] : (i == J ? wv : 0.0);
                 }
+#pragma unroll
+                for (int t = 0; t < 8; ++t) acc[t] = fma(v[t], wv, acc[t]);
             }
-        for (int t = 0; t < 4 && i0 + t <= J; ++t)
-            reduce_per_problem(acc[t], red, BP, B, part + (int64_t)blockIdx.x * B, sq, i0 + t);
+        reduce8_per_problem(acc, min(8, J + 1 - i0), red, BP, B, part + (int64_t)blockIdx.x * B, sq, i0);
     }
 }
 
 // w_p -= sum_i c[i][p] V_i,p ; npart[blk][p] = |w_p|^2.  Problems with
 // need[p] == 0 (when need is given) are left alone and contribute zeros.
+// Eight column loads in flight, two FMA chains (even / odd columns).
 __global__ void __launch_bounds__(kBT) k_bupdate(const double* __restrict__ V, int64_t n, int B, int BP, int J,
                                                  const double* __restrict__ c, double* __restrict__ w,
                                                  double* __restrict__ npart, const int* __restrict__ need)
@@ -459,8 +481,20 @@ __global__ void __launch_bounds__(kBT) k_bupdate(const double* __restrict__ V, i
     double nn = 0.0;
     if (p < B && (!need || need[p])) {
         for (int64_t r = r0 + rl; r < r1; r += nrl) {
-            double acc = w[r * B + p];
-            for (int i = 0; i < J; ++i) acc = fma(-c[i * B + p], V[i * vs + r * B + p], acc);
+            double acc = w[r * B + p], acc2 = 0.0;
+            int i = 0;
+            for (; i + 8 <= J; i += 8) {
+                double v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = V[(i + u) * vs + r * B + p];
+#pragma unroll
+                for (int u = 0; u < 8; u += 2) {
+                    acc = fma(-__ldg(c + (i + u) * B + p), v[u], acc);
+                    acc2 = fma(-__ldg(c + (i + u + 1) * B + p), v[u + 1], acc2);
+                }
+            }
+            for (; i < J; ++i) acc = fma(-__ldg(c + i * B + p), V[i * vs + r * B + p], acc);
+            acc += acc2;
             w[r * B + p] = acc;
             nn = fma(acc, acc, nn);
         }
@@ -521,25 +555,46 @@ __global__ void k_bscale(double* __restrict__ w, int64_t n, int B, const double*
     }
 }
 
-// out_i,p = sum_j V_j,p Y[i][j][p] for i < k: Y holds the Ritz coefficients
-// with the problem index fastest, so a warp's lanes (consecutive problems)
-// read them coalesced.
-__global__ void k_bgemm(const double* __restrict__ V, int64_t n, int B, int m, const double* __restrict__ Y, int k,
-                        double* __restrict__ out)
+// Ritz vectors of selected problems: for q < Bq, s = keep[q] (a column of the
+// Bs-wide basis V) and d = dst ? dst[q] : q (a column of the Bo-wide output),
+// out[i][r][d] = sum_j V[j][r][s] Y[i][j][s] for i < k.  With keep = identity
+// and dst = null this is the restart rotation; with keep = the surviving
+// problems it also compacts them; with dst = original indices it writes
+// finished problems' eigenvectors into the caller's layout.
+__global__ void k_bgemm_sel(const double* __restrict__ V, int64_t n, int Bs, int m, const double* __restrict__ Y,
+                            int k, double* __restrict__ out, int Bo, int Bq, const int* __restrict__ keep,
+                            const int* __restrict__ dst)
 {
-    const int64_t vs = n * (int64_t)B;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < vs; t += (int64_t)gridDim.x * blockDim.x) {
-        const int p = (int)(t % B);
+    const int64_t vs = n * (int64_t)Bs, os = n * (int64_t)Bo;
+    const int64_t total = n * (int64_t)Bq;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / Bq;
+        const int q = (int)(t - r * Bq);
+        const int s = keep[q];
+        const int d = dst ? dst[q] : q;
+        const double* v = V + r * Bs + s;
         for (int i0 = 0; i0 < k; i0 += 8) {
             double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             for (int j = 0; j < m; ++j) {
-                const double v = V[j * vs + t];
+                const double x = v[j * vs];
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (i0 + q < k) acc[q] = fma(v, __ldg(Y + ((size_t)(i0 + q) * m + j) * B + p), acc[q]);
+                for (int u = 0; u < 8; ++u)
+                    if (i0 + u < k) acc[u] = fma(x, __ldg(Y + ((size_t)(i0 + u) * m + j) * Bs + s), acc[u]);
             }
-            for (int q = 0; q < 8 && i0 + q < k; ++q) out[(i0 + q) * vs + t] = acc[q];
+            for (int u = 0; u < 8 && i0 + u < k; ++u) out[(i0 + u) * os + r * Bo + d] = acc[u];
         }
+    }
+}
+
+// out[r][q] = in[r][keep[q]] for r < rows, q < Bq (in has Bs columns)
+__global__ void k_bgather(const double* __restrict__ in, int64_t rows, int Bs, const int* __restrict__ keep, int Bq,
+                          double* __restrict__ out)
+{
+    const int64_t total = rows * (int64_t)Bq;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / Bq;
+        const int q = (int)(t - r * Bq);
+        out[t] = in[r * Bs + keep[q]];
     }
 }
 
@@ -653,8 +708,18 @@ namespace {
 
 constexpr size_t kSmemOptIn = 227 * 1024;   // dynamic shared memory per CTA on sm_103a
 
+// The per-Hamiltonian operands of a block product: hop values [nhop][B] and
+// diagonals [n][B] for the B problems being multiplied (all of a batch, or
+// the compacted subset a solve still iterates).
+struct BlockOperands {
+    const double* w;
+    const double* diag;
+    int B;
+};
+
 template <int TB, int U, int NT>
-void launch_bspmm(const ed_batch& bt, const double* X, double* Y, int64_t rows, cudaStream_t st)
+void launch_bspmm(const ed_batch& bt, const BlockOperands& o, const double* X, double* Y, int64_t rows,
+                  cudaStream_t st)
 {
     const size_t smem = (size_t)bt.nhop * TB * 8;
     static_assert(U <= kCrsPad, "batch overruns the padding");
@@ -663,19 +728,20 @@ void launch_bspmm(const ed_batch& bt, const double* X, double* Y, int64_t rows, 
         ED_CUDA(cudaFuncSetAttribute(k_bspmm<TB, U, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
     ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bspmm<TB, U, NT>, NT, smem));
-    dim3 grid((unsigned)(sms_b() * std::max(1, per_sm)), (unsigned)((bt.B + TB - 1) / TB));
-    k_bspmm<TB, U, NT><<<grid, NT, smem, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.nhop, bt.diag.p, X, Y,
-                                                 rows, bt.B);
+    dim3 grid((unsigned)(sms_b() * std::max(1, per_sm)), (unsigned)((o.B + TB - 1) / TB));
+    k_bspmm<TB, U, NT><<<grid, NT, smem, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, o.w, bt.nhop, o.diag, X, Y, rows,
+                                                 o.B);
     count_launch();
     ED_CUDA(cudaGetLastError());
 }
 
 template <int U, int TB>
-void launch_bspmm_warp(const ed_batch& bt, const double* X, double* Y, int64_t rows, cudaStream_t st)
+void launch_bspmm_warp(const ed_batch& bt, const BlockOperands& o, const double* X, double* Y, int64_t rows,
+                       cudaStream_t st)
 {
     static_assert(U <= kCrsPad, "batch overruns the padding");
-    dim3 grid((unsigned)(sms_b() * 8), (unsigned)((bt.B + TB - 1) / TB));
-    k_bspmm_warp<U, TB><<<grid, 256, 0, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, bt.w.p, bt.diag.p, X, Y, rows, bt.B);
+    dim3 grid((unsigned)(sms_b() * 8), (unsigned)((o.B + TB - 1) / TB));
+    k_bspmm_warp<U, TB><<<grid, 256, 0, st>>>(bt.rowptr.p, bt.col.p, bt.code.p, o.w, o.diag, X, Y, rows, o.B);
     count_launch();
     ED_CUDA(cudaGetLastError());
 }
@@ -683,17 +749,19 @@ void launch_bspmm_warp(const ed_batch& bt, const double* X, double* Y, int64_t r
 // One block-product variant on rows [0, rows): l1 = 1 reads the hop values
 // through L1 (TB 16 or 32 lanes per row); l1 = 0 stages the tile's hop table
 // in shared memory (TB 4, 8 or 16 Hamiltonians, 256 or 1024 threads).
-void bspmm_variant(const ed_batch& bt, int tb, int u, int nt, int l1, const double* X, double* Y, int64_t rows,
-                   cudaStream_t st)
+void bspmm_variant(const ed_batch& bt, const BlockOperands& o, int tb, int u, int nt, int l1, const double* X,
+                   double* Y, int64_t rows, cudaStream_t st)
 {
     if (l1) {
-        if (tb == 32) u == 4 ? launch_bspmm_warp<4, 32>(bt, X, Y, rows, st) : launch_bspmm_warp<8, 32>(bt, X, Y, rows, st);
-        else u == 4 ? launch_bspmm_warp<4, 16>(bt, X, Y, rows, st) : launch_bspmm_warp<8, 16>(bt, X, Y, rows, st);
+        if (tb == 32)
+            u == 4 ? launch_bspmm_warp<4, 32>(bt, o, X, Y, rows, st) : launch_bspmm_warp<8, 32>(bt, o, X, Y, rows, st);
+        else
+            u == 4 ? launch_bspmm_warp<4, 16>(bt, o, X, Y, rows, st) : launch_bspmm_warp<8, 16>(bt, o, X, Y, rows, st);
         return;
     }
 #define ED_BSPMM_CASE(TB_, U_, NT_)                                                   \
     if (tb == TB_ && u == U_ && nt == NT_) {                                          \
-        launch_bspmm<TB_, U_, NT_>(bt, X, Y, rows, st);                               \
+        launch_bspmm<TB_, U_, NT_>(bt, o, X, Y, rows, st);                            \
         return;                                                                       \
     }
     ED_BSPMM_CASE(4, 4, 256) ED_BSPMM_CASE(4, 8, 256) ED_BSPMM_CASE(8, 4, 256) ED_BSPMM_CASE(8, 8, 256)
@@ -704,11 +772,13 @@ void bspmm_variant(const ed_batch& bt, int tb, int u, int nt, int l1, const doub
     throw Error(ED_ERR_INTERNAL, "unknown block-product tile");
 }
 
+BlockOperands full_operands(const ed_batch& bt) { return {bt.w.p, bt.diag.p, bt.B}; }
+
 }  // namespace
 
 void batch_spmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
 {
-    bspmm_variant(bt, bt.tb, bt.unroll, bt.nt, bt.l1, X, Y, bt.n, st);
+    bspmm_variant(bt, full_operands(bt), bt.tb, bt.unroll, bt.nt, bt.l1, X, Y, bt.n, st);
 }
 
 // Pick the block-product tile that runs fastest on this data, timed on the
@@ -763,9 +833,9 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
         for (int u : {4, 8}) cands.push_back({tb, u, 256, 1});
     }
     for (const auto& c : cands) {
-        bspmm_variant(bt, c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
+        bspmm_variant(bt, full_operands(bt), c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
         ED_CUDA(cudaEventRecord(a, st));
-        for (int r = 0; r < 3; ++r) bspmm_variant(bt, c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
+        for (int r = 0; r < 3; ++r) bspmm_variant(bt, full_operands(bt), c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
         ED_CUDA(cudaEventRecord(b, st));
         ED_CUDA(cudaEventSynchronize(b));
         float ms = 0.f;
@@ -791,10 +861,12 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
 // Lockstep thick-restart Lanczos for the B problems of a batch: the
 // recurrences of lanczos_solve (local three-term step, full Gram-Schmidt pass
 // with a DGKS second pass, forced on the first step of a cycle), every scalar
-// per problem.  All problems restart together; converged ones keep iterating
-// (their pairs stay converged) until every problem has its nev pairs.  A
-// Krylov breakdown, which needs an exactly invariant subspace, is reported
-// as ED_ERR_BREAKDOWN for the batch; such a problem is solved with ed_lanczos.
+// per problem.  All active problems restart together.  At a restart the
+// problems whose nev pairs have converged retire: their Ritz vectors go to the
+// output at their own column, and the survivors' Krylov basis, hop values and
+// diagonals are compacted so that later cycles spend no FP64 work on them.  A
+// Krylov breakdown, which needs an exactly invariant subspace, is reported as
+// ED_ERR_BREAKDOWN for the batch; such a problem is solved with ed_lanczos.
 // A restart cycle runs without host round trips and is replayed as a CUDA
 // graph on the solver's own stream.
 void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V0, double* evals, double* evecs,
@@ -802,7 +874,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
 {
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t n = bt.n;
-    const int B = bt.B;
+    const int B0 = bt.B;
     const int nev = p.nev;
     ED_REQUIRE(nev >= 1 && nev + 2 < n, ED_ERR_ARG, "need 1 <= nev < n - 2");
     const double tol = p.tol > 0 ? p.tol : 1e-10;
@@ -811,22 +883,33 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     m64 = std::max<int64_t>(m64, nev + 2);
     m64 = std::min<int64_t>(m64, std::min<int64_t>(n - 1, 200));
     const int m = (int)m64;
-    int BP = 1;
-    while (BP < B) BP <<= 1;
-    ED_REQUIRE(BP <= kBT, ED_ERR_ARG, "at most 256 problems per batch");
+    ED_REQUIRE(B0 <= kBT, ED_ERR_ARG, "at most 256 problems per batch");
     SolveStream ss(caller_stream);
     cudaStream_t st = ss.s;
-    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 2, n / 256));
-    const int64_t vs = n * (int64_t)B;
-    DevBuf<double> V((size_t)vs * (m + 1)), V2((size_t)vs * (m + 1));
-    DevBuf<double> part((size_t)(m + 2) * nb * B), npart((size_t)nb * B);
-    DevBuf<double> sc((size_t)(m + 2) * B);
-    DevBuf<double> s2((size_t)6 * B);   // [0] alpha [1] |Hv|^2 [2] scratch [3] |w|^2 after a pass
-    DevBuf<int> need2(B), brk(B);
-    DevBuf<double> coef((size_t)m * (m + 1) * B);
-    DevBuf<double> betas((size_t)(m + 1) * B);
-    DevBuf<double> Yd((size_t)B * m * m);
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 4, n / 128));
+    const int64_t vs0 = n * (int64_t)B0;
+    DevBuf<double> V((size_t)vs0 * (m + 1)), V2((size_t)vs0 * (m + 1));
+    DevBuf<double> part((size_t)(m + 2) * nb * B0), npart((size_t)nb * B0);
+    DevBuf<double> sc((size_t)(m + 2) * B0);
+    DevBuf<double> s2((size_t)6 * B0);   // [0] alpha [1] |Hv|^2 [2] scratch [3] |w|^2 after a pass
+    DevBuf<int> need2(B0), brk(B0), iota(B0), keep(B0), dst(B0);
+    DevBuf<double> coef((size_t)m * (m + 1) * B0);
+    DevBuf<double> betas((size_t)(m + 1) * B0);
+    DevBuf<double> Yd((size_t)B0 * m * m);
+    DevBuf<double> wc[2], dc[2];          // compacted operands (allocated at the first retirement)
     ED_CUDA(cudaMemsetAsync(betas.p, 0, betas.bytes(), st));
+    std::vector<int> ident(B0);
+    for (int b = 0; b < B0; ++b) ident[b] = b;
+    ED_CUDA(cudaMemcpyAsync(iota.p, ident.data(), (size_t)B0 * 4, cudaMemcpyHostToDevice, st));
+
+    // the active problems: count, column -> original index, operands, layout
+    int B = B0, BP = 1;
+    auto set_bp = [&]() { BP = 1; while (BP < B) BP <<= 1; };
+    set_bp();
+    std::vector<int> orig = ident;
+    BlockOperands ops = full_operands(bt);
+    int64_t vs = vs0;
+
     auto grid_for = [&](int64_t work) { return (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 8, (work + 255) / 256)); };
     auto bsum = [&](const double* src, int Q, double* out, const int* mask) {
         k_bsum<<<(unsigned)((Q * B + 31) / 32), 256, 0, st>>>(src, nb, B, Q, out, mask); count_launch();
@@ -852,25 +935,45 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     inf.tile_l1 = bt.l1;
     inf.tile_unroll = bt.unroll;
     inf.tile_threads = bt.l1 ? 256 : bt.nt;
-    std::vector<std::vector<double>> T(B, std::vector<double>((size_t)m * m, 0.0)), theta(B), Y(B);
-    std::vector<double> coef_h((size_t)m * (m + 1) * B), beta_h((size_t)(m + 1) * B), Yall((size_t)B * m * m);
-    std::vector<int> brk_h(B);
+    std::vector<std::vector<double>> T(B0, std::vector<double>((size_t)m * m, 0.0)), theta(B0), Y(B0);
+    std::vector<double> coef_h((size_t)m * (m + 1) * B0), beta_h((size_t)(m + 1) * B0), Yall((size_t)B0 * m * m);
+    std::vector<int> brk_h(B0);
     std::vector<cudaEvent_t> ev(2 * (size_t)(m + 1), nullptr);
     for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
     struct EvG {
         std::vector<cudaEvent_t>& v;
         ~EvG() { for (auto e : v) if (e) cudaEventDestroy(e); }
     } evg{ev};
-    // Ritz coefficients of every problem, [i][j][p] (problem fastest)
+    // Ritz coefficients of the active problems, [i][j][column] (column fastest)
     auto pack_Y = [&]() {
-        for (int b = 0; b < B; ++b)
+        for (int q = 0; q < B; ++q) {
+            const std::vector<double>& Yb = Y[orig[q]];
             for (int i = 0; i < m; ++i)
-                for (int j = 0; j < m; ++j) Yall[((size_t)i * m + j) * B + b] = Y[b][(size_t)j + (size_t)m * i];
-        ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), Yall.size() * 8, cudaMemcpyHostToDevice, st));
+                for (int j = 0; j < m; ++j) Yall[((size_t)i * m + j) * B + q] = Yb[(size_t)j + (size_t)m * i];
+        }
+        ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), (size_t)m * m * B * 8, cudaMemcpyHostToDevice, st));
+    };
+    // output eigenvectors: [i][r][original index], i < nev
+    DevBuf<double> xtmp, ytmp;
+    double* X = evecs;
+    if (!X && p.verify) {
+        xtmp.alloc((size_t)vs0 * nev);
+        X = xtmp.p;
+    }
+    auto write_ritz = [&](const std::vector<int>& cols) {   // cols: active columns whose pairs are final
+        if (!X || cols.empty()) return;
+        std::vector<int> d(cols.size());
+        for (size_t i = 0; i < cols.size(); ++i) d[i] = orig[cols[i]];
+        ED_CUDA(cudaMemcpyAsync(keep.p, cols.data(), cols.size() * 4, cudaMemcpyHostToDevice, st));
+        ED_CUDA(cudaMemcpyAsync(dst.p, d.data(), d.size() * 4, cudaMemcpyHostToDevice, st));
+        k_bgemm_sel<<<grid_for(n * (int64_t)cols.size()), 256, 0, st>>>(V.p, n, B, m, Yd.p, nev, X, B0,
+                                                                        (int)cols.size(), keep.p, dst.p);
+        count_launch();
+        ED_CUDA(cudaStreamSynchronize(st));   // keep/dst are reused right away
     };
 
     auto enqueue_cycle = [&](int k, bool capturing) {
-        ED_CUDA(cudaMemsetAsync(coef.p, 0, coef.bytes(), st));
+        ED_CUDA(cudaMemsetAsync(coef.p, 0, (size_t)m * (m + 1) * B * 8, st));
         ED_CUDA(cudaMemsetAsync(brk.p, 0, (size_t)B * 4, st));
         for (int j = k; j < m; ++j) {
             double* vj = V.p + (int64_t)j * vs;
@@ -879,7 +982,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
             const bool first = (j == k);
             if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j], st, cudaEventRecordExternal));
             else ED_CUDA(cudaEventRecord(ev[2 * j], st));
-            batch_spmm(bt, vj, w, st);
+            bspmm_variant(bt, ops, bt.tb, bt.unroll, bt.nt, bt.l1, vj, w, n, st);
             if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j + 1], st, cudaEventRecordExternal));
             else ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
             if (!first) {
@@ -942,12 +1045,15 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
 
     double spmm_ms = 0.0;
     bool converged = false;
+    int finished = 0;
+    double retired_res = 0.0;
     int k = 0;
     for (;;) {
         run_cycle(k);
         inf.block_products += m - k;
-        ED_CUDA(cudaMemcpyAsync(coef_h.data(), coef.p, coef.bytes(), cudaMemcpyDeviceToHost, st));
-        ED_CUDA(cudaMemcpyAsync(beta_h.data(), betas.p, beta_h.size() * 8, cudaMemcpyDeviceToHost, st));
+        inf.problem_products += (int64_t)(m - k) * B;
+        ED_CUDA(cudaMemcpyAsync(coef_h.data(), coef.p, (size_t)m * (m + 1) * B * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaMemcpyAsync(beta_h.data(), betas.p, (size_t)(m + 1) * B * 8, cudaMemcpyDeviceToHost, st));
         ED_CUDA(cudaMemcpyAsync(brk_h.data(), brk.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
         ED_CUDA(cudaStreamSynchronize(st));
         for (int j = k; j < m; ++j) {
@@ -955,96 +1061,138 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
             ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * j], ev[2 * j + 1]));
             spmm_ms += ms;
         }
-        int nconv = 0;
+        std::vector<int> done, live;
         double maxres = 0.0;
-        for (int b = 0; b < B; ++b) {
-            if (brk_h[b]) {
+        for (int q = 0; q < B; ++q) {
+            if (brk_h[q]) {
                 inf.breakdowns++;
                 continue;
             }
+            const int b = orig[q];
             std::vector<double>& Tb = T[b];
             for (int j = k; j < m; ++j)
                 for (int i = 0; i <= j; ++i) {
-                    const double v = coef_h[((size_t)j * (m + 1) + i) * B + b];
+                    const double v = coef_h[((size_t)j * (m + 1) + i) * B + q];
                     Tb[(size_t)i * m + j] = v;
                     Tb[(size_t)j * m + i] = v;
                 }
             sym_eigen(m, Tb, theta[b], Y[b]);
-            const double bl = beta_h[(size_t)(m - 1) * B + b];
+            const double bl = beta_h[(size_t)(m - 1) * B + q];
             bool ok = true;
+            double rq = 0.0;
             for (int i = 0; i < nev; ++i) {
                 const double r = std::fabs(bl * Y[b][(size_t)(m - 1) + (size_t)m * i]);
-                maxres = std::max(maxres, r);
+                rq = std::max(rq, r);
                 if (!(r <= tol)) ok = false;
             }
-            nconv += ok ? 1 : 0;
+            maxres = std::max(maxres, rq);
+            if (ok) retired_res = std::max(retired_res, rq);
+            (ok ? done : live).push_back(q);
         }
         ED_REQUIRE(inf.breakdowns == 0, ED_ERR_BREAKDOWN,
                    "Krylov breakdown in a batched problem: solve it with ed_lanczos");
-        inf.converged = nconv;
-        inf.max_residual = maxres;
-        if (nconv == B) {
+        // worst estimate: problems still iterating and every retired one
+        inf.max_residual = std::max(maxres, retired_res);
+        pack_Y();
+        if (live.empty()) {
+            write_ritz(done);
+            finished += (int)done.size();
             converged = true;
             break;
         }
-        if (inf.restarts >= max_restarts) break;
+        if (inf.restarts >= max_restarts) {
+            std::vector<int> all(B);
+            for (int q = 0; q < B; ++q) all[q] = q;
+            write_ritz(all);
+            finished += (int)done.size();
+            break;
+        }
         ++inf.restarts;
         int kk = std::min(m - 2, nev + std::max(1, (m - nev) / 2));
         kk = std::max(kk, std::min(nev, m - 1));
-        pack_Y();
-        k_bgemm<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, m, Yd.p, kk, V2.p); count_launch();
-        ED_CUDA(cudaMemcpyAsync(V2.p + (int64_t)kk * vs, V.p + (int64_t)m * vs, (size_t)vs * 8, cudaMemcpyDeviceToDevice,
-                                st));
+        if (!done.empty()) {
+            // retire the converged problems and compact the survivors
+            write_ritz(done);
+            finished += (int)done.size();
+            const int Bn = (int)live.size();
+            const int64_t vsn = n * (int64_t)Bn;
+            ED_CUDA(cudaMemcpyAsync(keep.p, live.data(), (size_t)Bn * 4, cudaMemcpyHostToDevice, st));
+            k_bgemm_sel<<<grid_for(vsn), 256, 0, st>>>(V.p, n, B, m, Yd.p, kk, V2.p, Bn, Bn, keep.p, nullptr);
+            count_launch();
+            k_bgather<<<grid_for(vsn), 256, 0, st>>>(V.p + (int64_t)m * vs, n, B, keep.p, Bn, V2.p + (int64_t)kk * vsn);
+            count_launch();
+            const int nxt = (ops.w == wc[0].p) ? 1 : 0;
+            if (!wc[nxt].p) {
+                wc[nxt].alloc((size_t)bt.nhop * B0);
+                dc[nxt].alloc((size_t)vs0);
+            }
+            k_bgather<<<grid_for((int64_t)bt.nhop * Bn), 256, 0, st>>>(ops.w, bt.nhop, B, keep.p, Bn, wc[nxt].p);
+            count_launch();
+            k_bgather<<<grid_for(vsn), 256, 0, st>>>(ops.diag, n, B, keep.p, Bn, dc[nxt].p);
+            count_launch();
+            ED_CUDA(cudaGetLastError());
+            ops = {wc[nxt].p, dc[nxt].p, Bn};
+            std::vector<int> no(Bn);
+            for (int q = 0; q < Bn; ++q) no[q] = orig[live[q]];
+            orig = no;
+            B = Bn;
+            vs = vsn;
+            set_bp();
+            for (auto& x : cache.e) cudaGraphExecDestroy(x.exec);
+            cache.e.clear();
+        } else {
+            k_bgemm_sel<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, m, Yd.p, kk, V2.p, B, B, iota.p, nullptr);
+            count_launch();
+            ED_CUDA(cudaMemcpyAsync(V2.p + (int64_t)kk * vs, V.p + (int64_t)m * vs, (size_t)vs * 8,
+                                    cudaMemcpyDeviceToDevice, st));
+        }
         std::swap(V, V2);
-        for (int b = 0; b < B; ++b) {
+        for (int q = 0; q < B; ++q) {
+            const int b = orig[q];
             std::vector<double>& Tb = T[b];
             std::fill(Tb.begin(), Tb.end(), 0.0);
-            const double bl = beta_h[(size_t)(m - 1) * B + b];
+            const double bl = beta_h[(size_t)(m - 1) * (B + (int)done.size()) + (size_t)live[q]];
             for (int i = 0; i < kk; ++i) {
                 Tb[(size_t)i * m + i] = theta[b][i];
-                const double s = bl * Y[b][(size_t)(m - 1) + (size_t)m * i];
-                Tb[(size_t)i * m + kk] = s;
-                Tb[(size_t)kk * m + i] = s;
+                const double sv = bl * Y[b][(size_t)(m - 1) + (size_t)m * i];
+                Tb[(size_t)i * m + kk] = sv;
+                Tb[(size_t)kk * m + i] = sv;
             }
         }
         k = kk;
         ED_CUDA(cudaStreamSynchronize(st));
     }
-    for (int b = 0; b < B; ++b)
+    inf.converged = finished;
+    for (int b = 0; b < B0; ++b)
         for (int i = 0; i < nev; ++i) evals[(size_t)b * nev + i] = theta[b][i];
-    DevBuf<double> xtmp, ytmp;
-    double* X = evecs;
-    if (!X && p.verify) {
-        xtmp.alloc((size_t)vs * nev);
-        X = xtmp.p;
-    }
-    if (X) {
-        pack_Y();
-        k_bgemm<<<grid_for(vs), 256, 0, st>>>(V.p, n, B, m, Yd.p, nev, X); count_launch();
-    }
     if (p.verify && X) {
-        ytmp.alloc((size_t)vs);
-        std::vector<double> lam(B), res(B);
-        DevBuf<double> dl(B);
+        // true residuals of every Hamiltonian, through the full batch's operator
+        BP = 1;
+        while (BP < B0) BP <<= 1;
+        B = B0;
+        ytmp.alloc((size_t)vs0);
+        std::vector<double> lam(B0), res(B0);
+        DevBuf<double> dl(B0);
         double worst = 0.0;
         int ok_all = 0;
-        std::vector<char> okb(B, 1);
+        std::vector<char> okb(B0, 1);
         for (int i = 0; i < nev; ++i) {
-            for (int b = 0; b < B; ++b) lam[b] = evals[(size_t)b * nev + i];
-            ED_CUDA(cudaMemcpyAsync(dl.p, lam.data(), (size_t)B * 8, cudaMemcpyHostToDevice, st));
-            batch_spmm(bt, X + (int64_t)i * vs, ytmp.p, st);
+            for (int b = 0; b < B0; ++b) lam[b] = evals[(size_t)b * nev + i];
+            ED_CUDA(cudaMemcpyAsync(dl.p, lam.data(), (size_t)B0 * 8, cudaMemcpyHostToDevice, st));
+            batch_spmm(bt, X + (int64_t)i * vs0, ytmp.p, st);
             ++inf.block_products;
-            k_bresid<<<nb, kBT, 0, st>>>(ytmp.p, X + (int64_t)i * vs, n, B, BP, dl.p, part.p); count_launch();
+            inf.problem_products += B0;
+            k_bresid<<<nb, kBT, 0, st>>>(ytmp.p, X + (int64_t)i * vs0, n, B0, BP, dl.p, part.p); count_launch();
             bsum(part.p, 1, s2.p, nullptr);
-            ED_CUDA(cudaMemcpyAsync(res.data(), s2.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+            ED_CUDA(cudaMemcpyAsync(res.data(), s2.p, (size_t)B0 * 8, cudaMemcpyDeviceToHost, st));
             ED_CUDA(cudaStreamSynchronize(st));
-            for (int b = 0; b < B; ++b) {
+            for (int b = 0; b < B0; ++b) {
                 const double r = std::sqrt(res[b]);
                 worst = std::max(worst, r);
                 if (!(r <= tol)) okb[b] = 0;
             }
         }
-        for (int b = 0; b < B; ++b) ok_all += okb[b];
+        for (int b = 0; b < B0; ++b) ok_all += okb[b];
         inf.max_residual = worst;
         inf.converged = ok_all;
     }

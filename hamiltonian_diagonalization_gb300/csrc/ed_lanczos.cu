@@ -200,11 +200,18 @@ __global__ void __launch_bounds__(kThreads) k_mdot(const double* __restrict__ V,
         int r = lane;
         if (i < J) {
             const double* col = V + (int64_t)i * n + r0;
-            for (; r + 96 < len; r += 128) {
-                a0 = fma(col[r], sw[r], a0);
-                a1 = fma(col[r + 32], sw[r + 32], a1);
-                a2 = fma(col[r + 64], sw[r + 64], a2);
-                a3 = fma(col[r + 96], sw[r + 96], a3);
+            // 16 independent loads per lane in flight, four FMA chains
+            for (; r + 480 < len; r += 512) {
+                double x[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) x[u] = col[r + 32 * u];
+#pragma unroll
+                for (int u = 0; u < 16; u += 4) {
+                    a0 = fma(x[u], sw[r + 32 * u], a0);
+                    a1 = fma(x[u + 1], sw[r + 32 * (u + 1)], a1);
+                    a2 = fma(x[u + 2], sw[r + 32 * (u + 2)], a2);
+                    a3 = fma(x[u + 3], sw[r + 32 * (u + 3)], a3);
+                }
             }
             for (; r < len; r += 32) a0 = fma(col[r], sw[r], a0);
         } else {
@@ -257,17 +264,21 @@ __global__ void __launch_bounds__(kThreads) k_update(const double* __restrict__ 
     chunk(n, gridDim.x, blockIdx.x, r0, r1);
     double nn = 0.0;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
-        double acc = w[r];
+        // eight column loads in flight, two FMA chains (even / odd columns)
+        double acc = w[r], acc2 = 0.0;
         int i = 0;
-        for (; i + 4 <= J; i += 4) {
-            const double v0 = V[(int64_t)i * n + r], v1 = V[(int64_t)(i + 1) * n + r];
-            const double v2 = V[(int64_t)(i + 2) * n + r], v3 = V[(int64_t)(i + 3) * n + r];
-            acc = fma(sc[i], v0, acc);
-            acc = fma(sc[i + 1], v1, acc);
-            acc = fma(sc[i + 2], v2, acc);
-            acc = fma(sc[i + 3], v3, acc);
+        for (; i + 8 <= J; i += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = V[(int64_t)(i + u) * n + r];
+#pragma unroll
+            for (int u = 0; u < 8; u += 2) {
+                acc = fma(sc[i + u], v[u], acc);
+                acc2 = fma(sc[i + u + 1], v[u + 1], acc2);
+            }
         }
         for (; i < J; ++i) acc = fma(sc[i], V[(int64_t)i * n + r], acc);
+        acc += acc2;
         w[r] = acc;
         nn = fma(acc, acc, nn);
     }

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "ed_internal.h"
+#include "ed_lanczos.h"
 
 namespace edgb {
 
@@ -27,7 +28,7 @@ namespace {
 
 typedef __nv_bfloat16 bf16;
 
-constexpr int kIn = 32;
+constexpr int kIn = 64;   // orbital bits, V1, zero padding (up to 63 orbitals)
 constexpr int kOut = 8;
 constexpr int kLayers = 4;
 
@@ -47,17 +48,69 @@ __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// Stage a 64 x 32 tile of an operand into s[row][k] (row = m or n index,
+// stride 40 bf16 = 80 bytes).  The operand is P(mn, k) = P[mn*s_mn + k*s_k];
+// the tile is read in 16-byte pieces along whichever index is contiguous
+// (k when kfast, else mn), with element-wise bounds checks where a piece
+// crosses an edge or is not 16-byte aligned.
+__device__ __forceinline__ void stage_tile(bf16 (*s)[40], const bf16* __restrict__ P, int64_t s_mn, int64_t s_k,
+                                           bool kfast, int mn0, int MN, int k0, int kend)
+{
+    const bf16 zero = __float2bfloat16(0.f);
+    if (kfast) {
+        for (int c = threadIdx.x; c < 256; c += 128) {     // 64 rows x 4 pieces of 8 k
+            const int r = c >> 2, kc = (c & 3) * 8;
+            const int gmn = mn0 + r, gk = k0 + kc;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gmn < MN && gk < kend) {
+                const bf16* src = P + (int64_t)gmn * s_mn + gk;
+                if (gk + 8 <= kend && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                    v = *reinterpret_cast<const uint4*>(src);
+                } else {
+                    __align__(16) bf16 t[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) t[e] = (gk + e < kend) ? src[e] : zero;
+                    v = *reinterpret_cast<const uint4*>(t);
+                }
+            }
+            *reinterpret_cast<uint4*>(&s[r][kc]) = v;
+        }
+    } else {
+        for (int c = threadIdx.x; c < 256; c += 128) {     // 32 k x 8 pieces of 8 rows
+            const int kk = c >> 3, mc = (c & 7) * 8;
+            const int gk = k0 + kk, gmn = mn0 + mc;
+            __align__(16) bf16 t[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) t[e] = zero;
+            if (gk < kend && gmn < MN) {
+                const bf16* src = P + (int64_t)gk * s_k + gmn;
+                if (gmn + 8 <= MN && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                    *reinterpret_cast<uint4*>(t) = *reinterpret_cast<const uint4*>(src);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        if (gmn + e < MN) t[e] = src[e];
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < 8; ++e) s[mc + e][kk] = t[e];
+        }
+    }
+}
+
 template <class Epi>
 __global__ void __launch_bounds__(128) k_gemm(const bf16* __restrict__ A, int64_t sam, int64_t sak,
                                               const bf16* __restrict__ Bm, int64_t sbk, int64_t sbn, int M, int N, int K,
-                                              Epi epi)
+                                              int kchunk, Epi epi)
 {
     __shared__ __align__(16) bf16 sA[64][40];   // [m][k]
     __shared__ __align__(16) bf16 sB[64][40];   // [n][k]
     const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int g = lane >> 2, tq = lane & 3;
+    const bool a_kfast = sak == 1, b_kfast = sbk == 1;
     float acc[2][4][4];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -65,15 +118,9 @@ __global__ void __launch_bounds__(128) k_gemm(const bf16* __restrict__ A, int64_
         for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
-    const bf16 zero = __float2bfloat16(0.f);
-    for (int k0 = 0; k0 < K; k0 += 32) {
-        for (int i = threadIdx.x; i < 64 * 32; i += 128) {
-            const int r = i >> 5, c = i & 31;
-            const int gm = m0 + r, gk = k0 + c;
-            sA[r][c] = (gm < M && gk < K) ? A[(int64_t)gm * sam + (int64_t)gk * sak] : zero;
-            const int gn = n0 + r;
-            sB[r][c] = (gn < N && gk < K) ? Bm[(int64_t)gk * sbk + (int64_t)gn * sbn] : zero;
-        }
+    for (int k0 = kbeg; k0 < kend; k0 += 32) {
+        stage_tile(sA, A, sam, sak, a_kfast, m0, M, k0, kend);
+        stage_tile(sB, Bm, sbn, sbk, b_kfast, n0, N, k0, kend);
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < 32; kk += 16) {
@@ -113,10 +160,11 @@ __global__ void __launch_bounds__(128) k_gemm(const bf16* __restrict__ A, int64_
 
 template <class Epi>
 void gemm(const bf16* A, int64_t sam, int64_t sak, const bf16* B, int64_t sbk, int64_t sbn, int M, int N, int K,
-          Epi epi, cudaStream_t st)
+          Epi epi, cudaStream_t st, int splits = 1)
 {
-    dim3 grid((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64));
-    k_gemm<Epi><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, epi);
+    const int kchunk = ((K + splits - 1) / splits + 31) / 32 * 32;
+    dim3 grid((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64), (unsigned)splits);
+    k_gemm<Epi><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, kchunk, epi);
     count_launch();
     ED_CUDA(cudaGetLastError());
 }
@@ -158,12 +206,27 @@ struct EpiBackData {
     }
 };
 
-// Weight-gradient epilogue: plain FP32 store.
-struct EpiStore {
+// Weight-gradient epilogue of a split-K GEMM: split blockIdx.z stores its
+// partial sum to out[z*zstride + r*ld + c]; k_sum_splits adds the splits.
+struct EpiSplit {
     float* out;
     int ld;
-    __device__ void operator()(int r, int c, float v) const { out[(int64_t)r * ld + c] = v; }
+    int64_t zstride;
+    __device__ void operator()(int r, int c, float v) const
+    {
+        out[(int64_t)blockIdx.z * zstride + (int64_t)r * ld + c] = v;
+    }
 };
+
+// out[i] = sum_z part[z*count + i], splits added in order
+__global__ void k_sum_splits(const float* __restrict__ part, int S, int64_t count, float* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int z = 0; z < S; ++z) s += part[(int64_t)z * count + i];
+        out[i] = s;
+    }
+}
 
 // features of sample i: word bits as +-1, scaled V1, zero padding
 __global__ void k_features(const uint64_t* __restrict__ words, const float* __restrict__ v1, int64_t m, int norb,
@@ -209,27 +272,45 @@ __global__ void k_loss_grad(const float* __restrict__ Z4, const float* __restric
     if (threadIdx.x == 0) atomicAdd(loss, red[0]);
 }
 
-// db[c] = sum_i dZ[i][c]  (one block per column tile, FP32)
-__global__ void k_colsum(const float* __restrict__ dZ, int64_t m, int n, float* __restrict__ db)
+// Column sums of dZ (m x n, FP32) in row chunks: block (x, y) covers columns
+// [32x, 32x+32) of row chunk y with 8 row lanes of 32 consecutive columns
+// (coalesced); part[y*n + c] = the chunk's sum, added up by k_sum_splits.
+__global__ void __launch_bounds__(256) k_colsum_part(const float* __restrict__ dZ, int64_t m, int n,
+                                                     float* __restrict__ part)
 {
-    const int c = blockIdx.x;
-    __shared__ float red[256];
+    __shared__ float red[8][33];
+    const int c = blockIdx.x * 32 + (threadIdx.x & 31), rl = threadIdx.x >> 5;
+    const int64_t r0 = m * blockIdx.y / gridDim.y, r1 = m * (blockIdx.y + 1) / gridDim.y;
     float s = 0.f;
-    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s += dZ[i * n + c];
-    red[threadIdx.x] = s;
+    if (c < n)
+        for (int64_t i = r0 + rl; i < r1; i += 8) s += dZ[i * n + c];
+    red[rl][threadIdx.x & 31] = s;
     __syncthreads();
-    for (int k = 128; k; k >>= 1) {
-        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-        __syncthreads();
+    if (rl == 0 && c < n) {
+        float t = 0.f;
+        for (int l = 0; l < 8; ++l) t += red[l][threadIdx.x];
+        part[(int64_t)blockIdx.y * n + c] = t;
     }
-    if (threadIdx.x == 0) db[c] = red[0];
 }
 
-// Adam on the FP32 masters, refreshing the bf16 copies of the weights.
-__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
-                       float* __restrict__ m2, bf16* __restrict__ pb, int64_t n, float lr, float b1, float b2,
-                       float c1, float c2, float eps)
+// Training counters on the device, so that a captured training step replays
+// with the right values: ctr[0] = Adam step t, ctr[1] = fit step s (both
+// advanced at the start of a step, so 1-based inside it).
+__global__ void k_advance(int64_t* __restrict__ ctr)
 {
+    ctr[0] += 1;
+    ctr[1] += 1;
+}
+
+// Adam on the FP32 masters, refreshing the bf16 copies of the weights.  With
+// fit_total > 0 the rate decays linearly from lr0 to lr0/10 over the fit.
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, bf16* __restrict__ pb, int64_t n, float lr0,
+                       const int64_t* __restrict__ ctr, int64_t fit_total, float b1, float b2, float eps)
+{
+    const float t = (float)ctr[0];
+    const float lr = fit_total > 0 ? lr0 * (1.f - 0.9f * (float)(ctr[1] - 1) / (float)fit_total) : lr0;
+    const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float gi = g[i];
         const float a = b1 * m1[i] + (1.f - b1) * gi;
@@ -254,9 +335,11 @@ __global__ void k_to_bf16(const float* __restrict__ x, bf16* __restrict__ y, int
 // samples draw r with probability |psi_b(r)|^2 from the per-column
 // cumulative table cdf[b][r] (the configurations that carry the overlap).
 __global__ void k_make_batch(const uint64_t* __restrict__ basis, int64_t n, const double* __restrict__ psi, int nv,
-                             const float* __restrict__ v1s, const double* __restrict__ cdf, int64_t m, uint64_t seed,
-                             uint64_t* __restrict__ words, float* __restrict__ v1, float* __restrict__ target)
+                             const float* __restrict__ v1s, const double* __restrict__ cdf, int64_t m, uint64_t seed0,
+                             const int64_t* __restrict__ ctr, uint64_t* __restrict__ words, float* __restrict__ v1,
+                             float* __restrict__ target)
 {
+    const uint64_t seed = seed0 + 0x632BE59BD9B4E019ull * (uint64_t)ctr[1];
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
         uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(s + 1);
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -340,7 +423,8 @@ struct ed_mlp {
     int64_t woff[edgb::kLayers], boff[edgb::kLayers], nparam = 0;
     edgb::DevBuf<float> p, g, m1, m2;    // all parameters (weights then bias per layer)
     edgb::DevBuf<__nv_bfloat16> pb;      // bf16 copies (weights only used)
-    int64_t step = 0;
+    edgb::DevBuf<int64_t> ctr;           // [0] Adam step, [1] fit step (device-side)
+    edgb::DevBuf<float> ws, ws2;         // split-K and column-sum partials
     // activations sized for the largest batch seen
     int64_t cap = 0;
     edgb::DevBuf<__nv_bfloat16> X, Hb[3], dZb[4];
@@ -388,17 +472,28 @@ void mlp_forward(ed_mlp& net, int64_t m, cudaStream_t st)
     }
 }
 
-// backward from dZ[3] (set by the loss) into net.g
+constexpr int kMaxSplits = 16;
+
+// backward from dZ[3] (set by the loss) into net.g.  The weight gradients
+// reduce over the m samples: split-K GEMMs (up to 16 splits of >= 512
+// samples) whose partials k_sum_splits adds in order; the bias gradients are
+// coalesced column sums over up to 16 row chunks.
 void mlp_backward(ed_mlp& net, int64_t m, cudaStream_t st)
 {
+    const int S = (int)std::max<int64_t>(1, std::min<int64_t>(kMaxSplits, m / 512));
+    const int R = (int)std::max<int64_t>(1, std::min<int64_t>(kMaxSplits, m / 256));
     for (int l = kLayers - 1; l >= 0; --l) {
         const int K = net.dims[l], N = net.dims[l + 1];
         // dW_l = in^T dZ_l  (K x N), reduction over the m samples
         const bf16* in = l == 0 ? net.X.p : net.Hb[l - 1].p;
         const int ldin = l == 0 ? kIn : net.dims[l];
-        EpiStore es{net.g.p + net.woff[l], N};
-        gemm(in, 1, ldin, net.dZb[l].p, N, 1, K, N, (int)m, es, st);
-        k_colsum<<<N, 256, 0, st>>>(net.dZf[l].p, m, N, net.g.p + net.boff[l]);
+        EpiSplit es{net.ws.p, N, (int64_t)K * N};
+        gemm(in, 1, ldin, net.dZb[l].p, N, 1, K, N, (int)m, es, st, S);
+        k_sum_splits<<<grid_sz((int64_t)K * N), 256, 0, st>>>(net.ws.p, S, (int64_t)K * N, net.g.p + net.woff[l]);
+        count_launch();
+        k_colsum_part<<<dim3((unsigned)((N + 31) / 32), (unsigned)R), 256, 0, st>>>(net.dZf[l].p, m, N, net.ws2.p);
+        count_launch();
+        k_sum_splits<<<grid_sz(N), 256, 0, st>>>(net.ws2.p, R, N, net.g.p + net.boff[l]);
         count_launch();
         if (l > 0) {
             // dZ_{l-1} = (dZ_l W_l^T) * SiLU'(Z_{l-1})
@@ -425,13 +520,12 @@ double mlp_loss(ed_mlp& net, const float* target, int64_t m, cudaStream_t st)
     return l / (double)m;
 }
 
-void mlp_adam(ed_mlp& net, float lr, cudaStream_t st)
+void mlp_adam(ed_mlp& net, float lr, int64_t fit_total, cudaStream_t st)
 {
-    net.step++;
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = 1.f - std::pow(b1, (float)net.step), c2 = 1.f - std::pow(b2, (float)net.step);
-    k_adam<<<grid_sz(net.nparam), 256, 0, st>>>(net.p.p, net.g.p, net.m1.p, net.m2.p, net.pb.p, net.nparam, lr, b1, b2,
-                                                c1, c2, 1e-8f);
+    k_advance<<<1, 1, 0, st>>>(net.ctr.p);
+    count_launch();
+    k_adam<<<grid_sz(net.nparam), 256, 0, st>>>(net.p.p, net.g.p, net.m1.p, net.m2.p, net.pb.p, net.nparam, lr,
+                                                net.ctr.p, fit_total, 0.9f, 0.999f, 1e-8f);
     count_launch();
 }
 
@@ -447,7 +541,7 @@ ed_status ed_mlp_create(int norb, int hidden, uint64_t seed, ed_mlp** out)
 {
     return guard([&] {
         ED_REQUIRE(out, ED_ERR_ARG, "NULL output");
-        ED_REQUIRE(norb >= 2 && norb < kIn, ED_ERR_RANGE, "the network takes up to 31 orbitals");
+        ED_REQUIRE(norb >= 2 && norb < kIn && norb <= kMaxOrbitals, ED_ERR_RANGE, "orbital count out of range");
         ED_REQUIRE(hidden >= 64 && hidden % 64 == 0 && hidden <= 1024, ED_ERR_ARG, "hidden width: multiple of 64");
         ed_mlp* net = new ed_mlp();
         try {
@@ -479,6 +573,10 @@ ed_status ed_mlp_create(int norb, int hidden, uint64_t seed, ed_mlp** out)
             ED_CUDA(cudaMemcpy(net->p.p, h.data(), off * 4, cudaMemcpyHostToDevice));
             ED_CUDA(cudaMemset(net->m1.p, 0, off * 4));
             ED_CUDA(cudaMemset(net->m2.p, 0, off * 4));
+            net->ctr.alloc(2);
+            ED_CUDA(cudaMemset(net->ctr.p, 0, 2 * sizeof(int64_t)));
+            net->ws.alloc((size_t)kMaxSplits * hidden * std::max(hidden, kIn));
+            net->ws2.alloc((size_t)kMaxSplits * hidden);
             k_to_bf16<<<grid_sz(off), 256>>>(net->p.p, net->pb.p, off);
             count_launch();
             ED_CUDA(cudaDeviceSynchronize());
@@ -560,7 +658,7 @@ ed_status ed_mlp_train_step(ed_mlp* net, const uint64_t* words_dev, const float*
         mlp_forward(*net, m, nullptr);
         const double l = mlp_loss(*net, target_dev, m, nullptr);
         mlp_backward(*net, m, nullptr);
-        mlp_adam(*net, lr, nullptr);
+        mlp_adam(*net, lr, 0, nullptr);
         if (loss_host) *loss_host = l;
     });
 }
@@ -619,27 +717,56 @@ ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* basis, const double* v1_host, 
         }
         DevBuf<double> cdf(hc.size());
         ED_CUDA(cudaMemcpy(cdf.p, hc.data(), hc.size() * 8, cudaMemcpyHostToDevice));
-        double l = 0.0;
-        for (int s = 0; s < steps; ++s) {
-            // linear decay to a tenth of the rate over the run
-            const float lr_s = lr * (1.f - 0.9f * (float)s / (float)steps);
-            k_make_batch<<<grid_sz(batch), 256>>>(basis->words.p, n, psi_g.p, nv, dv1.p, cdf.p, batch,
-                                                   seed + 0x632BE59BD9B4E019ull * (uint64_t)(s + 1), net->words.p,
-                                                   net->v1.p, net->target.p);
+        // One training step (batch draw, forward, loss, backward, Adam with
+        // the rate decaying linearly to a tenth over the fit) reads its seed
+        // and rates from the device counters, so it is captured once as a
+        // CUDA graph on a private stream and replayed `steps` times.
+        SolveStream ss(nullptr);
+        cudaStream_t st = ss.s;
+        ED_CUDA(cudaMemsetAsync(net->ctr.p + 1, 0, sizeof(int64_t), st));
+        auto step = [&]() {
+            k_make_batch<<<grid_sz(batch), 256, 0, st>>>(basis->words.p, n, psi_g.p, nv, dv1.p, cdf.p, batch, seed,
+                                                         net->ctr.p, net->words.p, net->v1.p, net->target.p);
             count_launch();
-            mlp_features(*net, net->words.p, net->v1.p, batch, nullptr);
-            mlp_forward(*net, batch, nullptr);
-            const bool report = (s + 1 == steps) || ((s & 63) == 0);
-            if (report) l = mlp_loss(*net, net->target.p, batch, nullptr);
-            else {
-                k_loss_grad<<<grid_sz(batch), 256>>>(net->Z[3].p, net->target.p, batch, net->dZb[3].p,
-                                                     net->dZf[3].p, net->loss.p);
-                count_launch();
-            }
-            mlp_backward(*net, batch, nullptr);
-            mlp_adam(*net, lr_s, nullptr);
+            mlp_features(*net, net->words.p, net->v1.p, batch, st);
+            mlp_forward(*net, batch, st);
+            ED_CUDA(cudaMemsetAsync(net->loss.p, 0, 8, st));
+            k_loss_grad<<<grid_sz(batch), 256, 0, st>>>(net->Z[3].p, net->target.p, batch, net->dZb[3].p,
+                                                        net->dZf[3].p, net->loss.p);
+            count_launch();
+            mlp_backward(*net, batch, st);
+            mlp_adam(*net, lr, steps, st);
+        };
+        const uint64_t c0 = launch_count();
+        ED_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+        try {
+            step();
+        } catch (...) {
+            cudaGraph_t broken = nullptr;
+            cudaStreamEndCapture(st, &broken);
+            if (broken) cudaGraphDestroy(broken);
+            throw;
         }
-        ED_CUDA(cudaStreamSynchronize(nullptr));
+        cudaGraph_t graph = nullptr;
+        ED_CUDA(cudaStreamEndCapture(st, &graph));
+        const int64_t kernels = (int64_t)(launch_count() - c0);
+        count_launches(-kernels);
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ge = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ED_CUDA(ge);
+        struct ExecGuard {
+            cudaGraphExec_t e;
+            ~ExecGuard() { cudaGraphExecDestroy(e); }
+        } eg{exec};
+        for (int s = 0; s < steps; ++s) {
+            ED_CUDA(cudaGraphLaunch(exec, st));
+            count_launches(kernels);
+        }
+        double l = 0.0;
+        ED_CUDA(cudaMemcpyAsync(&l, net->loss.p, 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        l /= (double)batch;
         if (final_loss) *final_loss = l;
     });
 }

@@ -46,7 +46,7 @@ def run_plain(N, norb, sectors, v1s, nev, tol, seed):
     return time.perf_counter() - t0, evals, products
 
 
-def run_batched(N, norb, sectors, v1s, nev, tol, seed, batch_size=0):
+def run_batched(N, norb, sectors, v1s, nev, tol, seed, batch_size=0, ncv=0):
     """Each sector's Hamiltonians in batches of batch_size (0: all at once);
     a batch's [row][problem] vectors should stay within L2 for the block
     product's gathers to hit it."""
@@ -64,7 +64,7 @@ def run_batched(N, norb, sectors, v1s, nev, tol, seed, batch_size=0):
         b.GenerateFockSpace(N, norb, tlz)
         for j0 in range(0, len(lists), bs):
             batch = ed.HamiltonianBatch(b, lists[j0:j0 + bs])
-            ev, _, info = batch.solve(nev, tol=tol, seed=seed)
+            ev, _, info = batch.solve(nev, tol=tol, seed=seed, ncv=ncv)
             infos.append(info)
             for j in range(len(lists[j0:j0 + bs])):
                 evals[(tlz, j0 + j)] = ev[j]
@@ -72,8 +72,8 @@ def run_batched(N, norb, sectors, v1s, nev, tol, seed, batch_size=0):
     return time.perf_counter() - t0, evals, infos
 
 
-def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=2000, batch=4096, lr=1e-3,
-             hidden=256):
+def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=4000, batch=4096, lr=2e-3,
+             hidden=256, batch_size=0, ncv=0):
     """Batched + learned warm start.  Per sector: solve the training V1 points
     (a seeded random 3/4 of them) batched from random starts, fit the MLP on
     their ground states, then solve the held-out points batched from the
@@ -95,24 +95,31 @@ def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=2000, 
         t0 = time.perf_counter()
         b = ed.FermionFockBasis()
         b.GenerateFockSpace(N, norb, tlz)
-        bt = ed.HamiltonianBatch(b, [lists[j] for j in train])
-        ev_t, vec_t, inf_t = bt.solve(nev, tol=tol, seed=seed, want_vectors=True)
+        bs = batch_size or len(train)
+        ev_parts, psi_parts, inf_t = [], [], {"block_products": 0}
+        for j0 in range(0, len(train), bs):
+            bt = ed.HamiltonianBatch(b, [lists[j] for j in train[j0:j0 + bs]])
+            e, v, i = bt.solve(nev, tol=tol, seed=seed, want_vectors=True, ncv=ncv)
+            ev_parts.append(e)
+            psi_parts.append(v[0])
+            inf_t["block_products"] += i["block_products"]
+        ev_t = np.concatenate(ev_parts)
+        psi = torch.cat(psi_parts, dim=1).contiguous()
         t1 = time.perf_counter()
         net = ed.WarmStartMLP(norb, hidden, seed=seed)
-        psi = vec_t[0].contiguous()
         loss = net.fit(b, v1s[train], psi, steps=steps, batch=batch, lr=lr, seed=seed + 1)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         bh = ed.HamiltonianBatch(b, [lists[j] for j in held])
         V0 = torch.empty((bh.n, len(held)), dtype=torch.float64, device="cuda")
         net.warm_start(b, v1s[held], V0)
-        ev_w, vec_w, inf_w = bh.solve(nev, tol=tol, V0=V0, want_vectors=True)
+        ev_w, vec_w, inf_w = bh.solve(nev, tol=tol, V0=V0, want_vectors=True, ncv=ncv)
         torch.cuda.synchronize()
         t3 = time.perf_counter()
         total += t3 - t0
         # held-out from random starts, for the comparison only (not timed into the sweep)
         t4 = time.perf_counter()
-        ev_r, _, inf_r = bh.solve(nev, tol=tol, seed=seed + 2)
+        ev_r, _, inf_r = bh.solve(nev, tol=tol, seed=seed + 2, ncv=ncv)
         t5 = time.perf_counter()
         P = V0.cpu().numpy()
         T = vec_w[0].cpu().numpy()
@@ -141,8 +148,10 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--mode", default="both", choices=["plain", "batched", "both", "warm", "all"])
-    ap.add_argument("--mlp-steps", type=int, default=2000)
+    ap.add_argument("--mlp-steps", type=int, default=4000)
+    ap.add_argument("--mlp-lr", type=float, default=2e-3)
     ap.add_argument("--batch-size", type=int, default=0, help="Hamiltonians per batch (0: all of a sector)")
+    ap.add_argument("--ncv", type=int, default=0, help="Krylov dimension of the batched solves (0: 2*nev+21)")
     args = ap.parse_args()
     sectors = [int(s) for s in args.sectors.split(",")]
     v1s = np.linspace(0.5, 3.0, args.points)
@@ -150,12 +159,14 @@ def main():
     out = {"N": args.N, "norb": args.norb, "sectors": sectors, "points": args.points, "nev": args.nev,
            "tol": args.tol, "solves": nsolve}
     if args.mode in ("warm", "all"):
-        tw, ew, rec = run_warm(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, steps=args.mlp_steps)
+        tw, ew, rec = run_warm(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, steps=args.mlp_steps,
+                               lr=args.mlp_lr, batch_size=args.batch_size, ncv=args.ncv)
         out["batched_warm"] = {"seconds": tw, "solves_per_s": nsolve / tw, "per_sector": rec}
     if args.mode in ("batched", "both", "all"):
         # one untimed warm-up batch (module load, autotune code paths)
         run_batched(args.N, args.norb, sectors[:1], v1s[:2], args.nev, args.tol, args.seed)
-        tb, eb, infos = run_batched(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, args.batch_size)
+        tb, eb, infos = run_batched(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, args.batch_size,
+                                    args.ncv)
         out["batched"] = {"seconds": tb, "solves_per_s": nsolve / tb,
                           "block_products": [i["block_products"] for i in infos],
                           "restarts": [i["restarts"] for i in infos],

@@ -249,6 +249,8 @@ typedef struct {
     int tile_unroll;          /* autotuned loads in flight per lane                  */
     int tile_l1;              /* 1: hop values read through L1, 0: staged in shared memory */
     int tile_threads;         /* threads per CTA of the block product                */
+    int64_t problem_products; /* sum over block products of the Hamiltonians still
+                                 iterating (converged ones retire at restarts)        */
 } ed_batch_info;
 
 /* Shared pattern (int32 column + uint16 hop code per element) built once on

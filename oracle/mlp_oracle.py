@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-K_IN, K_OUT = 32, 8
+K_IN, K_OUT = 64, 8
 
 
 def bf16(x):
