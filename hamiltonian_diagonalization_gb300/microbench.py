@@ -1,12 +1,16 @@
 """Micro-benchmark of the Hamiltonian-vector products on one GPU.
 
     python -m hamiltonian_diagonalization_gb300.microbench --sector 11,31,0 --reps 20 [--upper] [--matfree]
+    python -m hamiltonian_diagonalization_gb300.microbench --sector 10,28,0 --batch 32 --reps 20
 
 Builds the sector's Hamiltonian (LLL Coulomb pseudopotentials, odd m) on the
 device, then times `reps` products with CUDA events on the launching stream
 and prints one JSON line: dimension, stored nonzeros, ms per product,
 algorithmic bytes per product (nnz*(8+4) + (n+1)*8 + 2*n*8 for stored CRS)
 and the implied GB/s.  Used for the SpMV roofline and its ncu profiles.
+With --batch B it times the block product of B Hamiltonians of the sector
+(the V1 sweep's shared pattern, ed_batch_spmm) instead and reports FP64 FMAs
+per second (one FMA per stored element per Hamiltonian, diagonal included).
 """
 from __future__ import annotations
 
@@ -24,6 +28,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--upper", action="store_true", help="store the upper triangle (the reference's layout)")
     ap.add_argument("--matfree", action="store_true", help="regenerate elements on the fly")
+    ap.add_argument("--batch", type=int, default=0, help="time the block product of this many Hamiltonians")
+    ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default tile (32 per row, L1)")
     args = ap.parse_args()
     import torch
 
@@ -31,6 +37,8 @@ def main():
     from hamiltonian_diagonalization_gb300 import _capi as C
 
     N, norb, tlz = (int(x) for x in args.sector.split(","))
+    if args.batch:
+        return batch_main(ed, C, torch, N, norb, tlz, args)
     H = ed.SpinlessFermionHamiltonian()
     H.Initialize(N, norb, twoLz=tlz)
     T = ed.QuarticTermTables(norb, ed.odd_coulomb_list(norb))
@@ -57,6 +65,35 @@ def main():
         by = nnz * 12 + (n + 1) * 8 + 2 * n * 8
         out.update({"nnz": nnz, "bytes_per_product": by, "GBps": by / ms / 1e6})
     print(json.dumps(out))
+
+
+def batch_main(ed, C, torch, N, norb, tlz, args):
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(N, norb, tlz)
+    base = ed.odd_coulomb_list(norb)
+    lists = []
+    for v1 in np.linspace(0.5, 3.0, args.batch):
+        v = base.copy()
+        v[1] = v1
+        lists.append(v)
+    bt = ed.HamiltonianBatch(b, lists, autotune=not args.no_autotune)
+    n, B = bt.n, bt.nham
+    X = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, (n, B))).cuda()
+    Y = torch.empty_like(X)
+    for _ in range(args.warmup):
+        bt.spmm(X, Y)
+    torch.cuda.synchronize()
+    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.reps):
+        bt.spmm(X, Y)
+    e.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(e) / args.reps
+    fma = (bt.nnz + n) * B
+    print(json.dumps({"sector": [N, norb, tlz], "n": n, "mode": "batch", "hamiltonians": B, "nnz_offdiag": bt.nnz,
+                      "ms_per_block_product": ms, "ms_per_hamiltonian_product": ms / B,
+                      "fp64_fma_per_s": fma / ms * 1e3, "fp64_tflops": 2 * fma / ms / 1e9}))
 
 
 if __name__ == "__main__":
