@@ -17,6 +17,8 @@ from .host import (  # noqa: F401
     clebsch_gordan,
     coulomb_pseudopotentials,
     dense_sym_eigen,
+    eigensystem_from_file,
+    eigensystem_to_file,
     odd_coulomb_list,
     solve_sector,
 )

@@ -96,6 +96,14 @@ _SIGS = {
     "ed_lanczos_device": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(SolveInfo)]),
     "ed_residuals": (c_int, [c_void_p, c_void_p, P(c_double), c_int, P(c_double)]),
     "ed_residuals_noalloc": (c_int, [c_void_p, c_void_p, P(c_double), c_int, P(c_double)]),
+    "ed_basis_rotate": (c_int, [c_void_p, c_i64, c_int, P(c_double), c_int, c_int, c_void_p, c_int]),
+    "ed_eigensystem_write": (c_int, [ctypes.c_char_p, c_int, c_int, P(c_double), ctypes.c_uint64, P(c_double)]),
+    "ed_eigensystem_read": (c_int, [ctypes.c_char_p, c_int, P(c_int), P(c_double), P(ctypes.c_uint64),
+                                    P(c_double)]),
+    "ed_crs_write": (c_int, [c_void_p, ctypes.c_char_p, c_int]),
+    "ed_crs_read": (c_int, [ctypes.c_char_p, c_int, c_int, P(c_void_p)]),
+    "ed_quartic_tables_write": (c_int, [ctypes.c_char_p, c_int, c_int, P(ctypes.c_uint16), P(c_double)]),
+    "ed_quartic_tables_read": (c_int, [ctypes.c_char_p, c_int, P(c_int), P(ctypes.c_uint16), P(c_double)]),
     "ed_kernel_launches": (c_u64, []),
     "ed_dense_sym_eigen": (c_int, [c_int, P(c_double), P(c_double), P(c_double)]),
     "ed_solve_sector": (c_int, [c_int, c_int, c_int, P(c_double), c_int, c_int, P(LanczosParams), P(c_double),

@@ -99,6 +99,10 @@ struct DevBuf {
         n = 0;
     }
     size_t bytes() const { return n * sizeof(T); }
+    // grow (without keeping the contents) when fewer than count elements are held
+    void alloc_at_least(size_t count) {
+        if (count > n) alloc(count);
+    }
 };
 
 // ------------------------------------------------------------ host tables

@@ -310,35 +310,6 @@ __global__ void __launch_bounds__(kThreads) k_scale(double* __restrict__ w, int6
         w[r] *= inv;
 }
 
-// out[:, t] = sum_{i<m} V[:, i] Y[i, t] for t < k (Y column-major, ld m).
-constexpr int kGT = 16;
-__global__ void __launch_bounds__(kThreads) k_gemm_vy(const double* __restrict__ V, int64_t n, int m,
-                                                      const double* __restrict__ Y, int ldy, int k,
-                                                      double* __restrict__ out)
-{
-    extern __shared__ double sy[];   // m * kGT
-    for (int t0 = 0; t0 < k; t0 += kGT) {
-        const int tn = min(kGT, k - t0);
-        __syncthreads();
-        for (int q = threadIdx.x; q < m * kGT; q += kThreads) {
-            const int i = q / kGT, t = q % kGT;
-            sy[q] = (t < tn) ? Y[(int64_t)(t0 + t) * ldy + i] : 0.0;
-        }
-        __syncthreads();
-        for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads) {
-            double acc[kGT];
-#pragma unroll
-            for (int t = 0; t < kGT; ++t) acc[t] = 0.0;
-            for (int i = 0; i < m; ++i) {
-                const double v = V[(int64_t)i * n + r];
-#pragma unroll
-                for (int t = 0; t < kGT; ++t) acc[t] = fma(v, sy[i * kGT + t], acc[t]);
-            }
-            for (int t = 0; t < tn; ++t) out[(int64_t)(t0 + t) * n + r] = acc[t];
-        }
-    }
-}
-
 // Seeded uniform(-1,1) vector (splitmix64 of seed and index).
 __global__ void k_random(double* __restrict__ v, int64_t n, uint64_t seed)
 {
@@ -413,6 +384,7 @@ struct Work {
     DevBuf<int> flags;               // [0] second pass wanted, [1] breakdown step + 1
     DevBuf<unsigned int> counters;   // last-block counters: [0] local dot, [1] multi-dot, [2] update
     DevBuf<double> Y;                // m x m Ritz coefficients
+    RotateScratch rot;               // restart rotation scratch
 
     void mdot(const double* Vb, int J, double* x, int local, const double* alpha, const double* beta_prev,
               double* coefcol, double* before, const int* run, const int* stop, cudaStream_t st)
@@ -461,14 +433,6 @@ double orthonormalise_column(Work& w, double* Vbase, int col, cudaStream_t st)
     ED_CUDA(cudaGetLastError());
     ED_CUDA(cudaStreamSynchronize(st));
     return nrm;
-}
-
-void gemm_vy(const double* V, int64_t n, int m, const double* Ydev, int ldy, int k, double* out, cudaStream_t st)
-{
-    const size_t smem = (size_t)m * kGT * 8;
-    if (smem > 48 * 1024) ED_CUDA(cudaFuncSetAttribute(k_gemm_vy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_gemm_vy<<<sm_count() * 4, kThreads, smem, st>>>(V, n, m, Ydev, ldy, k, out); ::edgb::count_launch();
-    ED_CUDA(cudaGetLastError());
 }
 
 void dense_solve(const ed_op& op, int nev, double* evals_host, double* evecs_dev, ed_solve_info* info,
@@ -735,8 +699,7 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
         int kk = std::min(m - 2, nev + std::max(1, (m - nev) / 2));
         kk = std::max(kk, std::min(nev, m - 1));
         if (hstop) kk = std::min(kk, m_eff);
-        ED_CUDA(cudaMemcpyAsync(w.Y.p, Y.data(), (size_t)m_eff * m_eff * 8, cudaMemcpyHostToDevice, st));
-        gemm_vy(w.V.p, n, m_eff, w.Y.p, m_eff, kk, w.V2.p, st);
+        rotate_basis(w.V.p, n, m_eff, Y.data(), m_eff, kk, w.V2.p, w.rot, 0, st);
         if (!hstop) {
             ED_CUDA(cudaMemcpyAsync(w.V2.p + (int64_t)kk * n, w.V.p + (int64_t)m * n, (size_t)n * 8,
                                     cudaMemcpyDeviceToDevice, st));
@@ -771,8 +734,7 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     }
     if (X) {
         if (nfound < nev) ED_CUDA(cudaMemsetAsync(X, 0, (size_t)n * nev * 8, st));
-        ED_CUDA(cudaMemcpyAsync(w.Y.p, Y.data(), (size_t)m_eff * m_eff * 8, cudaMemcpyHostToDevice, st));
-        gemm_vy(w.V.p, n, m_eff, w.Y.p, m_eff, nfound, X, st);
+        rotate_basis(w.V.p, n, m_eff, Y.data(), m_eff, nfound, X, w.rot, 0, st);
     }
     if (p.verify && X && nfound == nev) {
         std::vector<double> res(nev);

@@ -61,6 +61,21 @@ struct SolveStream {
     }
 };
 
+// Thick-restart basis rotation out[:, c] = sum_j V[:, j] Y[j, c], c < k
+// (V n x m and out n x k column-major on the device, Y host, column-major with
+// leading dimension ldy).  method 0: tensor cores (FP64-accurate digit
+// splitting) when m <= kRotateTensorMaxM, else FP64; 1: FP64; 2: tensor cores.
+constexpr int kRotateTensorMaxM = 64;
+struct RotateScratch {
+    DevBuf<double> y;
+    DevBuf<uint16_t> ydig;
+    DevBuf<int> yexp;
+    std::vector<uint16_t> ydig_h;
+    std::vector<int> yexp_h;
+};
+void rotate_basis(const double* V, int64_t n, int m, const double* Y_host, int ldy, int k, double* out,
+                  RotateScratch& sc, int method, cudaStream_t st);
+
 void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st);
 // Lowest p.nev eigenpairs; v0_dev may be null; evecs_dev (n*nev) may be null.
 void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,

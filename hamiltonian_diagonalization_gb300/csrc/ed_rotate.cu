@@ -1,0 +1,309 @@
+// Thick-restart basis rotation out[:, c] = sum_j V[:, j] Y[j, c] (K7): the
+// n x m by m x k product that turns the Krylov basis into Ritz vectors at
+// every restart (n*m*k FP64 multiply-adds, 1.4e9 at the headline size).
+//
+// Two kernels:
+//  - k_gemm_vy: plain FP64 (one thread per row, Y staged in shared memory);
+//  - k_rotate_oz: the same product on the BF16 tensor cores with FP64
+//    accuracy, by error-free splitting (the Ozaki scheme: Ozaki, Ogita,
+//    Oishi & Rump, Numer. Algorithms 59 (2012)).  Every row r of V is written
+//    as 2^e_r * sum_t a_t 2^(-7(t+1)) with eight signed 7-bit digits a_t, every
+//    column c of Y as 2^f_c * sum_u b_u 2^(-7(u+1)); digits are extracted from
+//    the FP64 bit patterns with integer operations.  A digit (|a| <= 127) is
+//    exact in bfloat16, a digit product (< 2^14) exact in the FP32
+//    accumulator, and the group C_d = sum_{t+u=d} sum_j a_t[j] b_u[j] of one
+//    anti-diagonal d stays an integer below 8 * 64 * 127^2 < 2^23 for
+//    m <= 64, so mma.sync accumulates it exactly.  The groups d = 0..9 are
+//    combined in FP64, out = 2^(e_r+f_c) sum_d 2^(-7(d+2)) C_d; the dropped
+//    groups d >= 10 weigh below 1e-18 of 2^(e_r+f_c), so the result is at
+//    least as accurate as an FP64 dot product (whose rounding is ~m * 1e-16).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "ed_lanczos.h"
+
+namespace edgb {
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kThreads = 256;
+constexpr int kGT = 16;
+constexpr int kOzRows = 64;      // rows of V per CTA
+constexpr int kOzCols = 32;      // columns of the output per CTA
+constexpr int kOzPlanes = 8;     // 7-bit digits per operand (56 bits)
+constexpr int kOzGroups = 10;    // anti-diagonals d = t + u kept: 0..9 (49 digit pairs)
+
+int rot_sms()
+{
+    int dev = 0, s = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return s;
+}
+
+// out[:, t] = sum_{i<m} V[:, i] Y[i, t] for t < k (Y column-major, ld m), FP64.
+__global__ void __launch_bounds__(kThreads) k_gemm_vy(const double* __restrict__ V, int64_t n, int m,
+                                                      const double* __restrict__ Y, int ldy, int k,
+                                                      double* __restrict__ out)
+{
+    extern __shared__ double sy[];   // m * kGT
+    for (int t0 = 0; t0 < k; t0 += kGT) {
+        const int tn = min(kGT, k - t0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < m * kGT; q += kThreads) {
+            const int i = q / kGT, t = q % kGT;
+            sy[q] = (t < tn) ? Y[(int64_t)(t0 + t) * ldy + i] : 0.0;
+        }
+        __syncthreads();
+        for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads) {
+            double acc[kGT];
+#pragma unroll
+            for (int t = 0; t < kGT; ++t) acc[t] = 0.0;
+            for (int i = 0; i < m; ++i) {
+                const double v = V[(int64_t)i * n + r];
+#pragma unroll
+                for (int t = 0; t < kGT; ++t) acc[t] = fma(v, sy[i * kGT + t], acc[t]);
+            }
+            for (int t = 0; t < tn; ++t) out[(int64_t)(t0 + t) * n + r] = acc[t];
+        }
+    }
+}
+
+// Biased exponent field of an FP64 value, 0 for zero and subnormals.
+__host__ __device__ __forceinline__ int exp_field(double v)
+{
+    uint64_t b;
+    memcpy(&b, &v, 8);
+    return (int)((b >> 52) & 0x7FF);
+}
+
+// Eight signed 7-bit digits of v / 2^e with |v| < 2^e: the 56-bit fixed-point
+// magnitude F = |v| 2^(56-e) (truncated) split into 7-bit groups, most
+// significant first.  Subnormals read as zero.
+__host__ __device__ __forceinline__ void digits7(double v, int e, int* d)
+{
+    uint64_t b;
+    memcpy(&b, &v, 8);
+    const int E = (int)((b >> 52) & 0x7FF);
+    if (E == 0) {
+        for (int t = 0; t < kOzPlanes; ++t) d[t] = 0;
+        return;
+    }
+    const uint64_t M = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int s = E - 1075 - e + 56;          // <= 3 because |v| < 2^e
+    const uint64_t F = s >= 0 ? (M << s) : (s > -64 ? (M >> -s) : 0ull);
+    const bool neg = (b >> 63) != 0;
+    for (int t = 0; t < kOzPlanes; ++t) {
+        const int x = (int)((F >> (49 - 7 * t)) & 127u);
+        d[t] = neg ? -x : x;
+    }
+}
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// One CTA: rows [r0, r0+64) of V against columns [c0, c0+32) of Y.
+// ydig: digit planes of Y for this column block, [plane][column][MP] bf16;
+// yexp: f_c per column.  Dynamic shared memory: the V digit planes
+// [8][64][MP+8], the Y planes [8][32][MP+8] and the 64 row exponents.
+template <int MP>
+__global__ void __launch_bounds__(128) k_rotate_oz(const double* __restrict__ V, int64_t n, int m,
+                                                   const bf16* __restrict__ ydig, const int* __restrict__ yexp,
+                                                   int k, double* __restrict__ out)
+{
+    constexpr int LD = MP + 8;   // row stride in bf16: conflict-free fragment loads
+    extern __shared__ __align__(16) unsigned char smem[];
+    bf16* sA = reinterpret_cast<bf16*>(smem);                       // [8][64][LD]
+    bf16* sB = sA + kOzPlanes * kOzRows * LD;                       // [8][32][LD]
+    int* se = reinterpret_cast<int*>(sB + kOzPlanes * kOzCols * LD);  // [64]
+    const int64_t r0 = (int64_t)blockIdx.x * kOzRows;
+    const int cb = blockIdx.y;
+    const int c0 = cb * kOzCols;
+    const bf16* yblk = ydig + (size_t)cb * kOzPlanes * kOzCols * MP;
+
+    for (int i = threadIdx.x; i < kOzRows; i += 128) se[i] = 0;
+    // Y planes: plain copy of this column block (MP is a multiple of 16)
+    for (int i = threadIdx.x; i < kOzPlanes * kOzCols * MP / 8; i += 128) {
+        const int e0 = i * 8;
+        const int pc = e0 / MP, j = e0 - pc * MP;                    // pc = plane*32 + column
+        *reinterpret_cast<uint4*>(sB + (size_t)pc * LD + j) = *reinterpret_cast<const uint4*>(yblk + e0);
+    }
+    __syncthreads();
+    // row exponents e_r = max over the row of (E - 1022), so |V[r][j]| < 2^e_r
+    for (int i = threadIdx.x; i < kOzRows * m; i += 128) {
+        const int rl = i % kOzRows, j = i / kOzRows;
+        const int64_t r = r0 + rl;
+        if (r < n) {
+            const int E = exp_field(V[(int64_t)j * n + r]);
+            if (E) atomicMax(&se[rl], E);
+        }
+    }
+    __syncthreads();
+    // V digit planes (zero beyond m and beyond n)
+    for (int i = threadIdx.x; i < kOzRows * MP; i += 128) {
+        const int rl = i % kOzRows, j = i / kOzRows;
+        const int64_t r = r0 + rl;
+        int d[kOzPlanes];
+        if (r < n && j < m && se[rl]) {
+            digits7(V[(int64_t)j * n + r], se[rl] - 1022, d);
+        } else {
+#pragma unroll
+            for (int t = 0; t < kOzPlanes; ++t) d[t] = 0;
+        }
+#pragma unroll
+        for (int t = 0; t < kOzPlanes; ++t) sA[((size_t)t * kOzRows + rl) * LD + j] = __int2bfloat16_rn(d[t]);
+    }
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, tq = lane & 3;
+    const int wr = warp * 16;                  // the warp's 16 rows
+    double dacc[4][4];
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) dacc[ni][e] = 0.0;
+    for (int dg = kOzGroups - 1; dg >= 0; --dg) {   // anti-diagonals 9..0, smallest first
+        float acc[4][4];
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[ni][e] = 0.f;
+        for (int t = max(0, dg - (kOzPlanes - 1)); t <= min(dg, kOzPlanes - 1); ++t) {
+            const int u = dg - t;
+            const bf16* A = sA + (size_t)t * kOzRows * LD;
+            const bf16* Bp = sB + (size_t)u * kOzCols * LD;
+#pragma unroll
+            for (int kk = 0; kk < MP; kk += 16) {
+                uint32_t af[4], bfr[4][2];
+                af[0] = *reinterpret_cast<const uint32_t*>(A + (wr + g) * LD + kk + tq * 2);
+                af[1] = *reinterpret_cast<const uint32_t*>(A + (wr + g + 8) * LD + kk + tq * 2);
+                af[2] = *reinterpret_cast<const uint32_t*>(A + (wr + g) * LD + kk + tq * 2 + 8);
+                af[3] = *reinterpret_cast<const uint32_t*>(A + (wr + g + 8) * LD + kk + tq * 2 + 8);
+#pragma unroll
+                for (int ni = 0; ni < 4; ++ni) {
+                    bfr[ni][0] = *reinterpret_cast<const uint32_t*>(Bp + (ni * 8 + g) * LD + kk + tq * 2);
+                    bfr[ni][1] = *reinterpret_cast<const uint32_t*>(Bp + (ni * 8 + g) * LD + kk + tq * 2 + 8);
+                }
+#pragma unroll
+                for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[ni], af, bfr[ni]);
+            }
+        }
+        const double w = ldexp(1.0, -7 * (dg + 2));
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) dacc[ni][e] = fma((double)acc[ni][e], w, dacc[ni][e]);
+    }
+    // scale by 2^(e_r + f_c) and store (column-major output)
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int rl = wr + g + ((e >= 2) ? 8 : 0);
+            const int cl = ni * 8 + tq * 2 + (e & 1);
+            const int64_t r = r0 + rl;
+            const int c = c0 + cl;
+            if (r < n && c < k) {
+                const int er = se[rl], fc = yexp[c];
+                const double v = (er && fc) ? ldexp(dacc[ni][e], (er - 1022) + (fc - 1022)) : 0.0;
+                out[(int64_t)c * n + r] = v;
+            }
+        }
+}
+
+template <int MP>
+void launch_rotate_oz(const double* V, int64_t n, int m, const bf16* ydig, const int* yexp, int k, double* out,
+                      cudaStream_t st)
+{
+    constexpr int LD = MP + 8;
+    const size_t smem = (size_t)kOzPlanes * (kOzRows + kOzCols) * LD * 2 + kOzRows * 4;
+    ED_CUDA(cudaFuncSetAttribute(k_rotate_oz<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((n + kOzRows - 1) / kOzRows), (unsigned)((k + kOzCols - 1) / kOzCols));
+    k_rotate_oz<MP><<<grid, 128, smem, st>>>(V, n, m, ydig, yexp, k, out);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+void rotate_basis(const double* V, int64_t n, int m, const double* Y_host, int ldy, int k, double* out,
+                  RotateScratch& sc, int method, cudaStream_t st)
+{
+    if (k <= 0 || n <= 0) return;
+    const bool tensor = method == 2 || (method == 0 && m <= kRotateTensorMaxM);
+    ED_REQUIRE(!tensor || m <= kRotateTensorMaxM, ED_ERR_ARG, "tensor-core rotation takes m <= 64");
+    if (!tensor) {
+        sc.y.alloc_at_least((size_t)ldy * k);
+        ED_CUDA(cudaMemcpyAsync(sc.y.p, Y_host, (size_t)ldy * k * 8, cudaMemcpyHostToDevice, st));
+        const size_t smem = (size_t)m * kGT * 8;
+        if (smem > 48 * 1024)
+            ED_CUDA(cudaFuncSetAttribute(k_gemm_vy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_gemm_vy<<<rot_sms() * 4, kThreads, smem, st>>>(V, n, m, sc.y.p, ldy, k, out);
+        count_launch();
+        ED_CUDA(cudaGetLastError());
+        return;
+    }
+    const int MP = (m + 15) / 16 * 16;
+    const int nblk = (k + kOzCols - 1) / kOzCols;
+    // digit planes of Y on the host: [block][plane][column][MP], exponents per column
+    sc.ydig_h.assign((size_t)nblk * kOzPlanes * kOzCols * MP, 0);
+    sc.yexp_h.assign((size_t)nblk * kOzCols, 0);
+    for (int c = 0; c < k; ++c) {
+        int E = 0;
+        for (int j = 0; j < m; ++j) E = std::max(E, exp_field(Y_host[(size_t)c * ldy + j]));
+        sc.yexp_h[c] = E;
+        if (!E) continue;
+        const int blk = c / kOzCols, cl = c % kOzCols;
+        for (int j = 0; j < m; ++j) {
+            int d[kOzPlanes];
+            digits7(Y_host[(size_t)c * ldy + j], E - 1022, d);
+            for (int t = 0; t < kOzPlanes; ++t) {
+                const bf16 h = __float2bfloat16((float)d[t]);   // exact: |d| <= 127
+                uint16_t bits;
+                memcpy(&bits, &h, 2);
+                sc.ydig_h[(((size_t)blk * kOzPlanes + t) * kOzCols + cl) * MP + j] = bits;
+            }
+        }
+    }
+    sc.ydig.alloc_at_least(sc.ydig_h.size());
+    sc.yexp.alloc_at_least(sc.yexp_h.size());
+    ED_CUDA(cudaMemcpyAsync(sc.ydig.p, sc.ydig_h.data(), sc.ydig_h.size() * 2, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(sc.yexp.p, sc.yexp_h.data(), sc.yexp_h.size() * 4, cudaMemcpyHostToDevice, st));
+    const bf16* yd = reinterpret_cast<const bf16*>(sc.ydig.p);
+    switch (MP) {
+    case 16: launch_rotate_oz<16>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+    case 32: launch_rotate_oz<32>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+    case 48: launch_rotate_oz<48>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+    default: launch_rotate_oz<64>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+    }
+    // the host staging is reused by the next call: wait until the copies have read it
+    ED_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace edgb
+
+using namespace edgb;
+
+extern "C" ed_status ed_basis_rotate(const double* V_dev, int64_t n, int m, const double* Y_host, int ldy, int k,
+                                     double* out_dev, int method)
+{
+    return guard([&] {
+        ED_REQUIRE(V_dev && Y_host && out_dev && n >= 1 && m >= 1 && k >= 1 && ldy >= m, ED_ERR_ARG, "bad argument");
+        ED_REQUIRE(method >= 0 && method <= 2, ED_ERR_ARG, "method: 0 auto, 1 FP64, 2 tensor cores");
+        RotateScratch sc;
+        rotate_basis(V_dev, n, m, Y_host, ldy, k, out_dev, sc, method, nullptr);
+        ED_CUDA(cudaStreamSynchronize(nullptr));
+    });
+}

@@ -108,6 +108,24 @@ class QuarticTermTables:
     def GetVkkkk(self, k1: int, k2: int, k3: int, k4: int) -> float:
         return float(self.m_vTable[(k4 * self.m_kMax + k3) * self.m_kMax + k2])
 
+    # term_tables_base.hpp:179-245 (4 labels); fmt "text" or "binary"
+    def ToFile(self, fileName: str, fmt: str = "text", mpi=None):
+        check(lib().ed_quartic_tables_write(fileName.encode(), int(fmt == "binary"), self.m_kMax,
+                                            self.m_kTable.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)),
+                                            _f64p(self.m_vTable)))
+
+    # term_tables_base.hpp:250-335
+    @classmethod
+    def FromFile(cls, fileName: str, fmt: str = "text", mpi=None) -> "QuarticTermTables":
+        K = ctypes.c_int()
+        b = int(fmt == "binary")
+        check(lib().ed_quartic_tables_read(fileName.encode(), b, ctypes.byref(K), None, None))
+        kt = np.empty(K.value ** 3, dtype=np.uint16)
+        vt = np.empty(K.value ** 3, dtype=np.float64)
+        check(lib().ed_quartic_tables_read(fileName.encode(), b, ctypes.byref(K),
+                                           kt.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)), _f64p(vt)))
+        return cls(K.value, ktable=kt, vtable=vt)
+
     def handle(self):
         if self._h is None:
             h = ctypes.c_void_p()
@@ -209,6 +227,17 @@ class CrsSparseMatrix:
                                col.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _f64p(val)))
         return rp, col, val
 
+    # crs_sparse_matrix.hpp:662-705
+    def ToFile(self, fileName: str, fmt: str = "text", mpi=None):
+        check(lib().ed_crs_write(self._h, fileName.encode(), int(fmt == "binary")))
+
+    # crs_sparse_matrix.hpp:710-740 (the final row start, absent from text files, is nnz)
+    @classmethod
+    def FromFile(cls, fileName: str, fmt: str = "text", upper: bool = True, mpi=None) -> "CrsSparseMatrix":
+        h = ctypes.c_void_p()
+        check(lib().ed_crs_read(fileName.encode(), int(fmt == "binary"), int(upper), ctypes.byref(h)))
+        return cls(h)
+
     def device_arrays(self):
         a, b, c = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
         check(lib().ed_crs_arrays(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
@@ -287,6 +316,19 @@ class SpinlessFermionHamiltonian:
         self.m_eigenvectors = evecs
         self.last_info = arp.last_info
         return ok
+
+    # hamiltonian_base.hpp:1204-1304
+    def EigensystemToFile(self, fileName: str, writeValues: bool = True, writeVectors: bool = False,
+                          fmt: str = "text", mpi=None):
+        eigensystem_to_file(fileName, self.m_eigenvalues, self.m_eigenvectors if writeVectors else None, fmt)
+
+    # hamiltonian_base.hpp:1309-1400
+    def EigensystemFromFile(self, fileName: str, readValues: bool = True, readVectors: bool = False,
+                            fmt: str = "text", mpi=None):
+        ev, vec = eigensystem_from_file(fileName, fmt, vectors=readVectors)
+        self.m_eigenvalues = ev
+        if readVectors:
+            self.m_eigenvectors = vec
 
 
 class MatrixVectorFunction:
@@ -394,6 +436,27 @@ class SpherePseudopotentialModel:
 
     def Diagonalize(self, **kw):
         return self.hamiltonian.LanczosDiagonalize(self.nev, **kw)
+
+
+def eigensystem_to_file(fileName: str, eigenvalues, eigenvectors=None, fmt: str = "text"):
+    """The reference's eigensystem file (text or binary); eigenvectors [nev, dim] or None."""
+    ev = np.ascontiguousarray(eigenvalues, dtype=np.float64)
+    vec = None if eigenvectors is None else np.ascontiguousarray(eigenvectors, dtype=np.float64)
+    dim = 0 if vec is None else int(vec.shape[-1])
+    check(lib().ed_eigensystem_write(fileName.encode(), int(fmt == "binary"), len(ev), _f64p(ev), dim,
+                                     None if vec is None else _f64p(vec)))
+
+
+def eigensystem_from_file(fileName: str, fmt: str = "text", vectors: bool = True):
+    """Read an eigensystem file: (eigenvalues, eigenvectors [nev, dim] or None)."""
+    b = int(fmt == "binary")
+    nev, dim = ctypes.c_int(), ctypes.c_uint64()
+    check(lib().ed_eigensystem_read(fileName.encode(), b, ctypes.byref(nev), None, ctypes.byref(dim), None))
+    ev = np.empty(nev.value)
+    vec = np.empty(nev.value * dim.value) if (vectors and dim.value) else None
+    check(lib().ed_eigensystem_read(fileName.encode(), b, ctypes.byref(nev), _f64p(ev), ctypes.byref(dim),
+                                    None if vec is None else _f64p(vec)))
+    return ev, (None if vec is None else vec.reshape(nev.value, dim.value))
 
 
 def solve_sector(N: int, norb: int, twoLz: int, pseudopotentials, nev: int, tol: float = 1e-10, v0=None,

@@ -229,6 +229,41 @@ ed_status ed_residuals(const ed_op* op, const double* x_dev, const double* lambd
 ed_status ed_residuals_noalloc(const ed_op* op, const double* x_dev, const double* lambda_host, int k,
                                double* res_host);
 
+/* Thick-restart basis rotation out = V Y[:, 0..k): V_dev n x m and out_dev
+ * n x k column-major device arrays, Y_host column-major with leading
+ * dimension ldy >= m.  method 1: FP64 FMAs; 2: BF16 tensor cores with
+ * FP64-accurate digit splitting (m <= 64); 0: the solver's choice (2 when
+ * m <= 64).  The step of ARPACK's dneupd/dnaupd that forms Ritz vectors from
+ * the Arnoldi basis (arpack_wrapper.hpp:873-883 call site); exported so the
+ * two methods can be compared.  Returns when out_dev is written. */
+ed_status ed_basis_rotate(const double* V_dev, int64_t n, int m, const double* Y_host, int ldy, int k,
+                          double* out_dev, int method);
+
+/* ------------------------------------------------------------- file formats */
+
+/* The reference's file formats (text = 0 or binary = 1), so that data moves
+ * between reference runs and this engine.  Host arrays.
+ * Eigensystem files: HamiltonianBase::EigensystemToFile / EigensystemFromFile
+ * (hamiltonians/hamiltonian_base.hpp:1204-1304, 1309-1400); evecs (nev x dim,
+ * vector after vector) may be NULL to write eigenvalues only.  Reading: call
+ * with evals = evecs = NULL to learn nev and dim (dim 0: no vectors stored). */
+ed_status ed_eigensystem_write(const char* path, int binary, int nev, const double* evals, uint64_t dim,
+                               const double* evecs);
+ed_status ed_eigensystem_read(const char* path, int binary, int* nev, double* evals, uint64_t* dim,
+                              double* evecs);
+/* CRS files: CrsSparseMatrix::ToFile / FromFile
+ * (utilities/data_structures/crs_sparse_matrix.hpp:662-740); int32 indices,
+ * so ED_ERR_RANGE above 2^31-1 nonzeros.  `upper` tells the reader whether
+ * the file holds the upper triangle (the reference's storage) or both. */
+ed_status ed_crs_write(const ed_crs* a, const char* path, int binary);
+ed_status ed_crs_read(const char* path, int binary, int upper, ed_crs** out);
+/* Quartic term-table files: TermTablesBase::ToFileBase / FromFileBase with 4
+ * labels (hamiltonians/term_tables_base.hpp:179-335).  Reading: call with
+ * ktable = vtable = NULL to learn norb, then with K^3-entry arrays. */
+ed_status ed_quartic_tables_write(const char* path, int binary, int norb, const uint16_t* ktable,
+                                  const double* vtable);
+ed_status ed_quartic_tables_read(const char* path, int binary, int* norb, uint16_t* ktable, double* vtable);
+
 /* ------------------------------------------------------ batched sweep K6 */
 
 /* Many Hamiltonians of one sector that differ only in their pseudopotentials
