@@ -14,7 +14,8 @@
 //    accumulator, and the group C_d = sum_{t+u=d} sum_j a_t[j] b_u[j] of one
 //    anti-diagonal d stays an integer below 8 * 64 * 127^2 < 2^23 for
 //    m <= 64, so mma.sync accumulates it exactly.  The groups d = 0..9 are
-//    combined in FP64, out = 2^(e_r+f_c) sum_d 2^(-7(d+2)) C_d; the dropped
+//    combined exactly in integers and rounded once to FP64,
+//    out = 2^(e_r+f_c) sum_d 2^(-7(d+2)) C_d; the dropped
 //    groups d >= 10 weigh below 1e-18 of 2^(e_r+f_c), so the result is at
 //    least as accurate as an FP64 dot product (whose rounding is ~m * 1e-16).
 #include <cuda_bf16.h>
@@ -113,12 +114,35 @@ __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// One CTA: rows [r0, r0+64) of V against columns [c0, c0+32) of Y.
+// Exact conversion of an integer with |x| < 2^53 to double, by integer
+// operations only (GB300's FP64 pipe is the scarce unit here).
+__device__ __forceinline__ double i53_to_double(long long x)
+{
+    if (x == 0) return 0.0;
+    const unsigned long long sgn = x < 0 ? 0x8000000000000000ull : 0ull;
+    const unsigned long long mag = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+    const int msb = 63 - __clzll((long long)mag);      // <= 52
+    const unsigned long long mant = (mag << (52 - msb)) & ((1ull << 52) - 1);
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)(msb + 1023) << 52) | mant));
+}
+
+// 2^e for a normal exponent, else ldexp.
+__device__ __forceinline__ double pow2(int e)
+{
+    if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
+    return ldexp(1.0, e);
+}
+
+// One CTA (8 warps): rows [r0, r0+64) of V against columns [c0, c0+32) of Y;
+// warp w owns rows 16*(w%4).. and columns 16*(w/4)...
 // ydig: digit planes of Y for this column block, [plane][column][MP] bf16;
 // yexp: f_c per column.  Dynamic shared memory: the V digit planes
 // [8][64][MP+8], the Y planes [8][32][MP+8] and the 64 row exponents.
+// The ten anti-diagonal groups are combined exactly in two int64 sums,
+// hi = sum_{d<5} C_d 2^(7(4-d)) and lo = sum_{d>=5} C_d 2^(7(9-d)) (each
+// below 2^52), and out = 2^(e_r+f_c-77) (hi 2^35 + lo) with one FP64 FMA.
 template <int MP>
-__global__ void __launch_bounds__(128) k_rotate_oz(const double* __restrict__ V, int64_t n, int m,
+__global__ void __launch_bounds__(256) k_rotate_oz(const double* __restrict__ V, int64_t n, int m,
                                                    const bf16* __restrict__ ydig, const int* __restrict__ yexp,
                                                    int k, double* __restrict__ out)
 {
@@ -131,17 +155,18 @@ __global__ void __launch_bounds__(128) k_rotate_oz(const double* __restrict__ V,
     const int cb = blockIdx.y;
     const int c0 = cb * kOzCols;
     const bf16* yblk = ydig + (size_t)cb * kOzPlanes * kOzCols * MP;
+    constexpr int NT = 256;
 
-    for (int i = threadIdx.x; i < kOzRows; i += 128) se[i] = 0;
+    for (int i = threadIdx.x; i < kOzRows; i += NT) se[i] = 0;
     // Y planes: plain copy of this column block (MP is a multiple of 16)
-    for (int i = threadIdx.x; i < kOzPlanes * kOzCols * MP / 8; i += 128) {
+    for (int i = threadIdx.x; i < kOzPlanes * kOzCols * MP / 8; i += NT) {
         const int e0 = i * 8;
         const int pc = e0 / MP, j = e0 - pc * MP;                    // pc = plane*32 + column
         *reinterpret_cast<uint4*>(sB + (size_t)pc * LD + j) = *reinterpret_cast<const uint4*>(yblk + e0);
     }
     __syncthreads();
     // row exponents e_r = max over the row of (E - 1022), so |V[r][j]| < 2^e_r
-    for (int i = threadIdx.x; i < kOzRows * m; i += 128) {
+    for (int i = threadIdx.x; i < kOzRows * m; i += NT) {
         const int rl = i % kOzRows, j = i / kOzRows;
         const int64_t r = r0 + rl;
         if (r < n) {
@@ -151,7 +176,7 @@ __global__ void __launch_bounds__(128) k_rotate_oz(const double* __restrict__ V,
     }
     __syncthreads();
     // V digit planes (zero beyond m and beyond n)
-    for (int i = threadIdx.x; i < kOzRows * MP; i += 128) {
+    for (int i = threadIdx.x; i < kOzRows * MP; i += NT) {
         const int rl = i % kOzRows, j = i / kOzRows;
         const int64_t r = r0 + rl;
         int d[kOzPlanes];
@@ -168,16 +193,18 @@ __global__ void __launch_bounds__(128) k_rotate_oz(const double* __restrict__ V,
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, tq = lane & 3;
-    const int wr = warp * 16;                  // the warp's 16 rows
-    double dacc[4][4];
+    const int wr = (warp & 3) * 16;            // the warp's 16 rows
+    const int wc = (warp >> 2) * 16;           // and 16 columns
+    long long hi[2][4], lo[2][4];
 #pragma unroll
-    for (int ni = 0; ni < 4; ++ni)
+    for (int ni = 0; ni < 2; ++ni)
 #pragma unroll
-        for (int e = 0; e < 4; ++e) dacc[ni][e] = 0.0;
-    for (int dg = kOzGroups - 1; dg >= 0; --dg) {   // anti-diagonals 9..0, smallest first
-        float acc[4][4];
+        for (int e = 0; e < 4; ++e) hi[ni][e] = lo[ni][e] = 0;
+#pragma unroll 1
+    for (int dg = 0; dg < kOzGroups; ++dg) {
+        float acc[2][4];
 #pragma unroll
-        for (int ni = 0; ni < 4; ++ni)
+        for (int ni = 0; ni < 2; ++ni)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[ni][e] = 0.f;
         for (int t = max(0, dg - (kOzPlanes - 1)); t <= min(dg, kOzPlanes - 1); ++t) {
@@ -186,38 +213,48 @@ __global__ void __launch_bounds__(128) k_rotate_oz(const double* __restrict__ V,
             const bf16* Bp = sB + (size_t)u * kOzCols * LD;
 #pragma unroll
             for (int kk = 0; kk < MP; kk += 16) {
-                uint32_t af[4], bfr[4][2];
+                uint32_t af[4], bfr[2][2];
                 af[0] = *reinterpret_cast<const uint32_t*>(A + (wr + g) * LD + kk + tq * 2);
                 af[1] = *reinterpret_cast<const uint32_t*>(A + (wr + g + 8) * LD + kk + tq * 2);
                 af[2] = *reinterpret_cast<const uint32_t*>(A + (wr + g) * LD + kk + tq * 2 + 8);
                 af[3] = *reinterpret_cast<const uint32_t*>(A + (wr + g + 8) * LD + kk + tq * 2 + 8);
 #pragma unroll
-                for (int ni = 0; ni < 4; ++ni) {
-                    bfr[ni][0] = *reinterpret_cast<const uint32_t*>(Bp + (ni * 8 + g) * LD + kk + tq * 2);
-                    bfr[ni][1] = *reinterpret_cast<const uint32_t*>(Bp + (ni * 8 + g) * LD + kk + tq * 2 + 8);
+                for (int ni = 0; ni < 2; ++ni) {
+                    bfr[ni][0] = *reinterpret_cast<const uint32_t*>(Bp + (wc + ni * 8 + g) * LD + kk + tq * 2);
+                    bfr[ni][1] = *reinterpret_cast<const uint32_t*>(Bp + (wc + ni * 8 + g) * LD + kk + tq * 2 + 8);
                 }
 #pragma unroll
-                for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[ni], af, bfr[ni]);
+                for (int ni = 0; ni < 2; ++ni) mma_bf16(acc[ni], af, bfr[ni]);
             }
         }
-        const double w = ldexp(1.0, -7 * (dg + 2));
+        // exact integer group sums into the two int64 accumulators
+        const bool upper = dg < 5;
+        const long long wgt = 1ll << (7 * (upper ? 4 - dg : 9 - dg));
 #pragma unroll
-        for (int ni = 0; ni < 4; ++ni)
+        for (int ni = 0; ni < 2; ++ni)
 #pragma unroll
-            for (int e = 0; e < 4; ++e) dacc[ni][e] = fma((double)acc[ni][e], w, dacc[ni][e]);
+            for (int e = 0; e < 4; ++e) {
+                const long long c = (long long)__float2int_rz(acc[ni][e]);
+                if (upper) hi[ni][e] += c * wgt;
+                else lo[ni][e] += c * wgt;
+            }
     }
-    // scale by 2^(e_r + f_c) and store (column-major output)
+    // scale by 2^(e_r + f_c - 77) and store (column-major output)
 #pragma unroll
-    for (int ni = 0; ni < 4; ++ni)
+    for (int ni = 0; ni < 2; ++ni)
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const int rl = wr + g + ((e >= 2) ? 8 : 0);
-            const int cl = ni * 8 + tq * 2 + (e & 1);
+            const int cl = wc + ni * 8 + tq * 2 + (e & 1);
             const int64_t r = r0 + rl;
             const int c = c0 + cl;
             if (r < n && c < k) {
                 const int er = se[rl], fc = yexp[c];
-                const double v = (er && fc) ? ldexp(dacc[ni][e], (er - 1022) + (fc - 1022)) : 0.0;
+                double v = 0.0;
+                if (er && fc) {
+                    v = fma(i53_to_double(hi[ni][e]), 34359738368.0 /* 2^35 */, i53_to_double(lo[ni][e]));
+                    v *= pow2((er - 1022) + (fc - 1022) - 77);
+                }
                 out[(int64_t)c * n + r] = v;
             }
         }
@@ -231,7 +268,7 @@ void launch_rotate_oz(const double* V, int64_t n, int m, const bf16* ydig, const
     const size_t smem = (size_t)kOzPlanes * (kOzRows + kOzCols) * LD * 2 + kOzRows * 4;
     ED_CUDA(cudaFuncSetAttribute(k_rotate_oz<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)((n + kOzRows - 1) / kOzRows), (unsigned)((k + kOzCols - 1) / kOzCols));
-    k_rotate_oz<MP><<<grid, 128, smem, st>>>(V, n, m, ydig, yexp, k, out);
+    k_rotate_oz<MP><<<grid, 256, smem, st>>>(V, n, m, ydig, yexp, k, out);
     count_launch();
     ED_CUDA(cudaGetLastError());
 }
