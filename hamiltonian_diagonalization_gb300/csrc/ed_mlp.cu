@@ -35,7 +35,8 @@ constexpr int kLayers = 4;
 // ------------------------------------------------------------- GEMM core
 // C[M,N] = sum_k A(m,k) B(k,n) with A(m,k) = A[m*sam + k*sak] and
 // B(k,n) = Bm[k*sbk + n*sbn] (bf16), FP32 accumulation in mma.sync
-// m16n8k16; 64x64 block tile, BK 32, four warps of 32x32.  Tiles are staged
+// m16n8k16; 64x64 block tile, 128 columns of K per stage, four warps of
+// 32x32.  Tiles are staged
 // through shared memory with bounds checks, so any strides (transposes)
 // and any M, N, K work; the epilogue functor receives (row, col, value).
 
@@ -48,18 +49,23 @@ __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// Stage a 64 x 32 tile of an operand into s[row][k] (row = m or n index,
-// stride 40 bf16 = 80 bytes).  The operand is P(mn, k) = P[mn*s_mn + k*s_k];
-// the tile is read in 16-byte pieces along whichever index is contiguous
-// (k when kfast, else mn), with element-wise bounds checks where a piece
-// crosses an edge or is not 16-byte aligned.
-__device__ __forceinline__ void stage_tile(bf16 (*s)[40], const bf16* __restrict__ P, int64_t s_mn, int64_t s_k,
+// K extent staged per synchronisation, and the shared-memory row stride
+// (BK + 8 bf16 = 272 bytes: 16-byte aligned rows, conflict-free fragments).
+constexpr int kBK = 128;
+constexpr int kLDS = kBK + 8;
+
+// Stage a 64 x kBK tile of an operand into s[row][k] (row = m or n index).
+// The operand is P(mn, k) = P[mn*s_mn + k*s_k]; the tile is read in 16-byte
+// pieces along whichever index is contiguous (k when kfast, else mn), with
+// element-wise bounds checks where a piece crosses an edge or is not 16-byte
+// aligned.
+__device__ __forceinline__ void stage_tile(bf16 (*s)[kLDS], const bf16* __restrict__ P, int64_t s_mn, int64_t s_k,
                                            bool kfast, int mn0, int MN, int k0, int kend)
 {
     const bf16 zero = __float2bfloat16(0.f);
     if (kfast) {
-        for (int c = threadIdx.x; c < 256; c += 128) {     // 64 rows x 4 pieces of 8 k
-            const int r = c >> 2, kc = (c & 3) * 8;
+        for (int c = threadIdx.x; c < 64 * kBK / 8; c += 128) {     // 64 rows x kBK/8 pieces of 8 k
+            const int r = c / (kBK / 8), kc = (c % (kBK / 8)) * 8;
             const int gmn = mn0 + r, gk = k0 + kc;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
             if (gmn < MN && gk < kend) {
@@ -76,7 +82,7 @@ __device__ __forceinline__ void stage_tile(bf16 (*s)[40], const bf16* __restrict
             *reinterpret_cast<uint4*>(&s[r][kc]) = v;
         }
     } else {
-        for (int c = threadIdx.x; c < 256; c += 128) {     // 32 k x 8 pieces of 8 rows
+        for (int c = threadIdx.x; c < kBK * 8; c += 128) {          // kBK k x 8 pieces of 8 rows
             const int kk = c >> 3, mc = (c & 7) * 8;
             const int gk = k0 + kk, gmn = mn0 + mc;
             __align__(16) bf16 t[8];
@@ -103,8 +109,8 @@ __global__ void __launch_bounds__(128) k_gemm(const bf16* __restrict__ A, int64_
                                               const bf16* __restrict__ Bm, int64_t sbk, int64_t sbn, int M, int N, int K,
                                               int kchunk, Epi epi)
 {
-    __shared__ __align__(16) bf16 sA[64][40];   // [m][k]
-    __shared__ __align__(16) bf16 sB[64][40];   // [n][k]
+    __shared__ __align__(16) bf16 sA[64][kLDS];   // [m][k]
+    __shared__ __align__(16) bf16 sB[64][kLDS];   // [n][k]
     const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
     const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -118,12 +124,12 @@ __global__ void __launch_bounds__(128) k_gemm(const bf16* __restrict__ A, int64_
         for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
-    for (int k0 = kbeg; k0 < kend; k0 += 32) {
+    for (int k0 = kbeg; k0 < kend; k0 += kBK) {
         stage_tile(sA, A, sam, sak, a_kfast, m0, M, k0, kend);
         stage_tile(sB, Bm, sbn, sbk, b_kfast, n0, N, k0, kend);
         __syncthreads();
 #pragma unroll
-        for (int kk = 0; kk < 32; kk += 16) {
+        for (int kk = 0; kk < min(kBK, kend - k0); kk += 16) {
             uint32_t af[2][4], bfr[4][2];
 #pragma unroll
             for (int mi = 0; mi < 2; ++mi) {
@@ -162,7 +168,7 @@ template <class Epi>
 void gemm(const bf16* A, int64_t sam, int64_t sak, const bf16* B, int64_t sbk, int64_t sbn, int M, int N, int K,
           Epi epi, cudaStream_t st, int splits = 1)
 {
-    const int kchunk = ((K + splits - 1) / splits + 31) / 32 * 32;
+    const int kchunk = ((K + splits - 1) / splits + kBK - 1) / kBK * kBK;
     dim3 grid((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64), (unsigned)splits);
     k_gemm<Epi><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, kchunk, epi);
     count_launch();

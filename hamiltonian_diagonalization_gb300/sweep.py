@@ -121,6 +121,15 @@ def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=4000, 
         t4 = time.perf_counter()
         ev_r, _, inf_r = bh.solve(nev, tol=tol, seed=seed + 2, ncv=ncv)
         t5 = time.perf_counter()
+        # the ground state alone (what the network predicts), warm vs random
+        torch.cuda.synchronize()
+        t6 = time.perf_counter()
+        ev_w1, _, inf_w1 = bh.solve(1, tol=tol, V0=V0)
+        torch.cuda.synchronize()
+        t7 = time.perf_counter()
+        ev_r1, _, inf_r1 = bh.solve(1, tol=tol, seed=seed + 3)
+        torch.cuda.synchronize()
+        t8 = time.perf_counter()
         P = V0.cpu().numpy()
         T = vec_w[0].cpu().numpy()
         ov = np.abs(np.sum(P * T, axis=0)) / np.linalg.norm(P, axis=0)
@@ -134,7 +143,12 @@ def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=4000, 
                     "train_products": inf_t["block_products"], "overlap_min": float(ov.min()),
                     "overlap_mean": float(ov.mean()),
                     "ground_energy_warm_vs_random_max_rel": float(np.max(np.abs(ev_w[:, 0] - ev_r[:, 0]) /
-                                                                         np.abs(ev_r[:, 0])))})
+                                                                         np.abs(ev_r[:, 0]))),
+                    "held_nev1_warm_products": inf_w1["block_products"],
+                    "held_nev1_random_products": inf_r1["block_products"],
+                    "held_nev1_warm_seconds": t7 - t6, "held_nev1_random_seconds": t8 - t7,
+                    "held_nev1_energy_warm_vs_random_max_rel": float(np.max(np.abs(ev_w1[:, 0] - ev_r1[:, 0]) /
+                                                                            np.abs(ev_r1[:, 0])))})
     return total, evals, rec
 
 

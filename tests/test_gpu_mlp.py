@@ -89,3 +89,11 @@ def test_training_and_warm_start_gain(cuda):
     ov = np.abs(np.sum(P * T, axis=0)) / np.linalg.norm(P, axis=0)
     assert np.min(ov) > 0.5, ov
     assert info_warm["block_products"] < info_rand["block_products"], (info_warm, info_rand)
+    # warm-started ground energies against the FP64 oracle (CPU build + ARPACK)
+    from oracle import oracle as O
+    words = O.basis(N, norb, 0)
+    for j, v1 in enumerate(held):
+        kt, vt = O.quartic_tables(norb, O.sweep_list(norb, v1))
+        rp, col, val = O.build_upper(words, norb, kt, vt)
+        e0 = O.lowest_eigenpairs(rp, col, val, 1, tol=1e-12)[0][0]
+        assert abs(ev_warm[j, 0] - e0) <= 1e-10 * abs(e0), (j, ev_warm[j, 0], e0)
