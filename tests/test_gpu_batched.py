@@ -83,3 +83,38 @@ def test_batched_solve_from_given_starts(cuda):
     assert info["converged"] == 2
     with pytest.raises(ed.EDError):
         batch.solve(2, V0=torch.zeros((batch.n, 2), dtype=torch.float64, device="cuda"))
+
+
+def test_converged_hamiltonians_retire_from_the_batch(cuda):
+    """A Hamiltonian that converges restarts ahead of the others leaves the
+    batch; its eigenpairs (written at retirement) and the survivors' match
+    one-at-a-time solves from the same start vectors."""
+    torch = cuda
+    N, norb, tlz, nev = 10, 28, 0, 4
+    v1s = [0.5, 2.1, 2.9]
+    lists = sweep_lists(norb, v1s)
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(N, norb, tlz)
+    n = b.GetStoredDimension()
+    rng = np.random.default_rng(7)
+    V0 = rng.uniform(-1, 1, (n, len(v1s)))
+    # Hamiltonian 1 starts next to its own lowest states (1e-3 of random left,
+    # so the Krylov space is not exactly invariant): it converges early
+    near = ed.solve_sector(N, norb, tlz, lists[1], nev, tol=1e-10, seed=3, want_vectors=True)["eigenvectors"]
+    r = rng.uniform(-1, 1, n)
+    V0[:, 1] = near.sum(axis=0) + 1e-3 * r / np.linalg.norm(r)
+    batch = ed.HamiltonianBatch(b, lists, autotune=False)
+    ev, vec, info = batch.solve(nev, tol=1e-10, V0=torch.from_numpy(np.ascontiguousarray(V0)).cuda(),
+                                want_vectors=True)
+    assert info["converged"] == len(v1s) and info["max_residual"] <= 1e-10
+    # retirement: fewer Hamiltonian-products than block products x batch size
+    assert info["problem_products"] < info["block_products"] * len(v1s), info
+    V = vec.cpu().numpy()                # [nev, n, nham]
+    for j, pp in enumerate(lists):
+        out = ed.solve_sector(N, norb, tlz, pp, nev, tol=1e-10, v0=V0[:, j], want_vectors=True)
+        assert np.max(np.abs(ev[j] - out["eigenvalues"]) / np.abs(out["eigenvalues"])) <= 1e-10, j
+        G = V[:, :, j] @ V[:, :, j].T
+        assert np.max(np.abs(G - np.eye(nev))) < 1e-9, j
+        # same eigenvectors up to sign (the levels are not degenerate here)
+        ov = np.abs(np.sum(V[:, :, j] * out["eigenvectors"], axis=1))
+        assert np.min(ov) > 1 - 1e-8, (j, ov)
