@@ -114,6 +114,18 @@ __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// Four 8x8 b16 matrices from shared memory: thread i supplies the address of
+// row i%8 of matrix i/8 (16-byte aligned) and receives, from matrix k, the
+// elements (row i/4, columns 2(i%4), 2(i%4)+1) in r[k] — the m16n8k16
+// fragment layout.
+__device__ __forceinline__ void ldsm_x4(uint32_t* r, const bf16* p)
+{
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
 // Exact conversion of an integer with |x| < 2^53 to double, by integer
 // operations only (GB300's FP64 pipe is the scarce unit here).
 __device__ __forceinline__ double i53_to_double(long long x)
@@ -175,19 +187,28 @@ __global__ void __launch_bounds__(256) k_rotate_oz(const double* __restrict__ V,
         }
     }
     __syncthreads();
-    // V digit planes (zero beyond m and beyond n)
-    for (int i = threadIdx.x; i < kOzRows * MP; i += NT) {
-        const int rl = i % kOzRows, j = i / kOzRows;
+    // V digit planes (zero beyond m and beyond n), two adjacent columns per
+    // thread so that each plane gets one 32-bit store
+    for (int i = threadIdx.x; i < kOzRows * MP / 2; i += NT) {
+        const int rl = i % kOzRows, j = 2 * (i / kOzRows);
         const int64_t r = r0 + rl;
-        int d[kOzPlanes];
-        if (r < n && j < m && se[rl]) {
-            digits7(V[(int64_t)j * n + r], se[rl] - 1022, d);
-        } else {
+        int d0[kOzPlanes], d1[kOzPlanes];
+        const bool live = r < n && se[rl];
+        if (live && j < m) digits7(V[(int64_t)j * n + r], se[rl] - 1022, d0);
+        else
 #pragma unroll
-            for (int t = 0; t < kOzPlanes; ++t) d[t] = 0;
+            for (int t = 0; t < kOzPlanes; ++t) d0[t] = 0;
+        if (live && j + 1 < m) digits7(V[(int64_t)(j + 1) * n + r], se[rl] - 1022, d1);
+        else
+#pragma unroll
+            for (int t = 0; t < kOzPlanes; ++t) d1[t] = 0;
+#pragma unroll
+        for (int t = 0; t < kOzPlanes; ++t) {
+            __nv_bfloat162 pr;
+            pr.x = __int2bfloat16_rn(d0[t]);
+            pr.y = __int2bfloat16_rn(d1[t]);
+            *reinterpret_cast<__nv_bfloat162*>(sA + ((size_t)t * kOzRows + rl) * LD + j) = pr;
         }
-#pragma unroll
-        for (int t = 0; t < kOzPlanes; ++t) sA[((size_t)t * kOzRows + rl) * LD + j] = __int2bfloat16_rn(d[t]);
     }
     __syncthreads();
 
@@ -211,20 +232,19 @@ __global__ void __launch_bounds__(256) k_rotate_oz(const double* __restrict__ V,
             const int u = dg - t;
             const bf16* A = sA + (size_t)t * kOzRows * LD;
             const bf16* Bp = sB + (size_t)u * kOzCols * LD;
+            // ldmatrix row addresses: A matrices (rows +0/+8, k +0/+8) in
+            // fragment order; B matrices (n tile 0/1, k +0/+8)
+            const int mi = lane >> 3, ri = lane & 7;
+            const bf16* pa = A + (wr + (mi & 1) * 8 + ri) * LD + (mi >> 1) * 8;
+            const bf16* pb = Bp + (wc + (mi >> 1) * 8 + ri) * LD + (mi & 1) * 8;
 #pragma unroll
             for (int kk = 0; kk < MP; kk += 16) {
-                uint32_t af[4], bfr[2][2];
-                af[0] = *reinterpret_cast<const uint32_t*>(A + (wr + g) * LD + kk + tq * 2);
-                af[1] = *reinterpret_cast<const uint32_t*>(A + (wr + g + 8) * LD + kk + tq * 2);
-                af[2] = *reinterpret_cast<const uint32_t*>(A + (wr + g) * LD + kk + tq * 2 + 8);
-                af[3] = *reinterpret_cast<const uint32_t*>(A + (wr + g + 8) * LD + kk + tq * 2 + 8);
-#pragma unroll
-                for (int ni = 0; ni < 2; ++ni) {
-                    bfr[ni][0] = *reinterpret_cast<const uint32_t*>(Bp + (wc + ni * 8 + g) * LD + kk + tq * 2);
-                    bfr[ni][1] = *reinterpret_cast<const uint32_t*>(Bp + (wc + ni * 8 + g) * LD + kk + tq * 2 + 8);
-                }
-#pragma unroll
-                for (int ni = 0; ni < 2; ++ni) mma_bf16(acc[ni], af, bfr[ni]);
+                uint32_t af[4], bq[4];
+                ldsm_x4(af, pa + kk);
+                ldsm_x4(bq, pb + kk);
+                const uint32_t b0[2] = {bq[0], bq[1]}, b1[2] = {bq[2], bq[3]};
+                mma_bf16(acc[0], af, b0);
+                mma_bf16(acc[1], af, b1);
             }
         }
         // exact integer group sums into the two int64 accumulators
@@ -339,7 +359,8 @@ extern "C" ed_status ed_basis_rotate(const double* V_dev, int64_t n, int m, cons
     return guard([&] {
         ED_REQUIRE(V_dev && Y_host && out_dev && n >= 1 && m >= 1 && k >= 1 && ldy >= m, ED_ERR_ARG, "bad argument");
         ED_REQUIRE(method >= 0 && method <= 2, ED_ERR_ARG, "method: 0 auto, 1 FP64, 2 tensor cores");
-        RotateScratch sc;
+        // scratch kept per host thread, so repeated calls do not allocate
+        static thread_local RotateScratch sc;
         rotate_basis(V_dev, n, m, Y_host, ldy, k, out_dev, sc, method, nullptr);
         ED_CUDA(cudaStreamSynchronize(nullptr));
     });

@@ -2,6 +2,7 @@
 
     python -m hamiltonian_diagonalization_gb300.microbench --sector 11,31,0 --reps 20 [--upper] [--matfree]
     python -m hamiltonian_diagonalization_gb300.microbench --sector 10,28,0 --batch 32 --reps 20
+    python -m hamiltonian_diagonalization_gb300.microbench --rotate 1371535,41,25 --reps 20
 
 Builds the sector's Hamiltonian (LLL Coulomb pseudopotentials, odd m) on the
 device, then times `reps` products with CUDA events on the launching stream
@@ -11,6 +12,8 @@ and the implied GB/s.  Used for the SpMV roofline and its ncu profiles.
 With --batch B it times the block product of B Hamiltonians of the sector
 (the V1 sweep's shared pattern, ed_batch_spmm) instead and reports FP64 FMAs
 per second (one FMA per stored element per Hamiltonian, diagonal included).
+With --rotate n,m,k it times the thick-restart rotation of an n x m basis
+into k Ritz vectors (ed_basis_rotate) in FP64 and on the tensor cores.
 """
 from __future__ import annotations
 
@@ -30,12 +33,15 @@ def main():
     ap.add_argument("--matfree", action="store_true", help="regenerate elements on the fly")
     ap.add_argument("--batch", type=int, default=0, help="time the block product of this many Hamiltonians")
     ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default tile (32 per row, L1)")
+    ap.add_argument("--rotate", default="", help="n,m,k: time the restart rotation instead")
     args = ap.parse_args()
     import torch
 
     import hamiltonian_diagonalization_gb300 as ed
     from hamiltonian_diagonalization_gb300 import _capi as C
 
+    if args.rotate:
+        return rotate_main(C, torch, args)
     N, norb, tlz = (int(x) for x in args.sector.split(","))
     if args.batch:
         return batch_main(ed, C, torch, N, norb, tlz, args)
@@ -94,6 +100,32 @@ def batch_main(ed, C, torch, N, norb, tlz, args):
     print(json.dumps({"sector": [N, norb, tlz], "n": n, "mode": "batch", "hamiltonians": B, "nnz_offdiag": bt.nnz,
                       "ms_per_block_product": ms, "ms_per_hamiltonian_product": ms / B,
                       "fp64_fma_per_s": fma / ms * 1e3, "fp64_tflops": 2 * fma / ms / 1e9}))
+
+
+def rotate_main(C, torch, args):
+    n, m, k = (int(x) for x in args.rotate.split(","))
+    V = torch.from_numpy(np.random.default_rng(1).standard_normal(n * m)).cuda()
+    out = torch.empty(n * k, dtype=torch.float64, device="cuda")
+    Y = np.asfortranarray(np.random.default_rng(2).standard_normal((m, m)))
+    yp = Y.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    res = {"rotate": [n, m, k]}
+    for method, name in ((1, "fp64"), (2, "tensor")):
+        def call():
+            st = C.lib().ed_basis_rotate(ctypes.c_void_p(V.data_ptr()), n, m, yp, m, k,
+                                         ctypes.c_void_p(out.data_ptr()), method)
+            assert st == 0, C.lib().ed_last_error()
+        for _ in range(args.warmup):
+            call()
+        torch.cuda.synchronize()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.reps):
+            call()
+        e.record()
+        torch.cuda.synchronize()
+        res[f"ms_{name}"] = a.elapsed_time(e) / args.reps
+    res["fp64_multiply_adds"] = n * m * k
+    print(json.dumps(res))
 
 
 if __name__ == "__main__":
