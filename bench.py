@@ -45,6 +45,15 @@ def start_vector(n: int, seed: int) -> np.ndarray:
     return v / np.linalg.norm(v)
 
 
+def max_over_ranks(value: float, device: str = "cpu") -> float:
+    """The slowest replica's value (the step time the job is charged)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -266,10 +275,7 @@ def run_gpu(args, ws, rank):
     # standalone SpMV timing on the same CRS for the roofline cross-check
     spmv_ms_alone = spmv_alone(L, C, kt, vt, n, torch)
     if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, "cuda")
     return {"ms": ms, "infos": infos, "ev": ev, "nnz": nnz, "n": n, "launches": launches, "clocks": clocks,
             "e2e_s": statistics.median(e2e_times), "ev_e2e": ev_e2e, "spmv_ms_alone": spmv_ms_alone,
             "phases": phases[-args.steps:]}

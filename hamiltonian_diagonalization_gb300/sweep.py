@@ -3,6 +3,7 @@ Lanczos versus the batched lockstep solver, with converged solves per second.
 
     python -m hamiltonian_diagonalization_gb300.sweep --N 10 --norb 28 --sectors 0,2,4,6,8 \\
         --points 64 --nev 4 --mode both
+    torchrun --nproc-per-node G -m hamiltonian_diagonalization_gb300.sweep --batch-size 32   # G replicas
 
 H(V1) = V1*P_1 + sum_{odd m >= 3} V_m^Coulomb P_m with V1 in
 linspace(0.5, 3.0, points).  `plain` calls ed_solve_sector once per
@@ -16,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import time
 
 import numpy as np
@@ -46,30 +48,83 @@ def run_plain(N, norb, sectors, v1s, nev, tol, seed):
     return time.perf_counter() - t0, evals, products
 
 
-def run_batched(N, norb, sectors, v1s, nev, tol, seed, batch_size=0, ncv=0):
-    """Each sector's Hamiltonians in batches of batch_size (0: all at once);
-    a batch's [row][problem] vectors should stay within L2 for the block
-    product's gathers to hit it."""
+def work_units(sectors, npoints: int, batch_size: int = 0):
+    """The sweep as independent units (sector, first V1 index, count): one
+    batch each.  Units share nothing, so replicas split them with no data
+    exchange."""
+    bs = batch_size or npoints
+    return [(tlz, j0, min(bs, npoints - j0)) for tlz in sectors for j0 in range(0, npoints, bs)]
+
+
+def shard(units, rank: int, world: int):
+    """Units of replica `rank` out of `world` (round robin)."""
+    return units[rank::world]
+
+
+def run_units(N, norb, units, v1s, nev, tol, seed, ncv=0):
+    """Solve the given units batched; returns (seconds, {(sector, j): eigenvalues}, infos)."""
     import torch
 
     import hamiltonian_diagonalization_gb300 as ed
     lists = sweep_lists(norb, v1s)
-    bs = batch_size or len(lists)
     evals = {}
     infos = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for tlz in sectors:
-        b = ed.FermionFockBasis()
-        b.GenerateFockSpace(N, norb, tlz)
-        for j0 in range(0, len(lists), bs):
-            batch = ed.HamiltonianBatch(b, lists[j0:j0 + bs])
-            ev, _, info = batch.solve(nev, tol=tol, seed=seed, ncv=ncv)
-            infos.append(info)
-            for j in range(len(lists[j0:j0 + bs])):
-                evals[(tlz, j0 + j)] = ev[j]
+    basis, cur = None, None
+    for (tlz, j0, cnt) in units:
+        if cur != tlz:
+            basis = ed.FermionFockBasis()
+            basis.GenerateFockSpace(N, norb, tlz)
+            cur = tlz
+        batch = ed.HamiltonianBatch(basis, lists[j0:j0 + cnt])
+        ev, _, info = batch.solve(nev, tol=tol, seed=seed, ncv=ncv)
+        infos.append(info)
+        for j in range(cnt):
+            evals[(tlz, j0 + j)] = ev[j]
     torch.cuda.synchronize()
     return time.perf_counter() - t0, evals, infos
+
+
+def run_batched(N, norb, sectors, v1s, nev, tol, seed, batch_size=0, ncv=0):
+    """Each sector's Hamiltonians in batches of batch_size (0: all at once);
+    a batch's [row][problem] vectors should stay within L2 for the block
+    product's gathers to hit it."""
+    return run_units(N, norb, work_units(sectors, len(v1s), batch_size), v1s, nev, tol, seed, ncv)
+
+
+def gather_to_rank0(obj):
+    """All replicas' objects on rank 0 (a list in rank order), None elsewhere;
+    host-side only, after the timed work."""
+    import torch.distributed as dist
+    out = [None] * dist.get_world_size()
+    dist.all_gather_object(out, obj)
+    return out if dist.get_rank() == 0 else None
+
+
+def run_replicas(args, sectors, v1s):
+    """Batched sweep over WORLD_SIZE replicas (one GPU each, torchrun): each
+    solves its round-robin share of the units; rank 0 merges the eigenvalues
+    and reports whole-job solves/s over the slowest replica."""
+    import torch
+    import torch.distributed as dist
+    rank, world = dist.get_rank(), dist.get_world_size()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)) % max(1, torch.cuda.device_count()))
+    units = work_units(sectors, len(v1s), args.batch_size)
+    mine = shard(units, rank, world)
+    run_units(args.N, args.norb, mine[:1], v1s, args.nev, args.tol, args.seed)    # warm-up (tuning, module load)
+    dist.barrier()
+    t, ev, infos = run_units(args.N, args.norb, mine, v1s, args.nev, args.tol, args.seed, args.ncv)
+    parts = gather_to_rank0({"seconds": t, "evals": {f"{k[0]},{k[1]}": v.tolist() for k, v in ev.items()},
+                             "max_residual": max([i["max_residual"] for i in infos] or [0.0])})
+    if parts is None:
+        return None
+    slowest = max(p["seconds"] for p in parts)
+    merged = {}
+    for p in parts:
+        merged.update(p["evals"])
+    return {"seconds": slowest, "replicas": world, "solves": len(merged),
+            "solves_per_s": len(merged) / slowest, "max_residual": max(p["max_residual"] for p in parts)}
 
 
 def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=4000, batch=4096, lr=2e-3,
@@ -170,6 +225,16 @@ def main():
     sectors = [int(s) for s in args.sectors.split(",")]
     v1s = np.linspace(0.5, 3.0, args.points)
     nsolve = len(sectors) * len(v1s)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        # replicas (torchrun): the batched sweep split over the ranks
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        r = run_replicas(args, sectors, v1s)
+        if r is not None:
+            print(json.dumps({"N": args.N, "norb": args.norb, "sectors": sectors, "points": args.points,
+                              "nev": args.nev, "tol": args.tol, "batched_replicas": r}))
+        dist.destroy_process_group()
+        return
     out = {"N": args.N, "norb": args.norb, "sectors": sectors, "points": args.points, "nev": args.nev,
            "tol": args.tol, "solves": nsolve}
     if args.mode in ("warm", "all"):
