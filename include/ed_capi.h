@@ -172,7 +172,8 @@ typedef struct {
     int max_restarts;   /* 0 -> 2000 (the reference's ARPACK iteration cap)           */
     double tol;         /* residual ||H x - theta x||_2 (x unit) required per pair     */
     uint64_t seed;      /* start vector uniform(-1,1) from this seed if none is given  */
-    int want_vectors;   /* 1 -> return eigenvectors                                    */
+    int want_vectors;   /* caller's note only: eigenvectors are written whenever the
+                           eigenvector pointer of the call is non-NULL              */
     int verify;         /* 1 -> recompute true residuals with extra products            */
 } ed_lanczos_params;
 
