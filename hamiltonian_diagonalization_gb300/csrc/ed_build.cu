@@ -10,8 +10,13 @@
 // into one value per hop (derive_hop_tables), so the element is
 // sign(state) * W[hop] bit for bit.  The diagonal is summed term by term in
 // the reference order.  Rows are generated one warp per row, sorted by
-// column in shared memory and written coalesced; a count pass sizes the
-// rows first.
+// column (in registers, k_fill_reg; in shared memory for rows or sectors too
+// large for 32-bit keys, k_fill) and written coalesced; a count pass sizes
+// the rows first.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+
 #include "ed_hop.cuh"
 
 namespace edgb {
@@ -31,40 +36,52 @@ __global__ void k_diag(const uint64_t* __restrict__ words, int64_t n, const doub
         diag[r] = diag_element(hv, words[r]);
 }
 
-// Number of stored entries of each row (upper: col >= row; full: all).
+// Number of stored entries of each row (upper: col >= row; full: all), and
+// the largest number of admissible hops of a row plus one (the diagonal
+// slot), which sizes the register-sort fill's per-warp task list.  With
+// nozero (no off-diagonal hop weight is zero) a row's count is the popcount
+// of its pairs' target masks.
 __global__ void k_count(const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ diag,
                         const double* __restrict__ w, int nw, const double* __restrict__ da,
-                        const double* __restrict__ db, const int* __restrict__ off, int K, int upper,
-                        int64_t* __restrict__ rowlen)
+                        const double* __restrict__ db, const int* __restrict__ off, int K, int upper, int nozero,
+                        int64_t* __restrict__ rowlen, int* __restrict__ maxtasks)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const HopView hv = load_hop_smem(smem, w, nw, da, db, off, K);
+    unsigned tmax = 0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t in = words[r];
         int64_t cnt = (fabs(diag[r]) < kSparseZeroTol) ? 0 : 1;
+        unsigned tasks = 1;
         for (uint64_t ta = in; ta; ta &= ta - 1) {
             const int a = __ffsll((long long)ta) - 1;
             for (uint64_t tb = ta & (ta - 1); tb; tb &= tb - 1) {
                 const int b = __ffsll((long long)tb) - 1;
+                const uint64_t m0 = hop_targets(in, a, b, K, upper != 0);
+                const int pc = __popcll(m0);
+                tasks += pc;
+                if (nozero) {
+                    cnt += pc;
+                    continue;
+                }
                 const int s = a + b;
                 const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
-                const int lo = pair_lo(s, K), pc = pair_cnt(s, K);
-                for (int ic = 0; ic < pc; ++ic) {
-                    const int c = lo + ic, d = s - c;
-                    if (c == a) continue;
-                    if ((rest >> c) & 1ull) continue;
-                    if ((rest >> d) & 1ull) continue;
+                for (uint64_t m = m0; m; m &= m - 1) {
+                    const int c = __ffsll((long long)m) - 1, d = s - c;
                     const uint64_t out = rest | (1ull << c) | (1ull << d);
-                    if (upper && out < in) continue;
-                    if (hop_element(hv, in, out, a, b, c, d) != 0.0) ++cnt;
+                    if (!hop_zero(hop_bits(hv, in, out, a, b, c, d))) ++cnt;
                 }
             }
         }
         rowlen[r] = cnt;
+        tmax = tasks > tmax ? tasks : tmax;
     }
+    tmax = __reduce_max_sync(0xffffffffu, tmax);
+    if ((threadIdx.x & 31) == 0) atomicMax(maxtasks, (int)tmax);
 }
 
-// One warp per row: generate (out word, value), sort by word, rank, store.
+// One warp per row: generate (out word, value), sort by word in shared
+// memory, rank, store.  Any row length the shared memory holds, any sector.
 __global__ void k_fill(const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ diag,
                        const double* __restrict__ w, int nw, const double* __restrict__ da,
                        const double* __restrict__ db, const int* __restrict__ off, int K, int N, int upper,
@@ -117,10 +134,10 @@ __global__ void k_fill(const uint64_t* __restrict__ words, int64_t n, const doub
                 if ((rest >> d) & 1ull) continue;
                 const uint64_t out = rest | (1ull << c) | (1ull << d);
                 if (upper && out < in) continue;
-                const double v = hop_element(hv, in, out, a, b, c, d);
-                if (v == 0.0) continue;
+                const uint64_t vb = hop_bits(hv, in, out, a, b, c, d);
+                if (hop_zero(vb)) continue;
                 const int slot = atomicAdd(counter, 1);
-                if (slot < cap) { keys[slot] = out; vals[slot] = v; }
+                if (slot < cap) { keys[slot] = out; vals[slot] = bits_to_double(vb); }
             }
         }
         __syncwarp();
@@ -170,6 +187,200 @@ __global__ void k_fill(const uint64_t* __restrict__ words, int64_t n, const doub
     }
 }
 
+// ---------------------------------------------------------------------------
+// k_fill_reg: the same rows, sorted in registers.  The admissible hops of
+// each occupied pair (hop_targets) are expanded into a task list (a, b, c)
+// in shared memory, so that every task yields an element unless its weight
+// is zero, and the tasks are spread evenly over the lanes.  Each element is
+// ranked as it is generated and stored as a 32-bit key (column << sb | slot),
+// sb = log2(cap), with its value at vals[slot]; the host takes this kernel
+// only when every key fits below 0xFFFFFFFF.  Slots follow the task order
+// (one ballot per 32 tasks) and reuse the task list's storage: a slot never
+// passes the task that fills it.  The keys, padded to 32*E with 0xFFFFFFFF,
+// are sorted by a bitonic network over the element index lane*E + e:
+// exchanges whose partner is nearer than E stay in one lane's registers, the
+// rest take one shuffle.  The sorted keys go back through a swizzled
+// shared-memory image (index i ^ ((i >> 5) & 31), conflict-free both ways)
+// and are written coalesced.
+
+constexpr int kFillMaxE = 32;   // 32 * 32 = 1024 elements per row at most
+
+__host__ __device__ inline size_t fill_reg_warp_bytes(int cap)
+{
+    return ((size_t)cap * 12 + 64 + 15) & ~(size_t)15;
+}
+
+__device__ __forceinline__ int swz(int i) { return i ^ ((i >> 5) & 31); }
+
+template <int E>
+__device__ __forceinline__ void sort_row_keys(uint32_t* keys, int cnt, int lane)
+{
+    uint32_t k[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int t = e * 32 + lane;
+        k[e] = t < cnt ? keys[t] : 0xFFFFFFFFu;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int kk = 2; kk <= 32 * E; kk <<= 1) {
+#pragma unroll
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            if (j >= E) {
+                const int lj = j / E;
+                const bool lower = (lane & lj) == 0;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const bool up = (((lane * E + e) & kk) == 0);
+                    const uint32_t o = __shfl_xor_sync(0xffffffffu, k[e], lj);
+                    k[e] = (up == lower) ? min(k[e], o) : max(k[e], o);
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    if ((e & j) == 0) {
+                        const bool up = (((lane * E + e) & kk) == 0);
+                        const uint32_t x = k[e], y = k[e ^ j];
+                        const uint32_t lo = min(x, y), hi = max(x, y);
+                        k[e] = up ? lo : hi;
+                        k[e ^ j] = up ? hi : lo;
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) keys[swz(lane * E + e)] = k[e];
+    __syncwarp();
+}
+
+// Sort with the smallest E (a power of two, at most EM) with 32*E >= cnt.
+template <int E, int EM>
+__device__ __forceinline__ void sort_row_dispatch(uint32_t* keys, int cnt, int lane)
+{
+    if constexpr (E < EM) {
+        if (cnt > 32 * E) {
+            sort_row_dispatch<E * 2, EM>(keys, cnt, lane);
+            return;
+        }
+    }
+    sort_row_keys<E>(keys, cnt, lane);
+}
+
+template <int EM>
+__global__ void __launch_bounds__(256) k_fill_reg(
+    const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ diag, const double* __restrict__ w,
+    int nw, const double* __restrict__ da, const double* __restrict__ db, const int* __restrict__ off, int K, int N,
+    int upper, const int64_t* __restrict__ rowptr, const uint64_t* __restrict__ hi, const uint64_t* __restrict__ lo_tab,
+    int L, int cap, int sb, int32_t* __restrict__ col, double* __restrict__ val, int* __restrict__ err)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const HopView hv = load_hop_smem(smem, w, nw, da, db, off, K);
+    const size_t tbytes = (hop_smem_bytes(K, nw) + 15) & ~(size_t)15;
+    const int warp_in_cta = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int npairs = N * (N - 1) / 2;
+    unsigned char* wbase = smem + tbytes + (size_t)warp_in_cta * fill_reg_warp_bytes(cap);
+    double* vals = reinterpret_cast<double*>(wbase);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(wbase + (size_t)cap * 8);
+    unsigned char* occ = wbase + (size_t)cap * 12;
+    const uint32_t smask = (uint32_t)cap - 1u;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = gw; r < n; r += nwarps) {
+        const uint64_t in = words[r];
+        const int64_t base = rowptr[r];
+        const int64_t want = rowptr[r + 1] - base;
+        for (int pos0 = 0; pos0 < K; pos0 += 32) {
+            const int pos = pos0 + lane;
+            const bool set = pos < K && ((in >> pos) & 1ull);
+            const unsigned m = __ballot_sync(0xffffffffu, set);
+            if (set) occ[__popc(m & lt) + __popcll(in & ((1ull << pos0) - 1ull))] = (unsigned char)pos;
+        }
+        __syncwarp();
+        // task list: the admissible (a, b, c) of every occupied pair
+        int total = 0;
+        for (int p0 = 0; p0 < npairs; p0 += 32) {
+            const int p = p0 + lane;
+            uint64_t m = 0;
+            int a = 0, b = 0;
+            if (p < npairs) {
+                int j = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)p)) * 0.5f);
+                while (j * (j - 1) / 2 > p) --j;
+                while ((j + 1) * j / 2 <= p) ++j;
+                a = occ[p - j * (j - 1) / 2];
+                b = occ[j];
+                m = hop_targets(in, a, b, K, upper != 0);
+            }
+            const int pc = __popcll(m);
+            int x = pc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            int pos = total + x - pc;
+            for (; m; m &= m - 1, ++pos)
+                if (pos < cap) keys[pos] = (uint32_t)(a | (b << 6) | ((__ffsll((long long)m) - 1) << 12));
+            total += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
+        if (total >= cap) {   // the count pass sized cap above every row's tasks
+            if (lane == 0) atomicOr(err, 4);
+            __syncwarp();
+            continue;
+        }
+        int cnt = 0;
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            const uint32_t task = t < total ? keys[t] : 0u;
+            __syncwarp();
+            uint32_t key = 0;
+            uint64_t vb = 0;
+            bool ok = false;
+            if (t < total) {
+                const int a = task & 63, b = (task >> 6) & 63, c = (task >> 12) & 63, d = a + b - c;
+                const uint64_t out = in ^ (1ull << a) ^ (1ull << b) ^ (1ull << c) ^ (1ull << d);
+                vb = hop_bits(hv, in, out, a, b, c, d);
+                if (!hop_zero(vb)) {
+                    const uint64_t rk = rank_in_sector(out, hi, lo_tab, L);
+                    if (rk == kMiss) atomicOr(err, 2);
+                    key = (uint32_t)rk << sb;
+                    ok = true;
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                const int slot = cnt + __popc(m & lt);
+                keys[slot] = key | (uint32_t)slot;
+                vals[slot] = bits_to_double(vb);
+            }
+            cnt += __popc(m);
+        }
+        const double dv = diag[r];
+        if (!(fabs(dv) < kSparseZeroTol)) {
+            if (lane == 0 && cnt < cap) {
+                keys[cnt] = ((uint32_t)r << sb) | (uint32_t)cnt;
+                vals[cnt] = dv;
+            }
+            ++cnt;
+        }
+        __syncwarp();
+        if (cnt != want || cnt > cap) {
+            if (lane == 0) atomicOr(err, 1);
+            __syncwarp();
+            continue;
+        }
+        if (cnt > 0) sort_row_dispatch<1, EM>(keys, cnt, lane);
+        for (int t = lane; t < cnt; t += 32) {
+            const uint32_t kk = keys[swz(t)];
+            col[base + t] = (int32_t)(kk >> sb);
+            val[base + t] = vals[kk & smask];
+        }
+        __syncwarp();
+    }
+}
+
 int sm_count()
 {
     int dev = 0, sms = 148;
@@ -208,12 +419,25 @@ void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, c
     DevBuf<double> diag(n);
     ham_diagonal(b, t, diag.p, st);
     DevBuf<int64_t> rowlen(n);
+    // with no zero off-diagonal weight every admissible hop is stored
+    int nozero = 1;
+    for (int s = 1; s <= 2 * K - 3 && nozero; ++s) {
+        const int cnt = pair_cnt(s, K);
+        for (int ia = 0; ia < cnt && nozero; ++ia)
+            for (int ic = 0; ic < cnt; ++ic)
+                if (ic != ia && t.hop.w[t.hop.hop_off[s] + ia * cnt + ic] == 0.0) { nozero = 0; break; }
+    }
+    DevBuf<int> maxtasks_dev(1);
+    ED_CUDA(cudaMemsetAsync(maxtasks_dev.p, 0, sizeof(int), st));
     ED_CUDA(cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     k_count<<<sm_count() * 4, 256, tsm, st>>>(b.words.p, n, diag.p, t.w_dev.p, nw, t.diag_a_dev.p, t.diag_b_dev.p,
-                                              t.hop_off_dev.p, K, a.upper, rowlen.p); ::edgb::count_launch();
+                                              t.hop_off_dev.p, K, a.upper, nozero, rowlen.p, maxtasks_dev.p);
+    ::edgb::count_launch();
     ED_CUDA(cudaGetLastError());
     exclusive_scan_i64(rowlen.p, a.rowptr.p, n, st);
     ED_CUDA(cudaMemcpyAsync(&a.nnz, a.rowptr.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    int maxtasks = 0;
+    ED_CUDA(cudaMemcpyAsync(&maxtasks, maxtasks_dev.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     const int64_t maxrow = reduce_max_i64_host(rowlen.p, n, st);
     ED_CUDA(cudaStreamSynchronize(st));
     a.max_row = (int)maxrow;
@@ -223,11 +447,51 @@ void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, c
     a.val.alloc((size_t)a.nnz + kCrsPad);
     ED_CUDA(cudaMemsetAsync(a.col.p + a.nnz, 0, kCrsPad * sizeof(int32_t), st));
     ED_CUDA(cudaMemsetAsync(a.val.p + a.nnz, 0, kCrsPad * sizeof(double), st));
-    int cap = 32;
-    while (cap < maxrow) cap <<= 1;
+    int cap = 32, sb = 5;
+    while (cap < maxrow) { cap <<= 1; ++sb; }
     const size_t tbytes = (tsm + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)cap * 16 + 4 + 64;
     const size_t budget = 200 * 1024;
+    DevBuf<int> err(1);
+    ED_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+    // register sort when a row's tasks and elements fit 32*kFillMaxE keys of
+    // (column << rsb | slot) below 0xFFFFFFFF; ED_FILL_SORT=smem selects the
+    // shared-memory sort for every sector
+    int rcap = 32, rsb = 5;
+    while (rcap < std::max<int64_t>(maxrow, maxtasks + 1)) { rcap <<= 1; ++rsb; }
+    const size_t reg_warp = fill_reg_warp_bytes(rcap);
+    const char* sort_env = std::getenv("ED_FILL_SORT");
+    const bool force_smem = sort_env && std::strcmp(sort_env, "smem") == 0;
+    if (!force_smem && rcap <= 32 * kFillMaxE &&
+        ((((uint64_t)(n - 1)) << rsb) | (uint64_t)(rcap - 1)) < 0xFFFFFFFFull && tbytes + reg_warp <= budget) {
+        const int smax = std::min<int>(8, (int)((budget - tbytes) / reg_warp));
+        auto launch = [&](auto kern) {
+            // warps per CTA: the most resident warps per SM, then the larger CTA
+            int wpc = smax, best = 0, occ_best = 1;
+            for (int c = smax; c >= 1; --c) {
+                const size_t sm_c = tbytes + (size_t)c * reg_warp;
+                ED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_c));
+                int ob = 0;
+                ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ob, kern, c * 32, sm_c));
+                if (ob * c > best) { best = ob * c; wpc = c; occ_best = ob < 1 ? 1 : ob; }
+            }
+            const size_t smem = tbytes + (size_t)wpc * reg_warp;
+            ED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<sm_count() * occ_best, wpc * 32, smem, st>>>(
+                b.words.p, n, diag.p, t.w_dev.p, nw, t.diag_a_dev.p, t.diag_b_dev.p, t.hop_off_dev.p, K, b.N,
+                a.upper, a.rowptr.p, b.hi.p, b.lo.p, b.low_bits, rcap, rsb, a.col.p, a.val.p, err.p);
+            ::edgb::count_launch();
+        };
+        if (rcap <= 128) launch(k_fill_reg<4>);
+        else if (rcap <= 512) launch(k_fill_reg<16>);
+        else launch(k_fill_reg<32>);
+        ED_CUDA(cudaGetLastError());
+        int herr = 0;
+        ED_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        ED_REQUIRE(herr == 0, ED_ERR_INTERNAL, "Hamiltonian fill: row count or rank check failed on the device");
+        return;
+    }
+    const size_t per_warp = (size_t)cap * 16 + 4 + 64;
     ED_REQUIRE(tbytes + per_warp <= budget, ED_ERR_RANGE, "Hamiltonian rows too long for the shared-memory sort");
     int wpc = (int)((budget - tbytes) / per_warp);
     if (wpc > 16) wpc = 16;
@@ -236,8 +500,6 @@ void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, c
     int occ_blocks = 0;
     ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_blocks, k_fill, wpc * 32, smem));
     if (occ_blocks < 1) occ_blocks = 1;
-    DevBuf<int> err(1);
-    ED_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
     k_fill<<<sm_count() * occ_blocks, wpc * 32, smem, st>>>(b.words.p, n, diag.p, t.w_dev.p, nw, t.diag_a_dev.p,
                                                              t.diag_b_dev.p, t.hop_off_dev.p, K, b.N, a.upper,
                                                              a.rowptr.p, b.hi.p, b.lo.p, b.low_bits, cap, a.col.p,

@@ -98,18 +98,15 @@ __global__ void __launch_bounds__(256) k_hv_matfree(const uint64_t* __restrict__
                 const int b = __ffsll((long long)tb) - 1;
                 const int s = a + b;
                 const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
-                const int lo = pair_lo(s, K), pc = pair_cnt(s, K);
-                for (int ic = 0; ic < pc; ++ic) {
-                    const int c = lo + ic, d = s - c;
-                    if (c == a) continue;
-                    if ((rest >> c) & 1ull) continue;
-                    if ((rest >> d) & 1ull) continue;
+                // admissible c ascending, the order of the reference's k2 loop
+                for (uint64_t m = hop_targets(in, a, b, K, false); m; m &= m - 1) {
+                    const int c = __ffsll((long long)m) - 1, d = s - c;
                     const uint64_t out = rest | (1ull << c) | (1ull << d);
-                    const double v = hop_element(hv, in, out, a, b, c, d);
-                    if (v == 0.0) continue;
+                    const uint64_t vb = hop_bits(hv, in, out, a, b, c, d);
+                    if (hop_zero(vb)) continue;
                     const uint64_t j = rank_in_sector(out, hi, lo_tab, L);
                     if (j >= (uint64_t)n) continue;   // cannot happen for a sector word; never read out of range
-                    acc = fma(v, __ldg(x + j), acc);
+                    acc = fma(bits_to_double(vb), __ldg(x + j), acc);
                 }
             }
         }

@@ -3,6 +3,7 @@
     python -m hamiltonian_diagonalization_gb300.microbench --sector 11,31,0 --reps 20 [--upper] [--matfree]
     python -m hamiltonian_diagonalization_gb300.microbench --sector 10,28,0 --batch 32 --reps 20
     python -m hamiltonian_diagonalization_gb300.microbench --rotate 1371535,41,25 --reps 20
+    python -m hamiltonian_diagonalization_gb300.microbench --sector 11,31,0 --build --reps 3 [--upper]
 
 Builds the sector's Hamiltonian (LLL Coulomb pseudopotentials, odd m) on the
 device, then times `reps` products with CUDA events on the launching stream
@@ -14,6 +15,9 @@ With --batch B it times the block product of B Hamiltonians of the sector
 per second (one FMA per stored element per Hamiltonian, diagonal included).
 With --rotate n,m,k it times the thick-restart rotation of an n x m basis
 into k Ritz vectors (ed_basis_rotate) in FP64 and on the tensor cores.
+With --build it times the whole CRS build (diagonal, count, scan, fill;
+host clock around a synchronised call, best of reps) with the register-sort
+fill and with the shared-memory fill (ED_FILL_SORT=smem).
 """
 from __future__ import annotations
 
@@ -34,6 +38,8 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="time the block product of this many Hamiltonians")
     ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default tile (32 per row, L1)")
     ap.add_argument("--rotate", default="", help="n,m,k: time the restart rotation instead")
+    ap.add_argument("--build", action="store_true",
+                    help="time the CRS build instead (register sort, then ED_FILL_SORT=smem)")
     args = ap.parse_args()
     import torch
 
@@ -45,6 +51,8 @@ def main():
     N, norb, tlz = (int(x) for x in args.sector.split(","))
     if args.batch:
         return batch_main(ed, C, torch, N, norb, tlz, args)
+    if args.build:
+        return build_main(ed, torch, N, norb, tlz, args)
     H = ed.SpinlessFermionHamiltonian()
     H.Initialize(N, norb, twoLz=tlz)
     T = ed.QuarticTermTables(norb, ed.odd_coulomb_list(norb))
@@ -71,6 +79,33 @@ def main():
         by = nnz * 12 + (n + 1) * 8 + 2 * n * 8
         out.update({"nnz": nnz, "bytes_per_product": by, "GBps": by / ms / 1e6})
     print(json.dumps(out))
+
+
+def build_main(ed, torch, N, norb, tlz, args):
+    import os
+    import time
+    T = ed.QuarticTermTables(norb, ed.odd_coulomb_list(norb))
+    res = {"sector": [N, norb, tlz], "mode": "build", "layout": "upper" if args.upper else "full"}
+    for name, env in (("register", None), ("smem", "smem")):
+        if env:
+            os.environ["ED_FILL_SORT"] = env
+        else:
+            os.environ.pop("ED_FILL_SORT", None)
+        times = []
+        for i in range(args.warmup + args.reps):
+            H = ed.SpinlessFermionHamiltonian()
+            H.Initialize(N, norb, twoLz=tlz)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            H.Add_CdCdCC_Terms(T, store_upper=args.upper)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+            res["n"], res["nnz"] = H.GetDimension(), H.m_crsSparseMatrix.GetNbrNonZeros()
+            del H
+        res[f"ms_build_{name}"] = 1e3 * min(times)
+    os.environ.pop("ED_FILL_SORT", None)
+    print(json.dumps(res))
 
 
 def batch_main(ed, C, torch, N, norb, tlz, args):

@@ -83,3 +83,17 @@ def test_stored_crs_at_scale_row_samples(cuda, oracle):
     first = col[rp[:-1][nonempty]]
     ndiag = int(np.sum(first == np.arange(n)[nonempty]))
     assert nf == 2 * (len(col)) - ndiag
+
+
+@pytest.mark.parametrize("case,upper", [((8, 22, 0), True), ((10, 28, 0), False), ((3, 40, 0), True)])
+def test_register_and_shared_memory_sorts_agree(cuda, oracle, monkeypatch, case, upper):
+    # the register-sort fill and the shared-memory fill (taken for rows or
+    # sectors too large for 32-bit keys) write identical arrays
+    N, norb, tlz = case
+    pp = oracle.sweep_list(norb, 0.9)
+    H1, _ = build_gpu(N, norb, tlz, pp, upper)
+    monkeypatch.setenv("ED_FILL_SORT", "smem")
+    H2, _ = build_gpu(N, norb, tlz, pp, upper)
+    a, b = H1.m_crsSparseMatrix.to_host(), H2.m_crsSparseMatrix.to_host()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(a[2].view(np.uint64), b[2].view(np.uint64))
