@@ -9,7 +9,9 @@ H(V1) = V1*P_1 + sum_{odd m >= 3} V_m^Coulomb P_m with V1 in
 linspace(0.5, 3.0, points).  `plain` calls ed_solve_sector once per
 Hamiltonian (basis, tables, CRS build and Lanczos each time, seeded random
 start); `batched` builds each sector's shared pattern once and solves all its
-Hamiltonians together (ed_batch_solve).  Prints one JSON line with both
+Hamiltonians together (ed_batch_solve); `warm` adds the learned MLP start for
+held-out points; `continuation` solves every stride-th point from random
+starts and the others from their nearest solved neighbour's eigenvectors.  Prints one JSON line with both
 timings, their ratio, and the largest eigenvalue difference between the two
 paths (the parity check of the batched solver).
 """
@@ -207,6 +209,72 @@ def run_warm(N, norb, sectors, v1s, nev, tol, seed, held_frac=0.25, steps=4000, 
     return total, evals, rec
 
 
+def continuation_plan(v1s, stride: int = 4):
+    """Anchor points of a continuation sweep (every stride-th V1, so that 64
+    points give 32 or 16 anchors: whole tiles of the block product) and, for
+    each other point, its nearest anchor (the lower one on a tie)."""
+    npts = len(v1s)
+    anchors = np.arange(0, npts, stride)
+    rest = np.array([i for i in range(npts) if i not in set(anchors.tolist())], dtype=int)
+    near = np.array([int(np.argmin(np.abs(v1s[anchors] - v1s[i]))) for i in rest], dtype=int)
+    return anchors, rest, near
+
+
+def continuation_start(vecs, near, nev: int, extra_weight: float = 0.1):
+    """Start vectors [n][len(near)] from anchor eigenvectors vecs [nev+extra][n][anchors]:
+    the sum of each nearest anchor's nev lowest states plus extra_weight times
+    its next ones (present in the start in case they cross below the nev-th
+    state between the two points), normalised."""
+    import torch
+    w = torch.full((vecs.shape[0],), extra_weight, dtype=vecs.dtype, device=vecs.device)
+    w[:nev] = 1.0
+    idx = torch.as_tensor(near, device=vecs.device, dtype=torch.long)
+    V0 = (vecs.index_select(2, idx) * w[:, None, None]).sum(0)
+    return (V0 / torch.linalg.vector_norm(V0, dim=0, keepdim=True)).contiguous()
+
+
+def run_continuation(N, norb, sectors, v1s, nev, tol, seed, stride=4, extra=2, extra_weight=0.1, batch_size=0,
+                     ncv=0):
+    """Batched + continuation warm start.  Per sector: solve the anchor points
+    (continuation_plan) batched from random starts for nev+extra states with
+    their vectors, then every other point batched from its nearest anchor's
+    states (continuation_start).  Same tolerance and convergence test as the
+    random-start sweep; returns (seconds, {(sector, j): eigenvalues}, records)."""
+    import torch
+
+    import hamiltonian_diagonalization_gb300 as ed
+    lists = sweep_lists(norb, v1s)
+    anchors, rest, near = continuation_plan(v1s, stride)
+    evals, rec = {}, []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for tlz in sectors:
+        ts = time.perf_counter()
+        b = ed.FermionFockBasis()
+        b.GenerateFockSpace(N, norb, tlz)
+        ba = ed.HamiltonianBatch(b, [lists[j] for j in anchors])
+        ev_a, vec_a, inf_a = ba.solve(nev + extra, tol=tol, seed=seed, want_vectors=True, ncv=ncv)
+        for k, j in enumerate(anchors):
+            evals[(tlz, int(j))] = ev_a[k, :nev]
+        bs = batch_size or len(rest)
+        prod_w = 0
+        for j0 in range(0, len(rest), bs):
+            sel = rest[j0:j0 + bs]
+            bw = ed.HamiltonianBatch(b, [lists[j] for j in sel])
+            V0 = continuation_start(vec_a, near[j0:j0 + bs], nev, extra_weight)
+            ev_w, _, inf_w = bw.solve(nev, tol=tol, V0=V0, ncv=ncv)
+            prod_w += inf_w["problem_products"]
+            for k, j in enumerate(sel):
+                evals[(tlz, int(j))] = ev_w[k]
+        del vec_a
+        torch.cuda.synchronize()
+        rec.append({"two_lz": tlz, "seconds": time.perf_counter() - ts, "anchors": len(anchors),
+                    "anchor_problem_products": inf_a["problem_products"], "warm_points": len(rest),
+                    "warm_problem_products": prod_w})
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, evals, rec
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--N", type=int, default=10)
@@ -216,7 +284,8 @@ def main():
     ap.add_argument("--nev", type=int, default=4)
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--mode", default="both", choices=["plain", "batched", "both", "warm", "all"])
+    ap.add_argument("--mode", default="both", choices=["plain", "batched", "both", "warm", "continuation", "all"])
+    ap.add_argument("--stride", type=int, default=4, help="continuation: one anchor every stride V1 points")
     ap.add_argument("--mlp-steps", type=int, default=4000)
     ap.add_argument("--mlp-lr", type=float, default=2e-3)
     ap.add_argument("--batch-size", type=int, default=0, help="Hamiltonians per batch (0: all of a sector)")
@@ -241,9 +310,14 @@ def main():
         tw, ew, rec = run_warm(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, steps=args.mlp_steps,
                                lr=args.mlp_lr, batch_size=args.batch_size, ncv=args.ncv)
         out["batched_warm"] = {"seconds": tw, "solves_per_s": nsolve / tw, "per_sector": rec}
-    if args.mode in ("batched", "both", "all"):
+    if args.mode in ("batched", "both", "continuation", "all"):
         # one untimed warm-up batch (module load, autotune code paths)
         run_batched(args.N, args.norb, sectors[:1], v1s[:2], args.nev, args.tol, args.seed)
+    if args.mode in ("continuation", "all"):
+        tc, ec, rec = run_continuation(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed,
+                                       stride=args.stride, batch_size=args.batch_size, ncv=args.ncv)
+        out["batched_continuation"] = {"seconds": tc, "solves_per_s": nsolve / tc, "per_sector": rec}
+    if args.mode in ("batched", "both", "all"):
         tb, eb, infos = run_batched(args.N, args.norb, sectors, v1s, args.nev, args.tol, args.seed, args.batch_size,
                                     args.ncv)
         out["batched"] = {"seconds": tb, "solves_per_s": nsolve / tb,
@@ -261,6 +335,9 @@ def main():
         out["speedup_batched_vs_plain"] = out["plain"]["seconds"] / out["batched"]["seconds"]
         out["max_rel_eigenvalue_diff"] = float(max(np.max(np.abs(eb[k] - ep[k]) / np.abs(ep[k])) for k in ep))
     if args.mode == "all":
+        out["speedup_batched_continuation_vs_plain"] = out["plain"]["seconds"] / out["batched_continuation"]["seconds"]
+        out["max_rel_eigenvalue_diff_continuation"] = float(max(np.max(np.abs(ec[k] - ep[k]) / np.abs(ep[k]))
+                                                                for k in ep))
         out["speedup_batched_warm_vs_plain"] = out["plain"]["seconds"] / out["batched_warm"]["seconds"]
         out["max_rel_eigenvalue_diff_warm"] = float(max(np.max(np.abs(ew[k] - ep[k]) / np.abs(ep[k])) for k in ep))
     print(json.dumps(out))

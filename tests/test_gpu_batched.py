@@ -118,3 +118,21 @@ def test_converged_hamiltonians_retire_from_the_batch(cuda):
         # same eigenvectors up to sign (the levels are not degenerate here)
         ov = np.abs(np.sum(V[:, :, j] * out["eigenvectors"], axis=1))
         assert np.min(ov) > 1 - 1e-8, (j, ov)
+
+
+def test_continuation_sweep_matches_random_starts(cuda):
+    # anchors from random starts, the rest from their nearest anchor's states:
+    # the same eigenvalues as random starts, in fewer products
+    from hamiltonian_diagonalization_gb300 import sweep
+    N, norb, nev = 8, 22, 3
+    v1s = np.linspace(0.5, 3.0, 16)
+    tc, ec, rec = sweep.run_continuation(N, norb, [0], v1s, nev, 1e-10, 1)
+    tb, eb, infos = sweep.run_batched(N, norb, [0], v1s, nev, 1e-10, 1)
+    assert sorted(ec) == sorted(eb)
+    for k in eb:
+        assert np.max(np.abs(ec[k] - eb[k]) / np.abs(eb[k])) <= 1e-10, k
+    r = rec[0]
+    assert r["anchors"] + r["warm_points"] == len(v1s)
+    per_warm = r["warm_problem_products"] / r["warm_points"]
+    per_random = infos[0]["problem_products"] / len(v1s)
+    assert per_warm < per_random, (per_warm, per_random)

@@ -64,3 +64,18 @@ def test_sharding_covers_every_unit_once():
     for world in (1, 2, 3, 8):
         got = [u for r in range(world) for u in sweep.shard(units, r, world)]
         assert sorted(got) == sorted(units)
+
+
+@pytest.mark.parametrize("npts,stride", [(64, 4), (5, 4), (9, 4), (12, 3), (1, 4)])
+def test_continuation_plan_covers_points_once(npts, stride):
+    import numpy as np
+
+    from hamiltonian_diagonalization_gb300 import sweep
+    v1s = np.linspace(0.5, 3.0, npts)
+    anchors, rest, near = sweep.continuation_plan(v1s, stride)
+    assert sorted(anchors.tolist() + rest.tolist()) == list(range(npts))
+    assert anchors[0] == 0 and np.all(np.diff(anchors) == stride)
+    step = v1s[1] - v1s[0] if npts > 1 else 0.0
+    for i, a in zip(rest, near):
+        d = np.abs(v1s[anchors] - v1s[i])
+        assert d[a] == d.min() and d[a] <= (stride - 1) * step + 1e-12
