@@ -388,7 +388,7 @@ def main():
                       "nnz_full": nnz},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (traffic or {}).get("bytes_per_launch"),
-                         "kernel": "k_spmv_full<8>", "bytes_per_launch": bytes_per,
+                         "kernel": "k_spmv_full<8,4>", "bytes_per_launch": bytes_per,
                          "avg_launch_ms": spmv_s * 1000.0, "standalone_launch_ms": r["spmv_ms_alone"],
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s"},

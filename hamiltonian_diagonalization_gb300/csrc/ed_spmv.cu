@@ -21,13 +21,14 @@ __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p);
 __device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
 
 // G lanes per row, each lane summing every G-th element of the row in one
-// FMA chain.  Measured on GB300 (N=11, 2S=30, same process, 20 products):
-// G=8 one chain 0.825 ms (5.1 TB/s, 75% of the measured copy peak); two
-// chains 0.885 ms, four chains 1.04 ms, G=4 or 16 >= 1.04 ms; deeper
-// unguarded batches (G=4, 8 loads in flight) 1.31 ms.  The extra chains cost
-// registers and FP64 additions without adding useful memory parallelism: the
-// warps of a full SM already keep the DRAM queue busy.
-template <int G>
+// FMA chain, with the loads of U of its elements issued ahead of their FMAs
+// (same element order, so U does not change y).  Measured on GB300 (N=11,
+// 2S=30, 30 products): G=8 U=4 0.835-0.841 ms, U=2 0.841, U=1 0.862, U=8
+// 0.869; G=4 U=2/4 0.90/0.93 ms, G=16 0.91 ms; two or four FMA chains per
+// lane 0.89-1.04 ms.  The extra chains cost registers and FP64 additions
+// without adding useful memory parallelism: the warps of a full SM already
+// keep the DRAM queue busy.
+template <int G, int U = 1>
 __global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                    const double* __restrict__ val, const double* __restrict__ x,
                                                    double* __restrict__ y, int64_t n)
@@ -41,7 +42,23 @@ __global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ r
         const bool valid = r < n;
         const int64_t s = valid ? rowptr[r] : 0, e = valid ? rowptr[r + 1] : 0;
         double acc = 0.0;
-        for (int64_t k = s + sub; k < e; k += G) acc = fma(ld_stream(val + k), __ldg(x + ld_stream(col + k)), acc);
+        if (U == 1) {
+            for (int64_t k = s + sub; k < e; k += G) acc = fma(ld_stream(val + k), __ldg(x + ld_stream(col + k)), acc);
+        } else {
+            for (int64_t k0 = s + sub; k0 < e; k0 += (int64_t)G * U) {
+                double v[U];
+                int c[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int64_t k = k0 + (int64_t)u * G;
+                    v[u] = k < e ? ld_stream(val + k) : 0.0;
+                    c[u] = k < e ? ld_stream(col + k) : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (k0 + (int64_t)u * G < e) acc = fma(v[u], __ldg(x + c[u]), acc);
+            }
+        }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
         if (valid && sub == 0) y[r] = acc;
@@ -130,9 +147,10 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
     const double avg = a.n ? (double)a.nnz / (double)a.n : 0.0;
     const int threads = 256;
     const int grid = sms() * 8;
-    if (!a.upper) {
-        if (avg >= 96) k_spmv_full<8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
-        else if (avg >= 24) k_spmv_full<4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+    if (!a.upper && avg >= 96) {
+        k_spmv_full<8, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+    } else if (!a.upper) {
+        if (avg >= 24) k_spmv_full<4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
         else k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else {
         ED_CUDA(cudaMemsetAsync(y, 0, (size_t)a.n * sizeof(double), st));
