@@ -533,9 +533,22 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     w.n = n;
     w.m = m;
     w.nb = (int)std::max<int64_t>(1, std::min<int64_t>(nsm * 4, n / 1024));
-    // multi-dot slices: about two blocks per SM, 512..4096 rows (a multiple of 128)
-    w.R = (int)std::min<int64_t>(4096, std::max<int64_t>(512, ((n + 2 * nsm - 1) / (2 * nsm) + 127) / 128 * 128));
-    w.nbm = (int)((n + w.R - 1) / w.R);
+    // multi-dot slices: three blocks per SM, a whole wave (a cap of 4096 rows
+    // gave 335 blocks at the headline size, 2 or 3 per SM, and a Lanczos phase
+    // 2 % longer; 2 or 4 blocks per SM measured 0.3 / 0.6 % longer than 3),
+    // at least 512 and at most 12288 rows (a multiple of 128)
+    {
+        int64_t nbt = (int64_t)nsm * 3, R = 0;
+        for (;;) {
+            R = std::max<int64_t>(512, ((n + nbt - 1) / nbt + 127) / 128 * 128);
+            if (R <= 12288) break;
+            nbt += nsm;
+        }
+        w.R = (int)R;
+        w.nbm = (int)((n + R - 1) / R);
+        if ((size_t)R * 8 > 48 * 1024)
+            ED_CUDA(cudaFuncSetAttribute(k_mdot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(R * 8)));
+    }
     w.V.alloc((size_t)n * (m + 1));
     w.V2.alloc((size_t)n * (m + 1));
     w.part.alloc((size_t)(m + 2) * std::max(w.nb, w.nbm));
