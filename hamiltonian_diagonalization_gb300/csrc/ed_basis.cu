@@ -16,6 +16,7 @@
 //   rank(w) = offset(hi[w>>L]) + rank(lo[w & mask]),  miss if classes differ.
 // Same words, same order, same indices as the reference: each word of the
 // sector has exactly one (h,l) split and both orders are the numeric order.
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 
@@ -139,7 +140,7 @@ __global__ void k_basis_fill(int H, int L, const int64_t* __restrict__ offs, con
         const int64_t cnt = counts[h];
         const uint16_t cls = need_class[h];
         if (lane == 0) hi[h] = ((uint64_t)cls << 48) | (uint64_t)off;
-        if (cnt == 0) continue;
+        if (cnt == 0 || !words) continue;
         const uint32_t start = class_start[cls];
         const uint64_t hw = (uint64_t)h << L;
         for (int64_t t = lane; t < cnt; t += 32) words[off + t] = hw | (uint64_t)class_list[start + t];
@@ -275,6 +276,46 @@ void basis_build(ed_basis& b, cudaStream_t st)
                                                          b.words.p, b.hi.p); ::edgb::count_launch();
     ED_CUDA(cudaGetLastError());
     ED_CUDA(cudaStreamSynchronize(st));
+}
+
+void basis_compact_tables(const ed_basis& b, cudaStream_t st)
+{
+    if (b.mf_lo.p || b.dim == 0) return;
+    const int norb = b.norb, L = std::min(13, norb), H = norb - L;
+    if (H > 23) return;   // high table over 64 MB: the matrix-free product keeps the main tables
+    const int max_sum_low = L * (L - 1) / 2;
+    const int nclass = (L + 1) * (max_sum_low + 1);
+    const uint64_t nl = 1ull << L;
+    std::vector<uint32_t> ccount(nclass, 0);
+    std::vector<uint32_t> lo(nl);
+    for (uint64_t l = 0; l < nl; ++l) {
+        int pop = __builtin_popcountll(l), sum = 0;
+        for (uint64_t x = l; x; x &= x - 1) sum += __builtin_ctzll(x);
+        const int cls = pop * (max_sum_low + 1) + sum;
+        lo[l] = ((uint32_t)cls << 16) | ccount[cls]++;   // classes < 2^16, ranks < C(13,6) < 2^16
+    }
+    DevBuf<uint32_t> d_ccount(nclass);
+    ED_CUDA(cudaMemcpyAsync(d_ccount.p, ccount.data(), nclass * 4, cudaMemcpyHostToDevice, st));
+    const int64_t nh = 1ll << H;
+    DevBuf<int64_t> counts(nh), offs(nh + 1);
+    DevBuf<uint16_t> need(nh);
+    DevBuf<uint64_t> hi(nh);
+    k_basis_count<<<grid_for(nh, 256), 256, 0, st>>>(H, L, b.N, b.sector_sum, max_sum_low, d_ccount.p, counts.p,
+                                                     need.p); ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    exclusive_scan_i64(counts.p, offs.p, nh, st);
+    k_basis_fill<<<grid_for(nh * 32, 256), 256, 0, st>>>(H, L, offs.p, counts.p, need.p, nullptr, nullptr, nullptr,
+                                                         hi.p); ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    DevBuf<uint32_t> dlo(nl);
+    ED_CUDA(cudaMemcpyAsync(dlo.p, lo.data(), nl * 4, cudaMemcpyHostToDevice, st));
+    int64_t total = 0;
+    ED_CUDA(cudaMemcpyAsync(&total, offs.p + nh, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    ED_REQUIRE(total == (int64_t)b.dim, ED_ERR_INTERNAL, "compact rank tables disagree with the basis size");
+    b.mf_hi = std::move(hi);
+    b.mf_lo = std::move(dlo);
+    b.mf_low_bits = L;
 }
 
 void basis_rank(const ed_basis& b, const uint64_t* words, uint64_t* idx, uint64_t m, cudaStream_t st)

@@ -61,7 +61,7 @@ int sms_b()
 }
 
 // Element code for the pair hop (a,b)->(c,d) of `in` (canonical direction
-// as in hop_element); keep = the hop exists in at least one Hamiltonian.
+// as in hop_bits); keep = the hop exists in at least one Hamiltonian.
 __device__ __forceinline__ uint16_t hop_code(const HopView& hv, uint64_t in, uint64_t out, int a, int b, int c, int d,
                                              bool& keep)
 {

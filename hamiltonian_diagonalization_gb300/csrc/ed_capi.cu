@@ -332,6 +332,7 @@ ed_status ed_hv_matfree(const ed_basis* b, const ed_terms* t, const double* x_de
         ED_NONNULL(y_dev);
         ED_REQUIRE(x_dev != y_dev, ED_ERR_ARG, "x and y must be distinct");
         cudaStream_t st = (cudaStream_t)stream;
+        basis_compact_tables(*b, st);
         DevBuf<double> diag(b->dim);
         ham_diagonal(*b, *t, diag.p, st);
         hv_matfree(*b, *t, diag.p, x_dev, y_dev, st);
@@ -369,6 +370,7 @@ ed_status ed_op_matfree(const ed_basis* b, const ed_terms* t, ed_op** out)
             op->terms = t;
             op->diag.alloc(b->dim ? b->dim : 1);
             if (b->dim) ham_diagonal(*b, *t, op->diag.p, nullptr);
+            basis_compact_tables(*b, nullptr);   // before any product is captured into a graph
             ED_CUDA(cudaStreamSynchronize(nullptr));
         } catch (...) {
             delete op;
@@ -511,6 +513,7 @@ ed_status ed_solve_sector(int N, int norb, int two_lz, const double* pp, int npp
             op.terms = &t;
             op.diag.alloc(b.dim);
             ham_diagonal(b, t, op.diag.p, nullptr);
+            basis_compact_tables(b, nullptr);
         } else {
             ham_build_crs(b, t, 0, a, nullptr);
             op.kind = ed_op::CRS;

@@ -158,6 +158,12 @@ struct ed_basis {
     edgb::DevBuf<uint64_t> words;   // dim ascending words
     edgb::DevBuf<uint64_t> hi;      // 2^high_bits: (class << 48) | offset
     edgb::DevBuf<uint64_t> lo;      // 2^low_bits : (class << 32) | rank in class
+    // Compact rank tables for the matrix-free product (basis_compact_tables):
+    // the same scheme with mf_low_bits (<= 13) low bits, whose 4-byte
+    // (class << 16) | rank entries fit in shared memory.  Built on first use.
+    mutable int mf_low_bits = 0;
+    mutable edgb::DevBuf<uint64_t> mf_hi;   // 2^(norb - mf_low_bits): (class << 48) | offset
+    mutable edgb::DevBuf<uint32_t> mf_lo;   // 2^mf_low_bits: (class << 16) | rank in class
 };
 
 struct ed_terms {
@@ -184,6 +190,7 @@ struct ed_crs {
 namespace edgb {
 void basis_build(ed_basis& b, cudaStream_t st);
 void basis_rank(const ed_basis& b, const uint64_t* words, uint64_t* idx, uint64_t m, cudaStream_t st);
+void basis_compact_tables(const ed_basis& b, cudaStream_t st);
 void terms_upload(ed_terms& t);
 void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream_t st);
 void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, cudaStream_t st);

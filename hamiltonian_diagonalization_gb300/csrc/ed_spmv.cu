@@ -11,6 +11,9 @@
 // serially into two chains, and only log2(G) shuffle additions per lane
 // remain.  Column and value streams are read once with evict-first loads so
 // that x stays resident in L2.
+#include <algorithm>
+#include <map>
+
 #include "ed_hop.cuh"
 
 namespace edgb {
@@ -19,6 +22,13 @@ namespace {
 
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
+
+// Byte offset of the low-word table in k_hv_matfree_c's shared memory (after
+// nw weights and 2K pair offsets, 16-byte aligned).
+__host__ __device__ inline size_t matfree_c_table_offset(int nw, int K)
+{
+    return ((size_t)nw * 8 + (size_t)2 * K * 4 + 15) & ~(size_t)15;
+}
 
 // G lanes per row, each lane summing every G-th element of the row in one
 // FMA chain, with the loads of U of its elements issued ahead of their FMAs
@@ -131,6 +141,53 @@ __global__ void __launch_bounds__(256) k_hv_matfree(const uint64_t* __restrict__
     }
 }
 
+// The same product with the compact rank tables: the per-hop weights, the
+// pair offsets and the 2^L-entry low-word table in shared memory, the
+// high-word table read through L1 (neighbouring rows mostly share its entry).
+// Same loops and FMA order as k_hv_matfree, so the same y.
+__global__ void __launch_bounds__(1024) k_hv_matfree_c(const uint64_t* __restrict__ words, int64_t n,
+                                                     const double* __restrict__ diag, const double* __restrict__ w,
+                                                     int nw, const int* __restrict__ off, int K,
+                                                     const uint64_t* __restrict__ mhi, const uint32_t* __restrict__ mlo,
+                                                     int L, const double* __restrict__ x, double* __restrict__ y)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* sw = reinterpret_cast<double*>(smem);
+    int* soff = reinterpret_cast<int*>(sw + nw);
+    uint32_t* slo = reinterpret_cast<uint32_t*>(smem + matfree_c_table_offset(nw, K));
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = w[i];
+    for (int i = threadIdx.x; i < 2 * K; i += blockDim.x) soff[i] = off[i];
+    for (int i = threadIdx.x; i < (1 << L); i += blockDim.x) slo[i] = mlo[i];
+    __syncthreads();
+    const HopView hv{sw, nullptr, nullptr, soff, K};
+    const uint64_t lmask = (1ull << L) - 1ull;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t in = words[r];
+        double acc = diag[r] * __ldg(x + r);
+        for (uint64_t ta = in; ta; ta &= ta - 1) {
+            const int a = __ffsll((long long)ta) - 1;
+            for (uint64_t tb = ta & (ta - 1); tb; tb &= tb - 1) {
+                const int b = __ffsll((long long)tb) - 1;
+                const int s = a + b;
+                const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
+                for (uint64_t m = hop_targets(in, a, b, K, false); m; m &= m - 1) {
+                    const int c = __ffsll((long long)m) - 1, d = s - c;
+                    const uint64_t out = rest | (1ull << c) | (1ull << d);
+                    const uint64_t vb = hop_bits(hv, in, out, a, b, c, d);
+                    if (hop_zero(vb)) continue;
+                    const uint64_t eh = __ldg(mhi + (out >> L));
+                    const uint32_t el = slo[out & lmask];
+                    if ((eh >> 48) != (uint64_t)(el >> 16)) continue;   // cannot happen for a sector word
+                    const uint64_t j = (eh & 0xFFFFFFFFFFFFull) + (el & 0xFFFFu);
+                    if (j >= (uint64_t)n) continue;                      // never read out of range
+                    acc = fma(bits_to_double(vb), __ldg(x + j), acc);
+                }
+            }
+        }
+        y[r] = acc;
+    }
+}
+
 int sms()
 {
     int dev = 0, s = 148;
@@ -166,6 +223,25 @@ void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const 
     if (b.dim == 0) return;
     const int K = t.norb;
     const int nw = (int)t.hop.w.size();
+    if (b.mf_lo.p) {
+        const int L = b.mf_low_bits;
+        const size_t smem = matfree_c_table_offset(nw, K) + ((size_t)4 << L);
+        if (smem <= 200 * 1024) {
+            static thread_local std::map<size_t, int> occ;   // CTAs per SM per shared-memory size
+            auto it = occ.find(smem);
+            if (it == occ.end()) {
+                ED_CUDA(cudaFuncSetAttribute(k_hv_matfree_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                int ob = 0;
+                ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ob, k_hv_matfree_c, 1024, smem));
+                it = occ.emplace(smem, std::max(1, ob)).first;
+            }
+            k_hv_matfree_c<<<sms() * it->second, 1024, smem, st>>>(b.words.p, (int64_t)b.dim, diag, t.w_dev.p, nw,
+                                                                   t.hop_off_dev.p, K, b.mf_hi.p, b.mf_lo.p, L, x, y);
+            count_launch();
+            ED_CUDA(cudaGetLastError());
+            return;
+        }
+    }
     const size_t smem = hop_smem_bytes(K, nw);
     ED_CUDA(cudaFuncSetAttribute(k_hv_matfree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_hv_matfree<<<sms() * 4, 256, smem, st>>>(b.words.p, (int64_t)b.dim, diag, t.w_dev.p, nw, t.diag_a_dev.p,

@@ -25,7 +25,9 @@ def apply(torch, H, x):
     return yd.cpu().numpy()
 
 
-@pytest.mark.parametrize("case", [(4, 10, 0), (6, 16, 4), (8, 22, 0), (10, 28, 2)])
+# (3, 40, 1): more than 36 orbitals, the matrix-free product on the main rank
+# tables; the others use its compact shared-memory tables
+@pytest.mark.parametrize("case", [(4, 10, 0), (6, 16, 4), (8, 22, 0), (10, 28, 2), (3, 40, 1)])
 def test_products_match_oracle(cuda, oracle, case):
     N, norb, tlz = case
     pp = oracle.odd_coulomb_list(norb)
