@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(1024) k_hv_matfree_c(const uint64_t* __restric
     for (int i = threadIdx.x; i < 2 * K; i += blockDim.x) soff[i] = off[i];
     for (int i = threadIdx.x; i < (1 << L); i += blockDim.x) slo[i] = mlo[i];
     __syncthreads();
-    const HopView hv{sw, nullptr, nullptr, soff, K};
+    const uint64_t* wb = reinterpret_cast<const uint64_t*>(sw);
     const uint64_t lmask = (1ull << L) - 1ull;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t in = words[r];
@@ -170,10 +170,18 @@ __global__ void __launch_bounds__(1024) k_hv_matfree_c(const uint64_t* __restric
                 const int b = __ffsll((long long)tb) - 1;
                 const int s = a + b;
                 const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
+                // per pair: the parity's (a,b) part and the hop-table bases of
+                // the two directions (hop_parity, hop_index)
+                const int lo = pair_lo(s, K), cnt = pair_cnt(s, K);
+                const uint32_t par_ab = (uint32_t)(1 + __popcll(in & bits_between(a, b))) & 1u;
+                const int ifwd = soff[s] + (a - lo) * cnt - lo;   // out > in: + c        (>= soff[s], c >= lo)
+                const int irev = soff[s] + (a - lo) - lo * cnt;   // out < in: + c * cnt
                 for (uint64_t m = hop_targets(in, a, b, K, false); m; m &= m - 1) {
                     const int c = __ffsll((long long)m) - 1, d = s - c;
-                    const uint64_t out = rest | (1ull << c) | (1ull << d);
-                    const uint64_t vb = hop_bits(hv, in, out, a, b, c, d);
+                    const uint64_t bc = 1ull << c, bd = 1ull << d;
+                    const uint64_t out = rest | bc | bd;
+                    const uint32_t par = par_ab ^ ((uint32_t)__popcll(rest & (bd - 1ull) & ~(bc + bc - 1ull)) & 1u);
+                    const uint64_t vb = wb[c < a ? ifwd + c : irev + c * cnt] ^ ((uint64_t)par << 63);   // c < a: out > in
                     if (hop_zero(vb)) continue;
                     const uint64_t eh = __ldg(mhi + (out >> L));
                     const uint32_t el = slo[out & lmask];
