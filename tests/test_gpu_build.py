@@ -97,3 +97,33 @@ def test_register_and_shared_memory_sorts_agree(cuda, oracle, monkeypatch, case,
     a, b = H1.m_crsSparseMatrix.to_host(), H2.m_crsSparseMatrix.to_host()
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert np.array_equal(a[2].view(np.uint64), b[2].view(np.uint64))
+
+
+@pytest.mark.parametrize("case", [(1, 9, 0), (2, 5, 0), (5, 5, 0), (2, 6, 1)])
+def test_edge_sectors_build_and_products(cuda, oracle, case):
+    # one particle (no pairs), a full shell (no admissible hop), a tiny sector
+    # and an empty one: both storages bit-exact, and the stored and
+    # matrix-free products
+    N, norb, tlz = case
+    pp = oracle.odd_coulomb_list(norb)
+    b = oracle.basis(N, norb, tlz)
+    T = ed.QuarticTermTables(norb, pp)
+    orp, ocol, oval = oracle.build_upper(b, norb, T.m_kTable, T.m_vTable)
+    for upper in (True, False):
+        H, _ = build_gpu(N, norb, tlz, pp, upper)
+        rp, col, val = H.m_crsSparseMatrix.to_host()
+        ref = (orp, ocol, oval) if upper else oracle.upper_to_full(orp, ocol, oval, len(b))
+        assert np.array_equal(rp, ref[0]) and np.array_equal(col, ref[1])
+        assert np.array_equal(val.view(np.uint64), ref[2].view(np.uint64))
+    x = np.random.default_rng(3).uniform(-1, 1, len(b))
+    yref = oracle.spmv_sym_upper(orp, ocol, oval, x)
+    for kw in ({"store_upper": False}, {"store_upper": True}, {"matrix_free": True}):
+        H = ed.SpinlessFermionHamiltonian()
+        H.Initialize(N, norb, twoLz=tlz)
+        H.Add_CdCdCC_Terms(T, **kw)
+        xd = cuda.from_numpy(x).cuda()
+        yd = cuda.empty_like(xd)
+        ed.MatrixVectorFunction(H).Simple(xd, yd)
+        cuda.cuda.synchronize()
+        scale = max(1.0, float(np.abs(yref).max())) if len(yref) else 1.0
+        assert np.allclose(yd.cpu().numpy(), yref, rtol=0, atol=1e-13 * scale), kw
