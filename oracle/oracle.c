@@ -2,8 +2,8 @@
  * CPU oracle for the LLL spinless-fermion exact-diagonalization hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is a plain-C restatement of the
- * reference algorithm (SimonDavenport/hamiltonian_diagonalization) used as
- * the checker for the CUDA library and as the timed CPU baseline.  Nothing
+ * reference algorithm (SimonDavenport/hamiltonian_diagonalization) that the
+ * tests compare the CUDA library against, and the timed CPU baseline.  Nothing
  * in the shipped library links, loads or calls it.
  *
  * Every function names the reference file:line it restates.  The loops keep
