@@ -247,8 +247,7 @@ def run_gpu(args, ws, rank):
     launches0 = L.ed_kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     infos = []
-    with ClockSampler(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else f"/tmp/clocks_rank{rank}.csv") as clk:
+    with ClockSampler(os.path.join(args.clock_log_dir, f"clocks_rank{rank}.csv")) as clk:
         barrier()
         torch.cuda.synchronize()
         e0.record()
@@ -329,6 +328,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncv", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--clock-log-dir", default="/tmp",
+                    help="directory for the raw nvidia-smi clock samples of the timed region")
     args = ap.parse_args()
     ws, rank = dist_env()
     if ws > 1:

@@ -1,8 +1,8 @@
 """CPU oracle for the LLL spinless-fermion exact-diagonalization hot path.
 
 TEST INFRASTRUCTURE ONLY.  Only the tests, ``__graft_entry__.smoke()`` and the
-CPU legs of ``bench.py`` import this module, and only as the checker or as the
-timed CPU baseline.  The shipped library never calls into it.
+CPU legs of ``bench.py`` import this module, and only as the reference the
+tests compare against or as the timed CPU baseline.  The shipped library never calls into it.
 
 It restates the reference (SimonDavenport/hamiltonian_diagonalization):
 
