@@ -1,12 +1,12 @@
 """FP64 CPU restatement of the warm-start MLP (forward, loss, backward).
 
 TEST INFRASTRUCTURE ONLY: what the tests compare the device training and
-inference kernels (ed_mlp_* in the library) against.  It rounds to bfloat16
-at exactly the points where the device stores bfloat16 (input features,
-weights, hidden activations, the gradients fed to the next matrix products)
-and computes everything else in FP64, so device/oracle differences reduce to
-the device's FP32 accumulation.  The network has no reference counterpart (the reference
-starts ARPACK from a random or file vector).
+inference kernels (ed_mlp_* in the library) against. It rounds to bfloat16 at
+exactly the points where the device stores bfloat16 (input features, weights,
+hidden activations, the gradients fed to the next matrix products) and
+computes everything else in FP64, so device/oracle differences reduce to the
+device's FP32 accumulation. The network has no reference counterpart (the
+reference starts ARPACK from a random or file vector).
 """
 from __future__ import annotations
 
