@@ -10,6 +10,7 @@ from .host import (  # noqa: F401
     HamiltonianBatch,
     MatrixVectorFunction,
     MpiWrapper,
+    Observables,
     QuarticTermTables,
     SpherePseudopotentialModel,
     SpinlessFermionHamiltonian,

@@ -82,6 +82,10 @@ _SIGS = {
     "ed_ham_build_crs": (c_int, [c_void_p, c_void_p, c_int, c_void_p, P(c_void_p)]),
     "ed_crs_free": (c_int, [c_void_p]),
     "ed_crs_info": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
+    "ed_obs_density": (c_int, [c_void_p, P(c_double), P(c_double)]),
+    "ed_obs_density_density": (c_int, [c_void_p, P(c_double), P(c_double)]),
+    "ed_obs_participation_ratio": (c_int, [c_void_p, P(c_double), P(c_double)]),
+    "ed_obs_most_probable": (c_int, [c_void_p, P(c_double), c_i64, P(c_u64), P(c_double), P(c_i64)]),
     "ed_crs_arrays": (c_int, [c_void_p, P(c_void_p), P(c_void_p), P(c_void_p)]),
     "ed_crs_get": (c_int, [c_void_p, P(c_i64), P(ctypes.c_int32), P(c_double)]),
     "ed_ham_diagonal": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

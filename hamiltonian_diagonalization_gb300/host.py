@@ -331,6 +331,80 @@ class SpinlessFermionHamiltonian:
             self.m_eigenvectors = vec
 
 
+class Observables:
+    """Observables of an eigenvector of a real sector Hamiltonian
+    (observables/fermion_observables.hpp:39), computed on the device.  The
+    methods take the Hamiltonian and an eigenvector index, as the reference
+    does (its eigenvectors after LanczosDiagonalize), or a basis and a host
+    vector (``*_of_vector``)."""
+
+    @staticmethod
+    def _vector(hamiltonian, eigenvectorIndex):
+        vecs = hamiltonian.m_eigenvectors
+        if vecs is None:
+            raise EDError(C.ED_ERR_ARG, "eigenvectors not calculated")
+        if not 0 <= eigenvectorIndex < len(vecs):
+            raise EDError(C.ED_ERR_ARG, "eigenvectorIndex out of range")
+        return hamiltonian.m_fockBasis, np.ascontiguousarray(vecs[eigenvectorIndex], dtype=np.float64)
+
+    @staticmethod
+    def density_of_vector(basis, psi) -> np.ndarray:
+        """rho[k] = sum_s psi_s^2 n_k(s) (fermion_observables.hpp:48-104)."""
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        rho = np.empty(basis.nbrOrbitals)
+        check(lib().ed_obs_density(basis.handle(), _f64p(psi), _f64p(rho)))
+        return rho
+
+    @staticmethod
+    def density_density_of_vector(basis, psi) -> np.ndarray:
+        """D[k, q] = sum_s psi_s^2 n_k(s) n_q(s) (fermion_observables.hpp:117-200)."""
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        K = basis.nbrOrbitals
+        t = np.empty(K * K)
+        check(lib().ed_obs_density_density(basis.handle(), _f64p(psi), _f64p(t)))
+        return t.reshape(K, K)
+
+    @staticmethod
+    def participation_ratio_of_vector(basis, psi) -> float:
+        """1 / sum_s |psi_s|^4 (fermion_observables.hpp:528-562)."""
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        r = ctypes.c_double()
+        check(lib().ed_obs_participation_ratio(basis.handle(), _f64p(psi), ctypes.byref(r)))
+        return float(r.value)
+
+    @staticmethod
+    def most_probable_of_vector(basis, psi, nbrStates: int):
+        """The nbrStates largest |psi_s| with their Fock words, descending
+        (fermion_observables.hpp:437-517)."""
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        k = max(int(nbrStates), 0)
+        states = np.empty(max(k, 1), dtype=np.uint64)
+        amps = np.empty(max(k, 1))
+        cnt = ctypes.c_int64()
+        check(lib().ed_obs_most_probable(basis.handle(), _f64p(psi), k,
+                                         states.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _f64p(amps),
+                                         ctypes.byref(cnt)))
+        m = int(cnt.value)
+        return states[:m].copy(), amps[:m].copy()
+
+    # the reference's call shapes (the MpiWrapper argument is accepted and ignored)
+    def DensityFunction(self, hamiltonian, eigenvectorIndex: int, mpi=None) -> np.ndarray:
+        return self.density_of_vector(*self._vector(hamiltonian, eigenvectorIndex))
+
+    def DensityDensityFunction(self, hamiltonian, eigenvectorIndex: int, mpi=None) -> np.ndarray:
+        return self.density_density_of_vector(*self._vector(hamiltonian, eigenvectorIndex))
+
+    def GetParticipationRatio(self, hamiltonian, eigenvectorIndex: int, mpi=None) -> float:
+        return self.participation_ratio_of_vector(*self._vector(hamiltonian, eigenvectorIndex))
+
+    def GetMostProbable(self, hamiltonian, nbrStates: int, mpi=None):
+        """Per eigenvector e: (states[e], amplitudes[e]) of the nbrStates largest |psi|."""
+        vecs = hamiltonian.m_eigenvectors
+        if vecs is None:
+            raise EDError(C.ED_ERR_ARG, "eigenvectors not calculated")
+        return [self.most_probable_of_vector(hamiltonian.m_fockBasis, v, nbrStates) for v in vecs]
+
+
 class MatrixVectorFunction:
     """H*v callback bound into the eigensolver (matrix_vector_routines.hpp:41)."""
 

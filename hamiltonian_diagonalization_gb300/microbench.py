@@ -4,6 +4,7 @@
     python -m hamiltonian_diagonalization_gb300.microbench --sector 10,28,0 --batch 32 --reps 20
     python -m hamiltonian_diagonalization_gb300.microbench --rotate 1371535,41,25 --reps 20
     python -m hamiltonian_diagonalization_gb300.microbench --sector 11,31,0 --build --reps 3 [--upper]
+    python -m hamiltonian_diagonalization_gb300.microbench --sector 11,31,0 --observables --reps 5
 
 Builds the sector's Hamiltonian (LLL Coulomb pseudopotentials, odd m) on the
 device, then times `reps` products with CUDA events on the launching stream
@@ -17,7 +18,9 @@ With --rotate n,m,k it times the thick-restart rotation of an n x m basis
 into k Ritz vectors (ed_basis_rotate) in FP64 and on the tensor cores.
 With --build it times the whole CRS build (diagonal, count, scan, fill;
 host clock around a synchronised call, best of reps) with the register-sort
-fill and with the shared-memory fill (ED_FILL_SORT=smem).
+fill and with the shared-memory fill (ED_FILL_SORT=smem).  With
+--observables it times the eigenvector observables (density, density-density,
+participation ratio, 100 most probable states) end to end from a host vector.
 """
 from __future__ import annotations
 
@@ -40,6 +43,8 @@ def main():
     ap.add_argument("--rotate", default="", help="n,m,k: time the restart rotation instead")
     ap.add_argument("--build", action="store_true",
                     help="time the CRS build instead (register sort, then ED_FILL_SORT=smem)")
+    ap.add_argument("--observables", action="store_true",
+                    help="time the eigenvector observables on a seeded unit vector of the sector")
     args = ap.parse_args()
     import torch
 
@@ -53,6 +58,8 @@ def main():
         return batch_main(ed, C, torch, N, norb, tlz, args)
     if args.build:
         return build_main(ed, torch, N, norb, tlz, args)
+    if args.observables:
+        return observables_main(ed, N, norb, tlz, args)
     H = ed.SpinlessFermionHamiltonian()
     H.Initialize(N, norb, twoLz=tlz)
     T = ed.QuarticTermTables(norb, ed.odd_coulomb_list(norb))
@@ -105,6 +112,30 @@ def build_main(ed, torch, N, norb, tlz, args):
             del H
         res[f"ms_build_{name}"] = 1e3 * min(times)
     os.environ.pop("ED_FILL_SORT", None)
+    print(json.dumps(res))
+
+
+def observables_main(ed, N, norb, tlz, args):
+    import time
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(N, norb, tlz)
+    n = b.GetStoredDimension()
+    psi = np.random.default_rng(3).standard_normal(n)
+    psi /= np.linalg.norm(psi)
+    O = ed.Observables
+    calls = {"density": lambda: O.density_of_vector(b, psi),
+             "density_density": lambda: O.density_density_of_vector(b, psi),
+             "participation_ratio": lambda: O.participation_ratio_of_vector(b, psi),
+             "most_probable_100": lambda: O.most_probable_of_vector(b, psi, 100)}
+    res = {"sector": [N, norb, tlz], "n": n, "mode": "observables",
+           "note": "host vector in, host results out (the H2D copy of psi included)"}
+    for name, f in calls.items():
+        for _ in range(args.warmup):
+            f()
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            f()
+        res[f"ms_{name}"] = 1e3 * (time.perf_counter() - t0) / args.reps
     print(json.dumps(res))
 
 

@@ -340,6 +340,28 @@ ed_status ed_mlp_fit(ed_mlp* net, const ed_basis* b, const double* v1_host, int 
  * basis word r at v1_host[j] (unnormalised; the solvers normalise). */
 ed_status ed_warm_start(ed_mlp* net, const ed_basis* b, const double* v1_host, int nham, double* V0_dev);
 
+/* ------------------------------------------------------------- observables */
+
+/* Observables of a real eigenvector psi_host (n doubles on the host) of the
+ * basis's sector: the reference's Observables (observables/fermion_observables.hpp)
+ * for a real Hamiltonian, as device reductions over the basis.  Deterministic:
+ * repeated calls return the same bits.  Orbital k is bit k of a Fock word. */
+/* rho_host[k] = sum_s psi_s^2 n_k(s), k < norb.  Replaces
+ * Observables::DensityFunction (fermion_observables.hpp:48-104). */
+ed_status ed_obs_density(const ed_basis* b, const double* psi_host, double* rho_host);
+/* table_host[k*norb + q] = sum_s psi_s^2 n_k(s) n_q(s) (symmetric; the diagonal
+ * is rho).  Replaces Observables::DensityDensityFunction (fermion_observables.hpp:117-200). */
+ed_status ed_obs_density_density(const ed_basis* b, const double* psi_host, double* table_host);
+/* *ratio = 1 / sum_s |psi_s|^4.  Replaces Observables::GetParticipationRatio
+ * (fermion_observables.hpp:528-562). */
+ed_status ed_obs_participation_ratio(const ed_basis* b, const double* psi_host, double* ratio);
+/* The min(k, n) entries of largest |psi_s| in descending order (ties: row
+ * ascending) with their Fock words; *count_out = min(k, n).  Replaces
+ * Observables::GetMostProbable (fermion_observables.hpp:437-517) for one
+ * eigenvector (the reference loops over all of them). */
+ed_status ed_obs_most_probable(const ed_basis* b, const double* psi_host, int64_t k, uint64_t* states_host,
+                               double* amps_host, int64_t* count_out);
+
 /* ------------------------------------------------------- one-call driver */
 
 /* Whole sector solve from host inputs: basis -> tables -> CRS (or matrix-free

@@ -20,6 +20,8 @@
 // Link with -ledgb300 (hamiltonian_diagonalization_gb300/libedgb300.so).
 #pragma once
 
+#include <algorithm>
+#include <complex>
 #include <cstdint>
 #include <functional>
 #include <iostream>
@@ -379,6 +381,77 @@ class SpinlessFermionHamiltonian {
     utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
     ed_crs* m_crs = nullptr;
     QuarticTermTables* m_terms = nullptr;
+};
+
+// observables/fermion_observables.hpp:39, for the eigenvectors of a real
+// Hamiltonian built here (H provides m_fockBasis and a column-major n x nev
+// m_eigenvectors, as SpinlessFermionHamiltonian<double> does).  Out-of-range
+// indices and missing eigenvectors throw EdError.
+struct Observables {
+    template <class H>
+    static const double* Vector(const H& hamiltonian, iSize_t eigenvectorIndex)
+    {
+        const size_t n = (size_t)hamiltonian.m_fockBasis.GetStoredDimension();
+        if (n == 0 || hamiltonian.m_eigenvectors.size() < n * ((size_t)eigenvectorIndex + 1))
+            throw utilities::EdError(ED_ERR_ARG, "eigenvector not calculated or eigenvectorIndex out of range");
+        return hamiltonian.m_eigenvectors.data() + n * eigenvectorIndex;
+    }
+    // fermion_observables.hpp:48: probabilityList[k] = <c+_k c_k>, k < norb
+    template <class H>
+    void DensityFunction(const H& hamiltonian, iSize_t eigenvectorIndex, double* probabilityList,
+                         utilities::MpiWrapper& mpi)
+    {
+        utilities::EdCheck(ed_obs_density(hamiltonian.m_fockBasis.handle(), Vector(hamiltonian, eigenvectorIndex),
+                                          probabilityList),
+                           &mpi);
+    }
+    // fermion_observables.hpp:117: probabilityList[k*norb + q] = <c+_k c_k c+_q c_q>
+    template <class H>
+    void DensityDensityFunction(const H& hamiltonian, iSize_t eigenvectorIndex, double* probabilityList,
+                                utilities::MpiWrapper& mpi)
+    {
+        utilities::EdCheck(ed_obs_density_density(hamiltonian.m_fockBasis.handle(),
+                                                  Vector(hamiltonian, eigenvectorIndex), probabilityList),
+                           &mpi);
+    }
+    // fermion_observables.hpp:528: 1 / sum |psi|^4
+    template <class H>
+    double GetParticipationRatio(const H& hamiltonian, iSize_t eigenvectorIndex, utilities::MpiWrapper& mpi)
+    {
+        double r = 0.0;
+        utilities::EdCheck(ed_obs_participation_ratio(hamiltonian.m_fockBasis.handle(),
+                                                      Vector(hamiltonian, eigenvectorIndex), &r),
+                           &mpi);
+        return r;
+    }
+    // fermion_observables.hpp:437: for every eigenvector e, the nbrStates
+    // largest |psi| in descending order at states/amplitudes + e*nbrStates
+    // (fewer, min(nbrStates, n), when the sector is smaller)
+    template <class H>
+    void GetMostProbable(const H& hamiltonian, iSize_t nbrStates, fock_t* states, double* amplitudes,
+                         utilities::MpiWrapper& mpi)
+    {
+        const size_t n = (size_t)hamiltonian.m_fockBasis.GetStoredDimension();
+        const size_t nev = n ? hamiltonian.m_eigenvectors.size() / n : 0;
+        const size_t k = std::min<size_t>(nbrStates, n);
+        for (size_t e = 0; e < nev; ++e) {
+            int64_t cnt = 0;
+            utilities::EdCheck(ed_obs_most_probable(hamiltonian.m_fockBasis.handle(),
+                                                    hamiltonian.m_eigenvectors.data() + n * e, (int64_t)k,
+                                                    states + e * k, amplitudes + e * k, &cnt),
+                               &mpi);
+        }
+    }
+    template <class H>
+    void GetMostProbable(const H& hamiltonian, iSize_t nbrStates, fock_t* states, std::complex<double>* amplitudes,
+                         utilities::MpiWrapper& mpi)
+    {
+        const size_t n = (size_t)hamiltonian.m_fockBasis.GetStoredDimension();
+        const size_t nev = n ? hamiltonian.m_eigenvectors.size() / n : 0;
+        std::vector<double> re(std::min<size_t>(nbrStates, n) * nev);
+        GetMostProbable(hamiltonian, nbrStates, states, re.data(), mpi);
+        for (size_t i = 0; i < re.size(); ++i) amplitudes[i] = re[i];
+    }
 };
 
 }  // namespace diagonalization

@@ -389,6 +389,44 @@ def lowest_eigenpairs(rowptr, col, val, nev: int, tol: float = 1e-12, v0=None, u
     return w, v
 
 
+# ------------------------------------------------------------ observables
+
+def density(words: np.ndarray, psi: np.ndarray, norb: int) -> np.ndarray:
+    """rho[k] = sum_s |psi_s|^2 n_k(s): Observables::DensityFunction
+    (fermion_observables.hpp:48-104), the state loop binning each occupied
+    orbital (bit k of the word) with the state's probability."""
+    p = np.asarray(psi, dtype=np.float64) ** 2
+    w = np.asarray(words, dtype=np.uint64)
+    return np.array([p[((w >> np.uint64(k)) & np.uint64(1)) == 1].sum() for k in range(norb)])
+
+
+def density_density(words: np.ndarray, psi: np.ndarray, norb: int) -> np.ndarray:
+    """D[k, q] = sum_s |psi_s|^2 n_k(s) n_q(s): Observables::DensityDensityFunction
+    (fermion_observables.hpp:117-200) -- the k = q bin gets n_k^2 = n_k and
+    every ordered pair of distinct occupied orbitals its (k, q) bin."""
+    p = np.asarray(psi, dtype=np.float64) ** 2
+    w = np.asarray(words, dtype=np.uint64)
+    occ = np.stack([((w >> np.uint64(k)) & np.uint64(1)).astype(np.float64) for k in range(norb)], axis=1)
+    return (occ * p[:, None]).T @ occ
+
+
+def participation_ratio(psi: np.ndarray) -> float:
+    """1 / sum_s |psi_s|^4: Observables::GetParticipationRatio
+    (fermion_observables.hpp:528-562; the code returns 1/sum, its 1/D factor
+    is commented out)."""
+    return 1.0 / float(np.sum(np.abs(np.asarray(psi, dtype=np.float64)) ** 4))
+
+
+def most_probable(words: np.ndarray, psi: np.ndarray, k: int):
+    """The min(k, n) largest |psi_s| in descending order with their words:
+    Observables::GetMostProbable (fermion_observables.hpp:437-517) for one
+    eigenvector; ties (unordered in the reference's partial quicksort) by row."""
+    psi = np.asarray(psi, dtype=np.float64)
+    m = min(int(k), len(psi))
+    order = np.lexsort((np.arange(len(psi)), -np.abs(psi)))[:m]
+    return np.asarray(words, dtype=np.uint64)[order], psi[order]
+
+
 # ----------------------------------------------- pin against the reference
 
 def ref_lib():

@@ -1,8 +1,10 @@
 // Exercises the reference-shaped C++ host classes (include/ed_host.hpp) the
 // way the reference's model layer drives them for one sector:
 // tables -> basis -> Add_CdCdCC_Terms -> LanczosDiagonalize, plus the
-// std::function product path of ArpackWrapper.  Prints one JSON line.
+// std::function product path of ArpackWrapper, and the ground state's
+// observables.  Prints one JSON line.
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <vector>
 
@@ -51,12 +53,28 @@ int main(int argc, char** argv)
     for (diagonalization::fock_t i = 0; i < dim; i += 97)
         rank_ok = rank_ok && H.m_fockBasis.FindFockStateIndex(0, words[i]) == i;
 
+    // observables of the ground state (fermion_observables.hpp)
+    diagonalization::Observables obs;
+    std::vector<double> rho(norb), dd((size_t)norb * norb);
+    obs.DensityFunction(H, 0, rho.data(), mpi);
+    obs.DensityDensityFunction(H, 0, dd.data(), mpi);
+    const double pr = obs.GetParticipationRatio(H, 0, mpi);
+    std::vector<diagonalization::fock_t> top(3 * nev);
+    std::vector<std::complex<double>> amp(3 * nev);
+    obs.GetMostProbable(H, 3, top.data(), amp.data(), mpi);
+    double nsum = 0.0;
+    for (double r : rho) nsum += r;
+
     std::printf("{\"ok\": %s, \"ok_host_product\": %s, \"rank_ok\": %s, \"dim\": %llu, \"nnz\": %lld, \"eigenvalues\": [",
                 ok ? "true" : "false", ok2 ? "true" : "false", rank_ok ? "true" : "false",
                 (unsigned long long)dim, (long long)H.GetNbrNonZeros());
     for (int i = 0; i < nev; ++i) std::printf("%s%.17g", i ? ", " : "", H.m_eigenvalues[i]);
     std::printf("], \"eigenvalues_host_product\": [");
     for (int i = 0; i < nev; ++i) std::printf("%s%.17g", i ? ", " : "", ev2[i]);
-    std::printf("], \"residual\": %.3e}\n", H.m_arpackWrapper.LastInfo().max_residual);
+    std::printf("], \"density\": [");
+    for (int k = 0; k < norb; ++k) std::printf("%s%.17g", k ? ", " : "", rho[k]);
+    std::printf("], \"density_sum\": %.17g, \"dd00\": %.17g, \"participation\": %.17g, \"top_state\": %llu, "
+                "\"top_amp\": %.17g", nsum, dd[0], pr, (unsigned long long)top[0], amp[0].real());
+    std::printf(", \"residual\": %.3e}\n", H.m_arpackWrapper.LastInfo().max_residual);
     return (ok && ok2 && rank_ok) ? 0 : 1;
 }

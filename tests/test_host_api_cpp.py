@@ -39,3 +39,8 @@ def test_host_classes_solve_sector(cuda, oracle, tmp_path):
     assert r["dim"] == len(b) and r["nnz"] == len(fv)
     assert np.max(np.abs(np.array(r["eigenvalues"]) - ref) / np.abs(ref)) < 1e-10
     assert np.max(np.abs(np.array(r["eigenvalues_host_product"]) - ref) / np.abs(ref)) < 1e-10
+    # the ground state's observables through the C++ Observables class
+    rho = np.array(r["density"])
+    assert abs(r["density_sum"] - 6) < 1e-9 and np.allclose(rho, rho[::-1], atol=1e-8)   # N; Lz reflection
+    assert abs(r["dd00"] - rho[0]) < 1e-12 and 1.0 <= r["participation"] <= len(b)
+    assert int(r["top_state"]) in set(int(w) for w in b)
