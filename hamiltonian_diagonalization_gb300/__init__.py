@@ -13,7 +13,10 @@ from .host import (  # noqa: F401
     Observables,
     QuarticTermTables,
     SpherePseudopotentialModel,
+    SphereTwoLevelPseudopotentialModel,
     SpinlessFermionHamiltonian,
+    TwoLevelFermionFockBasis,
+    TwoLevelSpinlessFermionHamiltonian,
     WarmStartMLP,
     clebsch_gordan,
     coulomb_pseudopotentials,

@@ -39,7 +39,7 @@ class EDError(RuntimeError):
 
 class LanczosParams(ctypes.Structure):
     _fields_ = [("nev", c_int), ("ncv", c_int), ("max_restarts", c_int), ("tol", c_double), ("seed", c_u64),
-                ("want_vectors", c_int), ("verify", c_int)]
+                ("want_vectors", c_int), ("verify", c_int), ("degeneracy_passes", c_int)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -82,6 +82,10 @@ _SIGS = {
     "ed_ham_build_crs": (c_int, [c_void_p, c_void_p, c_int, c_void_p, P(c_void_p)]),
     "ed_crs_free": (c_int, [c_void_p]),
     "ed_crs_info": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
+    "ed_basis2_build": (c_int, [c_int, c_int, c_int, c_void_p, P(c_void_p)]),
+    "ed_ham2_build_crs": (c_int, [c_void_p, c_void_p, c_void_p, P(c_double), P(c_double), c_int, c_void_p,
+                                  P(c_void_p)]),
+    "ed_basis_levels": (c_int, [c_void_p, P(c_int), P(c_int), P(c_int)]),
     "ed_obs_density": (c_int, [c_void_p, P(c_double), P(c_double)]),
     "ed_obs_density_density": (c_int, [c_void_p, P(c_double), P(c_double)]),
     "ed_obs_participation_ratio": (c_int, [c_void_p, P(c_double), P(c_double)]),

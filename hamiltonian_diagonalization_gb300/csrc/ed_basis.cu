@@ -99,9 +99,10 @@ __global__ void k_max_i64(const int64_t* __restrict__ in, int64_t n, unsigned lo
 }
 
 // counts[h] = size of the low class sector words with high half h need.
+// wh[i] is the Lz weight of bit L + i.
 __global__ void k_basis_count(int H, int L, int N, int64_t S, int max_sum_low,
-                              const uint32_t* __restrict__ class_count, int64_t* __restrict__ counts,
-                              uint16_t* __restrict__ need_class)
+                              const uint32_t* __restrict__ class_count, const int* __restrict__ wh,
+                              int64_t* __restrict__ counts, uint16_t* __restrict__ need_class)
 {
     const int64_t nh = 1ll << H;
     for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
@@ -109,7 +110,7 @@ __global__ void k_basis_count(int H, int L, int N, int64_t S, int max_sum_low,
         int64_t sum_h = 0;
         uint64_t t = (uint64_t)h;
         while (t) {
-            sum_h += __ffsll((long long)t) - 1 + L;
+            sum_h += wh[__ffsll((long long)t) - 1];
             t &= t - 1;
         }
         const int pl = N - pop_h;
@@ -216,12 +217,23 @@ int64_t reduce_max_i64_host(const int64_t* in, int64_t n, cudaStream_t st)
     return (int64_t)h;
 }
 
+std::vector<int> basis_weights(const ed_basis& b)
+{
+    std::vector<int> w(b.norb);
+    for (int k = 0; k < b.norb; ++k) w[k] = (b.levels == 2 && k >= b.norb1) ? k - b.norb1 + 1 : k;
+    return w;
+}
+
 void basis_build(ed_basis& b, cudaStream_t st)
 {
     const int N = b.N, norb = b.norb;
-    ED_REQUIRE(norb >= 1 && norb <= kMaxOrbitals, ED_ERR_RANGE, "norb must be in 1..40 on the device path");
+    const int maxbits = b.levels == 2 ? kMaxTwoLevelBits : kMaxOrbitals;
+    ED_REQUIRE(norb >= 1 && norb <= maxbits, ED_ERR_RANGE,
+               b.levels == 2 ? "two-level words limited to 48 bits (norb0 <= 23)" : "norb must be in 1..40 on the device path");
     ED_REQUIRE(N >= 1 && N <= norb && N < 64, ED_ERR_ARG, "need 1 <= N <= norb");
-    const int64_t t = (int64_t)b.two_lz + (int64_t)N * (norb - 1);
+    // Lz = sum over occupied bits of (2 w - (norbLz - 1)), norbLz the weight span
+    const int norb_lz = b.levels == 2 ? b.norb1 : norb;
+    const int64_t t = (int64_t)b.two_lz + (int64_t)N * (norb_lz - 1);
     b.dim = 0;
     b.sector_sum = -1;
     const int L = norb / 2, H = norb - L;
@@ -229,13 +241,16 @@ void basis_build(ed_basis& b, cudaStream_t st)
     b.high_bits = H;
     if (t % 2 != 0) return;
     const int64_t S = t / 2;
-    const int64_t smin = (int64_t)N * (N - 1) / 2;
-    const int64_t smax = smin + (int64_t)N * (norb - N);
+    std::vector<int> w = basis_weights(b), ws = w;
+    std::sort(ws.begin(), ws.end());
+    int64_t smin = 0, smax = 0;
+    for (int i = 0; i < N; ++i) smin += ws[i], smax += ws[norb - 1 - i];
     if (S < smin || S > smax) return;
     b.sector_sum = S;
 
-    // low tables on the host (2^L <= 2^20 words)
-    const int max_sum_low = L * (L - 1) / 2;
+    // low tables on the host (2^L <= 2^24 words)
+    int max_sum_low = 0;
+    for (int k = 0; k < L; ++k) max_sum_low += w[k];
     const int nclass = (L + 1) * (max_sum_low + 1);
     ED_REQUIRE(nclass < 0xFFFF, ED_ERR_RANGE, "too many low-word classes");
     const uint64_t nl = 1ull << L;
@@ -244,7 +259,7 @@ void basis_build(ed_basis& b, cudaStream_t st)
     std::vector<uint32_t> rank_in_class(nl);
     for (uint64_t l = 0; l < nl; ++l) {
         int pop = __builtin_popcountll(l), sum = 0;
-        for (uint64_t x = l; x; x &= x - 1) sum += __builtin_ctzll(x);
+        for (uint64_t x = l; x; x &= x - 1) sum += w[__builtin_ctzll(x)];
         const int cls = pop * (max_sum_low + 1) + sum;
         rank_in_class[l] = ccount[cls]++;
         lo[l] = ((uint64_t)cls << 32) | rank_in_class[l];
@@ -264,7 +279,10 @@ void basis_build(ed_basis& b, cudaStream_t st)
     const int64_t nh = 1ll << H;
     DevBuf<int64_t> counts(nh), offs(nh + 1);
     DevBuf<uint16_t> need(nh);
-    k_basis_count<<<grid_for(nh, 256), 256, 0, st>>>(H, L, N, S, max_sum_low, d_ccount.p, counts.p, need.p); ::edgb::count_launch();
+    DevBuf<int> d_wh(H);
+    ED_CUDA(cudaMemcpyAsync(d_wh.p, w.data() + L, (size_t)H * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_basis_count<<<grid_for(nh, 256), 256, 0, st>>>(H, L, N, S, max_sum_low, d_ccount.p, d_wh.p, counts.p, need.p);
+    ::edgb::count_launch();
     ED_CUDA(cudaGetLastError());
     exclusive_scan_i64(counts.p, offs.p, nh, st);
     int64_t dim = 0;
@@ -280,7 +298,7 @@ void basis_build(ed_basis& b, cudaStream_t st)
 
 void basis_compact_tables(const ed_basis& b, cudaStream_t st)
 {
-    if (b.mf_lo.p || b.dim == 0) return;
+    if (b.mf_lo.p || b.dim == 0 || b.levels != 1) return;
     const int norb = b.norb, L = std::min(13, norb), H = norb - L;
     if (H > 23) return;   // high table over 64 MB: the matrix-free product keeps the main tables
     const int max_sum_low = L * (L - 1) / 2;
@@ -300,8 +318,12 @@ void basis_compact_tables(const ed_basis& b, cudaStream_t st)
     DevBuf<int64_t> counts(nh), offs(nh + 1);
     DevBuf<uint16_t> need(nh);
     DevBuf<uint64_t> hi(nh);
-    k_basis_count<<<grid_for(nh, 256), 256, 0, st>>>(H, L, b.N, b.sector_sum, max_sum_low, d_ccount.p, counts.p,
-                                                     need.p); ::edgb::count_launch();
+    std::vector<int> wh(H);
+    for (int i = 0; i < H; ++i) wh[i] = L + i;   // one level: weights are positions
+    DevBuf<int> d_wh(H);
+    ED_CUDA(cudaMemcpyAsync(d_wh.p, wh.data(), (size_t)H * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_basis_count<<<grid_for(nh, 256), 256, 0, st>>>(H, L, b.N, b.sector_sum, max_sum_low, d_ccount.p, d_wh.p,
+                                                     counts.p, need.p); ::edgb::count_launch();
     ED_CUDA(cudaGetLastError());
     exclusive_scan_i64(counts.p, offs.p, nh, st);
     k_basis_fill<<<grid_for(nh * 32, 256), 256, 0, st>>>(H, L, offs.p, counts.p, need.p, nullptr, nullptr, nullptr,

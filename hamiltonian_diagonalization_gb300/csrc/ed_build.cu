@@ -14,8 +14,10 @@
 // large for 32-bit keys, k_fill) and written coalesced; a count pass sizes
 // the rows first.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "ed_hop.cuh"
 
@@ -381,6 +383,241 @@ __global__ void __launch_bounds__(256) k_fill_reg(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Two Landau levels: TwoLevelSpinlessFermionHamiltonian
+// (two_level_spinless_fermion_hamiltonian.hpp:143-470) as
+// SphereTwoLevelPseudopotentialModel::BuildHamiltonian calls it
+// (two_level_pseudopotential_model.cpp:190-215).  A state is one word
+// (first << n1) | second.  Every term acts within one level's word with the
+// other as a spectator, so an off-diagonal element is a one-level pair hop on
+// that word with that level's hop table; no cross-level sign arises (each of
+// the four operators passes the other level's particles, an even total).  The
+// diagonal is one running sum in the reference's call order: level-0
+// energies, level-1 energies (occupied k ascending), then the level-0 and
+// level-1 quartic diagonal terms.
+
+// Shared-memory image of both levels' hop tables (level 0 first, 16-byte aligned).
+__device__ __forceinline__ void load_two_level(unsigned char* smem, const double* w0, int nw0, const double* da0,
+                                               const double* db0, const int* off0, int K0, const double* w1, int nw1,
+                                               const double* da1, const double* db1, const int* off1, int K1,
+                                               HopView& h0, HopView& h1)
+{
+    h0 = load_hop_smem(smem, w0, nw0, da0, db0, off0, K0);
+    const size_t t0 = (hop_smem_bytes(K0, nw0) + 15) & ~(size_t)15;
+    h1 = load_hop_smem(smem + t0, w1, nw1, da1, db1, off1, K1);
+}
+
+__host__ __device__ inline size_t two_level_table_bytes(int K0, int nw0, int K1, int nw1)
+{
+    return ((hop_smem_bytes(K0, nw0) + 15) & ~(size_t)15) + ((hop_smem_bytes(K1, nw1) + 15) & ~(size_t)15);
+}
+
+__global__ void k_diag2(const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ e0,
+                        const double* __restrict__ e1, const double* __restrict__ da0, const double* __restrict__ db0,
+                        int K0, const double* __restrict__ da1, const double* __restrict__ db1, int K1,
+                        double* __restrict__ diag)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* sda0 = reinterpret_cast<double*>(smem);
+    double* sdb0 = sda0 + K0 * K0;
+    double* sda1 = sdb0 + K0 * K0;
+    double* sdb1 = sda1 + K1 * K1;
+    double* se0 = sdb1 + K1 * K1;
+    double* se1 = se0 + K0;
+    for (int i = threadIdx.x; i < K0 * K0; i += blockDim.x) { sda0[i] = da0[i]; sdb0[i] = db0[i]; }
+    for (int i = threadIdx.x; i < K1 * K1; i += blockDim.x) { sda1[i] = da1[i]; sdb1[i] = db1[i]; }
+    for (int i = threadIdx.x; i < K0; i += blockDim.x) se0[i] = e0[i];
+    for (int i = threadIdx.x; i < K1; i += blockDim.x) se1[i] = e1[i];
+    __syncthreads();
+    const HopView h0{nullptr, sda0, sdb0, nullptr, K0}, h1{nullptr, sda1, sdb1, nullptr, K1};
+    const uint64_t m1 = (1ull << K1) - 1ull;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t w = words[r], first = w >> K1, second = w & m1;
+        double acc = 0.0;
+        for (uint64_t t = first; t; t &= t - 1) acc = acc + se0[__ffsll((long long)t) - 1];
+        for (uint64_t t = second; t; t &= t - 1) acc = acc + se1[__ffsll((long long)t) - 1];
+        acc = diag_element(h0, first, acc);
+        diag[r] = diag_element(h1, second, acc);
+    }
+}
+
+__global__ void k_count2(const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ diag,
+                         const double* __restrict__ w0, int nw0, const double* __restrict__ da0,
+                         const double* __restrict__ db0, const int* __restrict__ off0, int K0, int nozero0,
+                         const double* __restrict__ w1, int nw1, const double* __restrict__ da1,
+                         const double* __restrict__ db1, const int* __restrict__ off1, int K1, int nozero1, int upper,
+                         int64_t* __restrict__ rowlen, int* __restrict__ maxtasks)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    HopView h0, h1;
+    load_two_level(smem, w0, nw0, da0, db0, off0, K0, w1, nw1, da1, db1, off1, K1, h0, h1);
+    const uint64_t m1 = (1ull << K1) - 1ull;
+    unsigned tmax = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t w = words[r];
+        int64_t cnt = (fabs(diag[r]) < kSparseZeroTol) ? 0 : 1;
+        unsigned tasks = 1;
+        for (int lvl = 0; lvl < 2; ++lvl) {
+            const uint64_t in = lvl ? (w & m1) : (w >> K1);
+            const HopView& hv = lvl ? h1 : h0;
+            const int K = lvl ? K1 : K0;
+            const bool nz = (lvl ? nozero1 : nozero0) != 0;
+            for (uint64_t ta = in; ta; ta &= ta - 1) {
+                const int a = __ffsll((long long)ta) - 1;
+                for (uint64_t tb = ta & (ta - 1); tb; tb &= tb - 1) {
+                    const int b = __ffsll((long long)tb) - 1;
+                    const uint64_t m0 = hop_targets(in, a, b, K, upper != 0);
+                    const int pc = __popcll(m0);
+                    tasks += pc;
+                    if (nz) {
+                        cnt += pc;
+                        continue;
+                    }
+                    const int s = a + b;
+                    const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
+                    for (uint64_t m = m0; m; m &= m - 1) {
+                        const int c = __ffsll((long long)m) - 1, d = s - c;
+                        if (!hop_zero(hop_bits(hv, in, rest | (1ull << c) | (1ull << d), a, b, c, d))) ++cnt;
+                    }
+                }
+            }
+        }
+        rowlen[r] = cnt;
+        tmax = tasks > tmax ? tasks : tmax;
+    }
+    tmax = __reduce_max_sync(0xffffffffu, tmax);
+    if ((threadIdx.x & 31) == 0) atomicMax(maxtasks, (int)tmax);
+}
+
+// One warp per row of the two-level Hamiltonian: the admissible hops of every
+// same-level occupied pair as tasks (level << 18 | a | b << 6 | c << 12, level
+// positions), ranked as generated, register-sorted and stored as k_fill_reg does.
+template <int EM>
+__global__ void __launch_bounds__(256) k_fill2(
+    const uint64_t* __restrict__ words, int64_t n, const double* __restrict__ diag, const double* __restrict__ w0,
+    int nw0, const double* __restrict__ da0, const double* __restrict__ db0, const int* __restrict__ off0, int K0,
+    const double* __restrict__ w1, int nw1, const double* __restrict__ da1, const double* __restrict__ db1,
+    const int* __restrict__ off1, int K1, int N, int upper, const int64_t* __restrict__ rowptr,
+    const uint64_t* __restrict__ hi, const uint64_t* __restrict__ lo_tab, int L, int cap, int sb,
+    int32_t* __restrict__ col, double* __restrict__ val, int* __restrict__ err)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    HopView h0, h1;
+    load_two_level(smem, w0, nw0, da0, db0, off0, K0, w1, nw1, da1, db1, off1, K1, h0, h1);
+    const size_t tbytes = two_level_table_bytes(K0, nw0, K1, nw1);
+    const int warp_in_cta = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int npairs = N * (N - 1) / 2;
+    const int K = K0 + K1;
+    unsigned char* wbase = smem + tbytes + (size_t)warp_in_cta * fill_reg_warp_bytes(cap);
+    double* vals = reinterpret_cast<double*>(wbase);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(wbase + (size_t)cap * 8);
+    unsigned char* occ = wbase + (size_t)cap * 12;
+    const uint32_t smask = (uint32_t)cap - 1u;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint64_t m1 = (1ull << K1) - 1ull;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = gw; r < n; r += nwarps) {
+        const uint64_t in = words[r], first = in >> K1, second = in & m1;
+        const int64_t base = rowptr[r];
+        const int64_t want = rowptr[r + 1] - base;
+        for (int pos0 = 0; pos0 < K; pos0 += 32) {
+            const int pos = pos0 + lane;
+            const bool set = pos < K && ((in >> pos) & 1ull);
+            const unsigned m = __ballot_sync(0xffffffffu, set);
+            if (set) occ[__popc(m & lt) + __popcll(in & ((1ull << pos0) - 1ull))] = (unsigned char)pos;
+        }
+        __syncwarp();
+        int total = 0;
+        for (int p0 = 0; p0 < npairs; p0 += 32) {
+            const int p = p0 + lane;
+            uint64_t m = 0;
+            uint32_t tag = 0;
+            if (p < npairs) {
+                int j = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)p)) * 0.5f);
+                while (j * (j - 1) / 2 > p) --j;
+                while ((j + 1) * j / 2 <= p) ++j;
+                const int a = occ[p - j * (j - 1) / 2], b = occ[j];
+                if (b < K1) {                           // both in level 1 (the low word)
+                    m = hop_targets(second, a, b, K1, upper != 0);
+                    tag = (1u << 18) | (uint32_t)a | ((uint32_t)b << 6);
+                } else if (a >= K1) {                   // both in level 0
+                    m = hop_targets(first, a - K1, b - K1, K0, upper != 0);
+                    tag = (uint32_t)(a - K1) | ((uint32_t)(b - K1) << 6);
+                }
+            }
+            const int pc = __popcll(m);
+            int x = pc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            int pos = total + x - pc;
+            for (; m; m &= m - 1, ++pos)
+                if (pos < cap) keys[pos] = tag | ((uint32_t)(__ffsll((long long)m) - 1) << 12);
+            total += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
+        if (total >= cap) {
+            if (lane == 0) atomicOr(err, 4);
+            __syncwarp();
+            continue;
+        }
+        int cnt = 0;
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            const uint32_t task = t < total ? keys[t] : 0u;
+            __syncwarp();
+            uint32_t key = 0;
+            uint64_t vb = 0;
+            bool ok = false;
+            if (t < total) {
+                const int lvl1 = (task >> 18) & 1;
+                const int a = task & 63, b = (task >> 6) & 63, c = (task >> 12) & 63, d = a + b - c;
+                const uint64_t sub = lvl1 ? second : first;
+                const uint64_t out_sub = sub ^ (1ull << a) ^ (1ull << b) ^ (1ull << c) ^ (1ull << d);
+                vb = hop_bits(lvl1 ? h1 : h0, sub, out_sub, a, b, c, d);
+                if (!hop_zero(vb)) {
+                    const uint64_t out = lvl1 ? ((first << K1) | out_sub) : ((out_sub << K1) | second);
+                    const uint64_t rk = rank_in_sector(out, hi, lo_tab, L);
+                    if (rk == kMiss) atomicOr(err, 2);
+                    key = (uint32_t)rk << sb;
+                    ok = true;
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                const int slot = cnt + __popc(m & lt);
+                keys[slot] = key | (uint32_t)slot;
+                vals[slot] = bits_to_double(vb);
+            }
+            cnt += __popc(m);
+        }
+        const double dv = diag[r];
+        if (!(fabs(dv) < kSparseZeroTol)) {
+            if (lane == 0 && cnt < cap) {
+                keys[cnt] = ((uint32_t)r << sb) | (uint32_t)cnt;
+                vals[cnt] = dv;
+            }
+            ++cnt;
+        }
+        __syncwarp();
+        if (cnt != want || cnt > cap) {
+            if (lane == 0) atomicOr(err, 1);
+            __syncwarp();
+            continue;
+        }
+        if (cnt > 0) sort_row_dispatch<1, EM>(keys, cnt, lane);
+        for (int t = lane; t < cnt; t += 32) {
+            const uint32_t kk = keys[swz(t)];
+            col[base + t] = (int32_t)(kk >> sb);
+            val[base + t] = vals[kk & smask];
+        }
+        __syncwarp();
+    }
+}
+
 int sm_count()
 {
     int dev = 0, sms = 148;
@@ -393,6 +630,7 @@ int sm_count()
 
 void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream_t st)
 {
+    ED_REQUIRE(b.levels == 1, ED_ERR_ARG, "a two-level basis takes the two-level Hamiltonian build");
     if (b.dim == 0) return;
     const int K = t.norb;
     const size_t smem = (size_t)2 * K * K * 8;
@@ -402,6 +640,7 @@ void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream
 
 void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, cudaStream_t st)
 {
+    ED_REQUIRE(b.levels == 1, ED_ERR_ARG, "a two-level basis takes the two-level Hamiltonian build");
     ED_REQUIRE(t.norb == b.norb, ED_ERR_ARG, "terms and basis have different orbital counts");
     const int64_t n = (int64_t)b.dim;
     ED_REQUIRE(n < (int64_t)0x7fffffff, ED_ERR_RANGE, "sector dimension exceeds int32 column indices");
@@ -509,6 +748,107 @@ void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, c
     ED_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     ED_CUDA(cudaStreamSynchronize(st));
     ED_REQUIRE(herr == 0, ED_ERR_INTERNAL, "Hamiltonian fill: row count or rank check failed on the device");
+}
+
+namespace {
+bool all_hops_nonzero(const ed_terms& t)
+{
+    const int K = t.norb;
+    for (int s = 1; s <= 2 * K - 3; ++s) {
+        const int cnt = pair_cnt(s, K);
+        for (int ia = 0; ia < cnt; ++ia)
+            for (int ic = 0; ic < cnt; ++ic)
+                if (ic != ia && t.hop.w[t.hop.hop_off[s] + ia * cnt + ic] == 0.0) return false;
+    }
+    return true;
+}
+}  // namespace
+
+void ham2_build_crs(const ed_basis& b, const ed_terms& t0, const ed_terms& t1, const double* e0_host,
+                    const double* e1_host, int upper, ed_crs& a, cudaStream_t st)
+{
+    ED_REQUIRE(b.levels == 2, ED_ERR_ARG, "the two-level build takes a two-level basis");
+    ED_REQUIRE(t0.norb == b.norb0 && t1.norb == b.norb1, ED_ERR_ARG,
+               "term tables must have norb0 (level 0) and norb0 + 2 (level 1) orbitals");
+    const int64_t n = (int64_t)b.dim;
+    ED_REQUIRE(n < (int64_t)0x7fffffff, ED_ERR_RANGE, "sector dimension exceeds int32 column indices");
+    a.n = n;
+    a.upper = upper ? 1 : 0;
+    a.rowptr.alloc(n + 1);
+    if (n == 0) {
+        ED_CUDA(cudaMemsetAsync(a.rowptr.p, 0, sizeof(int64_t), st));
+        a.nnz = 0;
+        return;
+    }
+    const int K0 = t0.norb, K1 = t1.norb;
+    const int nw0 = (int)t0.hop.w.size(), nw1 = (int)t1.hop.w.size();
+    // occupation energies with the reference's per-term filter (|E| > 1e-14)
+    std::vector<double> e0(K0, 0.0), e1(K1, 0.0);
+    for (int k = 0; k < K0; ++k)
+        if (e0_host && std::fabs(e0_host[k]) > kSparseZeroTol) e0[k] = e0_host[k];
+    for (int k = 0; k < K1; ++k)
+        if (e1_host && std::fabs(e1_host[k]) > kSparseZeroTol) e1[k] = e1_host[k];
+    DevBuf<double> de0(K0), de1(K1);
+    ED_CUDA(cudaMemcpyAsync(de0.p, e0.data(), K0 * 8, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(de1.p, e1.data(), K1 * 8, cudaMemcpyHostToDevice, st));
+    DevBuf<double> diag(n);
+    const size_t dsm = ((size_t)2 * K0 * K0 + (size_t)2 * K1 * K1 + K0 + K1) * 8;
+    k_diag2<<<sm_count() * 8, 256, dsm, st>>>(b.words.p, n, de0.p, de1.p, t0.diag_a_dev.p, t0.diag_b_dev.p, K0,
+                                             t1.diag_a_dev.p, t1.diag_b_dev.p, K1, diag.p);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    const size_t tsm = two_level_table_bytes(K0, nw0, K1, nw1);
+    DevBuf<int64_t> rowlen(n);
+    DevBuf<int> maxtasks_dev(1);
+    ED_CUDA(cudaMemsetAsync(maxtasks_dev.p, 0, sizeof(int), st));
+    ED_CUDA(cudaFuncSetAttribute(k_count2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    k_count2<<<sm_count() * 4, 256, tsm, st>>>(b.words.p, n, diag.p, t0.w_dev.p, nw0, t0.diag_a_dev.p,
+                                               t0.diag_b_dev.p, t0.hop_off_dev.p, K0, all_hops_nonzero(t0) ? 1 : 0,
+                                               t1.w_dev.p, nw1, t1.diag_a_dev.p, t1.diag_b_dev.p, t1.hop_off_dev.p, K1,
+                                               all_hops_nonzero(t1) ? 1 : 0, a.upper, rowlen.p, maxtasks_dev.p);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    exclusive_scan_i64(rowlen.p, a.rowptr.p, n, st);
+    ED_CUDA(cudaMemcpyAsync(&a.nnz, a.rowptr.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    int maxtasks = 0;
+    ED_CUDA(cudaMemcpyAsync(&maxtasks, maxtasks_dev.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int64_t maxrow = reduce_max_i64_host(rowlen.p, n, st);
+    ED_CUDA(cudaStreamSynchronize(st));
+    a.max_row = (int)maxrow;
+    a.col.alloc((size_t)a.nnz + kCrsPad);
+    a.val.alloc((size_t)a.nnz + kCrsPad);
+    ED_CUDA(cudaMemsetAsync(a.col.p + a.nnz, 0, kCrsPad * sizeof(int32_t), st));
+    ED_CUDA(cudaMemsetAsync(a.val.p + a.nnz, 0, kCrsPad * sizeof(double), st));
+    int cap = 32, sb = 5;
+    while (cap < std::max<int64_t>(maxrow, maxtasks + 1)) { cap <<= 1; ++sb; }
+    const size_t tbytes = tsm;
+    const size_t warp_b = fill_reg_warp_bytes(cap);
+    const size_t budget = 200 * 1024;
+    ED_REQUIRE(cap <= 32 * kFillMaxE && ((((uint64_t)(n - 1)) << sb) | (uint64_t)(cap - 1)) < 0xFFFFFFFFull &&
+                   tbytes + warp_b <= budget,
+               ED_ERR_RANGE, "two-level sector too large for the register-sort fill");
+    DevBuf<int> err(1);
+    ED_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+    const int wpc = std::min<int>(8, (int)((budget - tbytes) / warp_b));
+    const size_t smem = tbytes + (size_t)wpc * warp_b;
+    auto launch = [&](auto kern) {
+        ED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int ob = 0;
+        ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ob, kern, wpc * 32, smem));
+        kern<<<sm_count() * std::max(1, ob), wpc * 32, smem, st>>>(
+            b.words.p, n, diag.p, t0.w_dev.p, nw0, t0.diag_a_dev.p, t0.diag_b_dev.p, t0.hop_off_dev.p, K0, t1.w_dev.p,
+            nw1, t1.diag_a_dev.p, t1.diag_b_dev.p, t1.hop_off_dev.p, K1, b.N, a.upper, a.rowptr.p, b.hi.p, b.lo.p,
+            b.low_bits, cap, sb, a.col.p, a.val.p, err.p);
+        ::edgb::count_launch();
+    };
+    if (cap <= 128) launch(k_fill2<4>);
+    else if (cap <= 512) launch(k_fill2<16>);
+    else launch(k_fill2<32>);
+    ED_CUDA(cudaGetLastError());
+    int herr = 0;
+    ED_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    ED_REQUIRE(herr == 0, ED_ERR_INTERNAL, "two-level fill: row count or rank check failed on the device");
 }
 
 }  // namespace edgb

@@ -147,6 +147,40 @@ ed_status ed_basis_build(int N, int norb, int two_lz, ed_stream stream, ed_basis
     });
 }
 
+ed_status ed_basis2_build(int N, int norb0, int two_lz, ed_stream stream, ed_basis** out)
+{
+    return guarded([&] {
+        ED_NONNULL(out);
+        ED_REQUIRE(norb0 >= 1 && 2 * norb0 + 2 <= kMaxTwoLevelBits, ED_ERR_RANGE,
+                   "two-level basis: need 1 <= norb0 and 2*norb0 + 2 <= 48 bits");
+        *out = nullptr;
+        ed_basis* b = new ed_basis();
+        b->N = N;
+        b->levels = 2;
+        b->norb0 = norb0;
+        b->norb1 = norb0 + 2;
+        b->norb = 2 * norb0 + 2;
+        b->two_lz = two_lz;
+        try {
+            basis_build(*b, (cudaStream_t)stream);
+        } catch (...) {
+            delete b;
+            throw;
+        }
+        *out = b;
+    });
+}
+
+ed_status ed_basis_levels(const ed_basis* b, int* levels, int* norb0, int* norb1)
+{
+    return guarded([&] {
+        ED_NONNULL(b);
+        if (levels) *levels = b->levels;
+        if (norb0) *norb0 = b->levels == 2 ? b->norb0 : b->norb;
+        if (norb1) *norb1 = b->levels == 2 ? b->norb1 : 0;
+    });
+}
+
 ed_status ed_basis_free(ed_basis* b)
 {
     return guarded([&] { delete b; });
@@ -250,6 +284,26 @@ ed_status ed_ham_build_crs(const ed_basis* b, const ed_terms* t, int store_upper
         ed_crs* a = new ed_crs();
         try {
             ham_build_crs(*b, *t, store_upper, *a, (cudaStream_t)stream);
+        } catch (...) {
+            delete a;
+            throw;
+        }
+        *out = a;
+    });
+}
+
+ed_status ed_ham2_build_crs(const ed_basis* b, const ed_terms* t0, const ed_terms* t1, const double* energies0,
+                            const double* energies1, int store_upper, ed_stream stream, ed_crs** out)
+{
+    return guarded([&] {
+        ED_NONNULL(b);
+        ED_NONNULL(t0);
+        ED_NONNULL(t1);
+        ED_NONNULL(out);
+        *out = nullptr;
+        ed_crs* a = new ed_crs();
+        try {
+            ham2_build_crs(*b, *t0, *t1, energies0, energies1, store_upper, *a, (cudaStream_t)stream);
         } catch (...) {
             delete a;
             throw;

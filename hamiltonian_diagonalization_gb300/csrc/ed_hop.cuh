@@ -94,10 +94,11 @@ __device__ __forceinline__ bool hop_zero(uint64_t bits) { return (bits << 1) == 
 __device__ __forceinline__ double bits_to_double(uint64_t bits) { return __longlong_as_double((long long)bits); }
 
 // Diagonal element in the reference's term order (k4 ascending over the
-// occupied bits, k3 ascending over the others, k2 in {k3,k4} ascending).
-__device__ __forceinline__ double diag_element(const HopView& hv, uint64_t in)
+// occupied bits, k3 ascending over the others, k2 in {k3,k4} ascending),
+// added term by term to acc (0 for a one-level Hamiltonian; the running sum of
+// the earlier term groups for the two-level one).
+__device__ __forceinline__ double diag_element(const HopView& hv, uint64_t in, double acc = 0.0)
 {
-    double acc = 0.0;
     for (uint64_t t4 = in; t4; t4 &= t4 - 1) {
         const int k4 = __ffsll((long long)t4) - 1;
         const uint64_t others = in & ~(1ull << k4);

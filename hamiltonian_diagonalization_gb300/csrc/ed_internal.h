@@ -18,6 +18,7 @@ namespace edgb {
 // into a low and a high half of at most 20 bits each, and the per-hop tables
 // must fit in shared memory.
 constexpr int kMaxOrbitals = 40;
+constexpr int kMaxTwoLevelBits = 48;          // two-level words: norb0 + norb1 bits
 constexpr uint64_t kMiss = ~0ull;             // FindFockStateIndex miss code
 constexpr double kSparseZeroTol = 1e-14;      // hamiltonian_data.hpp:53
 constexpr double kCgEps = 1e-12;              // clebsch_gordan_coefficients.hpp:53
@@ -151,7 +152,13 @@ ED_HD int pair_cnt(int s, int K) {
 // ------------------------------------------------------------ handle types
 
 struct ed_basis {
+    // norb bits per word.  One level: bit k is orbital k (Lz weight k).  Two
+    // levels (TwoLevelFermionFockBasis): the low norb1 = norb0 + 2 bits are
+    // the second level's orbitals (weight j), the high norb0 bits the lowest
+    // level's (weight i + 1), so ascending words follow the reference's
+    // (first, second) order and the sector is a fixed sum of weights.
     int N = 0, norb = 0, two_lz = 0;
+    int levels = 1, norb0 = 0, norb1 = 0;
     int64_t sector_sum = -1;     // sum of occupied positions in the sector (-1: empty)
     uint64_t dim = 0;
     int low_bits = 0, high_bits = 0;
@@ -189,8 +196,11 @@ struct ed_crs {
 // ----------------------------------------------------- device-side entry points
 namespace edgb {
 void basis_build(ed_basis& b, cudaStream_t st);
+std::vector<int> basis_weights(const ed_basis& b);
 void basis_rank(const ed_basis& b, const uint64_t* words, uint64_t* idx, uint64_t m, cudaStream_t st);
 void basis_compact_tables(const ed_basis& b, cudaStream_t st);
+void ham2_build_crs(const ed_basis& b, const ed_terms& t0, const ed_terms& t1, const double* e0_host,
+                    const double* e1_host, int upper, ed_crs& a, cudaStream_t st);
 void terms_upload(ed_terms& t);
 void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream_t st);
 void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, cudaStream_t st);

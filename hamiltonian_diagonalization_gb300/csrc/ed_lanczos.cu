@@ -338,9 +338,53 @@ __global__ void __launch_bounds__(kThreads) k_resid_part(const double* __restric
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// Deflated operator, part 1: c_i = shift * X_i . x for the nlock locked
+// columns; per-block partials, summed in block order by the last block.
+__global__ void __launch_bounds__(kThreads) k_lock_dots(const double* __restrict__ X, int nlock,
+                                                        const double* __restrict__ x, int64_t n, double shift,
+                                                        double* __restrict__ part, unsigned int* __restrict__ counter)
+{
+    __shared__ double red[kThreads / 32];
+    int64_t r0, r1;
+    chunk(n, gridDim.x, blockIdx.x, r0, r1);
+    for (int i = 0; i < nlock; ++i) {
+        const double* xi = X + (int64_t)i * n;
+        double s = 0.0;
+        for (int64_t r = r0 + threadIdx.x; r < r1; r += kThreads) s = fma(xi[r], x[r], s);
+        s = block_sum(s, red);
+        if (threadIdx.x == 0) part[(int64_t)i * gridDim.x + blockIdx.x] = s;
+        __syncthreads();
+    }
+    if (!last_block(counter)) return;
+    double* coef = part + (int64_t)nlock * gridDim.x;
+    for (int i = 0; i < nlock; ++i) {
+        const double s = sum_parts(part + (int64_t)i * gridDim.x, gridDim.x, red);
+        if (threadIdx.x == 0) coef[i] = shift * s;
+        __syncthreads();
+    }
+}
+
+// Deflated operator, part 2: y += sum_i c_i X_i.
+__global__ void __launch_bounds__(kThreads) k_lock_axpy(double* __restrict__ y, const double* __restrict__ X,
+                                                        int nlock, const double* __restrict__ coef, int64_t n)
+{
+    for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads) {
+        double acc = y[r];
+        for (int i = 0; i < nlock; ++i) acc = fma(coef[i], X[(int64_t)i * n + r], acc);
+        y[r] = acc;
+    }
+}
+
 }  // namespace
 
 // -------------------------------------------------------------- operator
+
+namespace {
+bool op_on_host(const ed_op& op)
+{
+    return op.kind == ed_op::HOST || (op.kind == ed_op::DEFLATED && op.inner && op.inner->kind == ed_op::HOST);
+}
+}  // namespace
 
 void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st)
 {
@@ -358,6 +402,18 @@ void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st)
         ED_CUDA(cudaStreamSynchronize(st));
         op.fn(hx.data(), hy.data(), op.user);
         ED_CUDA(cudaMemcpyAsync(y, hy.data(), (size_t)op.n * 8, cudaMemcpyHostToDevice, st));
+        break;
+    }
+    case ed_op::DEFLATED: {
+        op_apply(*op.inner, x, y, st);
+        double* part = const_cast<double*>(op.lock_part.p);
+        k_lock_dots<<<op.lock_blocks, kThreads, 0, st>>>(op.lock, op.nlock, x, op.n, op.shift, part,
+                                                         const_cast<unsigned int*>(op.lock_counter.p));
+        ::edgb::count_launch();
+        k_lock_axpy<<<op.lock_blocks, kThreads, 0, st>>>(y, op.lock, op.nlock,
+                                                         part + (int64_t)op.nlock * op.lock_blocks, op.n);
+        ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
         break;
     }
     }
@@ -485,8 +541,9 @@ void residual_norms(const ed_op& op, const double* x, const double* lambda, int 
     }
 }
 
-void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
-                   double* evecs_dev, ed_solve_info* info, cudaStream_t caller_stream)
+namespace {
+void lanczos_once(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
+                  double* evecs_dev, ed_solve_info* info, cudaStream_t caller_stream)
 {
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t n = op.n;
@@ -615,7 +672,7 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
             ED_CUDA(cudaGetLastError());
         }
     };
-    const bool graphs = op.kind != ed_op::HOST;
+    const bool graphs = !op_on_host(op);
     CycleGraphs cache;
     auto run_cycle = [&](int k) {
         if (!graphs) {
@@ -768,6 +825,101 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
     inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (info) *info = inf;
     ED_REQUIRE(converged, ED_ERR_NOCONV, "Lanczos did not converge within the restart cap");
+}
+
+void add_info(ed_solve_info& a, const ed_solve_info& b)
+{
+    a.restarts += b.restarts;
+    a.matvecs += b.matvecs;
+    a.spmv_seconds += b.spmv_seconds;
+    a.breakdowns += b.breakdowns;
+}
+}  // namespace
+
+// One Krylov sequence sees one vector of each eigenspace, so a degenerate
+// eigenvalue comes out once (only rounding could add copies).  With
+// p.degeneracy_passes > 0, each further pass solves for the nev lowest pairs
+// of H + shift * X X^T, X the pairs found so far and shift above their spread:
+// the found eigenvalues move up, the complement keeps its spectrum, and any
+// value below the nev-th found (a further copy) is merged in.  The passes end
+// when one adds nothing.
+void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
+                   double* evecs_dev, ed_solve_info* info, cudaStream_t caller_stream)
+{
+    const int64_t n = op.n;
+    const int nev = p.nev;
+    if (p.degeneracy_passes <= 0 || n < 60 || n <= (int64_t)nev + 2) {
+        lanczos_once(op, p, v0_dev, evals_host, evecs_dev, info, caller_stream);
+        return;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const double tol = p.tol > 0 ? p.tol : 1e-10;
+    ed_lanczos_params q = p;
+    q.verify = 0;
+    q.degeneracy_passes = 0;
+    DevBuf<double> X((size_t)n * nev), Y((size_t)n * nev), Xn((size_t)n * nev);
+    std::vector<double> theta(nev), mu(nev);
+    ed_solve_info total, part;
+    std::memset(&total, 0, sizeof(total));
+    std::memset(&part, 0, sizeof(part));
+    lanczos_once(op, q, v0_dev, theta.data(), X.p, &part, caller_stream);
+    add_info(total, part);
+    SolveStream ss(caller_stream);
+    cudaStream_t st = ss.s;
+    ed_op D;
+    D.kind = ed_op::DEFLATED;
+    D.n = n;
+    D.inner = &op;
+    D.nlock = nev;
+    D.lock_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
+    D.lock_part.alloc((size_t)nev * (D.lock_blocks + 1));
+    D.lock_counter.alloc(1);
+    ED_CUDA(cudaMemsetAsync(D.lock_counter.p, 0, sizeof(unsigned int), st));
+    for (int pass = 1; pass <= p.degeneracy_passes; ++pass) {
+        D.lock = X.p;
+        D.shift = (theta[nev - 1] - theta[0]) + std::max(1.0, std::fabs(theta[nev - 1]));
+        ed_lanczos_params r = q;
+        r.seed = p.seed + 0x2545F4914F6CDD1Dull * (uint64_t)pass;
+        ED_CUDA(cudaStreamSynchronize(st));
+        lanczos_once(D, r, nullptr, mu.data(), Y.p, &part, caller_stream);
+        add_info(total, part);
+        const double thr = theta[nev - 1] - tol * std::max(1.0, std::fabs(theta[nev - 1]));
+        std::vector<std::pair<double, int>> all;
+        for (int i = 0; i < nev; ++i) all.push_back({theta[i], i});
+        int added = 0;
+        for (int i = 0; i < nev; ++i)
+            if (mu[i] < thr) {
+                all.push_back({mu[i], nev + i});
+                ++added;
+            }
+        if (!added) break;
+        std::stable_sort(all.begin(), all.end(),
+                         [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a.first < b.first; });
+        for (int i = 0; i < nev; ++i) {
+            const int src = all[i].second;
+            const double* from = src < nev ? X.p + (int64_t)src * n : Y.p + (int64_t)(src - nev) * n;
+            ED_CUDA(cudaMemcpyAsync(Xn.p + (int64_t)i * n, from, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+            theta[i] = all[i].first;
+        }
+        std::swap(X.p, Xn.p);
+    }
+    for (int i = 0; i < nev; ++i) evals_host[i] = theta[i];
+    if (evecs_dev) ED_CUDA(cudaMemcpyAsync(evecs_dev, X.p, (size_t)n * nev * 8, cudaMemcpyDeviceToDevice, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    total.converged = nev;
+    total.max_residual = part.max_residual;
+    if (p.verify) {
+        std::vector<double> res(nev);
+        residual_norms(op, X.p, theta.data(), nev, res.data(), st);
+        total.matvecs += nev;
+        total.max_residual = *std::max_element(res.begin(), res.end());
+        int nc = 0;
+        for (double rr : res) nc += (rr <= tol) ? 1 : 0;
+        total.converged = nc;
+    }
+    ED_CUDA(cudaStreamSynchronize(st));
+    total.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (info) *info = total;
 }
 
 }  // namespace edgb

@@ -6,7 +6,7 @@
 #include "ed_internal.h"
 
 struct ed_op {
-    enum Kind { CRS = 0, MATFREE = 1, HOST = 2 };
+    enum Kind { CRS = 0, MATFREE = 1, HOST = 2, DEFLATED = 3 };
     Kind kind = CRS;
     int64_t n = 0;
     const ed_crs* crs = nullptr;
@@ -16,6 +16,15 @@ struct ed_op {
     ed_host_matvec fn = nullptr;
     void* user = nullptr;
     mutable std::vector<double> hx, hy; // host staging for HOST operators
+    // DEFLATED: inner + shift * X X^T for nlock orthonormal device columns X
+    // (Wielandt deflation of converged eigenvectors); scratch for the dots
+    const ed_op* inner = nullptr;
+    const double* lock = nullptr;
+    int nlock = 0;
+    double shift = 0.0;
+    int lock_blocks = 0;
+    edgb::DevBuf<double> lock_part;     // nlock * lock_blocks partials, then nlock coefficients
+    edgb::DevBuf<unsigned int> lock_counter;
 };
 
 namespace edgb {

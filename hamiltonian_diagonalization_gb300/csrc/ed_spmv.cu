@@ -228,6 +228,7 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
 
 void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const double* x, double* y, cudaStream_t st)
 {
+    ED_REQUIRE(b.levels == 1, ED_ERR_ARG, "the matrix-free product takes a one-level basis");
     if (b.dim == 0) return;
     const int K = t.norb;
     const int nw = (int)t.hop.w.size();
@@ -235,13 +236,18 @@ void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const 
         const int L = b.mf_low_bits;
         const size_t smem = matfree_c_table_offset(nw, K) + ((size_t)4 << L);
         if (smem <= 200 * 1024) {
-            static thread_local std::map<size_t, int> occ;   // CTAs per SM per shared-memory size
-            auto it = occ.find(smem);
+            // the limit is set on every call: a sector with a smaller table
+            // may have lowered it since the last launch of this size
+            ED_CUDA(cudaFuncSetAttribute(k_hv_matfree_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int dev = 0;
+            ED_CUDA(cudaGetDevice(&dev));
+            // CTAs per SM per (device, shared-memory size)
+            static thread_local std::map<std::pair<int, size_t>, int> occ;
+            auto it = occ.find({dev, smem});
             if (it == occ.end()) {
-                ED_CUDA(cudaFuncSetAttribute(k_hv_matfree_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 int ob = 0;
                 ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ob, k_hv_matfree_c, 1024, smem));
-                it = occ.emplace(smem, std::max(1, ob)).first;
+                it = occ.emplace(std::make_pair(dev, smem), std::max(1, ob)).first;
             }
             k_hv_matfree_c<<<sms() * it->second, 1024, smem, st>>>(b.words.p, (int64_t)b.dim, diag, t.w_dev.p, nw,
                                                                    t.hop_off_dev.p, K, b.mf_hi.p, b.mf_lo.p, L, x, y);

@@ -201,6 +201,45 @@ class FermionFockBasis:
         self.free()
 
 
+class TwoLevelFermionFockBasis(FermionFockBasis):
+    """Two-Landau-level basis (two_level_fermion_fock_basis.hpp:62): states
+    are (first, second) pairs of lowest- and second-level words, stored on the
+    device as one word (first << nbrOrbitals2) | second, whose ascending
+    order is the reference's sort (two_level_fermion_fock_basis.cpp:34-46)."""
+
+    def GenerateFockSpace(self, nbrParticles: int, nbrOrbitals1: int, nbrOrbitals2: int, twoLz: int, mpi=None,
+                          stream=None) -> bool:
+        """TwoLevelFermionFockBasis::GenerateFockSpace with
+        TestAngularMomentumSector2LL for the sector twoLz
+        (two_level_fermion_fock_basis.cpp:289-470); True when empty."""
+        if int(nbrOrbitals2) != int(nbrOrbitals1) + 2:
+            raise EDError(C.ED_ERR_ARG, "the second level has nbrOrbitals1 + 2 orbitals on the sphere")
+        self.free()
+        h = ctypes.c_void_p()
+        check(lib().ed_basis2_build(int(nbrParticles), int(nbrOrbitals1), int(twoLz), stream, ctypes.byref(h)))
+        self._h = h
+        self.m_basisStored = True
+        self.nbrParticles, self.twoLz = int(nbrParticles), int(twoLz)
+        self.nbrOrbitals1, self.nbrOrbitals2 = int(nbrOrbitals1), int(nbrOrbitals2)
+        self.nbrOrbitals = self.nbrOrbitals1 + self.nbrOrbitals2
+        return self.GetStoredDimension() == 0
+
+    def GetWords(self) -> np.ndarray:
+        """The combined words, ascending."""
+        return FermionFockBasis.GetFockBasis(self)
+
+    def GetFockBasis(self, dim: int | None = None, mpi=None):
+        """(first, second) arrays (two_level_fermion_fock_basis.cpp:477-506)."""
+        w = FermionFockBasis.GetFockBasis(self, dim)
+        return w >> np.uint64(self.nbrOrbitals2), w & np.uint64((1 << self.nbrOrbitals2) - 1)
+
+    def FindFockStateIndex(self, offset: int, first: int, second: int) -> int:
+        """Index of the state (first, second) (+offset), UINT64_MAX when absent
+        (two_level_fermion_fock_basis.cpp:211-241)."""
+        word = (int(first) << self.nbrOrbitals2) | int(second)
+        return FermionFockBasis.FindFockStateIndex(self, offset, word)
+
+
 class CrsSparseMatrix:
     """Device CRS handle (crs_sparse_matrix.hpp:123) with int64 row pointers."""
 
@@ -303,7 +342,8 @@ class SpinlessFermionHamiltonian:
         return op
 
     def LanczosDiagonalize(self, nbrEigenvalues: int, tol: float = 1e-10, v0=None, seed: int = 0, ncv: int = 0,
-                           want_vectors: bool = True, verify: bool = True, max_restarts: int = 0):
+                           want_vectors: bool = True, verify: bool = True, max_restarts: int = 0,
+                           degeneracy_passes: int = 0):
         """hamiltonian_base.hpp:770-931 with the device Lanczos; eigenvalues ascending."""
         mv = MatrixVectorFunction(self)
         arp = ArpackWrapper()
@@ -311,7 +351,8 @@ class SpinlessFermionHamiltonian:
         evals = np.empty(nbrEigenvalues)
         evecs = np.empty((nbrEigenvalues, n)) if want_vectors else None
         ok = arp.DiagonalizeSymmetricMatrix(mv, evecs, evals, n, n, nbrEigenvalues, tol=tol, v0=v0, seed=seed,
-                                            ncv=ncv, verify=verify, max_restarts=max_restarts)
+                                            ncv=ncv, verify=verify, max_restarts=max_restarts,
+                                            degeneracy_passes=degeneracy_passes)
         self.m_eigenvalues = evals
         self.m_eigenvectors = evecs
         self.last_info = arp.last_info
@@ -433,13 +474,15 @@ class ArpackWrapper:
 
     def DiagonalizeSymmetricMatrix(self, MatrixVectorMultiply, eigenvectors, eigenvalues, nodeDim: int, fullDim: int,
                                    nbrEigenvalues: int, mpi=None, tol: float = 1e-10, v0=None, seed: int = 0,
-                                   ncv: int = 0, verify: bool = True, max_restarts: int = 0) -> bool:
+                                   ncv: int = 0, verify: bool = True, max_restarts: int = 0,
+                                   degeneracy_passes: int = 0) -> bool:
         """Lowest `nbrEigenvalues` eigenpairs.  MatrixVectorMultiply is either
         a MatrixVectorFunction (device product) or a Python callable
         f(x_host, y_host) on numpy arrays (the reference's std::function form).
         eigenvalues: float64 array (filled ascending); eigenvectors: array of
-        shape (nbrEigenvalues, n) or None.  Returns False on failure, like the
-        reference, with the status in last_status."""
+        shape (nbrEigenvalues, n) or None.  degeneracy_passes > 0 adds deflated
+        solves that recover further copies of degenerate eigenvalues.  Returns
+        False on failure, like the reference, with the status in last_status."""
         if nodeDim != fullDim:
             raise EDError(C.ED_ERR_ARG, "one device holds the whole vector: nodeDim must equal fullDim")
         n = int(fullDim)
@@ -459,7 +502,8 @@ class ArpackWrapper:
             check(lib().ed_op_host_callback(n, cb, None, ctypes.byref(op)))
         try:
             p = LanczosParams(nev=int(nbrEigenvalues), ncv=int(ncv), max_restarts=int(max_restarts or 0), tol=float(tol),
-                              seed=int(seed), want_vectors=int(eigenvectors is not None), verify=int(bool(verify)))
+                              seed=int(seed), want_vectors=int(eigenvectors is not None), verify=int(bool(verify)),
+                              degeneracy_passes=int(degeneracy_passes))
             info = SolveInfo()
             ev = np.empty(nbrEigenvalues)
             vec = np.empty(n * nbrEigenvalues) if eigenvectors is not None else None
@@ -507,6 +551,141 @@ class SpherePseudopotentialModel:
 
     def BuildHamiltonian(self, matrix_free: bool = False, store_upper: bool = False):
         self.hamiltonian.Add_CdCdCC_Terms(self.tables, store_upper=store_upper, matrix_free=matrix_free)
+
+    def Diagonalize(self, **kw):
+        return self.hamiltonian.LanczosDiagonalize(self.nev, **kw)
+
+
+class TwoLevelSpinlessFermionHamiltonian(SpinlessFermionHamiltonian):
+    """two_level_spinless_fermion_hamiltonian.hpp:52 for T = double: spinless
+    fermions in the two lowest Landau levels, terms within one level only (as
+    the reference codes them).  Add_CdC_Terms / Add_CdCdCC_Terms record each
+    level's tables; the device build (ed_ham2_build_crs) runs once when the
+    matrix is first needed and sums each entry in the reference model's call
+    order: level-0 and level-1 occupation energies, then the level-0 and level-1
+    quartic terms (two_level_pseudopotential_model.cpp:203-212)."""
+
+    def __init__(self):
+        super().__init__()
+        self.m_fockBasis = TwoLevelFermionFockBasis()
+        self._quartic = [None, None]
+        self._energies = [None, None]
+        self._store_upper = False
+
+    def Initialize(self, nbrParticles: int, nbrOrbitals: int, storageMethod=SPARSE_CRS, mpi=None,
+                   twoLz: int | None = None):
+        """nbrOrbitals = total over both levels, 2*(2S+1) + 2 (two_level_pseudopotential_model.cpp:73)."""
+        if nbrParticles <= 0 or nbrOrbitals < 4 or nbrOrbitals % 2:
+            raise EDError(C.ED_ERR_ARG, "need nbrParticles > 0 and nbrOrbitals = 2 * norb0 + 2")
+        self.m_nbrParticles, self.m_nbrOrbitals = int(nbrParticles), int(nbrOrbitals)
+        self.m_storageMethod = storageMethod
+        self.norb0 = (int(nbrOrbitals) - 2) // 2
+        if twoLz is not None:
+            self.m_fockBasis.GenerateFockSpace(nbrParticles, self.norb0, self.norb0 + 2, twoLz)
+
+    @staticmethod
+    def _same_level(*levels) -> int:
+        if any(lv not in (0, 1) for lv in levels):
+            raise EDError(C.ED_ERR_ARG, "level specification incorrect (set to 0,1 only)")
+        if len(set(levels)) != 1:
+            raise EDError(C.ED_ERR_ARG, "only coded for terms in the same level so far")
+        return int(levels[0])
+
+    def Add_CdC_Terms(self, energies, level1: int, level2: int, minRow: int = 0, maxRow: int | None = None,
+                      mpi=None):
+        """Occupation energies of one level (two_level_spinless_fermion_hamiltonian.hpp:143-270):
+        an array of that level's orbital count, or an object with m_vTable."""
+        lvl = self._same_level(level1, level2)
+        e = np.ascontiguousarray(getattr(energies, "m_vTable", energies), dtype=np.float64)
+        need = self.norb0 + 2 * lvl
+        if e.shape != (need,):
+            raise EDError(C.ED_ERR_ARG, f"level {lvl} energies need {need} values")
+        self._energies[lvl] = e
+        self.m_crsSparseMatrix = None
+
+    def Add_CdCdCC_Terms(self, termTables: QuarticTermTables, level1: int = 0, level2: int = 0, level3: int = 0,
+                         level4: int = 0, minRow: int = 0, maxRow: int | None = None, mpi=None,
+                         store_upper: bool = False, matrix_free: bool = False):
+        """Quartic terms of one level (two_level_spinless_fermion_hamiltonian.hpp:306-470)."""
+        if matrix_free:
+            raise EDError(C.ED_ERR_ARG, "the two-level Hamiltonian is built into CRS")
+        lvl = self._same_level(level1, level2, level3, level4)
+        if termTables.m_kMax != self.norb0 + 2 * lvl:
+            raise EDError(C.ED_ERR_ARG, f"level {lvl} tables need {self.norb0 + 2 * lvl} orbitals")
+        self._quartic[lvl] = termTables
+        self._store_upper = bool(store_upper)
+        self.m_crsSparseMatrix = None
+
+    def Build(self):
+        q = [t if t is not None else QuarticTermTables(self.norb0 + 2 * lv, [0.0])
+             for lv, t in enumerate(self._quartic)]
+        e0, e1 = self._energies
+        h = ctypes.c_void_p()
+        check(lib().ed_ham2_build_crs(self.m_fockBasis.handle(), q[0].handle(), q[1].handle(),
+                                      None if e0 is None else _f64p(e0), None if e1 is None else _f64p(e1),
+                                      int(self._store_upper), None, ctypes.byref(h)))
+        self.m_crsSparseMatrix = CrsSparseMatrix(h)
+        self.m_matrixFree = False
+        self._keep = q
+
+    def operator_handle(self):
+        if self.m_crsSparseMatrix is None:
+            self.Build()
+        return super().operator_handle()
+
+    def LanczosDiagonalize(self, nbrEigenvalues: int, **kw):
+        """As the one-level solve, with degeneracy passes on by default: the
+        levels do not mix, so every pair of level-0 and level-1 multiplets
+        (L0, L1) gives 2 min(L0, L1) + 1 states of one energy in a sector."""
+        if self.m_crsSparseMatrix is None:
+            self.Build()
+        kw.setdefault("degeneracy_passes", int(nbrEigenvalues))
+        return super().LanczosDiagonalize(nbrEigenvalues, **kw)
+
+
+class SphereTwoLevelPseudopotentialModel:
+    """Two-Landau-level sector driver (two_level_pseudopotential_model.cpp:61-215):
+    BuildTermTables (LLL tables of norb0 = 2S+1 orbitals, second-level tables
+    of norb0 + 2 from its own pseudopotentials), SetOccupationEnergies,
+    BuildFockBasis, BuildHamiltonian, Diagonalize."""
+
+    def __init__(self, nbrParticles: int, norb0: int, pseudopotentials, pseudopotentials2LL,
+                 nbrEigenvalues: int = 1):
+        self.N, self.norb0 = int(nbrParticles), int(norb0)
+        self.pp0 = np.ascontiguousarray(pseudopotentials, dtype=np.float64)
+        self.pp1 = np.ascontiguousarray(pseudopotentials2LL, dtype=np.float64)
+        self.nev = int(nbrEigenvalues)
+        self.twoLz = 0
+        self.energies = None
+        self.hamiltonian = None
+
+    def SetSector(self, twoLz: int):
+        self.twoLz = int(twoLz)
+
+    def BuildTermTables(self):
+        self.tables = (QuarticTermTables(self.norb0, self.pp0), QuarticTermTables(self.norb0 + 2, self.pp1))
+
+    def SetOccupationEnergies(self, energyLevels):
+        """energyLevels: norb0 lowest-level values followed by norb0 + 2 second-level ones
+        (two_level_pseudopotential_model.cpp:92-108)."""
+        e = np.ascontiguousarray(energyLevels, dtype=np.float64)
+        if len(e) != 2 * self.norb0 + 2:
+            raise EDError(C.ED_ERR_ARG, "Must specify same number of energy levels as orbitals")
+        self.energies = (e[:self.norb0].copy(), e[self.norb0:].copy())
+
+    def BuildFockBasis(self) -> bool:
+        self.hamiltonian = TwoLevelSpinlessFermionHamiltonian()
+        self.hamiltonian.Initialize(self.N, 2 * self.norb0 + 2, SPARSE_CRS)
+        return self.hamiltonian.m_fockBasis.GenerateFockSpace(self.N, self.norb0, self.norb0 + 2, self.twoLz)
+
+    def BuildHamiltonian(self, store_upper: bool = False):
+        H = self.hamiltonian
+        if self.energies is not None:
+            H.Add_CdC_Terms(self.energies[0], 0, 0)
+            H.Add_CdC_Terms(self.energies[1], 1, 1)
+        H.Add_CdCdCC_Terms(self.tables[0], 0, 0, 0, 0, store_upper=store_upper)
+        H.Add_CdCdCC_Terms(self.tables[1], 1, 1, 1, 1, store_upper=store_upper)
+        H.Build()
 
     def Diagonalize(self, **kw):
         return self.hamiltonian.LanczosDiagonalize(self.nev, **kw)

@@ -21,6 +21,11 @@ host clock around a synchronised call, best of reps) with the register-sort
 fill and with the shared-memory fill (ED_FILL_SORT=smem).  With
 --observables it times the eigenvector observables (density, density-density,
 participation ratio, 100 most probable states) end to end from a host vector.
+With --two-level the sector is N,norb0,twoLz of the two-Landau-level model
+(norb0 lowest-level orbitals, norb0 + 2 in the second level, odd-m Coulomb
+pseudopotential lists of those sizes for the two levels' tables, second-level
+occupation energy 1.0): it times the basis, the CRS build, the product and
+the --nev lowest eigenpairs with and without the degeneracy passes.
 """
 from __future__ import annotations
 
@@ -45,6 +50,8 @@ def main():
                     help="time the CRS build instead (register sort, then ED_FILL_SORT=smem)")
     ap.add_argument("--observables", action="store_true",
                     help="time the eigenvector observables on a seeded unit vector of the sector")
+    ap.add_argument("--two-level", action="store_true", help="two-Landau-level sector N,norb0,twoLz")
+    ap.add_argument("--nev", type=int, default=4, help="two-level: eigenpairs to solve for")
     args = ap.parse_args()
     import torch
 
@@ -60,6 +67,8 @@ def main():
         return build_main(ed, torch, N, norb, tlz, args)
     if args.observables:
         return observables_main(ed, N, norb, tlz, args)
+    if args.two_level:
+        return two_level_main(ed, C, torch, N, norb, tlz, args)
     H = ed.SpinlessFermionHamiltonian()
     H.Initialize(N, norb, twoLz=tlz)
     T = ed.QuarticTermTables(norb, ed.odd_coulomb_list(norb))
@@ -112,6 +121,62 @@ def build_main(ed, torch, N, norb, tlz, args):
             del H
         res[f"ms_build_{name}"] = 1e3 * min(times)
     os.environ.pop("ED_FILL_SORT", None)
+    print(json.dumps(res))
+
+
+def two_level_main(ed, C, torch, N, norb0, tlz, args):
+    import time
+    res = {"sector": [N, norb0, tlz], "mode": "two-level", "layout": "upper" if args.upper else "full"}
+    t0 = ed.QuarticTermTables(norb0, ed.odd_coulomb_list(norb0))
+    t1 = ed.QuarticTermTables(norb0 + 2, ed.odd_coulomb_list(norb0 + 2))
+    e1 = np.ones(norb0 + 2)
+
+    def make():
+        H = ed.TwoLevelSpinlessFermionHamiltonian()
+        H.Initialize(N, 2 * norb0 + 2)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        H.m_fockBasis.GenerateFockSpace(N, norb0, norb0 + 2, tlz)
+        torch.cuda.synchronize()
+        b = time.perf_counter()
+        H.Add_CdC_Terms(e1, 1, 1)
+        H.Add_CdCdCC_Terms(t0, 0, 0, 0, 0, store_upper=args.upper)
+        H.Add_CdCdCC_Terms(t1, 1, 1, 1, 1, store_upper=args.upper)
+        H.Build()
+        torch.cuda.synchronize()
+        return H, b - a, time.perf_counter() - b
+
+    tb, tc = [], []
+    for i in range(args.warmup + args.reps):
+        H, x, y = make()
+        if i >= args.warmup:
+            tb.append(x)
+            tc.append(y)
+    n, nnz = H.GetDimension(), H.m_crsSparseMatrix.GetNbrNonZeros()
+    res.update({"n": n, "nnz": nnz, "ms_basis": 1e3 * min(tb), "ms_build": 1e3 * min(tc)})
+    mv = ed.MatrixVectorFunction(H)
+    x = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, n)).cuda()
+    y = torch.empty_like(x)
+    for _ in range(3):
+        mv.Simple(x, y)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(20):
+        mv.Simple(x, y)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / 20
+    by = nnz * 12 + (n + 1) * 8 + 2 * n * 8
+    res.update({"ms_per_product": ms, "GBps": by / ms / 1e6})
+    for passes in (0, args.nev):
+        H.LanczosDiagonalize(args.nev, tol=1e-10, seed=1, degeneracy_passes=passes, want_vectors=False)
+        t = time.perf_counter()
+        ok = H.LanczosDiagonalize(args.nev, tol=1e-10, seed=1, degeneracy_passes=passes, want_vectors=False)
+        res[f"solve_passes{passes}"] = {"ok": bool(ok), "s": time.perf_counter() - t,
+                                        "eigenvalues": [float(v) for v in H.m_eigenvalues],
+                                        "matvecs": H.last_info["matvecs"],
+                                        "max_residual": H.last_info["max_residual"]}
     print(json.dumps(res))
 
 

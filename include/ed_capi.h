@@ -96,6 +96,16 @@ double ed_clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM);
  * Replaces FermionFockBasis::GenerateFockSpace (fermion_fock_basis.cpp:241-354)
  * with the TestAngularMomentumSector constraint. */
 ed_status ed_basis_build(int N, int norb, int two_lz, ed_stream stream, ed_basis** out);
+/* Two-Landau-level sector basis: N particles in norb0 = 2S+1 lowest-level
+ * orbitals and norb0 + 2 second-level orbitals with total 2Lz = two_lz,
+ * ordered as TwoLevelFermionFockBasis::GenerateFockSpace sorts it
+ * (two_level_fermion_fock_basis.cpp:289-470; TestAngularMomentumSector2LL,
+ * two_level_angular_momentum_constraint.hpp:41-70).  Each state is one word,
+ * (first << (norb0 + 2)) | second, so ascending words are the reference's
+ * (first, second) order; words of up to 48 bits (norb0 <= 23). */
+ed_status ed_basis2_build(int N, int norb0, int two_lz, ed_stream stream, ed_basis** out);
+/* levels (1 or 2) and the orbital counts of each level (norb1 = 0 for one level). */
+ed_status ed_basis_levels(const ed_basis* b, int* levels, int* norb0, int* norb1);
 ed_status ed_basis_free(ed_basis* b);
 ed_status ed_basis_dim(const ed_basis* b, uint64_t* dim);
 /* Device pointer to the n basis words (valid while the handle lives). */
@@ -130,6 +140,17 @@ ed_status ed_terms_free(ed_terms* t);
  * mapped_sparse_matrix.hpp:423-460, crs_sparse_matrix.hpp:193-254). */
 ed_status ed_ham_build_crs(const ed_basis* b, const ed_terms* t, int store_upper,
                            ed_stream stream, ed_crs** out);
+/* Two-Landau-level Hamiltonian into CRS for a basis from ed_basis2_build:
+ * level-0 quartic terms t0 (norb0 orbitals) and level-1 terms t1 (norb0 + 2
+ * orbitals, from the second level's pseudopotentials), plus optional
+ * occupation energies energies0[norb0] / energies1[norb0 + 2] (host, NULL for
+ * none).  Replaces SphereTwoLevelPseudopotentialModel::BuildHamiltonian
+ * (two_level_pseudopotential_model.cpp:190-215) over
+ * TwoLevelSpinlessFermionHamiltonian::Add_CdC_Terms / Add_CdCdCC_Terms
+ * (two_level_spinless_fermion_hamiltonian.hpp:143-470): same elements, signs,
+ * call-order summation of the diagonal and 1e-14 trims; columns ascending. */
+ed_status ed_ham2_build_crs(const ed_basis* b, const ed_terms* t0, const ed_terms* t1, const double* energies0,
+                            const double* energies1, int store_upper, ed_stream stream, ed_crs** out);
 ed_status ed_crs_free(ed_crs* a);
 ed_status ed_crs_info(const ed_crs* a, int64_t* n, int64_t* nnz, int* upper);
 ed_status ed_crs_arrays(const ed_crs* a, const int64_t** rowptr_dev, const int32_t** col_dev,
@@ -175,6 +196,12 @@ typedef struct {
     int want_vectors;   /* caller's note only: eigenvectors are written whenever the
                            eigenvector pointer of the call is non-NULL              */
     int verify;         /* 1 -> recompute true residuals with extra products            */
+    int degeneracy_passes;  /* 0 -> one Krylov sequence.  k > 0 -> up to k further solves
+                           of H + s X X^T (X the pairs found, s above their spread),
+                           each merging eigenvalues below the nev-th found: the extra
+                           copies of degenerate eigenvalues one start vector cannot
+                           see.  Ends early when a pass adds nothing.  The batched
+                           solver ignores it.                                         */
 } ed_lanczos_params;
 
 typedef struct {

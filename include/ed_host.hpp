@@ -207,6 +207,8 @@ class ArpackWrapper {
     void SetTolerance(double tol) { m_tol = tol; }
     void SetNcv(int ncv) { m_ncv = ncv; }
     void SetSeed(uint64_t seed) { m_seed = seed; }
+    // further deflated solves that recover copies of degenerate eigenvalues
+    void SetDegeneracyPasses(int passes) { m_degeneracyPasses = passes; }
     // start vector (host, nodeDim doubles) in place of --use-initial's file
     void SetInitialVector(const std::vector<double>& v) { m_initial = v; }
     const ed_solve_info& LastInfo() const { return m_info; }
@@ -258,6 +260,7 @@ class ArpackWrapper {
         p.seed = m_seed;
         p.want_vectors = eigenvectors != nullptr;
         p.verify = 1;
+        p.degeneracy_passes = m_degeneracyPasses;
         const double* v0 = ((int)m_initial.size() == n) ? m_initial.data() : nullptr;
         ed_status s = ed_lanczos(op, &p, v0, eigenvalues, eigenvectors, &m_info);
         m_status = s;
@@ -265,6 +268,7 @@ class ArpackWrapper {
         return true;
     }
     int m_maxIterations = 2000;
+    int m_degeneracyPasses = 0;
     int m_ncv = 0;
     double m_tol = 1e-10;
     uint64_t m_seed = 0;

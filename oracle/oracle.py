@@ -389,6 +389,114 @@ def lowest_eigenpairs(rowptr, col, val, nev: int, tol: float = 1e-12, v0=None, u
     return w, v
 
 
+# ------------------------------------------------------------ two Landau levels
+
+def basis2(N: int, norb0: int, two_lz: int):
+    """TwoLevelFermionFockBasis::GenerateFockSpace (two_level_fermion_fock_basis.cpp:289-470)
+    with TestAngularMomentumSector2LL (two_level_angular_momentum_constraint.hpp:41-70):
+    for n0 = 0..N every lowest-level word of n0 bits and every second-level word
+    of N - n0 bits (norb0 + 2 orbitals) whose Lz sum, 2i - (max-2) per
+    lowest-level bit and 2j - max per second-level bit with max = norb0 + 1,
+    equals two_lz; sorted by (first, second).  Returns (first, second)."""
+    from itertools import combinations
+    norb1 = norb0 + 2
+    mx = norb1 - 1
+    firsts, seconds = [], []
+    for n0 in range(N + 1):
+        n1 = N - n0
+        if n0 > norb0 or n1 > norb1:
+            continue
+        w0 = [sum(1 << i for i in c) for c in combinations(range(norb0), n0)]
+        l0 = [sum(2 * i - (mx - 2) for i in c) for c in combinations(range(norb0), n0)]
+        by_lz = {}
+        for c in combinations(range(norb1), n1):
+            by_lz.setdefault(sum(2 * j - mx for j in c), []).append(sum(1 << j for j in c))
+        for a, lz in zip(w0, l0):
+            for b in by_lz.get(two_lz - lz, ()):
+                firsts.append(a)
+                seconds.append(b)
+    order = sorted(range(len(firsts)), key=lambda i: (firsts[i], seconds[i]))
+    return (np.array([firsts[i] for i in order], dtype=np.uint64),
+            np.array([seconds[i] for i in order], dtype=np.uint64))
+
+
+def build_upper2(first: np.ndarray, second: np.ndarray, norb0: int, kt0, vt0, kt1, vt1, e0=None, e1=None):
+    """Upper-triangle CRS of the two-level Hamiltonian in the reference's call,
+    loop and summation order: SphereTwoLevelPseudopotentialModel::BuildHamiltonian
+    (two_level_pseudopotential_model.cpp:190-215) adds the quadratic
+    occupation energies of level 0 then level 1 (Add_CdC_Terms,
+    two_level_spinless_fermion_hamiltonian.hpp:143-270: diagonal E_k for every
+    occupied k, ascending), then the quartic terms of level 0 then level 1
+    (Add_CdCdCC_Terms, :306-470: the single-level loop on the level's word with
+    the other word fixed).  Every term is kept when |term| > 1e-14 and added to
+    its (row, column) entry in that order; entries below 1e-14 are trimmed
+    (mapped_sparse_matrix.hpp:423-460) and columns sorted.  Python loops:
+    small sectors only."""
+    norb1 = norb0 + 2
+    tol = 1e-14
+    n = len(first)
+    f_ = [int(x) for x in first]
+    s_ = [int(x) for x in second]
+    index = {(a, b): i for i, (a, b) in enumerate(zip(f_, s_))}
+    rows = [dict() for _ in range(n)]
+
+    def bits(w):
+        while w:
+            lo = w & -w
+            yield lo.bit_length() - 1, lo
+            w ^= lo
+
+    for lvl, E in ((0, e0), (1, e1)):
+        if E is None:
+            continue
+        for i in range(n):
+            for k, _ in bits(f_[i] if lvl == 0 else s_[i]):
+                v = float(E[k])
+                if abs(v) > tol:
+                    rows[i][i] = rows[i].get(i, 0.0) + v
+    for lvl, kt, vt, K in ((0, kt0, vt0, norb0), (1, kt1, vt1, norb1)):
+        mask = (1 << K) - 1
+        for i in range(n):
+            inw = f_[i] if lvl == 0 else s_[i]
+            t4 = inw
+            while t4:
+                k4o = t4 & -t4
+                k4 = k4o.bit_length() - 1
+                t3 = inw ^ k4o
+                while t3:
+                    k3o = t3 & -t3
+                    k3 = k3o.bit_length() - 1
+                    if k3 != k4:
+                        t2 = mask ^ (t3 ^ k3o)
+                        while t2:
+                            k2o = t2 & -t2
+                            k2 = k2o.bit_length() - 1
+                            idx = (k4 * K + k3) * K + k2
+                            k1 = int(kt[idx])
+                            if k1 < K:
+                                k1o = 1 << k1
+                                if ((not (k1o & inw) or (k1o & k3o) or (k1o & k4o)) and
+                                        (not (k2o & inw) or (k2o & k3o) or (k2o & k4o)) and not (k1o & k2o)):
+                                    out, sign = evaluate_cdcdcc(k1, k2, k3, k4, inw, K)
+                                    if sign != 0 and out >= inw:
+                                        j = index.get((out, s_[i]) if lvl == 0 else (f_[i], out))
+                                        if j is not None:
+                                            v = float(sign) * float(vt[idx])
+                                            if abs(v) > tol:
+                                                rows[i][j] = rows[i].get(j, 0.0) + v
+                            t2 ^= k2o
+                    t3 ^= k3o
+                t4 ^= k4o
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    cols, vals = [], []
+    for i in range(n):
+        kept = sorted((j, v) for j, v in rows[i].items() if not abs(v) < tol)
+        cols.extend(j for j, _ in kept)
+        vals.extend(v for _, v in kept)
+        rowptr[i + 1] = len(cols)
+    return rowptr, np.array(cols, dtype=np.int32), np.array(vals, dtype=np.float64)
+
+
 # ------------------------------------------------------------ observables
 
 def density(words: np.ndarray, psi: np.ndarray, norb: int) -> np.ndarray:

@@ -1,0 +1,143 @@
+"""Two-Landau-level path on the device against the oracle's restatement of
+TwoLevelFermionFockBasis and of the two-level Add_CdC / Add_CdCdCC terms:
+basis words and ranks exact, CRS bit-exact (upper and full storage, with and
+without occupation energies), lowest eigenvalues within 1e-10 relative."""
+import numpy as np
+import pytest
+
+import hamiltonian_diagonalization_gb300 as ed
+from hamiltonian_diagonalization_gb300 import _capi
+
+pytestmark = pytest.mark.gpu
+
+# (N, norb0, 2Lz): integer and half-integer flux, |Lz| > 0, one level empty
+# of a sector's states, the largest norb0 the 48-bit words allow
+CASES = [(2, 3, 0), (3, 5, 0), (3, 5, 2), (4, 6, 0), (4, 6, -2), (5, 6, 1), (5, 7, 0), (6, 7, 4), (6, 9, 0),
+         (4, 23, 0), (2, 23, -20)]
+
+
+def tables(oracle, norb0, seed):
+    rng = np.random.default_rng(seed)
+    t0 = ed.QuarticTermTables(norb0, oracle.odd_coulomb_list(norb0))
+    t1 = ed.QuarticTermTables(norb0 + 2, rng.uniform(-1.0, 2.0, norb0 + 1))
+    return t0, t1
+
+
+def build(N, norb0, tlz, t0, t1, e0=None, e1=None, upper=True):
+    H = ed.TwoLevelSpinlessFermionHamiltonian()
+    H.Initialize(N, 2 * norb0 + 2, twoLz=tlz)
+    if e0 is not None:
+        H.Add_CdC_Terms(e0, 0, 0)
+    if e1 is not None:
+        H.Add_CdC_Terms(e1, 1, 1)
+    H.Add_CdCdCC_Terms(t0, 0, 0, 0, 0, store_upper=upper)
+    H.Add_CdCdCC_Terms(t1, 1, 1, 1, 1, store_upper=upper)
+    H.Build()
+    return H
+
+
+@pytest.mark.parametrize("case", CASES + [(7, 9, 1)])
+def test_basis_and_ranks_exact(cuda, oracle, case):
+    N, norb0, tlz = case
+    B = ed.TwoLevelFermionFockBasis()
+    empty = B.GenerateFockSpace(N, norb0, norb0 + 2, tlz)
+    f, s = oracle.basis2(N, norb0, tlz)
+    assert empty == (len(f) == 0)
+    assert B.GetStoredDimension() == len(f)
+    if not len(f):
+        return
+    df, ds = B.GetFockBasis()
+    assert np.array_equal(df, f) and np.array_equal(ds, s)
+    for i in range(0, len(f), max(1, len(f) // 50)):
+        assert B.FindFockStateIndex(0, int(f[i]), int(s[i])) == i
+    # a word with one particle more or fewer is absent
+    assert B.FindFockStateIndex(0, int(f[0]), int(s[0]) ^ 1) == _capi.MISS
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_upper_crs_bit_exact(cuda, oracle, case):
+    N, norb0, tlz = case
+    t0, t1 = tables(oracle, norb0, 3 * norb0 + N)
+    f, s = oracle.basis2(N, norb0, tlz)
+    rng = np.random.default_rng(N)
+    e0 = rng.uniform(-0.5, 0.5, norb0)
+    e1 = 1.3 + rng.uniform(-0.5, 0.5, norb0 + 2)
+    e1[1] = 0.0                                          # a filtered term
+    for energies in ((None, None), (e0, e1)):
+        H = build(N, norb0, tlz, t0, t1, *energies, upper=True)
+        rp, col, val = H.m_crsSparseMatrix.to_host()
+        orp, ocol, oval = oracle.build_upper2(f, s, norb0, t0.m_kTable, t0.m_vTable, t1.m_kTable, t1.m_vTable,
+                                              *energies)
+        assert np.array_equal(rp, orp)
+        assert np.array_equal(col, ocol)
+        assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+
+
+@pytest.mark.parametrize("case", [(4, 6, 0), (6, 9, 0), (4, 23, 0)])
+def test_full_crs_is_exact_symmetric_completion(cuda, oracle, case):
+    N, norb0, tlz = case
+    t0, t1 = tables(oracle, norb0, 5)
+    e0, e1 = np.linspace(-0.2, 0.2, norb0), np.full(norb0 + 2, 0.7)
+    f, s = oracle.basis2(N, norb0, tlz)
+    H = build(N, norb0, tlz, t0, t1, e0, e1, upper=False)
+    rp, col, val = H.m_crsSparseMatrix.to_host()
+    up = oracle.build_upper2(f, s, norb0, t0.m_kTable, t0.m_vTable, t1.m_kTable, t1.m_vTable, e0, e1)
+    orp, ocol, oval = oracle.upper_to_full(*up, len(f))
+    assert np.array_equal(rp, orp)
+    assert np.array_equal(col, ocol)
+    assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+
+
+def test_empty_second_level_reduces_to_one_level(cuda, oracle):
+    """With no second-level interaction and its orbitals lifted by E = 100, the
+    lowest states are the single-level sector's (N=5, 2S=8, Lz=0)."""
+    N, norb0 = 5, 9
+    pp = oracle.odd_coulomb_list(norb0)
+    model = ed.SphereTwoLevelPseudopotentialModel(N, norb0, pp, np.zeros(norb0 + 1), nbrEigenvalues=4)
+    model.SetSector(0)
+    model.BuildTermTables()
+    model.SetOccupationEnergies(np.r_[np.zeros(norb0), np.full(norb0 + 2, 100.0)])
+    assert not model.BuildFockBasis()
+    model.BuildHamiltonian(store_upper=True)
+    assert model.Diagonalize(tol=1e-12, seed=7)
+    one = ed.SpinlessFermionHamiltonian()
+    one.Initialize(N, norb0, twoLz=0)
+    one.Add_CdCdCC_Terms(ed.QuarticTermTables(norb0, pp), store_upper=True)
+    one.LanczosDiagonalize(4, tol=1e-12, seed=7)
+    assert np.allclose(model.hamiltonian.m_eigenvalues, one.m_eigenvalues, rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("case,nev", [((6, 9, 0), 6), ((5, 7, 0), 8), ((6, 7, 4), 5)])
+def test_lowest_eigenvalues_with_degenerate_copies(cuda, oracle, case, nev):
+    """The levels do not mix, so sector eigenvalues E0(L0) + E1(L1) repeat
+    2 min(L0, L1) + 1 times; the dense oracle spectrum counts every copy."""
+    N, norb0, tlz = case
+    t0, t1 = tables(oracle, norb0, 11)
+    e0, e1 = np.zeros(norb0), np.full(norb0 + 2, 0.4)
+    f, s = oracle.basis2(N, norb0, tlz)
+    rp, col, val = oracle.build_upper2(f, s, norb0, t0.m_kTable, t0.m_vTable, t1.m_kTable, t1.m_vTable, e0, e1)
+    import scipy.sparse as sp
+    A = sp.csr_matrix((val, col, rp), shape=(len(f), len(f)))
+    A = (A + sp.triu(A, 1).T).toarray()
+    w = np.linalg.eigvalsh(A)[:nev]
+    H = build(N, norb0, tlz, t0, t1, e0, e1, upper=True)
+    assert H.LanczosDiagonalize(nev, tol=1e-10, seed=3, degeneracy_passes=0)
+    scale = max(1.0, float(np.max(np.abs(w))))
+    single = H.m_eigenvalues.copy()
+    assert H.LanczosDiagonalize(nev, tol=1e-10, seed=3)            # passes on by default here
+    assert np.max(np.abs(single - w)) > 1e-6                       # one sequence misses copies
+    assert np.max(np.abs(H.m_eigenvalues - w)) <= 1e-10 * scale
+    X = np.asarray(H.m_eigenvectors)
+    assert np.allclose(X @ X.T, np.eye(nev), atol=1e-8)
+    for k in range(nev):
+        v = X[k]
+        assert np.linalg.norm(A @ v - H.m_eigenvalues[k] * v) <= 1e-9 * scale
+
+
+def test_mixed_level_terms_refused(cuda, oracle):
+    H = ed.TwoLevelSpinlessFermionHamiltonian()
+    H.Initialize(3, 12, twoLz=0)
+    with pytest.raises(ed.EDError):
+        H.Add_CdCdCC_Terms(ed.QuarticTermTables(5, oracle.odd_coulomb_list(5)), 0, 1, 0, 1)
+    with pytest.raises(ed.EDError):
+        H.Add_CdC_Terms(np.zeros(5), 0, 2)
