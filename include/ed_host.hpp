@@ -242,6 +242,13 @@ class ArpackWrapper {
         return ok;
     }
 
+    // any engine operator (a two-level Hamiltonian's, for one)
+    bool DiagonalizeOperator(ed_op* op, double* eigenvectors, double* eigenvalues, int fullDim, int nbrEigenvalues,
+                             MpiWrapper& mpi)
+    {
+        return Run(op, eigenvectors, eigenvalues, fullDim, nbrEigenvalues, mpi);
+    }
+
   private:
     bool Fail(ed_status s, const std::string& msg, MpiWrapper& mpi)
     {
@@ -385,6 +392,220 @@ class SpinlessFermionHamiltonian {
     utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
     ed_crs* m_crs = nullptr;
     QuarticTermTables* m_terms = nullptr;
+};
+
+// term_tables.hpp QuadraticTermTables as the two-level model fills it: one
+// occupation energy per orbital of a level (GetVTable()->data(), length
+// GetDimension()).
+class QuadraticTermTables {
+  public:
+    void Initialize(iSize_t nbrOrbitals, const utilities::MpiWrapper&) { m_vTable.assign(nbrOrbitals, 0.0); }
+    std::vector<double>* GetVTable() { return &m_vTable; }
+    const std::vector<double>* GetVTable() const { return &m_vTable; }
+    iSize_t GetDimension() const { return (iSize_t)m_vTable.size(); }
+
+  private:
+    std::vector<double> m_vTable;
+};
+
+// two_level_fermion_fock_basis.hpp:62.  A state (first, second) is stored on
+// the device as one word (first << nbrOrbitals2) | second; the ascending order
+// of those words is the reference's (first, second) sort.
+class TwoLevelFermionFockBasis {
+  public:
+    TwoLevelFermionFockBasis() = default;
+    TwoLevelFermionFockBasis(const TwoLevelFermionFockBasis&) = delete;
+    TwoLevelFermionFockBasis& operator=(const TwoLevelFermionFockBasis&) = delete;
+    ~TwoLevelFermionFockBasis() { if (m_h) ed_basis_free(m_h); }
+
+    // two_level_fermion_fock_basis.cpp:289 with TestAngularMomentumSector2LL
+    // for the sector twoLz; returns true when the sector is empty
+    bool GenerateFockSpace(iSize_t nbrParticles, iSize_t nbrOrbitals1, iSize_t nbrOrbitals2, int twoLz,
+                           utilities::MpiWrapper& mpi)
+    {
+        if (nbrOrbitals2 != nbrOrbitals1 + 2)
+            throw utilities::EdError(ED_ERR_ARG, "the second level has nbrOrbitals1 + 2 orbitals on the sphere");
+        if (m_h) ed_basis_free(m_h);
+        m_h = nullptr;
+        utilities::EdCheck(ed_basis2_build((int)nbrParticles, (int)nbrOrbitals1, twoLz, nullptr, &m_h), &mpi);
+        m_nbrOrbitals2 = nbrOrbitals2;
+        m_basisStored = true;
+        return GetStoredDimension() == 0;
+    }
+    fock_t GetStoredDimension() const
+    {
+        uint64_t d = 0;
+        if (m_h) utilities::EdCheck(ed_basis_dim(m_h, &d));
+        return d;
+    }
+    // two_level_fermion_fock_basis.cpp:211: UINT64_MAX when absent
+    void FindFockStateIndex(fock_t offset, fock_t first, fock_t second, fock_t& index) const
+    {
+        const uint64_t word = (first << m_nbrOrbitals2) | second;
+        uint64_t idx = 0;
+        utilities::EdCheck(ed_basis_rank_host(m_h, &word, &idx, 1));
+        index = idx == ~0ull ? idx : idx + offset;
+    }
+    // two_level_fermion_fock_basis.cpp:477
+    void GetFockBasis(fock_t* buffer1, fock_t* buffer2, fock_t dim, utilities::MpiWrapper& mpi) const
+    {
+        std::vector<uint64_t> w(dim);
+        utilities::EdCheck(ed_basis_get(m_h, w.data(), dim), &mpi);
+        const uint64_t mask = (1ull << m_nbrOrbitals2) - 1ull;
+        for (fock_t i = 0; i < dim; ++i) {
+            buffer1[i] = w[i] >> m_nbrOrbitals2;
+            buffer2[i] = w[i] & mask;
+        }
+    }
+    ed_basis* handle() const { return m_h; }
+    bool m_basisStored = false;
+
+  private:
+    ed_basis* m_h = nullptr;
+    iSize_t m_nbrOrbitals2 = 0;
+};
+
+// two_level_spinless_fermion_hamiltonian.hpp:52 for T = double, driven as
+// SphereTwoLevelPseudopotentialModel::BuildHamiltonian does
+// (two_level_pseudopotential_model.cpp:190-215).  Add_CdC_Terms and
+// Add_CdCdCC_Terms record each level's tables (terms within one level only,
+// as in the reference); the device build runs once, at the first product or
+// solve, and sums each entry in that call order.
+template <typename T>
+class TwoLevelSpinlessFermionHamiltonian {
+    static_assert(sizeof(T) == sizeof(double), "the device path is real FP64");
+
+  public:
+    TwoLevelSpinlessFermionHamiltonian() = default;
+    TwoLevelSpinlessFermionHamiltonian(const TwoLevelSpinlessFermionHamiltonian&) = delete;
+    TwoLevelSpinlessFermionHamiltonian& operator=(const TwoLevelSpinlessFermionHamiltonian&) = delete;
+    ~TwoLevelSpinlessFermionHamiltonian() { Clear(); }
+
+    // nbrOrbitals = 2 (2S+1) + 2, both levels (two_level_pseudopotential_model.cpp:73)
+    void Initialize(iSize_t nbrParticles, iSize_t nbrOrbitals, utilities::storageMethod_t storageMethod,
+                    utilities::MpiWrapper& mpi, int twoLz = 0)
+    {
+        if (nbrParticles == 0 || nbrOrbitals < 4 || nbrOrbitals % 2) {
+            mpi.m_exitFlag = true;
+            throw utilities::EdError(ED_ERR_ARG, "need nbrParticles > 0 and nbrOrbitals = 2 * norb0 + 2");
+        }
+        m_norb0 = (nbrOrbitals - 2) / 2;
+        m_storageMethod = storageMethod;
+        m_fockBasis.GenerateFockSpace(nbrParticles, m_norb0, m_norb0 + 2, twoLz, mpi);
+    }
+    // two_level_spinless_fermion_hamiltonian.hpp:147
+    void Add_CdC_Terms(QuadraticTermTables* tables, iSize_t level1, iSize_t level2, fock_t /*minRow*/,
+                       fock_t /*maxRow*/, utilities::MpiWrapper& mpi)
+    {
+        const iSize_t lvl = Level(level1, level2, level2, level2, mpi);
+        if (tables->GetDimension() != m_norb0 + 2 * lvl) Refuse("occupation energies of the wrong length", mpi);
+        m_energies[lvl] = *tables->GetVTable();
+        Clear();
+    }
+    // two_level_spinless_fermion_hamiltonian.hpp:306
+    void Add_CdCdCC_Terms(QuarticTermTables* tables, iSize_t level1, iSize_t level2, iSize_t level3,
+                          iSize_t level4, fock_t /*minRow*/, fock_t /*maxRow*/, utilities::MpiWrapper& mpi,
+                          bool storeUpper = false)
+    {
+        const iSize_t lvl = Level(level1, level2, level3, level4, mpi);
+        m_quartic[lvl] = tables;
+        m_storeUpper = storeUpper;
+        Clear();
+    }
+    void Build(utilities::MpiWrapper& mpi)
+    {
+        Clear();
+        QuarticTermTables* q[2] = {m_quartic[0], m_quartic[1]};
+        for (int l = 0; l < 2; ++l)
+            if (!q[l]) {
+                m_zero[l].Initialize(m_norb0 + 2 * l, std::vector<double>{0.0});
+                q[l] = &m_zero[l];
+            }
+        utilities::EdCheck(ed_ham2_build_crs(m_fockBasis.handle(), q[0]->handle(), q[1]->handle(),
+                                             m_energies[0].empty() ? nullptr : m_energies[0].data(),
+                                             m_energies[1].empty() ? nullptr : m_energies[1].data(),
+                                             m_storeUpper ? 1 : 0, nullptr, &m_crs),
+                           &mpi);
+    }
+    fock_t GetFockSpaceDimension() const { return m_fockBasis.GetStoredDimension(); }
+    int64_t GetNbrNonZeros() const
+    {
+        int64_t nnz = 0;
+        if (m_crs) utilities::EdCheck(ed_crs_info(m_crs, nullptr, &nnz, nullptr));
+        return nnz;
+    }
+    void GetCrs(std::vector<int64_t>& rowStarts, std::vector<int32_t>& cols, std::vector<double>& data) const
+    {
+        int64_t n = 0, nnz = 0;
+        utilities::EdCheck(ed_crs_info(m_crs, &n, &nnz, nullptr));
+        rowStarts.resize(n + 1);
+        cols.resize(nnz);
+        data.resize(nnz);
+        utilities::EdCheck(ed_crs_get(m_crs, rowStarts.data(), cols.data(), data.data()));
+    }
+    void Apply(const double* x_dev, double* y_dev)
+    {
+        utilities::MpiWrapper mpi;
+        if (!m_crs) Build(mpi);
+        utilities::EdCheck(ed_spmv(m_crs, x_dev, y_dev, nullptr));
+    }
+    // hamiltonian_base.hpp:770.  The levels do not mix, so a sector's
+    // eigenvalues E0(L0) + E1(L1) repeat 2 min(L0, L1) + 1 times: the solve
+    // runs nbrEigenvalues degeneracy passes unless SetDegeneracyPasses was
+    // called on m_arpackWrapper with another count.
+    bool LanczosDiagonalize(iSize_t nbrEigenvalues, utilities::MpiWrapper& mpi, double tol = 1e-10,
+                            bool wantVectors = true)
+    {
+        if (!m_crs) Build(mpi);
+        const fock_t n = GetFockSpaceDimension();
+        m_eigenvalues.assign(nbrEigenvalues, 0.0);
+        m_eigenvectors.assign(wantVectors ? (size_t)n * nbrEigenvalues : 0, 0.0);
+        m_arpackWrapper.SetTolerance(tol);
+        if (!m_passesSet) m_arpackWrapper.SetDegeneracyPasses((int)nbrEigenvalues);
+        ed_op* op = nullptr;
+        utilities::EdCheck(ed_op_from_crs(m_crs, &op), &mpi);
+        const bool ok = m_arpackWrapper.DiagonalizeOperator(op, wantVectors ? m_eigenvectors.data() : nullptr,
+                                                            m_eigenvalues.data(), (int)n, (int)nbrEigenvalues, mpi);
+        ed_op_free(op);
+        return ok;
+    }
+    void SetDegeneracyPasses(int passes)
+    {
+        m_arpackWrapper.SetDegeneracyPasses(passes);
+        m_passesSet = true;
+    }
+    void Clear()
+    {
+        if (m_crs) ed_crs_free(m_crs);
+        m_crs = nullptr;
+    }
+
+    TwoLevelFermionFockBasis m_fockBasis;
+    utilities::linearAlgebra::ArpackWrapper m_arpackWrapper;
+    std::vector<double> m_eigenvalues;
+    std::vector<double> m_eigenvectors;   // column-major n x nev
+
+  private:
+    iSize_t Level(iSize_t l1, iSize_t l2, iSize_t l3, iSize_t l4, utilities::MpiWrapper& mpi)
+    {
+        if (l1 > 1 || l2 > 1 || l3 > 1 || l4 > 1) Refuse("level specification incorrect (set to 0,1 only)", mpi);
+        if (l1 != l2 || l2 != l3 || l3 != l4) Refuse("only coded for terms in the same level so far", mpi);
+        return l1;
+    }
+    [[noreturn]] void Refuse(const char* msg, utilities::MpiWrapper& mpi)
+    {
+        std::cerr << "\n\tERROR in TwoLevelSpinlessFermionHamiltonian: " << msg << std::endl;
+        mpi.m_exitFlag = true;
+        throw utilities::EdError(ED_ERR_ARG, msg);
+    }
+    iSize_t m_norb0 = 0;
+    utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
+    std::vector<double> m_energies[2];
+    QuarticTermTables* m_quartic[2] = {nullptr, nullptr};
+    QuarticTermTables m_zero[2];
+    bool m_storeUpper = false;
+    bool m_passesSet = false;
+    ed_crs* m_crs = nullptr;
 };
 
 // observables/fermion_observables.hpp:39, for the eigenvectors of a real

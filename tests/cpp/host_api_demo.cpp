@@ -1,8 +1,9 @@
 // Exercises the reference-shaped C++ host classes (include/ed_host.hpp) the
 // way the reference's model layer drives them for one sector:
 // tables -> basis -> Add_CdCdCC_Terms -> LanczosDiagonalize, plus the
-// std::function product path of ArpackWrapper, and the ground state's
-// observables.  Prints one JSON line.
+// std::function product path of ArpackWrapper, the ground state's
+// observables, and a two-level sector (N=4, norb0=6, Lz=0) as
+// SphereTwoLevelPseudopotentialModel builds it.  Prints one JSON line.
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -75,6 +76,40 @@ int main(int argc, char** argv)
     for (int k = 0; k < norb; ++k) std::printf("%s%.17g", k ? ", " : "", rho[k]);
     std::printf("], \"density_sum\": %.17g, \"dd00\": %.17g, \"participation\": %.17g, \"top_state\": %llu, "
                 "\"top_amp\": %.17g", nsum, dd[0], pr, (unsigned long long)top[0], amp[0].real());
-    std::printf(", \"residual\": %.3e}\n", H.m_arpackWrapper.LastInfo().max_residual);
-    return (ok && ok2 && rank_ok) ? 0 : 1;
+    // two levels: LLL tables of norb0 orbitals, second-level tables of norb0 + 2
+    // (odd-m Coulomb lists of those sizes), second-level occupation energy 0.4
+    const int n0 = 6;
+    std::vector<double> pp0(n0 - 1, 0.0), pp1(n0 + 1, 0.0), c0(n0), c1(n0 + 2);
+    utilities::EdCheck(ed_coulomb_pseudopotentials(n0, c0.data()));
+    utilities::EdCheck(ed_coulomb_pseudopotentials(n0 + 2, c1.data()));
+    for (int m = 1; m < n0 - 1; m += 2) pp0[m] = c0[m];
+    for (int m = 1; m < n0 + 1; m += 2) pp1[m] = c1[m];
+    diagonalization::QuarticTermTables q0, q1;
+    q0.Initialize(n0, pp0);
+    q1.Initialize(n0 + 2, pp1);
+    diagonalization::QuadraticTermTables e1;
+    e1.Initialize(n0 + 2, mpi);
+    for (double& e : *e1.GetVTable()) e = 0.4;
+    diagonalization::TwoLevelSpinlessFermionHamiltonian<double> H2;
+    H2.Initialize(4, 2 * n0 + 2, utilities::_SPARSE_CRS_, mpi, 0);
+    const diagonalization::fock_t dim2 = H2.GetFockSpaceDimension();
+    H2.Add_CdC_Terms(&e1, 1, 1, 0, dim2, mpi);
+    H2.Add_CdCdCC_Terms(&q0, 0, 0, 0, 0, 0, dim2, mpi);
+    H2.Add_CdCdCC_Terms(&q1, 1, 1, 1, 1, 0, dim2, mpi);
+    const bool ok3 = H2.LanczosDiagonalize(4, mpi, 1e-10);
+    std::vector<diagonalization::fock_t> f2(dim2), s2(dim2);
+    H2.m_fockBasis.GetFockBasis(f2.data(), s2.data(), dim2, mpi);
+    bool rank2_ok = true;
+    for (diagonalization::fock_t i = 0; i < dim2; i += 7) {
+        diagonalization::fock_t idx = 0;
+        H2.m_fockBasis.FindFockStateIndex(0, f2[i], s2[i], idx);
+        rank2_ok = rank2_ok && idx == i;
+    }
+    std::printf(", \"residual\": %.3e, \"two_level\": {\"ok\": %s, \"rank_ok\": %s, \"dim\": %llu, \"nnz\": %lld, "
+                "\"eigenvalues\": [",
+                H.m_arpackWrapper.LastInfo().max_residual, ok3 ? "true" : "false", rank2_ok ? "true" : "false",
+                (unsigned long long)dim2, (long long)H2.GetNbrNonZeros());
+    for (int i = 0; i < 4; ++i) std::printf("%s%.17g", i ? ", " : "", H2.m_eigenvalues[i]);
+    std::printf("]}}\n");
+    return (ok && ok2 && rank_ok && ok3 && rank2_ok) ? 0 : 1;
 }

@@ -44,3 +44,14 @@ def test_host_classes_solve_sector(cuda, oracle, tmp_path):
     assert abs(r["density_sum"] - 6) < 1e-9 and np.allclose(rho, rho[::-1], atol=1e-8)   # N; Lz reflection
     assert abs(r["dd00"] - rho[0]) < 1e-12 and 1.0 <= r["participation"] <= len(b)
     assert int(r["top_state"]) in set(int(w) for w in b)
+    # the two-level sector through TwoLevelSpinlessFermionHamiltonian (every degenerate copy)
+    t = r["two_level"]
+    assert t["ok"] and t["rank_ok"]
+    f, s = oracle.basis2(4, 6, 0)
+    kt0, vt0 = oracle.quartic_tables(6, oracle.odd_coulomb_list(6))
+    kt1, vt1 = oracle.quartic_tables(8, oracle.odd_coulomb_list(8))
+    u = oracle.build_upper2(f, s, 6, kt0, vt0, kt1, vt1, None, np.full(8, 0.4))
+    fr, fc, fv = oracle.upper_to_full(*u, len(f))
+    ref2 = np.linalg.eigvalsh(sp.csr_matrix((fv, fc, fr), shape=(len(f), len(f))).toarray())[:4]
+    assert t["dim"] == len(f) and t["nnz"] == len(fv)
+    assert np.max(np.abs(np.array(t["eigenvalues"]) - ref2)) < 1e-10 * max(1.0, np.abs(ref2).max())
