@@ -215,7 +215,15 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
     if (!a.upper && avg >= 96) {
         k_spmv_full<8, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else if (!a.upper) {
-        if (avg >= 24) k_spmv_full<4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        // rows of 24-96 elements (two-level sectors, small one-level ones):
+        // four lanes per row with four loads ahead, or eight lanes per row
+        // once x passes about 20 MB (measured on GB300: two-level N=7 sectors
+        // of 1.3-2.0M rows 4.3-4.5 TB/s with four lanes, 3.5-3.6 with eight;
+        // N=8 sectors of 2.9-5.9M rows 3.8-4.1 TB/s with eight, 2.9-3.0 with
+        // four)
+        if (avg >= 24 && a.n >= 2500000)
+            k_spmv_full<8, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        else if (avg >= 24) k_spmv_full<4, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
         else k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else {
         ED_CUDA(cudaMemsetAsync(y, 0, (size_t)a.n * sizeof(double), st));

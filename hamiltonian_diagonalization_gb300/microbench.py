@@ -25,7 +25,8 @@ With --two-level the sector is N,norb0,twoLz of the two-Landau-level model
 (norb0 lowest-level orbitals, norb0 + 2 in the second level, odd-m Coulomb
 pseudopotential lists of those sizes for the two levels' tables, second-level
 occupation energy 1.0): it times the basis, the CRS build, the product and
-the --nev lowest eigenpairs with and without the degeneracy passes.
+the --nev lowest eigenpairs with and without the degeneracy passes (with
+--build, the basis and the CRS build only).
 """
 from __future__ import annotations
 
@@ -63,12 +64,12 @@ def main():
     N, norb, tlz = (int(x) for x in args.sector.split(","))
     if args.batch:
         return batch_main(ed, C, torch, N, norb, tlz, args)
+    if args.two_level:
+        return two_level_main(ed, C, torch, N, norb, tlz, args)
     if args.build:
         return build_main(ed, torch, N, norb, tlz, args)
     if args.observables:
         return observables_main(ed, N, norb, tlz, args)
-    if args.two_level:
-        return two_level_main(ed, C, torch, N, norb, tlz, args)
     H = ed.SpinlessFermionHamiltonian()
     H.Initialize(N, norb, twoLz=tlz)
     T = ed.QuarticTermTables(norb, ed.odd_coulomb_list(norb))
@@ -154,6 +155,9 @@ def two_level_main(ed, C, torch, N, norb0, tlz, args):
             tc.append(y)
     n, nnz = H.GetDimension(), H.m_crsSparseMatrix.GetNbrNonZeros()
     res.update({"n": n, "nnz": nnz, "ms_basis": 1e3 * min(tb), "ms_build": 1e3 * min(tc)})
+    if args.build:                      # basis and CRS build only
+        print(json.dumps(res))
+        return
     mv = ed.MatrixVectorFunction(H)
     x = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, n)).cuda()
     y = torch.empty_like(x)
