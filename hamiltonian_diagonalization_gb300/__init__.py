@@ -5,9 +5,13 @@ ABI of libedgb300 (include/ed_capi.h)."""
 from ._capi import EDError, LanczosParams, SolveInfo, lib  # noqa: F401
 from .host import (  # noqa: F401
     ArpackWrapper,
+    ComplexCrsSparseMatrix,
+    ComplexQuarticTermTables,
+    ComplexSpinlessFermionHamiltonian,
     CrsSparseMatrix,
     FermionFockBasis,
     HamiltonianBatch,
+    InteractingOflModel,
     MatrixVectorFunction,
     MpiWrapper,
     Observables,

@@ -83,6 +83,15 @@ _SIGS = {
     "ed_crs_free": (c_int, [c_void_p]),
     "ed_crs_info": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
     "ed_basis2_build": (c_int, [c_int, c_int, c_int, c_void_p, P(c_void_p)]),
+    "ed_basis_momentum_build": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, P(c_void_p)]),
+    "ed_cterms_create": (c_int, [c_int, c_int, c_int, P(ctypes.c_uint16), P(c_double), P(c_double), P(c_void_p)]),
+    "ed_cterms_free": (c_int, [c_void_p]),
+    "ed_cham_build_crs": (c_int, [c_void_p, c_void_p, c_int, c_void_p, P(c_void_p)]),
+    "ed_ccrs_free": (c_int, [c_void_p]),
+    "ed_ccrs_info": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
+    "ed_ccrs_get": (c_int, [c_void_p, P(c_i64), P(ctypes.c_int32), P(c_double)]),
+    "ed_cspmv": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ed_clanczos": (c_int, [c_void_p, P(LanczosParams), P(c_double), P(c_double), P(c_double), P(SolveInfo)]),
     "ed_ham2_build_crs": (c_int, [c_void_p, c_void_p, c_void_p, P(c_double), P(c_double), c_int, c_void_p,
                                   P(c_void_p)]),
     "ed_basis_levels": (c_int, [c_void_p, P(c_int), P(c_int), P(c_int)]),

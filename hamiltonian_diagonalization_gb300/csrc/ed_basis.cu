@@ -126,6 +126,33 @@ __global__ void k_basis_count(int H, int L, int N, int64_t S, int max_sum_low,
     }
 }
 
+// Momentum sectors: the class of a low word is (popcount, sum kx mod X,
+// sum ky mod Y) with bit p at kx = p / Y, ky = p % Y; counts[h] as above.
+__global__ void k_basis_count_mom(int H, int L, int N, int X, int Y, int kx_tot, int ky_tot,
+                                  const uint32_t* __restrict__ class_count, int64_t* __restrict__ counts,
+                                  uint16_t* __restrict__ need_class)
+{
+    const int64_t nh = 1ll << H;
+    for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+        int sx = 0, sy = 0;
+        for (uint64_t t = (uint64_t)h; t; t &= t - 1) {
+            const int p = L + __ffsll((long long)t) - 1;
+            sx += p / Y;
+            sy += p % Y;
+        }
+        const int pl = N - __popcll((unsigned long long)h);
+        int64_t c = 0;
+        uint16_t cls = 0xFFFF;
+        if (pl >= 0 && pl <= L) {
+            const int cx = ((kx_tot - sx) % X + X) % X, cy = ((ky_tot - sy) % Y + Y) % Y;
+            cls = (uint16_t)((pl * X + cx) * Y + cy);
+            c = class_count[cls];
+        }
+        counts[h] = c;
+        need_class[h] = cls;
+    }
+}
+
 // One warp per high half: write its block of words and its hi-table entry.
 __global__ void k_basis_fill(int H, int L, const int64_t* __restrict__ offs, const int64_t* __restrict__ counts,
                              const uint16_t* __restrict__ need_class, const uint32_t* __restrict__ class_start,
@@ -224,8 +251,76 @@ std::vector<int> basis_weights(const ed_basis& b)
     return w;
 }
 
+namespace {
+// Momentum-sector basis (the optical-flux-lattice FermionFockBasis with
+// TestLinearMomentumSector2, linear_momentum_constraints_2D.cpp:38-79).
+void basis_build_momentum(ed_basis& b, cudaStream_t st)
+{
+    const int N = b.N, norb = b.norb, X = b.dimX, Y = b.dimY;
+    ED_REQUIRE(X >= 1 && Y >= 1 && norb == X * Y && norb <= kMaxOrbitals, ED_ERR_RANGE,
+               "momentum basis: need dimX * dimY <= 40 orbitals");
+    ED_REQUIRE(N >= 1 && N <= norb && N < 64, ED_ERR_ARG, "need 1 <= N <= norb");
+    ED_REQUIRE(b.kx_tot >= 0 && b.kx_tot < X && b.ky_tot >= 0 && b.ky_tot < Y, ED_ERR_ARG,
+               "need 0 <= kxTot < dimX and 0 <= kyTot < dimY");
+    const int L = norb / 2, H = norb - L;
+    b.low_bits = L;
+    b.high_bits = H;
+    b.dim = 0;
+    b.sector_sum = 0;
+    const int nclass = (L + 1) * X * Y;
+    ED_REQUIRE(nclass < 0xFFFF, ED_ERR_RANGE, "too many low-word classes");
+    const uint64_t nl = 1ull << L;
+    std::vector<uint32_t> ccount(nclass, 0), cstart(nclass, 0), clist(nl), rank_in_class(nl);
+    std::vector<uint64_t> lo(nl);
+    for (uint64_t l = 0; l < nl; ++l) {
+        int sx = 0, sy = 0;
+        for (uint64_t x = l; x; x &= x - 1) {
+            const int p = __builtin_ctzll(x);
+            sx += p / Y;
+            sy += p % Y;
+        }
+        const int cls = (__builtin_popcountll(l) * X + sx % X) * Y + sy % Y;
+        rank_in_class[l] = ccount[cls]++;
+        lo[l] = ((uint64_t)cls << 32) | rank_in_class[l];
+    }
+    uint32_t acc = 0;
+    for (int c = 0; c < nclass; ++c) { cstart[c] = acc; acc += ccount[c]; }
+    for (uint64_t l = 0; l < nl; ++l) clist[cstart[lo[l] >> 32] + rank_in_class[l]] = (uint32_t)l;
+    b.lo.alloc(nl);
+    b.hi.alloc(1ull << H);
+    DevBuf<uint32_t> d_ccount(nclass), d_cstart(nclass), d_clist(nl);
+    ED_CUDA(cudaMemcpyAsync(b.lo.p, lo.data(), nl * 8, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(d_ccount.p, ccount.data(), nclass * 4, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(d_cstart.p, cstart.data(), nclass * 4, cudaMemcpyHostToDevice, st));
+    ED_CUDA(cudaMemcpyAsync(d_clist.p, clist.data(), nl * 4, cudaMemcpyHostToDevice, st));
+    const int64_t nh = 1ll << H;
+    DevBuf<int64_t> counts(nh), offs(nh + 1);
+    DevBuf<uint16_t> need(nh);
+    k_basis_count_mom<<<grid_for(nh, 256), 256, 0, st>>>(H, L, N, X, Y, b.kx_tot, b.ky_tot, d_ccount.p, counts.p,
+                                                         need.p);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    exclusive_scan_i64(counts.p, offs.p, nh, st);
+    int64_t dim = 0;
+    ED_CUDA(cudaMemcpyAsync(&dim, offs.p + nh, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    b.dim = (uint64_t)dim;
+    b.words.alloc(dim > 0 ? (size_t)dim : 1);
+    k_basis_fill<<<grid_for(nh * 32, 256), 256, 0, st>>>(H, L, offs.p, counts.p, need.p, d_cstart.p, d_clist.p,
+                                                         b.words.p, b.hi.p);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    ED_CUDA(cudaStreamSynchronize(st));
+    if (dim == 0) b.sector_sum = -1;
+}
+}  // namespace
+
 void basis_build(ed_basis& b, cudaStream_t st)
 {
+    if (b.dimX > 0) {
+        basis_build_momentum(b, st);
+        return;
+    }
     const int N = b.N, norb = b.norb;
     const int maxbits = b.levels == 2 ? kMaxTwoLevelBits : kMaxOrbitals;
     ED_REQUIRE(norb >= 1 && norb <= maxbits, ED_ERR_RANGE,
@@ -298,7 +393,7 @@ void basis_build(ed_basis& b, cudaStream_t st)
 
 void basis_compact_tables(const ed_basis& b, cudaStream_t st)
 {
-    if (b.mf_lo.p || b.dim == 0 || b.levels != 1) return;
+    if (b.mf_lo.p || b.dim == 0 || b.levels != 1 || b.dimX > 0) return;
     const int norb = b.norb, L = std::min(13, norb), H = norb - L;
     if (H > 23) return;   // high table over 64 MB: the matrix-free product keeps the main tables
     const int max_sum_low = L * (L - 1) / 2;

@@ -618,6 +618,200 @@ __global__ void __launch_bounds__(256) k_fill2(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Complex momentum-conserving build: SpinlessFermionHamiltonian<dcmplx>
+// Add_CdC_Terms / Add_CdCdCC_Terms (spinless_fermion_hamiltonian.hpp:150-436)
+// as InteractingOflModel::BuildHamiltonian calls them with array-format
+// tables (interacting_ofl_model.cpp:1034-1052).  As in the one-level build,
+// an off-diagonal element is a pair hop (a,b) -> (c,d), here within one
+// momentum class, worth sign(state) * W[hop] with the same parity rule; the
+// stored (upper) element of row `in` is <out|H|in>, and a lower element of the
+// full storage is the conjugate of the upper element it mirrors,
+// sign * conj(W[reverse hop]).  The diagonal sums the occupation energies,
+// then the quartic diagonal terms, in the reference's order.
+
+struct CView {
+    const int* cls_off;
+    const uint16_t* pairs;
+    const int* pidx;
+    const int* w_off;
+    const double2* w;
+    const double2* da;
+    const double2* db;
+    const double2* e;
+    int K, X, Y;
+};
+
+__device__ __forceinline__ int pair_class(int a, int b, int X, int Y)
+{
+    return ((a / Y + b / Y) % X) * Y + (a % Y + b % Y) % Y;
+}
+
+__device__ __forceinline__ bool czero(double2 v)
+{
+    return ((__double_as_longlong(v.x) << 1) | (__double_as_longlong(v.y) << 1)) == 0;
+}
+
+__device__ __forceinline__ double2 cdiag_element(const CView& v, uint64_t in)
+{
+    double2 acc = make_double2(0.0, 0.0);
+    for (uint64_t t = in; t; t &= t - 1) {
+        const double2 e = __ldg(v.e + (__ffsll((long long)t) - 1));
+        acc.x = acc.x + e.x;
+        acc.y = acc.y + e.y;
+    }
+    for (uint64_t t4 = in; t4; t4 &= t4 - 1) {
+        const int k4 = __ffsll((long long)t4) - 1;
+        for (uint64_t t3 = in & ~(1ull << k4); t3; t3 &= t3 - 1) {
+            const int k3 = __ffsll((long long)t3) - 1;
+            const double2 p = __ldg(v.da + k4 * v.K + k3), q = __ldg(v.db + k4 * v.K + k3);
+            acc.x = acc.x + p.x;
+            acc.y = acc.y + p.y;
+            acc.x = acc.x + q.x;
+            acc.y = acc.y + q.y;
+        }
+    }
+    return acc;
+}
+
+// Weight of the hop (a,b) -> (c,d) of class P as stored in row `in`: the
+// upper element (d > b) or the conjugate of the mirrored upper one.
+__device__ __forceinline__ double2 chop_weight(const CView& v, int P, int ia, int ic, int cnt, bool upper_el)
+{
+    const int o = __ldg(v.w_off + P);
+    if (upper_el) return __ldg(v.w + o + ia * cnt + ic);
+    const double2 r = __ldg(v.w + o + ic * cnt + ia);
+    return make_double2(r.x, -r.y);
+}
+
+__global__ void k_cdiag(const uint64_t* __restrict__ words, int64_t n, CView v, double2* __restrict__ diag)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        diag[r] = cdiag_element(v, words[r]);
+}
+
+__global__ void k_ccount(const uint64_t* __restrict__ words, int64_t n, const double2* __restrict__ diag, CView v,
+                         int upper, int64_t* __restrict__ rowlen, int* __restrict__ maxtasks)
+{
+    unsigned tmax = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t in = words[r];
+        const double2 dg = diag[r];
+        int64_t cnt = hypot(dg.x, dg.y) < kSparseZeroTol ? 0 : 1;
+        unsigned tasks = 1;
+        for (uint64_t ta = in; ta; ta &= ta - 1) {
+            const int a = __ffsll((long long)ta) - 1;
+            for (uint64_t tb = ta & (ta - 1); tb; tb &= tb - 1) {
+                const int b = __ffsll((long long)tb) - 1;
+                const int P = pair_class(a, b, v.X, v.Y);
+                const int base = __ldg(v.cls_off + P), m = __ldg(v.cls_off + P + 1) - base;
+                const int ia = __ldg(v.pidx + a * v.K + b);
+                for (int ic = 0; ic < m; ++ic) {
+                    const int pr = __ldg(v.pairs + base + ic), c = pr & 255, d = pr >> 8;
+                    if (((in >> c) | (in >> d)) & 1ull) continue;
+                    if (upper && d < b) continue;
+                    ++tasks;
+                    if (!czero(chop_weight(v, P, ia, ic, m, d > b))) ++cnt;
+                }
+            }
+        }
+        rowlen[r] = cnt;
+        tmax = tasks > tmax ? tasks : tmax;
+    }
+    tmax = __reduce_max_sync(0xffffffffu, tmax);
+    if ((threadIdx.x & 31) == 0) atomicMax(maxtasks, (int)tmax);
+}
+
+__host__ __device__ inline size_t cfill_warp_bytes(int cap)
+{
+    return ((size_t)cap * 20 + 16 + 15) & ~(size_t)15;
+}
+
+// One warp per row: the lanes take the occupied pairs, append every nonzero
+// hop as (rank << sb | slot) with its complex value, the register sort orders
+// the row by column, and the row is written coalesced.
+template <int EM>
+__global__ void __launch_bounds__(256) k_cfill(const uint64_t* __restrict__ words, int64_t n,
+                                               const double2* __restrict__ diag, CView v, int N, int upper,
+                                               const int64_t* __restrict__ rowptr, const uint64_t* __restrict__ hi,
+                                               const uint64_t* __restrict__ lo_tab, int L, int cap, int sb,
+                                               int32_t* __restrict__ col, double2* __restrict__ val,
+                                               int* __restrict__ err)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp_in_cta = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wbase = smem + (size_t)warp_in_cta * cfill_warp_bytes(cap);
+    double2* vals = reinterpret_cast<double2*>(wbase);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(wbase + (size_t)cap * 16);
+    int* counter = reinterpret_cast<int*>(wbase + (size_t)cap * 20);
+    const uint32_t smask = (uint32_t)cap - 1u;
+    const int npairs = N * (N - 1) / 2;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = gw; r < n; r += nwarps) {
+        const uint64_t in = words[r];
+        const int64_t base = rowptr[r];
+        const int64_t want = rowptr[r + 1] - base;
+        if (lane == 0) *counter = 0;
+        __syncwarp();
+        for (int p = lane; p < npairs; p += 32) {
+            // the p-th occupied pair (i < j in occupied order)
+            int j = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)p)) * 0.5f);
+            while (j * (j - 1) / 2 > p) --j;
+            while ((j + 1) * j / 2 <= p) ++j;
+            const int i = p - j * (j - 1) / 2;
+            uint64_t t = in;
+            for (int q = 0; q < i; ++q) t &= t - 1;
+            const int a = __ffsll((long long)t) - 1;
+            for (int q = i; q < j; ++q) t &= t - 1;
+            const int b = __ffsll((long long)t) - 1;
+            const int P = pair_class(a, b, v.X, v.Y);
+            const int cb = __ldg(v.cls_off + P), m = __ldg(v.cls_off + P + 1) - cb;
+            const int ia = __ldg(v.pidx + a * v.K + b);
+            const uint64_t rest = in ^ (1ull << a) ^ (1ull << b);
+            for (int ic = 0; ic < m; ++ic) {
+                const int pr = __ldg(v.pairs + cb + ic), c = pr & 255, d = pr >> 8;
+                if (((in >> c) | (in >> d)) & 1ull) continue;
+                if (upper && d < b) continue;
+                double2 w = chop_weight(v, P, ia, ic, m, d > b);
+                if (czero(w)) continue;
+                if (hop_parity(in, a, b, c, d)) w = make_double2(-w.x, -w.y);
+                const uint64_t out = rest | (1ull << c) | (1ull << d);
+                const uint64_t rk = rank_in_sector(out, hi, lo_tab, L);
+                if (rk == kMiss) atomicOr(err, 2);
+                const int slot = atomicAdd(counter, 1);
+                if (slot < cap) {
+                    keys[slot] = ((uint32_t)rk << sb) | (uint32_t)slot;
+                    vals[slot] = w;
+                }
+            }
+        }
+        __syncwarp();
+        int cnt = *counter;
+        const double2 dv = diag[r];
+        if (!(hypot(dv.x, dv.y) < kSparseZeroTol)) {
+            if (lane == 0 && cnt < cap) {
+                keys[cnt] = ((uint32_t)r << sb) | (uint32_t)cnt;
+                vals[cnt] = dv;
+            }
+            ++cnt;
+        }
+        __syncwarp();
+        if (cnt != want || cnt > cap) {
+            if (lane == 0) atomicOr(err, 1);
+            __syncwarp();
+            continue;
+        }
+        if (cnt > 0) sort_row_dispatch<1, EM>(keys, cnt, lane);
+        for (int t2 = lane; t2 < cnt; t2 += 32) {
+            const uint32_t kk = keys[swz(t2)];
+            col[base + t2] = (int32_t)(kk >> sb);
+            val[base + t2] = vals[kk & smask];
+        }
+        __syncwarp();
+    }
+}
+
 int sm_count()
 {
     int dev = 0, sms = 148;
@@ -631,6 +825,7 @@ int sm_count()
 void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream_t st)
 {
     ED_REQUIRE(b.levels == 1, ED_ERR_ARG, "a two-level basis takes the two-level Hamiltonian build");
+    ED_REQUIRE(b.dimX == 0, ED_ERR_ARG, "a momentum basis takes the complex momentum-conserving build");
     if (b.dim == 0) return;
     const int K = t.norb;
     const size_t smem = (size_t)2 * K * K * 8;
@@ -641,6 +836,7 @@ void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream
 void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, cudaStream_t st)
 {
     ED_REQUIRE(b.levels == 1, ED_ERR_ARG, "a two-level basis takes the two-level Hamiltonian build");
+    ED_REQUIRE(b.dimX == 0, ED_ERR_ARG, "a momentum basis takes the complex momentum-conserving build");
     ED_REQUIRE(t.norb == b.norb, ED_ERR_ARG, "terms and basis have different orbital counts");
     const int64_t n = (int64_t)b.dim;
     ED_REQUIRE(n < (int64_t)0x7fffffff, ED_ERR_RANGE, "sector dimension exceeds int32 column indices");
@@ -849,6 +1045,76 @@ void ham2_build_crs(const ed_basis& b, const ed_terms& t0, const ed_terms& t1, c
     ED_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     ED_CUDA(cudaStreamSynchronize(st));
     ED_REQUIRE(herr == 0, ED_ERR_INTERNAL, "two-level fill: row count or rank check failed on the device");
+}
+
+void cham_build_crs(const ed_basis& b, const ed_cterms& t, int upper, ed_ccrs& a, cudaStream_t st)
+{
+    ED_REQUIRE(b.dimX > 0, ED_ERR_ARG, "the complex build takes a momentum basis");
+    ED_REQUIRE(t.norb == b.norb && t.dimX == b.dimX && t.dimY == b.dimY, ED_ERR_ARG,
+               "terms and basis have different momentum grids");
+    const int64_t n = (int64_t)b.dim;
+    ED_REQUIRE(n < (int64_t)0x7fffffff, ED_ERR_RANGE, "sector dimension exceeds int32 column indices");
+    a.n = n;
+    a.upper = upper ? 1 : 0;
+    a.rowptr.alloc(n + 1);
+    if (n == 0) {
+        ED_CUDA(cudaMemsetAsync(a.rowptr.p, 0, sizeof(int64_t), st));
+        a.nnz = 0;
+        return;
+    }
+    CView v{t.cls_off_dev.p, t.pairs_dev.p, t.pair_index_dev.p, t.w_off_dev.p,
+            reinterpret_cast<const double2*>(t.w_dev.p), reinterpret_cast<const double2*>(t.da_dev.p),
+            reinterpret_cast<const double2*>(t.db_dev.p), reinterpret_cast<const double2*>(t.e_dev.p), t.norb,
+            t.dimX, t.dimY};
+    DevBuf<double2> diag(n);
+    k_cdiag<<<sm_count() * 8, 256, 0, st>>>(b.words.p, n, v, diag.p);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    DevBuf<int64_t> rowlen(n);
+    DevBuf<int> maxtasks_dev(1);
+    ED_CUDA(cudaMemsetAsync(maxtasks_dev.p, 0, sizeof(int), st));
+    k_ccount<<<sm_count() * 4, 256, 0, st>>>(b.words.p, n, diag.p, v, a.upper, rowlen.p, maxtasks_dev.p);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    exclusive_scan_i64(rowlen.p, a.rowptr.p, n, st);
+    ED_CUDA(cudaMemcpyAsync(&a.nnz, a.rowptr.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    int maxtasks = 0;
+    ED_CUDA(cudaMemcpyAsync(&maxtasks, maxtasks_dev.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int64_t maxrow = reduce_max_i64_host(rowlen.p, n, st);
+    ED_CUDA(cudaStreamSynchronize(st));
+    a.max_row = (int)maxrow;
+    a.col.alloc((size_t)a.nnz + kCrsPad);
+    a.val.alloc(2 * ((size_t)a.nnz + kCrsPad));
+    ED_CUDA(cudaMemsetAsync(a.col.p + a.nnz, 0, kCrsPad * sizeof(int32_t), st));
+    ED_CUDA(cudaMemsetAsync(a.val.p + 2 * a.nnz, 0, 2 * kCrsPad * sizeof(double), st));
+    int cap = 32, sb = 5;
+    while (cap < std::max<int64_t>(maxrow, maxtasks + 1)) { cap <<= 1; ++sb; }
+    const size_t warp_b = cfill_warp_bytes(cap);
+    const size_t budget = 200 * 1024;
+    ED_REQUIRE(cap <= 32 * kFillMaxE && ((((uint64_t)(n - 1)) << sb) | (uint64_t)(cap - 1)) < 0xFFFFFFFFull &&
+                   warp_b <= budget,
+               ED_ERR_RANGE, "momentum sector too large for the register-sort fill");
+    DevBuf<int> err(1);
+    ED_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+    const int wpc = std::min<int>(8, (int)(budget / warp_b));
+    const size_t smem = (size_t)wpc * warp_b;
+    auto launch = [&](auto kern) {
+        ED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int ob = 0;
+        ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ob, kern, wpc * 32, smem));
+        kern<<<sm_count() * std::max(1, ob), wpc * 32, smem, st>>>(
+            b.words.p, n, diag.p, v, b.N, a.upper, a.rowptr.p, b.hi.p, b.lo.p, b.low_bits, cap, sb, a.col.p,
+            reinterpret_cast<double2*>(a.val.p), err.p);
+        ::edgb::count_launch();
+    };
+    if (cap <= 128) launch(k_cfill<4>);
+    else if (cap <= 512) launch(k_cfill<16>);
+    else launch(k_cfill<32>);
+    ED_CUDA(cudaGetLastError());
+    int herr = 0;
+    ED_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    ED_REQUIRE(herr == 0, ED_ERR_INTERNAL, "complex fill: row count or rank check failed on the device");
 }
 
 }  // namespace edgb

@@ -157,8 +157,11 @@ struct ed_basis {
     // the second level's orbitals (weight j), the high norb0 bits the lowest
     // level's (weight i + 1), so ascending words follow the reference's
     // (first, second) order and the sector is a fixed sum of weights.
+    // Momentum sectors (dimX > 0, the optical-flux-lattice basis): bit
+    // p = kx * dimY + ky, the sector fixes (sum kx mod dimX, sum ky mod dimY).
     int N = 0, norb = 0, two_lz = 0;
     int levels = 1, norb0 = 0, norb1 = 0;
+    int dimX = 0, dimY = 0, kx_tot = 0, ky_tot = 0;
     int64_t sector_sum = -1;     // sum of occupied positions in the sector (-1: empty)
     uint64_t dim = 0;
     int low_bits = 0, high_bits = 0;
@@ -193,8 +196,47 @@ struct ed_crs {
     edgb::DevBuf<double> val;
 };
 
+// Complex momentum-conserving terms (the optical-flux-lattice QuarticTermTables
+// and QuadraticTermTables in the array format): orbital p = kx * dimY + ky, a
+// pair's class is ((kx_a + kx_b) mod dimX, (ky_a + ky_b) mod dimY), and every
+// off-diagonal element is a pair hop within one class.  w holds, per class,
+// cnt x cnt complex hop weights [removed pair][created pair] with the four
+// ordered terms folded in the reference's visiting order and relative signs
+// +,-,-,+ (exact zero where no term survives the 1e-14 filters), da/db the
+// two diagonal terms of each ordered (k4, k3), and e the occupation energies.
+struct ed_cterms {
+    int norb = 0, dimX = 0, dimY = 0;
+    std::vector<uint16_t> ktab;     // reference layout, (K+1) K^2 / 2 entries
+    std::vector<double> vtab;       // same, complex as (re, im) pairs
+    std::vector<double> e;          // K complex energies (zero without Add_CdC_Terms)
+    std::vector<int> cls_off;       // dimX*dimY + 1: start of each class's pair list
+    std::vector<uint16_t> pairs;    // created/removed pairs c | d << 8, c < d, by class
+    std::vector<int> pair_index;    // K*K: (a, b), a < b -> index within its class
+    std::vector<int> w_off;         // dimX*dimY + 1: start of each class's weights
+    std::vector<double> w;          // complex hop weights
+    std::vector<double> da, db;     // K*K complex diagonal terms
+    edgb::DevBuf<int> cls_off_dev, pair_index_dev, w_off_dev;
+    edgb::DevBuf<uint16_t> pairs_dev;
+    edgb::DevBuf<double> w_dev, da_dev, db_dev, e_dev;
+};
+
+// Complex CRS (std::complex<double> values as (re, im) pairs).  upper = 1 is
+// the reference's storage: row = in-state, column = out-state >= in-state,
+// value <out|H|in>, applied as y_i += A_ij x_j, y_j += conj(A_ij) x_i.
+struct ed_ccrs {
+    int64_t n = 0, nnz = 0;
+    int upper = 0;
+    int max_row = 0;
+    edgb::DevBuf<int64_t> rowptr;
+    edgb::DevBuf<int32_t> col;
+    edgb::DevBuf<double> val;       // 2 * (nnz + kCrsPad)
+};
+
 // ----------------------------------------------------- device-side entry points
 namespace edgb {
+void cterms_derive(ed_cterms& t);
+void cham_build_crs(const ed_basis& b, const ed_cterms& t, int upper, ed_ccrs& a, cudaStream_t st);
+void cspmv(const ed_ccrs& a, const double* x, double* y, cudaStream_t st);
 void basis_build(ed_basis& b, cudaStream_t st);
 std::vector<int> basis_weights(const ed_basis& b);
 void basis_rank(const ed_basis& b, const uint64_t* words, uint64_t* idx, uint64_t m, cudaStream_t st);

@@ -236,7 +236,7 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
 
 void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const double* x, double* y, cudaStream_t st)
 {
-    ED_REQUIRE(b.levels == 1, ED_ERR_ARG, "the matrix-free product takes a one-level basis");
+    ED_REQUIRE(b.levels == 1 && b.dimX == 0, ED_ERR_ARG, "the matrix-free product takes a one-level Lz basis");
     if (b.dim == 0) return;
     const int K = t.norb;
     const int nw = (int)t.hop.w.size();

@@ -159,6 +159,21 @@ class FermionFockBasis:
         self.nbrParticles, self.nbrOrbitals, self.twoLz = int(nbrParticles), int(nbrOrbitals), int(twoLz)
         return self.GetStoredDimension() == 0
 
+    def GenerateFockSpaceMomentum(self, nbrParticles: int, dimX: int, dimY: int, kxTot: int, kyTot: int, mpi=None,
+                                  stream=None) -> bool:
+        """The momentum sector (kxTot, kyTot) of dimX*dimY orbitals p = kx*dimY + ky:
+        GenerateFockSpace with TestLinearMomentumSector2 (interacting_ofl_model.cpp:
+        994-1001, linear_momentum_constraints_2D.cpp:38-79); True when empty."""
+        self.free()
+        h = ctypes.c_void_p()
+        check(lib().ed_basis_momentum_build(int(nbrParticles), int(dimX), int(dimY), int(kxTot), int(kyTot), stream,
+                                            ctypes.byref(h)))
+        self._h = h
+        self.m_basisStored = True
+        self.nbrParticles, self.nbrOrbitals = int(nbrParticles), int(dimX) * int(dimY)
+        self.dimX, self.dimY, self.kxTot, self.kyTot = int(dimX), int(dimY), int(kxTot), int(kyTot)
+        return self.GetStoredDimension() == 0
+
     def handle(self):
         if self._h is None:
             raise EDError(C.ED_ERR_ARG, "basis not generated")
@@ -370,6 +385,199 @@ class SpinlessFermionHamiltonian:
         self.m_eigenvalues = ev
         if readVectors:
             self.m_eigenvectors = vec
+
+
+class ComplexQuarticTermTables:
+    """Complex momentum-conserving quartic terms of the optical-flux-lattice
+    model in the reference's array layout (interacting_ofl_model/term_tables.cpp:
+    95-200): (K+1) K^2 / 2 entries at (t1*K + t2 - t1(t1+1)/2)*K + k with
+    t1 = min(k3,k4), t2 = max(k3,k4); k1 = m_kTable[.. + k2] and
+    V(k1,k2,k3,k4) = m_vTable[.. + (k4 > k3 ? k1 : k2)].  The tables are the
+    input (the reference computes them from Bloch functions in BuildTermTables)."""
+
+    def __init__(self, dimX: int, dimY: int, ktable, vtable):
+        self.dimX, self.dimY = int(dimX), int(dimY)
+        K = self.m_kMax = self.dimX * self.dimY
+        dim = (K + 1) * K * K // 2
+        self.m_kTable = np.ascontiguousarray(ktable, dtype=np.uint16)
+        self.m_vTable = np.ascontiguousarray(vtable, dtype=np.complex128)
+        if self.m_kTable.shape != (dim,) or self.m_vTable.shape != (dim,):
+            raise EDError(C.ED_ERR_ARG, f"tables of {dim} entries expected for a {dimX} x {dimY} grid")
+
+    def _index(self, k3: int, k4: int) -> int:
+        t1, t2 = (k3, k4) if k4 > k3 else (k4, k3)
+        return t1 * self.m_kMax + t2 - t1 * (t1 + 1) // 2
+
+    # term_tables.cpp:108-126
+    def GetK1(self, k2: int, k3: int, k4: int) -> list:
+        return [int(self.m_kTable[self._index(k3, k4) * self.m_kMax + k2])]
+
+    # term_tables.cpp:157-175
+    def GetVkkkk(self, k1: int, k2: int, k3: int, k4: int) -> complex:
+        return complex(self.m_vTable[self._index(k3, k4) * self.m_kMax + (k1 if k4 > k3 else k2)])
+
+
+class ComplexCrsSparseMatrix:
+    """Device CRS of complex values (CrsSparseMatrix<dcmplx>)."""
+
+    def __init__(self, h):
+        self._h = h
+
+    def info(self):
+        n, nnz, up = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        check(lib().ed_ccrs_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(up)))
+        return int(n.value), int(nnz.value), bool(up.value)
+
+    def GetNbrRows(self) -> int:
+        return self.info()[0]
+
+    def GetNbrNonZeros(self) -> int:
+        return self.info()[1]
+
+    def to_host(self):
+        n, nnz, _ = self.info()
+        rp = np.empty(n + 1, dtype=np.int64)
+        col = np.empty(max(nnz, 0), dtype=np.int32)
+        val = np.empty(max(nnz, 0), dtype=np.complex128)
+        check(lib().ed_ccrs_get(self._h, rp.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                col.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _f64p(val.view(np.float64))))
+        return rp, col, val
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and C._LIB is not None:
+            C._LIB.ed_ccrs_free(self._h)
+            self._h = None
+
+
+class ComplexSpinlessFermionHamiltonian:
+    """spinless_fermion_hamiltonian.hpp:52 for T = dcmplx over a momentum
+    sector, as InteractingOflModel drives it (interacting_ofl_model.cpp:
+    952-1135): SetFockBasis, Add_CdC_Terms (diagonal occupation energies),
+    Add_CdCdCC_Terms, LanczosDiagonalize.  The device build runs at the first
+    product or solve; upper storage is the reference's (row in, column out >=
+    in, value <out|H|in>, Hermitian completion in the product), full storage
+    holds the completion explicitly.  Vectors are complex128."""
+
+    def __init__(self):
+        self.m_fockBasis = FermionFockBasis()
+        self.m_crsSparseMatrix = None
+        self._energies = None
+        self._tables = None
+        self._store_upper = False
+        self.m_eigenvalues = None
+        self.m_eigenvectors = None
+        self.last_info = None
+
+    def Initialize(self, nbrParticles: int, nbrOrbitals: int, storageMethod=SPARSE_CRS, mpi=None):
+        self.m_nbrParticles, self.m_nbrOrbitals = int(nbrParticles), int(nbrOrbitals)
+
+    def SetFockBasis(self, basis: FermionFockBasis):
+        self.m_fockBasis = basis
+        self.m_crsSparseMatrix = None
+
+    def Add_CdC_Terms(self, energies, minRow: int = 0, maxRow: int | None = None, mpi=None):
+        """Occupation energies E_k (QuadraticTermTables::GetEkk with k1 = k2,
+        spinless_fermion_hamiltonian.hpp:150-262): an array of K values or an
+        object with m_vTable."""
+        e = np.ascontiguousarray(getattr(energies, "m_vTable", energies), dtype=np.complex128)
+        self._energies = e
+        self.m_crsSparseMatrix = None
+
+    def Add_CdCdCC_Terms(self, termTables: ComplexQuarticTermTables, minRow: int = 0, maxRow: int | None = None,
+                         mpi=None, store_upper: bool = False):
+        self._tables = termTables
+        self._store_upper = bool(store_upper)
+        self.m_crsSparseMatrix = None
+
+    def Build(self):
+        t = self._tables
+        if t is None:
+            raise EDError(C.ED_ERR_ARG, "Add_CdCdCC_Terms first")
+        e = None
+        if self._energies is not None:
+            if self._energies.shape != (t.m_kMax,):
+                raise EDError(C.ED_ERR_ARG, f"{t.m_kMax} occupation energies expected")
+            e = np.ascontiguousarray(self._energies.view(np.float64))
+        vt = np.ascontiguousarray(t.m_vTable.view(np.float64))
+        th = ctypes.c_void_p()
+        check(lib().ed_cterms_create(t.m_kMax, t.dimX, t.dimY, t.m_kTable.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)),
+                                     _f64p(vt), None if e is None else _f64p(e), ctypes.byref(th)))
+        try:
+            h = ctypes.c_void_p()
+            check(lib().ed_cham_build_crs(self.m_fockBasis.handle(), th, int(self._store_upper), None,
+                                          ctypes.byref(h)))
+        finally:
+            lib().ed_cterms_free(th)
+        self.m_crsSparseMatrix = ComplexCrsSparseMatrix(h)
+
+    def GetDimension(self) -> int:
+        return self.m_fockBasis.GetStoredDimension()
+
+    def apply(self, x, y, stream=None):
+        """y = H x on device complex128 vectors (torch tensors or pointers)."""
+        if self.m_crsSparseMatrix is None:
+            self.Build()
+        check(lib().ed_cspmv(self.m_crsSparseMatrix._h, _dptr(x), _dptr(y), stream))
+
+    def LanczosDiagonalize(self, nbrEigenvalues: int, tol: float = 1e-10, v0=None, seed: int = 0, ncv: int = 0,
+                           want_vectors: bool = True, verify: bool = True, max_restarts: int = 0) -> bool:
+        """Lowest eigenpairs (hamiltonian_base.hpp:770-931 with the complex
+        driver); eigenvalues ascending, eigenvectors complex128 (nev, n)."""
+        if self.m_crsSparseMatrix is None:
+            self.Build()
+        n = self.GetDimension()
+        p = LanczosParams(nev=int(nbrEigenvalues), ncv=int(ncv), max_restarts=int(max_restarts or 0), tol=float(tol),
+                          seed=int(seed), want_vectors=int(bool(want_vectors)), verify=int(bool(verify)))
+        info = SolveInfo()
+        ev = np.empty(nbrEigenvalues)
+        vec = np.empty((nbrEigenvalues, n), dtype=np.complex128) if want_vectors else None
+        v0a = None if v0 is None else np.ascontiguousarray(np.asarray(v0, dtype=np.complex128).view(np.float64))
+        st = lib().ed_clanczos(self.m_crsSparseMatrix._h, ctypes.byref(p), None if v0a is None else _f64p(v0a),
+                               _f64p(ev), None if vec is None else _f64p(vec.view(np.float64)), ctypes.byref(info))
+        self.last_info = info.as_dict()
+        self.m_eigenvalues = ev
+        self.m_eigenvectors = vec
+        if st != C.ED_OK:
+            self.last_error = lib().ed_last_error().decode(errors="replace")
+            return False
+        return True
+
+
+class InteractingOflModel:
+    """Sector driver of the interacting optical-flux-lattice model
+    (interacting_ofl_model.cpp:97-105 SetSector, :952-1027 BuildFockBasis,
+    :1034-1060 BuildHamiltonian, :1067-1135 Diagonalize) for the array table
+    format, with the term tables and occupation energies given (the reference
+    computes them from the non-interacting band structure)."""
+
+    def __init__(self, nbrParticles: int, dimX: int, dimY: int, quarticTables: ComplexQuarticTermTables,
+                 energies=None, nbrEigenvalues: int = 1):
+        self.N, self.dimX, self.dimY = int(nbrParticles), int(dimX), int(dimY)
+        self.tables = quarticTables
+        self.energies = None if energies is None else np.asarray(energies, dtype=np.complex128)
+        self.nev = int(nbrEigenvalues)
+        self.kxTot = self.kyTot = 0
+        self.hamiltonian = None
+
+    def SetSector(self, kxSector: int, kySector: int):
+        self.kxTot, self.kyTot = int(kxSector), int(kySector)
+
+    def BuildFockBasis(self) -> bool:
+        basis = FermionFockBasis()
+        empty = basis.GenerateFockSpaceMomentum(self.N, self.dimX, self.dimY, self.kxTot, self.kyTot)
+        self.hamiltonian = ComplexSpinlessFermionHamiltonian()
+        self.hamiltonian.Initialize(self.N, self.dimX * self.dimY)
+        self.hamiltonian.SetFockBasis(basis)
+        return empty
+
+    def BuildHamiltonian(self, store_upper: bool = False):
+        if self.energies is not None:
+            self.hamiltonian.Add_CdC_Terms(self.energies)
+        self.hamiltonian.Add_CdCdCC_Terms(self.tables, store_upper=store_upper)
+        self.hamiltonian.Build()
+
+    def Diagonalize(self, **kw) -> bool:
+        return self.hamiltonian.LanczosDiagonalize(self.nev, **kw)
 
 
 class Observables:

@@ -54,6 +54,9 @@ typedef struct ed_basis ed_basis;   /* FermionFockBasis (basis/fermion_fock_basi
 typedef struct ed_terms ed_terms;   /* QuarticTermTables (fqhe_sphere/.../term_tables.hpp)      */
 typedef struct ed_crs ed_crs;       /* CrsSparseMatrix<double> (utilities/data_structures/crs_sparse_matrix.hpp:123) */
 typedef struct ed_op ed_op;         /* the H*v operator bound into the eigensolver               */
+typedef struct ed_cterms ed_cterms; /* complex QuarticTermTables + QuadraticTermTables of the
+                                       optical-flux-lattice model (interacting_ofl_model/term_tables.hpp) */
+typedef struct ed_ccrs ed_ccrs;     /* CrsSparseMatrix<dcmplx>                                    */
 
 /* ------------------------------------------------------------------ misc */
 int ed_version(void);
@@ -333,6 +336,49 @@ ed_status ed_batch_spmm(const ed_batch* bt, const double* X_dev, double* Y_dev, 
  * Hamiltonian; evecs_dev (may be NULL): nev consecutive [n][nham] arrays. */
 ed_status ed_batch_solve(const ed_batch* bt, const ed_lanczos_params* p, const double* V0_dev, double* evals_host,
                          double* evecs_dev, ed_batch_info* info);
+
+/* ------------------------------------- complex path (optical-flux-lattice model) */
+
+/* Momentum-sector basis: N particles on dimX*dimY orbitals p = kx*dimY + ky
+ * whose total (kx mod dimX, ky mod dimY) is (kxTot, kyTot), words ascending.
+ * Replaces FermionFockBasis::GenerateFockSpace with TestLinearMomentumSector2
+ * (interacting_ofl_model.cpp:994-1001, linear_momentum_constraints_2D.cpp:38-79).
+ * The rank, word and observable entries above accept the handle. */
+ed_status ed_basis_momentum_build(int N, int dimX, int dimY, int kxTot, int kyTot, ed_stream stream,
+                                  ed_basis** out);
+/* Complex term tables in the reference's array layout (QuarticTermTables,
+ * interacting_ofl_model/term_tables.cpp:95-200): ktable and vtable (complex as
+ * re, im pairs) of (norb+1)*norb*norb/2 entries at (t1*norb + t2 -
+ * t1(t1+1)/2)*norb + k, t1 = min(k3,k4), t2 = max(k3,k4); k1 = ktable[.. + k2]
+ * and V(k1,k2,k3,k4) = vtable[.. + (k4 > k3 ? k1 : k2)].  energies: norb
+ * complex occupation energies (QuadraticTermTables::GetEkk, :59-65) or NULL.
+ * The k-table must conserve the 2D momentum (FindK1, interacting_ofl_model.cpp:366-410). */
+ed_status ed_cterms_create(int norb, int dimX, int dimY, const uint16_t* ktable, const double* vtable,
+                           const double* energies, ed_cterms** out);
+ed_status ed_cterms_free(ed_cterms* t);
+/* SpinlessFermionHamiltonian<dcmplx>::Add_CdC_Terms + Add_CdCdCC_Terms
+ * (spinless_fermion_hamiltonian.hpp:150-436) as InteractingOflModel::
+ * BuildHamiltonian calls them (interacting_ofl_model.cpp:1034-1052).  Upper
+ * storage is the reference's: row = in-state, column = out-state >= in-state,
+ * value <out|H|in>; full storage adds each element's conjugate at the mirrored
+ * position.  Bit-exact against the reference's loops. */
+ed_status ed_cham_build_crs(const ed_basis* b, const ed_cterms* t, int store_upper, ed_stream stream,
+                            ed_ccrs** out);
+ed_status ed_ccrs_free(ed_ccrs* a);
+ed_status ed_ccrs_info(const ed_ccrs* a, int64_t* n, int64_t* nnz, int* upper);
+/* Host copies: n+1 row pointers, nnz columns, 2*nnz doubles (re, im). */
+ed_status ed_ccrs_get(const ed_ccrs* a, int64_t* rowptr, int32_t* col, double* val);
+/* y = H x on device complex vectors (re, im pairs) with the reference's
+ * Hermitian completion (SymmetricMatrixVectorMultiply<dcmplx>,
+ * sparse_linear_algebra.hpp:143-164). */
+ed_status ed_cspmv(const ed_ccrs* a, const double* x_dev, double* y_dev, ed_stream stream);
+/* Lowest nev eigenpairs of the complex Hermitian matrix by thick-restart
+ * Lanczos with complex Gram-Schmidt; v0_host (2n doubles) may be NULL,
+ * evecs_host receives nev vectors of n complex entries (re, im pairs).
+ * Replaces ArpackWrapper::DiagonalizeSymmetricMatrix<dcmplx> (znaupd_/
+ * zneupd_, arpack_wrapper.hpp:595-937); values ascending. */
+ed_status ed_clanczos(const ed_ccrs* a, const ed_lanczos_params* p, const double* v0_host, double* evals_host,
+                      double* evecs_host, ed_solve_info* info);
 
 /* ------------------------------------------------- learned warm start K10/K11 */
 

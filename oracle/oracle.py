@@ -497,6 +497,145 @@ def build_upper2(first: np.ndarray, second: np.ndarray, norb0: int, kt0, vt0, kt
     return rowptr, np.array(cols, dtype=np.int32), np.array(vals, dtype=np.float64)
 
 
+# ------------------------------------------- complex momentum path (OFL)
+
+def basis_momentum(N: int, X: int, Y: int, kx: int, ky: int) -> np.ndarray:
+    """FermionFockBasis::GenerateFockSpace with TestLinearMomentumSector2
+    (interacting_ofl_model.cpp:994-1001, linear_momentum_constraints_2D.cpp:38-79):
+    every N-bit word over X*Y orbitals (bit p at kx = p // Y, ky = p % Y) with
+    (sum kx mod X, sum ky mod Y) == (kx, ky), ascending."""
+    from itertools import combinations
+    K = X * Y
+    out = []
+    for c in combinations(range(K), N):
+        if sum(p // Y for p in c) % X == kx and sum(p % Y for p in c) % Y == ky:
+            out.append(sum(1 << p for p in c))
+    return np.array(sorted(out), dtype=np.uint64)
+
+
+def ofl_index(k3: int, k4: int, K: int) -> int:
+    """Triangular (k3, k4) index of the reference's OFL term tables
+    (interacting_ofl_model/term_tables.cpp:108-126)."""
+    t1, t2 = (k3, k4) if k4 > k3 else (k4, k3)
+    return t1 * K + t2 - t1 * (t1 + 1) // 2
+
+
+def ofl_k1(ktab, K: int, k2: int, k3: int, k4: int) -> int:
+    """QuarticTermTables::GetK1 (term_tables.cpp:108-126)."""
+    return int(ktab[ofl_index(k3, k4, K) * K + k2])
+
+
+def ofl_v(vtab, K: int, k1: int, k2: int, k3: int, k4: int) -> complex:
+    """QuarticTermTables::GetVkkkk (term_tables.cpp:157-175): the entry of
+    (min, max)(k3, k4) at k2, or at k1 when k4 > k3."""
+    return complex(vtab[ofl_index(k3, k4, K) * K + (k1 if k4 > k3 else k2)])
+
+
+def ofl_tables(X: int, Y: int, seed: int, scale: float = 1.0):
+    """Seeded momentum-conserving complex tables in the reference's layout:
+    k1 from FindK1's rule (interacting_ofl_model.cpp:366-410: kx1 = kx3 + kx4 -
+    kx2 and ky1 likewise, modulo the grid) and V uniform in the unit square
+    (the Bloch-overlap integrals of BuildTermTables are not restated).  Returns
+    (ktab uint16, vtab complex128), (K+1) K^2 / 2 entries each."""
+    K = X * Y
+    dim = (K + 1) * K * K // 2
+    ktab = np.zeros(dim, dtype=np.uint16)
+    for t1 in range(K):
+        for t2 in range(t1, K):
+            base = ofl_index(t1, t2, K) * K
+            for k2 in range(K):
+                kx = (t1 // Y + t2 // Y - k2 // Y) % X
+                ky = (t1 % Y + t2 % Y - k2 % Y) % Y
+                ktab[base + k2] = kx * Y + ky
+    rng = np.random.default_rng(seed)
+    vtab = scale * (rng.uniform(-1, 1, dim) + 1j * rng.uniform(-1, 1, dim))
+    # the diagonal terms V(k4,k3,k3,k4) and V(k3,k4,k3,k4) read the entries at
+    # k = min(k3,k4) and max(k3,k4): real there, as Hermitian tables have them,
+    # so that the completed operator is Hermitian
+    for t1 in range(K):
+        for t2 in range(t1, K):
+            base = ofl_index(t1, t2, K) * K
+            vtab[base + t1] = vtab[base + t1].real
+            vtab[base + t2] = vtab[base + t2].real
+    return ktab, vtab
+
+
+def build_upper_complex(words: np.ndarray, K: int, ktab, vtab, energies=None):
+    """Upper-triangle complex CRS of SpinlessFermionHamiltonian<dcmplx> in the
+    reference's loop and summation order (spinless_fermion_hamiltonian.hpp:150-436,
+    as InteractingOflModel::BuildHamiltonian calls it, interacting_ofl_model.cpp:
+    1047-1050): Add_CdC_Terms (E_k for every occupied k, ascending) then
+    Add_CdCdCC_Terms (k4 over occupied bits ascending, k3 over the others, k2 over
+    the complement of the higher occupied bits, k1 from the k-table, the occupancy
+    filters, Evaluate_CdCdCC, out >= in); each term kept when abs > 1e-14 and
+    added to entry (row = in, column = out) in arrival order; entries with abs <
+    1e-14 trimmed; columns ascending.  Python loops: small sectors only."""
+    tol = 1e-14
+    n = len(words)
+    ws = [int(w) for w in words]
+    index = {w: i for i, w in enumerate(ws)}
+    mask = (1 << K) - 1
+    rows = [dict() for _ in range(n)]
+    if energies is not None:
+        for i, w in enumerate(ws):
+            t = w
+            while t:
+                lo = t & -t
+                k = lo.bit_length() - 1
+                v = complex(energies[k])
+                if abs(v) > tol:
+                    rows[i][i] = rows[i].get(i, 0j) + v
+                t ^= lo
+    for i, inw in enumerate(ws):
+        t4 = inw
+        while t4:
+            k4o = t4 & -t4
+            k4 = k4o.bit_length() - 1
+            t3 = inw ^ k4o
+            while t3:
+                k3o = t3 & -t3
+                k3 = k3o.bit_length() - 1
+                if k3 != k4:
+                    t2 = mask ^ (t3 ^ k3o)
+                    while t2:
+                        k2o = t2 & -t2
+                        k2 = k2o.bit_length() - 1
+                        k1 = ofl_k1(ktab, K, k2, k3, k4)
+                        k1o = 1 << k1
+                        if ((not (k1o & inw) or (k1o & k3o) or (k1o & k4o)) and
+                                (not (k2o & inw) or (k2o & k3o) or (k2o & k4o)) and not (k1o & k2o)):
+                            out, sign = evaluate_cdcdcc(k1, k2, k3, k4, inw, K)
+                            if sign != 0 and out >= inw:
+                                j = index.get(out)
+                                if j is not None:
+                                    v = float(sign) * ofl_v(vtab, K, k1, k2, k3, k4)
+                                    if abs(v) > tol:
+                                        rows[i][j] = rows[i].get(j, 0j) + v
+                        t2 ^= k2o
+                t3 ^= k3o
+            t4 ^= k4o
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    cols, vals = [], []
+    for i in range(n):
+        kept = sorted((j, v) for j, v in rows[i].items() if not abs(v) < tol)
+        cols.extend(j for j, _ in kept)
+        vals.extend(v for _, v in kept)
+        rowptr[i + 1] = len(cols)
+    return rowptr, np.array(cols, dtype=np.int32), np.array(vals, dtype=np.complex128)
+
+
+def complex_upper_to_full(rowptr, col, val, n):
+    """The reference's Hermitian completion of the upper storage
+    (sparse_linear_algebra.hpp:148-164): M = U + conj(strictly upper U)^T,
+    as CRS with ascending columns."""
+    import scipy.sparse as sp
+    U = sp.csr_matrix((val, col, rowptr), shape=(n, n))
+    S = sp.triu(U, 1)
+    M = (U + S.conj().T).tocsr()
+    M.sort_indices()
+    return M.indptr.astype(np.int64), M.indices.astype(np.int32), M.data.astype(np.complex128)
+
+
 # ------------------------------------------------------------ observables
 
 def density(words: np.ndarray, psi: np.ndarray, norb: int) -> np.ndarray:

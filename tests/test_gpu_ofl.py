@@ -1,0 +1,137 @@
+"""Complex momentum path on the device (optical-flux-lattice model) against
+the oracle's restatement of the momentum basis and of
+SpinlessFermionHamiltonian<dcmplx>: basis words and ranks exact, complex CRS
+bit-exact in upper (the reference's) and full storage, products to 1e-13,
+eigenvalues to 1e-10 of dense spectra, residuals to 1e-9."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import hamiltonian_diagonalization_gb300 as ed
+from hamiltonian_diagonalization_gb300 import _capi
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(3, 3, 4, 0, 0), (4, 3, 4, 1, 2), (5, 3, 4, 2, 3), (6, 4, 4, 0, 1), (5, 4, 5, 3, 2), (4, 4, 6, 1, 5)]
+
+
+def tables(oracle, X, Y, seed):
+    kt, vt = oracle.ofl_tables(X, Y, seed)
+    return ed.ComplexQuarticTermTables(X, Y, kt, vt)
+
+
+def build(N, X, Y, kx, ky, T, energies=None, upper=True):
+    model = ed.InteractingOflModel(N, X, Y, T, energies)
+    model.SetSector(kx, ky)
+    empty = model.BuildFockBasis()
+    if not empty:
+        model.BuildHamiltonian(store_upper=upper)
+    return model, empty
+
+
+@pytest.mark.parametrize("case", CASES + [(2, 1, 3, 0, 2), (7, 4, 5, 3, 4)])
+def test_momentum_basis_and_ranks_exact(cuda, oracle, case):
+    N, X, Y, kx, ky = case
+    B = ed.FermionFockBasis()
+    empty = B.GenerateFockSpaceMomentum(N, X, Y, kx, ky)
+    b = oracle.basis_momentum(N, X, Y, kx, ky)
+    assert empty == (len(b) == 0)
+    assert B.GetStoredDimension() == len(b)
+    if len(b):
+        assert np.array_equal(B.GetFockBasis(), b)
+        idx = B.FindFockStateIndices(b)
+        assert np.array_equal(idx, np.arange(len(b), dtype=np.uint64))
+        assert B.FindFockStateIndex(0, int(b[0]) ^ 1) == _capi.MISS
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_complex_crs_bit_exact(cuda, oracle, case):
+    N, X, Y, kx, ky = case
+    K = X * Y
+    T = tables(oracle, X, Y, K + N)
+    b = oracle.basis_momentum(N, X, Y, kx, ky)
+    e = np.linspace(-0.4, 0.6, K) + 1e-3j * np.arange(K)
+    e[2] = 0.0                                         # a filtered term
+    for energies in (None, e):
+        model, _ = build(N, X, Y, kx, ky, T, energies, upper=True)
+        rp, col, val = model.hamiltonian.m_crsSparseMatrix.to_host()
+        orp, ocol, oval = oracle.build_upper_complex(b, K, T.m_kTable, T.m_vTable, energies)
+        assert np.array_equal(rp, orp)
+        assert np.array_equal(col, ocol)
+        assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+        full, _ = build(N, X, Y, kx, ky, T, energies, upper=False)
+        frp, fcol, fval = full.hamiltonian.m_crsSparseMatrix.to_host()
+        mrp, mcol, mval = oracle.complex_upper_to_full(orp, ocol, oval, len(b))
+        assert np.array_equal(frp, mrp) and np.array_equal(fcol, mcol)
+        assert np.array_equal(fval.view(np.uint64), mval.view(np.uint64))
+
+
+@pytest.mark.parametrize("case", [(5, 3, 4, 2, 3), (5, 4, 5, 3, 2)])
+def test_complex_products(cuda, oracle, case):
+    torch = cuda
+    N, X, Y, kx, ky = case
+    K = X * Y
+    T = tables(oracle, X, Y, 11)
+    b = oracle.basis_momentum(N, X, Y, kx, ky)
+    orp, ocol, oval = oracle.build_upper_complex(b, K, T.m_kTable, T.m_vTable)
+    mrp, mcol, mval = oracle.complex_upper_to_full(orp, ocol, oval, len(b))
+    M = sp.csr_matrix((mval, mcol, mrp), shape=(len(b), len(b)))
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, len(b)) + 1j * rng.uniform(-1, 1, len(b))
+    yref = M @ x
+    scale = np.abs(oval).max() * 50
+    for upper in (True, False):
+        model, _ = build(N, X, Y, kx, ky, T, upper=upper)
+        xd = torch.from_numpy(x.view(np.float64).copy()).cuda()
+        yd = torch.empty_like(xd)
+        model.hamiltonian.apply(xd, yd)
+        torch.cuda.synchronize()
+        y = yd.cpu().numpy().view(np.complex128)
+        assert np.max(np.abs(y - yref)) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("case,nev", [((3, 3, 4, 0, 0), 3), ((5, 3, 4, 2, 3), 4), ((6, 4, 4, 0, 1), 5),
+                                      ((5, 4, 5, 3, 2), 6), ((4, 4, 6, 1, 5), 4)])
+def test_complex_eigenpairs(cuda, oracle, case, nev):
+    N, X, Y, kx, ky = case
+    K = X * Y
+    T = tables(oracle, X, Y, 5)
+    e = np.linspace(-0.2, 0.3, K)
+    b = oracle.basis_momentum(N, X, Y, kx, ky)
+    orp, ocol, oval = oracle.build_upper_complex(b, K, T.m_kTable, T.m_vTable, e)
+    M = sp.csr_matrix(oracle.complex_upper_to_full(orp, ocol, oval, len(b))[::-1], shape=(len(b), len(b)))
+    A = M.toarray()
+    w = np.linalg.eigvalsh(A)[:nev]
+    for upper in (False, True):
+        model, _ = build(N, X, Y, kx, ky, T, e, upper=upper)
+        model.nev = nev
+        assert model.Diagonalize(tol=1e-10, seed=2), model.hamiltonian.last_info
+        H = model.hamiltonian
+        scale = max(1.0, float(np.abs(w).max()))
+        assert np.max(np.abs(H.m_eigenvalues - w)) <= 1e-10 * scale
+        X_ = H.m_eigenvectors
+        assert np.allclose(X_.conj() @ X_.T, np.eye(nev), atol=1e-8)
+        for k in range(nev):
+            assert np.linalg.norm(A @ X_[k] - H.m_eigenvalues[k] * X_[k]) <= 1e-9 * scale
+
+
+def test_lz_build_refuses_a_momentum_basis(cuda):
+    B = ed.FermionFockBasis()
+    B.GenerateFockSpaceMomentum(3, 3, 4, 0, 0)
+    H = ed.SpinlessFermionHamiltonian()
+    H.m_fockBasis = B
+    with pytest.raises(ed.EDError):
+        H.Add_CdCdCC_Terms(ed.QuarticTermTables(12, [0.0, 1.0]))
+
+
+def test_tables_that_break_momentum_are_refused(cuda, oracle):
+    kt, vt = oracle.ofl_tables(3, 4, 1)
+    kt = kt.copy()
+    i = oracle.ofl_index(0, 1, 12) * 12 + 5             # k3 = 0, k4 = 1, k2 = 5
+    kt[i] = (int(kt[i]) + 1) % 12
+    T = ed.ComplexQuarticTermTables(3, 4, kt, vt)
+    model = ed.InteractingOflModel(3, 3, 4, T)
+    model.SetSector(0, 0)
+    model.BuildFockBasis()
+    with pytest.raises(ed.EDError):
+        model.BuildHamiltonian()
