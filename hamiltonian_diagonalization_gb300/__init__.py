@@ -29,5 +29,6 @@ from .host import (  # noqa: F401
     eigensystem_to_file,
     odd_coulomb_list,
     solve_sector,
+    synthetic_ofl_tables,
 )
 

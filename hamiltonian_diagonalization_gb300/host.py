@@ -417,6 +417,35 @@ class ComplexQuarticTermTables:
         return complex(self.m_vTable[self._index(k3, k4) * self.m_kMax + (k1 if k4 > k3 else k2)])
 
 
+def synthetic_ofl_tables(dimX: int, dimY: int, seed: int = 0):
+    """Seeded complex quartic tables with the reference's momentum rule
+    (FindK1, interacting_ofl_model.cpp:366-410: kx1 = kx3 + kx4 - kx2 and ky1
+    likewise, modulo the grid) and values uniform in the unit square, real at
+    the entries the diagonal terms read (Hermitian tables have them real): a
+    stand-in input for benchmarks, since the reference derives the values from
+    its non-interacting band structure."""
+    X, Y = int(dimX), int(dimY)
+    K = X * Y
+    t1 = np.repeat(np.arange(K), K)
+    t2 = np.tile(np.arange(K), K)
+    keep = t2 >= t1
+    t1, t2 = t1[keep], t2[keep]
+    tri = t1 * K + t2 - t1 * (t1 + 1) // 2
+    order = np.argsort(tri)
+    t1, t2 = t1[order], t2[order]
+    k2 = np.arange(K)
+    kx = (t1[:, None] // Y + t2[:, None] // Y - k2[None, :] // Y) % X
+    ky = (t1[:, None] % Y + t2[:, None] % Y - k2[None, :] % Y) % Y
+    ktab = (kx * Y + ky).astype(np.uint16).ravel()
+    rng = np.random.default_rng(seed)
+    dim = len(ktab)
+    vtab = rng.uniform(-1, 1, dim) + 1j * rng.uniform(-1, 1, dim)
+    rows = np.arange(len(t1)) * K
+    vtab[rows + t1] = vtab[rows + t1].real
+    vtab[rows + t2] = vtab[rows + t2].real
+    return ComplexQuarticTermTables(X, Y, ktab, vtab)
+
+
 class ComplexCrsSparseMatrix:
     """Device CRS of complex values (CrsSparseMatrix<dcmplx>)."""
 

@@ -26,7 +26,10 @@ With --two-level the sector is N,norb0,twoLz of the two-Landau-level model
 pseudopotential lists of those sizes for the two levels' tables, second-level
 occupation energy 1.0): it times the basis, the CRS build, the product and
 the --nev lowest eigenpairs with and without the degeneracy passes (with
---build, the basis and the CRS build only).
+--build, the basis and the CRS build only).  With --ofl N,dimX,dimY,kxTot,kyTot
+it does the same for a complex optical-flux-lattice momentum sector built from
+seeded synthetic tables (synthetic_ofl_tables) and occupation energies
+linspace(-0.5, 0.5).
 """
 from __future__ import annotations
 
@@ -52,6 +55,7 @@ def main():
     ap.add_argument("--observables", action="store_true",
                     help="time the eigenvector observables on a seeded unit vector of the sector")
     ap.add_argument("--two-level", action="store_true", help="two-Landau-level sector N,norb0,twoLz")
+    ap.add_argument("--ofl", default="", help="N,dimX,dimY,kxTot,kyTot: complex optical-flux-lattice sector")
     ap.add_argument("--nev", type=int, default=4, help="two-level: eigenpairs to solve for")
     args = ap.parse_args()
     import torch
@@ -61,6 +65,8 @@ def main():
 
     if args.rotate:
         return rotate_main(C, torch, args)
+    if args.ofl:
+        return ofl_main(ed, torch, args)
     N, norb, tlz = (int(x) for x in args.sector.split(","))
     if args.batch:
         return batch_main(ed, C, torch, N, norb, tlz, args)
@@ -181,6 +187,55 @@ def two_level_main(ed, C, torch, N, norb0, tlz, args):
                                         "eigenvalues": [float(v) for v in H.m_eigenvalues],
                                         "matvecs": H.last_info["matvecs"],
                                         "max_residual": H.last_info["max_residual"]}
+    print(json.dumps(res))
+
+
+def ofl_main(ed, torch, args):
+    import time
+    N, X, Y, kx, ky = (int(v) for v in args.ofl.split(","))
+    T = ed.synthetic_ofl_tables(X, Y, 1)
+    e = np.linspace(-0.5, 0.5, X * Y)
+    res = {"ofl": [N, X, Y, kx, ky], "mode": "complex", "layout": "upper" if args.upper else "full"}
+    tb, tc = [], []
+    for i in range(args.warmup + args.reps):
+        model = ed.InteractingOflModel(N, X, Y, T, e, nbrEigenvalues=args.nev)
+        model.SetSector(kx, ky)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        model.BuildFockBasis()
+        torch.cuda.synchronize()
+        b = time.perf_counter()
+        model.BuildHamiltonian(store_upper=args.upper)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            tb.append(b - a)
+            tc.append(time.perf_counter() - b)
+    H = model.hamiltonian
+    n, nnz = H.GetDimension(), H.m_crsSparseMatrix.GetNbrNonZeros()
+    res.update({"n": n, "nnz": nnz, "ms_basis": 1e3 * min(tb), "ms_build": 1e3 * min(tc)})
+    if args.build:
+        print(json.dumps(res))
+        return
+    x = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, 2 * n)).cuda()
+    y = torch.empty_like(x)
+    for _ in range(3):
+        H.apply(x, y)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(20):
+        H.apply(x, y)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / 20
+    by = nnz * 20 + (n + 1) * 8 + 2 * n * 16
+    res.update({"ms_per_product": ms, "GBps": by / ms / 1e6})
+    model.Diagonalize(tol=1e-10, seed=1, want_vectors=False)
+    t = time.perf_counter()
+    ok = model.Diagonalize(tol=1e-10, seed=1, want_vectors=False)
+    res["solve"] = {"ok": bool(ok), "s": time.perf_counter() - t, "eigenvalues": [float(v) for v in H.m_eigenvalues],
+                    "matvecs": H.last_info["matvecs"], "restarts": H.last_info["restarts"],
+                    "spmv_s": H.last_info["spmv_seconds"], "max_residual": H.last_info["max_residual"]}
     print(json.dumps(res))
 
 
