@@ -24,6 +24,7 @@
 #include <complex>
 #include <cstdint>
 #include <functional>
+#include <utility>
 #include <iostream>
 #include <stdexcept>
 #include <string>
@@ -133,7 +134,32 @@ class FermionFockBasis {
     FermionFockBasis() = default;
     FermionFockBasis(const FermionFockBasis&) = delete;
     FermionFockBasis& operator=(const FermionFockBasis&) = delete;
+    FermionFockBasis(FermionFockBasis&& o) noexcept : m_basisStored(o.m_basisStored), m_h(o.m_h) { o.m_h = nullptr; }
+    FermionFockBasis& operator=(FermionFockBasis&& o) noexcept
+    {
+        if (this != &o) {
+            if (m_h) ed_basis_free(m_h);
+            m_h = o.m_h;
+            m_basisStored = o.m_basisStored;
+            o.m_h = nullptr;
+        }
+        return *this;
+    }
     ~FermionFockBasis() { if (m_h) ed_basis_free(m_h); }
+
+    // the optical-flux-lattice momentum sector: GenerateFockSpace with
+    // TestLinearMomentumSector2 (interacting_ofl_model.cpp:994-1001); true when empty
+    bool GenerateFockSpaceMomentum(iSize_t nbrParticles, iSize_t dimX, iSize_t dimY, iSize_t kxTot, iSize_t kyTot,
+                                   utilities::MpiWrapper& mpi)
+    {
+        if (m_h) ed_basis_free(m_h);
+        m_h = nullptr;
+        utilities::EdCheck(ed_basis_momentum_build((int)nbrParticles, (int)dimX, (int)dimY, (int)kxTot, (int)kyTot,
+                                                   nullptr, &m_h),
+                           &mpi);
+        m_basisStored = true;
+        return GetStoredDimension() == 0;
+    }
 
     // fermion_fock_basis.cpp:241: returns true when the sector is empty
     bool GenerateFockSpace(iSize_t nbrParticles, iSize_t nbrOrbitals, int twoLz, utilities::MpiWrapper& mpi)
@@ -606,6 +632,161 @@ class TwoLevelSpinlessFermionHamiltonian {
     bool m_storeUpper = false;
     bool m_passesSet = false;
     ed_crs* m_crs = nullptr;
+};
+
+// interacting_ofl_model/term_tables.hpp QuarticTermTables (array format):
+// (K+1) K^2 / 2 k1 values and complex V values at (t1*K + t2 - t1(t1+1)/2)*K
+// + k, t1 = min(k3,k4), t2 = max(k3,k4) (term_tables.cpp:95-200).
+class OflQuarticTermTables {
+  public:
+    void Initialize(iSize_t dimX, iSize_t dimY, const utilities::MpiWrapper&)
+    {
+        m_dimX = dimX;
+        m_dimY = dimY;
+        m_kMax = dimX * dimY;
+        const size_t dim = (size_t)(m_kMax + 1) * m_kMax * m_kMax / 2;
+        m_kTable.assign(dim, 0);
+        m_vTable.assign(dim, std::complex<double>(0.0, 0.0));
+    }
+    std::vector<kState_t>* GetKTable() { return &m_kTable; }
+    std::vector<std::complex<double>>* GetVTable() { return &m_vTable; }
+    void GetK1(kState_t* buf, iSize_t& nbrK1, kState_t k2, kState_t k3, kState_t k4) const
+    {
+        nbrK1 = 1;
+        buf[0] = m_kTable[(size_t)Tri(k3, k4) * m_kMax + k2];
+    }
+    std::complex<double> GetVkkkk(kState_t k1, kState_t k2, kState_t k3, kState_t k4) const
+    {
+        return m_vTable[(size_t)Tri(k3, k4) * m_kMax + (k4 > k3 ? k1 : k2)];
+    }
+    iSize_t m_dimX = 0, m_dimY = 0, m_kMax = 0;
+
+  private:
+    size_t Tri(kState_t k3, kState_t k4) const
+    {
+        const size_t t1 = k4 > k3 ? k3 : k4, t2 = k4 > k3 ? k4 : k3;
+        return t1 * m_kMax + t2 - t1 * (t1 + 1) / 2;
+    }
+    std::vector<kState_t> m_kTable;
+    std::vector<std::complex<double>> m_vTable;
+};
+
+// interacting_ofl_model/term_tables.hpp QuadraticTermTables: one complex
+// occupation energy per orbital (GetEkk, term_tables.cpp:59-65).
+class OflQuadraticTermTables {
+  public:
+    void Initialize(iSize_t nbrOrbitals, const utilities::MpiWrapper&)
+    {
+        m_vTable.assign(nbrOrbitals, std::complex<double>(0.0, 0.0));
+    }
+    std::vector<std::complex<double>>* GetVTable() { return &m_vTable; }
+    const std::vector<std::complex<double>>* GetVTable() const { return &m_vTable; }
+    iSize_t GetDimension() const { return (iSize_t)m_vTable.size(); }
+
+  private:
+    std::vector<std::complex<double>> m_vTable;
+};
+
+// spinless_fermion_hamiltonian.hpp:52 for T = dcmplx, as InteractingOflModel
+// drives it (interacting_ofl_model.cpp:952-1135): SetFockBasis (a momentum
+// sector), Add_CdC_Terms, Add_CdCdCC_Terms, LanczosDiagonalize.  The device
+// build runs at the first solve; vectors are std::complex<double>.
+template <>
+class SpinlessFermionHamiltonian<std::complex<double>> {
+  public:
+    SpinlessFermionHamiltonian() = default;
+    SpinlessFermionHamiltonian(const SpinlessFermionHamiltonian&) = delete;
+    SpinlessFermionHamiltonian& operator=(const SpinlessFermionHamiltonian&) = delete;
+    ~SpinlessFermionHamiltonian() { Clear(); }
+
+    void Initialize(iSize_t nbrParticles, iSize_t nbrOrbitals, utilities::storageMethod_t storageMethod,
+                    utilities::MpiWrapper&)
+    {
+        m_nbrParticles = nbrParticles;
+        m_nbrOrbitals = nbrOrbitals;
+        m_storageMethod = storageMethod;
+    }
+    void SetFockBasis(FermionFockBasis&& basis)
+    {
+        m_fockBasis = std::move(basis);
+        Clear();
+    }
+    void Add_CdC_Terms(OflQuadraticTermTables* tables, fock_t /*minRow*/, fock_t /*maxRow*/, utilities::MpiWrapper&)
+    {
+        m_energies = *tables->GetVTable();
+        Clear();
+    }
+    void Add_CdCdCC_Terms(OflQuarticTermTables* tables, fock_t /*minRow*/, fock_t /*maxRow*/, utilities::MpiWrapper&,
+                          bool storeUpper = false)
+    {
+        m_tables = tables;
+        m_storeUpper = storeUpper;
+        Clear();
+    }
+    void Build(utilities::MpiWrapper& mpi)
+    {
+        Clear();
+        if (!m_tables) throw utilities::EdError(ED_ERR_ARG, "Add_CdCdCC_Terms first");
+        ed_cterms* t = nullptr;
+        const double* e = m_energies.empty() ? nullptr : reinterpret_cast<const double*>(m_energies.data());
+        utilities::EdCheck(ed_cterms_create((int)m_tables->m_kMax, (int)m_tables->m_dimX, (int)m_tables->m_dimY,
+                                            m_tables->GetKTable()->data(),
+                                            reinterpret_cast<const double*>(m_tables->GetVTable()->data()), e, &t),
+                           &mpi);
+        const ed_status s = ed_cham_build_crs(m_fockBasis.handle(), t, m_storeUpper ? 1 : 0, nullptr, &m_crs);
+        ed_cterms_free(t);
+        utilities::EdCheck(s, &mpi);
+    }
+    fock_t GetFockSpaceDimension() const { return m_fockBasis.GetStoredDimension(); }
+    int64_t GetNbrNonZeros() const
+    {
+        int64_t nnz = 0;
+        if (m_crs) utilities::EdCheck(ed_ccrs_info(m_crs, nullptr, &nnz, nullptr));
+        return nnz;
+    }
+    // hamiltonian_base.hpp:770 with the complex driver; eigenvalues ascending
+    bool LanczosDiagonalize(iSize_t nbrEigenvalues, utilities::MpiWrapper& mpi, double tol = 1e-10,
+                            bool wantVectors = true)
+    {
+        if (!m_crs) Build(mpi);
+        const fock_t n = GetFockSpaceDimension();
+        m_eigenvalues.assign(nbrEigenvalues, 0.0);
+        m_eigenvectors.assign(wantVectors ? (size_t)n * nbrEigenvalues : 0, std::complex<double>(0.0, 0.0));
+        ed_lanczos_params p{};
+        p.nev = (int)nbrEigenvalues;
+        p.tol = tol;
+        p.verify = 1;
+        p.want_vectors = wantVectors;
+        const ed_status s = ed_clanczos(m_crs, &p, nullptr, m_eigenvalues.data(),
+                                        wantVectors ? reinterpret_cast<double*>(m_eigenvectors.data()) : nullptr,
+                                        &m_info);
+        if (s != ED_OK) {
+            std::cerr << "\n\tERROR in LanczosDiagonalize: " << ed_status_string(s) << ": " << ed_last_error()
+                      << std::endl;
+            mpi.m_exitFlag = true;
+            return false;
+        }
+        return true;
+    }
+    void Clear()
+    {
+        if (m_crs) ed_ccrs_free(m_crs);
+        m_crs = nullptr;
+    }
+    const ed_solve_info& LastInfo() const { return m_info; }
+
+    FermionFockBasis m_fockBasis;
+    std::vector<double> m_eigenvalues;
+    std::vector<std::complex<double>> m_eigenvectors;   // nev vectors of n entries
+
+  private:
+    iSize_t m_nbrParticles = 0, m_nbrOrbitals = 0;
+    utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
+    std::vector<std::complex<double>> m_energies;
+    OflQuarticTermTables* m_tables = nullptr;
+    bool m_storeUpper = false;
+    ed_ccrs* m_crs = nullptr;
+    ed_solve_info m_info{};
 };
 
 // observables/fermion_observables.hpp:39, for the eigenvectors of a real

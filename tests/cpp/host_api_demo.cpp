@@ -2,8 +2,10 @@
 // way the reference's model layer drives them for one sector:
 // tables -> basis -> Add_CdCdCC_Terms -> LanczosDiagonalize, plus the
 // std::function product path of ArpackWrapper, the ground state's
-// observables, and a two-level sector (N=4, norb0=6, Lz=0) as
-// SphereTwoLevelPseudopotentialModel builds it.  Prints one JSON line.
+// observables, a two-level sector (N=4, norb0=6, Lz=0) as
+// SphereTwoLevelPseudopotentialModel builds it, and a complex momentum sector
+// (N=4 on a 3x4 grid, momentum (1,2)) as InteractingOflModel builds it.
+// Prints one JSON line.
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -110,6 +112,41 @@ int main(int argc, char** argv)
                 H.m_arpackWrapper.LastInfo().max_residual, ok3 ? "true" : "false", rank2_ok ? "true" : "false",
                 (unsigned long long)dim2, (long long)H2.GetNbrNonZeros());
     for (int i = 0; i < 4; ++i) std::printf("%s%.17g", i ? ", " : "", H2.m_eigenvalues[i]);
+    std::printf("]}");
+
+    // complex momentum sector: tables with FindK1's momentum rule and
+    // exactly representable values, real where the diagonal terms read them
+    const int X = 3, Y = 4, K = X * Y;
+    diagonalization::OflQuarticTermTables oq;
+    oq.Initialize(X, Y, mpi);
+    for (int t1 = 0; t1 < K; ++t1)
+        for (int t2 = t1; t2 < K; ++t2) {
+            const size_t base = (size_t)(t1 * K + t2 - t1 * (t1 + 1) / 2) * K;
+            for (int k2 = 0; k2 < K; ++k2) {
+                const int kx = ((t1 / Y + t2 / Y - k2 / Y) % X + X) % X;
+                const int ky = ((t1 % Y + t2 % Y - k2 % Y) % Y + Y) % Y;
+                (*oq.GetKTable())[base + k2] = (diagonalization::kState_t)(kx * Y + ky);
+                const size_t i = base + k2;
+                const double re = (double)((i * 7919) % 1000) / 500.0 - 1.0;
+                const double im = (k2 == t1 || k2 == t2) ? 0.0 : (double)((i * 104729) % 1000) / 500.0 - 1.0;
+                (*oq.GetVTable())[i] = std::complex<double>(re, im);
+            }
+        }
+    diagonalization::OflQuadraticTermTables oe;
+    oe.Initialize(K, mpi);
+    for (int k = 0; k < K; ++k) (*oe.GetVTable())[k] = std::complex<double>(0.125 * k, 0.0);
+    diagonalization::FermionFockBasis mb;
+    mb.GenerateFockSpaceMomentum(4, X, Y, 1, 2, mpi);
+    diagonalization::SpinlessFermionHamiltonian<std::complex<double>> Hc;
+    Hc.Initialize(4, K, utilities::_SPARSE_MAPPED_, mpi);
+    Hc.SetFockBasis(std::move(mb));
+    const diagonalization::fock_t dimc = Hc.GetFockSpaceDimension();
+    Hc.Add_CdC_Terms(&oe, 0, dimc, mpi);
+    Hc.Add_CdCdCC_Terms(&oq, 0, dimc, mpi);
+    const bool ok4 = Hc.LanczosDiagonalize(3, mpi, 1e-10);
+    std::printf(", \"ofl\": {\"ok\": %s, \"dim\": %llu, \"nnz\": %lld, \"eigenvalues\": [", ok4 ? "true" : "false",
+                (unsigned long long)dimc, (long long)Hc.GetNbrNonZeros());
+    for (int i = 0; i < 3; ++i) std::printf("%s%.17g", i ? ", " : "", Hc.m_eigenvalues[i]);
     std::printf("]}}\n");
-    return (ok && ok2 && rank_ok && ok3 && rank2_ok) ? 0 : 1;
+    return (ok && ok2 && rank_ok && ok3 && rank2_ok && ok4) ? 0 : 1;
 }

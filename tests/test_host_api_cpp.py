@@ -55,3 +55,26 @@ def test_host_classes_solve_sector(cuda, oracle, tmp_path):
     ref2 = np.linalg.eigvalsh(sp.csr_matrix((fv, fc, fr), shape=(len(f), len(f))).toarray())[:4]
     assert t["dim"] == len(f) and t["nnz"] == len(fv)
     assert np.max(np.abs(np.array(t["eigenvalues"]) - ref2)) < 1e-10 * max(1.0, np.abs(ref2).max())
+    # the complex momentum sector through SpinlessFermionHamiltonian<std::complex<double>>
+    c = r["ofl"]
+    assert c["ok"]
+    X, Y = 3, 4
+    K = X * Y
+    kt, _ = oracle.ofl_tables(X, Y, 0)
+    i = np.arange(len(kt))
+    k2 = i % K
+    t1 = np.empty(len(kt), dtype=np.int64)
+    t2 = np.empty(len(kt), dtype=np.int64)
+    for a in range(K):
+        for bb in range(a, K):
+            base = oracle.ofl_index(a, bb, K) * K
+            t1[base:base + K], t2[base:base + K] = a, bb
+    re = ((i * 7919) % 1000) / 500.0 - 1.0
+    im = np.where((k2 == t1) | (k2 == t2), 0.0, ((i * 104729) % 1000) / 500.0 - 1.0)
+    vt = re + 1j * im
+    b = oracle.basis_momentum(4, X, Y, 1, 2)
+    u = oracle.build_upper_complex(b, K, kt, vt, 0.125 * np.arange(K) + 0j)
+    fr, fc, fv = oracle.complex_upper_to_full(*u, len(b))
+    ref3 = np.linalg.eigvalsh(sp.csr_matrix((fv, fc, fr), shape=(len(b), len(b))).toarray())[:3]
+    assert c["dim"] == len(b) and c["nnz"] == len(fv)
+    assert np.max(np.abs(np.array(c["eigenvalues"]) - ref3)) < 1e-10 * max(1.0, np.abs(ref3).max())
