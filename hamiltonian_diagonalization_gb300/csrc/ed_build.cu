@@ -676,12 +676,19 @@ __device__ __forceinline__ double2 cdiag_element(const CView& v, uint64_t in)
 
 // Weight of the hop (a,b) -> (c,d) of class P as stored in row `in`: the
 // upper element (d > b) or the conjugate of the mirrored upper one.
+// Negation as a sign-bit flip on the integer pipe (the FP64 pipe is the
+// scarce one on this part); identical to IEEE negation for every input.
+__device__ __forceinline__ double flip_sign(double x)
+{
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+
 __device__ __forceinline__ double2 chop_weight(const CView& v, int P, int ia, int ic, int cnt, bool upper_el)
 {
     const int o = __ldg(v.w_off + P);
     if (upper_el) return __ldg(v.w + o + ia * cnt + ic);
     const double2 r = __ldg(v.w + o + ic * cnt + ia);
-    return make_double2(r.x, -r.y);
+    return make_double2(r.x, flip_sign(r.y));
 }
 
 __global__ void k_cdiag(const uint64_t* __restrict__ words, int64_t n, CView v, double2* __restrict__ diag)
@@ -775,7 +782,7 @@ __global__ void __launch_bounds__(256) k_cfill(const uint64_t* __restrict__ word
                 if (upper && d < b) continue;
                 double2 w = chop_weight(v, P, ia, ic, m, d > b);
                 if (czero(w)) continue;
-                if (hop_parity(in, a, b, c, d)) w = make_double2(-w.x, -w.y);
+                if (hop_parity(in, a, b, c, d)) w = make_double2(flip_sign(w.x), flip_sign(w.y));
                 const uint64_t out = rest | (1ull << c) | (1ull << d);
                 const uint64_t rk = rank_in_sector(out, hi, lo_tab, L);
                 if (rk == kMiss) atomicOr(err, 2);

@@ -151,13 +151,27 @@ __device__ __forceinline__ void cchunk(int64_t n, int nb, int b, int64_t& r0, in
     if (r0 > n) r0 = n;
 }
 
-// part[(i*nb + b)*2 + {0,1}] = block b's share of V_i^H w (complex), i < J.
+// part[(i*nb + b)*2 + {0,1}] = block b's share of V_i^H w (complex), i < J,
+// and part[(J*nb + b)*2] its share of ||w||^2.
 __global__ void __launch_bounds__(kCThreads) k_cdots(const double2* __restrict__ V, int J, const double2* __restrict__ w,
                                                      int64_t n, double* __restrict__ part)
 {
     __shared__ double red[kCThreads / 32];
     int64_t r0, r1;
     cchunk(n, gridDim.x, blockIdx.x, r0, r1);
+    {
+        double s = 0.0;
+        for (int64_t r = r0 + threadIdx.x; r < r1; r += kCThreads) {
+            const double2 b = w[r];
+            s = fma(b.x, b.x, s);
+            s = fma(b.y, b.y, s);
+        }
+        s = cblock_sum(s, red);
+        if (threadIdx.x == 0) {
+            part[((int64_t)J * gridDim.x + blockIdx.x) * 2] = s;
+            part[((int64_t)J * gridDim.x + blockIdx.x) * 2 + 1] = 0.0;
+        }
+    }
     for (int i = 0; i < J; ++i) {
         const double2* vi = V + (int64_t)i * n;
         double re = 0.0, im = 0.0;
@@ -266,16 +280,21 @@ struct CWork {
 };
 
 // Orthogonalise w against V[0..J) twice (complex); returns the summed
-// coefficients V_i^H w of both passes.
-std::vector<cplx> cgram_schmidt(CWork& cw, const double2* V, int J, double2* w, cudaStream_t st)
+// coefficients V_i^H w of both passes.  norm_in: ||w|| before the passes;
+// norm_out: ||w|| after them, from the second pass's dots (Pythagoras: w
+// loses exactly V c of norm |c| to an orthonormal V), so a step needs two
+// host round trips.
+std::vector<cplx> cgram_schmidt(CWork& cw, const double2* V, int J, double2* w, cudaStream_t st,
+                                double* norm_in = nullptr, double* norm_out = nullptr)
 {
     std::vector<cplx> acc(J, cplx(0.0, 0.0));
-    if (J == 0) return acc;
     for (int pass = 0; pass < 2; ++pass) {
         k_cdots<<<cw.nb, kCThreads, 0, st>>>(V, J, w, cw.n, cw.part.p);
         count_launch();
         ED_CUDA(cudaGetLastError());
-        const std::vector<double> h = host_parts(cw.part, (size_t)J * cw.nb * 2, st);
+        const std::vector<double> h = host_parts(cw.part, (size_t)(J + 1) * cw.nb * 2, st);
+        double nn = 0.0;
+        for (int b = 0; b < cw.nb; ++b) nn += h[((size_t)J * cw.nb + b) * 2];
         std::vector<double> c(2 * (size_t)J);
         for (int i = 0; i < J; ++i) {
             double re = 0.0, im = 0.0;
@@ -287,6 +306,13 @@ std::vector<cplx> cgram_schmidt(CWork& cw, const double2* V, int J, double2* w, 
             c[2 * i + 1] = im;
             acc[i] += cplx(re, im);
         }
+        if (pass == 0 && norm_in) *norm_in = std::sqrt(nn);
+        if (pass == 1 && norm_out) {
+            double removed = 0.0;
+            for (int i = 0; i < J; ++i) removed += c[2 * i] * c[2 * i] + c[2 * i + 1] * c[2 * i + 1];
+            *norm_out = std::sqrt(std::max(0.0, nn - removed));
+        }
+        if (J == 0) break;
         ED_CUDA(cudaMemcpyAsync(cw.c.p, c.data(), c.size() * 8, cudaMemcpyHostToDevice, st));
         k_cupdate<<<csms() * 4, kCThreads, 0, st>>>(V, J, reinterpret_cast<const double2*>(cw.c.p), w, cw.n);
         count_launch();
@@ -585,16 +611,17 @@ void clanczos_solve(const ed_ccrs& a, const ed_lanczos_params& p, const double* 
             cspmv(a, reinterpret_cast<const double*>(vj), reinterpret_cast<double*>(w), st);
             ED_CUDA(cudaEventRecord(e1, st));
             ++inf.matvecs;
-            const double hnorm = cnorm(cw, w, st);
+            double hnorm = 0.0, b = 0.0;
+            const std::vector<cplx> c = cgram_schmidt(cw, col(Vb, 0), j + 1, w, st, &hnorm, &b);
             float ms = 0.f;
             ED_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             spmv_ms += ms;
-            const std::vector<cplx> c = cgram_schmidt(cw, col(Vb, 0), j + 1, w, st);
             for (int i = 0; i <= j; ++i) {
                 T[(size_t)i * m + j] = c[i].real();
                 T[(size_t)j * m + i] = c[i].real();
             }
-            double b = cnorm(cw, w, st);
+            // below 1e-6 of ||H v|| the Pythagorean norm loses digits: measure it
+            if (b < 1e-6 * hnorm) b = cnorm(cw, w, st);
             if (!(b > 1e-13 * std::max(1.0, hnorm))) {
                 // invariant subspace: continue from a fresh direction
                 ++inf.breakdowns;
