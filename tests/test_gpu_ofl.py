@@ -12,7 +12,9 @@ from hamiltonian_diagonalization_gb300 import _capi
 
 pytestmark = pytest.mark.gpu
 
-CASES = [(3, 3, 4, 0, 0), (4, 3, 4, 1, 2), (5, 3, 4, 2, 3), (6, 4, 4, 0, 1), (5, 4, 5, 3, 2), (4, 4, 6, 1, 5)]
+# grids down to one column or row, and the 40-orbital limit (5 x 8)
+CASES = [(3, 3, 4, 0, 0), (4, 3, 4, 1, 2), (5, 3, 4, 2, 3), (6, 4, 4, 0, 1), (5, 4, 5, 3, 2), (4, 4, 6, 1, 5),
+         (4, 1, 9, 0, 4), (3, 8, 1, 5, 0), (3, 5, 8, 2, 5)]
 
 
 def tables(oracle, X, Y, seed):
