@@ -217,12 +217,12 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
     } else if (!a.upper) {
         // rows of 24-96 elements (two-level sectors, small one-level ones):
         // four lanes per row with four loads ahead, or eight lanes per row
-        // once x passes about 20 MB (measured on GB300: two-level N=7 sectors
-        // of 1.3-2.0M rows 4.3-4.5 TB/s with four lanes, 3.5-3.6 with eight;
-        // N=8 sectors of 2.9-5.9M rows 3.8-4.1 TB/s with eight, 2.9-3.0 with
-        // four)
+        // with three ahead once x passes about 20 MB (measured on GB300:
+        // two-level N=7 sectors of 1.3-2.0M rows 4.3-4.6 TB/s with four lanes,
+        // 3.5-3.7 with eight; N=8 sectors of 4.2-5.9M rows 4.3-4.4 TB/s with
+        // eight and three ahead, 4.1 with four ahead, 2.9-3.0 with four lanes)
         if (avg >= 24 && a.n >= 2500000)
-            k_spmv_full<8, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+            k_spmv_full<8, 3><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
         else if (avg >= 24) k_spmv_full<4, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
         else k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else {
