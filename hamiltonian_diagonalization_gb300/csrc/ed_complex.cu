@@ -17,7 +17,8 @@
 // basis, the real projected matrix (alpha and beta of a Hermitian operator
 // are real) solved on the host, restart rotations of the complex basis by the
 // real Ritz coefficients.  It replaces ArpackWrapper's complex driver
-// (arpack_wrapper.hpp, znaupd_/zneupd_ with WHICH "SR").
+// (the T = dcmplx branches of arpack_wrapper.hpp:255-937, znaupd_/zneupd_
+// with WHICH "SR").
 #include <algorithm>
 #include <chrono>
 #include <cmath>

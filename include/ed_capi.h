@@ -376,7 +376,7 @@ ed_status ed_cspmv(const ed_ccrs* a, const double* x_dev, double* y_dev, ed_stre
  * Lanczos with complex Gram-Schmidt; v0_host (2n doubles) may be NULL,
  * evecs_host receives nev vectors of n complex entries (re, im pairs).
  * Replaces ArpackWrapper::DiagonalizeSymmetricMatrix<dcmplx> (znaupd_/
- * zneupd_, arpack_wrapper.hpp:595-937); values ascending. */
+ * zneupd_ branches, arpack_wrapper.hpp:255-937); values ascending. */
 ed_status ed_clanczos(const ed_ccrs* a, const ed_lanczos_params* p, const double* v0_host, double* evals_host,
                       double* evecs_host, ed_solve_info* info);
 
