@@ -623,20 +623,28 @@ class Observables:
             raise EDError(C.ED_ERR_ARG, "eigenvectors not calculated")
         if not 0 <= eigenvectorIndex < len(vecs):
             raise EDError(C.ED_ERR_ARG, "eigenvectorIndex out of range")
-        return hamiltonian.m_fockBasis, np.ascontiguousarray(vecs[eigenvectorIndex], dtype=np.float64)
+        v = np.asarray(vecs[eigenvectorIndex])
+        return hamiltonian.m_fockBasis, v if np.iscomplexobj(v) else np.ascontiguousarray(v, dtype=np.float64)
+
+    @staticmethod
+    def _magnitude(psi) -> np.ndarray:
+        """The observables depend on |psi| only: complex eigenvectors (the
+        optical-flux-lattice model's) enter through their moduli."""
+        psi = np.asarray(psi)
+        return np.ascontiguousarray(np.abs(psi) if np.iscomplexobj(psi) else psi, dtype=np.float64)
 
     @staticmethod
     def density_of_vector(basis, psi) -> np.ndarray:
-        """rho[k] = sum_s psi_s^2 n_k(s) (fermion_observables.hpp:48-104)."""
-        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        """rho[k] = sum_s |psi_s|^2 n_k(s) (fermion_observables.hpp:48-104)."""
+        psi = Observables._magnitude(psi)
         rho = np.empty(basis.nbrOrbitals)
         check(lib().ed_obs_density(basis.handle(), _f64p(psi), _f64p(rho)))
         return rho
 
     @staticmethod
     def density_density_of_vector(basis, psi) -> np.ndarray:
-        """D[k, q] = sum_s psi_s^2 n_k(s) n_q(s) (fermion_observables.hpp:117-200)."""
-        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        """D[k, q] = sum_s |psi_s|^2 n_k(s) n_q(s) (fermion_observables.hpp:117-200)."""
+        psi = Observables._magnitude(psi)
         K = basis.nbrOrbitals
         t = np.empty(K * K)
         check(lib().ed_obs_density_density(basis.handle(), _f64p(psi), _f64p(t)))
@@ -645,7 +653,7 @@ class Observables:
     @staticmethod
     def participation_ratio_of_vector(basis, psi) -> float:
         """1 / sum_s |psi_s|^4 (fermion_observables.hpp:528-562)."""
-        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        psi = Observables._magnitude(psi)
         r = ctypes.c_double()
         check(lib().ed_obs_participation_ratio(basis.handle(), _f64p(psi), ctypes.byref(r)))
         return float(r.value)
@@ -653,8 +661,10 @@ class Observables:
     @staticmethod
     def most_probable_of_vector(basis, psi, nbrStates: int):
         """The nbrStates largest |psi_s| with their Fock words, descending
-        (fermion_observables.hpp:437-517)."""
-        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        (fermion_observables.hpp:437-517); complex psi gives its complex
+        amplitudes."""
+        original = np.asarray(psi)
+        psi = Observables._magnitude(original)
         k = max(int(nbrStates), 0)
         states = np.empty(max(k, 1), dtype=np.uint64)
         amps = np.empty(max(k, 1))
@@ -663,6 +673,9 @@ class Observables:
                                          states.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _f64p(amps),
                                          ctypes.byref(cnt)))
         m = int(cnt.value)
+        if np.iscomplexobj(original) and m:
+            idx = basis.FindFockStateIndices(states[:m]).astype(np.int64)
+            return states[:m].copy(), original[idx].astype(np.complex128)
         return states[:m].copy(), amps[:m].copy()
 
     # the reference's call shapes (the MpiWrapper argument is accepted and ignored)

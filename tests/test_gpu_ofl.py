@@ -137,3 +137,29 @@ def test_tables_that_break_momentum_are_refused(cuda, oracle):
     model.BuildFockBasis()
     with pytest.raises(ed.EDError):
         model.BuildHamiltonian()
+
+
+def test_observables_of_complex_eigenvectors(cuda, oracle):
+    """fermion_observables.hpp on the model's complex eigenvectors: density,
+    density-density and participation ratio from |psi|, the most probable
+    states with their complex amplitudes."""
+    N, X, Y, kx, ky = 5, 4, 5, 3, 2
+    T = tables(oracle, X, Y, 5)
+    model, _ = build(N, X, Y, kx, ky, T, upper=False)
+    model.nev = 2
+    assert model.Diagonalize(tol=1e-10, seed=2)
+    H = model.hamiltonian
+    words = H.m_fockBasis.GetFockBasis()
+    psi = H.m_eigenvectors[0]
+    assert np.iscomplexobj(psi) and np.abs(psi.imag).max() > 1e-3
+    obs = ed.Observables()
+    K = X * Y
+    mag = np.abs(psi)
+    assert np.allclose(obs.DensityFunction(H, 0), oracle.density(words, mag, K), atol=1e-13)
+    assert np.allclose(obs.DensityDensityFunction(H, 0), oracle.density_density(words, mag, K), atol=1e-13)
+    assert abs(obs.GetParticipationRatio(H, 0) - oracle.participation_ratio(mag)) <= 1e-10 * len(words)
+    states, amps = ed.Observables.most_probable_of_vector(H.m_fockBasis, psi, 10)
+    ostates, _ = oracle.most_probable(words, mag, 10)
+    assert np.array_equal(states, ostates)
+    idx = np.searchsorted(words, states)
+    assert np.array_equal(amps, psi[idx])
