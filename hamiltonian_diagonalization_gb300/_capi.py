@@ -110,6 +110,8 @@ _SIGS = {
     "ed_op_free": (c_int, [c_void_p]),
     "ed_op_dim": (c_int, [c_void_p, P(c_i64)]),
     "ed_lanczos": (c_int, [c_void_p, P(LanczosParams), P(c_double), P(c_double), P(c_double), P(SolveInfo)]),
+    "ed_lanczos_two_level": (c_int, [c_void_p, c_void_p, P(LanczosParams), P(c_double), P(c_double), P(c_double),
+                                     P(SolveInfo)]),
     "ed_lanczos_device": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(SolveInfo)]),
     "ed_residuals": (c_int, [c_void_p, c_void_p, P(c_double), c_int, P(c_double)]),
     "ed_residuals_noalloc": (c_int, [c_void_p, c_void_p, P(c_double), c_int, P(c_double)]),

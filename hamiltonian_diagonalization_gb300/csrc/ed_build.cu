@@ -618,6 +618,39 @@ __global__ void __launch_bounds__(256) k_fill2(
     }
 }
 
+// Level-exchange ladder of the two-level basis: y += T x with T = L0- L1+
+// (dir > 0: one level-0 particle one orbital down, one level-1 particle one
+// up, total Lz unchanged) or its adjoint T^+ = L0+ L1- (dir < 0), the
+// angular-momentum ladder coefficients sqrt((S+m)(S-m+1)) of each level; a
+// particle moving to a neighbouring empty orbital passes nobody, so no sign.
+// The levels do not mix, so T commutes with the two-level Hamiltonian.
+__global__ void k_ladder2(const uint64_t* __restrict__ words, int64_t n, int K0, int K1, int dir,
+                          const uint64_t* __restrict__ hi, const uint64_t* __restrict__ lo_tab, int L,
+                          const double* __restrict__ x, double* __restrict__ y)
+{
+    const uint64_t m1 = (1ull << K1) - 1ull;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const double xr = x[r];
+        if (xr == 0.0) continue;
+        const uint64_t w = words[r], first = w >> K1, second = w & m1;
+        for (uint64_t ti = first; ti; ti &= ti - 1) {
+            const int i = __ffsll((long long)ti) - 1, i2 = dir > 0 ? i - 1 : i + 1;
+            if (i2 < 0 || i2 >= K0 || ((first >> i2) & 1ull)) continue;
+            const double c0 = dir > 0 ? sqrt((double)i * (double)(K0 - i)) : sqrt((double)(i + 1) * (double)(K0 - 1 - i));
+            const uint64_t f2 = first ^ (1ull << i) ^ (1ull << i2);
+            for (uint64_t tj = second; tj; tj &= tj - 1) {
+                const int j = __ffsll((long long)tj) - 1, j2 = dir > 0 ? j + 1 : j - 1;
+                if (j2 < 0 || j2 >= K1 || ((second >> j2) & 1ull)) continue;
+                const double c1 =
+                    dir > 0 ? sqrt((double)(K1 - 1 - j) * (double)(j + 1)) : sqrt((double)j * (double)(K1 - j));
+                const uint64_t out = (f2 << K1) | (second ^ (1ull << j) ^ (1ull << j2));
+                const uint64_t rk = rank_in_sector(out, hi, lo_tab, L);
+                if (rk != kMiss) atomicAdd(y + rk, c0 * c1 * xr);
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Complex momentum-conserving build: SpinlessFermionHamiltonian<dcmplx>
 // Add_CdC_Terms / Add_CdCdCC_Terms (spinless_fermion_hamiltonian.hpp:150-436)
@@ -1122,6 +1155,17 @@ void cham_build_crs(const ed_basis& b, const ed_cterms& t, int upper, ed_ccrs& a
     ED_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     ED_CUDA(cudaStreamSynchronize(st));
     ED_REQUIRE(herr == 0, ED_ERR_INTERNAL, "complex fill: row count or rank check failed on the device");
+}
+
+void two_level_ladder(const ed_basis& b, const double* x, double* y, int dir, cudaStream_t st)
+{
+    ED_REQUIRE(b.levels == 2, ED_ERR_ARG, "the level-exchange ladder takes a two-level basis");
+    const int64_t n = (int64_t)b.dim;
+    if (n == 0) return;
+    ED_CUDA(cudaMemsetAsync(y, 0, (size_t)n * 8, st));
+    k_ladder2<<<sm_count() * 8, 256, 0, st>>>(b.words.p, n, b.norb0, b.norb1, dir, b.hi.p, b.lo.p, b.low_bits, x, y);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
 }
 
 }  // namespace edgb

@@ -477,6 +477,30 @@ ed_status ed_lanczos_device(const ed_op* op, const ed_lanczos_params* p, const d
     });
 }
 
+ed_status ed_lanczos_two_level(const ed_basis* b, const ed_op* op, const ed_lanczos_params* p, const double* v0_host,
+                               double* evals_host, double* evecs_host, ed_solve_info* info)
+{
+    return guarded([&] {
+        ED_NONNULL(b);
+        ED_NONNULL(op);
+        ED_NONNULL(p);
+        ED_NONNULL(evals_host);
+        if (info) std::memset(info, 0, sizeof(*info));
+        const int64_t n = op->n;
+        ED_REQUIRE(n >= 1, ED_ERR_EMPTY, "operator has dimension 0");
+        ED_REQUIRE(p->nev >= 1 && p->nev <= n, ED_ERR_ARG, "need 1 <= nev <= n");
+        DevBuf<double> v0, ev;
+        if (v0_host) {
+            v0.alloc(n);
+            ED_CUDA(cudaMemcpy(v0.p, v0_host, (size_t)n * 8, cudaMemcpyHostToDevice));
+        }
+        if (evecs_host) ev.alloc((size_t)n * p->nev);
+        lanczos_solve_two_level(*b, *op, *p, v0.p, evals_host, ev.p, info, nullptr);
+        if (evecs_host)
+            ED_CUDA(cudaMemcpy(evecs_host, ev.p, (size_t)n * p->nev * 8, cudaMemcpyDeviceToHost));
+    });
+}
+
 ed_status ed_lanczos(const ed_op* op, const ed_lanczos_params* p, const double* v0_host, double* evals_host,
                      double* evecs_host, ed_solve_info* info)
 {

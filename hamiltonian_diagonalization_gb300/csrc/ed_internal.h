@@ -234,6 +234,7 @@ struct ed_ccrs {
 
 // ----------------------------------------------------- device-side entry points
 namespace edgb {
+void two_level_ladder(const ed_basis& b, const double* x, double* y, int dir, cudaStream_t st);
 void cterms_derive(ed_cterms& t);
 void cham_build_crs(const ed_basis& b, const ed_cterms& t, int upper, ed_ccrs& a, cudaStream_t st);
 void cspmv(const ed_ccrs& a, const double* x, double* y, cudaStream_t st);

@@ -375,6 +375,12 @@ __global__ void __launch_bounds__(kThreads) k_lock_axpy(double* __restrict__ y, 
     }
 }
 
+__global__ void __launch_bounds__(kThreads) k_mul(double* __restrict__ v, int64_t n, double s)
+{
+    for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kThreads)
+        v[r] *= s;
+}
+
 }  // namespace
 
 // -------------------------------------------------------------- operator
@@ -918,6 +924,171 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
         total.converged = nc;
     }
     ED_CUDA(cudaStreamSynchronize(st));
+    total.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (info) *info = total;
+}
+
+// Two-level solve: one Krylov sequence, then the copies of each degenerate
+// eigenvalue from the level-exchange ladder T = L0- L1+ and its adjoint,
+// which commute with the Hamiltonian (the levels do not mix) and map a
+// multiplet state |L0 m0>|L1 m1> to its neighbours in m0 at fixed total Lz.
+// For the found vectors in ascending order, each chain T^k x (both
+// directions) is orthogonalised against the vectors kept so far and kept when
+// something of it is left, until nev vectors are kept; those are then checked
+// by their true residuals (after a Rayleigh-Ritz step on their span if
+// needed).  The chain divides by ||T x||, which magnifies the Ritz vectors'
+// error components, so a failed check repeats the sequence two digits past
+// the target from the found vectors; should that fail too (a degeneracy the
+// ladder does not generate), the deflated passes take over.
+void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczos_params& p, const double* v0_dev,
+                             double* evals_host, double* evecs_dev, ed_solve_info* info, cudaStream_t caller)
+{
+    ED_REQUIRE(b.levels == 2 && (int64_t)b.dim == op.n, ED_ERR_ARG, "the ladder solve takes the operator's two-level basis");
+    const int64_t n = op.n;
+    const int nev = p.nev;
+    if (n < 60 || n <= (int64_t)nev + 2) {   // the dense path sees every copy
+        lanczos_once(op, p, v0_dev, evals_host, evecs_dev, info, caller);
+        return;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const double tol = p.tol > 0 ? p.tol : 1e-10;
+    ed_lanczos_params q = p;
+    q.verify = 0;
+    q.degeneracy_passes = 0;
+    DevBuf<double> X((size_t)n * nev);
+    std::vector<double> theta(nev);
+    ed_solve_info total, part;
+    std::memset(&total, 0, sizeof(total));
+    std::memset(&part, 0, sizeof(part));
+    SolveStream ss(caller);
+    cudaStream_t st = ss.s;
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 2, n / 2048));
+    DevBuf<double> A((size_t)n * nev), cur(n), u(n), v0w(n), lpart((size_t)nev * (nb + 1)), dpart(2 * (size_t)nb);
+    DevBuf<unsigned int> counter(1);
+    ED_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), st));
+    std::vector<double> lam;
+    int acc = 0;
+    auto norm = [&](const double* v) {
+        k_dot2<<<nb, kThreads, 0, st>>>(v, v, n, dpart.p);
+        ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
+        return std::sqrt(host_sum_parts(dpart.p, nb, st));
+    };
+    auto mul = [&](double* v, double sc) {
+        k_mul<<<sm_count() * 4, kThreads, 0, st>>>(v, n, sc);
+        ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
+    };
+    auto orth = [&](double* v) {
+        for (int pass = 0; pass < 2 && acc > 0; ++pass) {
+            k_lock_dots<<<nb, kThreads, 0, st>>>(A.p, acc, v, n, -1.0, lpart.p, counter.p);
+            ::edgb::count_launch();
+            k_lock_axpy<<<nb, kThreads, 0, st>>>(v, A.p, acc, lpart.p + (int64_t)acc * nb, n);
+            ::edgb::count_launch();
+            ED_CUDA(cudaGetLastError());
+        }
+    };
+    auto try_keep = [&](const double* v, double value) {
+        ED_CUDA(cudaMemcpyAsync(u.p, v, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        const double n0 = norm(u.p);
+        if (!(n0 > 0.0)) return;
+        orth(u.p);
+        const double n1 = norm(u.p);
+        if (!(n1 > 1e-6 * n0)) return;
+        mul(u.p, 1.0 / n1);
+        ED_CUDA(cudaMemcpyAsync(A.p + (int64_t)acc * n, u.p, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        lam.push_back(value);
+        ++acc;
+    };
+    const double lscale = (double)b.norb0 * b.norb1;   // the ladder's norm is below K0*K1/4
+    std::vector<double> res(nev, 0.0);
+    bool ok = false;
+    for (int attempt = 0; attempt < 2 && !ok; ++attempt) {
+        const double* v0a = v0_dev;
+        q.tol = attempt == 0 ? tol : tol * 1e-2;
+        if (attempt == 1) {
+            // start from the sum of the first attempt's vectors
+            std::vector<double> ones(nev, 1.0);
+            ED_CUDA(cudaMemsetAsync(v0w.p, 0, (size_t)n * 8, st));
+            ED_CUDA(cudaMemcpyAsync(lpart.p, ones.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
+            k_lock_axpy<<<nb, kThreads, 0, st>>>(v0w.p, X.p, nev, lpart.p, n);
+            ::edgb::count_launch();
+            ED_CUDA(cudaGetLastError());
+            v0a = v0w.p;
+        }
+        ED_CUDA(cudaStreamSynchronize(st));
+        lanczos_once(op, q, v0a, theta.data(), X.p, &part, caller);
+        add_info(total, part);
+        acc = 0;
+        lam.clear();
+        for (int k = 0; k < nev && acc < nev; ++k) {
+            const double* xk = X.p + (int64_t)k * n;
+            try_keep(xk, theta[k]);
+            for (int dir = 1; dir >= -1 && acc < nev; dir -= 2) {
+                ED_CUDA(cudaMemcpyAsync(cur.p, xk, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+                for (int step = 0; step < b.norb0 + b.norb1 && acc < nev; ++step) {
+                    two_level_ladder(b, cur.p, u.p, dir, st);
+                    const double nt = norm(u.p);
+                    if (!(nt > 1e-8 * lscale)) break;               // the end of the multiplet
+                    std::swap(cur.p, u.p);
+                    mul(cur.p, 1.0 / nt);
+                    try_keep(cur.p, theta[k]);
+                }
+            }
+        }
+        if (acc != nev) continue;
+        residual_norms(op, A.p, lam.data(), nev, res.data(), st);
+        total.matvecs += nev;
+        ok = *std::max_element(res.begin(), res.end()) <= tol;
+        if (ok) break;
+        // Rayleigh-Ritz on the kept span: P = A^T H A, A <- A Y
+        DevBuf<double> HA((size_t)n * nev), Ar((size_t)n * nev);
+        for (int i = 0; i < nev; ++i) op_apply(op, A.p + (int64_t)i * n, HA.p + (int64_t)i * n, st);
+        total.matvecs += nev;
+        std::vector<double> P((size_t)nev * nev);
+        for (int j = 0; j < nev; ++j) {
+            k_lock_dots<<<nb, kThreads, 0, st>>>(A.p, nev, HA.p + (int64_t)j * n, n, 1.0, lpart.p, counter.p);
+            ::edgb::count_launch();
+            ED_CUDA(cudaGetLastError());
+            std::vector<double> c(nev);
+            ED_CUDA(cudaMemcpyAsync(c.data(), lpart.p + (int64_t)nev * nb, (size_t)nev * 8, cudaMemcpyDeviceToHost, st));
+            ED_CUDA(cudaStreamSynchronize(st));
+            for (int i = 0; i < nev; ++i) P[(size_t)i * nev + j] = c[i];
+        }
+        for (int i = 0; i < nev; ++i)
+            for (int j = 0; j < i; ++j) {
+                const double a = 0.5 * (P[(size_t)i * nev + j] + P[(size_t)j * nev + i]);
+                P[(size_t)i * nev + j] = P[(size_t)j * nev + i] = a;
+            }
+        std::vector<double> ev, Y;
+        sym_eigen(nev, P, ev, Y);
+        RotateScratch rot;
+        rotate_basis(A.p, n, nev, Y.data(), nev, nev, Ar.p, rot, 0, st);
+        std::swap(A.p, Ar.p);
+        lam.assign(ev.begin(), ev.end());
+        residual_norms(op, A.p, lam.data(), nev, res.data(), st);
+        total.matvecs += nev;
+        ok = *std::max_element(res.begin(), res.end()) <= tol;
+    }
+    if (!ok) {
+        // a degeneracy the ladder does not generate: the deflated passes
+        ed_lanczos_params r = p;
+        if (r.degeneracy_passes <= 0) r.degeneracy_passes = nev;
+        ed_solve_info pi;
+        ED_CUDA(cudaStreamSynchronize(st));
+        lanczos_solve(op, r, v0_dev, evals_host, evecs_dev, &pi, caller);
+        add_info(total, pi);
+        total.converged = pi.converged;
+        total.max_residual = pi.max_residual;
+        total.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (info) *info = total;
+        return;
+    }
+    for (int i = 0; i < nev; ++i) evals_host[i] = lam[i];
+    if (evecs_dev) ED_CUDA(cudaMemcpyAsync(evecs_dev, A.p, (size_t)n * nev * 8, cudaMemcpyDeviceToDevice, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    total.converged = nev;
+    total.max_residual = *std::max_element(res.begin(), res.end());
     total.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (info) *info = total;
 }

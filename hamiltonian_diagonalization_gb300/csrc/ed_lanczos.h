@@ -90,4 +90,8 @@ void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st);
 void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
                    double* evecs_dev, ed_solve_info* info, cudaStream_t st);
 void residual_norms(const ed_op& op, const double* x, const double* lambda, int k, double* res, cudaStream_t st);
+// Lowest p.nev eigenpairs of a two-level Hamiltonian, every copy of a
+// degenerate eigenvalue from the level-exchange ladder of basis b.
+void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczos_params& p, const double* v0_dev,
+                             double* evals_host, double* evecs_dev, ed_solve_info* info, cudaStream_t caller);
 }  // namespace edgb

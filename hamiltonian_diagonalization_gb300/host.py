@@ -883,14 +883,43 @@ class TwoLevelSpinlessFermionHamiltonian(SpinlessFermionHamiltonian):
             self.Build()
         return super().operator_handle()
 
-    def LanczosDiagonalize(self, nbrEigenvalues: int, **kw):
-        """As the one-level solve, with degeneracy passes on by default: the
+    def LanczosDiagonalize(self, nbrEigenvalues: int, tol: float = 1e-10, v0=None, seed: int = 0, ncv: int = 0,
+                           want_vectors: bool = True, verify: bool = True, max_restarts: int = 0,
+                           degeneracy_passes: int | None = None):
+        """Lowest eigenpairs with every copy of a degenerate eigenvalue: the
         levels do not mix, so every pair of level-0 and level-1 multiplets
-        (L0, L1) gives 2 min(L0, L1) + 1 states of one energy in a sector."""
+        (L0, L1) gives 2 min(L0, L1) + 1 states of one energy in a sector.  By
+        default the copies come from the level-exchange ladder
+        (ed_lanczos_two_level); degeneracy_passes = k uses k deflated passes
+        instead, 0 the plain single-sequence solve."""
         if self.m_crsSparseMatrix is None:
             self.Build()
-        kw.setdefault("degeneracy_passes", int(nbrEigenvalues))
-        return super().LanczosDiagonalize(nbrEigenvalues, **kw)
+        if degeneracy_passes is not None:
+            return super().LanczosDiagonalize(nbrEigenvalues, tol=tol, v0=v0, seed=seed, ncv=ncv,
+                                              want_vectors=want_vectors, verify=verify, max_restarts=max_restarts,
+                                              degeneracy_passes=degeneracy_passes)
+        n = self.GetDimension()
+        op = self.operator_handle()
+        try:
+            p = LanczosParams(nev=int(nbrEigenvalues), ncv=int(ncv), max_restarts=int(max_restarts or 0),
+                              tol=float(tol), seed=int(seed), want_vectors=int(bool(want_vectors)),
+                              verify=int(bool(verify)))
+            info = SolveInfo()
+            ev = np.empty(nbrEigenvalues)
+            vec = np.empty((nbrEigenvalues, n)) if want_vectors else None
+            v0a = None if v0 is None else np.ascontiguousarray(v0, dtype=np.float64)
+            st = lib().ed_lanczos_two_level(self.m_fockBasis.handle(), op, ctypes.byref(p),
+                                            None if v0a is None else _f64p(v0a), _f64p(ev),
+                                            None if vec is None else _f64p(vec), ctypes.byref(info))
+        finally:
+            lib().ed_op_free(op)
+        self.last_info = info.as_dict()
+        self.m_eigenvalues = ev
+        self.m_eigenvectors = vec
+        if st != C.ED_OK:
+            self.last_error = lib().ed_last_error().decode(errors="replace")
+            return False
+        return True
 
 
 class SphereTwoLevelPseudopotentialModel:

@@ -228,6 +228,18 @@ typedef struct {
 ed_status ed_lanczos(const ed_op* op, const ed_lanczos_params* p, const double* v0_host,
                      double* evals_host, double* evecs_host, ed_solve_info* info);
 
+/* Two-level Hamiltonian (ed_ham2_build_crs on basis b): one Krylov sequence,
+ * then every copy of each degenerate eigenvalue from the level-exchange
+ * ladder L0- L1+ and its adjoint, which commute with H (the levels do not
+ * mix: eigenvalues E0(L0) + E1(L1) repeat 2 min(L0, L1) + 1 times); the kept
+ * vectors are checked by their residuals (a Rayleigh-Ritz step if needed, the
+ * degeneracy passes as the last resort).  Same arguments as ed_lanczos;
+ * replaces LanczosDiagonalize for TwoLevelSpinlessFermionHamiltonian
+ * (hamiltonian_base.hpp:770-931), whose ARPACK call returns copies only as
+ * rounding lets it. */
+ed_status ed_lanczos_two_level(const ed_basis* b, const ed_op* op, const ed_lanczos_params* p,
+                               const double* v0_host, double* evals_host, double* evecs_host, ed_solve_info* info);
+
 /* Same solve with device-resident start vector and outputs (n doubles /
  * n*nev doubles, column-major).  Either output may be NULL. */
 ed_status ed_lanczos_device(const ed_op* op, const ed_lanczos_params* p, const double* v0_dev,

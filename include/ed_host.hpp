@@ -576,9 +576,9 @@ class TwoLevelSpinlessFermionHamiltonian {
         utilities::EdCheck(ed_spmv(m_crs, x_dev, y_dev, nullptr));
     }
     // hamiltonian_base.hpp:770.  The levels do not mix, so a sector's
-    // eigenvalues E0(L0) + E1(L1) repeat 2 min(L0, L1) + 1 times: the solve
-    // runs nbrEigenvalues degeneracy passes unless SetDegeneracyPasses was
-    // called on m_arpackWrapper with another count.
+    // eigenvalues E0(L0) + E1(L1) repeat 2 min(L0, L1) + 1 times: every copy
+    // comes from the level-exchange ladder (ed_lanczos_two_level), or from
+    // deflated passes after SetDegeneracyPasses(k) (k = 0: one sequence).
     bool LanczosDiagonalize(iSize_t nbrEigenvalues, utilities::MpiWrapper& mpi, double tol = 1e-10,
                             bool wantVectors = true)
     {
@@ -587,11 +587,27 @@ class TwoLevelSpinlessFermionHamiltonian {
         m_eigenvalues.assign(nbrEigenvalues, 0.0);
         m_eigenvectors.assign(wantVectors ? (size_t)n * nbrEigenvalues : 0, 0.0);
         m_arpackWrapper.SetTolerance(tol);
-        if (!m_passesSet) m_arpackWrapper.SetDegeneracyPasses((int)nbrEigenvalues);
         ed_op* op = nullptr;
         utilities::EdCheck(ed_op_from_crs(m_crs, &op), &mpi);
-        const bool ok = m_arpackWrapper.DiagonalizeOperator(op, wantVectors ? m_eigenvectors.data() : nullptr,
-                                                            m_eigenvalues.data(), (int)n, (int)nbrEigenvalues, mpi);
+        bool ok = true;
+        if (m_passesSet) {
+            ok = m_arpackWrapper.DiagonalizeOperator(op, wantVectors ? m_eigenvectors.data() : nullptr,
+                                                     m_eigenvalues.data(), (int)n, (int)nbrEigenvalues, mpi);
+        } else {
+            ed_lanczos_params p{};
+            p.nev = (int)nbrEigenvalues;
+            p.tol = tol;
+            p.verify = 1;
+            p.want_vectors = wantVectors;
+            const ed_status s = ed_lanczos_two_level(m_fockBasis.handle(), op, &p, nullptr, m_eigenvalues.data(),
+                                                     wantVectors ? m_eigenvectors.data() : nullptr, &m_info);
+            if (s != ED_OK) {
+                std::cerr << "\n\tERROR in LanczosDiagonalize: " << ed_status_string(s) << ": " << ed_last_error()
+                          << std::endl;
+                mpi.m_exitFlag = true;
+                ok = false;
+            }
+        }
         ed_op_free(op);
         return ok;
     }
@@ -632,6 +648,7 @@ class TwoLevelSpinlessFermionHamiltonian {
     bool m_storeUpper = false;
     bool m_passesSet = false;
     ed_crs* m_crs = nullptr;
+    ed_solve_info m_info{};
 };
 
 // interacting_ofl_model/term_tables.hpp QuarticTermTables (array format):

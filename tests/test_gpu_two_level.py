@@ -124,8 +124,11 @@ def test_lowest_eigenvalues_with_degenerate_copies(cuda, oracle, case, nev):
     assert H.LanczosDiagonalize(nev, tol=1e-10, seed=3, degeneracy_passes=0)
     scale = max(1.0, float(np.max(np.abs(w))))
     single = H.m_eigenvalues.copy()
-    assert H.LanczosDiagonalize(nev, tol=1e-10, seed=3)            # passes on by default here
     assert np.max(np.abs(single - w)) > 1e-6                       # one sequence misses copies
+    assert H.LanczosDiagonalize(nev, tol=1e-10, seed=3, degeneracy_passes=nev), H.last_info
+    passes = H.m_eigenvalues.copy()
+    assert np.max(np.abs(passes - w)) <= 1e-10 * max(1.0, float(np.max(np.abs(w))))
+    assert H.LanczosDiagonalize(nev, tol=1e-10, seed=3), H.last_info   # the ladder, by default
     assert np.max(np.abs(H.m_eigenvalues - w)) <= 1e-10 * scale
     X = np.asarray(H.m_eigenvectors)
     assert np.allclose(X @ X.T, np.eye(nev), atol=1e-8)
