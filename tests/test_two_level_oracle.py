@@ -23,3 +23,38 @@ def test_sectors_partition_the_space(oracle, N, norb0):
             assert all(bin(int(a)).count("1") + bin(int(b)).count("1") == N for a, b in zip(f, s))
     assert sum(dims.values()) == total
     assert all(dims[t] == dims[-t] for t in dims)
+
+
+@pytest.mark.parametrize("N,norb0,tlz", [(4, 6, 0), (5, 7, 0), (6, 9, 0)])
+def test_level_exchange_ladder_commutes_with_h(oracle, N, norb0, tlz):
+    """T = L0- L1+ (one level-0 particle an orbital down, one level-1 particle
+    an orbital up, coefficients sqrt(i (K0 - i)) and sqrt((K1 - 1 - j)(j + 1)),
+    no fermionic sign for a move to a neighbouring orbital) maps the sector to
+    itself and commutes with the two-level Hamiltonian: the symmetry the
+    device solve uses to generate degenerate copies."""
+    import scipy.sparse as sp
+    n1 = norb0 + 2
+    f, s = oracle.basis2(N, norb0, tlz)
+    kt0, vt0 = oracle.quartic_tables(norb0, oracle.odd_coulomb_list(norb0))
+    kt1, vt1 = oracle.quartic_tables(n1, np.random.default_rng(norb0).uniform(-1, 2, n1 - 1))
+    u = oracle.build_upper2(f, s, norb0, kt0, vt0, kt1, vt1, None, np.full(n1, 0.4))
+    fr, fc, fv = oracle.upper_to_full(*u, len(f))
+    H = sp.csr_matrix((fv, fc, fr), shape=(len(f), len(f)))
+    index = {(int(a), int(b)): i for i, (a, b) in enumerate(zip(f, s))}
+    rows, cols, vals = [], [], []
+    for r, (a, b) in enumerate(zip(f, s)):
+        a, b = int(a), int(b)
+        for i in range(1, norb0):
+            if not (a >> i) & 1 or (a >> (i - 1)) & 1:
+                continue
+            for j in range(n1 - 1):
+                if not (b >> j) & 1 or (b >> (j + 1)) & 1:
+                    continue
+                k = index[(a ^ (1 << i) ^ (1 << (i - 1)), b ^ (1 << j) ^ (1 << (j + 1)))]
+                rows.append(k)
+                cols.append(r)
+                vals.append(np.sqrt(i * (norb0 - i)) * np.sqrt((n1 - 1 - j) * (j + 1)))
+    T = sp.csr_matrix((vals, (rows, cols)), shape=(len(f), len(f)))
+    assert T.nnz > 0
+    C = H @ T - T @ H
+    assert abs(C).max() <= 1e-12 * abs(H).max() * abs(T).max()
