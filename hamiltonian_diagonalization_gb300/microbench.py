@@ -58,6 +58,7 @@ def main():
     ap.add_argument("--two-level", action="store_true", help="two-Landau-level sector N,norb0,twoLz")
     ap.add_argument("--ofl", default="", help="N,dimX,dimY,kxTot,kyTot: complex optical-flux-lattice sector")
     ap.add_argument("--nev", type=int, default=4, help="two-level: eigenpairs to solve for")
+    ap.add_argument("--products-only", action="store_true", help="two-level / complex: stop after the products")
     args = ap.parse_args()
     import torch
 
@@ -180,6 +181,9 @@ def two_level_main(ed, C, torch, N, norb0, tlz, args):
     ms = a.elapsed_time(b) / 20
     by = nnz * 12 + (n + 1) * 8 + 2 * n * 8
     res.update({"ms_per_product": ms, "GBps": by / ms / 1e6})
+    if args.products_only:
+        print(json.dumps(res))
+        return
     for name, passes in (("single", 0), ("passes", args.nev), ("ladder", None)):
         H.LanczosDiagonalize(args.nev, tol=1e-10, seed=1, degeneracy_passes=passes, want_vectors=False)
         t = time.perf_counter()
@@ -230,6 +234,9 @@ def ofl_main(ed, torch, args):
     ms = a.elapsed_time(b) / 20
     by = nnz * 20 + (n + 1) * 8 + 2 * n * 16
     res.update({"ms_per_product": ms, "GBps": by / ms / 1e6})
+    if args.products_only:
+        print(json.dumps(res))
+        return
     model.Diagonalize(tol=1e-10, seed=1, want_vectors=False)
     t = time.perf_counter()
     ok = model.Diagonalize(tol=1e-10, seed=1, want_vectors=False)
