@@ -163,3 +163,18 @@ def test_observables_of_complex_eigenvectors(cuda, oracle):
     assert np.array_equal(states, ostates)
     idx = np.searchsorted(words, states)
     assert np.array_equal(amps, psi[idx])
+
+
+def test_empty_momentum_sector(cuda, oracle):
+    """A sector with no states: N=3 on a 1x3 grid has one word, whose ky sum
+    0+1+2 is 0 mod 3, so the sector ky = 1 is empty.  Building works and the
+    solve reports an empty operator."""
+    kt, vt = oracle.ofl_tables(1, 3, 0)
+    T = ed.ComplexQuarticTermTables(1, 3, kt, vt)
+    model = ed.InteractingOflModel(3, 1, 3, T)
+    model.SetSector(0, 1)
+    assert model.BuildFockBasis() is True
+    model.BuildHamiltonian()
+    assert model.hamiltonian.m_crsSparseMatrix.GetNbrRows() == 0
+    assert model.Diagonalize() is False
+    assert "dimension 0" in model.hamiltonian.last_error

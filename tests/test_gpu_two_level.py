@@ -144,3 +144,19 @@ def test_mixed_level_terms_refused(cuda, oracle):
         H.Add_CdCdCC_Terms(ed.QuarticTermTables(5, oracle.odd_coulomb_list(5)), 0, 1, 0, 1)
     with pytest.raises(ed.EDError):
         H.Add_CdC_Terms(np.zeros(5), 0, 2)
+
+
+def test_ladder_solve_refuses_a_one_level_basis(cuda, oracle):
+    import ctypes
+    one = ed.SpinlessFermionHamiltonian()
+    one.Initialize(4, 10, twoLz=0)
+    one.Add_CdCdCC_Terms(ed.QuarticTermTables(10, oracle.odd_coulomb_list(10)))
+    op = one.operator_handle()
+    try:
+        p = ed.LanczosParams(nev=2, tol=1e-10)
+        ev = np.empty(2)
+        st = ed.lib().ed_lanczos_two_level(one.m_fockBasis.handle(), op, ctypes.byref(p), None,
+                                           ev.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None, None)
+        assert st == _capi.ED_ERR_ARG
+    finally:
+        ed.lib().ed_op_free(op)
