@@ -388,6 +388,204 @@ void or_build_upper_fill(const uint64_t *basis, uint64_t n, int norb, const uint
     }
 }
 
+/* --------------------------------------------------------- two Landau levels */
+
+static int or_cmp_u64(const void *x, const void *y)
+{
+    uint64_t a = *(const uint64_t *)x, b = *(const uint64_t *)y;
+    return (a > b) - (a < b);
+}
+
+/* TwoLevelFermionFockBasis::GenerateFockSpace with TestAngularMomentumSector2LL
+ * (two_level_fermion_fock_basis.cpp:289-470, two_level_angular_momentum_constraint.hpp:41-70)
+ * as combined words (first << K1) | second, K1 = K0 + 2, ascending (the
+ * reference's (first, second) order): for every split n0 + n1 = N, every
+ * lowest-level word (weight of bit i: i + 1) paired with every second-level
+ * word (weight of bit j: j) whose weights sum to S = (2Lz + N(K1 - 1)) / 2.
+ * With out == NULL only counts. */
+uint64_t or_basis2_build(int N, int K0, int twoLz, uint64_t *out)
+{
+    const int K1 = K0 + 2;
+    const int64_t t = (int64_t)twoLz + (int64_t)N * (K1 - 1);
+    if (t % 2) return 0;
+    const int64_t S = t / 2;
+    uint64_t total = 0;
+    for (int n0 = 0; n0 <= N; ++n0) {
+        const int n1 = N - n0;
+        if (n0 > K0 || n1 > K1) continue;
+        const uint64_t c1 = or_binomial(K1, n1), c0 = or_binomial(K0, n0);
+        /* second-level words bucketed by weight */
+        const int wmax1 = K1 * K1;
+        uint64_t *cnt = (uint64_t *)calloc((size_t)wmax1 + 2, sizeof(uint64_t));
+        uint64_t *w1 = (uint64_t *)malloc((size_t)(c1 ? c1 : 1) * sizeof(uint64_t));
+        int *wt1 = (int *)malloc((size_t)(c1 ? c1 : 1) * sizeof(int));
+        uint64_t w = n1 ? ((1ull << n1) - 1ull) : 0ull;
+        for (uint64_t i = 0; i < c1; ++i) {
+            int s = 0;
+            for (uint64_t x = w; x; x &= x - 1) s += or_bitpos(x & (~x + 1));
+            w1[i] = w;
+            wt1[i] = s;
+            cnt[s + 1]++;
+            if (n1) w = or_next_hamming(w);
+        }
+        for (int k = 0; k <= wmax1; ++k) cnt[k + 1] += cnt[k];
+        uint64_t *sorted = (uint64_t *)malloc((size_t)(c1 ? c1 : 1) * sizeof(uint64_t));
+        uint64_t *fillp = (uint64_t *)malloc(((size_t)wmax1 + 1) * sizeof(uint64_t));
+        memcpy(fillp, cnt, ((size_t)wmax1 + 1) * sizeof(uint64_t));
+        for (uint64_t i = 0; i < c1; ++i) sorted[fillp[wt1[i]]++] = w1[i];
+        uint64_t a = n0 ? ((1ull << n0) - 1ull) : 0ull;
+        for (uint64_t i = 0; i < c0; ++i) {
+            int s0 = 0;
+            for (uint64_t x = a; x; x &= x - 1) s0 += or_bitpos(x & (~x + 1)) + 1;
+            const int64_t need = S - s0;
+            if (need >= 0 && need <= wmax1) {
+                for (uint64_t q = cnt[need]; q < cnt[need + 1]; ++q) {
+                    if (out) out[total] = (a << K1) | sorted[q];
+                    ++total;
+                }
+            }
+            if (n0) a = or_next_hamming(a);
+        }
+        free(cnt);
+        free(w1);
+        free(wt1);
+        free(sorted);
+        free(fillp);
+    }
+    if (out) qsort(out, (size_t)total, sizeof(uint64_t), or_cmp_u64);
+    return total;
+}
+
+/* The single-level quartic loop of or_build_row on one level's word `lw`
+ * (K orbitals, tables kt/vt) with the other level's bits `other` fixed at
+ * shift `osh`; the level's word sits at shift `lsh` of the combined word. */
+static void or_level_quartic(const uint64_t *basis, uint64_t n, uint64_t lw, int K, int lsh, uint64_t other,
+                             const uint16_t *kt, const double *vt, or_rowacc *acc)
+{
+    const uint64_t mask = (1ull << K) - 1ull;
+    const uint64_t highest = 1ull << (K - 1);
+    uint64_t t4 = lw;
+    while (t4) {
+        uint64_t k4o = t4 & (~t4 + 1);
+        int k4 = or_popcount(k4o - 1);
+        uint64_t t3 = lw ^ k4o;
+        while (t3) {
+            uint64_t k3o = t3 & (~t3 + 1);
+            int k3 = or_popcount(k3o - 1);
+            if (k3 != k4) {
+                uint64_t t2 = mask ^ (t3 ^ k3o);
+                while (t2) {
+                    uint64_t k2o = t2 & (~t2 + 1);
+                    int k2 = or_popcount(k2o - 1);
+                    size_t ti = ((size_t)k4 * K + k3) * K + k2;
+                    int k1 = kt[ti];
+                    if (k1 < K) {
+                        uint64_t k1o = 1ull << k1;
+                        if ((!(k1o & lw) || ((k1o & k3o) || (k1o & k4o))) &&
+                            (!(k2o & lw) || ((k2o & k3o) || (k2o & k4o))) && !(k1o & k2o)) {
+                            int sgn;
+                            uint64_t out = or_evaluate_cdcdcc(&sgn, k1o, k2o, k3o, k4o, lw, highest);
+                            if (sgn != 0 && out >= lw) {
+                                uint64_t j = or_find_index(basis, n, (out << lsh) | other);
+                                if (j < n) {
+                                    double el = (double)sgn * vt[ti];
+                                    if (fabs(el) > OR_SPARSE_ZERO_TOL) or_acc_add(acc, (int64_t)j, el);
+                                }
+                            }
+                        }
+                    }
+                    t2 ^= k2o;
+                }
+            }
+            t3 ^= k3o;
+        }
+        t4 ^= k4o;
+    }
+}
+
+/* One upper-triangle row of the two-level Hamiltonian in the model's call
+ * order (two_level_pseudopotential_model.cpp:190-215): level-0 then level-1
+ * occupation energies (Add_CdC_Terms, two_level_spinless_fermion_hamiltonian.hpp:
+ * 143-270), then the level-0 and level-1 quartic terms (Add_CdCdCC_Terms,
+ * :306-470), each on its level's word with the other fixed. */
+static void or_build2_row(const uint64_t *basis, uint64_t n, int K0, int64_t row, const uint16_t *kt0,
+                          const double *vt0, const uint16_t *kt1, const double *vt1, const double *e0,
+                          const double *e1, or_rowacc *acc)
+{
+    const int K1 = K0 + 2;
+    const uint64_t w = basis[row], first = w >> K1, second = w & ((1ull << K1) - 1ull);
+    if (acc->cap == 0) or_acc_grow(acc);
+    or_acc_reset(acc);
+    if (e0)
+        for (uint64_t x = first; x; x &= x - 1) {
+            double v = e0[or_bitpos(x & (~x + 1))];
+            if (fabs(v) > OR_SPARSE_ZERO_TOL) or_acc_add(acc, row, v);
+        }
+    if (e1)
+        for (uint64_t x = second; x; x &= x - 1) {
+            double v = e1[or_bitpos(x & (~x + 1))];
+            if (fabs(v) > OR_SPARSE_ZERO_TOL) or_acc_add(acc, row, v);
+        }
+    or_level_quartic(basis, n, first, K0, K1, second, kt0, vt0, acc);
+    or_level_quartic(basis, n, second, K1, 0, first << K1, kt1, vt1, acc);
+}
+
+int64_t or_build2_upper_count(const uint64_t *basis, uint64_t n, int K0, const uint16_t *kt0, const double *vt0,
+                              const uint16_t *kt1, const double *vt1, const double *e0, const double *e1,
+                              int64_t *rowlen, int nthreads)
+{
+    int64_t total = 0;
+    if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads) reduction(+ : total)
+#endif
+    {
+        or_rowacc acc = {0, 0, 0, 0, 0, 0};
+        or_entry *fin = 0;
+        int64_t fcap = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+        for (int64_t r = 0; r < (int64_t)n; ++r) {
+            or_build2_row(basis, n, K0, r, kt0, vt0, kt1, vt1, e0, e1, &acc);
+            int64_t m = or_row_finish(&acc, &fin, &fcap);
+            rowlen[r] = m;
+            total += m;
+        }
+        or_acc_free(&acc);
+        free(fin);
+    }
+    return total;
+}
+
+void or_build2_upper_fill(const uint64_t *basis, uint64_t n, int K0, const uint16_t *kt0, const double *vt0,
+                          const uint16_t *kt1, const double *vt1, const double *e0, const double *e1,
+                          const int64_t *rowptr, int32_t *col, double *val, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+        or_rowacc acc = {0, 0, 0, 0, 0, 0};
+        or_entry *fin = 0;
+        int64_t fcap = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+        for (int64_t r = 0; r < (int64_t)n; ++r) {
+            or_build2_row(basis, n, K0, r, kt0, vt0, kt1, vt1, e0, e1, &acc);
+            int64_t m = or_row_finish(&acc, &fin, &fcap);
+            for (int64_t t = 0; t < m; ++t) {
+                col[rowptr[r] + t] = (int32_t)fin[t].col;
+                val[rowptr[r] + t] = fin[t].val;
+            }
+        }
+        or_acc_free(&acc);
+        free(fin);
+    }
+}
+
 /* ------------------------------------------------------------------- SpMV */
 
 /* y = A x for A symmetric stored as its upper triangle in CRS:

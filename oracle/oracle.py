@@ -99,6 +99,14 @@ def lib():
         L.or_spmv_sym_upper_mt.argtypes = [_i64p, _i32p, _f64p, ctypes.c_int64, _f64p, _f64p, _f64p, ctypes.c_int]
         L.or_spmv_full.restype = None
         L.or_spmv_full.argtypes = [_i64p, _i32p, _f64p, ctypes.c_int64, _f64p, _f64p, ctypes.c_int]
+        L.or_basis2_build.restype = ctypes.c_uint64
+        L.or_basis2_build.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _u64p]
+        L.or_build2_upper_count.restype = ctypes.c_int64
+        L.or_build2_upper_count.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_int, _u16p, _f64p, _u16p, _f64p,
+                                            _f64p, _f64p, _i64p, ctypes.c_int]
+        L.or_build2_upper_fill.restype = None
+        L.or_build2_upper_fill.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_int, _u16p, _f64p, _u16p, _f64p,
+                                           _f64p, _f64p, _i64p, _i32p, _f64p, ctypes.c_int]
         L.or_num_procs.restype = ctypes.c_int
         _LIB = L
     return _LIB
@@ -634,6 +642,41 @@ def complex_upper_to_full(rowptr, col, val, n):
     M = (U + S.conj().T).tocsr()
     M.sort_indices()
     return M.indptr.astype(np.int64), M.indices.astype(np.int32), M.data.astype(np.complex128)
+
+
+def basis2_c(N: int, norb0: int, two_lz: int) -> np.ndarray:
+    """The two-level basis as combined words (first << (norb0+2)) | second,
+    ascending: the C restatement of basis2 (oracle.c or_basis2_build)."""
+    n = int(lib().or_basis2_build(N, norb0, two_lz, None))
+    out = np.empty(n, dtype=np.uint64)
+    if n:
+        lib().or_basis2_build(N, norb0, two_lz, _p(out, _u64p))
+    return out
+
+
+def build_upper2_c(words: np.ndarray, norb0: int, kt0, vt0, kt1, vt1, e0=None, e1=None,
+                   nthreads: int | None = None):
+    """The C restatement of build_upper2 (oracle.c or_build2_row: same loops,
+    same arrival-order accumulation) over combined words, multi-threaded over
+    rows: the CPU baseline of the two-level build."""
+    nt = nthreads or num_procs()
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    a0 = [np.ascontiguousarray(kt0, dtype=np.uint16), np.ascontiguousarray(vt0, dtype=np.float64)]
+    a1 = [np.ascontiguousarray(kt1, dtype=np.uint16), np.ascontiguousarray(vt1, dtype=np.float64)]
+    ee = [None if e is None else np.ascontiguousarray(e, dtype=np.float64) for e in (e0, e1)]
+    ep = [None if e is None else _p(e, _f64p) for e in ee]
+    n = len(w)
+    rowlen = np.zeros(n, dtype=np.int64)
+    L = lib()
+    L.or_build2_upper_count(_p(w, _u64p), n, norb0, _p(a0[0], _u16p), _p(a0[1], _f64p), _p(a1[0], _u16p),
+                            _p(a1[1], _f64p), ep[0], ep[1], _p(rowlen, _i64p), nt)
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(rowlen, out=rowptr[1:])
+    col = np.empty(int(rowptr[-1]), dtype=np.int32)
+    val = np.empty(int(rowptr[-1]), dtype=np.float64)
+    L.or_build2_upper_fill(_p(w, _u64p), n, norb0, _p(a0[0], _u16p), _p(a0[1], _f64p), _p(a1[0], _u16p),
+                           _p(a1[1], _f64p), ep[0], ep[1], _p(rowptr, _i64p), _p(col, _i32p), _p(val, _f64p), nt)
+    return rowptr, col, val
 
 
 # ------------------------------------------------------------ observables

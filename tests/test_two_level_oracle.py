@@ -58,3 +58,20 @@ def test_level_exchange_ladder_commutes_with_h(oracle, N, norb0, tlz):
     assert T.nnz > 0
     C = H @ T - T @ H
     assert abs(C).max() <= 1e-12 * abs(H).max() * abs(T).max()
+
+
+@pytest.mark.parametrize("N,norb0,tlz", [(3, 5, 0), (4, 6, -2), (5, 6, 1), (6, 9, 0)])
+def test_c_restatement_matches_python(oracle, N, norb0, tlz):
+    """oracle.c's two-level basis and build (the CPU baseline) agree bit for
+    bit with the Python loops."""
+    n1 = norb0 + 2
+    f, s = oracle.basis2(N, norb0, tlz)
+    words = np.array([(int(a) << n1) | int(b) for a, b in zip(f, s)], dtype=np.uint64)
+    assert np.array_equal(oracle.basis2_c(N, norb0, tlz), words)
+    kt0, vt0 = oracle.quartic_tables(norb0, oracle.odd_coulomb_list(norb0))
+    kt1, vt1 = oracle.quartic_tables(n1, np.random.default_rng(2).uniform(-1, 2, n1 - 1))
+    e0, e1 = np.linspace(-0.3, 0.3, norb0), np.full(n1, 0.7)
+    a = oracle.build_upper2(f, s, norb0, kt0, vt0, kt1, vt1, e0, e1)
+    b = oracle.build_upper2_c(words, norb0, kt0, vt0, kt1, vt1, e0, e1, nthreads=2)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(a[2].view(np.uint64), b[2].view(np.uint64))
