@@ -586,6 +586,239 @@ void or_build2_upper_fill(const uint64_t *basis, uint64_t n, int K0, const uint1
     }
 }
 
+/* ----------------------------------------- complex momentum path (OFL model) */
+
+/* FermionFockBasis::GenerateFockSpace with TestLinearMomentumSector2
+ * (interacting_ofl_model.cpp:994-1001, linear_momentum_constraints_2D.cpp:38-79):
+ * Gosper's successor over the N-bit words of X*Y orbitals (bit p at kx = p/Y,
+ * ky = p%Y), kept when (sum kx mod X, sum ky mod Y) = (kx, ky); ascending.
+ * With out == NULL only counts. */
+uint64_t or_basis_momentum(int N, int X, int Y, int kx, int ky, uint64_t *out)
+{
+    const int K = X * Y;
+    const uint64_t full = or_binomial(K, N);
+    uint64_t w = (1ull << N) - 1ull, c = 0;
+    for (uint64_t i = 0; i < full; ++i) {
+        int sx = 0, sy = 0;
+        for (uint64_t x = w; x; x &= x - 1) {
+            int p = or_bitpos(x & (~x + 1));
+            sx += p / Y;
+            sy += p % Y;
+        }
+        if (sx % X == kx && sy % Y == ky) {
+            if (out) out[c] = w;
+            ++c;
+        }
+        if (i + 1 < full) w = or_next_hamming(w);
+    }
+    return c;
+}
+
+typedef struct { int64_t col; double re, im; } or_centry;
+typedef struct { or_centry *e; int64_t n, cap; int32_t *slot; int64_t tcap; int64_t *pos; } or_crowacc;
+
+static void or_cacc_reset(or_crowacc *a)
+{
+    for (int64_t t = 0; t < a->n; ++t) a->slot[a->pos[t]] = -1;
+    a->n = 0;
+}
+
+static void or_cacc_grow(or_crowacc *a)
+{
+    int64_t ncap = a->cap ? 2 * a->cap : 1024;
+    a->e = (or_centry *)realloc(a->e, (size_t)ncap * sizeof(or_centry));
+    a->pos = (int64_t *)realloc(a->pos, (size_t)ncap * sizeof(int64_t));
+    a->cap = ncap;
+    free(a->slot);
+    a->tcap = 4 * ncap;
+    a->slot = (int32_t *)malloc((size_t)a->tcap * sizeof(int32_t));
+    for (int64_t i = 0; i < a->tcap; ++i) a->slot[i] = -1;
+    for (int64_t t = 0; t < a->n; ++t) {
+        uint64_t h = ((uint64_t)a->e[t].col * 0x9E3779B97F4A7C15ull) & (uint64_t)(a->tcap - 1);
+        while (a->slot[h] != -1) h = (h + 1) & (uint64_t)(a->tcap - 1);
+        a->slot[h] = (int32_t)t;
+        a->pos[t] = (int64_t)h;
+    }
+}
+
+/* entry(col) += (re, im), first insertion from (0, 0): Insert(i,j) += x with T = dcmplx */
+static void or_cacc_add(or_crowacc *a, int64_t col, double re, double im)
+{
+    if (a->n == a->cap) or_cacc_grow(a);
+    uint64_t h = ((uint64_t)col * 0x9E3779B97F4A7C15ull) & (uint64_t)(a->tcap - 1);
+    while (a->slot[h] != -1) {
+        or_centry *x = &a->e[a->slot[h]];
+        if (x->col == col) { x->re += re; x->im += im; return; }
+        h = (h + 1) & (uint64_t)(a->tcap - 1);
+    }
+    a->slot[h] = (int32_t)a->n;
+    a->pos[a->n] = (int64_t)h;
+    a->e[a->n].col = col;
+    a->e[a->n].re = 0.0 + re;
+    a->e[a->n].im = 0.0 + im;
+    a->n++;
+}
+
+static int or_cmp_centry(const void *x, const void *y)
+{
+    int64_t a = ((const or_centry *)x)->col, b = ((const or_centry *)y)->col;
+    return (a > b) - (a < b);
+}
+
+static int or_ofl_index(int k3, int k4, int K)
+{
+    const int t1 = k4 > k3 ? k3 : k4, t2 = k4 > k3 ? k4 : k3;
+    return t1 * K + t2 - t1 * (t1 + 1) / 2;
+}
+
+/* One upper-triangle row of SpinlessFermionHamiltonian<dcmplx> from the
+ * array-format OFL tables (spinless_fermion_hamiltonian.hpp:150-436 with
+ * interacting_ofl_model/term_tables.cpp:59-200): occupation energies, then the
+ * quartic loop of or_build_row with k1 = kTable[t*K + k2] and V =
+ * vTable[t*K + (k4 > k3 ? k1 : k2)], t the (k3, k4) triangle index; each
+ * term kept when abs > 1e-14 (hypot, the std::abs of std::complex). */
+static void or_cbuild_row(const uint64_t *basis, uint64_t n, int K, int64_t row, const uint16_t *kt,
+                          const double *vt, const double *e, or_crowacc *acc)
+{
+    const uint64_t in = basis[row];
+    const uint64_t mask = (1ull << K) - 1ull;
+    const uint64_t highest = 1ull << (K - 1);
+    if (acc->cap == 0) or_cacc_grow(acc);
+    or_cacc_reset(acc);
+    if (e)
+        for (uint64_t x = in; x; x &= x - 1) {
+            int k = or_bitpos(x & (~x + 1));
+            if (hypot(e[2 * k], e[2 * k + 1]) > OR_SPARSE_ZERO_TOL) or_cacc_add(acc, row, e[2 * k], e[2 * k + 1]);
+        }
+    uint64_t t4 = in;
+    while (t4) {
+        uint64_t k4o = t4 & (~t4 + 1);
+        int k4 = or_popcount(k4o - 1);
+        uint64_t t3 = in ^ k4o;
+        while (t3) {
+            uint64_t k3o = t3 & (~t3 + 1);
+            int k3 = or_popcount(k3o - 1);
+            if (k3 != k4) {
+                const size_t base = (size_t)or_ofl_index(k3, k4, K) * K;
+                uint64_t t2 = mask ^ (t3 ^ k3o);
+                while (t2) {
+                    uint64_t k2o = t2 & (~t2 + 1);
+                    int k2 = or_popcount(k2o - 1);
+                    int k1 = kt[base + k2];
+                    uint64_t k1o = 1ull << k1;
+                    if ((!(k1o & in) || ((k1o & k3o) || (k1o & k4o))) &&
+                        (!(k2o & in) || ((k2o & k3o) || (k2o & k4o))) && !(k1o & k2o)) {
+                        int sgn;
+                        uint64_t out = or_evaluate_cdcdcc(&sgn, k1o, k2o, k3o, k4o, in, highest);
+                        if (sgn != 0 && out >= in) {
+                            uint64_t j = or_find_index(basis, n, out);
+                            if (j < n) {
+                                const size_t vi = base + (size_t)(k4 > k3 ? k1 : k2);
+                                const double re = (double)sgn * vt[2 * vi], im = (double)sgn * vt[2 * vi + 1];
+                                if (hypot(re, im) > OR_SPARSE_ZERO_TOL) or_cacc_add(acc, (int64_t)j, re, im);
+                            }
+                        }
+                    }
+                    t2 ^= k2o;
+                }
+            }
+            t3 ^= k3o;
+        }
+        t4 ^= k4o;
+    }
+}
+
+static int64_t or_crow_finish(or_crowacc *acc, or_centry **out, int64_t *outcap)
+{
+    if (*outcap < acc->n) {
+        *outcap = acc->cap;
+        *out = (or_centry *)realloc(*out, (size_t)(*outcap) * sizeof(or_centry));
+    }
+    int64_t w = 0;
+    for (int64_t t = 0; t < acc->n; ++t)
+        if (!(hypot(acc->e[t].re, acc->e[t].im) < OR_SPARSE_ZERO_TOL)) (*out)[w++] = acc->e[t];
+    qsort(*out, (size_t)w, sizeof(or_centry), or_cmp_centry);
+    return w;
+}
+
+/* Count (col == NULL) or fill pass of the complex upper-triangle CRS. */
+int64_t or_cbuild_upper(const uint64_t *basis, uint64_t n, int K, const uint16_t *kt, const double *vt,
+                        const double *e, int64_t *rowlen, const int64_t *rowptr, int32_t *col, double *val,
+                        int nthreads)
+{
+    int64_t total = 0;
+    if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads) reduction(+ : total)
+#endif
+    {
+        or_crowacc acc = {0, 0, 0, 0, 0, 0};
+        or_centry *fin = 0;
+        int64_t fcap = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+        for (int64_t r = 0; r < (int64_t)n; ++r) {
+            or_cbuild_row(basis, n, K, r, kt, vt, e, &acc);
+            int64_t m = or_crow_finish(&acc, &fin, &fcap);
+            if (rowlen) rowlen[r] = m;
+            if (col)
+                for (int64_t t = 0; t < m; ++t) {
+                    col[rowptr[r] + t] = (int32_t)fin[t].col;
+                    val[2 * (rowptr[r] + t)] = fin[t].re;
+                    val[2 * (rowptr[r] + t) + 1] = fin[t].im;
+                }
+            total += m;
+        }
+        free(acc.e);
+        free(acc.slot);
+        free(acc.pos);
+        free(fin);
+    }
+    return total;
+}
+
+/* y = M x with the reference's Hermitian completion of the upper storage
+ * (sparse_linear_algebra.hpp:148-164 for T = dcmplx): y_i += A_ij x_j and,
+ * for j != i, y_j += conj(A_ij) x_i; complex as (re, im) pairs, rows split
+ * over threads with private y. */
+void or_cspmv_upper_mt(const int64_t *rowptr, const int32_t *col, const double *val, int64_t n, const double *x,
+                       double *y, double *scratch, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+#ifdef _OPENMP
+        const int t = omp_get_thread_num();
+#else
+        const int t = 0;
+#endif
+        double *yt = scratch + (size_t)t * 2 * n;
+        for (int64_t i = 0; i < 2 * n; ++i) yt[i] = 0.0;
+        const int64_t r0 = n * t / nthreads, r1 = n * (t + 1) / nthreads;
+        for (int64_t i = r0; i < r1; ++i) {
+            const double xr = x[2 * i], xi = x[2 * i + 1];
+            for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+                const int64_t c = col[k];
+                const double ar = val[2 * k], ai = val[2 * k + 1];
+                yt[2 * i] += ar * x[2 * c] - ai * x[2 * c + 1];
+                yt[2 * i + 1] += ar * x[2 * c + 1] + ai * x[2 * c];
+                if (c != i) {
+                    yt[2 * c] += ar * xr + ai * xi;
+                    yt[2 * c + 1] += ar * xi - ai * xr;
+                }
+            }
+        }
+    }
+    for (int64_t i = 0; i < 2 * n; ++i) {
+        double s = 0.0;
+        for (int t = 0; t < nthreads; ++t) s += scratch[(size_t)t * 2 * n + i];
+        y[i] = s;
+    }
+}
+
 /* ------------------------------------------------------------------- SpMV */
 
 /* y = A x for A symmetric stored as its upper triangle in CRS:

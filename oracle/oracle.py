@@ -107,6 +107,13 @@ def lib():
         L.or_build2_upper_fill.restype = None
         L.or_build2_upper_fill.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_int, _u16p, _f64p, _u16p, _f64p,
                                            _f64p, _f64p, _i64p, _i32p, _f64p, ctypes.c_int]
+        L.or_basis_momentum.restype = ctypes.c_uint64
+        L.or_basis_momentum.argtypes = [ctypes.c_int] * 5 + [_u64p]
+        L.or_cbuild_upper.restype = ctypes.c_int64
+        L.or_cbuild_upper.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_int, _u16p, _f64p, _f64p, _i64p, _i64p,
+                                      _i32p, _f64p, ctypes.c_int]
+        L.or_cspmv_upper_mt.restype = None
+        L.or_cspmv_upper_mt.argtypes = [_i64p, _i32p, _f64p, ctypes.c_int64, _f64p, _f64p, _f64p, ctypes.c_int]
         L.or_num_procs.restype = ctypes.c_int
         _LIB = L
     return _LIB
@@ -630,6 +637,52 @@ def build_upper_complex(words: np.ndarray, K: int, ktab, vtab, energies=None):
         vals.extend(v for _, v in kept)
         rowptr[i + 1] = len(cols)
     return rowptr, np.array(cols, dtype=np.int32), np.array(vals, dtype=np.complex128)
+
+
+def basis_momentum_c(N: int, X: int, Y: int, kx: int, ky: int) -> np.ndarray:
+    """C restatement of basis_momentum (oracle.c or_basis_momentum)."""
+    n = int(lib().or_basis_momentum(N, X, Y, kx, ky, None))
+    out = np.empty(n, dtype=np.uint64)
+    if n:
+        lib().or_basis_momentum(N, X, Y, kx, ky, _p(out, _u64p))
+    return out
+
+
+def build_upper_complex_c(words: np.ndarray, K: int, ktab, vtab, energies=None, nthreads: int | None = None):
+    """C restatement of build_upper_complex (oracle.c or_cbuild_row, same
+    loops and arrival-order accumulation), multi-threaded over rows: the CPU
+    baseline of the complex build."""
+    nt = nthreads or num_procs()
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    kt = np.ascontiguousarray(ktab, dtype=np.uint16)
+    vt = np.ascontiguousarray(np.asarray(vtab, dtype=np.complex128).view(np.float64))
+    e = None if energies is None else np.ascontiguousarray(np.asarray(energies, dtype=np.complex128).view(np.float64))
+    n = len(w)
+    rowlen = np.zeros(n, dtype=np.int64)
+    L = lib()
+    L.or_cbuild_upper(_p(w, _u64p), n, K, _p(kt, _u16p), _p(vt, _f64p), None if e is None else _p(e, _f64p),
+                      _p(rowlen, _i64p), None, None, None, nt)
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(rowlen, out=rowptr[1:])
+    col = np.empty(int(rowptr[-1]), dtype=np.int32)
+    val = np.empty(int(rowptr[-1]), dtype=np.complex128)
+    L.or_cbuild_upper(_p(w, _u64p), n, K, _p(kt, _u16p), _p(vt, _f64p), None if e is None else _p(e, _f64p),
+                      None, _p(rowptr, _i64p), _p(col, _i32p), _p(val.view(np.float64), _f64p), nt)
+    return rowptr, col, val
+
+
+def cspmv_upper(rowptr, col, val, x, nthreads: int | None = None) -> np.ndarray:
+    """The reference's complex upper-triangle product (or_cspmv_upper_mt)."""
+    nt = nthreads or num_procs()
+    n = len(rowptr) - 1
+    xv = np.ascontiguousarray(np.asarray(x, dtype=np.complex128).view(np.float64))
+    y = np.empty(2 * n)
+    scratch = np.empty(2 * n * nt)
+    v = np.ascontiguousarray(np.asarray(val, dtype=np.complex128).view(np.float64))
+    lib().or_cspmv_upper_mt(_p(np.ascontiguousarray(rowptr, dtype=np.int64), _i64p),
+                            _p(np.ascontiguousarray(col, dtype=np.int32), _i32p), _p(v, _f64p), n, _p(xv, _f64p),
+                            _p(y, _f64p), _p(scratch, _f64p), nt)
+    return y.view(np.complex128)
 
 
 def complex_upper_to_full(rowptr, col, val, n):

@@ -60,3 +60,23 @@ def test_completion_is_hermitian(oracle, N, X, Y, kx, ky):
     assert np.array_equal(U[off], U0[off])
     occ = np.array([[int(w) >> k & 1 for k in range(K)] for w in b])
     assert np.allclose(np.diag(U) - np.diag(U0), occ @ e, atol=1e-13)
+
+
+@pytest.mark.parametrize("N,X,Y,kx,ky", [(3, 3, 4, 0, 0), (5, 4, 5, 3, 2), (4, 4, 6, 1, 5)])
+def test_c_restatement_matches_python(oracle, N, X, Y, kx, ky):
+    """oracle.c's momentum basis, complex build and the reference's complex
+    upper-triangle product (the CPU baseline) agree with the Python loops:
+    basis and CRS bit for bit, product to rounding."""
+    K = X * Y
+    kt, vt = oracle.ofl_tables(X, Y, 5)
+    e = np.linspace(-0.4, 0.6, K) + 1e-3j * np.arange(K)
+    b = oracle.basis_momentum(N, X, Y, kx, ky)
+    assert np.array_equal(oracle.basis_momentum_c(N, X, Y, kx, ky), b)
+    a = oracle.build_upper_complex(b, K, kt, vt, e)
+    c = oracle.build_upper_complex_c(b, K, kt, vt, e, nthreads=2)
+    assert np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1])
+    assert np.array_equal(a[2].view(np.uint64), c[2].view(np.uint64))
+    M = oracle.complex_upper_to_full(*a, len(b))
+    A = sp.csr_matrix((M[2], M[1], M[0]), shape=(len(b), len(b)))
+    x = np.random.default_rng(1).uniform(-1, 1, len(b)) + 1j * np.random.default_rng(2).uniform(-1, 1, len(b))
+    assert np.max(np.abs(oracle.cspmv_upper(*c, x, nthreads=2) - A @ x)) <= 1e-12 * np.abs(a[2]).max() * 50
