@@ -13,11 +13,18 @@ reorthogonalisation -> verified residuals.
          vector in, eigenvalues and eigenvectors out, copies inside the timing
   roofline  the stored-CRS SpMV, algorithmic bytes per product
          nnz*(8+4) + (n+1)*8 + 2*n*8 over its average in-solve duration
-  cpu_baseline  the CPU oracle (a restatement of the reference's algorithm)
-         on the host cores, measured on bounded samples and scaled
+  max_rel_eig_vs_fixture  the eigenvalues against the committed ARPACK run
+         of the same Hamiltonian (tests/golden/arpack_n11_2s30_lz0.json)
+  sweep  the pseudopotential sweep N=10, 2S=27, 2Lz=0..8, 64 V1 points, 4
+         lowest each: converged solves/s of plain one-at-a-time GPU Lanczos,
+         batched Lanczos, and batched + warm start (eigenvector continuation),
+         with each mode's eigenvalues against the plain solves
+  cpu_baseline  one whole solve by the CPU oracle (a restatement of the
+         reference's algorithm) on all host cores: basis, build, ARPACK
 
-`--impl reference` times the same CPU restatement as the reference arm.
-The inputs (4.2 GB of CRS per product) are larger than the 129 MB L2.
+`--impl reference` times that whole CPU solve as the reference arm, one
+solve per step.  The inputs (4.2 GB of CRS per product) are larger than the
+129 MB L2.
 """
 from __future__ import annotations
 
@@ -113,59 +120,114 @@ class ClockSampler:
 
 # ------------------------------------------------------------- CPU oracle leg
 
-class CpuLeg:
-    """The CPU restatement of the reference path (oracle port) on all host
-    threads, measured on bounded samples of the solve.
+ARPACK_TOL = 1e-12   # the reference's ARPACK tolerance once initialised (its TOL is left unset)
 
-    Set-up (untimed): the full upper-triangle CRS built once by the oracle.
-    Each sample measures the full sector scan (basis), the quartic build of
-    one eighth of the rows (scaled by rows), and two products of the
-    reference's upper-triangle SpMV loop over the whole matrix (rows split
-    over threads like its MPI ranks).  Estimate = basis + build + products x
-    the product count ARPACK needed for this problem with the reference's
-    settings (recorded in tests/golden/arpack_n11_2s30_lz0.json).  ARPACK's
-    own dense work is not counted, so the estimate favours the CPU."""
+
+class CpuSolve:
+    """One whole solve of the workload by the CPU restatement of the
+    reference's path on all host threads: the sector scan (basis), the
+    quartic build of the upper-triangle CRS, and ARPACK's implicitly
+    restarted driver (SciPy's bundled dnaupd/dneupd, the family the reference
+    calls) with the reference's settings (which='SR', ncv = 2*nev+21, maxiter
+    2000, tol 1e-12) and the reference's upper-triangle product as the
+    operator, from the same seed-42 start vector; then the true residual of
+    every returned pair.  Nothing is sampled or extrapolated."""
 
     def __init__(self):
         from oracle import oracle as O
         self.O = O
         self.threads = O.num_procs()
-        self.kt, self.vt = O.quartic_tables(NORB, O.odd_coulomb_list(NORB))
-        self.b = O.basis(N_PART, NORB, TWO_LZ, self.threads)
-        t0 = time.perf_counter()
-        self.rp, self.col, self.val = O.build_upper(self.b, NORB, self.kt, self.vt, self.threads)
-        self.t_build_full = time.perf_counter() - t0
-        self.n = len(self.b)
-        self.x = np.random.default_rng(1).uniform(-1, 1, self.n)
-        fx = os.path.join(ROOT, "tests", "golden", "arpack_n11_2s30_lz0.json")
-        self.matvecs = json.load(open(fx))["matvecs"] if os.path.exists(fx) else None
-        self.arpack_fixture = json.load(open(fx)) if os.path.exists(fx) else None
 
-    def sample(self):
+    def solve(self):
+        import scipy.sparse.linalg as sla
         O = self.O
         t0 = time.perf_counter()
-        O.basis(N_PART, NORB, TWO_LZ, self.threads)
-        t_basis = time.perf_counter() - t0
-        rows = self.n // 8
-        r0 = (self.n - rows) // 2
-        t0 = time.perf_counter()
-        O.build_upper(self.b, NORB, self.kt, self.vt, self.threads, rows=(r0, r0 + rows))
-        t_build = (time.perf_counter() - t0) * self.n / rows
-        O.spmv_sym_upper(self.rp, self.col, self.val, self.x, self.threads)
-        t0 = time.perf_counter()
-        for _ in range(2):
-            O.spmv_sym_upper(self.rp, self.col, self.val, self.x, self.threads)
-        t_prod = (time.perf_counter() - t0) / 2
-        return {"t_basis": t_basis, "t_build": t_build, "t_prod": t_prod}
+        b = O.basis(N_PART, NORB, TWO_LZ, self.threads)
+        t1 = time.perf_counter()
+        kt, vt = O.quartic_tables(NORB, O.odd_coulomb_list(NORB))
+        rp, col, val = O.build_upper(b, NORB, kt, vt, self.threads)
+        t2 = time.perf_counter()
+        n = len(b)
+        count = [0]
 
-    def estimate(self, s, matvecs):
-        return s["t_basis"] + s["t_build"] + matvecs * s["t_prod"]
+        def mv(x):
+            count[0] += 1
+            return O.spmv_sym_upper(rp, col, val, np.ascontiguousarray(x, dtype=np.float64), self.threads)
 
-    def describe(self, s, matvecs):
-        return (f"oracle port on {self.threads} threads: full basis scan {s['t_basis']:.2f}s; quartic build of "
-                f"n/8 rows scaled to {s['t_build']:.1f}s (full build measured once: {self.t_build_full:.1f}s); "
-                f"reference upper-triangle SpMV {s['t_prod']:.3f}s/product over the whole matrix x {matvecs} "
-                f"products (ARPACK's count for this problem); ARPACK dense work not counted")
+        op = sla.LinearOperator((n, n), matvec=mv, dtype=np.float64)
+        w, v = sla.eigs(op, k=NEV, which="SR", tol=ARPACK_TOL, v0=start_vector(n, SEED), ncv=2 * NEV + 21,
+                        maxiter=2000)
+        t3 = time.perf_counter()
+        res = []
+        for i in range(NEV):
+            x = v[:, i].real
+            x = x / np.linalg.norm(x)
+            hx = O.spmv_sym_upper(rp, col, val, x, self.threads)
+            res.append(float(np.linalg.norm(hx - (x @ hx) * x)))
+        t4 = time.perf_counter()
+        return {"seconds": t4 - t0, "basis": t1 - t0, "build": t2 - t1, "arpack": t3 - t2, "residuals": t4 - t3,
+                "matvecs": count[0], "eigenvalues": np.sort(w.real), "max_residual": max(res), "nnz_upper": int(rp[-1])}
+
+    def describe(self, r):
+        return (f"one whole solve by the oracle port on {self.threads} threads (nothing scaled): sector scan "
+                f"{r['basis']:.2f}s, upper-triangle quartic build {r['build']:.1f}s ({r['nnz_upper']} elements), "
+                f"SciPy ARPACK eigs(which='SR', ncv={2 * NEV + 21}, tol={ARPACK_TOL:g}) with the reference's "
+                f"upper-triangle product {r['arpack']:.1f}s ({r['matvecs']} products), residual check "
+                f"{r['residuals']:.2f}s; max residual {r['max_residual']:.1e}")
+
+
+def load_fixture():
+    p = os.path.join(ROOT, "tests", "golden", "arpack_n11_2s30_lz0.json")
+    return json.load(open(p)) if os.path.exists(p) else None
+
+
+def max_rel_vs(ev, ref):
+    ev, ref = np.sort(np.asarray(ev, dtype=float)), np.sort(np.asarray(ref, dtype=float))
+    return float(np.max(np.abs(ev - ref) / np.abs(ref)))
+
+
+# ------------------------------------------------------------- sweep (config 2)
+
+SWEEP_N, SWEEP_NORB, SWEEP_SECTORS, SWEEP_POINTS, SWEEP_NEV = 10, 28, [0, 2, 4, 6, 8], 64, 4
+
+
+def run_sweep():
+    """The pseudopotential sweep N=10, 2S=27, 2Lz = 0..8, 64 V1 points in
+    [0.5, 3.0], 4 lowest each (320 solves) three ways: plain one-at-a-time
+    GPU Lanczos (ed_solve_sector per Hamiltonian), batched lockstep Lanczos
+    from random starts, and batched + warm started by eigenvector
+    continuation (anchor solves, shared-subspace Ritz step accepted on true
+    residuals, warm-started solves for the rest).  Each mode runs its first
+    sector once untimed, then the whole sweep timed with a device
+    synchronisation on both sides."""
+    from hamiltonian_diagonalization_gb300 import sweep as SW
+    v1s = np.linspace(0.5, 3.0, SWEEP_POINTS)
+    args = (SWEEP_N, SWEEP_NORB)
+    SW.run_plain(*args, SWEEP_SECTORS[:1], v1s[:1], SWEEP_NEV, TOL, 1)
+    tp, ep, products = SW.run_plain(*args, SWEEP_SECTORS, v1s, SWEEP_NEV, TOL, 1)
+    SW.run_batched(*args, SWEEP_SECTORS[:1], v1s, SWEEP_NEV, TOL, 1)
+    tb, eb, infos = SW.run_batched(*args, SWEEP_SECTORS, v1s, SWEEP_NEV, TOL, 1)
+    SW.run_subspace(*args, SWEEP_SECTORS[:1], v1s, SWEEP_NEV, TOL, 1)
+    ts, es, recs = SW.run_subspace(*args, SWEEP_SECTORS, v1s, SWEEP_NEV, TOL, 1)
+    solves = len(ep)
+
+    def dev(e):
+        return float(max(np.max(np.abs(e[k] - ep[k]) / np.abs(ep[k])) for k in ep))
+
+    return {"workload": "LLL Coulomb sphere N=10 2S=27, 2Lz=0,2,4,6,8 x 64 V1 in [0.5, 3.0], 4 lowest, "
+                        "residual 1e-10", "solves": solves, "unit": "solves/s",
+            "plain": {"seconds": tp, "solves_per_s": solves / tp, "products": products},
+            "batched": {"seconds": tb, "solves_per_s": solves / tb,
+                        "max_residual": max(i["max_residual"] for i in infos),
+                        "max_rel_eigenvalue_diff_vs_plain": dev(eb)},
+            "batched_warm": {"seconds": ts, "solves_per_s": solves / ts,
+                             "warm_start": "eigenvector continuation (anchor solves + shared-subspace Ritz step)",
+                             "max_residual": max(r["max_residual"] for r in recs),
+                             "max_rel_eigenvalue_diff_vs_plain": dev(es),
+                             "anchors": [sum(len(a) for a in r["anchors"]) for r in recs],
+                             "ritz_accepted": [r["ritz_accepted"] for r in recs],
+                             "fallback": [len(r["fallback"]) for r in recs]},
+            "ratio_batched_vs_plain": tp / tb, "ratio_batched_warm_vs_plain": tp / ts}
 
 
 # ------------------------------------------------------------- device leg
@@ -328,6 +390,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncv", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the pseudopotential sweep (solves/s) leg")
     ap.add_argument("--clock-log-dir", default="/tmp",
                     help="directory for the raw nvidia-smi clock samples of the timed region")
     args = ap.parse_args()
@@ -344,27 +407,25 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        leg = CpuLeg()
-        matvecs = leg.matvecs or 334
-        samples = []
+        leg = CpuSolve()
+        runs = []
         for i in range(args.warmup + args.steps):
-            s = leg.sample()
+            r = leg.solve()
             if i >= args.warmup:
-                samples.append(s)
-        ests = [leg.estimate(s, matvecs) for s in samples]
-        v = statistics.median(ests)
+                runs.append(r)
+        v = statistics.median(r["seconds"] for r in runs)
         line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": v * 1000.0, "higher_is_better": False, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (parameters only)", "config": config,
                 "impl": "reference",
+                "eigenvalues": [float(x) for x in runs[-1]["eigenvalues"]],
                 "cpu_baseline": {"value": v, "unit": "s", "cores": leg.threads, "kind": "port",
-                                 "sample": leg.describe(samples[-1], matvecs)},
-                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        if leg.arpack_fixture:
-            fx = leg.arpack_fixture
-            line["arpack_recorded"] = {"seconds": fx["seconds"], "matvecs": fx["matvecs"], "threads": fx["threads"],
-                                       "note": "one full CPU solve (oracle build + SciPy ARPACK), "
-                                               "tests/golden/make_arpack_fixture.py"}
+                                 "sample": leg.describe(runs[-1]) + "; every step is one such solve"},
+                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "steps_seconds": [r["seconds"] for r in runs]}
+        fx = load_fixture()
+        if fx:
+            line["max_rel_eig_vs_fixture"] = max_rel_vs(runs[-1]["eigenvalues"], fx["eigenvalues"])
         print(json.dumps(line))
         return
 
@@ -398,14 +459,18 @@ def main():
             "gpu_launches": int(r["launches"]),
             "phases_s": {k: statistics.median(p[k] for p in r["phases"]) for k in r["phases"][0]},
             "clocks": r["clocks"]}
+    fx = load_fixture()
+    if fx:
+        line["max_rel_eig_vs_fixture"] = max_rel_vs(r["ev"], fx["eigenvalues"])
+        line["fixture"] = "tests/golden/arpack_n11_2s30_lz0.json (oracle CRS + SciPy ARPACK, reference settings)"
+    if not args.no_sweep and rank == 0:
+        line["sweep"] = run_sweep()
     if not args.no_cpu and ws == 1:
         try:
-            leg = CpuLeg()
-            matvecs = leg.matvecs or int(infos[-1]["matvecs"])
-            s = leg.sample()
-            v = leg.estimate(s, matvecs)
-            line["cpu_baseline"] = {"value": v, "unit": "s", "cores": leg.threads, "kind": "port",
-                                    "sample": leg.describe(s, matvecs)}
+            leg = CpuSolve()
+            cr = leg.solve()
+            line["cpu_baseline"] = {"value": cr["seconds"], "unit": "s", "cores": leg.threads, "kind": "port",
+                                    "sample": leg.describe(cr)}
         except Exception as e:  # the CPU leg must not hide the device result
             line["cpu_baseline"] = {"value": None, "unit": "s", "cores": None, "kind": "port",
                                     "sample": f"failed: {e}"}

@@ -11,6 +11,7 @@ from .host import (  # noqa: F401
     CrsSparseMatrix,
     FermionFockBasis,
     HamiltonianBatch,
+    Subspace,
     InteractingOflModel,
     MatrixVectorFunction,
     MpiWrapper,

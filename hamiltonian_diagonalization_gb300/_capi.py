@@ -132,6 +132,13 @@ _SIGS = {
     "ed_batch_dims": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
     "ed_batch_spmm": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "ed_batch_solve": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(BatchInfo)]),
+    "ed_batch_solve_subset": (c_int, [c_void_p, P(c_int), c_int, P(LanczosParams), c_void_p, P(c_double), c_void_p,
+                                      P(BatchInfo)]),
+    "ed_subspace_create": (c_int, [c_i64, c_int, P(c_void_p)]),
+    "ed_subspace_free": (c_int, [c_void_p]),
+    "ed_subspace_dim": (c_int, [c_void_p, P(c_int)]),
+    "ed_subspace_add": (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, P(c_int)]),
+    "ed_batch_subspace_ritz": (c_int, [c_void_p, c_void_p, c_int, c_int, P(c_double), c_void_p, P(c_double)]),
     "ed_mlp_create": (c_int, [c_int, c_int, c_u64, P(c_void_p)]),
     "ed_mlp_free": (c_int, [c_void_p]),
     "ed_mlp_num_params": (c_int, [c_void_p, P(c_i64)]),

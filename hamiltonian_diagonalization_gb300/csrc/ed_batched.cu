@@ -30,21 +30,7 @@
 
 #include "ed_hop.cuh"
 #include "ed_lanczos.h"
-
-struct ed_batch {
-    int B = 0;                    // Hamiltonians
-    int K = 0, N = 0;
-    int64_t n = 0, nnz = 0;       // sector dimension, off-diagonal pattern entries
-    int nhop = 0;
-    edgb::DevBuf<int64_t> rowptr;
-    edgb::DevBuf<int32_t> col;    // nnz + pad
-    edgb::DevBuf<uint16_t> code;  // nnz + pad
-    edgb::DevBuf<double> w;       // [nhop][B] per-Hamiltonian hop values
-    edgb::DevBuf<double> diag;    // [n][B]
-    // tuned block-product tile: Hamiltonians per tile, loads in flight, threads
-    // per CTA, hop values through L1 (1) or staged in shared memory (0)
-    int tb = 32, unroll = 4, nt = 256, l1 = 1;
-};
+#include "ed_batch.h"
 
 namespace edgb {
 
@@ -52,13 +38,7 @@ namespace {
 
 constexpr uint16_t kCodeSign = 0x8000;
 
-int sms_b()
-{
-    int dev = 0, s = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
-    return s;
-}
+int sms_b() { return batch_sms(); }
 
 // Element code for the pair hop (a,b)->(c,d) of `in` (canonical direction
 // as in hop_bits); keep = the hop exists in at least one Hamiltonian.
@@ -670,6 +650,14 @@ void batch_create(ed_batch& bt, const ed_basis& basis, int K, int B, const uint1
         std::memcpy(&da[(size_t)b * K * K], hops[b].diag_a.data(), (size_t)K * K * 8);
         std::memcpy(&db[(size_t)b * K * K], hops[b].diag_b.data(), (size_t)K * K * 8);
     }
+    bt.ncoef = nhop + 2 * K * K;
+    bt.coef.assign((size_t)B * bt.ncoef, 0.0);
+    for (int b = 0; b < B; ++b) {
+        double* c = &bt.coef[(size_t)b * bt.ncoef];
+        std::memcpy(c, hops[b].w.data(), (size_t)nhop * 8);
+        std::memcpy(c + nhop, hops[b].diag_a.data(), (size_t)K * K * 8);
+        std::memcpy(c + nhop + K * K, hops[b].diag_b.data(), (size_t)K * K * 8);
+    }
     DevBuf<double> dwu(nhop), dda(da.size()), ddb(db.size());
     DevBuf<int> doff(2 * K);
     bt.w.alloc(wall.size());
@@ -721,15 +709,6 @@ void batch_create(ed_batch& bt, const ed_basis& basis, int K, int B, const uint1
 namespace {
 
 constexpr size_t kSmemOptIn = 227 * 1024;   // dynamic shared memory per CTA on sm_103a
-
-// The per-Hamiltonian operands of a block product: hop values [nhop][B] and
-// diagonals [n][B] for the B problems being multiplied (all of a batch, or
-// the compacted subset a solve still iterates).
-struct BlockOperands {
-    const double* w;
-    const double* diag;
-    int B;
-};
 
 template <int TB, int U, int NT>
 void launch_bspmm(const ed_batch& bt, const BlockOperands& o, const double* X, double* Y, int64_t rows,
@@ -786,13 +765,70 @@ void bspmm_variant(const ed_batch& bt, const BlockOperands& o, int tb, int u, in
     throw Error(ED_ERR_INTERNAL, "unknown block-product tile");
 }
 
+}  // namespace
+
+int batch_sms()
+{
+    int dev = 0, s = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return s;
+}
+
 BlockOperands full_operands(const ed_batch& bt) { return {bt.w.p, bt.diag.p, bt.B}; }
 
-}  // namespace
+BlockOperands gather_operands(const ed_batch& bt, const int* sel_host, int nsel, DevBuf<double>& w,
+                              DevBuf<double>& diag, cudaStream_t st)
+{
+    ED_REQUIRE(nsel >= 1 && nsel <= bt.B, ED_ERR_ARG, "selection of 1..B problems");
+    for (int q = 0; q < nsel; ++q)
+        ED_REQUIRE(sel_host[q] >= 0 && sel_host[q] < bt.B, ED_ERR_ARG, "selected problem out of range");
+    DevBuf<int> sel(nsel);
+    ED_CUDA(cudaMemcpyAsync(sel.p, sel_host, (size_t)nsel * 4, cudaMemcpyHostToDevice, st));
+    w.alloc((size_t)bt.nhop * nsel);
+    diag.alloc((size_t)bt.n * nsel);
+    const auto grid = [&](int64_t work) {
+        return (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 8, (work + 255) / 256));
+    };
+    k_bgather<<<grid((int64_t)bt.nhop * nsel), 256, 0, st>>>(bt.w.p, bt.nhop, bt.B, sel.p, nsel, w.p); count_launch();
+    k_bgather<<<grid(bt.n * nsel), 256, 0, st>>>(bt.diag.p, bt.n, bt.B, sel.p, nsel, diag.p); count_launch();
+    ED_CUDA(cudaGetLastError());
+    ED_CUDA(cudaStreamSynchronize(st));   // sel is freed on return
+    return {w.p, diag.p, nsel};
+}
+
+void batch_block_product(const ed_batch& bt, const BlockOperands& o, const double* X, double* Y, cudaStream_t st)
+{
+    const std::array<int, 4> t = batch_tile(bt, o, st);
+    bspmm_variant(bt, o, t[0], t[1], t[2], t[3], X, Y, bt.n, st);
+}
 
 void batch_spmm(const ed_batch& bt, const double* X, double* Y, cudaStream_t st)
 {
-    bspmm_variant(bt, full_operands(bt), bt.tb, bt.unroll, bt.nt, bt.l1, X, Y, bt.n, st);
+    batch_block_product(bt, full_operands(bt), X, Y, st);
+}
+
+void batch_residuals(const ed_batch& bt, const BlockOperands& o, const double* X, const double* lam, int k,
+                     double* res, cudaStream_t st)
+{
+    const int B = o.B;
+    int BP = 1;
+    while (BP < B) BP <<= 1;
+    const int64_t n = bt.n;
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 4, n / 128));
+    DevBuf<double> y((size_t)n * B), part((size_t)nb * B), s(B), dl(B);
+    std::vector<double> l(B), r(B);
+    for (int i = 0; i < k; ++i) {
+        for (int b = 0; b < B; ++b) l[b] = lam[(size_t)b * k + i];
+        ED_CUDA(cudaMemcpyAsync(dl.p, l.data(), (size_t)B * 8, cudaMemcpyHostToDevice, st));
+        const double* x = X + (int64_t)i * n * B;
+        batch_block_product(bt, o, x, y.p, st);
+        k_bresid<<<nb, kBT, 0, st>>>(y.p, x, n, B, BP, dl.p, part.p); count_launch();
+        k_bsum<<<(unsigned)((B + 31) / 32), 256, 0, st>>>(part.p, nb, B, 1, s.p, nullptr); count_launch();
+        ED_CUDA(cudaMemcpyAsync(r.data(), s.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        for (int b = 0; b < B; ++b) res[(size_t)b * k + i] = std::sqrt(r[b]);
+    }
 }
 
 // Pick the block-product tile that runs fastest on this data, timed on the
@@ -806,28 +842,35 @@ std::mutex g_tune_mu;
 std::map<std::vector<int64_t>, std::array<int, 4>> g_tune;
 }  // namespace
 
-void batch_autotune(ed_batch& bt, cudaStream_t st)
+namespace {
+
+// Problem counts share a tile choice within a power-of-two bucket (at least 4).
+int tile_bucket(int B)
+{
+    int b = 4;
+    while (b < B) b <<= 1;
+    return b;
+}
+
+// The fastest block-product tile for operands like o (o.B problems), timed
+// on the first rows of the pattern and remembered per (device, bucket of
+// o.B, hop types, mean row length).  Never call it during stream capture.
+std::array<int, 4> tune_tile(const ed_batch& bt, const BlockOperands& o, cudaStream_t st)
 {
     int dev = 0;
     ED_CUDA(cudaGetDevice(&dev));
     const int64_t mean_len = bt.n ? (bt.nnz + bt.n / 2) / bt.n : 0;
-    const std::vector<int64_t> key{dev, bt.B, bt.nhop, mean_len / 8};
+    const std::vector<int64_t> key{dev, tile_bucket(o.B), bt.nhop, mean_len / 8};
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tune.find(key);
-        if (it != g_tune.end()) {
-            bt.tb = it->second[0];
-            bt.unroll = it->second[1];
-            bt.nt = it->second[2];
-            bt.l1 = it->second[3];
-            return;
-        }
+        if (it != g_tune.end()) return it->second;
     }
     const char* verbose_env = std::getenv("ED_TUNE_VERBOSE");
     const bool verbose = verbose_env && verbose_env[0] == '1';
     const int64_t rows = std::min<int64_t>(bt.n, 65536);
-    DevBuf<double> X((size_t)bt.n * bt.B), Y((size_t)bt.n * bt.B);
-    k_brandom<<<sms_b() * 4, 256, 0, st>>>(X.p, bt.n * bt.B, 7); count_launch();
+    DevBuf<double> X((size_t)bt.n * o.B), Y((size_t)bt.n * o.B);
+    k_brandom<<<sms_b() * 4, 256, 0, st>>>(X.p, bt.n * o.B, 7); count_launch();
     cudaEvent_t a, b;
     ED_CUDA(cudaEventCreate(&a));
     ED_CUDA(cudaEventCreate(&b));
@@ -836,26 +879,26 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
     std::vector<std::array<int, 4>> cands;
     for (int tb : {4, 8, 16}) {
         const size_t smem = (size_t)bt.nhop * tb * 8;
-        if (smem > kSmemOptIn || (tb > 4 && bt.B <= tb / 2)) continue;
+        if (smem > kSmemOptIn || (tb > 4 && o.B <= tb / 2)) continue;
         for (int u : {4, 8}) {
             if (smem <= 110 * 1024) cands.push_back({tb, u, 256, 0});   // two or more CTAs per SM
             if (smem > 56 * 1024) cands.push_back({tb, u, 1024, 0});    // one large CTA per SM
         }
     }
     for (int tb : {16, 32}) {
-        if (bt.B <= tb / 2) continue;
+        if (o.B <= tb / 2) continue;
         for (int u : {4, 8}) cands.push_back({tb, u, 256, 1});
     }
     for (const auto& c : cands) {
-        bspmm_variant(bt, full_operands(bt), c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
+        bspmm_variant(bt, o, c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
         ED_CUDA(cudaEventRecord(a, st));
-        for (int r = 0; r < 3; ++r) bspmm_variant(bt, full_operands(bt), c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
+        for (int r = 0; r < 3; ++r) bspmm_variant(bt, o, c[0], c[1], c[2], c[3], X.p, Y.p, rows, st);
         ED_CUDA(cudaEventRecord(b, st));
         ED_CUDA(cudaEventSynchronize(b));
         float ms = 0.f;
         ED_CUDA(cudaEventElapsedTime(&ms, a, b));
         if (verbose)
-            std::fprintf(stderr, "ed_batch tune: B=%d tb=%d unroll=%d threads=%d l1=%d rows=%lld  %.4f ms\n", bt.B, c[0],
+            std::fprintf(stderr, "ed_batch tune: B=%d tb=%d unroll=%d threads=%d l1=%d rows=%lld  %.4f ms\n", o.B, c[0],
                          c[1], c[2], c[3], (long long)rows, ms / 3);
         if (ms < best) {
             best = ms;
@@ -864,12 +907,27 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[key] = pick;
+    return pick;
+}
+
+}  // namespace
+
+void batch_autotune(ed_batch& bt, cudaStream_t st)
+{
+    const std::array<int, 4> pick = tune_tile(bt, full_operands(bt), st);
     bt.tb = pick[0];
     bt.unroll = pick[1];
     bt.nt = pick[2];
     bt.l1 = pick[3];
-    std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tune[key] = pick;
+    bt.tuned = 1;
+}
+
+std::array<int, 4> batch_tile(const ed_batch& bt, const BlockOperands& o, cudaStream_t st)
+{
+    if (o.B == bt.B || !bt.tuned) return {bt.tb, bt.unroll, bt.nt, bt.l1};
+    return tune_tile(bt, o, st);
 }
 
 // Lockstep thick-restart Lanczos for the B problems of a batch: the
@@ -883,12 +941,12 @@ void batch_autotune(ed_batch& bt, cudaStream_t st)
 // ED_ERR_BREAKDOWN for the batch; such a problem is solved with ed_lanczos.
 // A restart cycle runs without host round trips and is replayed as a CUDA
 // graph on the solver's own stream.
-void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V0, double* evals, double* evecs,
-                 ed_batch_info* info, cudaStream_t caller_stream)
+void batch_solve(const ed_batch& bt, const int* sel, int nsel, const ed_lanczos_params& p, const double* V0,
+                 double* evals, double* evecs, ed_batch_info* info, cudaStream_t caller_stream)
 {
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t n = bt.n;
-    const int B0 = bt.B;
+    const int B0 = sel ? nsel : bt.B;
     const int nev = p.nev;
     ED_REQUIRE(nev >= 1 && nev + 2 < n, ED_ERR_ARG, "need 1 <= nev < n - 2");
     const double tol = p.tol > 0 ? p.tol : 1e-10;
@@ -927,7 +985,11 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     auto set_bp = [&]() { BP = 1; while (BP < B) BP <<= 1; };
     set_bp();
     std::vector<int> orig = ident;
-    BlockOperands ops = full_operands(bt);
+    // the selected problems' operands (gathered once), or the whole batch's
+    DevBuf<double> wsel, dsel;
+    const BlockOperands ops0 = sel ? gather_operands(bt, sel, nsel, wsel, dsel, st) : full_operands(bt);
+    BlockOperands ops = ops0;
+    std::array<int, 4> tile = batch_tile(bt, ops, st);
     int64_t vs = vs0;
 
     auto grid_for = [&](int64_t work) { return (int)std::max<int64_t>(1, std::min<int64_t>(sms_b() * 8, (work + 255) / 256)); };
@@ -951,10 +1013,10 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     }
     ed_batch_info inf;
     std::memset(&inf, 0, sizeof(inf));
-    inf.tile_hamiltonians = bt.tb;
-    inf.tile_l1 = bt.l1;
-    inf.tile_unroll = bt.unroll;
-    inf.tile_threads = bt.l1 ? 256 : bt.nt;
+    inf.tile_hamiltonians = tile[0];
+    inf.tile_l1 = tile[3];
+    inf.tile_unroll = tile[1];
+    inf.tile_threads = tile[3] ? 256 : tile[2];
     std::vector<std::vector<double>> T(B0, std::vector<double>((size_t)m * m, 0.0)), theta(B0), Y(B0);
     std::vector<double> coef_h((size_t)m * (m + 1) * B0), beta_h((size_t)(m + 1) * B0), Yall((size_t)B0 * m * m);
     std::vector<int> brk_h(B0);
@@ -974,7 +1036,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
         ED_CUDA(cudaMemcpyAsync(Yd.p, Yall.data(), (size_t)m * m * B * 8, cudaMemcpyHostToDevice, st));
     };
     // output eigenvectors: [i][r][original index], i < nev
-    DevBuf<double> xtmp, ytmp;
+    DevBuf<double> xtmp;
     double* X = evecs;
     if (!X && p.verify) {
         xtmp.alloc((size_t)vs0 * nev);
@@ -1002,7 +1064,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
             const bool first = (j == k);
             if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j], st, cudaEventRecordExternal));
             else ED_CUDA(cudaEventRecord(ev[2 * j], st));
-            bspmm_variant(bt, ops, bt.tb, bt.unroll, bt.nt, bt.l1, vj, w, n, st);
+            bspmm_variant(bt, ops, tile[0], tile[1], tile[2], tile[3], vj, w, n, st);
             if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j + 1], st, cudaEventRecordExternal));
             else ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
             if (!first) {
@@ -1158,6 +1220,7 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
             count_launch();
             ED_CUDA(cudaGetLastError());
             ops = {wc[nxt].p, dc[nxt].p, Bn};
+            tile = batch_tile(bt, ops, st);
             std::vector<int> no(Bn);
             for (int q = 0; q < Bn; ++q) no[q] = orig[live[q]];
             orig = no;
@@ -1192,33 +1255,22 @@ void batch_solve(const ed_batch& bt, const ed_lanczos_params& p, const double* V
     for (int b = 0; b < B0; ++b)
         for (int i = 0; i < nev; ++i) evals[(size_t)b * nev + i] = theta[b][i];
     if (p.verify && X) {
-        // true residuals of every Hamiltonian, through the full batch's operator
-        BP = 1;
-        while (BP < B0) BP <<= 1;
-        B = B0;
-        ytmp.alloc((size_t)vs0);
-        std::vector<double> lam(B0), res(B0);
-        DevBuf<double> dl(B0);
+        // true residuals of every problem, through its own operator
+        std::vector<double> res((size_t)B0 * nev);
+        batch_residuals(bt, ops0, X, evals, nev, res.data(), st);
+        inf.block_products += nev;
+        inf.problem_products += (int64_t)nev * B0;
         double worst = 0.0;
         int ok_all = 0;
-        std::vector<char> okb(B0, 1);
-        for (int i = 0; i < nev; ++i) {
-            for (int b = 0; b < B0; ++b) lam[b] = evals[(size_t)b * nev + i];
-            ED_CUDA(cudaMemcpyAsync(dl.p, lam.data(), (size_t)B0 * 8, cudaMemcpyHostToDevice, st));
-            batch_spmm(bt, X + (int64_t)i * vs0, ytmp.p, st);
-            ++inf.block_products;
-            inf.problem_products += B0;
-            k_bresid<<<nb, kBT, 0, st>>>(ytmp.p, X + (int64_t)i * vs0, n, B0, BP, dl.p, part.p); count_launch();
-            bsum(part.p, 1, s2.p, nullptr);
-            ED_CUDA(cudaMemcpyAsync(res.data(), s2.p, (size_t)B0 * 8, cudaMemcpyDeviceToHost, st));
-            ED_CUDA(cudaStreamSynchronize(st));
-            for (int b = 0; b < B0; ++b) {
-                const double r = std::sqrt(res[b]);
+        for (int b = 0; b < B0; ++b) {
+            bool ok = true;
+            for (int i = 0; i < nev; ++i) {
+                const double r = res[(size_t)b * nev + i];
                 worst = std::max(worst, r);
-                if (!(r <= tol)) okb[b] = 0;
+                if (!(r <= tol)) ok = false;
             }
+            ok_all += ok ? 1 : 0;
         }
-        for (int b = 0; b < B0; ++b) ok_all += okb[b];
         inf.max_residual = worst;
         inf.converged = ok_all;
     }
@@ -1283,7 +1335,7 @@ ed_status ed_batch_solve(const ed_batch* bt, const ed_lanczos_params* p, const d
     return guard([&] {
         ED_REQUIRE(bt && p && evals, ED_ERR_ARG, "NULL argument");
         if (info) std::memset(info, 0, sizeof(*info));
-        batch_solve(*bt, *p, V0, evals, evecs, info, nullptr);
+        batch_solve(*bt, nullptr, 0, *p, V0, evals, evecs, info, nullptr);
     });
 }
 

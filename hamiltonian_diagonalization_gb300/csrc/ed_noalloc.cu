@@ -17,9 +17,14 @@
 //    GPU (from several host threads or streams) race and must be serialised
 //    by the caller;
 //  - the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current, so make the first call
-//    before any stream capture.
+//    (cudaGetSymbolAddress) with that device current and keeps it, so make
+//    the first call before any stream capture; a cudaDeviceReset unloads the
+//    module and leaves that address stale, so the entry point must not be
+//    used after one;
+//  - it runs on the legacy default stream, which does not wait for work on
+//    non-blocking streams: x_dev must be complete before the call.
 #include <mutex>
+#include <string>
 
 #include "ed_lanczos.h"
 
@@ -113,6 +118,20 @@ __global__ void k_resid_total(double* __restrict__ scratch, int nb, int k)
 
 }  // namespace
 
+namespace {
+
+// The device on which ptr lives must be the current one: the scratch address
+// and the launch belong to the current device.
+void require_on_device(const void* ptr, int dev, const char* what)
+{
+    cudaPointerAttributes at{};
+    ED_CUDA(cudaPointerGetAttributes(&at, ptr));
+    ED_REQUIRE((at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == dev, ED_ERR_ARG,
+               std::string("ed_residuals_noalloc: ") + what + " is not memory of the current device");
+}
+
+}  // namespace
+
 }  // namespace edgb
 
 using namespace edgb;
@@ -120,7 +139,7 @@ using namespace edgb;
 extern "C" ed_status ed_residuals_noalloc(const ed_op* op, const double* x_dev, const double* lambda_host, int k,
                                           double* res_host)
 {
-    try {
+    return guard([&] {
         ED_REQUIRE(op && x_dev && lambda_host && res_host, ED_ERR_ARG, "NULL argument");
         ED_REQUIRE(k >= 1 && k <= kNoallocMaxVectors, ED_ERR_ARG,
                    "ed_residuals_noalloc takes 1..64 vectors per call");
@@ -128,12 +147,14 @@ extern "C" ed_status ed_residuals_noalloc(const ed_op* op, const double* x_dev, 
                    "ed_residuals_noalloc needs a stored full-storage CRS operator");
         const ed_crs& a = *op->crs;
         ED_REQUIRE(a.n >= 1, ED_ERR_EMPTY, "operator has dimension 0");
+        int dev = 0, sms = 148;
+        ED_CUDA(cudaGetDevice(&dev));
+        require_on_device(a.val.p, dev, "the operator's CRS");
+        require_on_device(x_dev, dev, "x_dev");
         double* scratch = scratch_for_current_device();
         // eigenvalues go through the tail of the scratch array (no buffer of our own)
         double* lam_dev = scratch + (int64_t)kNoallocMaxVectors * kNoallocMaxBlocks;
         ED_CUDA(cudaMemcpyAsync(lam_dev, lambda_host, (size_t)k * 8, cudaMemcpyHostToDevice, nullptr));
-        int dev = 0, sms = 148;
-        ED_CUDA(cudaGetDevice(&dev));
         ED_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         int64_t nb = a.n / 2048;
         if (nb > (int64_t)sms * 4) nb = (int64_t)sms * 4;
@@ -152,12 +173,5 @@ extern "C" ed_status ed_residuals_noalloc(const ed_op* op, const double* x_dev, 
         ED_CUDA(cudaGetLastError());
         ED_CUDA(cudaMemcpyAsync(res_host, lam_dev, (size_t)k * 8, cudaMemcpyDeviceToHost, nullptr));
         ED_CUDA(cudaStreamSynchronize(nullptr));
-        return ED_OK;
-    } catch (const Error& e) {
-        set_last_error(e.what());
-        return e.code;
-    } catch (...) {
-        set_last_error("ed_residuals_noalloc: unexpected failure");
-        return ED_ERR_INTERNAL;
-    }
+    });
 }

@@ -8,7 +8,7 @@
 // at HBM rate (12 bytes per nonzero) demands, so the kernels spend FP64
 // instructions only on the products: a row is owned by G lanes (G = 4 or 8
 // for the model's 200-350 nonzeros per row), each lane accumulates its share
-// serially into two chains, and only log2(G) shuffle additions per lane
+// serially into one FMA chain, and only log2(G) shuffle additions per lane
 // remain.  Column and value streams are read once with evict-first loads so
 // that x stays resident in L2.
 #include <algorithm>

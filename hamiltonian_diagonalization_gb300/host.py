@@ -1045,25 +1045,79 @@ class HamiltonianBatch:
         check(lib().ed_batch_spmm(self._h, _dptr(X), _dptr(Y), stream))
 
     def solve(self, nev: int, tol: float = 1e-10, V0=None, seed: int = 0, ncv: int = 0, want_vectors: bool = False,
-              verify: bool = True, max_restarts: int = 0):
-        """Lowest nev eigenpairs of every Hamiltonian.  V0: device [n][nham]
-        start vectors (torch tensor) or None.  Returns (evals [nham, nev],
-        evecs device tensor [nev, n, nham] or None, info dict)."""
+              verify: bool = True, max_restarts: int = 0, select=None):
+        """Lowest nev eigenpairs of every Hamiltonian (or of the Hamiltonians
+        listed in select, in that order).  V0: device [n][count] start vectors
+        (torch tensor) or None.  Returns (evals [count, nev], evecs device
+        tensor [nev, n, count] or None, info dict)."""
         p = C.LanczosParams(nev=nev, ncv=ncv, max_restarts=max_restarts, tol=tol, seed=seed,
                             want_vectors=int(want_vectors), verify=int(verify))
         info = C.BatchInfo()
-        ev = np.empty(self.nham * nev)
+        cnt = self.nham if select is None else len(select)
+        ev = np.empty(cnt * nev)
         vec = None
         if want_vectors:
             import torch
-            vec = torch.empty((nev, self.n, self.nham), dtype=torch.float64, device="cuda")
-        check(lib().ed_batch_solve(self._h, ctypes.byref(p), None if V0 is None else _dptr(V0), _f64p(ev),
-                                   None if vec is None else _dptr(vec), ctypes.byref(info)))
-        return ev.reshape(self.nham, nev), vec, info.as_dict()
+            vec = torch.empty((nev, self.n, cnt), dtype=torch.float64, device="cuda")
+        v0p = None if V0 is None else _dptr(V0)
+        vp = None if vec is None else _dptr(vec)
+        if select is None:
+            check(lib().ed_batch_solve(self._h, ctypes.byref(p), v0p, _f64p(ev), vp, ctypes.byref(info)))
+        else:
+            sel = np.ascontiguousarray(select, dtype=np.int32)
+            check(lib().ed_batch_solve_subset(self._h, sel.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(sel),
+                                              ctypes.byref(p), v0p, _f64p(ev), vp, ctypes.byref(info)))
+        return ev.reshape(cnt, nev), vec, info.as_dict()
+
+    def subspace_ritz(self, subspace: "Subspace", nev: int, nchk: int | None = None):
+        """Lowest nev Ritz pairs of every Hamiltonian in the subspace, with the
+        true residual norms of the first nchk (default nev) through the batch's
+        operator.  Returns (evals [nham, nev], X device tensor [nev, n, nham],
+        res [nham, nchk])."""
+        import torch
+        nchk = nev if nchk is None else nchk
+        ev = np.empty(self.nham * nev)
+        res = np.empty(max(1, self.nham * nchk))
+        X = torch.empty((nev, self.n, self.nham), dtype=torch.float64, device="cuda")
+        check(lib().ed_batch_subspace_ritz(self._h, subspace._h, nev, nchk, _f64p(ev), _dptr(X), _f64p(res)))
+        return ev.reshape(self.nham, nev), X, res[:self.nham * nchk].reshape(self.nham, nchk)
 
     def __del__(self):
         if getattr(self, "_h", None) is not None and C._LIB is not None:
             C._LIB.ed_batch_free(self._h)
+            self._h = None
+
+
+class Subspace:
+    """Orthonormal device vectors of one sector shared by the Ritz step of a
+    batch (ed_subspace_*).  No reference counterpart."""
+
+    def __init__(self, n: int, max_dim: int):
+        h = ctypes.c_void_p()
+        check(lib().ed_subspace_create(int(n), int(max_dim), ctypes.byref(h)))
+        self._h = h
+        self.n, self.max_dim = int(n), int(max_dim)
+
+    @property
+    def dim(self) -> int:
+        d = ctypes.c_int()
+        check(lib().ed_subspace_dim(self._h, ctypes.byref(d)))
+        return int(d.value)
+
+    def add(self, U, drop_tol: float = 1e-14) -> int:
+        """Append the columns of a device tensor U [groups, n, width] (the
+        layout of a batch solve's eigenvectors) after Gram-Schmidt; returns how
+        many were kept."""
+        if U.dim() == 2:
+            U = U[None]
+        kept = ctypes.c_int()
+        check(lib().ed_subspace_add(self._h, _dptr(U.contiguous()), int(U.shape[0]), int(U.shape[2]), float(drop_tol),
+                                    ctypes.byref(kept)))
+        return int(kept.value)
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and C._LIB is not None:
+            C._LIB.ed_subspace_free(self._h)
             self._h = None
 
 

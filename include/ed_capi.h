@@ -264,11 +264,15 @@ ed_status ed_residuals(const ed_op* op, const double* x_dev, const double* lambd
  * computes no residuals on a device).  The product is fused into the residual
  * and the only scratch is one file-scope device array of 513 KiB per device,
  * held until the process exits.  Limits: 1..64 vectors per call; a stored CRS
- * with both triangles only (ED_ERR_ARG otherwise).  All calls on a device
- * share that array, so calls that overlap on the GPU race: serialise them.
- * The first call on a device looks up the array's address with that device
- * current; make it before any stream capture.  Runs on the legacy default
- * stream and returns when res_host is filled. */
+ * with both triangles only; the CRS and x_dev on the current device
+ * (ED_ERR_ARG otherwise).  All calls on a device share that array, so calls
+ * that overlap on the GPU race: serialise them.  The first call on a device
+ * looks up the array's address with that device current and keeps it; make
+ * that call before any stream capture, and do not use the entry point after
+ * a cudaDeviceReset (the kept address is then stale).  It runs on the legacy
+ * default stream, which does not wait for non-blocking streams: x_dev must be
+ * complete before the call (synchronise the stream that wrote it).  Returns
+ * when res_host is filled. */
 ed_status ed_residuals_noalloc(const ed_op* op, const double* x_dev, const double* lambda_host, int k,
                                double* res_host);
 
@@ -348,6 +352,35 @@ ed_status ed_batch_spmm(const ed_batch* bt, const double* X_dev, double* Y_dev, 
  * Hamiltonian; evecs_dev (may be NULL): nev consecutive [n][nham] arrays. */
 ed_status ed_batch_solve(const ed_batch* bt, const ed_lanczos_params* p, const double* V0_dev, double* evals_host,
                          double* evecs_dev, ed_batch_info* info);
+/* The same solve for the Hamiltonians sel[0..nsel) of the batch only (no
+ * reference counterpart: the sweep's anchor and fallback solves).  V0_dev:
+ * [n][nsel] or NULL; evals_host: nsel*nev; evecs_dev: nev consecutive
+ * [n][nsel] arrays; both in the selection's order. */
+ed_status ed_batch_solve_subset(const ed_batch* bt, const int* sel, int nsel, const ed_lanczos_params* p,
+                                const double* V0_dev, double* evals_host, double* evecs_dev, ed_batch_info* info);
+
+/* -------------------------- shared-subspace Rayleigh-Ritz (eigenvector continuation)
+ * No reference counterpart: the reference solves every Hamiltonian of a
+ * pseudopotential sweep from scratch.  A subspace is an orthonormal set of up
+ * to 256 device vectors of one sector; ed_batch_subspace_ritz finds every
+ * batch Hamiltonian's lowest Ritz pairs in it and checks them with the
+ * batch's own operator. */
+typedef struct ed_subspace ed_subspace;
+ed_status ed_subspace_create(int64_t n, int max_dim, ed_subspace** out);
+ed_status ed_subspace_free(ed_subspace* sp);
+ed_status ed_subspace_dim(const ed_subspace* sp, int* dim);
+/* Append the columns of U_dev ([groups][n][width], e.g. the eigenvectors of
+ * ed_batch_solve) after two classical Gram-Schmidt passes against the
+ * subspace; a column keeping no more than drop_tol of its norm is dropped.
+ * *kept (may be NULL) = columns appended. */
+ed_status ed_subspace_add(ed_subspace* sp, const double* U_dev, int groups, int width, double drop_tol, int* kept);
+/* Lowest nev Ritz pairs of every Hamiltonian of the batch in the subspace:
+ * evals_host [nham][nev] ascending, X_dev nev consecutive [n][nham] arrays,
+ * res_host [nham][nchk] = ||H_b x - theta x|| of the first nchk pairs through
+ * the batch's block product.  The Hamiltonians must form a linear family of
+ * rank <= 8 (a pseudopotential sweep has rank 2), else ED_ERR_ARG. */
+ed_status ed_batch_subspace_ritz(const ed_batch* bt, const ed_subspace* sp, int nev, int nchk, double* evals_host,
+                                 double* X_dev, double* res_host);
 
 /* ------------------------------------- complex path (optical-flux-lattice model) */
 

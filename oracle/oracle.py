@@ -54,10 +54,12 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref() -> str | None:
-    """Compile oracle/_ref/libref.so from the reference sources, if they are here."""
-    src = os.environ.get("REFSRC", "/root/reference/src")
-    if not os.path.isdir(src):
+def build_ref(src: str | None = None) -> str | None:
+    """Compile oracle/_ref/libref.so from the reference's source directory
+    (src, else the REFSRC environment variable); None when neither names an
+    existing directory."""
+    src = src or os.environ.get("REFSRC")
+    if not src or not os.path.isdir(src):
         return None
     subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFSRC={src}"])
     return REF_PATH

@@ -2,11 +2,12 @@
 
 The reference repository ships no tests or fixtures for this path, so the
 fixtures here are outputs of the reference's primitives, compiled from its
-sources by ``make -C oracle ref`` into oracle/_ref/libref.so (a shim of ours
-calls them through a C ABI).  Run in a container where the reference tree is
-present:
+sources by ``make -C oracle ref REFSRC=<its src directory>`` into
+oracle/_ref/libref.so (a shim of ours calls them through a C ABI).  Run in a
+container where the reference tree is present (REFSRC names its src
+directory; the default is where this build mounts it):
 
-    python tests/golden/make_golden.py
+    REFSRC=/root/reference/src python tests/golden/make_golden.py
 
 Outputs (committed, a few hundred KB):
   ref_primitives.npz  random inputs and the reference's outputs for
@@ -36,6 +37,7 @@ SEED = 20261203
 
 
 def main():
+    O.build_ref(os.environ.get("REFSRC") or "/root/reference/src")
     R = O.ref_lib()
     if R is None:
         raise SystemExit("reference sources not present: cannot build oracle/_ref")
