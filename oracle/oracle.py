@@ -33,6 +33,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_HAM_PATH = os.path.join(HERE, "_ref", "libref_ham.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
 MISS = np.uint64(0xFFFFFFFFFFFFFFFF)
 SPARSE_ZERO_TOL = 1e-14          # hamiltonian_data.hpp:53
@@ -737,10 +738,10 @@ def build_upper2_c(words: np.ndarray, norb0: int, kt0, vt0, kt1, vt1, e0=None, e
 # ------------------------------------------------------------ observables
 
 def density(words: np.ndarray, psi: np.ndarray, norb: int) -> np.ndarray:
-    """rho[k] = sum_s |psi_s|^2 n_k(s): Observables::DensityFunction
+    """rho[k] = sum_s |psi_s|^2 n_k(s) (psi real or complex): Observables::DensityFunction
     (fermion_observables.hpp:48-104), the state loop binning each occupied
     orbital (bit k of the word) with the state's probability."""
-    p = np.asarray(psi, dtype=np.float64) ** 2
+    p = np.abs(np.asarray(psi)) ** 2
     w = np.asarray(words, dtype=np.uint64)
     return np.array([p[((w >> np.uint64(k)) & np.uint64(1)) == 1].sum() for k in range(norb)])
 
@@ -749,7 +750,7 @@ def density_density(words: np.ndarray, psi: np.ndarray, norb: int) -> np.ndarray
     """D[k, q] = sum_s |psi_s|^2 n_k(s) n_q(s): Observables::DensityDensityFunction
     (fermion_observables.hpp:117-200) -- the k = q bin gets n_k^2 = n_k and
     every ordered pair of distinct occupied orbitals its (k, q) bin."""
-    p = np.asarray(psi, dtype=np.float64) ** 2
+    p = np.abs(np.asarray(psi)) ** 2
     w = np.asarray(words, dtype=np.uint64)
     occ = np.stack([((w >> np.uint64(k)) & np.uint64(1)).astype(np.float64) for k in range(norb)], axis=1)
     return (occ * p[:, None]).T @ occ
@@ -759,14 +760,15 @@ def participation_ratio(psi: np.ndarray) -> float:
     """1 / sum_s |psi_s|^4: Observables::GetParticipationRatio
     (fermion_observables.hpp:528-562; the code returns 1/sum, its 1/D factor
     is commented out)."""
-    return 1.0 / float(np.sum(np.abs(np.asarray(psi, dtype=np.float64)) ** 4))
+    return 1.0 / float(np.sum(np.abs(np.asarray(psi)) ** 4))
 
 
 def most_probable(words: np.ndarray, psi: np.ndarray, k: int):
     """The min(k, n) largest |psi_s| in descending order with their words:
     Observables::GetMostProbable (fermion_observables.hpp:437-517) for one
-    eigenvector; ties (unordered in the reference's partial quicksort) by row."""
-    psi = np.asarray(psi, dtype=np.float64)
+    eigenvector (real or complex; ranked by modulus); ties (unordered in the
+    reference's partial quicksort) by row."""
+    psi = np.asarray(psi)
     m = min(int(k), len(psi))
     order = np.lexsort((np.arange(len(psi)), -np.abs(psi)))[:m]
     return np.asarray(words, dtype=np.uint64)[order], psi[order]
@@ -800,3 +802,79 @@ def ref_lib():
     L.ref_lz_ok.restype = ctypes.c_int
     L.ref_lz_ok.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
     return L
+
+
+# ------------------------- pin against the reference's basis, build, observables
+
+def ref_ham_lib():
+    """The reference's own sector basis, quartic build and observables
+    (oracle/_ref/libref_ham.so, built by `make ref` with the reference tree
+    present), or None."""
+    if not os.path.exists(REF_HAM_PATH):
+        try:
+            if build_ref() is None or not os.path.exists(REF_HAM_PATH):
+                return None
+        except Exception:
+            return None
+    L = ctypes.CDLL(REF_HAM_PATH)
+    L.refh_basis.restype = ctypes.c_uint64
+    L.refh_basis.argtypes = [ctypes.c_int] * 3 + [_u64p]
+    L.refh_build_crs_file.restype = ctypes.c_int64
+    L.refh_build_crs_file.argtypes = [ctypes.c_int] * 3 + [_u16p, _f64p, ctypes.c_char_p]
+    L.refh_observables.restype = ctypes.c_int
+    L.refh_observables.argtypes = [ctypes.c_int] * 3 + [_f64p, ctypes.c_int, ctypes.c_int, _f64p, _f64p, _f64p]
+    L.refh_most_probable_complex.restype = ctypes.c_int
+    L.refh_most_probable_complex.argtypes = [ctypes.c_int] * 3 + [_f64p, ctypes.c_int, ctypes.c_int, _u64p, _f64p]
+    return L
+
+
+def ref_basis(R, N: int, norb: int, two_lz: int) -> np.ndarray:
+    """FermionFockBasis::GenerateFockSpace of the reference (fermion_fock_basis.cpp:241-354)."""
+    n = R.refh_basis(N, norb, two_lz, None)
+    w = np.empty(n, dtype=np.uint64)
+    if n:
+        R.refh_basis(N, norb, two_lz, _p(w, _u64p))
+    return w
+
+
+def read_reference_crs(path: str):
+    """A CRS file in the reference's binary format (crs_sparse_matrix.hpp:662-705:
+    uint32 nnz, uint32 rows, int32 row starts, int32 columns, values)."""
+    raw = open(path, "rb").read()
+    nnz, rows = (int(x) for x in np.frombuffer(raw[:8], dtype=np.uint32))
+    o = 8
+    rp = np.frombuffer(raw[o:o + 4 * (rows + 1)], dtype=np.int32).astype(np.int64)
+    o += 4 * (rows + 1)
+    col = np.frombuffer(raw[o:o + 4 * nnz], dtype=np.int32).copy()
+    o += 4 * nnz
+    val = np.frombuffer(raw[o:o + 8 * nnz], dtype=np.float64).copy()
+    return rp, col, val
+
+
+def ref_build_upper(R, N: int, norb: int, two_lz: int, ktab, vtab):
+    """The reference's own SpinlessFermionHamiltonian<double>::Add_CdCdCC_Terms
+    (spinless_fermion_hamiltonian.hpp:282-436) into its mapped storage, trim and
+    CRS conversion, from the given term tables; (rowptr int64, col, val)."""
+    import tempfile
+    kt = np.ascontiguousarray(ktab, dtype=np.uint16)
+    vt = np.ascontiguousarray(vtab, dtype=np.float64)
+    fd, path = tempfile.mkstemp(suffix=".bin")
+    os.close(fd)
+    try:
+        nnz = R.refh_build_crs_file(N, norb, two_lz, _p(kt, _u16p), _p(vt, _f64p), path.encode())
+        if nnz < 0:
+            return None
+        return read_reference_crs(path)
+    finally:
+        os.unlink(path)
+
+
+def crs_digest(rowptr, col, val) -> str:
+    """SHA-256 of a CRS: row pointers as little-endian int64, columns as int32,
+    values as their FP64 bits."""
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(rowptr, dtype="<i8").tobytes())
+    h.update(np.ascontiguousarray(col, dtype="<i4").tobytes())
+    h.update(np.ascontiguousarray(val, dtype="<f8").tobytes())
+    return h.hexdigest()

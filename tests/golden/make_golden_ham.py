@@ -1,0 +1,101 @@
+"""Generate tests/golden/ref_hamiltonians.json from the reference's OWN sector
+basis, quartic Hamiltonian build and observables.
+
+The reference's FermionFockBasis::GenerateFockSpace,
+SpinlessFermionHamiltonian<double>::Add_CdCdCC_Terms (mapped storage, trim,
+CRS conversion) and Observables are compiled from its sources by
+``make -C oracle ref REFSRC=<its src directory>`` into
+oracle/_ref/libref_ham.so (oracle/ref_ham_shim.cpp drives them through a C
+ABI, against the one-rank MPI and compile-only Boost stand-ins in
+oracle/ref_stubs/).  Run where the reference tree is present:
+
+    REFSRC=/root/reference/src python tests/golden/make_golden_ham.py
+
+Outputs (committed):
+  ref_hamiltonians.json
+    crs          per sector and pseudopotential list: dimension, stored
+                 (upper-triangle) elements and the SHA-256 of the reference's
+                 CRS (row pointers as int64, columns as int32, values as FP64
+                 bits), built from the term tables the oracle computes
+    observables  density, density-density and participation ratio of seeded
+                 unit vectors on one sector
+    most_probable  the reference's most probable states and amplitudes of
+                 seeded complex unit vectors (its routine is only sound for
+                 complex vectors)
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle import oracle as O  # noqa: E402
+
+# (N, norb, 2Lz, pseudopotentials): the odd-m LLL Coulomb list, or V1 alone
+CRS_CASES = [(6, 16, 2, "coulomb"), (7, 19, 2, "coulomb"), (8, 22, 0, "coulomb"), (8, 22, 6, "coulomb"),
+             (9, 24, 1, "coulomb"), (10, 28, 0, "coulomb"), (8, 22, 0, "v1"), (9, 24, 1, "v1")]
+OBS_CASE = (8, 22, 0)
+OBS_SEED, OBS_NEV = 11, 2
+MP_CASE = (6, 16, 2)
+MP_SEED, MP_NEV, MP_K = 12, 2, 12
+
+
+def pseudopotentials(kind: str, norb: int) -> np.ndarray:
+    return O.odd_coulomb_list(norb) if kind == "coulomb" else np.array([0.0, 1.0])
+
+
+def seeded_vectors(seed: int, nev: int, n: int, complex_: bool = False) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((nev, n))
+    if complex_:
+        v = v + 1j * rng.standard_normal((nev, n))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def main():
+    O.build_ref(os.environ.get("REFSRC") or "/root/reference/src")
+    R = O.ref_ham_lib()
+    if R is None:
+        raise SystemExit("reference sources not present: cannot build oracle/_ref/libref_ham.so")
+    out = {"crs": {}, "observables": {}, "most_probable": {}}
+    for (N, norb, tlz, kind) in CRS_CASES:
+        kt, vt = O.quartic_tables(norb, pseudopotentials(kind, norb))
+        t0 = time.time()
+        rp, col, val = O.ref_build_upper(R, N, norb, tlz, kt, vt)
+        out["crs"][f"{N}_{norb}_{tlz}_{kind}"] = {"N": N, "norb": norb, "two_lz": tlz, "pseudopotentials": kind,
+                                                 "dim": len(rp) - 1, "nnz_upper": int(rp[-1]),
+                                                 "sha256": O.crs_digest(rp, col, val)}
+        print(N, norb, tlz, kind, len(rp) - 1, int(rp[-1]), f"{time.time() - t0:.1f}s", flush=True)
+    import ctypes
+    f64p = ctypes.POINTER(ctypes.c_double)
+    N, norb, tlz = OBS_CASE
+    n = len(O.ref_basis(R, N, norb, tlz))
+    ev = np.ascontiguousarray(seeded_vectors(OBS_SEED, OBS_NEV, n))
+    obs = []
+    for e in range(OBS_NEV):
+        dens, dd, pr = np.empty(norb), np.empty(norb * norb), np.empty(1)
+        R.refh_observables(N, norb, tlz, ev.ctypes.data_as(f64p), OBS_NEV, e, dens.ctypes.data_as(f64p),
+                           dd.ctypes.data_as(f64p), pr.ctypes.data_as(f64p))
+        obs.append({"density": dens.tolist(), "density_density": dd.tolist(), "participation_ratio": float(pr[0])})
+    out["observables"] = {"N": N, "norb": norb, "two_lz": tlz, "seed": OBS_SEED, "nev": OBS_NEV, "vectors": obs}
+    N, norb, tlz = MP_CASE
+    n = len(O.ref_basis(R, N, norb, tlz))
+    evc = seeded_vectors(MP_SEED, MP_NEV, n, complex_=True)
+    buf = np.ascontiguousarray(np.stack([evc.real, evc.imag], axis=-1).reshape(-1))
+    states = np.empty(MP_K * MP_NEV, dtype=np.uint64)
+    amps = np.empty(2 * MP_K * MP_NEV)
+    R.refh_most_probable_complex(N, norb, tlz, buf.ctypes.data_as(f64p), MP_NEV, MP_K,
+                                 states.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), amps.ctypes.data_as(f64p))
+    out["most_probable"] = {"N": N, "norb": norb, "two_lz": tlz, "seed": MP_SEED, "nev": MP_NEV, "k": MP_K,
+                            "states": [int(x) for x in states], "amplitudes_re": amps[0::2].tolist(),
+                            "amplitudes_im": amps[1::2].tolist()}
+    with open(os.path.join(HERE, "ref_hamiltonians.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -127,3 +127,22 @@ def test_edge_sectors_build_and_products(cuda, oracle, case):
         cuda.cuda.synchronize()
         scale = max(1.0, float(np.abs(yref).max())) if len(yref) else 1.0
         assert np.allclose(yd.cpu().numpy(), yref, rtol=0, atol=1e-13 * scale), kw
+
+
+def test_device_crs_matches_reference_build(cuda, oracle):
+    # the reference's own Add_CdCdCC_Terms (hash accumulation, trim, CRS
+    # conversion), compiled from its sources (tests/golden/make_golden_ham.py):
+    # the device's upper-triangle CRS has the same digest of row pointers,
+    # columns and FP64 value bits, up to the config-2 sector N=10, 2S=27
+    import json
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "ref_hamiltonians.json")
+    gold = json.load(open(path))["crs"]
+    for key, ent in gold.items():
+        N, norb, tlz = ent["N"], ent["norb"], ent["two_lz"]
+        pp = oracle.odd_coulomb_list(norb) if ent["pseudopotentials"] == "coulomb" else np.array([0.0, 1.0])
+        H, _ = build_gpu(N, norb, tlz, pp, upper=True)
+        rp, col, val = H.m_crsSparseMatrix.to_host()
+        assert len(rp) - 1 == ent["dim"] and int(rp[-1]) == ent["nnz_upper"], key
+        assert oracle.crs_digest(rp, col, val) == ent["sha256"], key
+        del H

@@ -82,3 +82,40 @@ def test_laughlin_density_is_uniform(cuda):
     assert abs(H.m_eigenvalues[0]) < 1e-9
     rho = ed.Observables().DensityFunction(H, 0)
     assert np.allclose(rho, N / norb, atol=1e-8), rho
+
+
+def test_observables_match_reference(cuda, oracle):
+    # the reference's own Observables compiled from its sources
+    # (tests/golden/make_golden_ham.py): real seeded vectors for the
+    # reductions, complex ones for the most probable states
+    import json
+    import os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ref_hamiltonians.json")))
+    o = g["observables"]
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(o["N"], o["norb"], o["two_lz"])
+    n = b.GetStoredDimension()
+    rng = np.random.default_rng(o["seed"])
+    ev = rng.standard_normal((o["nev"], n))
+    ev /= np.linalg.norm(ev, axis=1, keepdims=True)
+    for e, ref in enumerate(o["vectors"]):
+        assert np.max(np.abs(ed.Observables.density_of_vector(b, ev[e]) - ref["density"])) <= 1e-13
+        dd = ed.Observables.density_density_of_vector(b, ev[e]).ravel()
+        assert np.max(np.abs(dd - np.array(ref["density_density"]))) <= 1e-13
+        pr = ed.Observables.participation_ratio_of_vector(b, ev[e])
+        assert abs(pr - ref["participation_ratio"]) <= 1e-13 * ref["participation_ratio"]
+    m = g["most_probable"]
+    bm = ed.FermionFockBasis()
+    bm.GenerateFockSpace(m["N"], m["norb"], m["two_lz"])
+    n = bm.GetStoredDimension()
+    rng = np.random.default_rng(m["seed"])
+    v = rng.standard_normal((m["nev"], n))
+    v = v + 1j * rng.standard_normal((m["nev"], n))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    k = m["k"]
+    states = np.array(m["states"], dtype=np.uint64).reshape(m["nev"], k)
+    amps = (np.array(m["amplitudes_re"]) + 1j * np.array(m["amplitudes_im"])).reshape(m["nev"], k)
+    for e in range(m["nev"]):
+        s, a = ed.Observables.most_probable_of_vector(bm, v[e], k)
+        assert np.array_equal(s, states[e])
+        assert np.max(np.abs(a - amps[e])) <= 1e-15

@@ -113,3 +113,86 @@ def test_oracle_against_compiled_reference_random(oracle):
         o2, s2 = oracle.evaluate_cdcdcc(*ks, st, norb)
         assert s2 == s.value and (s2 == 0 or o2 == o)
         assert oracle.next_hamming(st) == R.ref_next_hamming(st)
+
+
+# ------------------------- the reference's own quartic build and observables
+
+@pytest.fixture(scope="module")
+def ref_ham():
+    with open(os.path.join(GOLD, "ref_hamiltonians.json")) as f:
+        return json.load(f)
+
+
+def _pp(oracle, kind, norb):
+    return oracle.odd_coulomb_list(norb) if kind == "coulomb" else np.array([0.0, 1.0])
+
+
+def test_build_upper_matches_reference_crs(oracle, ref_ham):
+    # Add_CdCdCC_Terms (spinless_fermion_hamiltonian.hpp:282-436) with the
+    # reference's hash accumulation, trim and CRS conversion: the oracle's
+    # upper-triangle CRS has the same rows, columns and FP64 value bits
+    for key, ent in ref_ham["crs"].items():
+        N, norb, tlz = ent["N"], ent["norb"], ent["two_lz"]
+        b = oracle.basis(N, norb, tlz)
+        assert len(b) == ent["dim"], key
+        kt, vt = oracle.quartic_tables(norb, _pp(oracle, ent["pseudopotentials"], norb))
+        rp, col, val = oracle.build_upper(b, norb, kt, vt)
+        assert int(rp[-1]) == ent["nnz_upper"], key
+        assert oracle.crs_digest(rp, col, val) == ent["sha256"], key
+
+
+def _seeded(seed, nev, n, complex_=False):
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((nev, n))
+    if complex_:
+        v = v + 1j * rng.standard_normal((nev, n))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def test_observables_match_reference(oracle, ref_ham):
+    # DensityFunction, DensityDensityFunction, GetParticipationRatio
+    # (fermion_observables.hpp:48-200, 528-562) on seeded unit vectors
+    g = ref_ham["observables"]
+    N, norb, tlz = g["N"], g["norb"], g["two_lz"]
+    b = oracle.basis(N, norb, tlz)
+    ev = _seeded(g["seed"], g["nev"], len(b))
+    for e, ref in enumerate(g["vectors"]):
+        d = oracle.density(b, ev[e], norb)
+        assert np.max(np.abs(d - np.array(ref["density"]))) <= 1e-13
+        dd = oracle.density_density(b, ev[e], norb)
+        assert np.max(np.abs(dd.ravel() - np.array(ref["density_density"]))) <= 1e-13
+        pr = oracle.participation_ratio(ev[e])
+        assert abs(pr - ref["participation_ratio"]) <= 1e-13 * ref["participation_ratio"]
+
+
+def test_most_probable_matches_reference_on_complex_vectors(oracle, ref_ham):
+    # GetMostProbable (fermion_observables.hpp:437-517) for complex vectors
+    # (the reference's routine copies complex-sized blocks, so it ranks real
+    # vectors' amplitudes in pairs; the build ranks |psi| as intended)
+    g = ref_ham["most_probable"]
+    N, norb, tlz, k = g["N"], g["norb"], g["two_lz"], g["k"]
+    b = oracle.basis(N, norb, tlz)
+    ev = _seeded(g["seed"], g["nev"], len(b), complex_=True)
+    states = np.array(g["states"], dtype=np.uint64).reshape(g["nev"], k)
+    amps = (np.array(g["amplitudes_re"]) + 1j * np.array(g["amplitudes_im"])).reshape(g["nev"], k)
+    for e in range(g["nev"]):
+        w, a = oracle.most_probable(b, ev[e], k)
+        assert np.array_equal(w, states[e])
+        assert np.max(np.abs(a - amps[e])) <= 1e-15
+
+
+def test_oracle_against_compiled_reference_hamiltonian(oracle):
+    R = oracle.ref_ham_lib()
+    if R is None:
+        pytest.skip("reference sources not present here (the fixtures above pin the oracle)")
+    rng = np.random.default_rng(21)
+    for (N, norb, tlz) in [(5, 14, 1), (6, 17, 0), (7, 18, 3)]:
+        b = oracle.basis(N, norb, tlz)
+        assert np.array_equal(oracle.ref_basis(R, N, norb, tlz), b)
+        pp = oracle.odd_coulomb_list(norb)
+        pp = pp * rng.uniform(0.5, 1.5, len(pp))
+        kt, vt = oracle.quartic_tables(norb, pp)
+        ref = oracle.ref_build_upper(R, N, norb, tlz, kt, vt)
+        got = oracle.build_upper(b, norb, kt, vt)
+        assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
+        assert np.array_equal(ref[2].view(np.uint64), got[2].view(np.uint64))
