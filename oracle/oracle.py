@@ -823,6 +823,10 @@ def ref_ham_lib():
     L.refh_build_crs_file.argtypes = [ctypes.c_int] * 3 + [_u16p, _f64p, ctypes.c_char_p]
     L.refh_observables.restype = ctypes.c_int
     L.refh_observables.argtypes = [ctypes.c_int] * 3 + [_f64p, ctypes.c_int, ctypes.c_int, _f64p, _f64p, _f64p]
+    L.refh2_basis.restype = ctypes.c_uint64
+    L.refh2_basis.argtypes = [ctypes.c_int] * 3 + [_u64p, _u64p]
+    L.refh2_build_crs_file.restype = ctypes.c_int64
+    L.refh2_build_crs_file.argtypes = [ctypes.c_int] * 3 + [_u16p, _f64p, _u16p, _f64p, _f64p, _f64p, ctypes.c_char_p]
     L.refh_most_probable_complex.restype = ctypes.c_int
     L.refh_most_probable_complex.argtypes = [ctypes.c_int] * 3 + [_f64p, ctypes.c_int, ctypes.c_int, _u64p, _f64p]
     return L
@@ -878,3 +882,35 @@ def crs_digest(rowptr, col, val) -> str:
     h.update(np.ascontiguousarray(col, dtype="<i4").tobytes())
     h.update(np.ascontiguousarray(val, dtype="<f8").tobytes())
     return h.hexdigest()
+
+
+def ref_basis2(R, N: int, norb0: int, two_lz: int):
+    """TwoLevelFermionFockBasis::GenerateFockSpace of the reference
+    (two_level_fermion_fock_basis.cpp:289-506); (first, second) words."""
+    n = R.refh2_basis(N, norb0, two_lz, None, None)
+    f = np.empty(n, dtype=np.uint64)
+    s = np.empty(n, dtype=np.uint64)
+    if n:
+        R.refh2_basis(N, norb0, two_lz, _p(f, _u64p), _p(s, _u64p))
+    return f, s
+
+
+def ref_build_upper2(R, N: int, norb0: int, two_lz: int, kt0, vt0, kt1, vt1, e0=None, e1=None):
+    """The reference's own two-level model build (two_level_pseudopotential_model.cpp:190-215:
+    Add_CdC_Terms of each level, then Add_CdCdCC_Terms of level 0 and level 1,
+    two_level_spinless_fermion_hamiltonian.hpp:143-470), trim and CRS conversion."""
+    import tempfile
+    a = [np.ascontiguousarray(x, dtype=t) for x, t in ((kt0, np.uint16), (vt0, np.float64), (kt1, np.uint16),
+                                                         (vt1, np.float64))]
+    e = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (e0, e1)]
+    fd, path = tempfile.mkstemp(suffix=".bin")
+    os.close(fd)
+    try:
+        nnz = R.refh2_build_crs_file(N, norb0, two_lz, _p(a[0], _u16p), _p(a[1], _f64p), _p(a[2], _u16p),
+                                     _p(a[3], _f64p), None if e[0] is None else _p(e[0], _f64p),
+                                     None if e[1] is None else _p(e[1], _f64p), path.encode())
+        if nnz < 0:
+            return None
+        return read_reference_crs(path)
+    finally:
+        os.unlink(path)

@@ -33,6 +33,9 @@
 #include "observables/fermion_observables.hpp"
 #include "fqhe_sphere/pseudopotential_model/angular_momentum_constraint.hpp"
 #include "fqhe_sphere/pseudopotential_model/term_tables.hpp"
+#include "basis/two_level_fermion_fock_basis.hpp"
+#include "hamiltonians/two_level_spinless_fermion_hamiltonian.hpp"
+#include "fqhe_sphere/pseudopotential_model/two_level_angular_momentum_constraint.hpp"
 
 // The reference defines its output-verbosity object in each program's main
 // file; this shim is such a program.
@@ -66,6 +69,25 @@ struct RefHamiltonian : diagonalization::SpinlessFermionHamiltonian<double> {
         this->ResetMatrixStorageMethod(utilities::_SPARSE_CRS_, diagonalization::_PARALLEL_, mpi);
     }
 };
+
+struct RefTwoLevelHamiltonian : diagonalization::TwoLevelSpinlessFermionHamiltonian<double> {
+    void ToCrs(utilities::MpiWrapper& mpi)
+    {
+        this->ResetMatrixStorageMethod(utilities::_SPARSE_CRS_, diagonalization::_PARALLEL_, mpi);
+    }
+};
+
+// The reference's two-level sector basis
+// (two_level_pseudopotential_model.cpp:114-145): norb0 lowest-level orbitals
+// and norb0 + 2 in the second level, maxLz2 = norb0 + 1.
+bool make_basis2(int N, int norb0, int twoLz, diagonalization::TwoLevelFermionFockBasis& basis)
+{
+    utilities::MpiWrapper& mpi = session();
+    const diagonalization::mState_t lz = (diagonalization::mState_t)twoLz;
+    const diagonalization::mState_t maxLz2 = (diagonalization::mState_t)(norb0 + 1);
+    return basis.GenerateFockSpace(N, norb0, norb0 + 2, std::bind(&diagonalization::TestAngularMomentumSector2LL,
+                                                                  std::placeholders::_1, lz, maxLz2), mpi);
+}
 
 // The reference's sector basis: 2Lz in twice units, maxLz = 2S = norb - 1.
 bool make_basis(int N, int norb, int twoLz, diagonalization::FermionFockBasis& basis)
@@ -116,6 +138,64 @@ int64_t refh_build_crs_file(int N, int norb, int twoLz, const uint16_t* ktab, co
     H.SetFockBasis(basis);
     H.Initialize(N, norb, utilities::_SPARSE_MAPPED_, mpi);
     H.Add_CdCdCC_Terms(&tables, 0, H.m_data.m_fockSpaceDim, mpi);
+    H.ToCrs(mpi);
+    H.m_crsSparseMatrix.ToFile(std::string(path), io::_BINARY_, mpi);
+    return (int64_t)H.m_crsSparseMatrix.GetNbrNonZeros();
+}
+
+// The reference's two-level basis (two_level_fermion_fock_basis.cpp:289-506):
+// dimension, and the (first, second) words when the buffers are given.
+uint64_t refh2_basis(int N, int norb0, int twoLz, uint64_t* first, uint64_t* second)
+{
+    diagonalization::TwoLevelFermionFockBasis basis;
+    if (make_basis2(N, norb0, twoLz, basis)) return 0;
+    const uint64_t dim = basis.GetStoredDimension();
+    if (first && second) {
+        std::vector<diagonalization::TwoLevelFockState>::const_iterator it;
+        basis.GetFirstState(0, it);
+        for (uint64_t i = 0; i < dim; ++i, basis.GetNextState(it)) {
+            first[i] = it->m_first;
+            second[i] = it->m_second;
+        }
+    }
+    return dim;
+}
+
+// The two-level model's Hamiltonian (two_level_pseudopotential_model.cpp:190-215):
+// occupation energies of each level (e0: norb0 values, e1: norb0 + 2; either
+// may be NULL), then the quartic terms of level 0 and of level 1 from their
+// tables, mapped storage, trim, CRS; written to path in the reference's binary
+// CRS format.  Returns the stored elements, or -1 for an empty sector.
+int64_t refh2_build_crs_file(int N, int norb0, int twoLz, const uint16_t* kt0, const double* vt0, const uint16_t* kt1,
+                             const double* vt1, const double* e0, const double* e1, const char* path)
+{
+    utilities::MpiWrapper& mpi = session();
+    diagonalization::TwoLevelFermionFockBasis basis;
+    if (make_basis2(N, norb0, twoLz, basis)) return -1;
+    diagonalization::QuarticTermTables q0, q1;
+    q0.Initialize(norb0, mpi);
+    q1.Initialize(norb0 + 2, mpi);
+    std::memcpy(q0.GetKTable()->data(), kt0, q0.GetKTable()->size() * sizeof(diagonalization::kState_t));
+    std::memcpy(q0.GetVTable()->data(), vt0, q0.GetVTable()->size() * sizeof(double));
+    std::memcpy(q1.GetKTable()->data(), kt1, q1.GetKTable()->size() * sizeof(diagonalization::kState_t));
+    std::memcpy(q1.GetVTable()->data(), vt1, q1.GetVTable()->size() * sizeof(double));
+    diagonalization::QuadraticTermTables c0, c1;
+    RefTwoLevelHamiltonian H;
+    H.SetFockBasis(basis);
+    H.Initialize(N, 2 * norb0 + 2, utilities::_SPARSE_MAPPED_, mpi);
+    const uint64_t dim = H.m_data.m_fockSpaceDim;
+    if (e0) {
+        c0.Initialize(norb0, mpi);
+        std::memcpy(c0.GetVTable()->data(), e0, sizeof(double) * norb0);
+        H.Add_CdC_Terms(&c0, 0, 0, 0, dim, mpi);
+    }
+    if (e1) {
+        c1.Initialize(norb0 + 2, mpi);
+        std::memcpy(c1.GetVTable()->data(), e1, sizeof(double) * (norb0 + 2));
+        H.Add_CdC_Terms(&c1, 1, 1, 0, dim, mpi);
+    }
+    H.Add_CdCdCC_Terms(&q0, 0, 0, 0, 0, 0, dim, mpi);
+    H.Add_CdCdCC_Terms(&q1, 1, 1, 1, 1, 0, dim, mpi);
     H.ToCrs(mpi);
     H.m_crsSparseMatrix.ToFile(std::string(path), io::_BINARY_, mpi);
     return (int64_t)H.m_crsSparseMatrix.GetNbrNonZeros();

@@ -17,6 +17,7 @@ Outputs (committed):
                  (upper-triangle) elements and the SHA-256 of the reference's
                  CRS (row pointers as int64, columns as int32, values as FP64
                  bits), built from the term tables the oracle computes
+    crs_two_level  the same for the two-Landau-level model's build
     observables  density, density-density and participation ratio of seeded
                  unit vectors on one sector
     most_probable  the reference's most probable states and amplitudes of
@@ -38,6 +39,10 @@ from oracle import oracle as O  # noqa: E402
 # (N, norb, 2Lz, pseudopotentials): the odd-m LLL Coulomb list, or V1 alone
 CRS_CASES = [(6, 16, 2, "coulomb"), (7, 19, 2, "coulomb"), (8, 22, 0, "coulomb"), (8, 22, 6, "coulomb"),
              (9, 24, 1, "coulomb"), (10, 28, 0, "coulomb"), (8, 22, 0, "v1"), (9, 24, 1, "v1")]
+# two Landau levels (N, norb0, 2Lz, with occupation energies): odd-m Coulomb
+# lists for each level's tables, energies linspace(-0.3, 0.2, norb0) and
+# linspace(0.9, 1.4, norb0 + 2)
+CRS2_CASES = [(4, 6, 0, True), (5, 8, 1, True), (6, 10, 0, False), (6, 10, 2, True), (7, 12, 1, True)]
 OBS_CASE = (8, 22, 0)
 OBS_SEED, OBS_NEV = 11, 2
 MP_CASE = (6, 16, 2)
@@ -70,6 +75,18 @@ def main():
                                                  "dim": len(rp) - 1, "nnz_upper": int(rp[-1]),
                                                  "sha256": O.crs_digest(rp, col, val)}
         print(N, norb, tlz, kind, len(rp) - 1, int(rp[-1]), f"{time.time() - t0:.1f}s", flush=True)
+    out["crs_two_level"] = {}
+    for (N, norb0, tlz, en) in CRS2_CASES:
+        kt0, vt0 = O.quartic_tables(norb0, O.odd_coulomb_list(norb0))
+        kt1, vt1 = O.quartic_tables(norb0 + 2, O.odd_coulomb_list(norb0 + 2))
+        e0 = np.linspace(-0.3, 0.2, norb0) if en else None
+        e1 = np.linspace(0.9, 1.4, norb0 + 2) if en else None
+        t0 = time.time()
+        rp, col, val = O.ref_build_upper2(R, N, norb0, tlz, kt0, vt0, kt1, vt1, e0, e1)
+        out["crs_two_level"][f"{N}_{norb0}_{tlz}_{int(en)}"] = {
+            "N": N, "norb0": norb0, "two_lz": tlz, "energies": en, "dim": len(rp) - 1, "nnz_upper": int(rp[-1]),
+            "sha256": O.crs_digest(rp, col, val)}
+        print("two-level", N, norb0, tlz, en, len(rp) - 1, int(rp[-1]), f"{time.time() - t0:.1f}s", flush=True)
     import ctypes
     f64p = ctypes.POINTER(ctypes.c_double)
     N, norb, tlz = OBS_CASE

@@ -160,3 +160,23 @@ def test_ladder_solve_refuses_a_one_level_basis(cuda, oracle):
         assert st == _capi.ED_ERR_ARG
     finally:
         ed.lib().ed_op_free(op)
+
+
+def test_device_crs_matches_reference_build(cuda, oracle):
+    # the reference's own two-level model build (its TwoLevelFermionFockBasis
+    # and TwoLevelSpinlessFermionHamiltonian compiled from its sources,
+    # tests/golden/make_golden_ham.py): same digest of row pointers, columns
+    # and FP64 value bits
+    import json
+    import os
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ref_hamiltonians.json")))
+    for key, ent in gold["crs_two_level"].items():
+        N, norb0, tlz = ent["N"], ent["norb0"], ent["two_lz"]
+        t0 = ed.QuarticTermTables(norb0, oracle.odd_coulomb_list(norb0))
+        t1 = ed.QuarticTermTables(norb0 + 2, oracle.odd_coulomb_list(norb0 + 2))
+        e0 = np.linspace(-0.3, 0.2, norb0) if ent["energies"] else None
+        e1 = np.linspace(0.9, 1.4, norb0 + 2) if ent["energies"] else None
+        H = build(N, norb0, tlz, t0, t1, e0, e1, upper=True)
+        rp, col, val = H.m_crsSparseMatrix.to_host()
+        assert len(rp) - 1 == ent["dim"] and int(rp[-1]) == ent["nnz_upper"], key
+        assert oracle.crs_digest(rp, col, val) == ent["sha256"], key

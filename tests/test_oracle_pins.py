@@ -196,3 +196,38 @@ def test_oracle_against_compiled_reference_hamiltonian(oracle):
         got = oracle.build_upper(b, norb, kt, vt)
         assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
         assert np.array_equal(ref[2].view(np.uint64), got[2].view(np.uint64))
+
+
+def test_two_level_build_matches_reference_crs(oracle, ref_ham):
+    # the two-level model's build (two_level_pseudopotential_model.cpp:190-215)
+    for key, ent in ref_ham["crs_two_level"].items():
+        N, norb0, tlz = ent["N"], ent["norb0"], ent["two_lz"]
+        f, s = oracle.basis2(N, norb0, tlz)
+        assert len(f) == ent["dim"], key
+        kt0, vt0 = oracle.quartic_tables(norb0, oracle.odd_coulomb_list(norb0))
+        kt1, vt1 = oracle.quartic_tables(norb0 + 2, oracle.odd_coulomb_list(norb0 + 2))
+        e0 = np.linspace(-0.3, 0.2, norb0) if ent["energies"] else None
+        e1 = np.linspace(0.9, 1.4, norb0 + 2) if ent["energies"] else None
+        rp, col, val = oracle.build_upper2(f, s, norb0, kt0, vt0, kt1, vt1, e0, e1)
+        assert int(rp[-1]) == ent["nnz_upper"], key
+        assert oracle.crs_digest(rp, col, val) == ent["sha256"], key
+
+
+def test_two_level_oracle_against_compiled_reference(oracle):
+    R = oracle.ref_ham_lib()
+    if R is None:
+        pytest.skip("reference sources not present here (the fixtures above pin the oracle)")
+    rng = np.random.default_rng(5)
+    for (N, norb0, tlz) in [(3, 5, 0), (5, 7, 2), (5, 9, 2)]:
+        f, s = oracle.basis2(N, norb0, tlz)
+        rf, rs = oracle.ref_basis2(R, N, norb0, tlz)
+        assert np.array_equal(f, rf) and np.array_equal(s, rs)
+        p0 = oracle.odd_coulomb_list(norb0) * rng.uniform(0.5, 1.5, norb0 - 1)
+        p1 = oracle.odd_coulomb_list(norb0 + 2) * rng.uniform(0.5, 1.5, norb0 + 1)
+        kt0, vt0 = oracle.quartic_tables(norb0, p0)
+        kt1, vt1 = oracle.quartic_tables(norb0 + 2, p1)
+        e0, e1 = rng.uniform(-1, 1, norb0), rng.uniform(0, 2, norb0 + 2)
+        ref = oracle.ref_build_upper2(R, N, norb0, tlz, kt0, vt0, kt1, vt1, e0, e1)
+        got = oracle.build_upper2(f, s, norb0, kt0, vt0, kt1, vt1, e0, e1)
+        assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
+        assert np.array_equal(ref[2].view(np.uint64), got[2].view(np.uint64))
