@@ -34,6 +34,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_HAM_PATH = os.path.join(HERE, "_ref", "libref_ham.so")
+REF_OFL_PATH = os.path.join(HERE, "_ref", "libref_ofl.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
 MISS = np.uint64(0xFFFFFFFFFFFFFFFF)
 SPARSE_ZERO_TOL = 1e-14          # hamiltonian_data.hpp:53
@@ -914,3 +915,58 @@ def ref_build_upper2(R, N: int, norb0: int, two_lz: int, kt0, vt0, kt1, vt1, e0=
         return read_reference_crs(path)
     finally:
         os.unlink(path)
+
+
+def ref_ofl_lib():
+    """The reference's own momentum-sector basis and complex optical-flux-lattice
+    build (oracle/_ref/libref_ofl.so), or None."""
+    if not os.path.exists(REF_OFL_PATH):
+        try:
+            if build_ref() is None or not os.path.exists(REF_OFL_PATH):
+                return None
+        except Exception:
+            return None
+    L = ctypes.CDLL(REF_OFL_PATH)
+    L.refo_basis.restype = ctypes.c_uint64
+    L.refo_basis.argtypes = [ctypes.c_int] * 5 + [_u64p]
+    L.refo_build_crs_file.restype = ctypes.c_int64
+    L.refo_build_crs_file.argtypes = [ctypes.c_int] * 5 + [_u16p, _f64p, _f64p, ctypes.c_char_p]
+    return L
+
+
+def ref_basis_momentum(R, N: int, X: int, Y: int, kx: int, ky: int) -> np.ndarray:
+    """The reference's momentum-sector basis (interacting_ofl_model.cpp:990-1000)."""
+    n = R.refo_basis(N, X, Y, kx, ky, None)
+    w = np.empty(n, dtype=np.uint64)
+    if n:
+        R.refo_basis(N, X, Y, kx, ky, _p(w, _u64p))
+    return w
+
+
+def ref_build_upper_complex(R, N: int, X: int, Y: int, kx: int, ky: int, ktab, vtab, energies=None):
+    """The reference's own complex build from array-format tables
+    (interacting_ofl_model.cpp:1034-1052: Add_CdC_Terms, Add_CdCdCC_Terms of
+    SpinlessFermionHamiltonian<dcmplx>), trim and CRS conversion;
+    (rowptr int64, col, complex values)."""
+    import tempfile
+    kt = np.ascontiguousarray(ktab, dtype=np.uint16)
+    vt = np.ascontiguousarray(vtab, dtype=np.complex128).view(np.float64)
+    e = None if energies is None else np.ascontiguousarray(energies, dtype=np.complex128).view(np.float64)
+    fd, path = tempfile.mkstemp(suffix=".bin")
+    os.close(fd)
+    try:
+        nnz = R.refo_build_crs_file(N, X, Y, kx, ky, _p(kt, _u16p), _p(vt, _f64p),
+                                    None if e is None else _p(e, _f64p), path.encode())
+        if nnz < 0:
+            return None
+        raw = open(path, "rb").read()
+    finally:
+        os.unlink(path)
+    nnz, rows = (int(x) for x in np.frombuffer(raw[:8], dtype=np.uint32))
+    o = 8
+    rp = np.frombuffer(raw[o:o + 4 * (rows + 1)], dtype=np.int32).astype(np.int64)
+    o += 4 * (rows + 1)
+    col = np.frombuffer(raw[o:o + 4 * nnz], dtype=np.int32).copy()
+    o += 4 * nnz
+    val = np.frombuffer(raw[o:o + 16 * nnz], dtype=np.complex128).copy()
+    return rp, col, val

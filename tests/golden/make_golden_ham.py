@@ -18,6 +18,8 @@ Outputs (committed):
                  CRS (row pointers as int64, columns as int32, values as FP64
                  bits), built from the term tables the oracle computes
     crs_two_level  the same for the two-Landau-level model's build
+    crs_complex  the same for the optical-flux-lattice model's complex build
+                 (values as (re, im) FP64 bits), on seeded array-format tables
     observables  density, density-density and participation ratio of seeded
                  unit vectors on one sector
     most_probable  the reference's most probable states and amplitudes of
@@ -43,6 +45,11 @@ CRS_CASES = [(6, 16, 2, "coulomb"), (7, 19, 2, "coulomb"), (8, 22, 0, "coulomb")
 # lists for each level's tables, energies linspace(-0.3, 0.2, norb0) and
 # linspace(0.9, 1.4, norb0 + 2)
 CRS2_CASES = [(4, 6, 0, True), (5, 8, 1, True), (6, 10, 0, False), (6, 10, 2, True), (7, 12, 1, True)]
+# optical flux lattice (N, X, Y, kx, ky, with energies): seeded synthetic
+# array-format tables (oracle.ofl_tables, seed X*Y + N), energies
+# linspace(-0.4, 0.6, X*Y) + 1e-3 i k
+CRSC_CASES = [(3, 3, 4, 1, 2, False), (4, 3, 4, 0, 0, True), (5, 4, 4, 2, 1, True), (6, 4, 5, 0, 3, True),
+              (7, 4, 5, 3, 4, True)]
 OBS_CASE = (8, 22, 0)
 OBS_SEED, OBS_NEV = 11, 2
 MP_CASE = (6, 16, 2)
@@ -87,6 +94,18 @@ def main():
             "N": N, "norb0": norb0, "two_lz": tlz, "energies": en, "dim": len(rp) - 1, "nnz_upper": int(rp[-1]),
             "sha256": O.crs_digest(rp, col, val)}
         print("two-level", N, norb0, tlz, en, len(rp) - 1, int(rp[-1]), f"{time.time() - t0:.1f}s", flush=True)
+    Rc = O.ref_ofl_lib()
+    out["crs_complex"] = {}
+    for (N, X, Y, kx, ky, en) in CRSC_CASES:
+        K = X * Y
+        kt, vt = O.ofl_tables(X, Y, K + N)
+        e = (np.linspace(-0.4, 0.6, K) + 1e-3j * np.arange(K)) if en else None
+        t0 = time.time()
+        rp, col, val = O.ref_build_upper_complex(Rc, N, X, Y, kx, ky, kt, vt, e)
+        out["crs_complex"][f"{N}_{X}_{Y}_{kx}_{ky}_{int(en)}"] = {
+            "N": N, "X": X, "Y": Y, "kx": kx, "ky": ky, "energies": en, "dim": len(rp) - 1,
+            "nnz_upper": int(rp[-1]), "sha256": O.crs_digest(rp, col, val.view(np.float64))}
+        print("complex", N, X, Y, kx, ky, en, len(rp) - 1, int(rp[-1]), f"{time.time() - t0:.1f}s", flush=True)
     import ctypes
     f64p = ctypes.POINTER(ctypes.c_double)
     N, norb, tlz = OBS_CASE

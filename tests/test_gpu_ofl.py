@@ -178,3 +178,22 @@ def test_empty_momentum_sector(cuda, oracle):
     assert model.hamiltonian.m_crsSparseMatrix.GetNbrRows() == 0
     assert model.Diagonalize() is False
     assert "dimension 0" in model.hamiltonian.last_error
+
+
+def test_device_crs_matches_reference_build(cuda, oracle):
+    # the reference's own complex build (its SpinlessFermionHamiltonian<dcmplx>,
+    # momentum-sector basis and array-format tables compiled from its sources,
+    # tests/golden/make_golden_ham.py): same digest of the device's CRS
+    import json
+    import os
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ref_hamiltonians.json")))
+    for key, ent in gold["crs_complex"].items():
+        N, X, Y, kx, ky = ent["N"], ent["X"], ent["Y"], ent["kx"], ent["ky"]
+        K = X * Y
+        T = tables(oracle, X, Y, K + N)
+        e = (np.linspace(-0.4, 0.6, K) + 1e-3j * np.arange(K)) if ent["energies"] else None
+        model, empty = build(N, X, Y, kx, ky, T, e, upper=True)
+        assert not empty
+        rp, col, val = model.hamiltonian.m_crsSparseMatrix.to_host()
+        assert len(rp) - 1 == ent["dim"] and int(rp[-1]) == ent["nnz_upper"], key
+        assert oracle.crs_digest(rp, col, np.ascontiguousarray(val).view(np.float64)) == ent["sha256"], key

@@ -231,3 +231,43 @@ def test_two_level_oracle_against_compiled_reference(oracle):
         got = oracle.build_upper2(f, s, norb0, kt0, vt0, kt1, vt1, e0, e1)
         assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
         assert np.array_equal(ref[2].view(np.uint64), got[2].view(np.uint64))
+
+
+def _ofl_case(oracle, ent):
+    N, X, Y = ent["N"], ent["X"], ent["Y"]
+    K = X * Y
+    kt, vt = oracle.ofl_tables(X, Y, K + N)
+    e = (np.linspace(-0.4, 0.6, K) + 1e-3j * np.arange(K)) if ent["energies"] else None
+    return kt, vt, e
+
+
+def test_complex_build_matches_reference_crs(oracle, ref_ham):
+    # the optical-flux-lattice model's complex build (interacting_ofl_model.cpp:
+    # 1034-1052) on seeded array-format tables; the Python loops and their C
+    # port both give the reference's CRS
+    for key, ent in ref_ham["crs_complex"].items():
+        N, X, Y, kx, ky = ent["N"], ent["X"], ent["Y"], ent["kx"], ent["ky"]
+        b = oracle.basis_momentum(N, X, Y, kx, ky)
+        assert len(b) == ent["dim"], key
+        kt, vt, e = _ofl_case(oracle, ent)
+        rp, col, val = oracle.build_upper_complex_c(b, X * Y, kt, vt, e)
+        assert int(rp[-1]) == ent["nnz_upper"], key
+        assert oracle.crs_digest(rp, col, val.view(np.float64)) == ent["sha256"], key
+        if ent["dim"] < 500:
+            rp2, col2, val2 = oracle.build_upper_complex(b, X * Y, kt, vt, e)
+            assert oracle.crs_digest(rp2, col2, np.asarray(val2).view(np.float64)) == ent["sha256"], key
+
+
+def test_complex_oracle_against_compiled_reference(oracle):
+    R = oracle.ref_ofl_lib()
+    if R is None:
+        pytest.skip("reference sources not present here (the fixtures above pin the oracle)")
+    for (N, X, Y, kx, ky) in [(4, 2, 5, 1, 3), (5, 3, 5, 2, 0)]:
+        b = oracle.basis_momentum(N, X, Y, kx, ky)
+        assert np.array_equal(oracle.ref_basis_momentum(R, N, X, Y, kx, ky), b)
+        kt, vt = oracle.ofl_tables(X, Y, 7 * N + X)
+        e = np.linspace(-1.0, 1.0, X * Y) + 0.01j
+        ref = oracle.ref_build_upper_complex(R, N, X, Y, kx, ky, kt, vt, e)
+        got = oracle.build_upper_complex_c(b, X * Y, kt, vt, e)
+        assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
+        assert np.array_equal(ref[2].view(np.uint64), got[2].view(np.uint64))
