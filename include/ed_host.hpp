@@ -9,8 +9,13 @@
 //   utilities::linearAlgebra::ArpackWrapper      utilities/wrappers/arpack_wrapper.hpp:187
 //   utilities::MpiWrapper                        a single-rank stand-in; accepted and ignored
 // Differences, all deliberate:
-//   - GenerateFockSpace takes the Lz sector (twice Lz) instead of a
-//     std::function predicate: the device enumerates the sector directly.
+//   - GenerateFockSpace accepts the reference's predicate (e.g.
+//     std::bind(&TestAngularMomentumSector, _1, twoLz, maxLz)) but the device
+//     enumerates one whole Lz sector: the predicate must select exactly one
+//     (found by evaluating it on a few words of every sector, and checked on
+//     the words built); a predicate that selects several sectors (the
+//     always-true one of a run without block diagonalisation) or splits one
+//     is refused.  The overload taking twice Lz directly is kept.
 //   - MatrixVectorFunction::Simple takes DEVICE vectors (the Krylov basis
 //     lives in HBM).  ArpackWrapper still accepts a host std::function
 //     product, called once per product with host vectors.
@@ -21,6 +26,8 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
+#include <cstdio>
 #include <complex>
 #include <cstdint>
 #include <functional>
@@ -129,23 +136,91 @@ class QuarticTermTables {
     ed_terms* m_h = nullptr;
 };
 
+// angular_momentum_constraint.hpp:41-62: the Lz of a word (twice units, orbital
+// k at 2k - max) equals lzTot.  The predicate the reference binds into
+// GenerateFockSpace; GenerateFockSpace below recognises the sector it selects.
+inline bool TestAngularMomentumSector(const fock_t state, const mState_t lzTot, const mState_t max)
+{
+    int lz = 0;
+    for (fock_t t = state; t; t &= t - 1) {
+        int k = 0;
+        while (!((t >> k) & 1u)) ++k;
+        lz += 2 * k - max;
+    }
+    return lz == lzTot;
+}
+
 class FermionFockBasis {
   public:
     FermionFockBasis() = default;
-    FermionFockBasis(const FermionFockBasis&) = delete;
-    FermionFockBasis& operator=(const FermionFockBasis&) = delete;
-    FermionFockBasis(FermionFockBasis&& o) noexcept : m_basisStored(o.m_basisStored), m_h(o.m_h) { o.m_h = nullptr; }
+    // A copy is the same sector built again on the device (the reference's
+    // SetFockBasis takes the basis by const reference and copies it).
+    FermionFockBasis(const FermionFockBasis& o) { CopyFrom(o); }
+    FermionFockBasis& operator=(const FermionFockBasis& o)
+    {
+        if (this != &o) CopyFrom(o);
+        return *this;
+    }
+    FermionFockBasis(FermionFockBasis&& o) noexcept
+        : m_basisStored(o.m_basisStored), m_h(o.m_h), m_kind(o.m_kind), m_par(o.m_par)
+    {
+        o.m_h = nullptr;
+    }
     FermionFockBasis& operator=(FermionFockBasis&& o) noexcept
     {
         if (this != &o) {
             if (m_h) ed_basis_free(m_h);
             m_h = o.m_h;
             m_basisStored = o.m_basisStored;
+            m_kind = o.m_kind;
+            m_par = o.m_par;
             o.m_h = nullptr;
         }
         return *this;
     }
     ~FermionFockBasis() { if (m_h) ed_basis_free(m_h); }
+
+    // fermion_fock_basis.cpp:241 with the reference's predicate argument: the
+    // Lz sector the predicate selects (see the header notes); true when empty
+    bool GenerateFockSpace(iSize_t nbrParticles, iSize_t nbrOrbitals, const std::function<bool(const fock_t)>& inSector,
+                           utilities::MpiWrapper& mpi)
+    {
+        const int N = (int)nbrParticles, K = (int)nbrOrbitals;
+        if (N < 1 || K < N || K > 64) {
+            std::cerr << "\n\tERROR in GenerateFockSpace: bad particle/orbital numbers" << std::endl;
+            mpi.m_exitFlag = true;
+            throw utilities::EdError(ED_ERR_ARG, "bad particle/orbital numbers");
+        }
+        // position sums S of the N-particle words; 2Lz = 2S - N (K - 1)
+        const int smin = N * (N - 1) / 2, smax = N * (2 * K - N - 1) / 2;
+        std::vector<int> chosen;
+        for (int S = smin; S <= smax; ++S) {
+            int yes = 0, tried = 0;
+            for (fock_t w : SectorWords(N, K, S)) {
+                ++tried;
+                yes += inSector(w) ? 1 : 0;
+            }
+            if (yes != 0 && yes != tried) Refuse(mpi, "the predicate splits an Lz sector; the device builds whole sectors");
+            if (yes) chosen.push_back(S);
+        }
+        if (chosen.size() > 1)
+            Refuse(mpi, "the predicate selects several Lz sectors; the device basis holds one (pass one sector)");
+        if (chosen.empty()) {
+            if (m_h) ed_basis_free(m_h);
+            m_h = nullptr;
+            m_basisStored = true;
+            return true;
+        }
+        const bool empty = GenerateFockSpace(nbrParticles, nbrOrbitals, 2 * chosen[0] - N * (K - 1), mpi);
+        // the words built satisfy the predicate (every word, or an even sample of 100,000)
+        const fock_t n = GetStoredDimension();
+        std::vector<fock_t> w(n);
+        if (n) GetFockBasis(w.data(), n, mpi);
+        const fock_t step = n > 100000 ? n / 100000 : 1;
+        for (fock_t i = 0; i < n; i += step)
+            if (!inSector(w[i])) Refuse(mpi, "a word of the selected sector fails the predicate");
+        return empty;
+    }
 
     // the optical-flux-lattice momentum sector: GenerateFockSpace with
     // TestLinearMomentumSector2 (interacting_ofl_model.cpp:994-1001); true when empty
@@ -158,6 +233,8 @@ class FermionFockBasis {
                                                    nullptr, &m_h),
                            &mpi);
         m_basisStored = true;
+        m_kind = 2;
+        m_par = {(int)nbrParticles, (int)dimX, (int)dimY, (int)kxTot, (int)kyTot};
         return GetStoredDimension() == 0;
     }
 
@@ -168,8 +245,12 @@ class FermionFockBasis {
         m_h = nullptr;
         utilities::EdCheck(ed_basis_build((int)nbrParticles, (int)nbrOrbitals, twoLz, nullptr, &m_h), &mpi);
         m_basisStored = true;
+        m_kind = 1;
+        m_par = {(int)nbrParticles, (int)nbrOrbitals, twoLz, 0, 0};
         return GetStoredDimension() == 0;
     }
+    iSize_t NbrParticles() const { return m_kind ? (iSize_t)m_par[0] : 0; }
+    iSize_t NbrOrbitals() const { return m_kind == 1 ? (iSize_t)m_par[1] : m_kind == 2 ? (iSize_t)(m_par[1] * m_par[2]) : 0; }
     fock_t GetStoredDimension() const
     {
         uint64_t d = 0;
@@ -196,7 +277,75 @@ class FermionFockBasis {
     bool m_basisStored = false;
 
   private:
+    // Up to three words of N particles among K orbitals whose positions sum to
+    // S: the lowest positions with the excess taken by the highest particles,
+    // the highest positions with the deficit taken by the lowest, and a
+    // seeded walk of sum-preserving moves from the first.
+    static std::vector<fock_t> SectorWords(int N, int K, int S)
+    {
+        std::vector<fock_t> out;
+        std::vector<int> lo(N), hi(N);
+        for (int i = 0; i < N; ++i) { lo[i] = i; hi[i] = K - N + i; }
+        int excess = S - N * (N - 1) / 2;
+        for (int i = N - 1; i >= 0 && excess > 0; --i) {
+            const int room = (K - N + i) - lo[i];
+            const int d = room < excess ? room : excess;
+            lo[i] += d;
+            excess -= d;
+        }
+        int deficit = N * (2 * K - N - 1) / 2 - S;
+        for (int i = 0; i < N && deficit > 0; ++i) {
+            const int room = hi[i] - i;
+            const int d = room < deficit ? room : deficit;
+            hi[i] -= d;
+            deficit -= d;
+        }
+        auto word = [](const std::vector<int>& p) {
+            fock_t w = 0;
+            for (int q : p) w |= (fock_t)1 << q;
+            return w;
+        };
+        out.push_back(word(lo));
+        if (word(hi) != out[0]) out.push_back(word(hi));
+        std::vector<int> p = lo;
+        uint64_t r = 0x9E3779B97F4A7C15ull ^ (uint64_t)S;
+        for (int t = 0; t < 64 * N; ++t) {   // move one particle up and another down by one
+            r ^= r << 13; r ^= r >> 7; r ^= r << 17;
+            const int a = (int)(r % (uint64_t)N), b = (int)((r >> 20) % (uint64_t)N);
+            if (a == b) continue;
+            const int up = p[a] + 1, down = p[b] - 1;
+            if (up >= K || down < 0 || up == down) continue;
+            bool clash = false;
+            for (int i = 0; i < N; ++i)
+                if (i != a && i != b && (p[i] == up || p[i] == down)) clash = true;
+            if (clash || up == p[b] || down == p[a]) continue;
+            p[a] = up;
+            p[b] = down;
+        }
+        const fock_t wm = word(p);
+        if (wm != out[0] && (out.size() < 2 || wm != out[1])) out.push_back(wm);
+        return out;
+    }
+    void Refuse(utilities::MpiWrapper& mpi, const char* why)
+    {
+        std::cerr << "\n\tERROR in GenerateFockSpace: " << why << std::endl;
+        mpi.m_exitFlag = true;
+        throw utilities::EdError(ED_ERR_ARG, why);
+    }
+    void CopyFrom(const FermionFockBasis& o)
+    {
+        utilities::MpiWrapper mpi;
+        if (m_h) ed_basis_free(m_h);
+        m_h = nullptr;
+        m_kind = 0;
+        m_basisStored = o.m_basisStored;
+        if (o.m_kind == 1 && o.m_h) GenerateFockSpace(o.m_par[0], o.m_par[1], o.m_par[2], mpi);
+        else if (o.m_kind == 2 && o.m_h) GenerateFockSpaceMomentum(o.m_par[0], o.m_par[1], o.m_par[2], o.m_par[3], o.m_par[4], mpi);
+        m_basisStored = o.m_basisStored;
+    }
     ed_basis* m_h = nullptr;
+    int m_kind = 0;                           // 0 none, 1 Lz sector, 2 momentum sector
+    std::array<int, 5> m_par{};               // the generation parameters
 };
 
 template <typename T>
@@ -237,6 +386,13 @@ class ArpackWrapper {
     void SetDegeneracyPasses(int passes) { m_degeneracyPasses = passes; }
     // start vector (host, nodeDim doubles) in place of --use-initial's file
     void SetInitialVector(const std::vector<double>& v) { m_initial = v; }
+    // arpack_wrapper.hpp: --use-initial reads the start vector (raw FP64,
+    // nodeDim values) from the initial-vector file; --store-final writes the
+    // final vector there (here the lowest eigenvector, a restart vector)
+    void SetUseInitial(bool use) { m_useInitial = use; }
+    void SetStoreFinal(bool store) { m_storeFinal = store; }
+    void SetInitialVectorFile(const std::string& name) { m_initialFile = name; }
+    void SetFinalVectorFile(const std::string& name) { m_finalFile = name; }
     const ed_solve_info& LastInfo() const { return m_info; }
 
     // arpack_wrapper.hpp:595: generic host product (std::function form)
@@ -294,10 +450,24 @@ class ArpackWrapper {
         p.want_vectors = eigenvectors != nullptr;
         p.verify = 1;
         p.degeneracy_passes = m_degeneracyPasses;
+        if (m_useInitial && !m_initialFile.empty()) {
+            std::vector<double> v(n);
+            FILE* f = std::fopen(m_initialFile.c_str(), "rb");
+            const bool read = f && std::fread(v.data(), sizeof(double), (size_t)n, f) == (size_t)n;
+            if (f) std::fclose(f);
+            if (!read) return Fail(ED_ERR_ARG, "cannot read " + std::to_string(n) + " values from " + m_initialFile, mpi);
+            m_initial = v;
+        }
         const double* v0 = ((int)m_initial.size() == n) ? m_initial.data() : nullptr;
         ed_status s = ed_lanczos(op, &p, v0, eigenvalues, eigenvectors, &m_info);
         m_status = s;
         if (s != ED_OK) return Fail(s, ed_last_error(), mpi);
+        if (m_storeFinal && !m_finalFile.empty() && eigenvectors) {
+            FILE* f = std::fopen(m_finalFile.c_str(), "wb");
+            const bool wrote = f && std::fwrite(eigenvectors, sizeof(double), (size_t)n, f) == (size_t)n;
+            if (f) std::fclose(f);
+            if (!wrote) return Fail(ED_ERR_ARG, "cannot write " + m_finalFile, mpi);
+        }
         return true;
     }
     int m_maxIterations = 2000;
@@ -306,6 +476,8 @@ class ArpackWrapper {
     double m_tol = 1e-10;
     uint64_t m_seed = 0;
     std::vector<double> m_initial;
+    bool m_useInitial = false, m_storeFinal = false;
+    std::string m_initialFile, m_finalFile;
     ed_solve_info m_info{};
     ed_status m_status = ED_OK;
 };
@@ -325,20 +497,31 @@ class SpinlessFermionHamiltonian {
     SpinlessFermionHamiltonian& operator=(const SpinlessFermionHamiltonian&) = delete;
     ~SpinlessFermionHamiltonian() { Clear(); }
 
-    // spinless_fermion_hamiltonian.hpp:59 (+ the sector, which the reference
-    // passes to its basis separately)
+    // hamiltonian_base.hpp:597
+    void SetFockBasis(const FermionFockBasis& fockBasis) { m_fockBasis = fockBasis; }
+    void SetFockBasis(FermionFockBasis&& fockBasis) { m_fockBasis = std::move(fockBasis); }
+
+    // spinless_fermion_hamiltonian.hpp:59, after SetFockBasis (the reference's
+    // model sequence): the basis set must hold nbrParticles in nbrOrbitals
     void Initialize(iSize_t nbrParticles, iSize_t nbrOrbitals, utilities::storageMethod_t storageMethod,
-                    utilities::MpiWrapper& mpi, int twoLz = 0)
+                    utilities::MpiWrapper& mpi)
     {
-        if (nbrParticles == 0 || nbrOrbitals == 0 || nbrParticles >= 64 || nbrParticles > nbrOrbitals) {
-            std::cerr << "\n\tERROR: bad particle/orbital numbers" << std::endl;
+        CheckNumbers(nbrParticles, nbrOrbitals, mpi);
+        if (!m_fockBasis.handle() || m_fockBasis.NbrParticles() != nbrParticles ||
+            m_fockBasis.NbrOrbitals() != nbrOrbitals) {
+            std::cerr << "\n\tERROR: set a Fock basis of these particle/orbital numbers first" << std::endl;
             mpi.m_exitFlag = true;
-            throw utilities::EdError(ED_ERR_ARG, "bad particle/orbital numbers");
+            throw utilities::EdError(ED_ERR_ARG, "SetFockBasis before Initialize (or pass the sector)");
         }
-        m_nbrParticles = nbrParticles;
-        m_nbrOrbitals = nbrOrbitals;
-        m_storageMethod = storageMethod;
+        SetData(nbrParticles, nbrOrbitals, storageMethod);
+    }
+    // the same with the sector given (twice Lz): the basis is built here
+    void Initialize(iSize_t nbrParticles, iSize_t nbrOrbitals, utilities::storageMethod_t storageMethod,
+                    utilities::MpiWrapper& mpi, int twoLz)
+    {
+        CheckNumbers(nbrParticles, nbrOrbitals, mpi);
         m_fockBasis.GenerateFockSpace(nbrParticles, nbrOrbitals, twoLz, mpi);
+        SetData(nbrParticles, nbrOrbitals, storageMethod);
     }
     // spinless_fermion_hamiltonian.hpp:282.  The whole sector is built in one
     // device call; minRow/maxRow are accepted for signature compatibility.
@@ -389,7 +572,24 @@ class SpinlessFermionHamiltonian {
         else utilities::EdCheck(ed_op_matfree(m_fockBasis.handle(), m_terms->handle(), &op));
         return op;
     }
-    // hamiltonian_base.hpp:770
+    // hamiltonian_base.hpp:770, the reference's call shape: the product of mv
+    // (this Hamiltonian's), the table arguments accepted as the reference
+    // passes them; eigenvalues ascending, eigenvectors n x nev column-major
+    template <class L1, class L2>
+    bool LanczosDiagonalize(L1* /*quadraticLookUpTables*/, L2* /*quarticLookUpTables*/,
+                            MatrixVectorFunction<T, L1, L2>& mv, iSize_t& nbrEigenvalues, utilities::MpiWrapper& mpi)
+    {
+        SetNbrEigenvalues(nbrEigenvalues, mpi);
+        nbrEigenvalues = m_data.m_nbrEigenvalues;
+        const fock_t n = GetFockSpaceDimension();
+        m_eigenvalues.assign(nbrEigenvalues, 0.0);
+        m_eigenvectors.assign((size_t)n * nbrEigenvalues, 0.0);
+        const bool ok = m_arpackWrapper.DiagonalizeSymmetricMatrix(mv, m_eigenvectors.data(), m_eigenvalues.data(),
+                                                                   (int)n, (int)n, (int)nbrEigenvalues, mpi);
+        m_data.m_eigenvectorsCalculated = ok;
+        return ok;
+    }
+    // the same with the tolerance and vectors as arguments
     bool LanczosDiagonalize(iSize_t nbrEigenvalues, utilities::MpiWrapper& mpi, double tol = 1e-10,
                             bool wantVectors = true)
     {
@@ -398,9 +598,55 @@ class SpinlessFermionHamiltonian {
         m_eigenvectors.assign(wantVectors ? (size_t)n * nbrEigenvalues : 0, 0.0);
         MatrixVectorFunction<T> mv(*this, mpi);
         m_arpackWrapper.SetTolerance(tol);
-        return m_arpackWrapper.DiagonalizeSymmetricMatrix(mv, wantVectors ? m_eigenvectors.data() : nullptr,
-                                                          m_eigenvalues.data(), (int)n, (int)n, (int)nbrEigenvalues,
-                                                          mpi);
+        const bool ok = m_arpackWrapper.DiagonalizeSymmetricMatrix(mv, wantVectors ? m_eigenvectors.data() : nullptr,
+                                                                   m_eigenvalues.data(), (int)n, (int)n,
+                                                                   (int)nbrEigenvalues, mpi);
+        m_data.m_nbrEigenvalues = nbrEigenvalues;
+        m_data.m_eigenvectorsCalculated = ok && wantVectors;
+        return ok;
+    }
+    // hamiltonian_base.hpp:634-758: every eigenpair of the dense matrix (the
+    // reference's choice below dimension 60), the lowest nbrEigenvalues kept
+    bool FullDiagonalize(iSize_t& nbrEigenvalues, utilities::MpiWrapper& mpi)
+    {
+        SetNbrEigenvalues(nbrEigenvalues, mpi);
+        nbrEigenvalues = m_data.m_nbrEigenvalues;
+        const fock_t n = GetFockSpaceDimension();
+        if (n > 20000) {
+            std::cerr << "\n\tERROR in FullDiagonalize: dimension too large for a dense solve" << std::endl;
+            mpi.m_exitFlag = true;
+            return false;
+        }
+        std::vector<int64_t> rs;
+        std::vector<int32_t> cs;
+        std::vector<double> vs;
+        GetCrs(rs, cs, vs);
+        int upper = 0;
+        utilities::EdCheck(ed_crs_info(m_crs, nullptr, nullptr, &upper), &mpi);
+        std::vector<double> dense((size_t)n * n, 0.0), w(n), z((size_t)n * n);
+        for (fock_t i = 0; i < n; ++i)
+            for (int64_t k = rs[i]; k < rs[i + 1]; ++k) {
+                dense[(size_t)i * n + cs[k]] = vs[k];
+                if (upper) dense[(size_t)cs[k] * n + i] = vs[k];
+            }
+        utilities::EdCheck(ed_dense_sym_eigen((int)n, dense.data(), w.data(), z.data()), &mpi);
+        m_eigenvalues.assign(w.begin(), w.begin() + nbrEigenvalues);
+        m_eigenvectors.assign(z.begin(), z.begin() + (size_t)n * nbrEigenvalues);
+        m_data.m_eigenvectorsCalculated = true;
+        return true;
+    }
+    // hamiltonian_base.hpp:568-594 (the ARPACK vector files of one run)
+    void UpdateArpackFileNames(const std::string& inFileName, const std::string& outFileName,
+                               utilities::MpiWrapper&)
+    {
+        m_arpackWrapper.SetInitialVectorFile(inFileName);
+        m_arpackWrapper.SetFinalVectorFile(outFileName);
+    }
+    // hamiltonian_base.hpp:603
+    void SetNbrEigenvalues(iSize_t nbrEigenvalues, const utilities::MpiWrapper&)
+    {
+        const fock_t n = GetFockSpaceDimension();
+        m_data.m_nbrEigenvalues = nbrEigenvalues > n ? (iSize_t)n : nbrEigenvalues;
     }
     void Clear()
     {
@@ -408,14 +654,35 @@ class SpinlessFermionHamiltonian {
         m_crs = nullptr;
     }
 
+    // hamiltonian_data.hpp: the fields the reference's callers read
+    struct HamiltonianData {
+        iSize_t m_nbrParticles = 0, m_nbrOrbitals = 0, m_nbrEigenvalues = 0;
+        fock_t m_fockSpaceDim = 0;
+        utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
+        bool m_eigenvectorsCalculated = false;
+    } m_data;
     FermionFockBasis m_fockBasis;
     utilities::linearAlgebra::ArpackWrapper m_arpackWrapper;
     std::vector<double> m_eigenvalues;
     std::vector<double> m_eigenvectors;   // column-major n x nev
 
   private:
-    iSize_t m_nbrParticles = 0, m_nbrOrbitals = 0;
-    utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
+    void CheckNumbers(iSize_t nbrParticles, iSize_t nbrOrbitals, utilities::MpiWrapper& mpi)
+    {
+        if (nbrParticles == 0 || nbrOrbitals == 0 || nbrParticles >= 64 || nbrParticles > nbrOrbitals) {
+            std::cerr << "\n\tERROR: bad particle/orbital numbers" << std::endl;
+            mpi.m_exitFlag = true;
+            throw utilities::EdError(ED_ERR_ARG, "bad particle/orbital numbers");
+        }
+    }
+    void SetData(iSize_t nbrParticles, iSize_t nbrOrbitals, utilities::storageMethod_t storageMethod)
+    {
+        m_data.m_nbrParticles = nbrParticles;
+        m_data.m_nbrOrbitals = nbrOrbitals;
+        m_data.m_storageMethod = storageMethod;
+        m_data.m_fockSpaceDim = m_fockBasis.GetStoredDimension();
+        m_data.m_eigenvectorsCalculated = false;
+    }
     ed_crs* m_crs = nullptr;
     QuarticTermTables* m_terms = nullptr;
 };

@@ -4,11 +4,14 @@
 // std::function product path of ArpackWrapper, the ground state's
 // observables, a two-level sector (N=4, norb0=6, Lz=0) as
 // SphereTwoLevelPseudopotentialModel builds it, and a complex momentum sector
-// (N=4 on a 3x4 grid, momentum (1,2)) as InteractingOflModel builds it.
-// Prints one JSON line.
+// (N=4 on a 3x4 grid, momentum (1,2)) as InteractingOflModel builds it, and
+// the reference's own model sequence written as it reads there (a predicate
+// basis, SetFockBasis, Initialize, Add_CdCdCC_Terms, FullDiagonalize or
+// LanczosDiagonalize).  Prints one JSON line.
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <functional>
 #include <vector>
 
 #include "ed_host.hpp"
@@ -147,6 +150,65 @@ int main(int argc, char** argv)
     std::printf(", \"ofl\": {\"ok\": %s, \"dim\": %llu, \"nnz\": %lld, \"eigenvalues\": [", ok4 ? "true" : "false",
                 (unsigned long long)dimc, (long long)Hc.GetNbrNonZeros());
     for (int i = 0; i < 3; ++i) std::printf("%s%.17g", i ? ", " : "", Hc.m_eigenvalues[i]);
-    std::printf("]}}\n");
-    return (ok && ok2 && rank_ok && ok3 && rank2_ok && ok4) ? 0 : 1;
+    std::printf("]}");
+
+    // The reference's model sequence as it is written there
+    // (pseudopotential_model.cpp:160-189 BuildFockBasis, :233-249
+    // BuildHamiltonian, pseudopotential_model_base.hpp:235-275 BaseDiagonalize):
+    // the sector of a std::bind predicate, SetFockBasis, Initialize with
+    // mapped storage, Add_CdCdCC_Terms over all rows, then FullDiagonalize
+    // below dimension 60 and LanczosDiagonalize with a MatrixVectorFunction
+    // above it.  Run for the sector above and for a small one.
+    bool ok5 = true;
+    std::printf(", \"reference_sequence\": [");
+    const int seqN[2] = {N, 4}, seqOrb[2] = {norb, 10};
+    for (int c = 0; c < 2; ++c) {
+        const int n5 = seqN[c], k5 = seqOrb[c];
+        std::vector<double> pc(k5);
+        utilities::EdCheck(ed_coulomb_pseudopotentials(k5, pc.data()));
+        std::vector<double> p5(pc.begin(), pc.begin() + (k5 - 1));
+        for (size_t m = 0; m < p5.size(); m += 2) p5[m] = 0.0;
+        diagonalization::QuadraticTermTables m_quadraticTables;
+        diagonalization::QuarticTermTables m_quarticTables;
+        m_quarticTables.Initialize(k5, p5);
+        diagonalization::SpinlessFermionHamiltonian<double> m_hamiltonian;
+        const diagonalization::mState_t totalLz = (diagonalization::mState_t)(c == 0 ? twoLz : 0);
+        const diagonalization::mState_t maxLz = (diagonalization::mState_t)(k5 - 1);
+        diagonalization::FermionFockBasis basis;
+        const bool isZeroDimensional = basis.GenerateFockSpace(
+            n5, k5, std::bind(&diagonalization::TestAngularMomentumSector, std::placeholders::_1, totalLz, maxLz), mpi);
+        m_hamiltonian.SetFockBasis(basis);
+        m_hamiltonian.Initialize(n5, k5, utilities::_SPARSE_MAPPED_, mpi);
+        m_hamiltonian.Add_CdCdCC_Terms(&m_quarticTables, 0, m_hamiltonian.m_data.m_fockSpaceDim, mpi);
+        diagonalization::iSize_t nbrEigenvaluesToFind = nev;
+        bool done = false;
+        const bool full = m_hamiltonian.m_data.m_fockSpaceDim < 60;
+        if (full) {
+            done = m_hamiltonian.FullDiagonalize(nbrEigenvaluesToFind, mpi);
+        } else {
+            diagonalization::MatrixVectorFunction<double, diagonalization::QuadraticTermTables,
+                                                  diagonalization::QuarticTermTables>
+                mv(m_hamiltonian, mpi);
+            done = m_hamiltonian.LanczosDiagonalize(&m_quadraticTables, &m_quarticTables, mv, nbrEigenvaluesToFind, mpi);
+        }
+        ok5 = ok5 && done && !isZeroDimensional;
+        std::printf("%s{\"N\": %d, \"norb\": %d, \"two_lz\": %d, \"ok\": %s, \"full\": %s, \"dim\": %llu, \"eigenvalues\": [",
+                    c ? ", " : "", n5, k5, (int)totalLz, done ? "true" : "false", full ? "true" : "false",
+                    (unsigned long long)m_hamiltonian.m_data.m_fockSpaceDim);
+        for (diagonalization::iSize_t i = 0; i < nbrEigenvaluesToFind; ++i)
+            std::printf("%s%.17g", i ? ", " : "", m_hamiltonian.m_eigenvalues[i]);
+        std::printf("]}");
+    }
+    // a predicate that selects every sector (the reference's run without
+    // block diagonalisation) is refused: the device builds one sector
+    bool refused = false;
+    try {
+        diagonalization::FermionFockBasis all;
+        utilities::MpiWrapper mpi2;
+        all.GenerateFockSpace(4, 10, [](const diagonalization::fock_t) { return true; }, mpi2);
+    } catch (const utilities::EdError&) {
+        refused = true;
+    }
+    std::printf("], \"all_sectors_refused\": %s}\n", refused ? "true" : "false");
+    return (ok && ok2 && rank_ok && ok3 && rank2_ok && ok4 && ok5 && refused) ? 0 : 1;
 }

@@ -172,8 +172,11 @@ def test_device_crs_matches_reference_build(cuda, oracle):
     gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ref_hamiltonians.json")))
     for key, ent in gold["crs_two_level"].items():
         N, norb0, tlz = ent["N"], ent["norb0"], ent["two_lz"]
-        t0 = ed.QuarticTermTables(norb0, oracle.odd_coulomb_list(norb0))
-        t1 = ed.QuarticTermTables(norb0 + 2, oracle.odd_coulomb_list(norb0 + 2))
+        # the term tables the reference run was given (the oracle's)
+        kt0, vt0 = oracle.quartic_tables(norb0, oracle.odd_coulomb_list(norb0))
+        kt1, vt1 = oracle.quartic_tables(norb0 + 2, oracle.odd_coulomb_list(norb0 + 2))
+        t0 = ed.QuarticTermTables(norb0, ktable=kt0, vtable=vt0)
+        t1 = ed.QuarticTermTables(norb0 + 2, ktable=kt1, vtable=vt1)
         e0 = np.linspace(-0.3, 0.2, norb0) if ent["energies"] else None
         e1 = np.linspace(0.9, 1.4, norb0 + 2) if ent["energies"] else None
         H = build(N, norb0, tlz, t0, t1, e0, e1, upper=True)

@@ -78,3 +78,27 @@ def test_host_classes_solve_sector(cuda, oracle, tmp_path):
     ref3 = np.linalg.eigvalsh(sp.csr_matrix((fv, fc, fr), shape=(len(b), len(b))).toarray())[:3]
     assert c["dim"] == len(b) and c["nnz"] == len(fv)
     assert np.max(np.abs(np.array(c["eigenvalues"]) - ref3)) < 1e-10 * max(1.0, np.abs(ref3).max())
+
+
+@pytest.mark.gpu
+def test_reference_model_sequence_runs_as_written(cuda, oracle, tmp_path):
+    # the reference's BuildFockBasis -> BuildHamiltonian -> BaseDiagonalize
+    # sequence through ed_host.hpp: a std::bind(TestAngularMomentumSector)
+    # basis, SetFockBasis, Initialize, Add_CdCdCC_Terms, then FullDiagonalize
+    # (dimension < 60) or LanczosDiagonalize(&quadratic, &quartic, mv, nev, mpi)
+    import scipy.sparse as sp
+    exe = compile_demo(tmp_path)
+    out = subprocess.run([exe, "6", "16", "2"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    r = json.loads(out.stdout.strip().splitlines()[-1])
+    assert r["all_sectors_refused"]
+    seq = r["reference_sequence"]
+    assert [c["full"] for c in seq] == [False, True]
+    for c in seq:
+        assert c["ok"]
+        b = oracle.basis(c["N"], c["norb"], c["two_lz"])
+        assert c["dim"] == len(b)
+        kt, vt = oracle.quartic_tables(c["norb"], oracle.odd_coulomb_list(c["norb"]))
+        fr, fc, fv = oracle.upper_to_full(*oracle.build_upper(b, c["norb"], kt, vt), len(b))
+        ref = np.linalg.eigvalsh(sp.csr_matrix((fv, fc, fr), shape=(len(b), len(b))).toarray())[:len(c["eigenvalues"])]
+        assert np.max(np.abs(np.array(c["eigenvalues"]) - ref)) <= 1e-10 * max(1.0, np.abs(ref).max())
