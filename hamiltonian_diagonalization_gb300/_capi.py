@@ -134,6 +134,7 @@ _SIGS = {
     "ed_batch_solve": (c_int, [c_void_p, P(LanczosParams), c_void_p, P(c_double), c_void_p, P(BatchInfo)]),
     "ed_batch_solve_subset": (c_int, [c_void_p, P(c_int), c_int, P(LanczosParams), c_void_p, P(c_double), c_void_p,
                                       P(BatchInfo)]),
+    "ed_sym_eigen_batched": (c_int, [c_int, c_int, P(c_double), P(c_double), P(c_double)]),
     "ed_subspace_create": (c_int, [c_i64, c_int, P(c_void_p)]),
     "ed_subspace_free": (c_int, [c_void_p]),
     "ed_subspace_dim": (c_int, [c_void_p, P(c_int)]),

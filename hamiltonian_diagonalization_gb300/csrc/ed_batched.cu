@@ -1147,7 +1147,7 @@ void batch_solve(const ed_batch& bt, const int* sel, int nsel, const ed_lanczos_
             ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * j], ev[2 * j + 1]));
             spmm_ms += ms;
         }
-        std::vector<int> done, live;
+        std::vector<int> done, live, solved;
         double maxres = 0.0;
         for (int q = 0; q < B; ++q) {
             if (brk_h[q]) {
@@ -1162,7 +1162,25 @@ void batch_solve(const ed_batch& bt, const int* sel, int nsel, const ed_lanczos_
                     Tb[(size_t)i * m + j] = v;
                     Tb[(size_t)j * m + i] = v;
                 }
-            sym_eigen(m, Tb, theta[b], Y[b]);
+            solved.push_back(q);
+        }
+        // every active problem's projected matrix in one device launch
+        if (m <= kDeviceEigenMax) {
+            const size_t mm = (size_t)m * m;
+            std::vector<double> Ts(solved.size() * mm), Es(solved.size() * m), Zs(solved.size() * mm);
+            for (size_t t = 0; t < solved.size(); ++t)
+                std::copy(T[orig[solved[t]]].begin(), T[orig[solved[t]]].end(), Ts.begin() + t * mm);
+            if (!solved.empty()) sym_eigen_batched(m, (int)solved.size(), Ts.data(), Es.data(), Zs.data(), st);
+            for (size_t t = 0; t < solved.size(); ++t) {
+                const int b = orig[solved[t]];
+                theta[b].assign(Es.begin() + t * m, Es.begin() + (t + 1) * m);
+                Y[b].assign(Zs.begin() + t * mm, Zs.begin() + (t + 1) * mm);
+            }
+        } else {
+            for (int q : solved) sym_eigen(m, T[orig[q]], theta[orig[q]], Y[orig[q]]);
+        }
+        for (int q : solved) {
+            const int b = orig[q];
             const double bl = beta_h[(size_t)(m - 1) * B + q];
             bool ok = true;
             double rq = 0.0;

@@ -540,9 +540,21 @@ ed_status ed_dense_sym_eigen(int m, const double* a, double* evals, double* evec
         ED_NONNULL(evals);
         ED_REQUIRE(m >= 1 && m <= 20000, ED_ERR_ARG, "m out of range");
         std::vector<double> A(a, a + (size_t)m * m), ev, vec;
-        sym_eigen(m, A, ev, vec);
+        sym_eigen_small(m, A, ev, vec, nullptr);
         std::memcpy(evals, ev.data(), (size_t)m * 8);
         if (evecs) std::memcpy(evecs, vec.data(), (size_t)m * m * 8);
+    });
+}
+
+ed_status ed_sym_eigen_batched(int m, int count, const double* a, double* evals, double* evecs)
+{
+    return guarded([&] {
+        ED_NONNULL(a);
+        ED_NONNULL(evals);
+        ED_NONNULL(evecs);
+        ED_REQUIRE(m >= 1 && m <= kDeviceEigenMax, ED_ERR_RANGE, "m must be 1..128");
+        ED_REQUIRE(count >= 1, ED_ERR_ARG, "count must be positive");
+        sym_eigen_batched(m, count, a, evals, evecs, nullptr);
     });
 }
 

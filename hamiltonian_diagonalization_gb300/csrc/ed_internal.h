@@ -131,6 +131,19 @@ HopTables derive_hop_tables(int norb, const uint16_t* ktab, const double* vtab);
 // component i of eigenvector j).
 void sym_eigen(int m, const std::vector<double>& a, std::vector<double>& evals, std::vector<double>& evecs);
 
+// The same decompositions on the device (ed_eigen_dev.cu, FP64 Jacobi, one CTA
+// per matrix) for m <= kDeviceEigenMax.  sym_eigen_device: count matrices
+// already on the device (row-major) to device eigenvalues (count x m,
+// ascending) and eigenvectors (count x m x m, column-major).
+// sym_eigen_batched: the same from and to host arrays.  sym_eigen_small: the
+// projected problem of a solver restart, on the device when m fits, else on
+// the host.
+constexpr int kDeviceEigenMax = 128;
+void sym_eigen_device(int m, int count, const double* A_dev, double* evals_dev, double* evecs_dev, cudaStream_t st);
+void sym_eigen_batched(int m, int count, const double* a_host, double* evals_host, double* evecs_host, cudaStream_t st);
+void sym_eigen_small(int m, const std::vector<double>& a, std::vector<double>& evals, std::vector<double>& evecs,
+                     cudaStream_t st);
+
 // ------------------------------------------------------------- pair indexing
 
 // Helpers shared by host and device code for the per-hop table layout.

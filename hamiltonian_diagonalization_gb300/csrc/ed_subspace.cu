@@ -277,18 +277,48 @@ __global__ void __launch_bounds__(256) k_ts_combine(const double* __restrict__ A
 
 int grid1(int64_t work) { return (int)std::max<int64_t>(1, std::min<int64_t>(batch_sms() * 8, (work + 255) / 256)); }
 
-// C (host, p x q row-major) = A^T B over n rows
-void ts_gram(const double* A, int lda, int p, const double* Bm, int ldb, int q, int64_t n, double* C_host,
-             cudaStream_t st)
+// C_dev (p x q row-major) = A^T B over n rows
+void ts_gram_dev(const double* A, int lda, int p, const double* Bm, int ldb, int q, int64_t n, double* C_dev,
+                 cudaStream_t st)
 {
     const int ntiles = ((p + kTile - 1) / kTile) * ((q + kTile - 1) / kTile);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(std::max(1, batch_sms() * 2 / ntiles), n / kRows));
-    DevBuf<double> part((size_t)nb * ntiles * kTile * kTile), C((size_t)p * q);
+    DevBuf<double> part((size_t)nb * ntiles * kTile * kTile);
     k_ts_gram<<<dim3((unsigned)nb, (unsigned)ntiles), 256, 0, st>>>(A, lda, p, Bm, ldb, q, n, part.p); count_launch();
-    k_ts_gram_sum<<<grid1((int64_t)p * q), 256, 0, st>>>(part.p, nb, ntiles, p, q, C.p); count_launch();
+    k_ts_gram_sum<<<grid1((int64_t)p * q), 256, 0, st>>>(part.p, nb, ntiles, p, q, C_dev); count_launch();
     ED_CUDA(cudaGetLastError());
-    ED_CUDA(cudaMemcpyAsync(C_host, C.p, (size_t)p * q * 8, cudaMemcpyDeviceToHost, st));
-    ED_CUDA(cudaStreamSynchronize(st));
+    ED_CUDA(cudaStreamSynchronize(st));   // part is freed on return
+}
+
+// M[b] = sum_k alpha[b][k] (A_k + A_k^T) / 2 for the B Hamiltonians (d x d each)
+__global__ void k_sub_assemble(const double* __restrict__ Ak, int r, int d, const double* __restrict__ alpha, int B,
+                               double* __restrict__ M)
+{
+    const int64_t dd = (int64_t)d * d, total = dd * B;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int b = (int)(t / dd);
+        const int64_t e = t - (int64_t)b * dd;
+        const int i = (int)(e / d), j = (int)(e % d);
+        double s = 0.0;
+        for (int k = 0; k < r; ++k)
+            s = fma(alpha[b * r + k], 0.5 * (Ak[k * dd + (int64_t)i * d + j] + Ak[k * dd + (int64_t)j * d + i]), s);
+        M[t] = s;
+    }
+}
+
+// Mi[i][c][b] = Z_b[c + d i] (the Ritz coefficients of the nev lowest pairs
+// in the combine layout), evals_out[b][i] = E[b][i]
+__global__ void k_sub_ritz_coef(const double* __restrict__ Z, const double* __restrict__ E, int d, int B, int nev,
+                                double* __restrict__ Mi, double* __restrict__ evals_out)
+{
+    const int64_t total = (int64_t)nev * d * B;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int b = (int)(t % B);
+        const int64_t ic = t / B;
+        const int c = (int)(ic % d), i = (int)(ic / d);
+        Mi[t] = Z[(int64_t)b * d * d + c + (int64_t)d * i];
+        if (c == 0) evals_out[(int64_t)b * nev + i] = E[(int64_t)b * d + i];
+    }
 }
 
 void ts_combine(const double* A, int lda, int p, const double* M_dev, int q, double* Y, int ldy, int64_t n,
@@ -449,35 +479,54 @@ void batch_subspace_ritz(const ed_batch& bt, const ed_subspace& sp, int nev, int
     SolveStream ss(caller);
     cudaStream_t st = ss.s;
     // projected matrices of the basis members
-    DevBuf<double> HQ((size_t)n * d);
-    std::vector<std::vector<double>> A(r, std::vector<double>((size_t)d * d));
+    DevBuf<double> HQ((size_t)n * d), Akd((size_t)r * d * d);
     for (int k = 0; k < r; ++k) {
         batch_apply(bt, basis[k], sp.Q.p, sp.max_dim, HQ.p, d, d, st);
-        ts_gram(sp.Q.p, sp.max_dim, d, HQ.p, d, d, n, A[k].data(), st);
+        ts_gram_dev(sp.Q.p, sp.max_dim, d, HQ.p, d, d, n, Akd.p + (size_t)k * d * d, st);
     }
     HQ.release();
     // every Hamiltonian's projected matrix and its lowest nev Ritz pairs
-    std::vector<double> Mi((size_t)nev * d * B), M((size_t)d * d), th, Yv;
-    for (int b = 0; b < B; ++b) {
-        for (int i = 0; i < d; ++i)
-            for (int j = 0; j <= i; ++j) {
-                double s = 0.0;
-                for (int k = 0; k < r; ++k) {
-                    const double* Ak = A[k].data();
-                    s += alpha[(size_t)b * r + k] * 0.5 * (Ak[(size_t)i * d + j] + Ak[(size_t)j * d + i]);
+    DevBuf<double> Md((size_t)nev * d * B);
+    if (d <= kDeviceEigenMax) {
+        // assembled, solved (one CTA per Hamiltonian) and laid out on the device
+        DevBuf<double> al((size_t)B * r), Mall((size_t)B * d * d), E((size_t)B * d), Z((size_t)B * d * d),
+            ev((size_t)B * nev);
+        ED_CUDA(cudaMemcpyAsync(al.p, alpha.data(), alpha.size() * 8, cudaMemcpyHostToDevice, st));
+        k_sub_assemble<<<grid1((int64_t)B * d * d), 256, 0, st>>>(Akd.p, r, d, al.p, B, Mall.p); count_launch();
+        ED_CUDA(cudaGetLastError());
+        sym_eigen_device(d, B, Mall.p, E.p, Z.p, st);
+        k_sub_ritz_coef<<<grid1((int64_t)nev * d * B), 256, 0, st>>>(Z.p, E.p, d, B, nev, Md.p, ev.p); count_launch();
+        ED_CUDA(cudaGetLastError());
+        ED_CUDA(cudaMemcpyAsync(evals, ev.p, (size_t)B * nev * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+    } else {
+        // subspaces above the device eigensolver's size: the same on the host
+        std::vector<std::vector<double>> A(r, std::vector<double>((size_t)d * d));
+        for (int k = 0; k < r; ++k)
+            ED_CUDA(cudaMemcpyAsync(A[k].data(), Akd.p + (size_t)k * d * d, (size_t)d * d * 8, cudaMemcpyDeviceToHost,
+                                    st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        std::vector<double> Mi((size_t)nev * d * B), M((size_t)d * d), th, Yv;
+        for (int b = 0; b < B; ++b) {
+            for (int i = 0; i < d; ++i)
+                for (int j = 0; j <= i; ++j) {
+                    double s = 0.0;
+                    for (int k = 0; k < r; ++k) {
+                        const double* Ak = A[k].data();
+                        s += alpha[(size_t)b * r + k] * 0.5 * (Ak[(size_t)i * d + j] + Ak[(size_t)j * d + i]);
+                    }
+                    M[(size_t)i * d + j] = s;
+                    M[(size_t)j * d + i] = s;
                 }
-                M[(size_t)i * d + j] = s;
-                M[(size_t)j * d + i] = s;
+            sym_eigen(d, M, th, Yv);
+            for (int i = 0; i < nev; ++i) {
+                evals[(size_t)b * nev + i] = th[i];
+                for (int c = 0; c < d; ++c) Mi[((size_t)i * d + c) * B + b] = Yv[(size_t)c + (size_t)d * i];
             }
-        sym_eigen(d, M, th, Yv);
-        for (int i = 0; i < nev; ++i) {
-            evals[(size_t)b * nev + i] = th[i];
-            for (int c = 0; c < d; ++c) Mi[((size_t)i * d + c) * B + b] = Yv[(size_t)c + (size_t)d * i];
         }
+        ED_CUDA(cudaMemcpyAsync(Md.p, Mi.data(), Mi.size() * 8, cudaMemcpyHostToDevice, st));
     }
     // Ritz vectors in the batch layout, then their true residuals
-    DevBuf<double> Md(Mi.size());
-    ED_CUDA(cudaMemcpyAsync(Md.p, Mi.data(), Mi.size() * 8, cudaMemcpyHostToDevice, st));
     for (int i = 0; i < nev; ++i)
         ts_combine(sp.Q.p, sp.max_dim, d, Md.p + (size_t)i * d * B, B, X + (int64_t)i * n * B, B, n, st);
     if (nchk > 0) {
