@@ -1164,8 +1164,9 @@ void batch_solve(const ed_batch& bt, const int* sel, int nsel, const ed_lanczos_
                 }
             solved.push_back(q);
         }
-        // every active problem's projected matrix in one device launch
-        if (m <= kDeviceEigenMax) {
+        // the active problems' projected matrices in one device launch (a
+        // batch large enough to beat the host)
+        if (m <= kDeviceEigenMax && (int)solved.size() >= kDeviceEigenMinBatch) {
             const size_t mm = (size_t)m * m;
             std::vector<double> Ts(solved.size() * mm), Es(solved.size() * m), Zs(solved.size() * mm);
             for (size_t t = 0; t < solved.size(); ++t)

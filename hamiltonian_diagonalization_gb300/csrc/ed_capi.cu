@@ -540,7 +540,7 @@ ed_status ed_dense_sym_eigen(int m, const double* a, double* evals, double* evec
         ED_NONNULL(evals);
         ED_REQUIRE(m >= 1 && m <= 20000, ED_ERR_ARG, "m out of range");
         std::vector<double> A(a, a + (size_t)m * m), ev, vec;
-        sym_eigen_small(m, A, ev, vec, nullptr);
+        sym_eigen(m, A, ev, vec);
         std::memcpy(evals, ev.data(), (size_t)m * 8);
         if (evecs) std::memcpy(evecs, vec.data(), (size_t)m * m * 8);
     });

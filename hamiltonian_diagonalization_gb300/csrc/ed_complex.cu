@@ -371,7 +371,7 @@ void cdense_solve(const ed_ccrs& a, int nev, double* evals, double* evecs_dev, e
             R[(size_t)(i + n) * m + j] = h.imag();
         }
     std::vector<double> ev, vec;
-    sym_eigen_small(m, R, ev, vec, st);
+    sym_eigen(m, R, ev, vec);
     std::vector<std::vector<cplx>> kept;
     std::vector<double> vals;
     for (int k = 0; k < m && (int)kept.size() < nev; ++k) {
@@ -644,7 +644,7 @@ void clanczos_solve(const ed_ccrs& a, const ed_lanczos_params& p, const double* 
                 T[(size_t)(j + 1) * m + j] = b;
             }
         }
-        sym_eigen_small(m, T, theta, Y, st);
+        sym_eigen(m, T, theta, Y);
         const double bl = beta[m - 1];
         int nconv = 0;
         double maxres = 0.0;

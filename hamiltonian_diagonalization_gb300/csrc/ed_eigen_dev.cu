@@ -11,8 +11,9 @@
 // is m_pad - 1 steps (m_pad = m rounded up to even, with a dummy index for odd
 // m); each step rotates m_pad / 2 disjoint pairs (p, q) at once: rows, then
 // columns of A in shared memory, then the columns of the accumulated
-// eigenvector matrix V in global memory; the rotated 2 x 2 block is then set
-// from Rutishauser's formulas (a_pq = 0 exactly, a_pp - t a_pq, a_qq + t a_pq).
+// eigenvector matrix V (in shared memory too up to m = 118, else in global
+// memory), with the rotated 2 x 2 block set from
+// Rutishauser's formulas (a_pq = 0 exactly, a_pp - t a_pq, a_qq + t a_pq).
 // A pair is rotated only when |a_pq| > 1e-16 sqrt(|a_pp a_qq|) (or when
 // a_pp a_qq = 0 and a_pq != 0), and the iteration ends after a sweep that
 // rotates no pair.  Jacobi is at least as accurate as the Householder + QR
@@ -20,6 +21,7 @@
 // with their columns.
 #include <algorithm>
 #include <cmath>
+#include <map>
 
 #include "ed_internal.h"
 
@@ -36,9 +38,11 @@ __device__ __forceinline__ int rr_player(int x, int r, int mp)
     return x == 0 ? 0 : ((x - 1 + r) % (mp - 1)) + 1;
 }
 
-// A: count matrices, m x m row-major; evals count x m; Vw: count x m x m
-// column-major (V[i + m j] = component i of eigenvector j), the accumulator,
-// then sorted into evecs (same layout).
+// A: count matrices, m x m row-major; evals count x m; the accumulated
+// eigenvectors V (V[i + vld j] = component i of eigenvector j) in shared
+// memory after A when VS (m up to 118), else in Vw (count x m x m, global),
+// then sorted into evecs (count x m x m, column-major).
+template <bool VS>
 __global__ void __launch_bounds__(kEigThreads) k_sym_jacobi(const double* __restrict__ Ain, int m,
                                                             double* __restrict__ evals, double* __restrict__ Vw,
                                                             double* __restrict__ evecs, int max_sweeps)
@@ -46,7 +50,7 @@ __global__ void __launch_bounds__(kEigThreads) k_sym_jacobi(const double* __rest
     extern __shared__ double smem[];
     const int ld = m + 1;                            // padded row stride
     double* a = smem;                                // m x ld
-    double* cs = a + (size_t)m * ld;                 // cos per pair
+    double* cs = a + (size_t)(VS ? 2 : 1) * m * ld;  // cos per pair (after A, and V when VS)
     double* sn = cs + kEigMax / 2;                   // sin per pair
     double* tn = sn + kEigMax / 2;                   // tan per pair
     double* apq0 = tn + kEigMax / 2;                 // the pair's a_pq, a_pp, a_qq before the rotation
@@ -58,11 +62,12 @@ __global__ void __launch_bounds__(kEigThreads) k_sym_jacobi(const double* __rest
     __shared__ int rank[kEigMax];
     const int mat = blockIdx.x;
     const double* A = Ain + (size_t)mat * m * m;
-    double* V = Vw + (size_t)mat * m * m;
+    const int vld = VS ? ld : m;                     // column stride of V
+    double* V = VS ? a + (size_t)m * ld : Vw + (size_t)mat * m * m;
     for (int t = threadIdx.x; t < m * m; t += kEigThreads) {
         const int i = t / m, j = t % m;
         a[i * ld + j] = A[t];
-        V[t] = (t % (m + 1) == 0) ? 1.0 : 0.0;      // identity
+        V[i + (size_t)vld * j] = (i == j) ? 1.0 : 0.0;   // identity
     }
     __syncthreads();
     const int mp = m + (m & 1);
@@ -113,30 +118,29 @@ __global__ void __launch_bounds__(kEigThreads) k_sym_jacobi(const double* __rest
                 a[q * ld + j] = fma(s, x, c * y);
             }
             __syncthreads();
-            // columns p, q of A and of V
+            // columns p, q of A and of V; the rotated 2 x 2 block (rows p, q
+            // of columns p, q, written only by this pair's threads) from the
+            // exact formulas
             for (int t = threadIdx.x; t < npairs * m; t += kEigThreads) {
                 const int k = t / m, i = t % m;
                 const int p = pp[k];
                 if (p < 0) continue;
                 const int q = qq[k];
                 const double c = cs[k], s = sn[k];
-                const double x = a[i * ld + p], y = a[i * ld + q];
-                a[i * ld + p] = c * x - s * y;
-                a[i * ld + q] = fma(s, x, c * y);
-                const double vx = V[i + (size_t)m * p], vy = V[i + (size_t)m * q];
-                V[i + (size_t)m * p] = c * vx - s * vy;
-                V[i + (size_t)m * q] = fma(s, vx, c * vy);
-            }
-            __syncthreads();
-            // the rotated 2 x 2 blocks from the exact formulas
-            for (int k = threadIdx.x; k < npairs; k += kEigThreads) {
-                const int p = pp[k];
-                if (p < 0) continue;
-                const int q = qq[k];
-                a[p * ld + p] = fma(-tn[k], apq0[k], app0[k]);
-                a[q * ld + q] = fma(tn[k], apq0[k], aqq0[k]);
-                a[p * ld + q] = 0.0;
-                a[q * ld + p] = 0.0;
+                if (i == p) {
+                    a[p * ld + p] = fma(-tn[k], apq0[k], app0[k]);
+                    a[p * ld + q] = 0.0;
+                } else if (i == q) {
+                    a[q * ld + q] = fma(tn[k], apq0[k], aqq0[k]);
+                    a[q * ld + p] = 0.0;
+                } else {
+                    const double x = a[i * ld + p], y = a[i * ld + q];
+                    a[i * ld + p] = c * x - s * y;
+                    a[i * ld + q] = fma(s, x, c * y);
+                }
+                const double vx = V[i + (size_t)vld * p], vy = V[i + (size_t)vld * q];
+                V[i + (size_t)vld * p] = c * vx - s * vy;
+                V[i + (size_t)vld * q] = fma(s, vx, c * vy);
             }
             __syncthreads();
         }
@@ -158,25 +162,57 @@ __global__ void __launch_bounds__(kEigThreads) k_sym_jacobi(const double* __rest
     double* out = evecs + (size_t)mat * m * m;
     for (int t = threadIdx.x; t < m * m; t += kEigThreads) {
         const int j = t / m, i = t % m;              // column j, row i
-        out[i + (size_t)m * rank[j]] = V[i + (size_t)m * j];
+        out[i + (size_t)m * rank[j]] = V[i + (size_t)vld * j];
     }
 }
 
-size_t jacobi_smem(int m) { return (size_t)m * (m + 1) * 8 + (size_t)3 * kEigMax * 8 + (size_t)kEigMax * 4; }
+size_t jacobi_smem(int m, bool vs)
+{
+    return (size_t)(vs ? 2 : 1) * m * (m + 1) * 8 + (size_t)3 * kEigMax * 8 + (size_t)kEigMax * 4;
+}
+constexpr size_t kSmemLimit = 227 * 1024 - 2048;   // dynamic shared memory per CTA, less the static arrays
 
 }  // namespace
 
-void sym_eigen_device(int m, int count, const double* A_dev, double* evals_dev, double* evecs_dev, cudaStream_t st)
+// Device scratch of the eigensolver, kept per host thread and device and
+// grown on demand, so that a solver restart costs no allocation.
+struct EigWork {
+    DevBuf<double> V, A, E, Z;
+    int smem_set[2] = {0, 0};
+};
+EigWork& eig_work()
+{
+    thread_local std::map<int, EigWork> work;
+    int dev = 0;
+    ED_CUDA(cudaGetDevice(&dev));
+    return work[dev];
+}
+
+void jacobi_launch(int m, int count, const double* A_dev, double* evals_dev, double* evecs_dev, EigWork& w,
+                   cudaStream_t st)
 {
     ED_REQUIRE(m >= 1 && m <= kEigMax, ED_ERR_RANGE, "device eigensolver: 1 <= m <= 128");
-    if (count <= 0) return;
-    DevBuf<double> V((size_t)count * m * m);
-    const size_t smem = jacobi_smem(m);
-    ED_CUDA(cudaFuncSetAttribute(k_sym_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_sym_jacobi<<<count, kEigThreads, smem, st>>>(A_dev, m, evals_dev, V.p, evecs_dev, 60);
+    const bool vs = jacobi_smem(m, true) <= kSmemLimit;
+    const size_t smem = jacobi_smem(m, vs);
+    if ((int)smem > w.smem_set[vs]) {
+        ED_CUDA(cudaFuncSetAttribute(vs ? k_sym_jacobi<true> : k_sym_jacobi<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        w.smem_set[vs] = (int)smem;
+    }
+    if (vs) {
+        k_sym_jacobi<true><<<count, kEigThreads, smem, st>>>(A_dev, m, evals_dev, nullptr, evecs_dev, 60);
+    } else {
+        w.V.alloc_at_least((size_t)count * m * m);
+        k_sym_jacobi<false><<<count, kEigThreads, smem, st>>>(A_dev, m, evals_dev, w.V.p, evecs_dev, 60);
+    }
     count_launch();
     ED_CUDA(cudaGetLastError());
-    ED_CUDA(cudaStreamSynchronize(st));   // V is freed on return
+}
+
+void sym_eigen_device(int m, int count, const double* A_dev, double* evals_dev, double* evecs_dev, cudaStream_t st)
+{
+    if (count <= 0) return;
+    jacobi_launch(m, count, A_dev, evals_dev, evecs_dev, eig_work(), st);
 }
 
 // Host matrices in and out (the restart bookkeeping of the solvers keeps the
@@ -185,25 +221,17 @@ void sym_eigen_device(int m, int count, const double* A_dev, double* evals_dev, 
 void sym_eigen_batched(int m, int count, const double* a_host, double* evals_host, double* evecs_host,
                        cudaStream_t st)
 {
-    DevBuf<double> A((size_t)count * m * m), E((size_t)count * m), Z((size_t)count * m * m);
-    ED_CUDA(cudaMemcpyAsync(A.p, a_host, A.bytes(), cudaMemcpyHostToDevice, st));
-    sym_eigen_device(m, count, A.p, E.p, Z.p, st);
-    ED_CUDA(cudaMemcpyAsync(evals_host, E.p, E.bytes(), cudaMemcpyDeviceToHost, st));
-    ED_CUDA(cudaMemcpyAsync(evecs_host, Z.p, Z.bytes(), cudaMemcpyDeviceToHost, st));
+    if (count <= 0) return;
+    EigWork& w = eig_work();
+    const size_t mm = (size_t)count * m * m;
+    w.A.alloc_at_least(mm);
+    w.E.alloc_at_least((size_t)count * m);
+    w.Z.alloc_at_least(mm);
+    ED_CUDA(cudaMemcpyAsync(w.A.p, a_host, mm * 8, cudaMemcpyHostToDevice, st));
+    jacobi_launch(m, count, w.A.p, w.E.p, w.Z.p, w, st);
+    ED_CUDA(cudaMemcpyAsync(evals_host, w.E.p, (size_t)count * m * 8, cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaMemcpyAsync(evecs_host, w.Z.p, mm * 8, cudaMemcpyDeviceToHost, st));
     ED_CUDA(cudaStreamSynchronize(st));
-}
-
-void sym_eigen_small(int m, const std::vector<double>& a, std::vector<double>& evals, std::vector<double>& evecs,
-                     cudaStream_t st)
-{
-    ED_REQUIRE(m >= 1 && (int64_t)a.size() >= (int64_t)m * m, ED_ERR_ARG, "sym_eigen_small: bad size");
-    if (m > kDeviceEigenMax) {
-        sym_eigen(m, a, evals, evecs);
-        return;
-    }
-    evals.resize(m);
-    evecs.resize((size_t)m * m);
-    sym_eigen_batched(m, 1, a.data(), evals.data(), evecs.data(), st);
 }
 
 }  // namespace edgb

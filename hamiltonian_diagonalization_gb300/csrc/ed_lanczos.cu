@@ -514,7 +514,7 @@ void dense_solve(const ed_op& op, int nev, double* evals_host, double* evecs_dev
     for (int64_t i = 0; i < n; ++i)
         for (int64_t j = 0; j < n; ++j) A[(size_t)i * n + j] = 0.5 * (hx[(size_t)j * n + i] + hx[(size_t)i * n + j]);
     std::vector<double> ev, vec;
-    sym_eigen_small((int)n, A, ev, vec, st);
+    sym_eigen((int)n, A, ev, vec);
     for (int i = 0; i < nev; ++i) evals_host[i] = ev[i];
     if (evecs_dev)
         ED_CUDA(cudaMemcpyAsync(evecs_dev, vec.data(), (size_t)n * nev * 8, cudaMemcpyHostToDevice, st));
@@ -742,7 +742,7 @@ void lanczos_once(const ed_op& op, const ed_lanczos_params& p, const double* v0_
         std::vector<double> Tm((size_t)m_eff * m_eff);
         for (int i = 0; i < m_eff; ++i)
             for (int j = 0; j < m_eff; ++j) Tm[(size_t)i * m_eff + j] = T[(size_t)i * m + j];
-        sym_eigen_small(m_eff, Tm, theta, Y, st);
+        sym_eigen(m_eff, Tm, theta, Y);
         beta_last = hstop ? 0.0 : beta_h[m - 1];
         int nconv = 0;
         double maxres = 0.0;
@@ -1061,7 +1061,7 @@ void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczo
                 P[(size_t)i * nev + j] = P[(size_t)j * nev + i] = a;
             }
         std::vector<double> ev, Y;
-        sym_eigen_small(nev, P, ev, Y, st);
+        sym_eigen(nev, P, ev, Y);
         RotateScratch rot;
         rotate_basis(A.p, n, nev, Y.data(), nev, nev, Ar.p, rot, 0, st);
         std::swap(A.p, Ar.p);

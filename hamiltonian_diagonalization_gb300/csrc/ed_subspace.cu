@@ -487,7 +487,7 @@ void batch_subspace_ritz(const ed_batch& bt, const ed_subspace& sp, int nev, int
     HQ.release();
     // every Hamiltonian's projected matrix and its lowest nev Ritz pairs
     DevBuf<double> Md((size_t)nev * d * B);
-    if (d <= kDeviceEigenMax) {
+    if (d <= kDeviceEigenMax && B >= kDeviceEigenMinBatch) {
         // assembled, solved (one CTA per Hamiltonian) and laid out on the device
         DevBuf<double> al((size_t)B * r), Mall((size_t)B * d * d), E((size_t)B * d), Z((size_t)B * d * d),
             ev((size_t)B * nev);
@@ -500,7 +500,8 @@ void batch_subspace_ritz(const ed_batch& bt, const ed_subspace& sp, int nev, int
         ED_CUDA(cudaMemcpyAsync(evals, ev.p, (size_t)B * nev * 8, cudaMemcpyDeviceToHost, st));
         ED_CUDA(cudaStreamSynchronize(st));
     } else {
-        // subspaces above the device eigensolver's size: the same on the host
+        // subspaces above the device eigensolver's size, or too few
+        // Hamiltonians to beat the host: the same on the host
         std::vector<std::vector<double>> A(r, std::vector<double>((size_t)d * d));
         for (int k = 0; k < r; ++k)
             ED_CUDA(cudaMemcpyAsync(A[k].data(), Akd.p + (size_t)k * d * d, (size_t)d * d * 8, cudaMemcpyDeviceToHost,

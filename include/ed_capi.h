@@ -245,17 +245,19 @@ ed_status ed_lanczos_two_level(const ed_basis* b, const ed_op* op, const ed_lanc
 ed_status ed_lanczos_device(const ed_op* op, const ed_lanczos_params* p, const double* v0_dev,
                             double* evals_host, double* evecs_dev, ed_solve_info* info);
 
-/* Dense symmetric eigen-decomposition in FP64: a is m*m row-major (host),
- * evals ascending, evecs column-major (may be NULL).  On the device (cyclic
- * Jacobi) for m <= 128, on the host (Householder tridiagonalisation +
- * implicit QR with Wilkinson shifts) above.  The projected-matrix solver of
- * ed_lanczos, exposed for reuse; replaces the small dense problems the
- * reference hands to LAPACK dsyevr_ (utilities/wrappers/lapack_wrapper.hpp:479-540,
- * FullDiagonalize, hamiltonians/hamiltonian_base.hpp:634-758). */
+/* Dense symmetric eigen-decomposition on the host (FP64; Householder
+ * tridiagonalisation + implicit QR with Wilkinson shifts): a is m*m row-major,
+ * evals ascending, evecs column-major (may be NULL).  The projected-matrix
+ * solver of ed_lanczos (one small matrix per restart solves faster on a host
+ * core than on one SM's FP64 pipe), exposed for reuse; replaces the small
+ * dense problems the reference hands to LAPACK dsyevr_
+ * (utilities/wrappers/lapack_wrapper.hpp:479-540, FullDiagonalize,
+ * hamiltonians/hamiltonian_base.hpp:634-758). */
 ed_status ed_dense_sym_eigen(int m, const double* a, double* evals, double* evecs);
-/* count such m x m matrices (1 <= m <= 128) at once on the device, one CTA
- * each: a count*m*m, evals count*m, evecs count*m*m (host arrays).  The
- * batched solver's and the subspace Ritz step's projected problems; the
+/* count such m x m matrices (1 <= m <= 128) at once on the device (FP64
+ * cyclic Jacobi, one CTA each): a count*m*m, evals count*m, evecs count*m*m
+ * (host arrays).  The projected problems of the batched solver and of the
+ * subspace Ritz step, where a batch solves in the time of one matrix; the
  * batched counterpart of the dsyevr_ calls above. */
 ed_status ed_sym_eigen_batched(int m, int count, const double* a, double* evals, double* evecs);
 
