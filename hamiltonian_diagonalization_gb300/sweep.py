@@ -437,6 +437,136 @@ def run_subspace(N, norb, sectors, v1s, nev, tol, seed, ncv=0, **kw):
     return time.perf_counter() - t0, evals, recs
 
 
+def warm_started_solve(N, norb, tlz, pp, nev, v0, tol=1e-10, seed=1, matrix_free=True, mix=None,
+                       want_vectors=False):
+    """One sector solve from a warm start v0 with the seeded random start as
+    the fallback: v0 is not used when it is missing, not finite or zero, and
+    the solve is repeated from the random start when the warm one does not
+    converge all nev pairs.  For nev > 1 the random start is mixed in at mix
+    (default 0.1) times the unit warm vector's norm, because a start that is
+    one eigenvector of a symmetric problem holds nothing of the states of the
+    other symmetry classes.  Returns (result of solve_sector, fallback)."""
+    import hamiltonian_diagonalization_gb300 as ed
+    if mix is None:
+        mix = 0.1 if nev > 1 else 0.0
+    use = v0 is not None
+    if use:
+        v0 = np.asarray(v0, dtype=np.float64)
+        nrm = float(np.linalg.norm(v0))
+        use = bool(np.isfinite(nrm) and nrm > 0.0)
+    if use:
+        v0 = v0 / nrm
+        if mix > 0.0:
+            r = np.random.default_rng(seed).uniform(-1.0, 1.0, len(v0))
+            v0 = v0 + mix * r / np.linalg.norm(r)
+        out = ed.solve_sector(N, norb, tlz, pp, nev, tol=tol, v0=v0, matrix_free=matrix_free,
+                              want_vectors=want_vectors)
+        if out["info"]["converged"] >= nev:
+            return out, False
+    return ed.solve_sector(N, norb, tlz, pp, nev, tol=tol, seed=seed, matrix_free=matrix_free,
+                           want_vectors=want_vectors), True
+
+
+def matfree_warm_start(N, norb, tlz, nevs=(1, 3), train_v1s=None, target_v1=None, mixes=(0.0,),
+                       steps=3000, batch=4096, lr=2e-3, hidden=256, seed=1, tol=1e-10):
+    """The learned warm start of a matrix-free solve.
+
+    The network is trained on this sector's ground states at the training V1
+    points (by default every second point of the V1 sweep linspace(0.5, 3.0,
+    64) up to 0.82, solved together on the batch's shared pattern).  It
+    predicts the ground state of the target Hamiltonian: the LLL Coulomb list,
+    with V1 = target_v1 when given.  The matrix-free Lanczos of each nev in
+    nevs then starts from:
+      random   the seeded uniform start, which is also the fallback when a
+               warm solve does not converge;
+      nearest  the training ground state nearest in V1 (the continuation start);
+      mlp      the prediction, mixed with mix times its norm of the random start
+               for each mix in mixes (mix 0: the prediction alone);
+      delta    the nearest ground state with each amplitude scaled by the
+               network's change of |psi| from the nearest V1 to the target
+               (exp(f(x, V1_target) - f(x, V1_nearest)), capped at e^{+-3}):
+               the network's learned V1 dependence, without its sign output;
+      extrap   linear extrapolation in V1 from the two nearest ground states
+               (sign-aligned), the same correction without a network.
+    Returns the times, products, eigenvalue agreement with the random start,
+    and the overlaps of the prediction and of the nearest ground state with
+    the converged ground state."""
+    import torch
+
+    import hamiltonian_diagonalization_gb300 as ed
+    pp = ed.odd_coulomb_list(norb)
+    if target_v1 is not None:
+        pp[1] = target_v1
+    target = float(pp[1])
+    if train_v1s is None:
+        train_v1s = np.linspace(0.5, 3.0, 64)[0:11:2]
+    train = np.asarray(train_v1s, dtype=float)
+    b = ed.FermionFockBasis()
+    b.GenerateFockSpace(N, norb, tlz)
+    n = b.GetStoredDimension()
+    rec = {"N": N, "norb": norb, "two_lz": tlz, "n": n, "target_v1": target, "train_v1": train.tolist()}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bt = ed.HamiltonianBatch(b, sweep_lists(norb, train))
+    _, vec, inf_t = bt.solve(1, tol=tol, seed=seed, want_vectors=True)
+    psi = vec[0].contiguous()
+    del bt, vec
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    net = ed.WarmStartMLP(norb, hidden, seed=seed)
+    loss = net.fit(b, train, psi, steps=steps, batch=batch, lr=lr, seed=seed + 1)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    order = np.argsort(np.abs(train - target), kind="stable")
+    i0, i1 = int(order[0]), int(order[min(1, len(order) - 1)])
+    V0 = torch.empty((n, 2), dtype=torch.float64, device="cuda")
+    net.warm_start(b, np.array([target, train[i0]]), V0)
+    near_d = psi[:, i0]
+    ratio = V0[:, 0].abs() / V0[:, 1].abs()
+    ratio = torch.where(torch.isfinite(ratio), ratio, torch.ones_like(ratio)).clamp(np.exp(-3.0), np.exp(3.0))
+    delta = (near_d * ratio).cpu().numpy()
+    pred = V0[:, 0].cpu().numpy()
+    near = near_d.cpu().numpy()
+    second = psi[:, i1].cpu().numpy()
+    del V0, psi, near_d, ratio
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    if np.dot(second, near) < 0:
+        second = -second
+    extrap = near + (target - train[i0]) / (train[i1] - train[i0]) * (second - near) if i1 != i0 else near
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(-1.0, 1.0, n)
+    r /= np.linalg.norm(r)
+    pn = np.linalg.norm(pred)
+    rec.update({"train_solve_s": t1 - t0, "train_block_products": inf_t["block_products"], "fit_s": t2 - t1,
+                "fit_loss": loss, "predict_s": t3 - t2, "prediction_finite": bool(np.isfinite(pn) and pn > 0),
+                "solves": {}})
+    starts = [("nearest", near), ("extrap", extrap)]
+    if rec["prediction_finite"]:
+        starts += [("delta", delta)] + [(f"mlp_mix{m:g}", pred / pn + m * r) for m in mixes]
+
+    for nev in nevs:
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        rand = ed.solve_sector(N, norb, tlz, pp, nev, tol=tol, seed=seed, matrix_free=True, want_vectors=True)
+        tr = time.perf_counter() - ta
+        g = rand["eigenvectors"][0]
+        res = {"random": {"s": tr, "products": rand["info"]["matvecs"], "max_residual": rand["info"]["max_residual"]},
+               "eigenvalues": rand["eigenvalues"].tolist()}
+        for name, v0 in starts:
+            torch.cuda.synchronize()
+            ta = time.perf_counter()
+            out, fallback = warm_started_solve(N, norb, tlz, pp, nev, v0, tol=tol, seed=seed, mix=0.0)
+            tw = time.perf_counter() - ta
+            res[name] = {"s": tw, "products": out["info"]["matvecs"], "fallback": bool(fallback),
+                         "overlap": abs(float(np.dot(g, v0))) / (np.linalg.norm(v0) * np.linalg.norm(g)),
+                         "max_residual": out["info"]["max_residual"],
+                         "max_rel_eig_diff": float(np.max(np.abs(out["eigenvalues"] - rand["eigenvalues"]) /
+                                                          np.abs(rand["eigenvalues"])))}
+        rec["solves"][str(nev)] = res
+    return rec
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--N", type=int, default=10)
@@ -454,7 +584,15 @@ def main():
     ap.add_argument("--mlp-lr", type=float, default=2e-3)
     ap.add_argument("--batch-size", type=int, default=0, help="Hamiltonians per batch (0: all of a sector)")
     ap.add_argument("--ncv", type=int, default=0, help="Krylov dimension of the batched solves (0: 2*nev+21)")
+    ap.add_argument("--matfree-steps", type=int, default=20000, help="training steps of --matfree-warm")
+    ap.add_argument("--matfree-warm", action="store_true",
+                    help="the learned warm start of one matrix-free solve (the LLL Coulomb Hamiltonian of --N, "
+                         "--norb, first sector) instead of a sweep")
     args = ap.parse_args()
+    if args.matfree_warm:
+        print(json.dumps(matfree_warm_start(args.N, args.norb, int(args.sectors.split(",")[0]),
+                                            steps=args.matfree_steps, lr=args.mlp_lr, seed=args.seed)))
+        return
     sectors = [int(s) for s in args.sectors.split(",")]
     known = {"plain", "batched", "warm", "continuation", "subspace"}
     modes = {"both": {"plain", "batched"}, "all": set(known)}.get(args.mode, set(args.mode.split(",")))
