@@ -13,10 +13,13 @@
 // (cterms_derive); the device build and product are in ed_build.cu and here.
 //
 // The eigensolver is a thick-restart Lanczos on complex vectors stored as
-// (re, im) pairs: full complex Gram-Schmidt (two passes) against the Krylov
-// basis, the real projected matrix (alpha and beta of a Hermitian operator
-// are real) solved on the host, restart rotations of the complex basis by the
-// real Ritz coefficients.  It replaces ArpackWrapper's complex driver
+// (re, im) pairs, run like the real solver: each restart cycle is one CUDA
+// graph in which every step (product, local three-term step, complex
+// classical Gram-Schmidt against the whole basis with a DGKS-gated second
+// pass, normalisation) keeps its scalars in device memory; the host reads the
+// real projected matrix (alpha and beta of a Hermitian operator are real)
+// once per cycle, solves it, and restarts by rotating the complex basis with
+// the real Ritz coefficients.  It replaces ArpackWrapper's complex driver
 // (the T = dcmplx branches of arpack_wrapper.hpp:255-937, znaupd_/zneupd_
 // with WHICH "SR").
 #include <algorithm>
@@ -152,60 +155,266 @@ __device__ __forceinline__ void cchunk(int64_t n, int nb, int b, int64_t& r0, in
     if (r0 > n) r0 = n;
 }
 
-// part[(i*nb + b)*2 + {0,1}] = block b's share of V_i^H w (complex), i < J,
-// and part[(J*nb + b)*2] its share of ||w||^2.
-__global__ void __launch_bounds__(kCThreads) k_cdots(const double2* __restrict__ V, int J, const double2* __restrict__ w,
-                                                     int64_t n, double* __restrict__ part)
+constexpr double kCDgksEta = 0.7071067811865476;
+
+__device__ __forceinline__ double cwarp_sum(double v)
 {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Completion of a reduction launch without a second kernel: every block calls
+// this after writing its partials; it returns true in exactly one block, the
+// last to arrive, which then sees every block's partials and resets the
+// counter for the next launch.  Nothing waits on another block.
+__device__ __forceinline__ bool clast_block(unsigned int* counter)
+{
+    __shared__ unsigned int ticket;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
+    __syncthreads();
+    const bool last = ticket == gridDim.x - 1;
+    if (last) {
+        __threadfence();
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+    return last;
+}
+
+// Sum of nb partials (stride st) in a fixed order, whichever block runs it; in
+// thread 0.
+__device__ __forceinline__ double csum_parts(const double* p, int nb, int stride, double* red)
+{
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += kCThreads) s += __ldcg(p + (int64_t)i * stride);
+    return cblock_sum(s, red);
+}
+
+// Local step scalars of step j (w = H v_j): alpha = Re v_j^H w into
+// coefcol[j] (a Hermitian operator's alpha is real), beta_{j-1} into
+// coefcol[j-1], ||w||^2 into *hv2; the last block writes them.
+__global__ void __launch_bounds__(kCThreads) k_clocal(const double2* __restrict__ vj, const double2* __restrict__ w,
+                                                      int64_t n, double* __restrict__ part,
+                                                      unsigned int* __restrict__ counter, double* __restrict__ coefcol,
+                                                      int j, const double* __restrict__ beta_prev,
+                                                      double* __restrict__ hv2, const int* __restrict__ stop)
+{
+    if (*stop) return;
     __shared__ double red[kCThreads / 32];
     int64_t r0, r1;
     cchunk(n, gridDim.x, blockIdx.x, r0, r1);
-    {
-        double s = 0.0;
-        for (int64_t r = r0 + threadIdx.x; r < r1; r += kCThreads) {
-            const double2 b = w[r];
-            s = fma(b.x, b.x, s);
-            s = fma(b.y, b.y, s);
+    double a = 0.0, b = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCThreads) {
+        const double2 v = vj[r], x = w[r];
+        a = fma(v.x, x.x, a);
+        a = fma(v.y, x.y, a);
+        b = fma(x.x, x.x, b);
+        b = fma(x.y, x.y, b);
+    }
+    a = cblock_sum(a, red);
+    b = cblock_sum(b, red);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = a;
+        part[gridDim.x + blockIdx.x] = b;
+    }
+    if (!clast_block(counter)) return;
+    a = csum_parts(part, gridDim.x, 1, red);
+    b = csum_parts(part + gridDim.x, gridDim.x, 1, red);
+    if (threadIdx.x == 0) {
+        coefcol[j] = a;
+        coefcol[j - 1] = *beta_prev;
+        *hv2 = b;
+    }
+}
+
+// Complex multi-dot against the Krylov basis, R rows per block (R double2 of
+// dynamic shared memory hold the block's slice of w): the block's shares of
+// V_i^H w (i < J) and of ||w||^2 go to part[(i*nb + b)*2 + {re, im}].  With
+// local != 0 the three-term step w -= alpha v_{J-1} + beta v_{J-2} (real
+// alpha, beta) is applied to the slice while it is staged and written back.
+// Warps take the columns in turn, eight loads per lane in flight.  The last
+// block sums the partials column by column in a fixed order: c[i] (i < J;
+// Re c[i] also added to coefcol[i] when coefcol is given) and *before =
+// ||w||^2.  Runs when run is null or *run != 0, and stop is clear.
+__global__ void __launch_bounds__(kCThreads) k_cmdot(const double2* __restrict__ V, int64_t n, int R, int J,
+                                                     double2* __restrict__ w, int local,
+                                                     const double* __restrict__ alpha,
+                                                     const double* __restrict__ beta_prev, double* __restrict__ part,
+                                                     unsigned int* __restrict__ counter, double2* __restrict__ c,
+                                                     double* __restrict__ coefcol, double* __restrict__ before,
+                                                     const int* __restrict__ run, const int* __restrict__ stop)
+{
+    if ((run && !*run) || (stop && *stop)) return;
+    extern __shared__ double2 csw[];
+    const int64_t r0 = (int64_t)blockIdx.x * R;
+    const int len = (int)min((int64_t)R, n - r0);
+    if (local) {
+        const double a = *alpha, b = *beta_prev;
+        const double2* vj = V + (int64_t)(J - 1) * n + r0;
+        const double2* vjm1 = V + (int64_t)(J - 2) * n + r0;
+        for (int i = threadIdx.x; i < len; i += kCThreads) {
+            const double2 p = vj[i], q = vjm1[i];
+            double2 x = w[r0 + i];
+            x.x = fma(-b, q.x, fma(-a, p.x, x.x));
+            x.y = fma(-b, q.y, fma(-a, p.y, x.y));
+            w[r0 + i] = x;
+            csw[i] = x;
         }
-        s = cblock_sum(s, red);
-        if (threadIdx.x == 0) {
-            part[((int64_t)J * gridDim.x + blockIdx.x) * 2] = s;
-            part[((int64_t)J * gridDim.x + blockIdx.x) * 2 + 1] = 0.0;
+    } else {
+        for (int i = threadIdx.x; i < len; i += kCThreads) csw[i] = w[r0 + i];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nb = gridDim.x;
+    for (int i = warp; i <= J; i += kCThreads / 32) {
+        double re0 = 0.0, re1 = 0.0, im0 = 0.0, im1 = 0.0;
+        int r = lane;
+        if (i < J) {
+            const double2* col = V + (int64_t)i * n + r0;
+            for (; r + 224 < len; r += 256) {
+                double2 x[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) x[u] = col[r + 32 * u];
+#pragma unroll
+                for (int u = 0; u < 8; u += 2) {
+                    const double2 s0 = csw[r + 32 * u], s1 = csw[r + 32 * (u + 1)];
+                    re0 = fma(x[u].x, s0.x, re0);
+                    re0 = fma(x[u].y, s0.y, re0);
+                    im0 = fma(x[u].x, s0.y, im0);
+                    im0 = fma(-x[u].y, s0.x, im0);
+                    re1 = fma(x[u + 1].x, s1.x, re1);
+                    re1 = fma(x[u + 1].y, s1.y, re1);
+                    im1 = fma(x[u + 1].x, s1.y, im1);
+                    im1 = fma(-x[u + 1].y, s1.x, im1);
+                }
+            }
+            for (; r < len; r += 32) {
+                const double2 x = col[r], s0 = csw[r];
+                re0 = fma(x.x, s0.x, re0);
+                re0 = fma(x.y, s0.y, re0);
+                im0 = fma(x.x, s0.y, im0);
+                im0 = fma(-x.y, s0.x, im0);
+            }
+        } else {
+            for (; r < len; r += 32) {
+                const double2 s0 = csw[r];
+                re0 = fma(s0.x, s0.x, re0);
+                re0 = fma(s0.y, s0.y, re0);
+            }
+        }
+        const double re = cwarp_sum(re0 + re1), im = cwarp_sum(im0 + im1);
+        if (lane == 0) {
+            part[((int64_t)i * nb + blockIdx.x) * 2] = re;
+            part[((int64_t)i * nb + blockIdx.x) * 2 + 1] = im;
         }
     }
-    for (int i = 0; i < J; ++i) {
-        const double2* vi = V + (int64_t)i * n;
+    if (!clast_block(counter)) return;
+    for (int i = warp; i <= J; i += kCThreads / 32) {
         double re = 0.0, im = 0.0;
-        for (int64_t r = r0 + threadIdx.x; r < r1; r += kCThreads) {
-            const double2 a = vi[r], b = w[r];
-            re = fma(a.x, b.x, re);
-            re = fma(a.y, b.y, re);
-            im = fma(a.x, b.y, im);
-            im = fma(-a.y, b.x, im);
+        for (int b = lane; b < nb; b += 32) {
+            re += __ldcg(part + ((int64_t)i * nb + b) * 2);
+            im += __ldcg(part + ((int64_t)i * nb + b) * 2 + 1);
         }
-        re = cblock_sum(re, red);
-        im = cblock_sum(im, red);
-        if (threadIdx.x == 0) {
-            part[((int64_t)i * gridDim.x + blockIdx.x) * 2] = re;
-            part[((int64_t)i * gridDim.x + blockIdx.x) * 2 + 1] = im;
+        re = cwarp_sum(re);
+        im = cwarp_sum(im);
+        if (lane == 0) {
+            if (i < J) {
+                c[i] = make_double2(re, im);
+                if (coefcol) coefcol[i] += re;
+            } else {
+                *before = re;
+            }
         }
     }
 }
 
-// w -= sum_i c_i V_i (c complex, device).
-__global__ void __launch_bounds__(kCThreads) k_cupdate(const double2* __restrict__ V, int J,
-                                                       const double2* __restrict__ c, double2* __restrict__ w,
-                                                       int64_t n)
+// w -= V[:, 0..J) c (complex c) and a per-block partial of ||w||^2.  The last
+// block then finishes the pass:
+//   mode 1 (first pass): *need2 = force2 or ||w||^2 < eta^2 *before (the
+//          DGKS test); without a second pass also beta and the breakdown test;
+//   mode 2 (second pass): beta and the breakdown test;
+//   mode 0: nothing (the counter is not touched).
+// beta = ||w||; breakdown (stop = j + 1) when beta <= 1e-12 sqrt(*ref2).
+__global__ void __launch_bounds__(kCThreads) k_cupd(const double2* __restrict__ V, int64_t n, int J,
+                                                    const double2* __restrict__ c, double2* __restrict__ w,
+                                                    double* __restrict__ npart, unsigned int* __restrict__ counter,
+                                                    int mode, int force2, const double* __restrict__ before,
+                                                    int* __restrict__ need2, double* __restrict__ beta,
+                                                    const double* __restrict__ ref2, int j,
+                                                    const int* __restrict__ run, int* __restrict__ stop)
 {
+    if ((run && !*run) || (stop && *stop)) return;
+    extern __shared__ double2 cc[];
+    __shared__ double red[kCThreads / 32];
+    for (int i = threadIdx.x; i < J; i += kCThreads) cc[i] = c[i];
+    __syncthreads();
+    int64_t r0, r1;
+    cchunk(n, gridDim.x, blockIdx.x, r0, r1);
+    double nn = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCThreads) {
+        double2 a = w[r], b = make_double2(0.0, 0.0);
+        int i = 0;
+        for (; i + 4 <= J; i += 4) {
+            double2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = V[(int64_t)(i + u) * n + r];
+#pragma unroll
+            for (int u = 0; u < 4; u += 2) {
+                const double2 c0 = cc[i + u], c1 = cc[i + u + 1];
+                a.x = fma(-c0.x, v[u].x, a.x);
+                a.x = fma(c0.y, v[u].y, a.x);
+                a.y = fma(-c0.x, v[u].y, a.y);
+                a.y = fma(-c0.y, v[u].x, a.y);
+                b.x = fma(-c1.x, v[u + 1].x, b.x);
+                b.x = fma(c1.y, v[u + 1].y, b.x);
+                b.y = fma(-c1.x, v[u + 1].y, b.y);
+                b.y = fma(-c1.y, v[u + 1].x, b.y);
+            }
+        }
+        for (; i < J; ++i) {
+            const double2 v = V[(int64_t)i * n + r], c0 = cc[i];
+            a.x = fma(-c0.x, v.x, a.x);
+            a.x = fma(c0.y, v.y, a.x);
+            a.y = fma(-c0.x, v.y, a.y);
+            a.y = fma(-c0.y, v.x, a.y);
+        }
+        a.x += b.x;
+        a.y += b.y;
+        w[r] = a;
+        nn = fma(a.x, a.x, nn);
+        nn = fma(a.y, a.y, nn);
+    }
+    nn = cblock_sum(nn, red);
+    if (threadIdx.x == 0) npart[blockIdx.x] = nn;
+    if (mode == 0 || !clast_block(counter)) return;
+    const double s = csum_parts(npart, gridDim.x, 1, red);
+    if (threadIdx.x == 0) {
+        bool finish = true;
+        if (mode == 1) {
+            const int again = (force2 || s < kCDgksEta * kCDgksEta * (*before)) ? 1 : 0;
+            *need2 = again;
+            finish = !again;
+        }
+        if (finish) {
+            const double b = sqrt(s);
+            *beta = b;
+            if (!(b > 1e-12 * sqrt(fmax(*ref2, 0.0)))) *stop = j + 1;
+        }
+    }
+}
+
+// w /= *beta unless the cycle stopped.
+__global__ void __launch_bounds__(kCThreads) k_cscale_dev(double2* __restrict__ w, int64_t n,
+                                                          const double* __restrict__ beta, const int* __restrict__ stop)
+{
+    if (*stop) return;
+    const double inv = 1.0 / *beta;
     for (int64_t r = blockIdx.x * (int64_t)kCThreads + threadIdx.x; r < n; r += (int64_t)gridDim.x * kCThreads) {
         double2 a = w[r];
-        for (int i = 0; i < J; ++i) {
-            const double2 v = V[(int64_t)i * n + r], ci = c[i];
-            a.x = fma(-ci.x, v.x, a.x);
-            a.x = fma(ci.y, v.y, a.x);
-            a.y = fma(-ci.x, v.y, a.y);
-            a.y = fma(-ci.y, v.x, a.y);
-        }
+        a.x *= inv;
+        a.y *= inv;
         w[r] = a;
     }
 }
@@ -273,54 +482,37 @@ std::vector<double> host_parts(const DevBuf<double>& part, size_t count, cudaStr
     return h;
 }
 
-// Working state of one complex solve.
+// Working state of one complex solve: reduction partials, the projected
+// matrix's columns as the device accumulates them (coef, (m+1) per step),
+// beta, the current pass's coefficients, the step scalars (scal: 0 ||w||^2
+// before the first pass, 1 ||H v_j||^2, 2 before the second pass, 3 scratch)
+// and the flags (need2, stop) and completion counters of the cycle's kernels.
 struct CWork {
     int64_t n = 0;
-    int nb = 1;
-    DevBuf<double> part, c;
-};
+    int m = 0;
+    int nb = 1;            // blocks of the row-chunked kernels
+    int R = 512, nbm = 1;  // multi-dot: rows per block, blocks
+    DevBuf<double> part, npart, coef, beta, c, scal;
+    DevBuf<int> flags;
+    DevBuf<unsigned int> counters;
 
-// Orthogonalise w against V[0..J) twice (complex); returns the summed
-// coefficients V_i^H w of both passes.  norm_in: ||w|| before the passes;
-// norm_out: ||w|| after them, from the second pass's dots (Pythagoras: w
-// loses exactly V c of norm |c| to an orthonormal V), so a step needs two
-// host round trips.
-std::vector<cplx> cgram_schmidt(CWork& cw, const double2* V, int J, double2* w, cudaStream_t st,
-                                double* norm_in = nullptr, double* norm_out = nullptr)
-{
-    std::vector<cplx> acc(J, cplx(0.0, 0.0));
-    for (int pass = 0; pass < 2; ++pass) {
-        k_cdots<<<cw.nb, kCThreads, 0, st>>>(V, J, w, cw.n, cw.part.p);
+    void mdot(const double2* V, int J, double2* w, int local, const double* alpha, const double* beta_prev,
+              double* coefcol, double* before, const int* run, const int* stop, cudaStream_t st)
+    {
+        k_cmdot<<<nbm, kCThreads, (size_t)R * 16, st>>>(V, n, R, J, w, local, alpha, beta_prev, part.p,
+                                                        counters.p + 1, reinterpret_cast<double2*>(c.p), coefcol,
+                                                        before, run, stop);
         count_launch();
-        ED_CUDA(cudaGetLastError());
-        const std::vector<double> h = host_parts(cw.part, (size_t)(J + 1) * cw.nb * 2, st);
-        double nn = 0.0;
-        for (int b = 0; b < cw.nb; ++b) nn += h[((size_t)J * cw.nb + b) * 2];
-        std::vector<double> c(2 * (size_t)J);
-        for (int i = 0; i < J; ++i) {
-            double re = 0.0, im = 0.0;
-            for (int b = 0; b < cw.nb; ++b) {
-                re += h[((size_t)i * cw.nb + b) * 2];
-                im += h[((size_t)i * cw.nb + b) * 2 + 1];
-            }
-            c[2 * i] = re;
-            c[2 * i + 1] = im;
-            acc[i] += cplx(re, im);
-        }
-        if (pass == 0 && norm_in) *norm_in = std::sqrt(nn);
-        if (pass == 1 && norm_out) {
-            double removed = 0.0;
-            for (int i = 0; i < J; ++i) removed += c[2 * i] * c[2 * i] + c[2 * i + 1] * c[2 * i + 1];
-            *norm_out = std::sqrt(std::max(0.0, nn - removed));
-        }
-        if (J == 0) break;
-        ED_CUDA(cudaMemcpyAsync(cw.c.p, c.data(), c.size() * 8, cudaMemcpyHostToDevice, st));
-        k_cupdate<<<csms() * 4, kCThreads, 0, st>>>(V, J, reinterpret_cast<const double2*>(cw.c.p), w, cw.n);
-        count_launch();
-        ED_CUDA(cudaGetLastError());
     }
-    return acc;
-}
+    void update(const double2* V, int J, double2* w, int mode, int force2, const double* before, int* need2,
+                double* b, const double* ref2, int j, const int* run, int* stop, cudaStream_t st)
+    {
+        k_cupd<<<nb, kCThreads, (size_t)J * 16, st>>>(V, n, J, reinterpret_cast<const double2*>(c.p), w, npart.p,
+                                                      counters.p + 2, mode, force2, before, need2, b, ref2, j, run,
+                                                      stop);
+        count_launch();
+    }
+};
 
 double cnorm(CWork& cw, const double2* w, cudaStream_t st)
 {
@@ -338,6 +530,21 @@ void cscale(double2* w, int64_t n, double s, cudaStream_t st)
     k_cscale<<<csms() * 4, kCThreads, 0, st>>>(w, n, s);
     count_launch();
     ED_CUDA(cudaGetLastError());
+}
+
+// Orthogonalise column col of V against columns [0, col) twice, then
+// normalise it; fails on a zero or non-finite result.
+void corthonormalise(CWork& cw, double2* V, int col, cudaStream_t st)
+{
+    double2* x = V + (int64_t)col * cw.n;
+    for (int pass = 0; col > 0 && pass < 2; ++pass) {
+        cw.mdot(V, col, x, 0, nullptr, nullptr, nullptr, cw.scal.p + 3, nullptr, nullptr, st);
+        cw.update(V, col, x, 0, 0, nullptr, nullptr, nullptr, nullptr, 0, nullptr, nullptr, st);
+        ED_CUDA(cudaGetLastError());
+    }
+    const double nrm = cnorm(cw, x, st);
+    ED_REQUIRE(nrm > 0.0 && std::isfinite(nrm), ED_ERR_ARG, "start vector is zero or not finite");
+    cscale(x, cw.n, 1.0 / nrm, st);
 }
 
 // Dense path (dimension below 60, as the real solver): M applied to the unit
@@ -573,89 +780,174 @@ void clanczos_solve(const ed_ccrs& a, const ed_lanczos_params& p, const double* 
     m64 = std::min<int64_t>(m64, n - 1);
     m64 = std::min<int64_t>(m64, 1000);
     const int m = (int)m64;
+    const int nsm = csms();
     CWork cw;
     cw.n = n;
-    cw.nb = (int)std::max<int64_t>(1, std::min<int64_t>(csms() * 4, n / 1024));
-    cw.part.alloc((size_t)(m + 2) * cw.nb * 2);
+    cw.m = m;
+    cw.nb = (int)std::max<int64_t>(1, std::min<int64_t>(nsm * 4, n / 1024));
+    // multi-dot slices: three blocks per SM, 512 to 6144 rows (96 KB of
+    // shared memory) a block, a multiple of 128
+    {
+        int64_t nbt = (int64_t)nsm * 3, R = 0;
+        for (;;) {
+            R = std::max<int64_t>(512, ((n + nbt - 1) / nbt + 127) / 128 * 128);
+            if (R <= 6144) break;
+            nbt += nsm;
+        }
+        cw.R = (int)R;
+        cw.nbm = (int)((n + R - 1) / R);
+        if ((size_t)R * 16 > 48 * 1024)
+            ED_CUDA(cudaFuncSetAttribute(k_cmdot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(R * 16)));
+    }
+    cw.part.alloc((size_t)(m + 2) * std::max(cw.nb, cw.nbm) * 2);
+    cw.npart.alloc(cw.nb);
+    cw.coef.alloc((size_t)(m + 1) * (m + 1));
+    cw.beta.alloc(m + 2);
     cw.c.alloc(2 * (size_t)(m + 2));
+    cw.scal.alloc(4);
+    cw.flags.alloc(2);
+    cw.counters.alloc(4);
+    ED_CUDA(cudaMemsetAsync(cw.beta.p, 0, (m + 2) * 8, st));
+    ED_CUDA(cudaMemsetAsync(cw.counters.p, 0, 4 * sizeof(unsigned int), st));
     DevBuf<double> Vb(2 * (size_t)n * (m + 1)), V2b(2 * (size_t)n * (m + 1));
     auto col = [&](DevBuf<double>& B, int j) { return reinterpret_cast<double2*>(B.p + 2 * (size_t)n * j); };
     RotateScratch rot;
     if (v0_dev) ED_CUDA(cudaMemcpyAsync(Vb.p, v0_dev, 2 * (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
     else {
-        k_crandom<<<csms() * 4, kCThreads, 0, st>>>(Vb.p, 2 * n, p.seed);
+        k_crandom<<<nsm * 4, kCThreads, 0, st>>>(Vb.p, 2 * n, p.seed);
         count_launch();
         ED_CUDA(cudaGetLastError());
     }
-    {
-        const double nrm = cnorm(cw, col(Vb, 0), st);
-        ED_REQUIRE(nrm > 0.0 && std::isfinite(nrm), ED_ERR_ARG, "start vector is zero or not finite");
-        cscale(col(Vb, 0), n, 1.0 / nrm, st);
-    }
-    std::vector<double> T((size_t)m * m, 0.0), theta, Y;
-    std::vector<double> beta(m + 1, 0.0);
-    int k = 0;
-    bool converged = false;
-    float spmv_ms = 0.f;
-    cudaEvent_t e0, e1;
-    ED_CUDA(cudaEventCreate(&e0));
-    ED_CUDA(cudaEventCreate(&e1));
-    struct EvG {
-        cudaEvent_t a, b;
-        ~EvG() { cudaEventDestroy(a); cudaEventDestroy(b); }
-    } evg{e0, e1};
-    for (;;) {
+    corthonormalise(cw, col(Vb, 0), 0, st);
+
+    std::vector<cudaEvent_t> ev(2 * (m + 1), nullptr);
+    for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
+    struct EvGuard {
+        std::vector<cudaEvent_t>& v;
+        ~EvGuard() { for (auto e : v) if (e) cudaEventDestroy(e); }
+    } evguard{ev};
+
+    // One restart cycle, steps k..m-1, all on the device (the real solver's
+    // scheme): the step scalars stay in device memory, the second
+    // Gram-Schmidt pass and a breakdown are flags that later kernels read, and
+    // the cycle is replayed as one CUDA graph.
+    int* need2 = cw.flags.p;
+    int* stop = cw.flags.p + 1;
+    auto enqueue_cycle = [&](double2* V, int k, bool capturing) {
+        ED_CUDA(cudaMemsetAsync(cw.flags.p, 0, 2 * sizeof(int), st));
+        ED_CUDA(cudaMemsetAsync(cw.coef.p + (size_t)k * (m + 1), 0, (size_t)(m - k) * (m + 1) * 8, st));
         for (int j = k; j < m; ++j) {
-            double2* vj = col(Vb, j);
-            double2* w = col(Vb, j + 1);
-            ED_CUDA(cudaEventRecord(e0, st));
+            double2* vj = V + (int64_t)j * n;
+            double2* w = V + (int64_t)(j + 1) * n;
+            double* coefcol = cw.coef.p + (size_t)j * (m + 1);
+            const bool first = (j == k);
+            if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j], st, cudaEventRecordExternal));
+            else ED_CUDA(cudaEventRecord(ev[2 * j], st));
             cspmv(a, reinterpret_cast<const double*>(vj), reinterpret_cast<double*>(w), st);
-            ED_CUDA(cudaEventRecord(e1, st));
-            ++inf.matvecs;
-            double hnorm = 0.0, b = 0.0;
-            const std::vector<cplx> c = cgram_schmidt(cw, col(Vb, 0), j + 1, w, st, &hnorm, &b);
-            float ms = 0.f;
-            ED_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            spmv_ms += ms;
-            for (int i = 0; i <= j; ++i) {
-                T[(size_t)i * m + j] = c[i].real();
-                T[(size_t)j * m + i] = c[i].real();
-            }
-            // below 1e-6 of ||H v|| the Pythagorean norm loses digits: measure it
-            if (b < 1e-6 * hnorm) b = cnorm(cw, w, st);
-            if (!(b > 1e-13 * std::max(1.0, hnorm))) {
-                // invariant subspace: continue from a fresh direction
-                ++inf.breakdowns;
-                k_crandom<<<csms() * 4, kCThreads, 0, st>>>(reinterpret_cast<double*>(w), 2 * n,
-                                                           p.seed + 0x51ED2701ull * (uint64_t)(inf.matvecs + 1));
+            if (capturing) ED_CUDA(cudaEventRecordWithFlags(ev[2 * j + 1], st, cudaEventRecordExternal));
+            else ED_CUDA(cudaEventRecord(ev[2 * j + 1], st));
+            if (!first) {
+                k_clocal<<<cw.nb, kCThreads, 0, st>>>(vj, w, n, cw.part.p, cw.counters.p, coefcol, j,
+                                                      cw.beta.p + (j - 1), cw.scal.p + 1, stop);
                 count_launch();
-                ED_CUDA(cudaGetLastError());
-                cgram_schmidt(cw, col(Vb, 0), j + 1, w, st);
-                const double nr = cnorm(cw, w, st);
-                ED_REQUIRE(nr > 0.0, ED_ERR_INTERNAL, "no direction left after a Krylov breakdown");
-                cscale(w, n, 1.0 / nr, st);
-                b = 0.0;
-            } else {
-                cscale(w, n, 1.0 / b, st);
             }
-            beta[j] = b;
-            if (j + 1 < m) {
-                T[(size_t)j * m + j + 1] = b;
-                T[(size_t)(j + 1) * m + j] = b;
-            }
+            const int J = j + 1;
+            const double* ref2 = first ? cw.scal.p : cw.scal.p + 1;
+            cw.mdot(V, J, w, first ? 0 : 1, first ? nullptr : coefcol + j, first ? nullptr : cw.beta.p + (j - 1),
+                    coefcol, cw.scal.p, nullptr, stop, st);
+            cw.update(V, J, w, 1, first ? 1 : 0, cw.scal.p, need2, cw.beta.p + j, ref2, j, nullptr, stop, st);
+            cw.mdot(V, J, w, 0, nullptr, nullptr, coefcol, cw.scal.p + 2, need2, stop, st);
+            cw.update(V, J, w, 2, 0, nullptr, nullptr, cw.beta.p + j, ref2, j, need2, stop, st);
+            k_cscale_dev<<<cw.nb, kCThreads, 0, st>>>(w, n, cw.beta.p + j, stop);
+            count_launch();
+            ED_CUDA(cudaGetLastError());
         }
-        sym_eigen(m, T, theta, Y);
-        const double bl = beta[m - 1];
+    };
+    CycleGraphs cache;
+    auto run_cycle = [&](int k) {
+        double2* V = col(Vb, 0);
+        CycleGraphs::Entry* g = cache.find(k, Vb.p);
+        if (!g) {
+            const uint64_t c0 = launch_count();
+            ED_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            try {
+                enqueue_cycle(V, k, true);
+            } catch (...) {
+                cudaGraph_t broken = nullptr;
+                cudaStreamEndCapture(st, &broken);
+                if (broken) cudaGraphDestroy(broken);
+                throw;
+            }
+            cudaGraph_t graph = nullptr;
+            ED_CUDA(cudaStreamEndCapture(st, &graph));
+            const int64_t kernels = (int64_t)(launch_count() - c0);
+            count_launches(-kernels);
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            ED_CUDA(e);
+            cache.e.push_back({k, Vb.p, exec, kernels});
+            g = &cache.e.back();
+        }
+        ED_CUDA(cudaGraphLaunch(g->exec, st));
+        count_launches(g->kernels);
+    };
+
+    std::vector<double> T((size_t)m * m, 0.0), coef_h((size_t)(m + 1) * (m + 1)), beta_h(m + 1);
+    std::vector<double> theta, Y, prev_theta;
+    int k = 0, m_eff = m;
+    bool converged = false;
+    double spmv_ms = 0.0;
+    for (;;) {
+        run_cycle(k);
+        inf.matvecs += m - k;
+        int hstop = 0;
+        ED_CUDA(cudaMemcpyAsync(&hstop, stop, sizeof(int), cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaMemcpyAsync(coef_h.data(), cw.coef.p, coef_h.size() * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaMemcpyAsync(beta_h.data(), cw.beta.p, (size_t)(m + 1) * 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        for (int j = k; j < m; ++j) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev[2 * j], ev[2 * j + 1]) == cudaSuccess) spmv_ms += ms;
+        }
+        (void)cudaGetLastError();
+        m_eff = hstop ? hstop : m;
+        if (hstop) {
+            ++inf.breakdowns;
+            inf.matvecs -= m - hstop;   // the steps after the breakdown launched no product work
+        }
+        for (int j = k; j < m_eff; ++j)
+            for (int i = 0; i <= j; ++i) {
+                const double v = coef_h[(size_t)j * (m + 1) + i];
+                T[(size_t)i * m + j] = v;
+                T[(size_t)j * m + i] = v;
+            }
+        std::vector<double> Tm((size_t)m_eff * m_eff);
+        for (int i = 0; i < m_eff; ++i)
+            for (int j = 0; j < m_eff; ++j) Tm[(size_t)i * m_eff + j] = T[(size_t)i * m + j];
+        sym_eigen(m_eff, Tm, theta, Y);
+        const double bl = hstop ? 0.0 : beta_h[m - 1];
         int nconv = 0;
         double maxres = 0.0;
-        for (int i = 0; i < nev; ++i) {
-            const double r = std::fabs(bl * Y[(size_t)(m - 1) + (size_t)m * i]);
+        const int want = std::min(nev, m_eff);
+        for (int i = 0; i < want; ++i) {
+            const double r = std::fabs(bl * Y[(size_t)(m_eff - 1) + (size_t)m_eff * i]);
             maxres = std::max(maxres, r);
             if (r <= tol) ++nconv;
         }
         inf.converged = nconv;
         inf.max_residual = maxres;
-        if (nconv == nev) {
+        // after a breakdown accept only once a cycle leaves the nev lowest
+        // values unchanged (a fresh direction may uncover more copies of a
+        // degenerate eigenvalue), or when the whole space is spanned
+        bool stable = !hstop || (int64_t)m_eff >= n;
+        if (hstop && !stable && (int)prev_theta.size() >= nev && m_eff >= nev) {
+            stable = true;
+            for (int i = 0; i < nev; ++i)
+                if (std::fabs(theta[i] - prev_theta[i]) > tol * std::max(1.0, std::fabs(theta[i]))) stable = false;
+        }
+        prev_theta.assign(theta.begin(), theta.begin() + std::min<int>(nev, (int)theta.size()));
+        if (m_eff >= nev && nconv == nev && stable) {
             converged = true;
             break;
         }
@@ -663,28 +955,45 @@ void clanczos_solve(const ed_ccrs& a, const ed_lanczos_params& p, const double* 
         ++inf.restarts;
         int kk = std::min(m - 2, nev + std::max(1, (m - nev) / 4));
         kk = std::max(kk, std::min(nev, m - 1));
-        rotate_basis(Vb.p, 2 * n, m, Y.data(), m, kk, V2b.p, rot, 0, st);
-        ED_CUDA(cudaMemcpyAsync(col(V2b, kk), col(Vb, m), 2 * (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        if (hstop) kk = std::min(kk, m_eff);
+        rotate_basis(Vb.p, 2 * n, m_eff, Y.data(), m_eff, kk, V2b.p, rot, 0, st);
+        if (!hstop) {
+            ED_CUDA(cudaMemcpyAsync(col(V2b, kk), col(Vb, m), 2 * (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        } else {
+            k_crandom<<<nsm * 4, kCThreads, 0, st>>>(reinterpret_cast<double*>(col(V2b, kk)), 2 * n,
+                                                     p.seed + 0x51ED2701ull * (uint64_t)inf.restarts);
+            count_launch();
+            ED_CUDA(cudaGetLastError());
+            corthonormalise(cw, col(V2b, 0), kk, st);
+        }
         std::swap(Vb.p, V2b.p);
         std::fill(T.begin(), T.end(), 0.0);
         for (int i = 0; i < kk; ++i) {
             T[(size_t)i * m + i] = theta[i];
-            const double s = bl * Y[(size_t)(m - 1) + (size_t)m * i];
-            T[(size_t)i * m + kk] = s;
-            T[(size_t)kk * m + i] = s;
+            if (!hstop) {
+                const double s = bl * Y[(size_t)(m_eff - 1) + (size_t)m_eff * i];
+                T[(size_t)i * m + kk] = s;
+                T[(size_t)kk * m + i] = s;
+            }
         }
         k = kk;
         ED_CUDA(cudaStreamSynchronize(st));
     }
-    for (int i = 0; i < nev; ++i) evals[i] = theta[i];
+    // an unconverged run can end inside a breakdown cycle with fewer Ritz
+    // pairs than requested: report the ones there are, NaN for the rest
+    const int nfound = std::min(nev, m_eff);
+    for (int i = 0; i < nev; ++i) evals[i] = i < nfound ? theta[i] : std::nan("");
     DevBuf<double> xtmp;
     double* Xo = evecs_dev;
     if (!Xo && p.verify) {
         xtmp.alloc(2 * (size_t)n * nev);
         Xo = xtmp.p;
     }
-    if (Xo) rotate_basis(Vb.p, 2 * n, m, Y.data(), m, nev, Xo, rot, 0, st);
-    if (p.verify && Xo) {
+    if (Xo) {
+        if (nfound < nev) ED_CUDA(cudaMemsetAsync(Xo, 0, 2 * (size_t)n * nev * 8, st));
+        rotate_basis(Vb.p, 2 * n, m_eff, Y.data(), m_eff, nfound, Xo, rot, 0, st);
+    }
+    if (p.verify && Xo && nfound == nev) {
         DevBuf<double> yv(2 * (size_t)n);
         double worst = 0.0;
         int nc = 0;

@@ -243,6 +243,9 @@ def ofl_main(ed, torch, args):
     res["solve"] = {"ok": bool(ok), "s": time.perf_counter() - t, "eigenvalues": [float(v) for v in H.m_eigenvalues],
                     "matvecs": H.last_info["matvecs"], "restarts": H.last_info["restarts"],
                     "spmv_s": H.last_info["spmv_seconds"], "max_residual": H.last_info["max_residual"]}
+    # what a step costs beyond its product (Gram-Schmidt, restarts, the host)
+    res["solve"]["overhead_ms_per_step"] = 1e3 * (res["solve"]["s"] - H.last_info["spmv_seconds"]) / max(
+        1, H.last_info["matvecs"])
     print(json.dumps(res))
 
 

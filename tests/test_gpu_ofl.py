@@ -117,6 +117,32 @@ def test_complex_eigenpairs(cuda, oracle, case, nev):
             assert np.linalg.norm(A @ X_[k] - H.m_eigenvalues[k] * X_[k]) <= 1e-9 * scale
 
 
+def test_complex_solver_through_breakdowns(cuda, oracle):
+    # no interaction and energies k mod 3: H is diagonal with a handful of
+    # distinct, highly degenerate values, so every Krylov sequence breaks
+    # down after a few steps and each degenerate copy needs a fresh direction
+    N, X, Y, kx, ky = 6, 4, 4, 0, 1
+    K = X * Y
+    kt, vt = oracle.ofl_tables(X, Y, 5)
+    T = ed.ComplexQuarticTermTables(X, Y, kt, np.zeros_like(vt))
+    e = (np.arange(K) % 3).astype(float)
+    b = oracle.basis_momentum(N, X, Y, kx, ky)
+    orp, ocol, oval = oracle.build_upper_complex(b, K, T.m_kTable, T.m_vTable, e)
+    A = oracle.complex_upper_to_full(orp, ocol, oval, len(b))
+    w = np.linalg.eigvalsh(sp.csr_matrix(A[::-1], shape=(len(b), len(b))).toarray())
+    nev = 8
+    assert w[nev - 1] == w[0]          # the lowest value alone has more than nev copies
+    for upper in (False, True):
+        model, _ = build(N, X, Y, kx, ky, T, e, upper=upper)
+        model.nev = nev
+        assert model.Diagonalize(tol=1e-10, seed=3), model.hamiltonian.last_info
+        H = model.hamiltonian
+        assert H.last_info["breakdowns"] >= 1
+        assert np.max(np.abs(H.m_eigenvalues - w[:nev])) <= 1e-10
+        X_ = H.m_eigenvectors
+        assert np.allclose(X_.conj() @ X_.T, np.eye(nev), atol=1e-8)
+
+
 def test_lz_build_refuses_a_momentum_basis(cuda):
     B = ed.FermionFockBasis()
     B.GenerateFockSpaceMomentum(3, 3, 4, 0, 0)
