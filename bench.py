@@ -335,10 +335,14 @@ def run_gpu(args, ws, rank):
         e2e_times.append(a.elapsed_time(b2) / 1000.0)
     # standalone SpMV timing on the same CRS for the roofline cross-check
     spmv_ms_alone = spmv_alone(L, C, kt, vt, n, torch)
+    # the FP64 ceiling of the product: this device's measured FMA issue rate
+    fma_rate = ctypes.c_double()
+    C.check(L.ed_fp64_fma_rate(20000, 4, ctypes.byref(fma_rate)))
     if ws > 1:
         ms = max_over_ranks(ms, "cuda")
     return {"ms": ms, "infos": infos, "ev": ev, "nnz": nnz, "n": n, "launches": launches, "clocks": clocks,
             "e2e_s": statistics.median(e2e_times), "ev_e2e": ev_e2e, "spmv_ms_alone": spmv_ms_alone,
+            "fp64_fma_per_s": fma_rate.value,
             "phases": phases[-args.steps:]}
 
 
@@ -450,10 +454,15 @@ def main():
                       "nnz_full": nnz},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (traffic or {}).get("bytes_per_launch"),
-                         "kernel": "k_spmv_full<8,4>", "bytes_per_launch": bytes_per,
+                         "kernel": "k_spmv_rows<8,4,2>", "bytes_per_launch": bytes_per,
                          "avg_launch_ms": spmv_s * 1000.0, "standalone_launch_ms": r["spmv_ms_alone"],
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s"},
+            # the product's other ceiling on GB300: one DFMA per stored element
+            # plus 12 DADD a row (k_spmv_rows<8,4,2>'s reduction) against the
+            # FP64 FMA rate measured here by ed_fp64_fma_rate
+            "fp64_pipe": {"ops_per_launch": nnz + 12 * n, "achieved_per_s": (nnz + 12 * n) / spmv_s,
+                          "peak_per_s": r["fp64_fma_per_s"], "frac": (nnz + 12 * n) / spmv_s / r["fp64_fma_per_s"]},
             "e2e": {"value": r["e2e_s"], "unit": "s", "h2d_bytes_per_step": n * 8 + NORB * 8,
                     "d2h_bytes_per_step": n * NEV * 8 + NEV * 8},
             "gpu_launches": int(r["launches"]),

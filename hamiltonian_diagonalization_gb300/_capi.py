@@ -103,6 +103,9 @@ _SIGS = {
     "ed_crs_get": (c_int, [c_void_p, P(c_i64), P(ctypes.c_int32), P(c_double)]),
     "ed_ham_diagonal": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "ed_spmv": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ed_spmv_kernel": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "ed_fp64_fma_rate": (c_int, [c_int, c_int, P(c_double)]),
+    "ed_crs_set_product_kernel": (c_int, [c_void_p, c_int]),
     "ed_hv_matfree": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "ed_op_from_crs": (c_int, [c_void_p, P(c_void_p)]),
     "ed_op_matfree": (c_int, [c_void_p, c_void_p, P(c_void_p)]),

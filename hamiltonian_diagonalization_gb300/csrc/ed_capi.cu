@@ -375,6 +375,38 @@ ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream
     });
 }
 
+ed_status ed_spmv_kernel(const ed_crs* a, int kernel, const double* x_dev, double* y_dev, ed_stream stream)
+{
+    return guarded([&] {
+        ED_NONNULL(a);
+        if (a->n == 0) return;
+        ED_NONNULL(x_dev);
+        ED_NONNULL(y_dev);
+        ED_REQUIRE(x_dev != y_dev, ED_ERR_ARG, "x and y must be distinct");
+        spmv_kernel(*a, kernel, x_dev, y_dev, (cudaStream_t)stream);
+    });
+}
+
+ed_status ed_crs_set_product_kernel(ed_crs* a, int kernel)
+{
+    return guarded([&] {
+        ED_NONNULL(a);
+        ED_REQUIRE(kernel >= 0 && kernel <= 5, ED_ERR_ARG, "kernel: 0 (chosen by shape) or 1-5 (ed_spmv_kernel)");
+        ED_REQUIRE(kernel == 0 || !a->upper, ED_ERR_ARG, "kernels 1-5 take full storage");
+        a->product_kernel = kernel;
+    });
+}
+
+ed_status ed_fp64_fma_rate(int iters, int blocks_per_sm, double* fma_per_second)
+{
+    return guarded([&] {
+        ED_NONNULL(fma_per_second);
+        ED_REQUIRE(iters >= 1 && iters <= (1 << 24) && blocks_per_sm >= 1 && blocks_per_sm <= 32, ED_ERR_ARG,
+                   "1 <= iters <= 2^24, 1 <= blocks_per_sm <= 32");
+        *fma_per_second = measure_dfma_rate(iters, blocks_per_sm);
+    });
+}
+
 ed_status ed_hv_matfree(const ed_basis* b, const ed_terms* t, const double* x_dev, double* y_dev, ed_stream stream)
 {
     return guarded([&] {

@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <cstddef>
+#include <memory>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -202,6 +203,22 @@ struct ed_terms {
     edgb::DevBuf<double> diag_b_dev;  // hop.diag_b
 };
 
+// Sliced-ELL copy of a full-storage CRS (SELL-C-sigma with C = 32): within
+// windows of kSellWindow rows the rows are ordered by length (longest first)
+// and cut into chunks of 32; chunk c holds its rows column-major, element j
+// of its lane l at off[c] + 32 j + l, padded with zeros to the chunk's
+// longest row len[c].  row[32 c + l] is the CRS row of lane l (-1: none).
+// The product reads it with one lane per row: coalesced loads, no cross-lane
+// reduction, and lanes of a chunk that finish together.
+struct ed_sell {
+    int64_t nchunks = 0, nnz_pad = 0;
+    edgb::DevBuf<int64_t> off;
+    edgb::DevBuf<int32_t> len;
+    edgb::DevBuf<int32_t> row;
+    edgb::DevBuf<int32_t> col;
+    edgb::DevBuf<double> val;
+};
+
 struct ed_crs {
     int64_t n = 0, nnz = 0;
     int upper = 0;
@@ -209,6 +226,12 @@ struct ed_crs {
     edgb::DevBuf<int64_t> rowptr;
     edgb::DevBuf<int32_t> col;
     edgb::DevBuf<double> val;
+    // the product's sliced-ELL copy (full storage), made on the first
+    // product outside a stream capture; state 0 not yet tried, 1 made,
+    // -1 not made (upper storage, short rows, or not enough free memory)
+    mutable std::unique_ptr<ed_sell> sell;
+    mutable int sell_state = 0;
+    int product_kernel = 0;   // 0: chosen by shape; else an ed_spmv_kernel id for every product
 };
 
 // Complex momentum-conserving terms (the optical-flux-lattice QuarticTermTables
@@ -263,6 +286,14 @@ void terms_upload(ed_terms& t);
 void ham_diagonal(const ed_basis& b, const ed_terms& t, double* diag, cudaStream_t st);
 void ham_build_crs(const ed_basis& b, const ed_terms& t, int upper, ed_crs& a, cudaStream_t st);
 void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st);
+// Make the product's sliced-ELL copy of a full-storage CRS now (a no-op when
+// made, declined, or the stream is capturing); solvers call it before they
+// capture their cycles.
+void spmv_prepare(const ed_crs& a, cudaStream_t st);
+// kernel 0: as spmv; 1: row lanes k_spmv_full<8,4>; 2, 3: shared reduction k_spmv_rows<8,4,2>,
+// <8,2,2>; 4, 5: sliced ELL k_spmv_sell<16>, <8> (full storage)
+void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st);
+double measure_dfma_rate(int iters, int blocks_per_sm);
 void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const double* x, double* y,
                 cudaStream_t st);
 void exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);

@@ -392,6 +392,14 @@ bool op_on_host(const ed_op& op)
 }
 }  // namespace
 
+// Work a product does once per operator (the stored CRS's sliced-ELL copy),
+// done before a solver captures its cycles.
+void op_prepare(const ed_op& op, cudaStream_t st)
+{
+    if (op.kind == ed_op::CRS) spmv_prepare(*op.crs, st);
+    else if (op.kind == ed_op::DEFLATED && op.inner) op_prepare(*op.inner, st);
+}
+
 void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st)
 {
     switch (op.kind) {
@@ -563,6 +571,7 @@ void lanczos_once(const ed_op& op, const ed_lanczos_params& p, const double* v0_
     SolveStream ss(caller_stream);
     cudaStream_t st = ss.s;
     const int nsm = sm_count();
+    op_prepare(op, st);
 
     if (v0_dev) {
         // a start vector must be finite and nonzero on every path
@@ -940,6 +949,10 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
 // error components, so a failed check repeats the sequence two digits past
 // the target from the found vectors; should that fail too (a degeneracy the
 // ladder does not generate), the deflated passes take over.
+// Rayleigh-Ritz rounds that refine the ladder's copies before a sequence is
+// repeated (round 0 on the kept span, then widened by the residuals).
+constexpr int kLadderRefineRounds = 5;
+
 void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczos_params& p, const double* v0_dev,
                              double* evals_host, double* evecs_dev, ed_solve_info* info, cudaStream_t caller)
 {
@@ -1041,34 +1054,67 @@ void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczo
         total.matvecs += nev;
         ok = *std::max_element(res.begin(), res.end()) <= tol;
         if (ok) break;
-        // Rayleigh-Ritz on the kept span: P = A^T H A, A <- A Y
-        DevBuf<double> HA((size_t)n * nev), Ar((size_t)n * nev);
-        for (int i = 0; i < nev; ++i) op_apply(op, A.p + (int64_t)i * n, HA.p + (int64_t)i * n, st);
-        total.matvecs += nev;
-        std::vector<double> P((size_t)nev * nev);
-        for (int j = 0; j < nev; ++j) {
-            k_lock_dots<<<nb, kThreads, 0, st>>>(A.p, nev, HA.p + (int64_t)j * n, n, 1.0, lpart.p, counter.p);
+        // The ladder multiplies a Ritz vector's error by up to its norm, so the
+        // copies can miss the bar that the sequence met.  Refine them in
+        // place: Rayleigh-Ritz on the kept span, then on the span widened by
+        // the residuals R = H A - A diag(lam) (one step of a block Krylov
+        // space), a few times, 2 nev products and a residual check a round.
+        DevBuf<double> W((size_t)n * 2 * nev), HW((size_t)n * 2 * nev), Ar((size_t)n * nev);
+        ED_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), st));
+        DevBuf<double> wpart((size_t)2 * nev * (nb + 1));
+        RotateScratch rot;
+        auto dots = [&](const double* B, int m, const double* v, double scale) {
+            k_lock_dots<<<nb, kThreads, 0, st>>>(B, m, v, n, scale, wpart.p, counter.p);
             ::edgb::count_launch();
             ED_CUDA(cudaGetLastError());
-            std::vector<double> c(nev);
-            ED_CUDA(cudaMemcpyAsync(c.data(), lpart.p + (int64_t)nev * nb, (size_t)nev * 8, cudaMemcpyDeviceToHost, st));
-            ED_CUDA(cudaStreamSynchronize(st));
-            for (int i = 0; i < nev; ++i) P[(size_t)i * nev + j] = c[i];
-        }
-        for (int i = 0; i < nev; ++i)
-            for (int j = 0; j < i; ++j) {
-                const double a = 0.5 * (P[(size_t)i * nev + j] + P[(size_t)j * nev + i]);
-                P[(size_t)i * nev + j] = P[(size_t)j * nev + i] = a;
+        };
+        for (int round = 0; round < kLadderRefineRounds && !ok; ++round) {
+            // W = [A, Q], Q orthonormal residual directions (none in round 0)
+            ED_CUDA(cudaMemcpyAsync(W.p, A.p, (size_t)n * nev * 8, cudaMemcpyDeviceToDevice, st));
+            for (int i = 0; i < nev; ++i) op_apply(op, A.p + (int64_t)i * n, HW.p + (int64_t)i * n, st);
+            total.matvecs += nev;
+            int m = nev;
+            if (round > 0) {
+                for (int i = 0; i < nev; ++i) {
+                    double* w = W.p + (int64_t)m * n;
+                    // w = H a_i - lam_i a_i, against the columns so far (twice)
+                    ED_CUDA(cudaMemcpyAsync(w, HW.p + (int64_t)i * n, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+                    for (int pass = 0; pass < 2; ++pass) {
+                        dots(W.p, m, w, -1.0);
+                        k_lock_axpy<<<nb, kThreads, 0, st>>>(w, W.p, m, wpart.p + (int64_t)m * nb, n);
+                        ::edgb::count_launch();
+                        ED_CUDA(cudaGetLastError());
+                    }
+                    const double nw = norm(w);
+                    if (!(nw > 1e-14 * std::max(1.0, std::fabs(lam[i])))) continue;   // nothing new
+                    mul(w, 1.0 / nw);
+                    op_apply(op, w, HW.p + (int64_t)m * n, st);
+                    ++total.matvecs;
+                    ++m;
+                }
             }
-        std::vector<double> ev, Y;
-        sym_eigen(nev, P, ev, Y);
-        RotateScratch rot;
-        rotate_basis(A.p, n, nev, Y.data(), nev, nev, Ar.p, rot, 0, st);
-        std::swap(A.p, Ar.p);
-        lam.assign(ev.begin(), ev.end());
-        residual_norms(op, A.p, lam.data(), nev, res.data(), st);
-        total.matvecs += nev;
-        ok = *std::max_element(res.begin(), res.end()) <= tol;
+            // P = W^T H W (symmetrised), lowest nev Ritz pairs
+            std::vector<double> P((size_t)m * m), c(m);
+            for (int j = 0; j < m; ++j) {
+                dots(W.p, m, HW.p + (int64_t)j * n, 1.0);
+                ED_CUDA(cudaMemcpyAsync(c.data(), wpart.p + (int64_t)m * nb, (size_t)m * 8, cudaMemcpyDeviceToHost, st));
+                ED_CUDA(cudaStreamSynchronize(st));
+                for (int i = 0; i < m; ++i) P[(size_t)i * m + j] = c[i];
+            }
+            for (int i = 0; i < m; ++i)
+                for (int j = 0; j < i; ++j) {
+                    const double a = 0.5 * (P[(size_t)i * m + j] + P[(size_t)j * m + i]);
+                    P[(size_t)i * m + j] = P[(size_t)j * m + i] = a;
+                }
+            std::vector<double> ev, Y;
+            sym_eigen(m, P, ev, Y);
+            rotate_basis(W.p, n, m, Y.data(), m, nev, Ar.p, rot, 0, st);
+            std::swap(A.p, Ar.p);
+            lam.assign(ev.begin(), ev.begin() + nev);
+            residual_norms(op, A.p, lam.data(), nev, res.data(), st);
+            total.matvecs += nev;
+            ok = *std::max_element(res.begin(), res.end()) <= tol;
+        }
     }
     if (!ok) {
         // a degeneracy the ladder does not generate: the deflated passes

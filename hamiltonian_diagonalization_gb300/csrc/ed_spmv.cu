@@ -4,15 +4,24 @@
 // -> SymmetricMatrixVectorMultiply (utilities/mathematics/sparse_linear_algebra.hpp:143-164):
 //   y[i] += a*x[c]; if (i != c) y[c] += a*x[i]   over the stored upper triangle.
 //
-// On GB300 FP64 FMA issues at about 0.6e12/s, which is what streaming the CRS
-// at HBM rate (12 bytes per nonzero) demands, so the kernels spend FP64
-// instructions only on the products: a row is owned by G lanes (G = 4 or 8
-// for the model's 200-350 nonzeros per row), each lane accumulates its share
-// serially into one FMA chain, and only log2(G) shuffle additions per lane
-// remain.  Column and value streams are read once with evict-first loads so
-// that x stays resident in L2.
+// On GB300 the FP64 pipe issues about 0.53e12 FMA/s (ed_fp64_fma_rate), less
+// than streaming the CRS at HBM rate (12 bytes per element) demands, so the
+// products are FP64-bound before they are HBM-bound and spend FP64
+// instructions only where they must: one FMA per element, as few additions
+// as the reduction allows, and no FP64 instruction issued for lanes with no
+// element.  Full storage takes one of two layouts:
+//  - rows of 96 and more elements (the one-level sectors): k_spmv_rows, 8
+//    lanes on each of two consecutive rows, each lane one FMA chain over its
+//    share of the row, the two rows' sums reduce-scattered (12 additions a
+//    row instead of 24);
+//  - shorter rows (two-level sectors): k_spmv_sell over a sliced-ELL copy
+//    (rows sorted by length within windows, chunks of 32 rows transposed), one
+//    lane a row, no reduction, and the lanes of a chunk finish together.
+// Column and value streams are read once with evict-first loads so that x
+// stays resident in L2.
 #include <algorithm>
 #include <map>
+#include <memory>
 
 #include "ed_hop.cuh"
 
@@ -72,6 +81,219 @@ __global__ void __launch_bounds__(256) k_spmv_full(const int64_t* __restrict__ r
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
         if (valid && sub == 0) y[r] = acc;
+    }
+}
+
+// Reduce-scatter of R row sums held by each of the G lanes of a group: while
+// a lane holds more than one row it keeps half of them (the upper half when
+// the partner bit is set) and adds the partner's copy of that half; once it
+// holds one row the remaining steps are plain butterfly additions.  Returns
+// the row's total and sets `row` to its index in the group; lanes whose
+// butterfly bits are zero own the result.  log2(G) - log2(R) + R - 1
+// additions a lane for R rows, against R log2(G) for R separate butterflies.
+template <int G, int R>
+__device__ __forceinline__ double reduce_scatter_rows(const double (&acc)[R], int sub, int& row)
+{
+    double v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = acc[t];
+    int base = 0;
+#pragma unroll
+    for (int o = G / 2, c = R; o >= 1; o >>= 1) {
+        if (c > 1) {
+            const bool hi = (sub & o) != 0;
+#pragma unroll
+            for (int t = 0; t < R / 2; ++t) {
+                if (t < c / 2) {
+                    const double send = hi ? v[t] : v[t + c / 2];
+                    const double keep = hi ? v[t + c / 2] : v[t];
+                    v[t] = keep + __shfl_xor_sync(0xffffffffu, send, o, G);
+                }
+            }
+            if (hi) base += c / 2;
+            c /= 2;
+        } else {
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], o, G);
+        }
+    }
+    row = base;
+    return v[0];
+}
+
+// Row lanes with a shared reduction: a group of G lanes takes R consecutive
+// rows one after another (the same lane-strided FMA chain per row as
+// k_spmv_full, U loads ahead), keeping one sum per row in registers, and
+// reduce-scatters the R sums (reduce_scatter_rows).  Rows of 50-70 elements
+// (the two-level sectors) waste fewer lanes with G = 4 and two loads ahead,
+// and their reduction is a large share of the FP64 work: a row costs
+// G log2 G additions in k_spmv_full, G (log2 G - log2 R + R - 1) / R here.
+// Same element order within each lane; the row sum is added in another
+// order, so y can differ from k_spmv_full's in the last bits.
+template <int G, int U, int R>
+__global__ void __launch_bounds__(256) k_spmv_rows(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                   const double* __restrict__ val, const double* __restrict__ x,
+                                                   double* __restrict__ y, int64_t n)
+{
+    static_assert(R >= 1 && R <= G && (R & (R - 1)) == 0, "R a power of two up to G");
+    constexpr int RPW = (32 / G) * R;   // rows per warp step
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {   // warp-uniform loop
+        const int64_t g0 = rb + (int64_t)grp * R;
+        double acc[R];
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+            const int64_t r = g0 + t;
+            const bool valid = r < n;
+            const int64_t s = valid ? rowptr[r] : 0, e = valid ? rowptr[r + 1] : 0;
+            double a = 0.0;
+            for (int64_t k0 = s + sub; k0 < e; k0 += (int64_t)G * U) {
+                double v[U];
+                int c[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int64_t k = k0 + (int64_t)u * G;
+                    v[u] = k < e ? ld_stream(val + k) : 0.0;
+                    c[u] = k < e ? ld_stream(col + k) : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (k0 + (int64_t)u * G < e) a = fma(v[u], __ldg(x + c[u]), a);
+            }
+            acc[t] = a;
+        }
+        int t = 0;
+        const double w = reduce_scatter_rows<G, R>(acc, sub, t);
+        constexpr int kButterflyMask = G / R - 1;
+        const int64_t r = g0 + t;
+        if ((sub & kButterflyMask) == 0 && r < n) y[r] = w;
+    }
+}
+
+// ------------------------------------------------------------ sliced ELL
+
+constexpr int kSellC = 32;          // rows per chunk (one warp)
+constexpr int kSellWindow = 1024;   // rows per sorting window (32 chunks)
+
+// Order of each window's rows by length, longest first (ties by row): the
+// window's slots row[w0 + i] (-1 past the last row) and its chunks' padded
+// lengths clen (the first, longest, row of each chunk).  A bitonic sort of
+// (complemented length, slot) keys in shared memory, one CTA per window.
+__global__ void __launch_bounds__(1024) k_sell_order(const int64_t* __restrict__ rowptr, int64_t n,
+                                                     int32_t* __restrict__ row, int32_t* __restrict__ clen)
+{
+    __shared__ uint64_t key[kSellWindow];
+    const int64_t w0 = (int64_t)blockIdx.x * kSellWindow;
+    const int cnt = (int)min((int64_t)kSellWindow, n - w0);
+    for (int i = threadIdx.x; i < kSellWindow; i += blockDim.x) {
+        uint64_t k = ~0ull;   // empty slots sort last
+        if (i < cnt) {
+            const int64_t len = rowptr[w0 + i + 1] - rowptr[w0 + i];
+            k = ((uint64_t)(0x7FFFFFFFu - (uint32_t)min(len, (int64_t)0x7FFFFFFF)) << 32) | (uint32_t)i;
+        }
+        key[i] = k;
+    }
+    __syncthreads();
+    for (int size = 2; size <= kSellWindow; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < kSellWindow; i += blockDim.x) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const uint64_t a = key[i], b = key[j];
+                    if ((a > b) == ((i & size) == 0)) {
+                        key[i] = b;
+                        key[j] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < kSellWindow; i += blockDim.x) {
+        const uint64_t k = key[i];
+        row[w0 + i] = k == ~0ull ? -1 : (int32_t)(w0 + (int64_t)(uint32_t)k);
+    }
+    for (int c = threadIdx.x; c < kSellWindow / kSellC; c += blockDim.x) {
+        const uint64_t k = key[c * kSellC];
+        clen[w0 / kSellC + c] = k == ~0ull ? 0 : (int32_t)(0x7FFFFFFFu - (uint32_t)(k >> 32));
+    }
+}
+
+__global__ void k_sell_sizes(const int32_t* __restrict__ clen, int64_t nchunks, int64_t* __restrict__ sizes)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nchunks; c += (int64_t)gridDim.x * blockDim.x)
+        sizes[c] = (int64_t)clen[c] * kSellC;
+}
+
+// One warp per chunk: lane l copies its row's elements into the chunk,
+// element j at off[c] + 32 j + l, and pads to the chunk's length with zero
+// values at the row's own column (any valid index would do).
+__global__ void __launch_bounds__(256) k_sell_fill(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                   const double* __restrict__ val, const int32_t* __restrict__ row,
+                                                   const int32_t* __restrict__ clen, const int64_t* __restrict__ off,
+                                                   int64_t nchunks, int32_t* __restrict__ scol,
+                                                   double* __restrict__ sval)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nchunks; c += nwarps) {
+        const int L = clen[c];
+        if (L == 0) continue;
+        const int r = row[c * kSellC + lane];
+        const int64_t s = r >= 0 ? rowptr[r] : 0;
+        const int len = r >= 0 ? (int)(rowptr[r + 1] - s) : 0;
+        const int pad = r >= 0 ? r : 0;
+        const int64_t o = off[c] + lane;
+        for (int j = 0; j < L; ++j) {
+            const bool in = j < len;
+            scol[o + (int64_t)j * kSellC] = in ? col[s + j] : pad;
+            sval[o + (int64_t)j * kSellC] = in ? val[s + j] : 0.0;
+        }
+    }
+}
+
+// y = A x from the sliced-ELL copy: one warp per chunk, lane l accumulates
+// its row in one FMA chain in CRS element order (then the padding's exact
+// zeros), U elements' loads issued ahead of their FMAs.  All 32 lanes of a
+// chunk run the same number of steps, and each load instruction reads 32
+// consecutive values and columns.
+template <int U, int CH = 1>
+__global__ void __launch_bounds__(256) k_spmv_sell(const int64_t* __restrict__ off, const int32_t* __restrict__ clen,
+                                                   const int32_t* __restrict__ row, const int32_t* __restrict__ scol,
+                                                   const double* __restrict__ sval, const double* __restrict__ x,
+                                                   double* __restrict__ y, int64_t nchunks)
+{
+    static_assert(CH == 1 || (CH == 2 && U % 2 == 0), "one chain, or two over an even unroll");
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nchunks; c += nwarps) {
+        const int L = clen[c];
+        const int r = row[c * kSellC + lane];
+        const double* vp = sval + off[c] + lane;
+        const int32_t* cp = scol + off[c] + lane;
+        double acc[CH];
+#pragma unroll
+        for (int h = 0; h < CH; ++h) acc[h] = 0.0;
+        int j = 0;
+        for (; j + U <= L; j += U) {
+            double v[U];
+            int cc[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                v[u] = ld_stream(vp + (int64_t)(j + u) * kSellC);
+                cc[u] = ld_stream(cp + (int64_t)(j + u) * kSellC);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc[u % CH] = fma(v[u], __ldg(x + cc[u]), acc[u % CH]);
+        }
+        for (; j < L; ++j)
+            acc[0] = fma(ld_stream(vp + (int64_t)j * kSellC), __ldg(x + ld_stream(cp + (int64_t)j * kSellC)), acc[0]);
+        double t = acc[0];
+#pragma unroll
+        for (int h = 1; h < CH; ++h) t += acc[h];
+        if (r >= 0) y[r] = t;
     }
 }
 
@@ -196,6 +418,23 @@ __global__ void __launch_bounds__(1024) k_hv_matfree_c(const uint64_t* __restric
     }
 }
 
+// FP64 FMA issue rate (a measurement aid for the products' FP64 ceiling):
+// eight independent chains r = r * a + b per thread, iters steps each.
+__global__ void __launch_bounds__(256) k_dfma_rate(int iters, double a, double b, double* __restrict__ sink)
+{
+    double r[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r[i] = 1e-3 * threadIdx.x + i;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) r[i] = fma(r[i], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += r[i];
+    if (s == -1.0) sink[0] = s;   // keeps the chains; never true for these inputs
+}
+
 int sms()
 {
     int dev = 0, s = 148;
@@ -206,25 +445,148 @@ int sms()
 
 }  // namespace
 
+namespace {
+
+void sell_build(const ed_crs& a, cudaStream_t st)
+{
+    const int64_t n = a.n;
+    const int64_t nwin = (n + kSellWindow - 1) / kSellWindow;
+    auto sl = std::make_unique<ed_sell>();
+    sl->nchunks = nwin * (kSellWindow / kSellC);
+    sl->row.alloc((size_t)nwin * kSellWindow);
+    sl->len.alloc((size_t)sl->nchunks);
+    sl->off.alloc((size_t)sl->nchunks + 1);
+    k_sell_order<<<(unsigned)nwin, 1024, 0, st>>>(a.rowptr.p, n, sl->row.p, sl->len.p);
+    count_launch();
+    {
+        DevBuf<int64_t> sizes((size_t)sl->nchunks);
+        k_sell_sizes<<<sms() * 4, 256, 0, st>>>(sl->len.p, sl->nchunks, sizes.p);
+        count_launch();
+        exclusive_scan_i64(sizes.p, sl->off.p, sl->nchunks, st);
+        ED_CUDA(cudaMemcpyAsync(&sl->nnz_pad, sl->off.p + sl->nchunks, 8, cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+    }
+    // the copy must leave room: decline when it would take more than half
+    // of the free device memory
+    size_t free_b = 0, total_b = 0;
+    ED_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = (size_t)sl->nnz_pad * 12 + (size_t)kCrsPad * 12;
+    if (need > free_b / 2) {
+        a.sell_state = -1;
+        return;
+    }
+    sl->col.alloc((size_t)sl->nnz_pad + kCrsPad);
+    sl->val.alloc((size_t)sl->nnz_pad + kCrsPad);
+    ED_CUDA(cudaMemsetAsync(sl->col.p + sl->nnz_pad, 0, kCrsPad * 4, st));
+    ED_CUDA(cudaMemsetAsync(sl->val.p + sl->nnz_pad, 0, kCrsPad * 8, st));
+    k_sell_fill<<<sms() * 8, 256, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, sl->row.p, sl->len.p, sl->off.p,
+                                           sl->nchunks, sl->col.p, sl->val.p);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+    a.sell = std::move(sl);
+    a.sell_state = 1;
+}
+
+bool stream_capturing(cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ED_CUDA(cudaStreamIsCapturing(st, &cs));
+    return cs != cudaStreamCaptureStatusNone;
+}
+
+template <int U, int CH = 1>
+void sell_launch(const ed_crs& a, const double* x, double* y, cudaStream_t st)
+{
+    const ed_sell& sl = *a.sell;
+    k_spmv_sell<U, CH><<<sms() * 8, 256, 0, st>>>(sl.off.p, sl.len.p, sl.row.p, sl.col.p, sl.val.p, x, y,
+                                                  sl.nchunks);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+// Full-storage matrices of at least kSellMinRows rows and fewer than
+// kSellMaxAvg elements a row on average get the sliced-ELL copy.
+constexpr int64_t kSellMinRows = 4096;
+constexpr double kSellMaxAvg = 96.0;
+
+void spmv_prepare(const ed_crs& a, cudaStream_t st)
+{
+    if (a.product_kernel >= 4 && a.sell_state == 0 && a.n > 0 && !stream_capturing(st)) {
+        sell_build(a, st);
+        return;
+    }
+    if (a.sell_state != 0) return;
+    // one-level sectors (96 and more elements a row) stay with the row lanes
+    if (a.upper || a.n < kSellMinRows || (double)a.nnz >= kSellMaxAvg * (double)a.n) {
+        a.sell_state = -1;
+        return;
+    }
+    if (stream_capturing(st)) return;
+    sell_build(a, st);
+}
+
+void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st)
+{
+    if (a.n == 0) return;
+    ED_REQUIRE(kernel >= 0 && kernel <= 5, ED_ERR_ARG,
+               "kernel: 0 (chosen by shape), 1 (row lanes 8x4), 2 / 3 (shared reduction 8x4x2 / 8x2x2), "
+               "4 / 5 (sliced ELL, 16 / 8 loads ahead)");
+    if (kernel == 0) {
+        spmv(a, x, y, st);
+        return;
+    }
+    ED_REQUIRE(!a.upper, ED_ERR_ARG, "the row and sliced-ELL kernels take full storage");
+    const int threads = 256;
+    const int grid = sms() * 8;
+    const int64_t* rp = a.rowptr.p;
+    switch (kernel) {
+    case 1: k_spmv_full<8, 4><<<grid, threads, 0, st>>>(rp, a.col.p, a.val.p, x, y, a.n); break;
+    case 2: k_spmv_rows<8, 4, 2><<<grid, threads, 0, st>>>(rp, a.col.p, a.val.p, x, y, a.n); break;
+    case 3: k_spmv_rows<8, 2, 2><<<grid, threads, 0, st>>>(rp, a.col.p, a.val.p, x, y, a.n); break;
+    default:
+        if (a.sell_state == 0 && !stream_capturing(st)) sell_build(a, st);   // any size here
+        ED_REQUIRE(a.sell_state == 1, ED_ERR_RANGE, "no sliced-ELL copy (not enough free device memory)");
+        if (kernel == 4) sell_launch<16>(a, x, y, st);
+        else sell_launch<8>(a, x, y, st);
+        return;
+    }
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
 void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
 {
     if (a.n == 0) return;
-    const double avg = a.n ? (double)a.nnz / (double)a.n : 0.0;
+    if (a.product_kernel > 0) {
+        spmv_kernel(a, a.product_kernel, x, y, st);
+        return;
+    }
+    if (a.sell_state == 0) spmv_prepare(a, st);   // waits for a solver's explicit call while capturing
+    if (a.sell_state == 1) {
+        // rows of fewer than 96 elements (two-level sectors, small one-level
+        // ones), measured on GB300 at two-level N=8, 2S=18 (2.03M rows of 59
+        // on average) / 2S=21 (5.90M rows of 73): sliced ELL with 16 loads
+        // ahead 0.305 / 1.052 ms (8 ahead 0.326 / 1.110, 24 0.303 / 1.045,
+        // 32 0.310 / 1.055) against the best row kernels 0.333 / 1.197
+        sell_launch<16>(a, x, y, st);
+        return;
+    }
+    const double avg = (double)a.nnz / (double)a.n;
     const int threads = 256;
     const int grid = sms() * 8;
-    if (!a.upper && avg >= 96) {
-        k_spmv_full<8, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+    if (!a.upper && avg >= 24) {
+        // one-level sectors (190-260 elements a row): 8 lanes, 4 loads ahead,
+        // two rows a group (GB300, N=11 2S=30: 0.826-0.838 ms against
+        // 0.828-0.841 for k_spmv_full<8,4> and 0.90 for sliced ELL with 16
+        // loads ahead; N=10 2S=27: 0.1219-0.1226 against 0.1219-0.1232 and
+        // 0.14); also the short-row sectors below kSellMinRows rows
+        if (avg >= kSellMaxAvg)
+            k_spmv_rows<8, 4, 2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        else k_spmv_rows<8, 2, 2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else if (!a.upper) {
-        // rows of 24-96 elements (two-level sectors, small one-level ones):
-        // four lanes per row with four loads ahead, or eight lanes per row
-        // with three ahead once x passes about 20 MB (measured on GB300:
-        // two-level N=7 sectors of 1.3-2.0M rows 4.3-4.6 TB/s with four lanes,
-        // 3.5-3.7 with eight; N=8 sectors of 4.2-5.9M rows 4.3-4.4 TB/s with
-        // eight and three ahead, 4.1 with four ahead, 2.9-3.0 with four lanes)
-        if (avg >= 24 && a.n >= 2500000)
-            k_spmv_full<8, 3><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
-        else if (avg >= 24) k_spmv_full<4, 4><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
-        else k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else {
         ED_CUDA(cudaMemsetAsync(y, 0, (size_t)a.n * sizeof(double), st));
         if (avg >= 48) k_spmv_upper<8><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
@@ -270,6 +632,30 @@ void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const 
                                                 t.diag_b_dev.p, t.hop_off_dev.p, K, b.hi.p, b.lo.p, b.low_bits, x, y);
     count_launch();
     ED_CUDA(cudaGetLastError());
+}
+
+// DFMA per second of the whole device: blocks_per_sm * SMs blocks of 256
+// threads, 8 chains of iters FMAs each; the second of two launches timed.
+double measure_dfma_rate(int iters, int blocks_per_sm)
+{
+    const int grid = sms() * blocks_per_sm;
+    DevBuf<double> sink(1);
+    cudaEvent_t e0, e1;
+    ED_CUDA(cudaEventCreate(&e0));
+    ED_CUDA(cudaEventCreate(&e1));
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {
+        ED_CUDA(cudaEventRecord(e0, nullptr));
+        k_dfma_rate<<<grid, 256>>>(iters, 1.0 - 1e-12, 1e-12, sink.p);
+        count_launch();
+        ED_CUDA(cudaEventRecord(e1, nullptr));
+        ED_CUDA(cudaEventSynchronize(e1));
+        ED_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ED_CUDA(cudaGetLastError());
+    return (double)grid * 256 * 8 * (double)iters / (ms * 1e-3);
 }
 
 }  // namespace edgb

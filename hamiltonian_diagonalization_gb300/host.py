@@ -292,6 +292,16 @@ class CrsSparseMatrix:
         check(lib().ed_crs_read(fileName.encode(), int(fmt == "binary"), int(upper), ctypes.byref(h)))
         return cls(h)
 
+    def set_product_kernel(self, kernel: int):
+        """Kernel of every later product, eigensolvers included
+        (ed_crs_set_product_kernel; 0 restores the choice by shape)."""
+        check(lib().ed_crs_set_product_kernel(self._h, int(kernel)))
+
+    def multiply(self, x, y, kernel: int = 0, stream=None):
+        """y = A x on device vectors with a chosen product kernel
+        (ed_spmv_kernel: 0 by shape, 1 row lanes, 2-3 shared-reduction rows, 4-5 sliced ELL)."""
+        check(lib().ed_spmv_kernel(self._h, int(kernel), _dptr(x), _dptr(y), stream))
+
     def device_arrays(self):
         a, b, c = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
         check(lib().ed_crs_arrays(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))

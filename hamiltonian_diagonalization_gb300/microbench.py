@@ -59,12 +59,24 @@ def main():
     ap.add_argument("--ofl", default="", help="N,dimX,dimY,kxTot,kyTot: complex optical-flux-lattice sector")
     ap.add_argument("--nev", type=int, default=4, help="two-level: eigenpairs to solve for")
     ap.add_argument("--products-only", action="store_true", help="two-level / complex: stop after the products")
+    ap.add_argument("--kernel", type=int, default=0,
+                    help="full-storage product kernel (ed_spmv_kernel): 0 by shape, 1 row lanes, "
+                         "2-3 shared-reduction rows, 4-5 sliced ELL")
+    ap.add_argument("--fp64-rate", action="store_true", help="measure the FP64 FMA issue rate instead")
     args = ap.parse_args()
     import torch
 
     import hamiltonian_diagonalization_gb300 as ed
     from hamiltonian_diagonalization_gb300 import _capi as C
 
+    if args.fp64_rate:
+        out = {"mode": "fp64_fma_rate"}
+        for bps in (2, 4, 8):
+            r = ctypes.c_double()
+            C.check(C.lib().ed_fp64_fma_rate(20000, bps, ctypes.byref(r)))
+            out[f"fma_per_s_{bps}_blocks_per_sm"] = r.value
+        print(json.dumps(out))
+        return
     if args.rotate:
         return rotate_main(C, torch, args)
     if args.ofl:
@@ -86,19 +98,31 @@ def main():
     mv = ed.MatrixVectorFunction(H)
     x = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, n)).cuda()
     y = torch.empty_like(x)
+    if args.kernel:
+        crs = H.m_crsSparseMatrix
+        product = lambda: crs.multiply(x, y, args.kernel)   # noqa: E731
+    else:
+        product = lambda: mv.Simple(x, y)   # noqa: E731
+    import time
+    torch.cuda.synchronize()
+    t_first = time.perf_counter()
+    product()                      # the first product also makes the sliced-ELL copy
+    torch.cuda.synchronize()
+    ms_first = 1e3 * (time.perf_counter() - t_first)
     for _ in range(args.warmup):
-        mv.Simple(x, y)
+        product()
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = C.lib().ed_kernel_launches()
     a.record()
     for _ in range(args.reps):
-        mv.Simple(x, y)
+        product()
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / args.reps
     out = {"sector": [N, norb, tlz], "n": n, "mode": "matfree" if args.matfree else ("upper" if args.upper else "full"),
-           "ms_per_product": ms, "launches": int(C.lib().ed_kernel_launches() - launches0)}
+           "kernel": args.kernel, "ms_per_product": ms, "ms_first_product": ms_first,
+           "launches": int(C.lib().ed_kernel_launches() - launches0)}
     if not args.matfree:
         nnz = H.m_crsSparseMatrix.GetNbrNonZeros()
         by = nnz * 12 + (n + 1) * 8 + 2 * n * 8
@@ -169,18 +193,24 @@ def two_level_main(ed, C, torch, N, norb0, tlz, args):
     mv = ed.MatrixVectorFunction(H)
     x = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, n)).cuda()
     y = torch.empty_like(x)
+    if args.kernel:
+        crs = H.m_crsSparseMatrix
+        crs.set_product_kernel(args.kernel)      # the solves below use it too
+        product = lambda: crs.multiply(x, y, args.kernel)   # noqa: E731
+    else:
+        product = lambda: mv.Simple(x, y)   # noqa: E731
     for _ in range(3):
-        mv.Simple(x, y)
+        product()
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record()
     for _ in range(20):
-        mv.Simple(x, y)
+        product()
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / 20
     by = nnz * 12 + (n + 1) * 8 + 2 * n * 8
-    res.update({"ms_per_product": ms, "GBps": by / ms / 1e6})
+    res.update({"kernel": args.kernel, "ms_per_product": ms, "GBps": by / ms / 1e6})
     if args.products_only:
         print(json.dumps(res))
         return

@@ -170,6 +170,25 @@ ed_status ed_ham_diagonal(const ed_basis* b, const ed_terms* t, double* diag_dev
  * -> SymmetricMatrixVectorMultiply (utilities/mathematics/sparse_linear_algebra.hpp:78-168). */
 ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream stream);
 
+/* The same product with a chosen kernel of the full storage, for measuring
+ * and testing them side by side: 0 as ed_spmv (chosen by shape), 1 the
+ * row-lane kernel (8 lanes a row, 4 loads ahead), 2 / 3 the shared-reduction
+ * kernel (8 lanes take two consecutive rows and reduce-scatter their sums; 4 /
+ * 2 loads ahead), 4 / 5 the sliced-ELL kernel (one lane a row over a
+ * length-sorted, chunk-transposed copy made on first use; 16 / 8 loads
+ * ahead).  ED_ERR_ARG for 1-5 on upper-triangle storage; ED_ERR_RANGE for 4-5
+ * when the copy does not fit in half the free device memory. */
+ed_status ed_spmv_kernel(const ed_crs* a, int kernel, const double* x_dev, double* y_dev, ed_stream stream);
+
+/* Use kernel (an ed_spmv_kernel id; 0 restores the choice by shape) for every
+ * later product of a, including those inside the eigensolvers. */
+ed_status ed_crs_set_product_kernel(ed_crs* a, int kernel);
+
+/* Measured FP64 FMA issue rate of the current device (FMA per second): a
+ * kernel of blocks_per_sm blocks per SM, 256 threads, eight independent FMA
+ * chains of iters steps per thread; the ceiling of the FP64 products. */
+ed_status ed_fp64_fma_rate(int iters, int blocks_per_sm, double* fma_per_second);
+
 /* y = H x with the matrix elements regenerated on the fly from the basis and
  * the term tables (no stored matrix).  Stands in for the reference's
  * unfinished MatrixVectorFunction::Recalculate (matrix_vector_routines.hpp:112-143). */

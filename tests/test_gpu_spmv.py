@@ -43,6 +43,31 @@ def test_products_match_oracle(cuda, oracle, case):
         assert np.max(np.abs(y - yref)) <= 1e-13 * scale, kw
 
 
+@pytest.mark.parametrize("case", [(4, 10, 0), (6, 16, 4), (8, 22, 0), (10, 28, 2), (2, 9, 2), (3, 9, 0)])
+def test_row_kernels_match_oracle(cuda, oracle, case):
+    # every full-storage kernel (row lanes, shared-reduction rows, sliced ELL) on every sector,
+    # including ones with fewer rows than a tile and with empty rows
+    torch = cuda
+    N, norb, tlz = case
+    pp = oracle.odd_coulomb_list(norb)
+    b = oracle.basis(N, norb, tlz)
+    kt, vt = oracle.quartic_tables(norb, pp)
+    urp, ucol, uval = oracle.build_upper(b, norb, kt, vt)
+    x = np.random.default_rng(6).uniform(-1, 1, len(b))
+    yref = oracle.spmv_sym_upper(urp, ucol, uval, x)
+    scale = np.abs(uval).max() * np.abs(x).max() * 50
+    H, _ = setup(N, norb, tlz, pp)
+    xd = torch.from_numpy(x).cuda()
+    for kernel in range(1, 6):
+        yd = torch.full_like(xd, np.nan)
+        H.m_crsSparseMatrix.multiply(xd, yd, kernel)
+        torch.cuda.synchronize()
+        assert np.max(np.abs(yd.cpu().numpy() - yref)) <= 1e-13 * scale, kernel
+    Hu, _ = setup(N, norb, tlz, pp, upper=True)
+    with pytest.raises(ed.EDError):
+        Hu.m_crsSparseMatrix.multiply(xd, torch.empty_like(xd), 2)
+
+
 def test_linearity_and_symmetry_at_scale(cuda, oracle):
     N, norb, tlz = 11, 31, 0
     pp = oracle.odd_coulomb_list(norb)
