@@ -16,6 +16,8 @@ from .host import (  # noqa: F401
     MatrixVectorFunction,
     MpiWrapper,
     Observables,
+    QuadraticTermHashTables,
+    QuarticTermHashTables,
     QuarticTermTables,
     SpherePseudopotentialModel,
     SphereTwoLevelPseudopotentialModel,
@@ -28,6 +30,7 @@ from .host import (  # noqa: F401
     dense_sym_eigen,
     eigensystem_from_file,
     eigensystem_to_file,
+    hash_key,
     odd_coulomb_list,
     solve_sector,
     synthetic_ofl_tables,

@@ -85,6 +85,13 @@ _SIGS = {
     "ed_basis2_build": (c_int, [c_int, c_int, c_int, c_void_p, P(c_void_p)]),
     "ed_basis_momentum_build": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, P(c_void_p)]),
     "ed_cterms_create": (c_int, [c_int, c_int, c_int, P(ctypes.c_uint16), P(c_double), P(c_double), P(c_void_p)]),
+    "ed_cterms_create_hash": (c_int, [c_int, c_int, c_int, ctypes.c_uint32, P(c_u64), P(ctypes.c_uint16), ctypes.c_uint32,
+                                      P(c_u64), P(c_double), ctypes.c_uint32, P(c_u64), P(ctypes.c_uint16),
+                                      ctypes.c_uint32, P(c_u64), P(c_double), P(c_void_p)]),
+    "ed_term_hash_write": (c_int, [ctypes.c_char_p, c_int, c_int, ctypes.c_uint32, P(c_u64), P(ctypes.c_uint16),
+                                   ctypes.c_uint32, P(c_u64), P(c_double)]),
+    "ed_term_hash_read": (c_int, [ctypes.c_char_p, c_int, P(ctypes.c_uint32), P(c_u64), P(ctypes.c_uint16),
+                                  P(ctypes.c_uint32), P(c_u64), P(c_double)]),
     "ed_cterms_free": (c_int, [c_void_p]),
     "ed_cham_build_crs": (c_int, [c_void_p, c_void_p, c_int, c_void_p, P(c_void_p)]),
     "ed_ccrs_free": (c_int, [c_void_p]),

@@ -22,7 +22,7 @@ LIB = os.path.join(PKG, "libedgb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ed_terms.cpp", "ed_eigen.cpp", "ed_basis.cu", "ed_build.cu", "ed_spmv.cu", "ed_lanczos.cu",
            "ed_capi.cu", "ed_noalloc.cu", "ed_batched.cu", "ed_mlp.cu", "ed_rotate.cu", "ed_io.cpp", "ed_observables.cu",
-           "ed_complex.cu", "ed_subspace.cu", "ed_eigen_dev.cu"]
+           "ed_complex.cu", "ed_subspace.cu", "ed_eigen_dev.cu", "ed_term_hash.cpp"]
 
 
 def nvcc() -> str:

@@ -427,6 +427,144 @@ class ComplexQuarticTermTables:
         return complex(self.m_vTable[self._index(k3, k4) * self.m_kMax + (k1 if k4 > k3 else k2)])
 
 
+def hash_key(*labels) -> int:
+    """utilities::Key of the reference's multi-key hash tables
+    (utilities/data_structures/multi_key_hash.hpp:59-92,
+    general/serialize.hpp:96-130): two labels (k1 << 32) | k2, three
+    (k2 << 48) | (k3 << 32) | (k4 << 16), four (k1 << 48) | (k2 << 32) |
+    (k3 << 16) | k4."""
+    if len(labels) == 2:
+        return (int(labels[0]) << 32) | int(labels[1])
+    if len(labels) in (3, 4):
+        a = list(labels) + [0] * (4 - len(labels))
+        return (int(a[0]) << 48) | (int(a[1]) << 32) | (int(a[2]) << 16) | int(a[3])
+    raise EDError(C.ED_ERR_ARG, "two, three or four labels")
+
+
+class _TermHashTables:
+    """TermHashTables<dcmplx> (hamiltonians/term_hash_tables_base.hpp:44-276):
+    a k-table (keys of nlabels - 1 labels, each with one k1; a key may repeat)
+    and a value table (keys of nlabels labels, complex values), kept as flat
+    key/value arrays in the order of the reference's file, with dictionaries
+    for the look-ups.  Files in its binary or text layout (ed_term_hash_write /
+    ed_term_hash_read)."""
+
+    NLABELS = 4
+
+    def __init__(self):
+        self.m_kMax = 0
+        self.Clear()
+
+    def Initialize(self, kMax: int):
+        self.m_kMax = int(kMax)
+
+    def Clear(self):
+        self.kkeys = np.zeros(0, dtype=np.uint64)
+        self.kvals = np.zeros(0, dtype=np.uint16)
+        self.vkeys = np.zeros(0, dtype=np.uint64)
+        self.vvals = np.zeros(0, dtype=np.complex128)
+        self._kd = self._vd = None
+
+    def _set(self, kkeys, kvals, vkeys, vvals):
+        self.kkeys = np.ascontiguousarray(kkeys, dtype=np.uint64)
+        self.kvals = np.ascontiguousarray(kvals, dtype=np.uint16)
+        self.vkeys = np.ascontiguousarray(vkeys, dtype=np.uint64)
+        self.vvals = np.ascontiguousarray(vvals, dtype=np.complex128)
+        self._kd = self._vd = None
+
+    def _klookup(self, key: int) -> list:
+        if self._kd is None:
+            d = {}
+            for k, v in zip(self.kkeys.tolist(), self.kvals.tolist()):
+                d.setdefault(k, []).append(v)
+            self._kd = d
+        return list(self._kd.get(int(key), []))
+
+    def _vlookup(self, key: int) -> complex:
+        if self._vd is None:
+            d = {}
+            for k, v in zip(self.vkeys.tolist(), self.vvals.tolist()):
+                d.setdefault(k, v)
+            self._vd = d
+        return complex(self._vd.get(int(key), 0.0))
+
+    def GetMaxKCount(self) -> int:
+        if self.kkeys.size == 0:
+            return 1
+        _, counts = np.unique(self.kkeys, return_counts=True)
+        return int(counts.max())
+
+    def ToFile(self, fileName: str, fmt: str = "binary", mpi=None):
+        vv = np.ascontiguousarray(self.vvals.view(np.float64))
+        check(lib().ed_term_hash_write(fileName.encode(), int(fmt == "binary"), self.NLABELS, len(self.kkeys),
+                                       self.kkeys.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                       self.kvals.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)), len(self.vkeys),
+                                       self.vkeys.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _f64p(vv)))
+
+    def FromFile(self, fileName: str, fmt: str = "binary", mpi=None):
+        nk, nv = ctypes.c_uint32(), ctypes.c_uint32()
+        b = int(fmt == "binary")
+        check(lib().ed_term_hash_read(fileName.encode(), b, ctypes.byref(nk), None, None, ctypes.byref(nv), None,
+                                      None))
+        kk = np.empty(nk.value, dtype=np.uint64)
+        kv = np.empty(nk.value, dtype=np.uint16)
+        vk = np.empty(nv.value, dtype=np.uint64)
+        vv = np.empty(2 * nv.value, dtype=np.float64)
+        check(lib().ed_term_hash_read(fileName.encode(), b, ctypes.byref(nk),
+                                      kk.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                      kv.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)), ctypes.byref(nv),
+                                      vk.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _f64p(vv)))
+        self._set(kk, kv, vk, vv.view(np.complex128))
+
+
+class QuarticTermHashTables(_TermHashTables):
+    """interacting_ofl_model/term_hash_tables.hpp QuarticTermHashTables
+    (term_hash_tables.cpp): k1 for (k2, k3, k4) and V(k1, k2, k3, k4)."""
+
+    NLABELS = 4
+
+    # term_hash_tables_base.hpp:229-247: every (k2, k3, k4), k3 == k4 included
+    def SetQuarticFromArray(self, quarticArray: ComplexQuarticTermTables):
+        K = self.m_kMax = quarticArray.m_kMax
+        k2, k3, k4 = (a.ravel() for a in np.meshgrid(np.arange(K), np.arange(K), np.arange(K), indexing="ij"))
+        t1, t2 = np.minimum(k3, k4), np.maximum(k3, k4)
+        t = t1 * K + t2 - t1 * (t1 + 1) // 2
+        k1 = quarticArray.m_kTable[t * K + k2].astype(np.int64)
+        v = quarticArray.m_vTable[t * K + np.where(k4 > k3, k1, k2)]
+        u = np.uint64
+        kk = (k2.astype(u) << u(48)) | (k3.astype(u) << u(32)) | (k4.astype(u) << u(16))
+        vk = (k1.astype(u) << u(48)) | (k2.astype(u) << u(32)) | (k3.astype(u) << u(16)) | k4.astype(u)
+        self._set(kk, k1, vk, v)
+
+    # term_hash_tables.cpp: GetK1 (k-table look-up), GetVkkkk (0 when absent)
+    def GetK1(self, k2: int, k3: int, k4: int) -> list:
+        return self._klookup(hash_key(k2, k3, k4))
+
+    def GetVkkkk(self, k1: int, k2: int, k3: int, k4: int) -> complex:
+        return self._vlookup(hash_key(k1, k2, k3, k4))
+
+
+class QuadraticTermHashTables(_TermHashTables):
+    """interacting_ofl_model/term_hash_tables.hpp QuadraticTermHashTables:
+    k1 for k2 and E(k1, k2)."""
+
+    NLABELS = 2
+
+    # term_hash_tables_base.hpp:262-275, from occupation energies (the array
+    # QuadraticTermTables: GetK1(k2) = k2, GetEkk(k1, k2) = E[k1])
+    def SetQuadraticFromArray(self, quadraticArray):
+        e = np.ascontiguousarray(getattr(quadraticArray, "m_vTable", quadraticArray), dtype=np.complex128)
+        K = self.m_kMax = len(e)
+        k = np.arange(K, dtype=np.uint64)
+        self._set(k, k.astype(np.uint16), (k << np.uint64(32)) | k, e)
+
+    def GetK1(self, k2: int) -> list:
+        return self._klookup(int(k2))
+
+    def GetEkk(self, k1: int, k2: int) -> complex:
+        return self._vlookup(hash_key(k1, k2))
+
+
 def synthetic_ofl_tables(dimX: int, dimY: int, seed: int = 0):
     """Seeded complex quartic tables with the reference's momentum rule
     (FindK1, interacting_ofl_model.cpp:366-410: kx1 = kx3 + kx4 - kx2 and ky1
@@ -516,22 +654,62 @@ class ComplexSpinlessFermionHamiltonian:
 
     def Add_CdC_Terms(self, energies, minRow: int = 0, maxRow: int | None = None, mpi=None):
         """Occupation energies E_k (QuadraticTermTables::GetEkk with k1 = k2,
-        spinless_fermion_hamiltonian.hpp:150-262): an array of K values or an
-        object with m_vTable."""
-        e = np.ascontiguousarray(getattr(energies, "m_vTable", energies), dtype=np.complex128)
-        self._energies = e
+        spinless_fermion_hamiltonian.hpp:150-262): an array of K values, an
+        object with m_vTable, or QuadraticTermHashTables (diagonal)."""
+        if isinstance(energies, QuadraticTermHashTables):
+            self._energies = energies
+        else:
+            self._energies = np.ascontiguousarray(getattr(energies, "m_vTable", energies), dtype=np.complex128)
         self.m_crsSparseMatrix = None
 
-    def Add_CdCdCC_Terms(self, termTables: ComplexQuarticTermTables, minRow: int = 0, maxRow: int | None = None,
-                         mpi=None, store_upper: bool = False):
+    def Add_CdCdCC_Terms(self, termTables, minRow: int = 0, maxRow: int | None = None, mpi=None,
+                         store_upper: bool = False):
+        """termTables: ComplexQuarticTermTables (array format) or
+        QuarticTermHashTables (hash format, momentum-conserving)."""
         self._tables = termTables
         self._store_upper = bool(store_upper)
         self.m_crsSparseMatrix = None
+
+    def _terms_from_hash(self, t: QuarticTermHashTables):
+        K = t.m_kMax
+        q = self._energies
+        if q is not None and not isinstance(q, QuadraticTermHashTables):
+            if q.shape != (K,):
+                raise EDError(C.ED_ERR_ARG, f"{K} occupation energies expected")
+            qq = QuadraticTermHashTables()
+            qq.SetQuadraticFromArray(q)
+            q = qq
+        if q is None:
+            q = QuadraticTermHashTables()
+        u64p, u16p = ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint16)
+        vv = np.ascontiguousarray(t.vvals.view(np.float64))
+        qv = np.ascontiguousarray(q.vvals.view(np.float64))
+        dimX = getattr(self, "dimX", None) or self.m_fockBasis.dimX
+        dimY = getattr(self, "dimY", None) or self.m_fockBasis.dimY
+        th = ctypes.c_void_p()
+        check(lib().ed_cterms_create_hash(K, dimX, dimY, len(t.kkeys), t.kkeys.ctypes.data_as(u64p),
+                                          t.kvals.ctypes.data_as(u16p), len(t.vkeys), t.vkeys.ctypes.data_as(u64p),
+                                          _f64p(vv), len(q.kkeys), q.kkeys.ctypes.data_as(u64p),
+                                          q.kvals.ctypes.data_as(u16p), len(q.vkeys), q.vkeys.ctypes.data_as(u64p),
+                                          _f64p(qv), ctypes.byref(th)))
+        return th
 
     def Build(self):
         t = self._tables
         if t is None:
             raise EDError(C.ED_ERR_ARG, "Add_CdCdCC_Terms first")
+        if isinstance(t, QuarticTermHashTables):
+            th = self._terms_from_hash(t)
+            try:
+                h = ctypes.c_void_p()
+                check(lib().ed_cham_build_crs(self.m_fockBasis.handle(), th, int(self._store_upper), None,
+                                              ctypes.byref(h)))
+            finally:
+                lib().ed_cterms_free(th)
+            self.m_crsSparseMatrix = ComplexCrsSparseMatrix(h)
+            return
+        if isinstance(self._energies, QuadraticTermHashTables):
+            raise EDError(C.ED_ERR_ARG, "hash-format quadratic terms go with hash-format quartic terms")
         e = None
         if self._energies is not None:
             if self._energies.shape != (t.m_kMax,):
@@ -585,11 +763,14 @@ class ComplexSpinlessFermionHamiltonian:
 class InteractingOflModel:
     """Sector driver of the interacting optical-flux-lattice model
     (interacting_ofl_model.cpp:97-105 SetSector, :952-1027 BuildFockBasis,
-    :1034-1060 BuildHamiltonian, :1067-1135 Diagonalize) for the array table
-    format, with the term tables and occupation energies given (the reference
-    computes them from the non-interacting band structure)."""
+    :1034-1060 BuildHamiltonian, :1067-1135 Diagonalize), with the term tables
+    and occupation energies given (the reference computes them from the
+    non-interacting band structure).  The tables are in the array format until
+    ConvertTableFormat (:597-618) turns them into hash tables; TermsToFile and
+    TermsFromFile (:623-691) store and read hash tables under the reference's
+    file names."""
 
-    def __init__(self, nbrParticles: int, dimX: int, dimY: int, quarticTables: ComplexQuarticTermTables,
+    def __init__(self, nbrParticles: int, dimX: int, dimY: int, quarticTables: ComplexQuarticTermTables | None,
                  energies=None, nbrEigenvalues: int = 1):
         self.N, self.dimX, self.dimY = int(nbrParticles), int(dimX), int(dimY)
         self.tables = quarticTables
@@ -597,6 +778,54 @@ class InteractingOflModel:
         self.nev = int(nbrEigenvalues)
         self.kxTot = self.kyTot = 0
         self.hamiltonian = None
+        self.m_tableFormat = "array"
+        self.m_quarticHashTables = QuarticTermHashTables()
+        self.m_quadraticHashTables = QuadraticTermHashTables()
+
+    def ConvertTableFormat(self):
+        """Array tables to hash tables (interacting_ofl_model.cpp:597-618);
+        the arrays are dropped, as the reference clears them."""
+        if self.m_tableFormat != "array":
+            return
+        K = self.dimX * self.dimY
+        self.m_quarticHashTables.Clear()
+        self.m_quadraticHashTables.Clear()
+        self.m_quarticHashTables.Initialize(K)
+        self.m_quadraticHashTables.Initialize(K)
+        self.m_quadraticHashTables.SetQuadraticFromArray(
+            self.energies if self.energies is not None else np.zeros(K, dtype=np.complex128))
+        self.m_quarticHashTables.SetQuarticFromArray(self.tables)
+        self.tables = None
+        self.energies = None
+        self.m_tableFormat = "hash"
+
+    def _term_file_names(self, outPath: str):
+        import os
+        tail = f"_table_kx_{self.dimX}_ky_{self.dimY}.dat"
+        return (os.path.join(outPath, "quadratic_coefficient" + tail), os.path.join(outPath, "quartic_coefficient" + tail))
+
+    def TermsToFile(self, outPath: str, fmt: str = "binary"):
+        """The hash tables to quadratic_/quartic_coefficient_table_kx_X_ky_Y.dat
+        in outPath (interacting_ofl_model.cpp:623-651); the array format's own
+        complex table files are not written here."""
+        if self.m_tableFormat != "hash":
+            raise EDError(C.ED_ERR_ARG, "ConvertTableFormat first: only hash-format term files are written")
+        fq, f4 = self._term_file_names(outPath)
+        self.m_quadraticHashTables.ToFile(fq, fmt)
+        self.m_quarticHashTables.ToFile(f4, fmt)
+
+    def TermsFromFile(self, outPath: str, fmt: str = "binary"):
+        """Hash tables from the files TermsToFile writes
+        (interacting_ofl_model.cpp:656-691); the model then builds from them."""
+        K = self.dimX * self.dimY
+        fq, f4 = self._term_file_names(outPath)
+        self.m_quarticHashTables.Initialize(K)
+        self.m_quadraticHashTables.Initialize(K)
+        self.m_quarticHashTables.FromFile(f4, fmt)
+        self.m_quadraticHashTables.FromFile(fq, fmt)
+        self.tables = None
+        self.energies = None
+        self.m_tableFormat = "hash"
 
     def SetSector(self, kxSector: int, kySector: int):
         self.kxTot, self.kyTot = int(kxSector), int(kySector)
@@ -610,9 +839,13 @@ class InteractingOflModel:
         return empty
 
     def BuildHamiltonian(self, store_upper: bool = False):
-        if self.energies is not None:
-            self.hamiltonian.Add_CdC_Terms(self.energies)
-        self.hamiltonian.Add_CdCdCC_Terms(self.tables, store_upper=store_upper)
+        if self.m_tableFormat == "hash":
+            self.hamiltonian.Add_CdC_Terms(self.m_quadraticHashTables)
+            self.hamiltonian.Add_CdCdCC_Terms(self.m_quarticHashTables, store_upper=store_upper)
+        else:
+            if self.energies is not None:
+                self.hamiltonian.Add_CdC_Terms(self.energies)
+            self.hamiltonian.Add_CdCdCC_Terms(self.tables, store_upper=store_upper)
         self.hamiltonian.Build()
 
     def Diagonalize(self, **kw) -> bool:

@@ -428,6 +428,33 @@ ed_status ed_basis_momentum_build(int N, int dimX, int dimY, int kxTot, int kyTo
 ed_status ed_cterms_create(int norb, int dimX, int dimY, const uint16_t* ktable, const double* vtable,
                            const double* energies, ed_cterms** out);
 ed_status ed_cterms_free(ed_cterms* t);
+/* The same terms from the reference's hash-table format (TermHashTables,
+ * hamiltonians/term_hash_tables_base.hpp:44-276, as InteractingOflModel::
+ * ConvertTableFormat fills it, interacting_ofl_model.cpp:597-618): the quartic
+ * k-table (nk keys of (k2, k3, k4) packed as (k2 << 48) | (k3 << 32) | (k4 <<
+ * 16), each with one k1) and value table (nv keys of (k1, k2, k3, k4) packed
+ * as (k1 << 48) | (k2 << 32) | (k3 << 16) | k4, complex values as re, im
+ * pairs), and optionally the quadratic ones (k-table keys k2 with k1 values,
+ * value keys (k1 << 32) | k2).  The tables must be momentum-conserving: one
+ * k1 for every (k2, k3, k4), k1 = k2 in the quadratic tables, and values that
+ * the array layout holds (ED_ERR_ARG otherwise).  Same result as
+ * ed_cterms_create on the arrays they were filled from. */
+ed_status ed_cterms_create_hash(int norb, int dimX, int dimY, uint32_t nk, const uint64_t* kkeys,
+                                const uint16_t* kvals, uint32_t nv, const uint64_t* vkeys, const double* vvals,
+                                uint32_t nqk, const uint64_t* qkkeys, const uint16_t* qkvals, uint32_t nqv,
+                                const uint64_t* qvkeys, const double* qvvals, ed_cterms** out);
+/* The hash-table files of TermHashTables::ToFileBase / FromFileBase
+ * (term_hash_tables_base.hpp:139-205 with multi_key_hash.hpp:480-682): the
+ * header line, then the k-table (nlabels - 1 labels) and the value table
+ * (nlabels labels: 4 quartic, 2 quadratic), binary (uint32 count, uint64 keys,
+ * then uint16 k1 values or (re, im) doubles) or text (count and label count,
+ * then one tab-separated entry a line at 15 significant digits).
+ * ed_term_hash_read: with NULL arrays it sets nk and nv to the entry counts;
+ * with arrays of at least *nk and *nv entries it fills them. */
+ed_status ed_term_hash_write(const char* path, int binary, int nlabels, uint32_t nk, const uint64_t* kkeys,
+                             const uint16_t* kvals, uint32_t nv, const uint64_t* vkeys, const double* vvals);
+ed_status ed_term_hash_read(const char* path, int binary, uint32_t* nk, uint64_t* kkeys, uint16_t* kvals,
+                            uint32_t* nv, uint64_t* vkeys, double* vvals);
 /* SpinlessFermionHamiltonian<dcmplx>::Add_CdC_Terms + Add_CdCdCC_Terms
  * (spinless_fermion_hamiltonian.hpp:150-436) as InteractingOflModel::
  * BuildHamiltonian calls them (interacting_ofl_model.cpp:1034-1052).  Upper

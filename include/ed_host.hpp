@@ -35,6 +35,7 @@
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "ed_capi.h"
@@ -71,6 +72,11 @@ inline void EdCheck(ed_status s, MpiWrapper* mpi = nullptr)
 }
 
 }  // namespace utilities
+
+// utilities/wrappers/io_wrapper.hpp:24
+namespace io {
+enum fileFormat_t { _TEXT_ = 0, _BINARY_ = 1 };
+}
 
 namespace diagonalization {
 
@@ -250,6 +256,9 @@ class FermionFockBasis {
         return GetStoredDimension() == 0;
     }
     iSize_t NbrParticles() const { return m_kind ? (iSize_t)m_par[0] : 0; }
+    // the momentum grid of a momentum sector (0 for other bases)
+    iSize_t DimX() const { return m_kind == 2 ? (iSize_t)m_par[1] : 0; }
+    iSize_t DimY() const { return m_kind == 2 ? (iSize_t)m_par[2] : 0; }
     iSize_t NbrOrbitals() const { return m_kind == 1 ? (iSize_t)m_par[1] : m_kind == 2 ? (iSize_t)(m_par[1] * m_par[2]) : 0; }
     fock_t GetStoredDimension() const
     {
@@ -971,6 +980,149 @@ class OflQuadraticTermTables {
     std::vector<std::complex<double>> m_vTable;
 };
 
+// hamiltonians/term_hash_tables_base.hpp:44-276 TermHashTables<dcmplx>: the
+// k-table (keys of nlabels - 1 labels, each with one k1; a key may repeat)
+// and the value table, kept as the flat key and value lists of its files;
+// keys packed as utilities::Key does (two labels (k1 << 32) | k2, three
+// (k2 << 48) | (k3 << 32) | (k4 << 16), four (k1 << 48) | (k2 << 32) |
+// (k3 << 16) | k4).  Files through ed_term_hash_write / ed_term_hash_read.
+class OflTermHashTablesBase {
+  public:
+    explicit OflTermHashTablesBase(int nbrLabels) : m_nbrLabels(nbrLabels) {}
+    void Initialize(kState_t kMax) { m_kMax = kMax; }
+    void Clear()
+    {
+        m_kKeys.clear();
+        m_kValues.clear();
+        m_vKeys.clear();
+        m_vValues.clear();
+        m_kLookup.clear();
+        m_vLookup.clear();
+    }
+    iSize_t GetMaxKCount() const
+    {
+        std::unordered_map<uint64_t, iSize_t> c;
+        iSize_t m = 1;
+        for (uint64_t k : m_kKeys) m = std::max(m, ++c[k]);
+        return m;
+    }
+    void ToFile(const std::string& fileName, io::fileFormat_t format, utilities::MpiWrapper& mpi) const
+    {
+        utilities::EdCheck(ed_term_hash_write(fileName.c_str(), format == io::_BINARY_ ? 1 : 0, m_nbrLabels,
+                                              (uint32_t)m_kKeys.size(), m_kKeys.data(), m_kValues.data(),
+                                              (uint32_t)m_vKeys.size(), m_vKeys.data(),
+                                              reinterpret_cast<const double*>(m_vValues.data())),
+                           &mpi);
+    }
+    void FromFile(const std::string& fileName, io::fileFormat_t format, utilities::MpiWrapper& mpi)
+    {
+        uint32_t nk = 0, nv = 0;
+        const int b = format == io::_BINARY_ ? 1 : 0;
+        utilities::EdCheck(ed_term_hash_read(fileName.c_str(), b, &nk, nullptr, nullptr, &nv, nullptr, nullptr), &mpi);
+        Clear();
+        m_kKeys.resize(nk);
+        m_kValues.resize(nk);
+        m_vKeys.resize(nv);
+        m_vValues.resize(nv);
+        utilities::EdCheck(ed_term_hash_read(fileName.c_str(), b, &nk, m_kKeys.data(), m_kValues.data(), &nv,
+                                             m_vKeys.data(), reinterpret_cast<double*>(m_vValues.data())),
+                           &mpi);
+        Index();
+    }
+    static uint64_t Key(uint32_t k1, uint32_t k2) { return ((uint64_t)k1 << 32) | k2; }
+    static uint64_t Key(uint16_t k2, uint16_t k3, uint16_t k4)
+    {
+        return ((uint64_t)k2 << 48) | ((uint64_t)k3 << 32) | ((uint64_t)k4 << 16);
+    }
+    static uint64_t Key(uint16_t k1, uint16_t k2, uint16_t k3, uint16_t k4)
+    {
+        return ((uint64_t)k1 << 48) | ((uint64_t)k2 << 32) | ((uint64_t)k3 << 16) | k4;
+    }
+
+    kState_t m_kMax = 0;
+    std::vector<uint64_t> m_kKeys, m_vKeys;
+    std::vector<kState_t> m_kValues;
+    std::vector<std::complex<double>> m_vValues;
+
+  protected:
+    void Insert(uint64_t kkey, kState_t k1, uint64_t vkey, std::complex<double> v)
+    {
+        m_kKeys.push_back(kkey);
+        m_kValues.push_back(k1);
+        m_vKeys.push_back(vkey);
+        m_vValues.push_back(v);
+    }
+    void Index()
+    {
+        m_kLookup.clear();
+        m_vLookup.clear();
+        for (size_t i = 0; i < m_kKeys.size(); ++i) m_kLookup[m_kKeys[i]].push_back(m_kValues[i]);
+        for (size_t i = 0; i < m_vKeys.size(); ++i) m_vLookup.emplace(m_vKeys[i], m_vValues[i]);
+    }
+    void K1(kState_t* buf, iSize_t& nbr, uint64_t key) const
+    {
+        nbr = 0;   // a missing key has no k1 (the reference leaves the count unset)
+        auto it = m_kLookup.find(key);
+        if (it == m_kLookup.end()) return;
+        for (kState_t k : it->second) buf[nbr++] = k;
+    }
+    std::complex<double> V(uint64_t key) const
+    {
+        auto it = m_vLookup.find(key);
+        return it == m_vLookup.end() ? std::complex<double>(0.0, 0.0) : it->second;
+    }
+
+  private:
+    int m_nbrLabels;
+    std::unordered_map<uint64_t, std::vector<kState_t>> m_kLookup;
+    std::unordered_map<uint64_t, std::complex<double>> m_vLookup;
+};
+
+// interacting_ofl_model/term_hash_tables.hpp QuarticTermHashTables
+class OflQuarticTermHashTables : public OflTermHashTablesBase {
+  public:
+    OflQuarticTermHashTables() : OflTermHashTablesBase(4) {}
+    // term_hash_tables_base.hpp:229-247: every (k2, k3, k4)
+    void SetQuarticFromArray(OflQuarticTermTables* a)
+    {
+        Clear();
+        m_kMax = (kState_t)a->m_kMax;
+        kState_t k1 = 0;
+        iSize_t n = 0;
+        for (kState_t k2 = 0; k2 < m_kMax; ++k2)
+            for (kState_t k3 = 0; k3 < m_kMax; ++k3)
+                for (kState_t k4 = 0; k4 < m_kMax; ++k4) {
+                    a->GetK1(&k1, n, k2, k3, k4);
+                    Insert(Key(k2, k3, k4), k1, Key(k1, k2, k3, k4), a->GetVkkkk(k1, k2, k3, k4));
+                }
+        Index();
+    }
+    void GetK1(kState_t* buf, iSize_t& nbrK1, kState_t k2, kState_t k3, kState_t k4) const
+    {
+        K1(buf, nbrK1, Key(k2, k3, k4));
+    }
+    std::complex<double> GetVkkkk(kState_t k1, kState_t k2, kState_t k3, kState_t k4) const
+    {
+        return V(Key(k1, k2, k3, k4));
+    }
+};
+
+// interacting_ofl_model/term_hash_tables.hpp QuadraticTermHashTables
+class OflQuadraticTermHashTables : public OflTermHashTablesBase {
+  public:
+    OflQuadraticTermHashTables() : OflTermHashTablesBase(2) {}
+    // term_hash_tables_base.hpp:262-275 (the array tables: k1 = k2)
+    void SetQuadraticFromArray(OflQuadraticTermTables* a)
+    {
+        Clear();
+        m_kMax = (kState_t)a->GetDimension();
+        for (kState_t k = 0; k < m_kMax; ++k) Insert(k, k, Key((uint32_t)k, (uint32_t)k), (*a->GetVTable())[k]);
+        Index();
+    }
+    void GetK1(kState_t* buf, iSize_t& nbrK1, kState_t k2) const { K1(buf, nbrK1, k2); }
+    std::complex<double> GetEkk(kState_t k1, kState_t k2) const { return V(Key((uint32_t)k1, (uint32_t)k2)); }
+};
+
 // spinless_fermion_hamiltonian.hpp:52 for T = dcmplx, as InteractingOflModel
 // drives it (interacting_ofl_model.cpp:952-1135): SetFockBasis (a momentum
 // sector), Add_CdC_Terms, Add_CdCdCC_Terms, LanczosDiagonalize.  The device
@@ -1004,12 +1156,47 @@ class SpinlessFermionHamiltonian<std::complex<double>> {
                           bool storeUpper = false)
     {
         m_tables = tables;
+        m_hashTables = nullptr;
+        m_storeUpper = storeUpper;
+        Clear();
+    }
+    // the hash-format branch of InteractingOflModel::BuildHamiltonian
+    // (interacting_ofl_model.cpp:1046-1049); momentum-conserving tables only
+    void Add_CdC_Terms(OflQuadraticTermHashTables* tables, fock_t /*minRow*/, fock_t /*maxRow*/,
+                       utilities::MpiWrapper&)
+    {
+        m_hashEnergies = tables;
+        Clear();
+    }
+    void Add_CdCdCC_Terms(OflQuarticTermHashTables* tables, fock_t /*minRow*/, fock_t /*maxRow*/,
+                          utilities::MpiWrapper&, bool storeUpper = false)
+    {
+        m_hashTables = tables;
+        m_tables = nullptr;
         m_storeUpper = storeUpper;
         Clear();
     }
     void Build(utilities::MpiWrapper& mpi)
     {
         Clear();
+        if (m_hashTables) {
+            const OflQuarticTermHashTables& q = *m_hashTables;
+            static const OflQuadraticTermHashTables none;
+            const OflQuadraticTermHashTables& d = m_hashEnergies ? *m_hashEnergies : none;
+            ed_cterms* t = nullptr;
+            utilities::EdCheck(
+                ed_cterms_create_hash((int)m_nbrOrbitals, (int)m_fockBasis.DimX(), (int)m_fockBasis.DimY(),
+                                      (uint32_t)q.m_kKeys.size(), q.m_kKeys.data(), q.m_kValues.data(),
+                                      (uint32_t)q.m_vKeys.size(), q.m_vKeys.data(),
+                                      reinterpret_cast<const double*>(q.m_vValues.data()), (uint32_t)d.m_kKeys.size(),
+                                      d.m_kKeys.data(), d.m_kValues.data(), (uint32_t)d.m_vKeys.size(),
+                                      d.m_vKeys.data(), reinterpret_cast<const double*>(d.m_vValues.data()), &t),
+                &mpi);
+            const ed_status s = ed_cham_build_crs(m_fockBasis.handle(), t, m_storeUpper ? 1 : 0, nullptr, &m_crs);
+            ed_cterms_free(t);
+            utilities::EdCheck(s, &mpi);
+            return;
+        }
         if (!m_tables) throw utilities::EdError(ED_ERR_ARG, "Add_CdCdCC_Terms first");
         ed_cterms* t = nullptr;
         const double* e = m_energies.empty() ? nullptr : reinterpret_cast<const double*>(m_energies.data());
@@ -1068,6 +1255,8 @@ class SpinlessFermionHamiltonian<std::complex<double>> {
     utilities::storageMethod_t m_storageMethod = utilities::_SPARSE_CRS_;
     std::vector<std::complex<double>> m_energies;
     OflQuarticTermTables* m_tables = nullptr;
+    OflQuarticTermHashTables* m_hashTables = nullptr;
+    OflQuadraticTermHashTables* m_hashEnergies = nullptr;
     bool m_storeUpper = false;
     ed_ccrs* m_crs = nullptr;
     ed_solve_info m_info{};

@@ -931,7 +931,76 @@ def ref_ofl_lib():
     L.refo_basis.argtypes = [ctypes.c_int] * 5 + [_u64p]
     L.refo_build_crs_file.restype = ctypes.c_int64
     L.refo_build_crs_file.argtypes = [ctypes.c_int] * 5 + [_u16p, _f64p, _f64p, ctypes.c_char_p]
+    if hasattr(L, "refo_hash_files"):
+        L.refo_hash_files.restype = ctypes.c_int
+        L.refo_hash_files.argtypes = [ctypes.c_int] * 2 + [_u16p, _f64p, _f64p, ctypes.c_char_p, ctypes.c_char_p,
+                                                           ctypes.c_int]
+        L.refo_hash_read.restype = ctypes.c_int
+        L.refo_hash_read.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _u16p,
+                                     ctypes.POINTER(ctypes.c_uint32), _f64p]
+        L.refo_build_crs_file_hash.restype = ctypes.c_int64
+        L.refo_build_crs_file_hash.argtypes = [ctypes.c_int] * 5 + [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                                                    ctypes.c_char_p]
     return L
+
+
+def _read_reference_ccrs(path: str):
+    """A complex CRS file of the reference's binary format: (rowptr int64,
+    col, complex values)."""
+    raw = open(path, "rb").read()
+    nnz, rows = (int(x) for x in np.frombuffer(raw[:8], dtype=np.uint32))
+    o = 8
+    rp = np.frombuffer(raw[o:o + 4 * (rows + 1)], dtype=np.int32).astype(np.int64)
+    o += 4 * (rows + 1)
+    col = np.frombuffer(raw[o:o + 4 * nnz], dtype=np.int32).copy()
+    o += 4 * nnz
+    val = np.frombuffer(raw[o:o + 16 * nnz], dtype=np.complex128).copy()
+    return rp, col, val
+
+
+def ref_hash_files(R, X: int, Y: int, ktab, vtab, energies, quartic_path: str, quadratic_path: str,
+                   binary: bool = True):
+    """The reference's hash tables filled from array tables
+    (term_hash_tables_base.hpp:229-275 SetQuarticFromArray /
+    SetQuadraticFromArray) and written by its ToFile (:139-170)."""
+    kt = np.ascontiguousarray(ktab, dtype=np.uint16)
+    vt = np.ascontiguousarray(vtab, dtype=np.complex128).view(np.float64)
+    e = None if energies is None else np.ascontiguousarray(energies, dtype=np.complex128).view(np.float64)
+    rc = R.refo_hash_files(X, Y, _p(kt, _u16p), _p(vt, _f64p), None if e is None else _p(e, _f64p),
+                           quartic_path.encode(), quadratic_path.encode(), int(binary))
+    if rc != 0:
+        raise RuntimeError("reference hash-table writer failed")
+
+
+def ref_hash_read(R, K: int, quartic_path: str, binary: bool = True):
+    """What the reference reads back from a quartic hash-table file (FromFile,
+    GetK1, GetVkkkk): (first k1 [K,K,K] with 65535 where none, k1 counts
+    [K,K,K], V [K,K,K,K] complex), indexed [k2,k3,k4] and [k1,k2,k3,k4]."""
+    k1 = np.empty(K ** 3, dtype=np.uint16)
+    nk = np.empty(K ** 3, dtype=np.uint32)
+    v = np.empty(2 * K ** 4, dtype=np.float64)
+    if R.refo_hash_read(K, quartic_path.encode(), int(binary), _p(k1, _u16p),
+                        nk.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _p(v, _f64p)) != 0:
+        raise RuntimeError("reference hash-table reader failed")
+    return k1.reshape(K, K, K), nk.reshape(K, K, K), v.view(np.complex128).reshape(K, K, K, K)
+
+
+def ref_build_upper_complex_hash(R, N: int, X: int, Y: int, kx: int, ky: int, quartic_path: str,
+                                 quadratic_path: str, binary: bool = True):
+    """The reference's own complex build from hash-table files (the
+    hash-format branch of interacting_ofl_model.cpp:1046-1049); (rowptr
+    int64, col, complex values), or None for an empty sector."""
+    import tempfile
+    fd, path = tempfile.mkstemp(suffix=".bin")
+    os.close(fd)
+    try:
+        nnz = R.refo_build_crs_file_hash(N, X, Y, kx, ky, quartic_path.encode(), quadratic_path.encode(),
+                                         int(binary), path.encode())
+        if nnz < 0:
+            return None
+        return _read_reference_ccrs(path)
+    finally:
+        os.unlink(path)
 
 
 def ref_basis_momentum(R, N: int, X: int, Y: int, kx: int, ky: int) -> np.ndarray:

@@ -152,6 +152,44 @@ int main(int argc, char** argv)
     for (int i = 0; i < 3; ++i) std::printf("%s%.17g", i ? ", " : "", Hc.m_eigenvalues[i]);
     std::printf("]}");
 
+    // the same terms in the hash-table format, as InteractingOflModel's
+    // ConvertTableFormat, TermsToFile / TermsFromFile and hash-format
+    // BuildHamiltonian use them (interacting_ofl_model.cpp:597-691, 1046-1049)
+    diagonalization::OflQuarticTermHashTables qh;
+    diagonalization::OflQuadraticTermHashTables dh;
+    qh.Initialize(K);
+    dh.Initialize(K);
+    dh.SetQuadraticFromArray(&oe);
+    qh.SetQuarticFromArray(&oq);
+    qh.ToFile("quartic_coefficient_table_kx_3_ky_4.dat", io::_BINARY_, mpi);
+    dh.ToFile("quadratic_coefficient_table_kx_3_ky_4.dat", io::_BINARY_, mpi);
+    diagonalization::OflQuarticTermHashTables qh2;
+    diagonalization::OflQuadraticTermHashTables dh2;
+    qh2.Initialize(K);
+    dh2.Initialize(K);
+    qh2.FromFile("quartic_coefficient_table_kx_3_ky_4.dat", io::_BINARY_, mpi);
+    dh2.FromFile("quadratic_coefficient_table_kx_3_ky_4.dat", io::_BINARY_, mpi);
+    diagonalization::kState_t k1buf[4];
+    diagonalization::iSize_t nk1 = 0;
+    qh2.GetK1(k1buf, nk1, 2, 5, 7);
+    diagonalization::kState_t k1arr = 0;
+    diagonalization::iSize_t na = 0;
+    oq.GetK1(&k1arr, na, 2, 5, 7);
+    const bool lookups_ok = nk1 == 1 && k1buf[0] == k1arr && qh2.GetVkkkk(k1arr, 2, 5, 7) == oq.GetVkkkk(k1arr, 2, 5, 7) &&
+                            qh2.GetMaxKCount() == 1;
+    diagonalization::FermionFockBasis mb2;
+    mb2.GenerateFockSpaceMomentum(4, X, Y, 1, 2, mpi);
+    diagonalization::SpinlessFermionHamiltonian<std::complex<double>> Hh;
+    Hh.Initialize(4, K, utilities::_SPARSE_MAPPED_, mpi);
+    Hh.SetFockBasis(std::move(mb2));
+    Hh.Add_CdC_Terms(&dh2, 0, dimc, mpi);
+    Hh.Add_CdCdCC_Terms(&qh2, 0, dimc, mpi);
+    const bool ok6 = Hh.LanczosDiagonalize(3, mpi, 1e-10);
+    bool same = ok6 && Hh.GetNbrNonZeros() == Hc.GetNbrNonZeros();
+    for (int i = 0; i < 3 && same; ++i) same = Hh.m_eigenvalues[i] == Hc.m_eigenvalues[i];
+    std::printf(", \"ofl_hash\": {\"ok\": %s, \"lookups_ok\": %s, \"same_as_array\": %s}", ok6 ? "true" : "false",
+                lookups_ok ? "true" : "false", same ? "true" : "false");
+
     // The reference's model sequence as it is written there
     // (pseudopotential_model.cpp:160-189 BuildFockBasis, :233-249
     // BuildHamiltonian, pseudopotential_model_base.hpp:235-275 BaseDiagonalize):

@@ -25,6 +25,17 @@ Outputs (committed):
     most_probable  the reference's most probable states and amplitudes of
                  seeded complex unit vectors (its routine is only sound for
                  complex vectors)
+    crs_complex_hash  the same complex builds through the reference's
+                 hash-table path (TermsFromFile + the hash branch of
+                 BuildHamiltonian) from hash-table files written by this
+                 project's writer (ed_term_hash_write), binary and text
+    hash_writer_defect  the entries the reference's own hash-table writer
+                 drops (its gather's duplicate removal skips the second-
+                 smallest key), for each grid of crs_complex_hash
+  ofl_hash_ref_2x3_{quartic,quadratic}.{bin,txt}
+                 hash-table files written by the reference itself (2 x 3 grid,
+                 tables oracle.ofl_tables(2, 3, 11), energies linspace(-0.4,
+                 0.6, 6) + 1e-3 i k), for the reader tests
 """
 import json
 import os
@@ -50,6 +61,8 @@ CRS2_CASES = [(4, 6, 0, True), (5, 8, 1, True), (6, 10, 0, False), (6, 10, 2, Tr
 # linspace(-0.4, 0.6, X*Y) + 1e-3 i k
 CRSC_CASES = [(3, 3, 4, 1, 2, False), (4, 3, 4, 0, 0, True), (5, 4, 4, 2, 1, True), (6, 4, 5, 0, 3, True),
               (7, 4, 5, 3, 4, True)]
+# complex builds through hash-table files (a subset of CRSC_CASES)
+CRSCH_CASES = [(3, 3, 4, 1, 2, False), (4, 3, 4, 0, 0, True), (6, 4, 5, 0, 3, True)]
 OBS_CASE = (8, 22, 0)
 OBS_SEED, OBS_NEV = 11, 2
 MP_CASE = (6, 16, 2)
@@ -106,6 +119,47 @@ def main():
             "N": N, "X": X, "Y": Y, "kx": kx, "ky": ky, "energies": en, "dim": len(rp) - 1,
             "nnz_upper": int(rp[-1]), "sha256": O.crs_digest(rp, col, val.view(np.float64))}
         print("complex", N, X, Y, kx, ky, en, len(rp) - 1, int(rp[-1]), f"{time.time() - t0:.1f}s", flush=True)
+    out["crs_complex_hash"] = {}
+    out["hash_writer_defect"] = {}
+    import tempfile
+    sys.path.insert(0, ROOT)
+    import hamiltonian_diagonalization_gb300 as ed
+    tmp = tempfile.mkdtemp()
+    for (N, X, Y, kx, ky, en) in CRSCH_CASES:
+        K = X * Y
+        kt, vt = O.ofl_tables(X, Y, K + N)
+        e = (np.linspace(-0.4, 0.6, K) + 1e-3j * np.arange(K)) if en else None
+        model = ed.InteractingOflModel(N, X, Y, ed.ComplexQuarticTermTables(X, Y, kt, vt), e)
+        model.ConvertTableFormat()
+        for fmt in ("binary", "text"):
+            d = os.path.join(tmp, f"{N}_{X}_{Y}_{fmt}")
+            os.makedirs(d, exist_ok=True)
+            model.TermsToFile(d, fmt)
+            fq, f4 = model._term_file_names(d)
+            rp, col, val = O.ref_build_upper_complex_hash(Rc, N, X, Y, kx, ky, f4, fq, fmt == "binary")
+            out["crs_complex_hash"][f"{N}_{X}_{Y}_{kx}_{ky}_{int(en)}_{fmt}"] = {
+                "N": N, "X": X, "Y": Y, "kx": kx, "ky": ky, "energies": en, "format": fmt, "dim": len(rp) - 1,
+                "nnz_upper": int(rp[-1]), "sha256": O.crs_digest(rp, col, val.view(np.float64))}
+            print("complex hash", N, X, Y, kx, ky, en, fmt, len(rp) - 1, int(rp[-1]), flush=True)
+        # what the reference's own writer leaves out
+        f4, fq = os.path.join(tmp, "ref_q.bin"), os.path.join(tmp, "ref_d.bin")
+        O.ref_hash_files(Rc, X, Y, kt, vt, e, f4, fq, True)
+        for name, path, full in (("quartic", f4, model.m_quarticHashTables),
+                                 ("quadratic", fq, model.m_quadraticHashTables)):
+            cls = ed.QuarticTermHashTables if name == "quartic" else ed.QuadraticTermHashTables
+            h = cls()
+            h.FromFile(path, "binary")
+            out["hash_writer_defect"][f"{X}_{Y}_{name}"] = {
+                "written_k": len(h.kkeys), "written_v": len(h.vkeys), "expected": len(full.kkeys),
+                "missing_k_keys": sorted(set(full.kkeys.tolist()) - set(h.kkeys.tolist())),
+                "missing_v_keys": sorted(set(full.vkeys.tolist()) - set(h.vkeys.tolist()))}
+    # small reference-written files for the reader tests
+    X, Y = 2, 3
+    kt, vt = O.ofl_tables(X, Y, 11)
+    e = np.linspace(-0.4, 0.6, X * Y) + 1e-3j * np.arange(X * Y)
+    for binary, ext in ((True, "bin"), (False, "txt")):
+        O.ref_hash_files(Rc, X, Y, kt, vt, e, os.path.join(HERE, f"ofl_hash_ref_2x3_quartic.{ext}"),
+                         os.path.join(HERE, f"ofl_hash_ref_2x3_quadratic.{ext}"), binary)
     import ctypes
     f64p = ctypes.POINTER(ctypes.c_double)
     N, norb, tlz = OBS_CASE

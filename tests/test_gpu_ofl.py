@@ -223,3 +223,80 @@ def test_device_crs_matches_reference_build(cuda, oracle):
         rp, col, val = model.hamiltonian.m_crsSparseMatrix.to_host()
         assert len(rp) - 1 == ent["dim"] and int(rp[-1]) == ent["nnz_upper"], key
         assert oracle.crs_digest(rp, col, np.ascontiguousarray(val).view(np.float64)) == ent["sha256"], key
+
+
+def test_hash_format_build_matches_reference_hash_path(cuda, oracle, tmp_path):
+    # hash-table files from this project's writer, built by the reference's own
+    # hash path (TermsFromFile + the hash branch of BuildHamiltonian,
+    # tests/golden/make_golden_ham.py) and here from the same files: same
+    # digest; binary files give the array path's digest, text ones keep 15
+    # significant digits
+    import json
+    import os
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ref_hamiltonians.json")))
+    for key, ent in gold["crs_complex_hash"].items():
+        N, X, Y, kx, ky, fmt = ent["N"], ent["X"], ent["Y"], ent["kx"], ent["ky"], ent["format"]
+        K = X * Y
+        kt, vt = oracle.ofl_tables(X, Y, K + N)
+        e = (np.linspace(-0.4, 0.6, K) + 1e-3j * np.arange(K)) if ent["energies"] else None
+        m = ed.InteractingOflModel(N, X, Y, ed.ComplexQuarticTermTables(X, Y, kt, vt), e)
+        m.ConvertTableFormat()
+        d = str(tmp_path / key)
+        os.makedirs(d)
+        m.TermsToFile(d, fmt)
+        m2 = ed.InteractingOflModel(N, X, Y, None)
+        m2.TermsFromFile(d, fmt)
+        m2.SetSector(kx, ky)
+        assert not m2.BuildFockBasis()
+        m2.BuildHamiltonian(store_upper=True)
+        rp, col, val = m2.hamiltonian.m_crsSparseMatrix.to_host()
+        assert len(rp) - 1 == ent["dim"] and int(rp[-1]) == ent["nnz_upper"], key
+        assert oracle.crs_digest(rp, col, np.ascontiguousarray(val).view(np.float64)) == ent["sha256"], key
+
+
+def test_hash_build_refuses_what_the_arrays_cannot_hold(cuda, oracle, tmp_path):
+    import os
+    X, Y, N = 2, 3, 3
+    K = X * Y
+    kt, vt = oracle.ofl_tables(X, Y, 11)
+
+    def model_with(quartic, quadratic):
+        m = ed.InteractingOflModel(N, X, Y, None)
+        m.m_tableFormat = "hash"
+        m.m_quarticHashTables, m.m_quadraticHashTables = quartic, quadratic
+        m.SetSector(0, 0)
+        m.BuildFockBasis()
+        return m
+
+    T = ed.ComplexQuarticTermTables(X, Y, kt, vt)
+    good = ed.QuarticTermHashTables()
+    good.SetQuarticFromArray(T)
+    diag = ed.QuadraticTermHashTables()
+    diag.SetQuadraticFromArray(np.linspace(-0.4, 0.6, K))
+    model_with(good, diag).BuildHamiltonian()      # builds
+    # the reference's own file lacks the k1 of (0, 0, 1): refused, not read past
+    ref = ed.QuarticTermHashTables()
+    ref.FromFile(os.path.join(os.path.dirname(__file__), "golden", "ofl_hash_ref_2x3_quartic.bin"), "binary")
+    with pytest.raises(ed.EDError):
+        model_with(ref, diag).BuildHamiltonian()
+    # two k1 for one (k2, k3, k4): not momentum-conserving
+    two = ed.QuarticTermHashTables()
+    two._set(np.append(good.kkeys, good.kkeys[5]), np.append(good.kvals, (good.kvals[5] + 1) % K),
+             good.vkeys, good.vvals)
+    with pytest.raises(ed.EDError):
+        model_with(two, diag).BuildHamiltonian()
+    # an off-diagonal one-body term
+    off = ed.QuadraticTermHashTables()
+    off._set(diag.kkeys, np.roll(diag.kvals, 1), diag.vkeys, diag.vvals)
+    with pytest.raises(ed.EDError):
+        model_with(good, off).BuildHamiltonian()
+    # two values for one array slot
+    bad = ed.QuarticTermHashTables()
+    vv = good.vvals.copy()
+    k2, k3, k4 = 1, 0, 2                            # k4 > k3: its value sits in slot k1
+    k1 = T.GetK1(k2, k3, k4)[0]
+    i = int(np.nonzero(good.vkeys == np.uint64(ed.hash_key(k1, k2, k3, k4)))[0][0])
+    vv[i] += 0.5
+    bad._set(good.kkeys, good.kvals, good.vkeys, vv)
+    with pytest.raises(ed.EDError):
+        model_with(bad, diag).BuildHamiltonian()

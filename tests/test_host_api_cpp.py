@@ -26,10 +26,13 @@ def test_host_classes_compile(edlib, tmp_path):
 @pytest.mark.gpu
 def test_host_classes_solve_sector(cuda, oracle, tmp_path):
     exe = compile_demo(tmp_path)
-    out = subprocess.run([exe, "6", "16", "0"], capture_output=True, text=True, timeout=300)
+    out = subprocess.run([exe, "6", "16", "0"], capture_output=True, text=True, timeout=300, cwd=str(tmp_path))
     assert out.returncode == 0, out.stdout + out.stderr
     r = json.loads(out.stdout.strip().splitlines()[-1])
     assert r["ok"] and r["ok_host_product"] and r["rank_ok"]
+    # hash-format terms through files: same matrix, same eigenvalues as the arrays
+    h = r["ofl_hash"]
+    assert h["ok"] and h["lookups_ok"] and h["same_as_array"]
     import scipy.sparse as sp
     pp = oracle.odd_coulomb_list(16)
     b = oracle.basis(6, 16, 0)
