@@ -39,7 +39,7 @@ class EDError(RuntimeError):
 
 class LanczosParams(ctypes.Structure):
     _fields_ = [("nev", c_int), ("ncv", c_int), ("max_restarts", c_int), ("tol", c_double), ("seed", c_u64),
-                ("want_vectors", c_int), ("verify", c_int), ("degeneracy_passes", c_int)]
+                ("want_vectors", c_int), ("verify", c_int), ("degeneracy_passes", c_int), ("diagonal_check", c_int)]
 
 
 class SolveInfo(ctypes.Structure):

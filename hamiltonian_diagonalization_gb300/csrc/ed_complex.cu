@@ -769,6 +769,9 @@ void clanczos_solve(const ed_ccrs& a, const ed_lanczos_params& p, const double* 
     std::memset(&inf, 0, sizeof(inf));
     SolveStream ss(caller);
     cudaStream_t st = ss.s;
+    if (p.diagonal_check &&
+        diagonal_spectrum(a.rowptr.p, a.col.p, a.val.p, 1, n, nev, evals, evecs_dev, info, st))
+        return;
     if (n < 60 || n <= (int64_t)nev + 2) {
         cdense_solve(a, nev, evals, evecs_dev, &inf, st);
         inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

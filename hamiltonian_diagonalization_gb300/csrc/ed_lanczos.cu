@@ -842,6 +842,165 @@ void lanczos_once(const ed_op& op, const ed_lanczos_params& p, const double* v0_
     ED_REQUIRE(converged, ED_ERR_NOCONV, "Lanczos did not converge within the restart cap");
 }
 
+// ------------------------------------------------------------ diagonal matrices
+
+// A stored matrix with no off-diagonal element above the reference's
+// 1e-14 (HamiltonianBase::MatrixDiagonalCheck, hamiltonian_base.hpp:378-449)
+// has its spectrum on the diagonal.  Values are double or complex (double2).
+__device__ __forceinline__ double dmod(double v) { return fabs(v); }
+__device__ __forceinline__ double dmod(double2 v) { return hypot(v.x, v.y); }
+__device__ __forceinline__ double dreal(double v) { return v; }
+__device__ __forceinline__ double dreal(double2 v) { return v.x; }
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_crs_offdiag(const int64_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                          int64_t n, int* __restrict__ flag)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+            if (col[k] != r && dmod(val[k]) > kSparseZeroTol) {
+                atomicOr(flag, 1);
+                break;
+            }
+    }
+}
+
+// d[r] = the real part of the stored diagonal of row r (0 when none)
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_crs_diag(const int64_t* __restrict__ rowptr,
+                                                       const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                       int64_t n, double* __restrict__ d)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+            if (col[k] == r) s += dreal(val[k]);
+        d[r] = s;
+    }
+}
+
+__device__ __forceinline__ bool pair_less(double av, int64_t ai, double bv, int64_t bi)
+{
+    return av < bv || (av == bv && ai < bi);
+}
+
+// Selection step t: the smallest (d[j], j) above (selv[t-1], seli[t-1]) in the
+// lexicographic order (values, then index), so that t = 0..nev-1 give the nev
+// smallest entries in ascending order, each copy of a repeated value at its
+// own index.  Block partials, finished by the last block.
+__global__ void __launch_bounds__(kThreads) k_select_next(const double* __restrict__ d, int64_t n, int t,
+                                                          double* __restrict__ selv, int64_t* __restrict__ seli,
+                                                          double* __restrict__ pv, int64_t* __restrict__ pi,
+                                                          unsigned int* __restrict__ counter)
+{
+    __shared__ double sv[kThreads];
+    __shared__ int64_t si[kThreads];
+    const double lv = t > 0 ? selv[t - 1] : -INFINITY;
+    const int64_t li = t > 0 ? seli[t - 1] : -1;
+    double bv = INFINITY;
+    int64_t bi = n;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const double v = d[j];
+        if (pair_less(lv, li, v, j) && pair_less(v, j, bv, bi)) {
+            bv = v;
+            bi = j;
+        }
+    }
+    sv[threadIdx.x] = bv;
+    si[threadIdx.x] = bi;
+    __syncthreads();
+    for (int o = kThreads / 2; o; o >>= 1) {
+        if (threadIdx.x < o && pair_less(sv[threadIdx.x + o], si[threadIdx.x + o], sv[threadIdx.x], si[threadIdx.x])) {
+            sv[threadIdx.x] = sv[threadIdx.x + o];
+            si[threadIdx.x] = si[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        pv[blockIdx.x] = sv[0];
+        pi[blockIdx.x] = si[0];
+    }
+    if (!last_block(counter)) return;
+    if (threadIdx.x == 0) {
+        double v = INFINITY;
+        int64_t i = n;
+        for (unsigned b = 0; b < gridDim.x; ++b) {
+            const double x = __ldcg(pv + b);
+            const int64_t y = __ldcg(pi + b);
+            if (pair_less(x, y, v, i)) {
+                v = x;
+                i = y;
+            }
+        }
+        selv[t] = v;
+        seli[t] = i;
+    }
+}
+
+// column t of the eigenvectors = the unit vector at seli[t] (stride values
+// per entry: 1 real, 2 complex)
+__global__ void k_unit_columns(const int64_t* __restrict__ seli, int nev, int64_t n, int stride, double* __restrict__ X)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nev; t += gridDim.x * blockDim.x)
+        X[((int64_t)t * n + seli[t]) * stride] = 1.0;
+}
+
+template <class T>
+bool diagonal_spectrum_impl(const int64_t* rowptr, const int32_t* col, const T* val, int64_t n, int nev,
+                            double* evals_host, double* evecs_dev, int stride, ed_solve_info* info, cudaStream_t st)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const int grid = sm_count() * 4;
+    DevBuf<int> flag(1);
+    ED_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+    k_crs_offdiag<T><<<grid, kThreads, 0, st>>>(rowptr, col, val, n, flag.p);
+    ::edgb::count_launch();
+    ED_CUDA(cudaGetLastError());
+    int h = 0;
+    ED_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    if (h) return false;
+    DevBuf<double> d(n), selv(nev), pv(grid);
+    DevBuf<int64_t> seli(nev), pi(grid);
+    DevBuf<unsigned int> counter(1);
+    ED_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), st));
+    k_crs_diag<T><<<grid, kThreads, 0, st>>>(rowptr, col, val, n, d.p);
+    ::edgb::count_launch();
+    for (int t = 0; t < nev; ++t) {
+        k_select_next<<<grid, kThreads, 0, st>>>(d.p, n, t, selv.p, seli.p, pv.p, pi.p, counter.p);
+        ::edgb::count_launch();
+    }
+    ED_CUDA(cudaGetLastError());
+    ED_CUDA(cudaMemcpyAsync(evals_host, selv.p, (size_t)nev * 8, cudaMemcpyDeviceToHost, st));
+    if (evecs_dev) {
+        ED_CUDA(cudaMemsetAsync(evecs_dev, 0, (size_t)n * nev * stride * 8, st));
+        k_unit_columns<<<1, 256, 0, st>>>(seli.p, nev, n, stride, evecs_dev);
+        ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
+    }
+    ED_CUDA(cudaStreamSynchronize(st));
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->converged = nev;
+        info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return true;
+}
+
+}  // namespace
+
+bool diagonal_spectrum(const int64_t* rowptr, const int32_t* col, const double* val, int complex_values, int64_t n,
+                       int nev, double* evals_host, double* evecs_dev, ed_solve_info* info, cudaStream_t st)
+{
+    if (complex_values)
+        return diagonal_spectrum_impl(rowptr, col, reinterpret_cast<const double2*>(val), n, nev, evals_host,
+                                      evecs_dev, 2, info, st);
+    return diagonal_spectrum_impl(rowptr, col, val, n, nev, evals_host, evecs_dev, 1, info, st);
+}
+
+namespace {
+
 void add_info(ed_solve_info& a, const ed_solve_info& b)
 {
     a.restarts += b.restarts;
@@ -863,6 +1022,11 @@ void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0
 {
     const int64_t n = op.n;
     const int nev = p.nev;
+    if (p.diagonal_check && op.kind == ed_op::CRS && n >= 1 && nev >= 1 && nev <= n) {
+        SolveStream ss(caller_stream);
+        const ed_crs& a = *op.crs;
+        if (diagonal_spectrum(a.rowptr.p, a.col.p, a.val.p, 0, n, nev, evals_host, evecs_dev, info, ss.s)) return;
+    }
     if (p.degeneracy_passes <= 0 || n < 60 || n <= (int64_t)nev + 2) {
         lanczos_once(op, p, v0_dev, evals_host, evecs_dev, info, caller_stream);
         return;
@@ -959,6 +1123,11 @@ void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczo
     ED_REQUIRE(b.levels == 2 && (int64_t)b.dim == op.n, ED_ERR_ARG, "the ladder solve takes the operator's two-level basis");
     const int64_t n = op.n;
     const int nev = p.nev;
+    if (p.diagonal_check && op.kind == ed_op::CRS && n >= 1 && nev >= 1 && nev <= n) {
+        SolveStream ds(caller);
+        const ed_crs& a = *op.crs;
+        if (diagonal_spectrum(a.rowptr.p, a.col.p, a.val.p, 0, n, nev, evals_host, evecs_dev, info, ds.s)) return;
+    }
     if (n < 60 || n <= (int64_t)nev + 2) {   // the dense path sees every copy
         lanczos_once(op, p, v0_dev, evals_host, evecs_dev, info, caller);
         return;

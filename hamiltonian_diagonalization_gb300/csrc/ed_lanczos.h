@@ -92,6 +92,13 @@ void op_prepare(const ed_op& op, cudaStream_t st);
 void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
                    double* evecs_dev, ed_solve_info* info, cudaStream_t st);
 void residual_norms(const ed_op& op, const double* x, const double* lambda, int k, double* res, cudaStream_t st);
+// The nev lowest eigenpairs of a stored matrix (n rows, values double or,
+// with complex_values, (re, im) pairs) when no off-diagonal element exceeds
+// 1e-14 in modulus: its nev smallest diagonal entries ascending (ties by
+// index), each with its unit vector in evecs_dev (n * nev, real or complex
+// layout; may be null).  Returns false, doing nothing more, otherwise.
+bool diagonal_spectrum(const int64_t* rowptr, const int32_t* col, const double* val, int complex_values, int64_t n,
+                       int nev, double* evals_host, double* evecs_dev, ed_solve_info* info, cudaStream_t st);
 // Lowest p.nev eigenpairs of a two-level Hamiltonian, every copy of a
 // degenerate eigenvalue from the level-exchange ladder of basis b.
 void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczos_params& p, const double* v0_dev,

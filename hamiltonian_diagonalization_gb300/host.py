@@ -368,8 +368,11 @@ class SpinlessFermionHamiltonian:
 
     def LanczosDiagonalize(self, nbrEigenvalues: int, tol: float = 1e-10, v0=None, seed: int = 0, ncv: int = 0,
                            want_vectors: bool = True, verify: bool = True, max_restarts: int = 0,
-                           degeneracy_passes: int = 0):
-        """hamiltonian_base.hpp:770-931 with the device Lanczos; eigenvalues ascending."""
+                           degeneracy_passes: int = 0, diagonal_check: bool = True):
+        """hamiltonian_base.hpp:770-931 with the device Lanczos; eigenvalues
+        ascending.  diagonal_check: a stored matrix without off-diagonal
+        elements is solved from its diagonal (MatrixDiagonalCheck, :378-449 and
+        :803-850), each copy of a repeated value with its own unit vector."""
         mv = MatrixVectorFunction(self)
         arp = ArpackWrapper()
         n = self.GetDimension()
@@ -377,7 +380,7 @@ class SpinlessFermionHamiltonian:
         evecs = np.empty((nbrEigenvalues, n)) if want_vectors else None
         ok = arp.DiagonalizeSymmetricMatrix(mv, evecs, evals, n, n, nbrEigenvalues, tol=tol, v0=v0, seed=seed,
                                             ncv=ncv, verify=verify, max_restarts=max_restarts,
-                                            degeneracy_passes=degeneracy_passes)
+                                            degeneracy_passes=degeneracy_passes, diagonal_check=diagonal_check)
         self.m_eigenvalues = evals
         self.m_eigenvectors = evecs
         self.last_info = arp.last_info
@@ -737,14 +740,17 @@ class ComplexSpinlessFermionHamiltonian:
         check(lib().ed_cspmv(self.m_crsSparseMatrix._h, _dptr(x), _dptr(y), stream))
 
     def LanczosDiagonalize(self, nbrEigenvalues: int, tol: float = 1e-10, v0=None, seed: int = 0, ncv: int = 0,
-                           want_vectors: bool = True, verify: bool = True, max_restarts: int = 0) -> bool:
+                           want_vectors: bool = True, verify: bool = True, max_restarts: int = 0,
+                           diagonal_check: bool = True) -> bool:
         """Lowest eigenpairs (hamiltonian_base.hpp:770-931 with the complex
-        driver); eigenvalues ascending, eigenvectors complex128 (nev, n)."""
+        driver); eigenvalues ascending, eigenvectors complex128 (nev, n).
+        diagonal_check as the real class's."""
         if self.m_crsSparseMatrix is None:
             self.Build()
         n = self.GetDimension()
         p = LanczosParams(nev=int(nbrEigenvalues), ncv=int(ncv), max_restarts=int(max_restarts or 0), tol=float(tol),
-                          seed=int(seed), want_vectors=int(bool(want_vectors)), verify=int(bool(verify)))
+                          seed=int(seed), want_vectors=int(bool(want_vectors)), verify=int(bool(verify)),
+                          diagonal_check=int(bool(diagonal_check)))
         info = SolveInfo()
         ev = np.empty(nbrEigenvalues)
         vec = np.empty((nbrEigenvalues, n), dtype=np.complex128) if want_vectors else None
@@ -968,7 +974,7 @@ class ArpackWrapper:
     def DiagonalizeSymmetricMatrix(self, MatrixVectorMultiply, eigenvectors, eigenvalues, nodeDim: int, fullDim: int,
                                    nbrEigenvalues: int, mpi=None, tol: float = 1e-10, v0=None, seed: int = 0,
                                    ncv: int = 0, verify: bool = True, max_restarts: int = 0,
-                                   degeneracy_passes: int = 0) -> bool:
+                                   degeneracy_passes: int = 0, diagonal_check: bool = False) -> bool:
         """Lowest `nbrEigenvalues` eigenpairs.  MatrixVectorMultiply is either
         a MatrixVectorFunction (device product) or a Python callable
         f(x_host, y_host) on numpy arrays (the reference's std::function form).
@@ -996,7 +1002,7 @@ class ArpackWrapper:
         try:
             p = LanczosParams(nev=int(nbrEigenvalues), ncv=int(ncv), max_restarts=int(max_restarts or 0), tol=float(tol),
                               seed=int(seed), want_vectors=int(eigenvectors is not None), verify=int(bool(verify)),
-                              degeneracy_passes=int(degeneracy_passes))
+                              degeneracy_passes=int(degeneracy_passes), diagonal_check=int(bool(diagonal_check)))
             info = SolveInfo()
             ev = np.empty(nbrEigenvalues)
             vec = np.empty(n * nbrEigenvalues) if eigenvectors is not None else None
@@ -1128,25 +1134,26 @@ class TwoLevelSpinlessFermionHamiltonian(SpinlessFermionHamiltonian):
 
     def LanczosDiagonalize(self, nbrEigenvalues: int, tol: float = 1e-10, v0=None, seed: int = 0, ncv: int = 0,
                            want_vectors: bool = True, verify: bool = True, max_restarts: int = 0,
-                           degeneracy_passes: int | None = None):
+                           degeneracy_passes: int | None = None, diagonal_check: bool = True):
         """Lowest eigenpairs with every copy of a degenerate eigenvalue: the
         levels do not mix, so every pair of level-0 and level-1 multiplets
         (L0, L1) gives 2 min(L0, L1) + 1 states of one energy in a sector.  By
         default the copies come from the level-exchange ladder
         (ed_lanczos_two_level); degeneracy_passes = k uses k deflated passes
-        instead, 0 the plain single-sequence solve."""
+        instead, 0 the plain single-sequence solve.  diagonal_check as the
+        one-level class's."""
         if self.m_crsSparseMatrix is None:
             self.Build()
         if degeneracy_passes is not None:
             return super().LanczosDiagonalize(nbrEigenvalues, tol=tol, v0=v0, seed=seed, ncv=ncv,
                                               want_vectors=want_vectors, verify=verify, max_restarts=max_restarts,
-                                              degeneracy_passes=degeneracy_passes)
+                                              degeneracy_passes=degeneracy_passes, diagonal_check=diagonal_check)
         n = self.GetDimension()
         op = self.operator_handle()
         try:
             p = LanczosParams(nev=int(nbrEigenvalues), ncv=int(ncv), max_restarts=int(max_restarts or 0),
                               tol=float(tol), seed=int(seed), want_vectors=int(bool(want_vectors)),
-                              verify=int(bool(verify)))
+                              verify=int(bool(verify)), diagonal_check=int(bool(diagonal_check)))
             info = SolveInfo()
             ev = np.empty(nbrEigenvalues)
             vec = np.empty((nbrEigenvalues, n)) if want_vectors else None

@@ -224,6 +224,13 @@ typedef struct {
                            copies of degenerate eigenvalues one start vector cannot
                            see.  Ends early when a pass adds nothing.  The batched
                            solver ignores it.                                         */
+    int diagonal_check;  /* 1 -> a stored matrix (CRS operator, complex CRS) with no
+                           off-diagonal element above 1e-14 in modulus is solved
+                           directly: its nev lowest diagonal entries, each with its
+                           own unit vector (HamiltonianBase::MatrixDiagonalCheck and
+                           the shortcut after it, hamiltonian_base.hpp:378-449,
+                           660-700, 803-850; the reference gives every copy of a
+                           repeated value the same normalised indicator vector).    */
 } ed_lanczos_params;
 
 typedef struct {

@@ -393,6 +393,11 @@ class ArpackWrapper {
     void SetSeed(uint64_t seed) { m_seed = seed; }
     // further deflated solves that recover copies of degenerate eigenvalues
     void SetDegeneracyPasses(int passes) { m_degeneracyPasses = passes; }
+    // a stored matrix with no off-diagonal element is solved from its
+    // diagonal (HamiltonianBase::MatrixDiagonalCheck and its shortcut,
+    // hamiltonian_base.hpp:378-449, 803-850); the Hamiltonian classes turn
+    // it on, as the reference's LanczosDiagonalize does the check
+    void SetDiagonalCheck(bool check) { m_diagonalCheck = check; }
     // start vector (host, nodeDim doubles) in place of --use-initial's file
     void SetInitialVector(const std::vector<double>& v) { m_initial = v; }
     // arpack_wrapper.hpp: --use-initial reads the start vector (raw FP64,
@@ -459,6 +464,7 @@ class ArpackWrapper {
         p.want_vectors = eigenvectors != nullptr;
         p.verify = 1;
         p.degeneracy_passes = m_degeneracyPasses;
+        p.diagonal_check = m_diagonalCheck ? 1 : 0;
         if (m_useInitial && !m_initialFile.empty()) {
             std::vector<double> v(n);
             FILE* f = std::fopen(m_initialFile.c_str(), "rb");
@@ -481,6 +487,7 @@ class ArpackWrapper {
     }
     int m_maxIterations = 2000;
     int m_degeneracyPasses = 0;
+    bool m_diagonalCheck = false;
     int m_ncv = 0;
     double m_tol = 1e-10;
     uint64_t m_seed = 0;
@@ -593,6 +600,7 @@ class SpinlessFermionHamiltonian {
         const fock_t n = GetFockSpaceDimension();
         m_eigenvalues.assign(nbrEigenvalues, 0.0);
         m_eigenvectors.assign((size_t)n * nbrEigenvalues, 0.0);
+        m_arpackWrapper.SetDiagonalCheck(true);
         const bool ok = m_arpackWrapper.DiagonalizeSymmetricMatrix(mv, m_eigenvectors.data(), m_eigenvalues.data(),
                                                                    (int)n, (int)n, (int)nbrEigenvalues, mpi);
         m_data.m_eigenvectorsCalculated = ok;
@@ -607,6 +615,7 @@ class SpinlessFermionHamiltonian {
         m_eigenvectors.assign(wantVectors ? (size_t)n * nbrEigenvalues : 0, 0.0);
         MatrixVectorFunction<T> mv(*this, mpi);
         m_arpackWrapper.SetTolerance(tol);
+        m_arpackWrapper.SetDiagonalCheck(true);
         const bool ok = m_arpackWrapper.DiagonalizeSymmetricMatrix(mv, wantVectors ? m_eigenvectors.data() : nullptr,
                                                                    m_eigenvalues.data(), (int)n, (int)n,
                                                                    (int)nbrEigenvalues, mpi);
@@ -867,6 +876,7 @@ class TwoLevelSpinlessFermionHamiltonian {
         utilities::EdCheck(ed_op_from_crs(m_crs, &op), &mpi);
         bool ok = true;
         if (m_passesSet) {
+            m_arpackWrapper.SetDiagonalCheck(true);
             ok = m_arpackWrapper.DiagonalizeOperator(op, wantVectors ? m_eigenvectors.data() : nullptr,
                                                      m_eigenvalues.data(), (int)n, (int)nbrEigenvalues, mpi);
         } else {
@@ -875,6 +885,7 @@ class TwoLevelSpinlessFermionHamiltonian {
             p.tol = tol;
             p.verify = 1;
             p.want_vectors = wantVectors;
+            p.diagonal_check = 1;
             const ed_status s = ed_lanczos_two_level(m_fockBasis.handle(), op, &p, nullptr, m_eigenvalues.data(),
                                                      wantVectors ? m_eigenvectors.data() : nullptr, &m_info);
             if (s != ED_OK) {
@@ -1228,6 +1239,7 @@ class SpinlessFermionHamiltonian<std::complex<double>> {
         p.tol = tol;
         p.verify = 1;
         p.want_vectors = wantVectors;
+        p.diagonal_check = 1;
         const ed_status s = ed_clanczos(m_crs, &p, nullptr, m_eigenvalues.data(),
                                         wantVectors ? reinterpret_cast<double*>(m_eigenvectors.data()) : nullptr,
                                         &m_info);

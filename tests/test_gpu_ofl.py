@@ -135,7 +135,8 @@ def test_complex_solver_through_breakdowns(cuda, oracle):
     for upper in (False, True):
         model, _ = build(N, X, Y, kx, ky, T, e, upper=upper)
         model.nev = nev
-        assert model.Diagonalize(tol=1e-10, seed=3), model.hamiltonian.last_info
+        # the Krylov path itself (the diagonal shortcut off)
+        assert model.Diagonalize(tol=1e-10, seed=3, diagonal_check=False), model.hamiltonian.last_info
         H = model.hamiltonian
         assert H.last_info["breakdowns"] >= 1
         assert np.max(np.abs(H.m_eigenvalues - w[:nev])) <= 1e-10
@@ -300,3 +301,27 @@ def test_hash_build_refuses_what_the_arrays_cannot_hold(cuda, oracle, tmp_path):
     bad._set(good.kkeys, good.kvals, good.vkeys, vv)
     with pytest.raises(ed.EDError):
         model_with(bad, diag).BuildHamiltonian()
+
+
+def test_diagonal_matrix_is_solved_from_its_diagonal(cuda, oracle):
+    # no interaction: the stored matrix is diagonal, and LanczosDiagonalize
+    # takes the reference's shortcut (MatrixDiagonalCheck): the nev lowest
+    # diagonal entries, no product, each copy of a repeated value its own
+    # unit vector (the reference gives every copy the same one)
+    N, X, Y, kx, ky = 6, 4, 4, 0, 1
+    K = X * Y
+    kt, vt = oracle.ofl_tables(X, Y, 5)
+    T = ed.ComplexQuarticTermTables(X, Y, kt, np.zeros_like(vt))
+    e = (np.arange(K) % 3).astype(float) + 0.25 * (np.arange(K) % 2)
+    b = oracle.basis_momentum(N, X, Y, kx, ky)
+    d = np.sort(np.array([sum(e[k] for k in range(K) if (w >> k) & 1) for w in b]))
+    for upper in (False, True):
+        model, _ = build(N, X, Y, kx, ky, T, e, upper=upper)
+        model.nev = 9
+        assert model.Diagonalize(tol=1e-10, seed=3)
+        H = model.hamiltonian
+        assert H.last_info["matvecs"] == 0 and H.last_info["converged"] == 9
+        assert np.max(np.abs(H.m_eigenvalues - d[:9])) <= 1e-12
+        V = H.m_eigenvectors
+        assert np.array_equal(np.abs(V).sum(axis=1), np.ones(9))              # unit vectors
+        assert np.allclose(V.conj() @ V.T, np.eye(9))                          # distinct positions

@@ -183,3 +183,26 @@ def test_device_crs_matches_reference_build(cuda, oracle):
         rp, col, val = H.m_crsSparseMatrix.to_host()
         assert len(rp) - 1 == ent["dim"] and int(rp[-1]) == ent["nnz_upper"], key
         assert oracle.crs_digest(rp, col, val) == ent["sha256"], key
+
+
+@pytest.mark.parametrize("upper", [False, True])
+def test_diagonal_two_level_matrix_from_its_diagonal(cuda, oracle, upper):
+    # occupation energies only: the stored matrix is diagonal, and the solve
+    # takes the reference's shortcut (MatrixDiagonalCheck) with no product, on
+    # the ladder path and the single-sequence path alike
+    N, norb0, tlz = 5, 7, 2
+    t0 = ed.QuarticTermTables(norb0, np.zeros(norb0 - 1))
+    t1 = ed.QuarticTermTables(norb0 + 2, np.zeros(norb0 + 1))
+    e0 = np.linspace(-0.3, 0.2, norb0)
+    e1 = np.linspace(0.9, 1.4, norb0 + 2)
+    H = build(N, norb0, tlz, t0, t1, e0, e1, upper=upper)
+    f, s = oracle.basis2(N, norb0, tlz)
+    d = np.array([sum(e0[k] for k in range(norb0) if (a >> k) & 1) + sum(e1[k] for k in range(norb0 + 2) if (c >> k) & 1)
+                  for a, c in zip(f, s)])
+    want = np.sort(d)[:6]
+    for passes in (None, 0):
+        assert H.LanczosDiagonalize(6, tol=1e-10, seed=2, degeneracy_passes=passes)
+        assert H.last_info["matvecs"] == 0
+        assert np.max(np.abs(H.m_eigenvalues - want)) <= 1e-12
+        V = H.m_eigenvectors
+        assert np.allclose(V @ V.T, np.eye(6)) and np.array_equal(np.abs(V).sum(axis=1), np.ones(6))
