@@ -842,6 +842,27 @@ void lanczos_once(const ed_op& op, const ed_lanczos_params& p, const double* v0_
     ED_REQUIRE(converged, ED_ERR_NOCONV, "Lanczos did not converge within the restart cap");
 }
 
+// ------------------------------------------------------------ two-level start
+
+// Keep the entries of the block 2 M0 in {0, 1} (M0 = the lowest level's Lz,
+// from its norb0 high bits: orbital i has 2 m = 2 i - (norb0 - 1)) and zero
+// the rest; *kept counts the block.  No term mixes the levels, so H keeps M0:
+// a Krylov space started inside the block stays there.
+__global__ void __launch_bounds__(kThreads) k_keep_m0_block(const uint64_t* __restrict__ words, int64_t n, int K0,
+                                                            int K1, double* __restrict__ v,
+                                                            unsigned long long* __restrict__ kept)
+{
+    unsigned long long c = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        int two_m0 = 0;
+        for (uint64_t f = words[r] >> K1; f; f &= f - 1) two_m0 += 2 * (__ffsll((long long)f) - 1) - (K0 - 1);
+        if (two_m0 == 0 || two_m0 == 1) ++c;
+        else v[r] = 0.0;
+    }
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(kept, c);
+}
+
 // ------------------------------------------------------------ diagonal matrices
 
 // A stored matrix with no off-diagonal element above the reference's
@@ -1184,9 +1205,30 @@ void lanczos_solve_two_level(const ed_basis& b, const ed_op& op, const ed_lanczo
     };
     const double lscale = (double)b.norb0 * b.norb1;   // the ladder's norm is below K0*K1/4
     std::vector<double> res(nev, 0.0);
+    // At Lz = 0 every multiplet (L0, L1) has exactly one member in the block
+    // 2 M0 in {0, 1} (its members span M0 = -min(L0, L1) .. min(L0, L1)), so
+    // a sequence started there meets each multiplet once, with no copy for
+    // rounding to grow, and the ladder supplies the copies.  Elsewhere, or
+    // with a caller's start, the start covers the whole sector.
+    DevBuf<double> vblock;
+    const double* v0_seq = v0_dev;
+    if (!v0_dev && b.two_lz == 0) {
+        vblock.alloc(n);
+        DevBuf<unsigned long long> kept(1);
+        ED_CUDA(cudaMemsetAsync(kept.p, 0, sizeof(unsigned long long), st));
+        k_random<<<sm_count() * 4, kThreads, 0, st>>>(vblock.p, n, p.seed);
+        ::edgb::count_launch();
+        k_keep_m0_block<<<sm_count() * 4, kThreads, 0, st>>>(b.words.p, n, b.norb0, b.norb1, vblock.p, kept.p);
+        ::edgb::count_launch();
+        ED_CUDA(cudaGetLastError());
+        unsigned long long hk = 0;
+        ED_CUDA(cudaMemcpyAsync(&hk, kept.p, sizeof(hk), cudaMemcpyDeviceToHost, st));
+        ED_CUDA(cudaStreamSynchronize(st));
+        if (hk >= (unsigned long long)nev + 2) v0_seq = vblock.p;
+    }
     bool ok = false;
     for (int attempt = 0; attempt < 2 && !ok; ++attempt) {
-        const double* v0a = v0_dev;
+        const double* v0a = v0_seq;
         q.tol = attempt == 0 ? tol : tol * 1e-2;
         if (attempt == 1) {
             // start from the sum of the first attempt's vectors
