@@ -126,6 +126,17 @@ __device__ __forceinline__ void ldsm_x4(uint32_t* r, const bf16* p)
                  : "r"(a));
 }
 
+// Two integers of magnitude below 2^7 as a bf16 pair (x = a in the low
+// half): float(x) is 1.5 * 2^23 + x read back minus 1.5 * 2^23 (exact for
+// |x| < 2^22, on the FP32 pipe), and its top 16 bits are exactly the bf16 of
+// x because x has at most 7 significant bits.
+__device__ __forceinline__ uint32_t bf16x2_of_small_ints(int a, int b)
+{
+    const float fa = __int_as_float(0x4B400000 + a) - 12582912.0f;
+    const float fb = __int_as_float(0x4B400000 + b) - 12582912.0f;
+    return __byte_perm((uint32_t)__float_as_int(fa), (uint32_t)__float_as_int(fb), 0x7632);
+}
+
 // Exact conversion of an integer with |x| < 2^53 to double, by integer
 // operations only (GB300's FP64 pipe is the scarce unit here).
 __device__ __forceinline__ double i53_to_double(long long x)
@@ -280,6 +291,178 @@ __global__ void __launch_bounds__(256) k_rotate_oz(const double* __restrict__ V,
         }
 }
 
+// The same product with V's digits in registers.  One warp takes 16 rows
+// (tiles over the rows, grid-strided) and all k <= 8 NT8 output columns: each
+// lane loads the MP/2 values of its mma.m16n8k16 A-fragment positions (rows
+// g and g + 8 of the tile, columns 16 s + 2 tq + {0, 1, 8, 9} for k-step s,
+// g = lane / 4, tq = lane % 4), takes the row exponents by shuffles among the
+// four lanes of a row, splits every value into its eight 7-bit digits and
+// packs them straight into the fragments of the eight planes (each digit's
+// bf16 bits from a float add on the FP32 pipe, not a conversion).  Y's digit
+// planes sit in shared memory, padded to an even number of 8-column tiles, and
+// one ldmatrix.x4 gives the B fragments of two output tiles.  The
+// anti-diagonal groups and their exact int64 combination are k_rotate_oz's,
+// so the results are the same bits.  No shared memory per row tile.
+template <int MP, int NT8>
+__global__ void __launch_bounds__(256, 1) k_rotate_ozr(const double* __restrict__ V, int64_t n, int m,
+                                                       const bf16* __restrict__ ydig, const int* __restrict__ yexp,
+                                                       int k, double* __restrict__ out)
+{
+    constexpr int KS = MP / 16;           // k-steps
+    constexpr int NC = NT8 * 8;           // output columns computed
+    constexpr int NCP = (NT8 + 1) / 2 * 16;   // columns held: an even number of 8-column tiles (zeros beyond NC)
+    constexpr int LDB = MP + 8;           // bf16 row stride of the Y planes: conflict-free ldmatrix rows
+    __shared__ __align__(16) bf16 sB[kOzPlanes * NCP * LDB];
+    __shared__ int sfe[NC];
+    // Y planes of the first NC columns (host layout [plane][32 columns][MP]),
+    // zero columns up to NCP
+    for (int i = threadIdx.x; i < kOzPlanes * NCP * MP; i += blockDim.x) {
+        const int t = i / (NCP * MP), rem = i - t * NCP * MP, c = rem / MP, j = rem - c * MP;
+        sB[(t * NCP + c) * LDB + j] = c < NC ? ydig[((size_t)t * kOzCols + c) * MP + j] : __float2bfloat16(0.f);
+    }
+    for (int c = threadIdx.x; c < NC; c += blockDim.x) sfe[c] = c < k ? yexp[c] : 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t ntiles = (n + 15) / 16;
+    for (int64_t tile = warp; tile < ntiles; tile += nwarps) {
+        const int64_t ra = tile * 16 + g, rb = ra + 8;
+        // the lane's values at k-step s: q = 0,1 (row ra, columns 16s+2tq+{0,1}),
+        // 2,3 (row rb, same), 4,5 (row ra, +8), 6,7 (row rb, +8); read once for
+        // the row exponents and once more (from L1) for the digits, so that
+        // the values of one k-step at a time are live
+        auto value = [&](int s, int q) -> double {
+            const int j = 16 * s + 2 * tq + (q & 1) + ((q & 4) ? 8 : 0);
+            const int64_t r = (q & 2) ? rb : ra;
+            return (j < m && r < n) ? V[(int64_t)j * n + r] : 0.0;
+        };
+        int emax_a = 0, emax_b = 0;
+#pragma unroll
+        for (int s = 0; s < KS; ++s)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int E = exp_field(value(s, q));
+                if (q & 2) emax_b = max(emax_b, E);
+                else emax_a = max(emax_a, E);
+            }
+        // row exponents over the four lanes of a row
+        emax_a = max(emax_a, __shfl_xor_sync(0xffffffffu, emax_a, 1));
+        emax_a = max(emax_a, __shfl_xor_sync(0xffffffffu, emax_a, 2));
+        emax_b = max(emax_b, __shfl_xor_sync(0xffffffffu, emax_b, 1));
+        emax_b = max(emax_b, __shfl_xor_sync(0xffffffffu, emax_b, 2));
+        // A fragments of the eight planes: af[t][s][i], i = 0 (row ra, k 2tq..),
+        // 1 (row rb), 2 (row ra, k 2tq+8..), 3 (row rb, k +8)
+        uint32_t af[kOzPlanes][KS][4];
+#pragma unroll
+        for (int s = 0; s < KS; ++s) {
+            double vs[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) vs[q] = value(s, q);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int e = (i & 1) ? emax_b : emax_a;
+                int d0[kOzPlanes], d1[kOzPlanes];
+                if (e) {
+                    digits7(vs[2 * i], e - 1022, d0);
+                    digits7(vs[2 * i + 1], e - 1022, d1);
+                } else {
+#pragma unroll
+                    for (int t = 0; t < kOzPlanes; ++t) d0[t] = d1[t] = 0;
+                }
+#pragma unroll
+                for (int t = 0; t < kOzPlanes; ++t) af[t][s][i] = bf16x2_of_small_ints(d0[t], d1[t]);
+            }
+        }
+        // two output tiles of 8 columns at a time, so that only their int64
+        // sums are live beside the fragments
+#pragma unroll 1
+        for (int nt0 = 0; nt0 < NT8; nt0 += 2) {
+            long long hi[2][4], lo[2][4];
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) hi[nt][e] = lo[nt][e] = 0;
+            const int ntn = min(2, NT8 - nt0);
+#pragma unroll
+            for (int dg = 0; dg < kOzGroups; ++dg) {
+                float acc[2][4];
+#pragma unroll
+                for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
+#pragma unroll
+                for (int t = 0; t < kOzPlanes; ++t) {
+                    const int u = dg - t;
+                    if (u < 0 || u >= kOzPlanes) continue;
+#pragma unroll
+                    for (int ks = 0; ks < KS; ++ks) {
+                        // matrices (tile nt0, k 0-7), (nt0, k 8-15), (nt0+1, k 0-7), (nt0+1, k 8-15)
+                        const int mi = lane >> 3, ri = lane & 7;
+                        uint32_t bq[4];
+                        ldsm_x4(bq, sB + (u * NCP + (nt0 + (mi >> 1)) * 8 + ri) * LDB + 16 * ks + (mi & 1) * 8);
+                        const uint32_t b0[2] = {bq[0], bq[1]}, b1[2] = {bq[2], bq[3]};
+                        mma_bf16(acc[0], af[t][ks], b0);
+                        if (ntn > 1) mma_bf16(acc[1], af[t][ks], b1);
+                    }
+                }
+                const bool upper = dg < 5;
+                const long long wgt = 1ll << (7 * (upper ? 4 - dg : 9 - dg));
+#pragma unroll
+                for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const long long c = (long long)__float2int_rz(acc[nt][e]);
+                        if (upper) hi[nt][e] += c * wgt;
+                        else lo[nt][e] += c * wgt;
+                    }
+            }
+            // scale by 2^(e_r + f_c - 77) and store (column-major output)
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int64_t r = (e >= 2) ? rb : ra;
+                    const int c = (nt0 + nt) * 8 + tq * 2 + (e & 1);
+                    if (nt < ntn && r < n && c < k) {
+                        const int er = (e >= 2) ? emax_b : emax_a, fc = sfe[c];
+                        double x = 0.0;
+                        if (er && fc) {
+                            x = fma(i53_to_double(hi[nt][e]), 34359738368.0 /* 2^35 */, i53_to_double(lo[nt][e]));
+                            x *= pow2((er - 1022) + (fc - 1022) - 77);
+                        }
+                        out[(int64_t)c * n + r] = x;
+                    }
+                }
+        }
+    }
+}
+
+template <int MP, int NT8>
+void launch_rotate_ozr(const double* V, int64_t n, int m, const bf16* ydig, const int* yexp, int k, double* out,
+                       cudaStream_t st)
+{
+    // one resident CTA of 8 warps per SM (about 250 registers a thread),
+    // the warps striding over the 16-row tiles
+    const int64_t tiles = (n + 15) / 16;
+    const int64_t grid = std::min<int64_t>((int64_t)rot_sms(), (tiles + 7) / 8);
+    k_rotate_ozr<MP, NT8><<<(unsigned)std::max<int64_t>(1, grid), 256, 0, st>>>(V, n, m, ydig, yexp, k, out);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+template <int MP>
+void launch_rotate_ozr_k(const double* V, int64_t n, int m, const bf16* ydig, const int* yexp, int k, double* out,
+                         cudaStream_t st)
+{
+    switch ((k + 7) / 8) {
+    case 1: launch_rotate_ozr<MP, 1>(V, n, m, ydig, yexp, k, out, st); break;
+    case 2: launch_rotate_ozr<MP, 2>(V, n, m, ydig, yexp, k, out, st); break;
+    case 3: launch_rotate_ozr<MP, 3>(V, n, m, ydig, yexp, k, out, st); break;
+    default: launch_rotate_ozr<MP, 4>(V, n, m, ydig, yexp, k, out, st); break;
+    }
+}
+
 template <int MP>
 void launch_rotate_oz(const double* V, int64_t n, int m, const bf16* ydig, const int* yexp, int k, double* out,
                       cudaStream_t st)
@@ -299,7 +482,7 @@ void rotate_basis(const double* V, int64_t n, int m, const double* Y_host, int l
                   RotateScratch& sc, int method, cudaStream_t st)
 {
     if (k <= 0 || n <= 0) return;
-    const bool tensor = method == 2 || (method == 0 && m <= kRotateTensorMaxM);
+    const bool tensor = method >= 2 || (method == 0 && m <= kRotateTensorMaxM);
     ED_REQUIRE(!tensor || m <= kRotateTensorMaxM, ED_ERR_ARG, "tensor-core rotation takes m <= 64");
     if (!tensor) {
         sc.y.alloc_at_least((size_t)ldy * k);
@@ -339,11 +522,21 @@ void rotate_basis(const double* V, int64_t n, int m, const double* Y_host, int l
     ED_CUDA(cudaMemcpyAsync(sc.ydig.p, sc.ydig_h.data(), sc.ydig_h.size() * 2, cudaMemcpyHostToDevice, st));
     ED_CUDA(cudaMemcpyAsync(sc.yexp.p, sc.yexp_h.data(), sc.yexp_h.size() * 4, cudaMemcpyHostToDevice, st));
     const bf16* yd = reinterpret_cast<const bf16*>(sc.ydig.p);
-    switch (MP) {
-    case 16: launch_rotate_oz<16>(V, n, m, yd, sc.yexp.p, k, out, st); break;
-    case 32: launch_rotate_oz<32>(V, n, m, yd, sc.yexp.p, k, out, st); break;
-    case 48: launch_rotate_oz<48>(V, n, m, yd, sc.yexp.p, k, out, st); break;
-    default: launch_rotate_oz<64>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+    // digits of V in registers (k_rotate_ozr) up to 32 output columns and
+    // m <= 48 (at m = 64 its fragments no longer fit beside the sums)
+    if (method != 3 && k <= kOzCols && MP <= 48) {
+        switch (MP) {
+        case 16: launch_rotate_ozr_k<16>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+        case 32: launch_rotate_ozr_k<32>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+        default: launch_rotate_ozr_k<48>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+        }
+    } else {
+        switch (MP) {
+        case 16: launch_rotate_oz<16>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+        case 32: launch_rotate_oz<32>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+        case 48: launch_rotate_oz<48>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+        default: launch_rotate_oz<64>(V, n, m, yd, sc.yexp.p, k, out, st); break;
+        }
     }
     // the host staging is reused by the next call: wait until the copies have read it
     ED_CUDA(cudaStreamSynchronize(st));
@@ -358,7 +551,8 @@ extern "C" ed_status ed_basis_rotate(const double* V_dev, int64_t n, int m, cons
 {
     return guard([&] {
         ED_REQUIRE(V_dev && Y_host && out_dev && n >= 1 && m >= 1 && k >= 1 && ldy >= m, ED_ERR_ARG, "bad argument");
-        ED_REQUIRE(method >= 0 && method <= 2, ED_ERR_ARG, "method: 0 auto, 1 FP64, 2 tensor cores");
+        ED_REQUIRE(method >= 0 && method <= 3, ED_ERR_ARG,
+                   "method: 0 auto, 1 FP64, 2 tensor cores, 3 tensor cores with V's digits staged in shared memory");
         // scratch kept per host thread, so repeated calls do not allocate
         static thread_local RotateScratch sc;
         rotate_basis(V_dev, n, m, Y_host, ldy, k, out_dev, sc, method, nullptr);

@@ -339,7 +339,7 @@ def rotate_main(C, torch, args):
     Y = np.asfortranarray(np.random.default_rng(2).standard_normal((m, m)))
     yp = Y.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     res = {"rotate": [n, m, k]}
-    for method, name in ((1, "fp64"), (2, "tensor")):
+    for method, name in ((1, "fp64"), (2, "tensor"), (3, "tensor_shared_digits")):
         def call():
             st = C.lib().ed_basis_rotate(ctypes.c_void_p(V.data_ptr()), n, m, yp, m, k,
                                          ctypes.c_void_p(out.data_ptr()), method)

@@ -313,8 +313,10 @@ ed_status ed_residuals_noalloc(const ed_op* op, const double* x_dev, const doubl
 /* Thick-restart basis rotation out = V Y[:, 0..k): V_dev n x m and out_dev
  * n x k column-major device arrays, Y_host column-major with leading
  * dimension ldy >= m.  method 1: FP64 FMAs; 2: BF16 tensor cores with
- * FP64-accurate digit splitting (m <= 64); 0: the solver's choice (2 when
- * m <= 64).  The step of ARPACK's dneupd/dnaupd that forms Ritz vectors from
+ * FP64-accurate digit splitting (m <= 64; V's digits in registers for
+ * m <= 48 and k <= 32, else staged in shared memory); 3: the same with V's
+ * digits always staged in shared memory (same bits as 2); 0: the solver's
+ * choice (2 when m <= 64).  The step of ARPACK's dneupd/dnaupd that forms Ritz vectors from
  * the Arnoldi basis (arpack_wrapper.hpp:873-883 call site); exported so the
  * two methods can be compared.  Returns when out_dev is written. */
 ed_status ed_basis_rotate(const double* V_dev, int64_t n, int m, const double* Y_host, int ldy, int k,

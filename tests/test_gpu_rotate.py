@@ -49,6 +49,21 @@ def test_tensor_rotation_matches_fp64(cuda, n, m, k):
     assert err1 <= 4e-15, err1
     assert err2 <= 4e-15, err2          # at least as accurate as FP64 FMAs
     assert np.all(out2[5] == 0.0) and np.all(out2[:, 1] == 0.0)
+    # the register-digit kernel and the shared-memory one give the same bits
+    st3, out3 = rotate(torch, V, Y, k, 3)
+    assert st3 == 0 and np.array_equal(out2, out3)
+
+
+@pytest.mark.parametrize("n,m,k", [(1371535, 41, 17), (1371535, 41, 10), (20011, 48, 32), (5003, 33, 9), (17, 5, 3)])
+def test_register_and_shared_digit_kernels_agree(cuda, n, m, k):
+    # the headline's restart shapes and edge sizes: bit-identical results
+    torch = cuda
+    rng = np.random.default_rng(n + m + k)
+    V = rng.standard_normal((n, m)) * np.exp(rng.uniform(-6, 0, (n, 1)))
+    Y = rng.standard_normal((m, m))
+    st2, out2 = rotate(torch, V, Y, k, 2)
+    st3, out3 = rotate(torch, V, Y, k, 3)
+    assert st2 == 0 and st3 == 0 and np.array_equal(out2, out3)
 
 
 def test_tensor_rotation_rejects_large_m(cuda):
