@@ -11,7 +11,8 @@ reorthogonalisation -> verified residuals.
          left in HBM), seconds per solve, CUDA events on the launching stream
   e2e    the one-call public API ed_solve_sector from host buffers: start
          vector in, eigenvalues and eigenvectors out, copies inside the timing
-  roofline  the stored-CRS SpMV, algorithmic bytes per product
+  roofline  the stored-CRS SpMV (the fixed-point integer kernel with its two
+         passes over x), algorithmic bytes per product
          nnz*(8+4) + (n+1)*8 + 2*n*8 over its average in-solve duration
   max_rel_eig_vs_fixture  the eigenvalues against the committed ARPACK run
          of the same Hamiltonian (tests/golden/arpack_n11_2s30_lz0.json)
@@ -454,15 +455,17 @@ def main():
                       "nnz_full": nnz},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (traffic or {}).get("bytes_per_launch"),
-                         "kernel": "k_spmv_rows<8,4,2>", "bytes_per_launch": bytes_per,
+                         "kernel": "k_spmv_fix<8,8> (+ k_fix_exp, k_fix_conv on x)", "bytes_per_launch": bytes_per,
                          "avg_launch_ms": spmv_s * 1000.0, "standalone_launch_ms": r["spmv_ms_alone"],
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s"},
-            # the product's other ceiling on GB300: one DFMA per stored element
-            # plus 12 DADD a row (k_spmv_rows<8,4,2>'s reduction) against the
-            # FP64 FMA rate measured here by ed_fp64_fma_rate
-            "fp64_pipe": {"ops_per_launch": nnz + 12 * n, "achieved_per_s": (nnz + 12 * n) / spmv_s,
-                          "peak_per_s": r["fp64_fma_per_s"], "frac": (nnz + 12 * n) / spmv_s / r["fp64_fma_per_s"]},
+            # the FP64 row kernel's floor on GB300 (one DFMA per stored element
+            # plus 12 DADD a row at the FP64 FMA rate measured here by
+            # ed_fp64_fma_rate), which the integer-pipe product is not bound by
+            "fp64_pipe": {"product_fp64_ops": 0, "fp64_row_kernel_ops": nnz + 12 * n,
+                          "peak_per_s": r["fp64_fma_per_s"],
+                          "fp64_row_kernel_floor_ms": (nnz + 12 * n) / r["fp64_fma_per_s"] * 1e3,
+                          "product_ms": spmv_s * 1e3},
             "e2e": {"value": r["e2e_s"], "unit": "s", "h2d_bytes_per_step": n * 8 + NORB * 8,
                     "d2h_bytes_per_step": n * NEV * 8 + NEV * 8},
             "gpu_launches": int(r["launches"]),

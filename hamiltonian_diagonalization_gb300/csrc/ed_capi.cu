@@ -391,8 +391,8 @@ ed_status ed_crs_set_product_kernel(ed_crs* a, int kernel)
 {
     return guarded([&] {
         ED_NONNULL(a);
-        ED_REQUIRE(kernel >= 0 && kernel <= 5, ED_ERR_ARG, "kernel: 0 (chosen by shape) or 1-5 (ed_spmv_kernel)");
-        ED_REQUIRE(kernel == 0 || !a->upper, ED_ERR_ARG, "kernels 1-5 take full storage");
+        ED_REQUIRE(kernel >= 0 && kernel <= 6, ED_ERR_ARG, "kernel: 0 (chosen by shape) or 1-6 (ed_spmv_kernel)");
+        ED_REQUIRE(kernel == 0 || !a->upper, ED_ERR_ARG, "kernels 1-6 take full storage");
         a->product_kernel = kernel;
     });
 }

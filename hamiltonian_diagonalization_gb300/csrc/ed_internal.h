@@ -3,10 +3,13 @@
 
 #include <cstdint>
 #include <cstddef>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -219,6 +222,24 @@ struct ed_sell {
     edgb::DevBuf<double> val;
 };
 
+// Fixed-point copy of a full-storage CRS's values for the integer-pipe
+// product: value a = A 2^(ea - 1080) with A = round(a 2^(1080 - ea)),
+// |A| < 2^58 (ea the largest biased exponent field of the values, at least
+// 1), held as the pair (A mod 2^30, floor(A / 2^30)) of 32-bit integers in
+// one 64-bit word.  x is converted the same way into a per-stream scratch
+// before each product; part holds the per-block exponent maxima of x and,
+// after them, the vector's exponent bound.
+struct ed_fixq {
+    int ea = 1;
+    edgb::DevBuf<int64_t> val;   // nnz + kCrsPad pairs (zero pairs after the last row)
+    struct Scratch {
+        edgb::DevBuf<int64_t> xq;
+        edgb::DevBuf<int> part;
+    };
+    std::mutex mu;
+    std::map<std::pair<int, cudaStream_t>, std::unique_ptr<Scratch>> scratch;   // by (device, stream)
+};
+
 struct ed_crs {
     int64_t n = 0, nnz = 0;
     int upper = 0;
@@ -231,6 +252,10 @@ struct ed_crs {
     // -1 not made (upper storage, short rows, or not enough free memory)
     mutable std::unique_ptr<ed_sell> sell;
     mutable int sell_state = 0;
+    // the integer-pipe product's fixed-point values (full storage, rows of
+    // 96 and more elements on average), same states
+    mutable std::unique_ptr<ed_fixq> fixq;
+    mutable int fix_state = 0;
     int product_kernel = 0;   // 0: chosen by shape; else an ed_spmv_kernel id for every product
 };
 
@@ -291,7 +316,8 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st);
 // capture their cycles.
 void spmv_prepare(const ed_crs& a, cudaStream_t st);
 // kernel 0: as spmv; 1: row lanes k_spmv_full<8,4>; 2, 3: shared reduction k_spmv_rows<8,4,2>,
-// <8,2,2>; 4, 5: sliced ELL k_spmv_sell<16>, <8> (full storage)
+// <8,2,2>; 4, 5: sliced ELL k_spmv_sell<16>, <8>; 6: fixed-point integer rows k_spmv_fix<8,4>
+// (full storage)
 void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st);
 double measure_dfma_rate(int iters, int blocks_per_sm);
 void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const double* x, double* y,

@@ -31,6 +31,7 @@ namespace {
 
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
+__device__ __forceinline__ int2 ld_stream(const int2* p) { return __ldcs(p); }
 
 // Byte offset of the low-word table in k_hv_matfree_c's shared memory (after
 // nw weights and 2K pair offsets, 16-byte aligned).
@@ -168,6 +169,235 @@ __global__ void __launch_bounds__(256) k_spmv_rows(const int64_t* __restrict__ r
         constexpr int kButterflyMask = G / R - 1;
         const int64_t r = g0 + t;
         if ((sub & kButterflyMask) == 0 && r < n) y[r] = w;
+    }
+}
+
+// ------------------------------------------------------------ fixed point
+//
+// The integer-pipe product.  GB300 issues about 0.53e12 FP64 FMA/s but far
+// more 32-bit integer multiply-adds, so the one-level product runs in exact
+// fixed-point integer arithmetic and leaves the FP64 pipe alone:
+//  - the values and x are rounded to 58-bit fixed point relative to the
+//    largest binary exponent of each (a = A 2^(ea-1080), x = X 2^(ex-1080),
+//    |A|, |X| < 2^58) and split into 30-bit limbs, A = ah 2^30 + al with
+//    0 <= al < 2^30;
+//  - each element's A X = ah xh 2^60 + (ah xl + al xh) 2^30 + al xl takes
+//    four 32x32->64-bit multiply-adds (mad.wide.s32) into int64 partial sums
+//    of eight elements, which are added into the lane's int128 row sum;
+//  - the lanes' sums are added (exact: a row of at most 2048 elements sums
+//    to less than 2^127) and rounded once to FP64, to nearest:
+//    y = round(S 2^(ea+ex-2160)).
+// y therefore does not depend on the element order or the lane split, and
+// it differs from the exact product of the FP64 inputs only by the
+// fixed-point rounding of the inputs (half a unit of 2^-58 of the largest |a|
+// and |x|) and the final rounding.  A non-finite entry of x makes every
+// entry of y NaN; matrices with a non-finite value or a row longer than 2048
+// elements keep the FP64 kernels.
+
+constexpr int kFixPartPerSm = 2;     // blocks of the exponent pass per SM
+constexpr int kFixMaxRow = 2048;     // |S| < 2048 * 2^116 = 2^127
+
+// Biased exponent field, 1 for zeros and subnormals (their scale).
+__device__ __forceinline__ int fix_exp(double v)
+{
+    const int e = (int)(((uint64_t)__double_as_longlong(v) >> 52) & 0x7FF);
+    return e ? e : 1;
+}
+
+// The limb pair (A mod 2^30, floor(A / 2^30)) of A = round(v 2^(1080 - E)),
+// rounded to nearest with ties away from zero, as one 64-bit word (limb
+// A mod 2^30 in the low half).  |v| < 2^(E - 1022) gives |A| < 2^58.
+__device__ __forceinline__ int64_t fix_pair(double v, int E)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    const uint64_t m = (b & ((1ull << 52) - 1)) | (e ? (1ull << 52) : 0ull);
+    const int sh = (e ? e : 1) - E + 5;   // <= 5: m 2^sh < 2^58
+    uint64_t q = 0;
+    if (sh >= 0) q = m << sh;
+    else if (sh > -64) q = (m + (1ull << (-sh - 1))) >> -sh;
+    const int64_t A = (b >> 63) ? -(int64_t)q : (int64_t)q;
+    const uint32_t lo = (uint32_t)(A & ((1 << 30) - 1));
+    const uint32_t hi = (uint32_t)(int32_t)(A >> 30);
+    return (int64_t)(((uint64_t)hi << 32) | lo);
+}
+
+// Per-block maxima of fix_exp over v[0, n) into part[blockIdx.x].
+__global__ void __launch_bounds__(256) k_fix_exp(const double* __restrict__ v, int64_t n, int* __restrict__ part)
+{
+    __shared__ int sm[8];
+    int m = 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, fix_exp(v[i]));
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int r = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = max(r, sm[w]);
+        part[blockIdx.x] = r;
+    }
+}
+
+// q[i] = fix_pair(v[i], E) with E the maximum of part[0, nparts); block 0
+// also stores E in part[nparts] for the product.
+__global__ void __launch_bounds__(256) k_fix_conv(const double* __restrict__ v, int64_t n, int* __restrict__ part,
+                                                  int nparts, int64_t* __restrict__ q)
+{
+    __shared__ int sE;
+    if (threadIdx.x < 32) {
+        int m = 1;
+        for (int i = threadIdx.x; i < nparts; i += 32) m = max(m, part[i]);
+        m = __reduce_max_sync(0xffffffffu, m);
+        if (threadIdx.x == 0) {
+            sE = m;
+            if (blockIdx.x == 0) part[nparts] = m;
+        }
+    }
+    __syncthreads();
+    const int E = sE;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        q[i] = fix_pair(v[i], E);
+}
+
+__device__ __forceinline__ long long mul_wide(int a, int b)
+{
+    long long d;
+    asm("mul.wide.s32 %0, %1, %2;" : "=l"(d) : "r"(a), "r"(b));
+    return d;
+}
+
+__device__ __forceinline__ long long mad_wide(int a, int b, long long c)
+{
+    long long d;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
+}
+
+// +-(w1 2^64 + w0) 2^sc rounded to the nearest double (ties to even), by
+// integer operations only; subnormal and infinite results included.
+__device__ __forceinline__ double round_u128(unsigned long long w1, unsigned long long w0, bool neg, int sc)
+{
+    int nb;                  // bit length of the magnitude
+    unsigned long long t;    // its 64 leading bits, the first at bit 63
+    bool st;                 // a set bit below them
+    if (w1) {
+        const int z = __clzll((long long)w1);
+        nb = 128 - z;
+        t = z ? (w1 << z) | (w0 >> (64 - z)) : w1;
+        st = (z ? (w0 << z) : w0) != 0;
+    } else if (w0) {
+        const int z = __clzll((long long)w0);
+        nb = 64 - z;
+        t = w0 << z;
+        st = false;
+    } else {
+        return 0.0;
+    }
+    const unsigned long long sign = neg ? (1ull << 63) : 0ull;
+    const int eb = nb + sc + 1022;   // biased exponent of a normal result
+    if (eb >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+    const int drop = eb >= 1 ? 11 : 12 - eb;   // bits of t below the last place kept
+    unsigned long long mant, rnd, stk;
+    if (drop <= 63) {
+        mant = t >> drop;
+        rnd = (t >> (drop - 1)) & 1ull;
+        stk = ((t & ((1ull << (drop - 1)) - 1ull)) != 0 || st) ? 1ull : 0ull;
+    } else if (drop == 64) {
+        mant = 0;
+        rnd = t >> 63;
+        stk = ((t << 1) != 0 || st) ? 1ull : 0ull;
+    } else {
+        mant = 0;
+        rnd = 0;
+        stk = 1;
+    }
+    mant += rnd & (stk | (mant & 1ull));
+    // a carry out of the 53 bits moves into the exponent field by itself
+    const unsigned long long bits = eb >= 1 ? ((unsigned long long)(eb - 1) << 52) + mant : mant;
+    return __longlong_as_double((long long)(sign | bits));
+}
+
+// round(S 2^sc) for a two's complement S.
+__device__ __forceinline__ double round_i128(__int128 S, int sc)
+{
+    const bool neg = S < 0;
+    const unsigned __int128 M = neg ? (unsigned __int128)(-S) : (unsigned __int128)S;
+    return round_u128((unsigned long long)(M >> 64), (unsigned long long)M, neg, sc);
+}
+
+// The one-level row kernel on the fixed-point values: G lanes per row, each
+// lane one element in G, U elements' loads issued ahead of their
+// multiply-adds, the lanes' int128 sums added and rounded by the first lane.
+// xexp points at the exponent bound of x (k_fix_conv).
+template <int G, int U, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_spmv_fix(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                  const int2* __restrict__ aq, const int2* __restrict__ xq,
+                                                  const int* __restrict__ xexp, int ea, double* __restrict__ y,
+                                                  int64_t n)
+{
+    // per element |ah xh| <= 2^56, |ah xl + al xh| < 2^59, 0 <= al xl < 2^60
+    static_assert(U >= 1 && U <= 8, "eight elements' products fit the int64 partial sums");
+    constexpr int RPW = 32 / G;
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int ex = __ldg(xexp);
+    const bool finite = ex < 2047;
+    const int sc = ea + ex - 2160;
+    for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {   // warp-uniform loop
+        const int64_t r = rb + grp;
+        const bool valid = r < n;
+        const int64_t s = valid ? rowptr[r] : 0;
+        const int len = valid ? (int)(rowptr[r + 1] - s) : 0;
+        const int2* ap = aq + s;
+        const int32_t* cp = col + s;
+        __int128 acc = 0;
+        for (int j0 = sub; j0 < len; j0 += G * U) {
+            int2 av[U];
+            int cc[U];
+            if (j0 + (U - 1) * G < len) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    av[u] = ld_stream(ap + j0 + u * G);
+                    cc[u] = ld_stream(cp + j0 + u * G);
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const bool in = j0 + u * G < len;
+                    av[u] = in ? ld_stream(ap + j0 + u * G) : make_int2(0, 0);
+                    cc[u] = in ? ld_stream(cp + j0 + u * G) : 0;
+                }
+            }
+            int2 xv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) xv[u] = __ldg(xq + cc[u]);
+            long long p2 = mul_wide(av[0].y, xv[0].y);
+            long long p1 = mad_wide(av[0].x, xv[0].y, mul_wide(av[0].y, xv[0].x));
+            long long p0 = mul_wide(av[0].x, xv[0].x);
+#pragma unroll
+            for (int u = 1; u < U; ++u) {
+                p2 = mad_wide(av[u].y, xv[u].y, p2);
+                p1 = mad_wide(av[u].y, xv[u].x, p1);
+                p1 = mad_wide(av[u].x, xv[u].y, p1);
+                p0 = mad_wide(av[u].x, xv[u].x, p0);
+            }
+            acc += ((__int128)p2 << 60) + ((__int128)p1 << 30) + (__int128)p0;
+        }
+        long long hi = (long long)(acc >> 64);
+        unsigned long long lo = (unsigned long long)acc;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            const long long ohi = __shfl_xor_sync(0xffffffffu, hi, o, G);
+            const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, o, G);
+            const unsigned long long t = lo + olo;
+            hi += ohi + (t < lo ? 1 : 0);
+            lo = t;
+        }
+        if (valid && sub == 0)
+            y[r] = finite ? round_i128(((__int128)hi << 64) | (__int128)lo, sc)
+                          : __longlong_as_double(0x7FF8000000000000ll);
     }
 }
 
@@ -507,13 +737,110 @@ void sell_launch(const ed_crs& a, const double* x, double* y, cudaStream_t st)
 }  // namespace
 
 // Full-storage matrices of at least kSellMinRows rows and fewer than
-// kSellMaxAvg elements a row on average get the sliced-ELL copy.
+// kSellMaxAvg elements a row on average get the sliced-ELL copy; the others
+// of full storage (the one-level sectors) the fixed-point copy.
 constexpr int64_t kSellMinRows = 4096;
 constexpr double kSellMaxAvg = 96.0;
 
+namespace {
+
+int fix_parts() { return sms() * kFixPartPerSm; }
+
+// The fixed-point copy of the values (declined when it would take more than
+// half of the free device memory, or when a value is not finite).
+void fix_build(const ed_crs& a, cudaStream_t st)
+{
+    size_t free_b = 0, total_b = 0;
+    ED_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = (size_t)(a.nnz + kCrsPad) * 8 + (size_t)a.n * 8;
+    if (need > free_b / 2 || a.max_row > kFixMaxRow) {
+        a.fix_state = -1;
+        return;
+    }
+    auto fq = std::make_unique<ed_fixq>();
+    const int P = fix_parts();
+    DevBuf<int> part((size_t)P + 1);
+    fq->val.alloc((size_t)(a.nnz + kCrsPad));
+    ED_CUDA(cudaMemsetAsync(fq->val.p + a.nnz, 0, (size_t)kCrsPad * 8, st));
+    k_fix_exp<<<P, 256, 0, st>>>(a.val.p, a.nnz, part.p);
+    count_launch();
+    k_fix_conv<<<sms() * 8, 256, 0, st>>>(a.val.p, a.nnz, part.p, P, fq->val.p);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+    int ea = 1;
+    ED_CUDA(cudaMemcpyAsync(&ea, part.p + P, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    if (ea >= 2047) {
+        a.fix_state = -1;
+        return;
+    }
+    fq->ea = ea;
+    a.fixq = std::move(fq);
+    a.fix_state = 1;
+}
+
+// The stream's scratch for x's fixed-point copy, made on first use outside a
+// capture; nullptr while capturing without one.
+ed_fixq::Scratch* fix_scratch(const ed_crs& a, cudaStream_t st)
+{
+    ed_fixq& f = *a.fixq;
+    int dev = 0;
+    ED_CUDA(cudaGetDevice(&dev));
+    // the legacy and per-thread streams have the same handle on every device
+    const std::pair<int, cudaStream_t> key(dev, st);
+    std::lock_guard<std::mutex> lk(f.mu);
+    auto it = f.scratch.find(key);
+    if (it != f.scratch.end()) return it->second.get();
+    if (stream_capturing(st)) return nullptr;
+    auto sc = std::make_unique<ed_fixq::Scratch>();
+    sc->xq.alloc((size_t)a.n);
+    sc->part.alloc((size_t)fix_parts() + 1);
+    return f.scratch.emplace(key, std::move(sc)).first->second.get();
+}
+
+bool fix_shape(const ed_crs& a)
+{
+    return !a.upper && a.n > 0 && (double)a.nnz >= kSellMaxAvg * (double)a.n;
+}
+
+// The fixed-point copy and this stream's scratch, made when missing and not
+// capturing; false when either is not there.
+bool fix_ready(const ed_crs& a, cudaStream_t st)
+{
+    if (a.fix_state == 0 && !stream_capturing(st)) fix_build(a, st);
+    return a.fix_state == 1 && fix_scratch(a, st) != nullptr;
+}
+
+void fix_launch(const ed_crs& a, const double* x, double* y, cudaStream_t st)
+{
+    const ed_fixq& f = *a.fixq;
+    ed_fixq::Scratch& sc = *fix_scratch(a, st);
+    const int P = fix_parts();
+    k_fix_exp<<<P, 256, 0, st>>>(x, a.n, sc.part.p);
+    count_launch();
+    k_fix_conv<<<sms() * 4, 256, 0, st>>>(x, a.n, sc.part.p, P, sc.xq.p);
+    count_launch();
+    // 8 lanes a row, 8 loads ahead, at most 64 registers: four CTAs per SM
+    // (GB300, N=11 2S=30 with the two conversion passes: 0.772 ms; 71
+    // registers and three CTAs 0.877; 4 loads ahead 0.862; 48 or 40
+    // registers with spills 0.88-1.03)
+    k_spmv_fix<8, 8, 4><<<sms() * 8, 256, 0, st>>>(a.rowptr.p, a.col.p, reinterpret_cast<const int2*>(f.val.p),
+                                                   reinterpret_cast<const int2*>(sc.xq.p), sc.part.p + P, f.ea, y,
+                                                   a.n);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
 void spmv_prepare(const ed_crs& a, cudaStream_t st)
 {
-    if (a.product_kernel >= 4 && a.sell_state == 0 && a.n > 0 && !stream_capturing(st)) {
+    if (a.n > 0 && !stream_capturing(st) &&
+        (a.product_kernel == 6 || (a.product_kernel == 0 && fix_shape(a)))) {
+        fix_ready(a, st);
+    }
+    if ((a.product_kernel == 4 || a.product_kernel == 5) && a.sell_state == 0 && a.n > 0 &&
+        !stream_capturing(st)) {
         sell_build(a, st);
         return;
     }
@@ -530,14 +857,21 @@ void spmv_prepare(const ed_crs& a, cudaStream_t st)
 void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st)
 {
     if (a.n == 0) return;
-    ED_REQUIRE(kernel >= 0 && kernel <= 5, ED_ERR_ARG,
+    ED_REQUIRE(kernel >= 0 && kernel <= 6, ED_ERR_ARG,
                "kernel: 0 (chosen by shape), 1 (row lanes 8x4), 2 / 3 (shared reduction 8x4x2 / 8x2x2), "
-               "4 / 5 (sliced ELL, 16 / 8 loads ahead)");
+               "4 / 5 (sliced ELL, 16 / 8 loads ahead), 6 (fixed-point integer rows 8x4)");
     if (kernel == 0) {
         spmv(a, x, y, st);
         return;
     }
-    ED_REQUIRE(!a.upper, ED_ERR_ARG, "the row and sliced-ELL kernels take full storage");
+    ED_REQUIRE(!a.upper, ED_ERR_ARG, "the row, sliced-ELL and fixed-point kernels take full storage");
+    if (kernel == 6) {
+        ED_REQUIRE(fix_ready(a, st), ED_ERR_RANGE,
+                   "no fixed-point copy (a non-finite value, a row of more than 2048 elements, not enough free "
+                   "device memory, or a first product on this stream inside a capture)");
+        fix_launch(a, x, y, st);
+        return;
+    }
     const int threads = 256;
     const int grid = sms() * 8;
     const int64_t* rp = a.rowptr.p;
@@ -582,9 +916,15 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
         // 0.828-0.841 for k_spmv_full<8,4> and 0.90 for sliced ELL with 16
         // loads ahead; N=10 2S=27: 0.1219-0.1226 against 0.1219-0.1232 and
         // 0.14); also the short-row sectors below kSellMinRows rows
-        if (avg >= kSellMaxAvg)
+        if (avg >= kSellMaxAvg) {
+            if (fix_ready(a, st)) {
+                fix_launch(a, x, y, st);
+                return;
+            }
             k_spmv_rows<8, 4, 2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
-        else k_spmv_rows<8, 2, 2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        } else {
+            k_spmv_rows<8, 2, 2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
+        }
     } else if (!a.upper) {
         k_spmv_full<2><<<grid, threads, 0, st>>>(a.rowptr.p, a.col.p, a.val.p, x, y, a.n);
     } else {

@@ -167,7 +167,12 @@ ed_status ed_ham_diagonal(const ed_basis* b, const ed_terms* t, double* diag_dev
 
 /* y = H x from a stored CRS (either storage).  Device vectors of n doubles.
  * Replaces MatrixVectorFunction::Simple (hamiltonians/matrix_vector_routines.hpp:94-104)
- * -> SymmetricMatrixVectorMultiply (utilities/mathematics/sparse_linear_algebra.hpp:78-168). */
+ * -> SymmetricMatrixVectorMultiply (utilities/mathematics/sparse_linear_algebra.hpp:78-168).
+ * Full storage with 96 and more elements a row on average (the one-level
+ * sectors) uses the fixed-point integer kernel (kernel 6 below): the first
+ * product makes a fixed-point copy of the values (8 bytes an element) and,
+ * per stream, an n-element scratch for x; products of one matrix on one
+ * stream must not overlap (they share that stream's scratch). */
 ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream stream);
 
 /* The same product with a chosen kernel of the full storage, for measuring
@@ -176,8 +181,16 @@ ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream
  * kernel (8 lanes take two consecutive rows and reduce-scatter their sums; 4 /
  * 2 loads ahead), 4 / 5 the sliced-ELL kernel (one lane a row over a
  * length-sorted, chunk-transposed copy made on first use; 16 / 8 loads
- * ahead).  ED_ERR_ARG for 1-5 on upper-triangle storage; ED_ERR_RANGE for 4-5
- * when the copy does not fit in half the free device memory. */
+ * ahead), 6 the fixed-point integer kernel (8 lanes a row, 4 loads ahead):
+ * values and x rounded to 58-bit fixed point relative to their largest
+ * binary exponents, each row's sum formed exactly in integers and rounded
+ * once to FP64, so y does not depend on the element order; a non-finite
+ * entry of x gives NaN in every entry of y.  ED_ERR_ARG for 1-6 on
+ * upper-triangle storage; ED_ERR_RANGE for 4-6 when the copy does not fit
+ * in half the free device memory, for 6 also when a value is not finite, a
+ * row has more than 2048 elements, or the stream's first product is inside
+ * a capture.  The values must not change after the first product (the
+ * copies are made once). */
 ed_status ed_spmv_kernel(const ed_crs* a, int kernel, const double* x_dev, double* y_dev, ed_stream stream);
 
 /* Use kernel (an ed_spmv_kernel id; 0 restores the choice by shape) for every
