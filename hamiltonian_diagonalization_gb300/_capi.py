@@ -113,6 +113,7 @@ _SIGS = {
     "ed_spmv_kernel": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "ed_fp64_fma_rate": (c_int, [c_int, c_int, P(c_double)]),
     "ed_crs_set_product_kernel": (c_int, [c_void_p, c_int]),
+    "ed_spmv_staged_wait_test": (c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_longlong, ctypes.POINTER(c_int)]),
     "ed_hv_matfree": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "ed_op_from_crs": (c_int, [c_void_p, P(c_void_p)]),
     "ed_op_matfree": (c_int, [c_void_p, c_void_p, P(c_void_p)]),

@@ -387,12 +387,24 @@ ed_status ed_spmv_kernel(const ed_crs* a, int kernel, const double* x_dev, doubl
     });
 }
 
+ed_status ed_spmv_staged_wait_test(const ed_crs* a, const double* x_dev, double* y_dev, long long wait_cycles,
+                                   int* timeouts)
+{
+    return guarded([&] {
+        ED_NONNULL(a);
+        ED_NONNULL(x_dev);
+        ED_NONNULL(y_dev);
+        ED_NONNULL(timeouts);
+        *timeouts = spmv_staged_wait_test(*a, x_dev, y_dev, wait_cycles, nullptr);
+    });
+}
+
 ed_status ed_crs_set_product_kernel(ed_crs* a, int kernel)
 {
     return guarded([&] {
         ED_NONNULL(a);
-        ED_REQUIRE(kernel >= 0 && kernel <= 6, ED_ERR_ARG, "kernel: 0 (chosen by shape) or 1-6 (ed_spmv_kernel)");
-        ED_REQUIRE(kernel == 0 || !a->upper, ED_ERR_ARG, "kernels 1-6 take full storage");
+        ED_REQUIRE(kernel >= 0 && kernel <= 7, ED_ERR_ARG, "kernel: 0 (chosen by shape) or 1-7 (ed_spmv_kernel)");
+        ED_REQUIRE(kernel == 0 || !a->upper, ED_ERR_ARG, "kernels 1-7 take full storage");
         a->product_kernel = kernel;
     });
 }

@@ -232,6 +232,10 @@ struct ed_sell {
 struct ed_fixq {
     int ea = 1;
     edgb::DevBuf<int64_t> val;   // nnz + kCrsPad pairs (zero pairs after the last row)
+    // the staged kernel's ring: stage capacity (elements) and stage count,
+    // 0 when it does not fit; err counts its waits that ran out
+    int stage_elems = 0, stages = 0;
+    edgb::DevBuf<int> err;
     struct Scratch {
         edgb::DevBuf<int64_t> xq;
         edgb::DevBuf<int> part;
@@ -316,9 +320,15 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st);
 // capture their cycles.
 void spmv_prepare(const ed_crs& a, cudaStream_t st);
 // kernel 0: as spmv; 1: row lanes k_spmv_full<8,4>; 2, 3: shared reduction k_spmv_rows<8,4,2>,
-// <8,2,2>; 4, 5: sliced ELL k_spmv_sell<16>, <8>; 6: fixed-point integer rows k_spmv_fix<8,4>
-// (full storage)
+// <8,2,2>; 4, 5: sliced ELL k_spmv_sell<16>, <8>; 6: fixed-point integer rows k_spmv_fix<8,8>;
+// 7: the same with the rows staged in shared memory by bulk copies, k_spmv_fix_staged (full storage)
 void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st);
+// Throws when a staged product's wait ran out since the last call (reads a
+// device word: synchronises the stream).
+void spmv_check(const ed_crs& a, cudaStream_t st);
+// The staged kernel with stage 0 never filled and every wait limited to
+// cycles: returns the number of waits that ran out (reset afterwards).
+int spmv_staged_wait_test(const ed_crs& a, const double* x, double* y, long long cycles, cudaStream_t st);
 double measure_dfma_rate(int iters, int blocks_per_sm);
 void hv_matfree(const ed_basis& b, const ed_terms& t, const double* diag, const double* x, double* y,
                 cudaStream_t st);

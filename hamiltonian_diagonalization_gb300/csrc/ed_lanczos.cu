@@ -400,6 +400,13 @@ void op_prepare(const ed_op& op, cudaStream_t st)
     else if (op.kind == ed_op::DEFLATED && op.inner) op_prepare(*op.inner, st);
 }
 
+// Throws when one of the operator's products ran out of a bounded wait.
+void op_check(const ed_op& op, cudaStream_t st)
+{
+    if (op.kind == ed_op::CRS) spmv_check(*op.crs, st);
+    else if (op.kind == ed_op::DEFLATED && op.inner) op_check(*op.inner, st);
+}
+
 void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st)
 {
     switch (op.kind) {
@@ -836,6 +843,7 @@ void lanczos_once(const ed_op& op, const ed_lanczos_params& p, const double* v0_
         inf.converged = nc;
     }
     ED_CUDA(cudaStreamSynchronize(st));
+    op_check(op, st);
     inf.spmv_seconds = spmv_ms * 1e-3;
     inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (info) *info = inf;

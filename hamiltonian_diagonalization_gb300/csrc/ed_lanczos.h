@@ -88,6 +88,8 @@ void rotate_basis(const double* V, int64_t n, int m, const double* Y_host, int l
 void op_apply(const ed_op& op, const double* x, double* y, cudaStream_t st);
 // once-per-operator work of the product, before a solver captures its cycles
 void op_prepare(const ed_op& op, cudaStream_t st);
+// throws when one of the operator's products ran out of a bounded wait
+void op_check(const ed_op& op, cudaStream_t st);
 // Lowest p.nev eigenpairs; v0_dev may be null; evecs_dev (n*nev) may be null.
 void lanczos_solve(const ed_op& op, const ed_lanczos_params& p, const double* v0_dev, double* evals_host,
                    double* evecs_dev, ed_solve_info* info, cudaStream_t st);

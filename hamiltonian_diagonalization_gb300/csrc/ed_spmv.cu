@@ -20,6 +20,8 @@
 // Column and value streams are read once with evict-first loads so that x
 // stays resident in L2.
 #include <algorithm>
+#include <cmath>
+#include <string>
 #include <map>
 #include <memory>
 
@@ -401,6 +403,289 @@ __global__ void __launch_bounds__(256, MINB) k_spmv_fix(const int64_t* __restric
     }
 }
 
+// ------------------------------------------------ staged fixed-point product
+//
+// k_spmv_fix's arithmetic with the rows' values and columns streamed into
+// shared memory by bulk copies (cp.async.bulk, completion counted on an
+// mbarrier), so that a warp waits only for its gathers of x, not for the
+// DRAM stream in front of them.  Measured on GB300 it is the slower kernel
+// (N=11 2S=30: 1.71 ms against 0.77): shared memory holds three stages of
+// 16 rows, and with one warp a row the per-row reduction and rounding take
+// four times k_spmv_fix's instructions (8 lanes a row, four rows a warp),
+// which makes it issue-bound; it is kept as the bulk-copy path, selected by
+// ed_spmv_kernel 7.  One producer warp keeps a ring of stages
+// filled, each stage the 16 consecutive rows of one row block (row blocks
+// round-robin over the CTAs, one CTA per SM); 16 consumer warps take one row
+// of each stage, 32 lanes on it, and release the slot on a second mbarrier.
+// A stage larger than a slot is read from global memory instead.  Every
+// wait is bounded (kFixWaitCycles): when one runs out, the CTA stops, the
+// row of each waiting warp is set to NaN, the error word is incremented and
+// the producer waits (bounded again) for the copies it issued.
+
+constexpr int kStageRows = 16;
+constexpr int kStageConsumers = 16;                          // warps: one row of a stage each
+constexpr int kStageThreads = (kStageConsumers + 1) * 32;    // and the producer warp
+constexpr int kStageMaxSlots = 4;
+constexpr int kStageMetaStride = 20;                         // [17], [18]: the A and C copy origins
+constexpr int kStageHeader = 128 + kStageMaxSlots * kStageMetaStride * 8;   // barriers, abort word, meta
+constexpr long long kFixWaitCycles = 1ll << 31;             // about a second
+
+__host__ __device__ constexpr int fix_acap(int se) { return (se + 2 + 15) / 16 * 16; }
+__host__ __device__ constexpr int fix_ccap(int se) { return (se + 8 + 31) / 32 * 32; }
+__host__ __device__ constexpr size_t fix_slot_bytes(int se) { return (size_t)fix_acap(se) * 8 + (size_t)fix_ccap(se) * 4; }
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t a)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+
+// Whether the barrier's phase of the given parity has completed; a thread
+// whose phase is pending is suspended until it completes or about
+// kFixSuspendNs pass, so that waiting warps leave the issue slots to the
+// working ones.
+constexpr uint32_t kFixSuspendNs = 20000;
+
+__device__ __forceinline__ bool mbar_test(uint32_t a, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity), "r"(kFixSuspendNs)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the completion of the barrier's phase of the given parity, for
+// at most limit clock cycles.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, long long limit)
+{
+    if (mbar_test(a, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_test(a, parity))
+        if (clock64() - t0 > limit) return false;
+    return true;
+}
+
+__device__ __forceinline__ uint64_t evict_first_policy()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// bytes (a multiple of 16) from global src to shared dst, both 16-byte
+// aligned, counted on mbarrier mb; evict-first in L2 so that x stays.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mb, uint64_t pol)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(mb), "l"(pol)
+        : "memory");
+}
+
+// One row's exact sum, this lane's share: elements lane, lane + 32, ... of
+// the row's len (A pairs at ap, columns at cp), U gathers of x ahead.
+template <int U, bool GLOBAL>
+__device__ __forceinline__ __int128 fix_row(const int2* ap, const int32_t* cp, int len, int lane,
+                                            const int2* __restrict__ xq)
+{
+    __int128 acc = 0;
+    for (int j0 = lane; j0 < len; j0 += 32 * U) {
+        int2 av[U];
+        int cc[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = j0 + 32 * u;
+            const bool in = j < len;
+            if (GLOBAL) {
+                av[u] = in ? ld_stream(ap + j) : make_int2(0, 0);
+                cc[u] = in ? ld_stream(cp + j) : 0;
+            } else {
+                av[u] = in ? ap[j] : make_int2(0, 0);
+                cc[u] = in ? cp[j] : 0;
+            }
+        }
+        int2 xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = __ldg(xq + cc[u]);
+        long long p2 = mul_wide(av[0].y, xv[0].y);
+        long long p1 = mad_wide(av[0].x, xv[0].y, mul_wide(av[0].y, xv[0].x));
+        long long p0 = mul_wide(av[0].x, xv[0].x);
+#pragma unroll
+        for (int u = 1; u < U; ++u) {
+            p2 = mad_wide(av[u].y, xv[u].y, p2);
+            p1 = mad_wide(av[u].y, xv[u].x, p1);
+            p1 = mad_wide(av[u].x, xv[u].y, p1);
+            p0 = mad_wide(av[u].x, xv[u].x, p0);
+        }
+        acc += ((__int128)p2 << 60) + ((__int128)p1 << 30) + (__int128)p0;
+    }
+    return acc;
+}
+
+// stall > 0 is the bounded-wait test: stage 0 is never filled and every wait
+// gives up after stall cycles.
+template <int U>
+__global__ void __launch_bounds__(kStageThreads, 1)
+    k_spmv_fix_staged(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                      const int2* __restrict__ aq, const int2* __restrict__ xq, const int* __restrict__ xexp, int ea,
+                      double* __restrict__ y, int64_t n, int se, int ns, int* __restrict__ err, long long stall)
+{
+    static_assert(U >= 1 && U <= 8, "eight elements' products fit the int64 partial sums");
+    extern __shared__ __align__(128) unsigned char fsm[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(fsm);
+    uint64_t* empty = full + kStageMaxSlots;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(fsm + 64);
+    int64_t* meta = reinterpret_cast<int64_t*>(fsm + 128);
+    const int acap = fix_acap(se), ccap = fix_ccap(se);
+    int2* abuf = reinterpret_cast<int2*>(fsm + kStageHeader);
+    int32_t* cbuf = reinterpret_cast<int32_t*>(fsm + kStageHeader + (size_t)ns * acap * 8);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < ns; ++i) {
+            mbar_init(smem_addr(full + i), 1);
+            mbar_init(smem_addr(empty + i), kStageConsumers);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const long long limit = stall > 0 ? stall : kFixWaitCycles;
+    const int64_t nblocks = (n + kStageRows - 1) / kStageRows;
+    if (warp == kStageConsumers) {
+        // producer.  The element bounds of 32 stages come in one load (lane l
+        // holds stage sb + l's), the next 32 stages' loaded while these are
+        // issued; the two batches alternate registers, so that no register
+        // move waits for a load in flight.
+        const uint64_t pol = evict_first_policy();
+        int last[kStageMaxSlots];   // the latest stage issued with copies into each slot, -1 none
+#pragma unroll
+        for (int i = 0; i < kStageMaxSlots; ++i) last[i] = -1;
+        auto load_batch = [&](int sb, int64_t& b0, int64_t& b1) {
+            const int64_t gl = blockIdx.x + (int64_t)(sb + lane) * gridDim.x;
+            b0 = gl < nblocks ? rowptr[gl * kStageRows] : 0;
+            b1 = gl < nblocks ? rowptr[min(gl * kStageRows + kStageRows, n)] : 0;
+        };
+        // issues stages sb .. sb + 31 from the bounds c0, c1 (loading the next
+        // batch into n0, n1); false at the last stage or when stopped
+        auto run = [&](int sb, const int64_t& c0, const int64_t& c1, int64_t& n0, int64_t& n1) -> bool {
+            load_batch(sb + 32, n0, n1);
+            for (int i = 0; i < 32; ++i) {
+                const int s = sb + i;
+                if (blockIdx.x + (int64_t)s * gridDim.x >= nblocks) return false;
+                const int slot = s % ns;
+                bool ok = s < ns || mbar_wait(smem_addr(empty + slot), (uint32_t)((s / ns - 1) & 1), limit);
+                ok = __all_sync(0xffffffffu, ok) && !*abort_flag;
+                if (!ok) {
+                    if (lane == 0) {
+                        atomicAdd(err, 1);
+                        *abort_flag = 1;
+                    }
+                    return false;
+                }
+                const int64_t k0 = __shfl_sync(0xffffffffu, c0, i), k1 = __shfl_sync(0xffffffffu, c1, i);
+                if (lane == 0) {
+                    int64_t* mt = meta + slot * kStageMetaStride;
+                    const int64_t k0a = k0 & ~1ll, k1a = (k1 + 1) & ~1ll, k0c = k0 & ~3ll, k1c = (k1 + 3) & ~3ll;
+                    const bool fits = k1a - k0a <= acap && k1c - k0c <= ccap;
+                    mt[17] = fits ? k0a : -1;
+                    mt[18] = k0c;
+                    const uint32_t fb = smem_addr(full + slot);
+                    // the slot's previous copies have landed: its stage was consumed
+                    last[slot] = -1;
+                    if (stall > 0 && s == 0) {
+                        // never filled: the consumers' waits run out
+                    } else if (fits && k1 > k0) {
+                        const uint32_t ba = (uint32_t)((k1a - k0a) * 8), bc = (uint32_t)((k1c - k0c) * 4);
+                        mbar_expect_tx(fb, ba + bc);
+                        bulk_load(smem_addr(abuf + (size_t)slot * acap), aq + k0a, ba, fb, pol);
+                        bulk_load(smem_addr(cbuf + (size_t)slot * ccap), col + k0c, bc, fb, pol);
+                        last[slot] = s;
+                    } else {
+                        mbar_arrive(fb);
+                    }
+                }
+                __syncwarp();
+            }
+            return true;
+        };
+        int64_t a0, a1, b0, b1;
+        load_batch(0, a0, a1);
+        for (int sb = 0;; sb += 64) {
+            if (!run(sb, a0, a1, b0, b1)) break;
+            if (!run(sb + 32, b0, b1, a0, a1)) break;
+        }
+        // no copy of this CTA outlives it
+        if (lane == 0)
+            for (int i = 0; i < ns; ++i)
+                if (last[i] >= 0 && !mbar_wait(smem_addr(full + i), (uint32_t)((last[i] / ns) & 1), limit))
+                    atomicAdd(err, 1);
+        return;
+    }
+    // consumers: lanes 0 and 1 hold the bounds of this warp's row in the
+    // coming stage, loaded one stage ahead
+    const int ex = __ldg(xexp);
+    const bool finite = ex < 2047;
+    const int sc = ea + ex - 2160;
+    int64_t rp = 0;
+    if (lane < 2 && blockIdx.x < nblocks) rp = rowptr[min((int64_t)blockIdx.x * kStageRows + warp + lane, n)];
+    int s = 0;
+    for (int64_t g = blockIdx.x; g < nblocks; g += gridDim.x, ++s) {
+        const int slot = s % ns;
+        const int64_t r = g * kStageRows + warp;
+        bool ok = mbar_wait(smem_addr(full + slot), (uint32_t)((s / ns) & 1), limit);
+        ok = __all_sync(0xffffffffu, ok) && !*abort_flag;
+        if (!ok) {
+            if (lane == 0) {
+                atomicAdd(err, 1);
+                *abort_flag = 1;
+                if (r < n) y[r] = __longlong_as_double(0x7FF8000000000000ll);
+            }
+            break;
+        }
+        const int64_t ks = __shfl_sync(0xffffffffu, rp, 0), ke = __shfl_sync(0xffffffffu, rp, 1);
+        const int64_t gn = g + gridDim.x;
+        if (lane < 2 && gn < nblocks) rp = rowptr[min(gn * kStageRows + warp + lane, n)];
+        const int64_t* mt = meta + slot * kStageMetaStride;
+        const int64_t k0a = mt[17], k0c = mt[18];
+        const int len = (int)(ke - ks);
+        __int128 acc;
+        if (k0a >= 0)
+            acc = fix_row<U, false>(abuf + (size_t)slot * acap + (ks - k0a), cbuf + (size_t)slot * ccap + (ks - k0c),
+                                    len, lane, xq);
+        else
+            acc = fix_row<U, true>(aq + ks, col + ks, len, lane, xq);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(empty + slot));
+        long long hi = (long long)(acc >> 64);
+        unsigned long long lo = (unsigned long long)acc;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long ohi = __shfl_xor_sync(0xffffffffu, hi, o);
+            const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, o);
+            const unsigned long long t = lo + olo;
+            hi += ohi + (t < lo ? 1 : 0);
+            lo = t;
+        }
+        if (lane == 0 && r < n)
+            y[r] = finite ? round_i128(((__int128)hi << 64) | (__int128)lo, sc)
+                          : __longlong_as_double(0x7FF8000000000000ll);
+    }
+}
+
 // ------------------------------------------------------------ sliced ELL
 
 constexpr int kSellC = 32;          // rows per chunk (one warp)
@@ -775,6 +1060,21 @@ void fix_build(const ed_crs& a, cudaStream_t st)
         return;
     }
     fq->ea = ea;
+    // the staged kernel's ring: slots of 1.5 average stages (at least two
+    // slots; up to four while the shared memory lasts)
+    int smem_max = 0, dev = 0;
+    ED_CUDA(cudaGetDevice(&dev));
+    ED_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t room = (size_t)std::max(0, smem_max - kStageHeader);
+    const double avg = (double)a.nnz / (double)std::max<int64_t>(1, a.n);
+    int se = (int)std::min(65536.0, std::max(2048.0, std::ceil(1.5 * kStageRows * avg / 32.0) * 32.0));
+    if (2 * fix_slot_bytes(se) > room) se = (int)((room / 2 - 512) / 12) / 32 * 32;
+    const int ns = se >= 1024 ? (int)std::min<size_t>(kStageMaxSlots, room / fix_slot_bytes(se)) : 0;
+    fq->stage_elems = ns >= 2 ? se : 0;
+    fq->stages = ns >= 2 ? ns : 0;
+    fq->err.alloc(1);
+    ED_CUDA(cudaMemsetAsync(fq->err.p, 0, sizeof(int), st));
+    ED_CUDA(cudaStreamSynchronize(st));
     a.fixq = std::move(fq);
     a.fix_state = 1;
 }
@@ -811,19 +1111,43 @@ bool fix_ready(const ed_crs& a, cudaStream_t st)
     return a.fix_state == 1 && fix_scratch(a, st) != nullptr;
 }
 
-void fix_launch(const ed_crs& a, const double* x, double* y, cudaStream_t st)
+// x's fixed-point copy into the stream's scratch; returns the scratch.
+ed_fixq::Scratch& fix_convert_x(const ed_crs& a, const double* x, cudaStream_t st)
 {
-    const ed_fixq& f = *a.fixq;
     ed_fixq::Scratch& sc = *fix_scratch(a, st);
     const int P = fix_parts();
     k_fix_exp<<<P, 256, 0, st>>>(x, a.n, sc.part.p);
     count_launch();
     k_fix_conv<<<sms() * 4, 256, 0, st>>>(x, a.n, sc.part.p, P, sc.xq.p);
     count_launch();
+    return sc;
+}
+
+void fix_launch_staged(const ed_crs& a, const double* x, double* y, long long stall, cudaStream_t st)
+{
+    const ed_fixq& f = *a.fixq;
+    ED_REQUIRE(f.stages >= 2, ED_ERR_RANGE, "the staged product's ring does not fit in shared memory");
+    ed_fixq::Scratch& sc = fix_convert_x(a, x, st);
+    const size_t smem = kStageHeader + (size_t)f.stages * fix_slot_bytes(f.stage_elems);
+    ED_CUDA(cudaFuncSetAttribute(k_spmv_fix_staged<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_spmv_fix_staged<8><<<sms(), kStageThreads, smem, st>>>(
+        a.rowptr.p, a.col.p, reinterpret_cast<const int2*>(f.val.p), reinterpret_cast<const int2*>(sc.xq.p),
+        sc.part.p + fix_parts(), f.ea, y, a.n, f.stage_elems, f.stages, f.err.p, stall);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+void fix_launch(const ed_crs& a, const double* x, double* y, cudaStream_t st)
+{
+    const ed_fixq& f = *a.fixq;
+    ed_fixq::Scratch& sc = fix_convert_x(a, x, st);
+    const int P = fix_parts();
     // 8 lanes a row, 8 loads ahead, at most 64 registers: four CTAs per SM
     // (GB300, N=11 2S=30 with the two conversion passes: 0.772 ms; 71
     // registers and three CTAs 0.877; 4 loads ahead 0.862; 48 or 40
-    // registers with spills 0.88-1.03)
+    // registers with spills 0.88-1.03; each warp's next row tile prefetched
+    // into L2 by cp.async.bulk.prefetch 0.99; the rows staged in shared
+    // memory by bulk copies, k_spmv_fix_staged, 1.71)
     k_spmv_fix<8, 8, 4><<<sms() * 8, 256, 0, st>>>(a.rowptr.p, a.col.p, reinterpret_cast<const int2*>(f.val.p),
                                                    reinterpret_cast<const int2*>(sc.xq.p), sc.part.p + P, f.ea, y,
                                                    a.n);
@@ -857,19 +1181,21 @@ void spmv_prepare(const ed_crs& a, cudaStream_t st)
 void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st)
 {
     if (a.n == 0) return;
-    ED_REQUIRE(kernel >= 0 && kernel <= 6, ED_ERR_ARG,
+    ED_REQUIRE(kernel >= 0 && kernel <= 7, ED_ERR_ARG,
                "kernel: 0 (chosen by shape), 1 (row lanes 8x4), 2 / 3 (shared reduction 8x4x2 / 8x2x2), "
-               "4 / 5 (sliced ELL, 16 / 8 loads ahead), 6 (fixed-point integer rows 8x4)");
+               "4 / 5 (sliced ELL, 16 / 8 loads ahead), 6 (fixed-point integer rows 8x8), 7 (the same, rows "
+               "staged in shared memory by bulk copies)");
     if (kernel == 0) {
         spmv(a, x, y, st);
         return;
     }
     ED_REQUIRE(!a.upper, ED_ERR_ARG, "the row, sliced-ELL and fixed-point kernels take full storage");
-    if (kernel == 6) {
+    if (kernel == 6 || kernel == 7) {
         ED_REQUIRE(fix_ready(a, st), ED_ERR_RANGE,
                    "no fixed-point copy (a non-finite value, a row of more than 2048 elements, not enough free "
                    "device memory, or a first product on this stream inside a capture)");
-        fix_launch(a, x, y, st);
+        if (kernel == 6) fix_launch(a, x, y, st);
+        else fix_launch_staged(a, x, y, 0, st);
         return;
     }
     const int threads = 256;
@@ -888,6 +1214,31 @@ void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaSt
     }
     count_launch();
     ED_CUDA(cudaGetLastError());
+}
+
+void spmv_check(const ed_crs& a, cudaStream_t st)
+{
+    if (a.fix_state != 1 || !a.fixq->err.p) return;
+    int e = 0;
+    ED_CUDA(cudaMemcpyAsync(&e, a.fixq->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    if (e == 0) return;
+    ED_CUDA(cudaMemsetAsync(a.fixq->err.p, 0, sizeof(int), st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    throw Error(ED_ERR_CUDA, "a staged product's copy wait ran out (" + std::to_string(e) + " waits)");
+}
+
+int spmv_staged_wait_test(const ed_crs& a, const double* x, double* y, long long cycles, cudaStream_t st)
+{
+    ED_REQUIRE(!a.upper && cycles > 0, ED_ERR_ARG, "full storage and a positive wait limit");
+    ED_REQUIRE(fix_ready(a, st), ED_ERR_RANGE, "no fixed-point copy");
+    fix_launch_staged(a, x, y, cycles, st);
+    int e = 0;
+    ED_CUDA(cudaMemcpyAsync(&e, a.fixq->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    ED_CUDA(cudaMemsetAsync(a.fixq->err.p, 0, sizeof(int), st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    return e;
 }
 
 void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)

@@ -181,21 +181,32 @@ ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream
  * kernel (8 lanes take two consecutive rows and reduce-scatter their sums; 4 /
  * 2 loads ahead), 4 / 5 the sliced-ELL kernel (one lane a row over a
  * length-sorted, chunk-transposed copy made on first use; 16 / 8 loads
- * ahead), 6 the fixed-point integer kernel (8 lanes a row, 4 loads ahead):
+ * ahead), 6 the fixed-point integer kernel (8 lanes a row, 8 loads ahead):
  * values and x rounded to 58-bit fixed point relative to their largest
  * binary exponents, each row's sum formed exactly in integers and rounded
  * once to FP64, so y does not depend on the element order; a non-finite
- * entry of x gives NaN in every entry of y.  ED_ERR_ARG for 1-6 on
- * upper-triangle storage; ED_ERR_RANGE for 4-6 when the copy does not fit
- * in half the free device memory, for 6 also when a value is not finite, a
- * row has more than 2048 elements, or the stream's first product is inside
- * a capture.  The values must not change after the first product (the
- * copies are made once). */
+ * entry of x gives NaN in every entry of y; 7 the same arithmetic with the
+ * rows' values and columns streamed into shared memory by bulk copies (a
+ * producer warp and a ring of stages of 16 rows, one consumer warp a row;
+ * the same bits as 6).  ED_ERR_ARG for 1-7 on upper-triangle storage;
+ * ED_ERR_RANGE for 4-7 when the copy does not fit in half the free device
+ * memory, for 6-7 also when a value is not finite, a row has more than 2048
+ * elements, or the stream's first product is inside a capture.  The values
+ * must not change after the first product (the copies are made once). */
 ed_status ed_spmv_kernel(const ed_crs* a, int kernel, const double* x_dev, double* y_dev, ed_stream stream);
 
 /* Use kernel (an ed_spmv_kernel id; 0 restores the choice by shape) for every
  * later product of a, including those inside the eigensolvers. */
 ed_status ed_crs_set_product_kernel(ed_crs* a, int kernel);
+
+/* A test of the staged kernel's (ed_spmv_kernel 7) bounded waits on the
+ * legacy stream: the kernel runs with its first stage never filled and every
+ * wait limited to wait_cycles SM clock cycles, so that the waits run out; it
+ * returns, leaves NaN in the rows of the waiting warps, and *timeouts is the
+ * number of waits that ran out (their error word is then reset).  The device
+ * stays usable. */
+ed_status ed_spmv_staged_wait_test(const ed_crs* a, const double* x_dev, double* y_dev, long long wait_cycles,
+                                   int* timeouts);
 
 /* Measured FP64 FMA issue rate of the current device (FMA per second): a
  * kernel of blocks_per_sm blocks per SM, 256 threads, eight independent FMA

@@ -58,7 +58,7 @@ def test_row_kernels_match_oracle(cuda, oracle, case):
     scale = np.abs(uval).max() * np.abs(x).max() * 50
     H, _ = setup(N, norb, tlz, pp)
     xd = torch.from_numpy(x).cuda()
-    for kernel in range(1, 7):
+    for kernel in range(1, 8):
         yd = torch.full_like(xd, np.nan)
         H.m_crsSparseMatrix.multiply(xd, yd, kernel)
         torch.cuda.synchronize()
@@ -144,10 +144,12 @@ def test_fixed_point_product_is_exactly_rounded(cuda, case):
     xs[1][::7] = 0.0
     for x in xs:
         xd = torch.from_numpy(x).cuda()
-        yd = torch.full_like(xd, np.nan)
-        H.m_crsSparseMatrix.multiply(xd, yd, 6)
-        torch.cuda.synchronize()
-        assert np.array_equal(yd.cpu().numpy().view(np.uint64), _fix_product(rp, col, val, x).view(np.uint64))
+        ref = _fix_product(rp, col, val, x).view(np.uint64)
+        for kernel in (6, 7):          # registers, and rows staged in shared memory
+            yd = torch.full_like(xd, np.nan)
+            H.m_crsSparseMatrix.multiply(xd, yd, kernel)
+            torch.cuda.synchronize()
+            assert np.array_equal(yd.cpu().numpy().view(np.uint64), ref), kernel
 
 
 def test_fixed_point_product_error_below_fp64(cuda):
@@ -200,3 +202,31 @@ def test_fixed_point_product_edges(cuda):
     Hu, _ = setup(10, 28, 2, ed.odd_coulomb_list(28), upper=True)
     with pytest.raises(ed.EDError):
         Hu.m_crsSparseMatrix.multiply(xd, torch.empty_like(xd), 6)
+
+
+def test_staged_product_matches_at_scale_and_wait_runs_out(cuda):
+    # the headline sector: the staged kernel gives the register kernel's bits;
+    # then its first stage is never filled and every wait is limited to about
+    # a millisecond: the waits run out, the call returns the count, and the
+    # device stays usable
+    import ctypes
+    from hamiltonian_diagonalization_gb300 import _capi as C
+    torch = cuda
+    H, _ = setup(11, 31, 0, ed.odd_coulomb_list(31))
+    n = H.GetDimension()
+    xd = torch.from_numpy(np.random.default_rng(15).uniform(-1, 1, n)).cuda()
+    y6, y7 = torch.empty_like(xd), torch.empty_like(xd)
+    H.m_crsSparseMatrix.multiply(xd, y6, 6)
+    H.m_crsSparseMatrix.multiply(xd, y7, 7)
+    torch.cuda.synchronize()
+    assert torch.equal(y6, y7)
+    yt = torch.zeros_like(xd)
+    timeouts = ctypes.c_int(0)
+    C.check(C.lib().ed_spmv_staged_wait_test(H.m_crsSparseMatrix._h, ctypes.c_void_p(xd.data_ptr()),
+                                             ctypes.c_void_p(yt.data_ptr()), 2_000_000, ctypes.byref(timeouts)))
+    assert timeouts.value >= 16                    # every consumer warp of the stalled CTA
+    assert torch.isnan(yt[:16]).all()              # the rows of the never-filled stage
+    y7b = torch.empty_like(xd)
+    H.m_crsSparseMatrix.multiply(xd, y7b, 7)
+    torch.cuda.synchronize()
+    assert torch.equal(y7b, y6)
