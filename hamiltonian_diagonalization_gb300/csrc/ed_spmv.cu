@@ -25,6 +25,7 @@
 #include <map>
 #include <memory>
 
+#include "ed_fixed.cuh"
 #include "ed_hop.cuh"
 
 namespace edgb {
@@ -199,31 +200,6 @@ __global__ void __launch_bounds__(256) k_spmv_rows(const int64_t* __restrict__ r
 constexpr int kFixPartPerSm = 2;     // blocks of the exponent pass per SM
 constexpr int kFixMaxRow = 2048;     // |S| < 2048 * 2^116 = 2^127
 
-// Biased exponent field, 1 for zeros and subnormals (their scale).
-__device__ __forceinline__ int fix_exp(double v)
-{
-    const int e = (int)(((uint64_t)__double_as_longlong(v) >> 52) & 0x7FF);
-    return e ? e : 1;
-}
-
-// The limb pair (A mod 2^30, floor(A / 2^30)) of A = round(v 2^(1080 - E)),
-// rounded to nearest with ties away from zero, as one 64-bit word (limb
-// A mod 2^30 in the low half).  |v| < 2^(E - 1022) gives |A| < 2^58.
-__device__ __forceinline__ int64_t fix_pair(double v, int E)
-{
-    const uint64_t b = (uint64_t)__double_as_longlong(v);
-    const int e = (int)((b >> 52) & 0x7FF);
-    const uint64_t m = (b & ((1ull << 52) - 1)) | (e ? (1ull << 52) : 0ull);
-    const int sh = (e ? e : 1) - E + 5;   // <= 5: m 2^sh < 2^58
-    uint64_t q = 0;
-    if (sh >= 0) q = m << sh;
-    else if (sh > -64) q = (m + (1ull << (-sh - 1))) >> -sh;
-    const int64_t A = (b >> 63) ? -(int64_t)q : (int64_t)q;
-    const uint32_t lo = (uint32_t)(A & ((1 << 30) - 1));
-    const uint32_t hi = (uint32_t)(int32_t)(A >> 30);
-    return (int64_t)(((uint64_t)hi << 32) | lo);
-}
-
 // Per-block maxima of fix_exp over v[0, n) into part[blockIdx.x].
 __global__ void __launch_bounds__(256) k_fix_exp(const double* __restrict__ v, int64_t n, int* __restrict__ part)
 {
@@ -260,72 +236,6 @@ __global__ void __launch_bounds__(256) k_fix_conv(const double* __restrict__ v, 
     const int E = sE;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         q[i] = fix_pair(v[i], E);
-}
-
-__device__ __forceinline__ long long mul_wide(int a, int b)
-{
-    long long d;
-    asm("mul.wide.s32 %0, %1, %2;" : "=l"(d) : "r"(a), "r"(b));
-    return d;
-}
-
-__device__ __forceinline__ long long mad_wide(int a, int b, long long c)
-{
-    long long d;
-    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
-    return d;
-}
-
-// +-(w1 2^64 + w0) 2^sc rounded to the nearest double (ties to even), by
-// integer operations only; subnormal and infinite results included.
-__device__ __forceinline__ double round_u128(unsigned long long w1, unsigned long long w0, bool neg, int sc)
-{
-    int nb;                  // bit length of the magnitude
-    unsigned long long t;    // its 64 leading bits, the first at bit 63
-    bool st;                 // a set bit below them
-    if (w1) {
-        const int z = __clzll((long long)w1);
-        nb = 128 - z;
-        t = z ? (w1 << z) | (w0 >> (64 - z)) : w1;
-        st = (z ? (w0 << z) : w0) != 0;
-    } else if (w0) {
-        const int z = __clzll((long long)w0);
-        nb = 64 - z;
-        t = w0 << z;
-        st = false;
-    } else {
-        return 0.0;
-    }
-    const unsigned long long sign = neg ? (1ull << 63) : 0ull;
-    const int eb = nb + sc + 1022;   // biased exponent of a normal result
-    if (eb >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
-    const int drop = eb >= 1 ? 11 : 12 - eb;   // bits of t below the last place kept
-    unsigned long long mant, rnd, stk;
-    if (drop <= 63) {
-        mant = t >> drop;
-        rnd = (t >> (drop - 1)) & 1ull;
-        stk = ((t & ((1ull << (drop - 1)) - 1ull)) != 0 || st) ? 1ull : 0ull;
-    } else if (drop == 64) {
-        mant = 0;
-        rnd = t >> 63;
-        stk = ((t << 1) != 0 || st) ? 1ull : 0ull;
-    } else {
-        mant = 0;
-        rnd = 0;
-        stk = 1;
-    }
-    mant += rnd & (stk | (mant & 1ull));
-    // a carry out of the 53 bits moves into the exponent field by itself
-    const unsigned long long bits = eb >= 1 ? ((unsigned long long)(eb - 1) << 52) + mant : mant;
-    return __longlong_as_double((long long)(sign | bits));
-}
-
-// round(S 2^sc) for a two's complement S.
-__device__ __forceinline__ double round_i128(__int128 S, int sc)
-{
-    const bool neg = S < 0;
-    const unsigned __int128 M = neg ? (unsigned __int128)(-S) : (unsigned __int128)S;
-    return round_u128((unsigned long long)(M >> 64), (unsigned long long)M, neg, sc);
 }
 
 // The one-level row kernel on the fixed-point values: G lanes per row, each
@@ -379,13 +289,8 @@ __global__ void __launch_bounds__(256, MINB) k_spmv_fix(const int64_t* __restric
             long long p1 = mad_wide(av[0].x, xv[0].y, mul_wide(av[0].y, xv[0].x));
             long long p0 = mul_wide(av[0].x, xv[0].x);
 #pragma unroll
-            for (int u = 1; u < U; ++u) {
-                p2 = mad_wide(av[u].y, xv[u].y, p2);
-                p1 = mad_wide(av[u].y, xv[u].x, p1);
-                p1 = mad_wide(av[u].x, xv[u].y, p1);
-                p0 = mad_wide(av[u].x, xv[u].x, p0);
-            }
-            acc += ((__int128)p2 << 60) + ((__int128)p1 << 30) + (__int128)p0;
+            for (int u = 1; u < U; ++u) fix_mac(av[u], xv[u], p2, p1, p0);
+            acc += fix_combine(p2, p1, p0);
         }
         long long hi = (long long)(acc >> 64);
         unsigned long long lo = (unsigned long long)acc;
@@ -525,13 +430,8 @@ __device__ __forceinline__ __int128 fix_row(const int2* ap, const int32_t* cp, i
         long long p1 = mad_wide(av[0].x, xv[0].y, mul_wide(av[0].y, xv[0].x));
         long long p0 = mul_wide(av[0].x, xv[0].x);
 #pragma unroll
-        for (int u = 1; u < U; ++u) {
-            p2 = mad_wide(av[u].y, xv[u].y, p2);
-            p1 = mad_wide(av[u].y, xv[u].x, p1);
-            p1 = mad_wide(av[u].x, xv[u].y, p1);
-            p0 = mad_wide(av[u].x, xv[u].x, p0);
-        }
-        acc += ((__int128)p2 << 60) + ((__int128)p1 << 30) + (__int128)p0;
+        for (int u = 1; u < U; ++u) fix_mac(av[u], xv[u], p2, p1, p0);
+        acc += fix_combine(p2, p1, p0);
     }
     return acc;
 }
@@ -670,19 +570,8 @@ __global__ void __launch_bounds__(kStageThreads, 1)
             acc = fix_row<U, true>(aq + ks, col + ks, len, lane, xq);
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(empty + slot));
-        long long hi = (long long)(acc >> 64);
-        unsigned long long lo = (unsigned long long)acc;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const long long ohi = __shfl_xor_sync(0xffffffffu, hi, o);
-            const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, o);
-            const unsigned long long t = lo + olo;
-            hi += ohi + (t < lo ? 1 : 0);
-            lo = t;
-        }
-        if (lane == 0 && r < n)
-            y[r] = finite ? round_i128(((__int128)hi << 64) | (__int128)lo, sc)
-                          : __longlong_as_double(0x7FF8000000000000ll);
+        acc = warp_sum_i128(acc);
+        if (lane == 0 && r < n) y[r] = finite ? round_i128(acc, sc) : __longlong_as_double(0x7FF8000000000000ll);
     }
 }
 
