@@ -98,6 +98,7 @@ _SIGS = {
     "ed_ccrs_info": (c_int, [c_void_p, P(c_i64), P(c_i64), P(c_int)]),
     "ed_ccrs_get": (c_int, [c_void_p, P(c_i64), P(ctypes.c_int32), P(c_double)]),
     "ed_cspmv": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ed_cspmv_kernel": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "ed_clanczos": (c_int, [c_void_p, P(LanczosParams), P(c_double), P(c_double), P(c_double), P(SolveInfo)]),
     "ed_ham2_build_crs": (c_int, [c_void_p, c_void_p, c_void_p, P(c_double), P(c_double), c_int, c_void_p,
                                   P(c_void_p)]),

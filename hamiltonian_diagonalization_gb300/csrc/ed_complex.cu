@@ -29,6 +29,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ed_fixed.cuh"
 #include "ed_lanczos.h"
 
 namespace edgb {
@@ -85,6 +86,87 @@ __global__ void __launch_bounds__(kCThreads) k_cspmv_full(const int64_t* __restr
             im += __shfl_xor_sync(0xffffffffu, im, o, G);
         }
         if (valid && sub == 0) y[r] = make_double2(re, im);
+    }
+}
+
+// The same product on the integer pipes in exact fixed-point arithmetic (the
+// real kernel's scheme, ed_fixed.cuh): the values' real and imaginary parts
+// share one 58-bit exponent bound ea, x's parts another ex, each element is
+// two limb pairs (16 bytes, as the FP64 value), and per element
+//   re += ar xr - ai xi,  im += ar xi + ai xr
+// takes 16 mad.wide.s32 into six int64 partial sums of U <= 4 elements,
+// flushed into the lane's two 128-bit sums; the G lanes' sums are added
+// exactly and rounded once to FP64 (rows of at most 1024 elements keep
+// |S| < 2^127).  4 DFMA an element made the FP64 kernel FP64-bound at 2.6 TB/s.
+template <int G, int U, int MINB = 1>
+__global__ void __launch_bounds__(kCThreads, MINB) k_cspmv_fix(const int64_t* __restrict__ rowptr,
+                                                         const int32_t* __restrict__ col,
+                                                         const int4* __restrict__ aq, const int4* __restrict__ xq,
+                                                         const int* __restrict__ xexp, int ea,
+                                                         double2* __restrict__ y, int64_t n)
+{
+    // per element |r2| <= 2^57, |r1| < 2^60, |r0| < 2^61 (the same for im)
+    static_assert(U >= 1 && U <= 4, "four elements' products fit the int64 partial sums");
+    constexpr int RPW = 32 / G;
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int ex = __ldg(xexp);
+    const bool finite = ex < 2047;
+    const int sc = ea + ex - 2160;
+    for (int64_t rb = warp * RPW; rb < n; rb += nwarps * RPW) {   // warp-uniform loop
+        const int64_t r = rb + grp;
+        const bool valid = r < n;
+        const int64_t s = valid ? rowptr[r] : 0;
+        const int len = valid ? (int)(rowptr[r + 1] - s) : 0;
+        const int4* ap = aq + s;
+        const int32_t* cp = col + s;
+        __int128 sre = 0, sim = 0;
+        for (int j0 = sub; j0 < len; j0 += G * U) {
+            int4 av[U];
+            int cc[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const bool in = j0 + u * G < len;
+                av[u] = in ? __ldcs(ap + j0 + u * G) : make_int4(0, 0, 0, 0);
+                cc[u] = in ? __ldcs(cp + j0 + u * G) : 0;
+            }
+            int4 xv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) xv[u] = __ldg(xq + cc[u]);
+            long long r2 = 0, r1 = 0, r0 = 0, i2 = 0, i1 = 0, i0 = 0;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int2 ar = make_int2(av[u].x, av[u].y), ai = make_int2(av[u].z, av[u].w);
+                const int2 nai = make_int2(-av[u].z, -av[u].w);
+                const int2 xr = make_int2(xv[u].x, xv[u].y), xi = make_int2(xv[u].z, xv[u].w);
+                fix_mac(ar, xr, r2, r1, r0);
+                fix_mac(nai, xi, r2, r1, r0);
+                fix_mac(ar, xi, i2, i1, i0);
+                fix_mac(ai, xr, i2, i1, i0);
+            }
+            sre += fix_combine(r2, r1, r0);
+            sim += fix_combine(i2, i1, i0);
+        }
+        long long rh = (long long)(sre >> 64), ih = (long long)(sim >> 64);
+        unsigned long long rl = (unsigned long long)sre, il = (unsigned long long)sim;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            const long long orh = __shfl_xor_sync(0xffffffffu, rh, o, G), oih = __shfl_xor_sync(0xffffffffu, ih, o, G);
+            const unsigned long long orl = __shfl_xor_sync(0xffffffffu, rl, o, G);
+            const unsigned long long oil = __shfl_xor_sync(0xffffffffu, il, o, G);
+            const unsigned long long tr = rl + orl, ti = il + oil;
+            rh += orh + (tr < rl ? 1 : 0);
+            ih += oih + (ti < il ? 1 : 0);
+            rl = tr;
+            il = ti;
+        }
+        if (valid && sub == 0) {
+            const double nan = __longlong_as_double(0x7FF8000000000000ll);
+            y[r] = finite ? make_double2(round_i128(((__int128)rh << 64) | (__int128)rl, sc),
+                                         round_i128(((__int128)ih << 64) | (__int128)il, sc))
+                          : make_double2(nan, nan);
+        }
     }
 }
 
@@ -731,9 +813,100 @@ void cterms_derive(ed_cterms& t)
 
 // ------------------------------------------------------------ product
 
-void cspmv(const ed_ccrs& a, const double* x, double* y, cudaStream_t st)
+namespace {
+
+constexpr int kCFixMaxRow = 1024;   // |S| < 1024 * 2^117 = 2^127
+
+int cfix_parts() { return csms() * 2; }
+
+bool capturing(cudaStream_t st)
 {
-    if (a.n == 0) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ED_CUDA(cudaStreamIsCapturing(st, &cs));
+    return cs != cudaStreamCaptureStatusNone;
+}
+
+// The fixed-point copy of the values (declined when it would take more than
+// half of the free device memory, for long rows or a non-finite value).
+void cfix_build(const ed_ccrs& a, cudaStream_t st)
+{
+    size_t free_b = 0, total_b = 0;
+    ED_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = (size_t)(a.nnz + kCrsPad) * 16 + (size_t)a.n * 16;
+    if (a.upper || need > free_b / 2 || a.max_row > kCFixMaxRow) {
+        a.fix_state = -1;
+        return;
+    }
+    auto fq = std::make_unique<ed_fixq>();
+    const int P = cfix_parts();
+    DevBuf<int> part((size_t)P + 1);
+    fq->val.alloc(2 * (size_t)(a.nnz + kCrsPad));
+    ED_CUDA(cudaMemsetAsync(fq->val.p + 2 * a.nnz, 0, (size_t)kCrsPad * 16, st));
+    k_fix_exp<<<P, 256, 0, st>>>(a.val.p, 2 * a.nnz, part.p);
+    count_launch();
+    k_fix_conv<<<csms() * 8, 256, 0, st>>>(a.val.p, 2 * a.nnz, part.p, P, fq->val.p);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+    int ea = 1;
+    ED_CUDA(cudaMemcpyAsync(&ea, part.p + P, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ED_CUDA(cudaStreamSynchronize(st));
+    if (ea >= 2047) {
+        a.fix_state = -1;
+        return;
+    }
+    fq->ea = ea;
+    a.fixq = std::move(fq);
+    a.fix_state = 1;
+}
+
+// This stream's scratch (x's 2n fixed-point words), made outside a capture.
+ed_fixq::Scratch* cfix_scratch(const ed_ccrs& a, cudaStream_t st)
+{
+    ed_fixq& f = *a.fixq;
+    int dev = 0;
+    ED_CUDA(cudaGetDevice(&dev));
+    const std::pair<int, cudaStream_t> key(dev, st);
+    std::lock_guard<std::mutex> lk(f.mu);
+    auto it = f.scratch.find(key);
+    if (it != f.scratch.end()) return it->second.get();
+    if (capturing(st)) return nullptr;
+    auto sc = std::make_unique<ed_fixq::Scratch>();
+    sc->xq.alloc(2 * (size_t)a.n);
+    sc->part.alloc((size_t)cfix_parts() + 1);
+    return f.scratch.emplace(key, std::move(sc)).first->second.get();
+}
+
+bool cfix_ready(const ed_ccrs& a, cudaStream_t st)
+{
+    if (a.fix_state == 0 && !capturing(st)) cfix_build(a, st);
+    return a.fix_state == 1 && cfix_scratch(a, st) != nullptr;
+}
+
+void cfix_launch(const ed_ccrs& a, const double* x, double* y, cudaStream_t st)
+{
+    const ed_fixq& f = *a.fixq;
+    ed_fixq::Scratch& sc = *cfix_scratch(a, st);
+    const int P = cfix_parts();
+    k_fix_exp<<<P, 256, 0, st>>>(x, 2 * a.n, sc.part.p);
+    count_launch();
+    k_fix_conv<<<csms() * 4, 256, 0, st>>>(x, 2 * a.n, sc.part.p, P, sc.xq.p);
+    count_launch();
+    const double avg = (double)a.nnz / (double)a.n;
+    const int4* A = reinterpret_cast<const int4*>(f.val.p);
+    const int4* X = reinterpret_cast<const int4*>(sc.xq.p);
+    double2* yy = reinterpret_cast<double2*>(y);
+    // 8 lanes a row, 4 elements ahead, at most 64 registers: four CTAs per SM
+    // (GB300, N=10 on 5x6: 1.363 ms; 92 registers and two CTAs 1.77, 2
+    // ahead 2.69, 16 lanes 2.72, 48 registers with spills 1.62; the FP64
+    // kernel 2.31)
+    if (avg >= 48) k_cspmv_fix<8, 4, 4><<<csms() * 8, kCThreads, 0, st>>>(a.rowptr.p, a.col.p, A, X, sc.part.p + P, f.ea, yy, a.n);
+    else k_cspmv_fix<4, 4, 4><<<csms() * 8, kCThreads, 0, st>>>(a.rowptr.p, a.col.p, A, X, sc.part.p + P, f.ea, yy, a.n);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
+void cspmv_fp64(const ed_ccrs& a, const double* x, double* y, cudaStream_t st)
+{
     const double avg = (double)a.nnz / (double)a.n;
     const int grid = csms() * 8;
     const double2* v = reinterpret_cast<const double2*>(a.val.p);
@@ -749,6 +922,45 @@ void cspmv(const ed_ccrs& a, const double* x, double* y, cudaStream_t st)
     }
     count_launch();
     ED_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+void cspmv_prepare(const ed_ccrs& a, cudaStream_t st)
+{
+    if (a.n > 0 && !a.upper && !capturing(st)) cfix_ready(a, st);
+}
+
+// Full storage takes the integer-pipe kernel (made on first use outside a
+// capture); the reference's upper storage and declined matrices the FP64 one.
+void cspmv(const ed_ccrs& a, const double* x, double* y, cudaStream_t st)
+{
+    if (a.n == 0) return;
+    if (!a.upper && cfix_ready(a, st)) {
+        cfix_launch(a, x, y, st);
+        return;
+    }
+    cspmv_fp64(a, x, y, st);
+}
+
+void cspmv_kernel(const ed_ccrs& a, int kernel, const double* x, double* y, cudaStream_t st)
+{
+    ED_REQUIRE(kernel >= 0 && kernel <= 2, ED_ERR_ARG,
+               "kernel: 0 (chosen by storage), 1 (FP64 rows), 2 (fixed-point integer rows)");
+    if (a.n == 0) return;
+    if (kernel == 0) {
+        cspmv(a, x, y, st);
+        return;
+    }
+    if (kernel == 1) {
+        cspmv_fp64(a, x, y, st);
+        return;
+    }
+    ED_REQUIRE(!a.upper, ED_ERR_ARG, "the fixed-point kernel takes full storage");
+    ED_REQUIRE(cfix_ready(a, st), ED_ERR_RANGE,
+               "no fixed-point copy (a non-finite value, a row of more than 1024 elements, not enough free device "
+               "memory, or a first product on this stream inside a capture)");
+    cfix_launch(a, x, y, st);
 }
 
 // ------------------------------------------------------------ eigensolver
@@ -772,6 +984,7 @@ void clanczos_solve(const ed_ccrs& a, const ed_lanczos_params& p, const double* 
     if (p.diagonal_check &&
         diagonal_spectrum(a.rowptr.p, a.col.p, a.val.p, 1, n, nev, evals, evecs_dev, info, st))
         return;
+    cspmv_prepare(a, st);   // before the cycles are captured
     if (n < 60 || n <= (int64_t)nev + 2) {
         cdense_solve(a, nev, evals, evecs_dev, &inf, st);
         inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1128,6 +1341,16 @@ extern "C" ed_status ed_ccrs_get(const ed_ccrs* a, int64_t* rowptr, int32_t* col
             ED_CUDA(cudaMemcpy(col, a->col.p, (size_t)a->nnz * 4, cudaMemcpyDeviceToHost));
             ED_CUDA(cudaMemcpy(val, a->val.p, (size_t)a->nnz * 16, cudaMemcpyDeviceToHost));
         }
+    });
+}
+
+extern "C" ed_status ed_cspmv_kernel(const ed_ccrs* a, int kernel, const double* x_dev, double* y_dev,
+                                     ed_stream stream)
+{
+    return guard([&] {
+        ED_REQUIRE(a && x_dev && y_dev, ED_ERR_ARG, "null argument");
+        ED_REQUIRE(x_dev != y_dev, ED_ERR_ARG, "x and y must be distinct");
+        cspmv_kernel(*a, kernel, x_dev, y_dev, (cudaStream_t)stream);
     });
 }
 

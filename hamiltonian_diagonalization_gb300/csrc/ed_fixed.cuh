@@ -1,5 +1,5 @@
 // Exact fixed-point arithmetic on the integer pipes, for the stored-CRS
-// products (ed_spmv.cu).
+// products (ed_spmv.cu, ed_complex.cu).
 //
 // A value v is held as A = round(v 2^(1080 - E)), |A| < 2^58 when
 // |v| < 2^(E - 1022) (E a bound on the biased exponent field), split into
@@ -103,6 +103,44 @@ __device__ __forceinline__ double round_i128(__int128 S, int sc)
     const bool neg = S < 0;
     const unsigned __int128 M = neg ? (unsigned __int128)(-S) : (unsigned __int128)S;
     return round_u128((unsigned long long)(M >> 64), (unsigned long long)M, neg, sc);
+}
+
+// Per-block maxima of fix_exp over v[0, n) into part[blockIdx.x].
+__global__ void __launch_bounds__(256) k_fix_exp(const double* __restrict__ v, int64_t n, int* __restrict__ part)
+{
+    __shared__ int sm[8];
+    int m = 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, fix_exp(v[i]));
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int r = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = max(r, sm[w]);
+        part[blockIdx.x] = r;
+    }
+}
+
+// q[i] = fix_pair(v[i], E) with E the maximum of part[0, nparts); block 0
+// also stores E in part[nparts] for the product.
+__global__ void __launch_bounds__(256) k_fix_conv(const double* __restrict__ v, int64_t n, int* __restrict__ part,
+                                                  int nparts, int64_t* __restrict__ q)
+{
+    __shared__ int sE;
+    if (threadIdx.x < 32) {
+        int m = 1;
+        for (int i = threadIdx.x; i < nparts; i += 32) m = max(m, part[i]);
+        m = __reduce_max_sync(0xffffffffu, m);
+        if (threadIdx.x == 0) {
+            sE = m;
+            if (blockIdx.x == 0) part[nparts] = m;
+        }
+    }
+    __syncthreads();
+    const int E = sE;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        q[i] = fix_pair(v[i], E);
 }
 
 // p2, p1, p0 += the three limb products of a b (weights 2^60, 2^30, 1).

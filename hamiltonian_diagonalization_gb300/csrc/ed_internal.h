@@ -297,6 +297,11 @@ struct ed_ccrs {
     edgb::DevBuf<int64_t> rowptr;
     edgb::DevBuf<int32_t> col;
     edgb::DevBuf<double> val;       // 2 * (nnz + kCrsPad)
+    // the integer-pipe product's fixed-point values (full storage): the real
+    // and imaginary parts as two limb pairs an element, 2 * (nnz + kCrsPad)
+    // words, one exponent bound; state 0 not yet tried, 1 made, -1 declined
+    mutable std::unique_ptr<ed_fixq> fixq;
+    mutable int fix_state = 0;
 };
 
 // ----------------------------------------------------- device-side entry points
@@ -305,6 +310,10 @@ void two_level_ladder(const ed_basis& b, const double* x, double* y, int dir, cu
 void cterms_derive(ed_cterms& t);
 void cham_build_crs(const ed_basis& b, const ed_cterms& t, int upper, ed_ccrs& a, cudaStream_t st);
 void cspmv(const ed_ccrs& a, const double* x, double* y, cudaStream_t st);
+// kernel 0: as cspmv; 1: the FP64 row kernel; 2: the fixed-point integer kernel (full storage)
+void cspmv_kernel(const ed_ccrs& a, int kernel, const double* x, double* y, cudaStream_t st);
+// the complex product's fixed-point copy, made before a solver captures its cycles
+void cspmv_prepare(const ed_ccrs& a, cudaStream_t st);
 void basis_build(ed_basis& b, cudaStream_t st);
 std::vector<int> basis_weights(const ed_basis& b);
 void basis_rank(const ed_basis& b, const uint64_t* words, uint64_t* idx, uint64_t m, cudaStream_t st);

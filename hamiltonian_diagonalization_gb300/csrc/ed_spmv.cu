@@ -200,44 +200,6 @@ __global__ void __launch_bounds__(256) k_spmv_rows(const int64_t* __restrict__ r
 constexpr int kFixPartPerSm = 2;     // blocks of the exponent pass per SM
 constexpr int kFixMaxRow = 2048;     // |S| < 2048 * 2^116 = 2^127
 
-// Per-block maxima of fix_exp over v[0, n) into part[blockIdx.x].
-__global__ void __launch_bounds__(256) k_fix_exp(const double* __restrict__ v, int64_t n, int* __restrict__ part)
-{
-    __shared__ int sm[8];
-    int m = 1;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        m = max(m, fix_exp(v[i]));
-    m = __reduce_max_sync(0xffffffffu, m);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int r = sm[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = max(r, sm[w]);
-        part[blockIdx.x] = r;
-    }
-}
-
-// q[i] = fix_pair(v[i], E) with E the maximum of part[0, nparts); block 0
-// also stores E in part[nparts] for the product.
-__global__ void __launch_bounds__(256) k_fix_conv(const double* __restrict__ v, int64_t n, int* __restrict__ part,
-                                                  int nparts, int64_t* __restrict__ q)
-{
-    __shared__ int sE;
-    if (threadIdx.x < 32) {
-        int m = 1;
-        for (int i = threadIdx.x; i < nparts; i += 32) m = max(m, part[i]);
-        m = __reduce_max_sync(0xffffffffu, m);
-        if (threadIdx.x == 0) {
-            sE = m;
-            if (blockIdx.x == 0) part[nparts] = m;
-        }
-    }
-    __syncthreads();
-    const int E = sE;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        q[i] = fix_pair(v[i], E);
-}
-
 // The one-level row kernel on the fixed-point values: G lanes per row, each
 // lane one element in G, U elements' loads issued ahead of their
 // multiply-adds, the lanes' int128 sums added and rounded by the first lane.

@@ -298,8 +298,9 @@ class CrsSparseMatrix:
         check(lib().ed_crs_set_product_kernel(self._h, int(kernel)))
 
     def multiply(self, x, y, kernel: int = 0, stream=None):
-        """y = A x on device vectors with a chosen product kernel
-        (ed_spmv_kernel: 0 by shape, 1 row lanes, 2-3 shared-reduction rows, 4-5 sliced ELL)."""
+        """y = A x on device vectors with a chosen product kernel (ed_spmv_kernel:
+        0 by shape, 1 row lanes, 2-3 shared-reduction rows, 4-5 sliced ELL,
+        6 fixed-point integer rows, 7 the same with bulk-copy staging)."""
         check(lib().ed_spmv_kernel(self._h, int(kernel), _dptr(x), _dptr(y), stream))
 
     def device_arrays(self):
@@ -613,6 +614,12 @@ class ComplexCrsSparseMatrix:
 
     def GetNbrNonZeros(self) -> int:
         return self.info()[1]
+
+    def multiply(self, x, y, kernel: int = 0, stream=None):
+        """y = A x on device complex vectors (float64 (re, im) pairs) with a
+        chosen kernel (ed_cspmv_kernel: 0 by storage, 1 FP64 rows, 2
+        fixed-point integer rows)."""
+        check(lib().ed_cspmv_kernel(self._h, int(kernel), _dptr(x), _dptr(y), stream))
 
     def to_host(self):
         n, nnz, _ = self.info()

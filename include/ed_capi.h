@@ -502,8 +502,23 @@ ed_status ed_ccrs_info(const ed_ccrs* a, int64_t* n, int64_t* nnz, int* upper);
 ed_status ed_ccrs_get(const ed_ccrs* a, int64_t* rowptr, int32_t* col, double* val);
 /* y = H x on device complex vectors (re, im pairs) with the reference's
  * Hermitian completion (SymmetricMatrixVectorMultiply<dcmplx>,
- * sparse_linear_algebra.hpp:143-164). */
+ * sparse_linear_algebra.hpp:143-164).  Full storage uses the fixed-point
+ * integer kernel (ed_cspmv_kernel 2): the first product makes a fixed-point
+ * copy of the values (16 bytes an element) and, per stream, a 2n-word scratch
+ * for x; products of one matrix on one stream must not overlap. */
 ed_status ed_cspmv(const ed_ccrs* a, const double* x_dev, double* y_dev, ed_stream stream);
+/* The same product with a chosen kernel, for measuring and testing them side
+ * by side: 0 as ed_cspmv, 1 the FP64 row kernel (4 FMA an element), 2 the
+ * fixed-point integer kernel for full storage: the values' and x's real and
+ * imaginary parts rounded to 58-bit fixed point relative to the largest
+ * binary exponent of each, each row's real and imaginary sums formed exactly
+ * in integers and rounded once to FP64 (y does not depend on element order; a
+ * non-finite entry of x gives NaN in every entry of y).  ED_ERR_ARG for 2 on
+ * upper-triangle storage; ED_ERR_RANGE for 2 when the copy does not fit in
+ * half the free device memory, a value is not finite, a row has more than
+ * 1024 elements, or the stream's first product is inside a capture.  Returns
+ * after enqueueing on stream. */
+ed_status ed_cspmv_kernel(const ed_ccrs* a, int kernel, const double* x_dev, double* y_dev, ed_stream stream);
 /* Lowest nev eigenpairs of the complex Hermitian matrix by thick-restart
  * Lanczos with complex Gram-Schmidt; v0_host (2n doubles) may be NULL,
  * evecs_host receives nev vectors of n complex entries (re, im pairs).

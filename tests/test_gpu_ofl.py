@@ -325,3 +325,82 @@ def test_diagonal_matrix_is_solved_from_its_diagonal(cuda, oracle):
         V = H.m_eigenvectors
         assert np.array_equal(np.abs(V).sum(axis=1), np.ones(9))              # unit vectors
         assert np.allclose(V.conj() @ V.T, np.eye(9))                          # distinct positions
+
+
+def _fix_ints(v):
+    """The fixed-point integers A = round(v 2^(1080 - E)) (nearest, ties away
+    from zero) of float64 v and E, the largest biased exponent field (>= 1)."""
+    b = np.ascontiguousarray(v, dtype=np.float64).view(np.uint64)
+    e = ((b >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
+    m = (b & np.uint64((1 << 52) - 1)).astype(np.int64) + np.where(e > 0, 1 << 52, 0)
+    ee = np.maximum(e, 1)
+    E = int(ee.max()) if len(ee) else 1
+    sh = ee - E + 5
+    q = np.zeros(len(m), dtype=np.int64)
+    pos = sh >= 0
+    q[pos] = m[pos] << sh[pos]
+    neg = (sh < 0) & (sh > -64)
+    k = -sh[neg]
+    q[neg] = (m[neg] + (np.int64(1) << (k - 1))) >> k
+    return np.where((b >> np.uint64(63)).astype(bool), -q, q), E
+
+
+def _round(S, sc):
+    return S / (1 << -sc) if sc < 0 else float(S << sc)   # one rounding to nearest even
+
+
+@pytest.mark.parametrize("case", [(5, 3, 4, 2, 3), (4, 4, 6, 1, 5)])
+def test_fixed_point_complex_product_is_exactly_rounded(cuda, oracle, case):
+    # the integer kernel against the exact integer sums of its fixed-point
+    # inputs rounded once, bit for bit; the FP64 kernel to 1e-13
+    torch = cuda
+    N, X, Y, kx, ky = case
+    T = tables(oracle, X, Y, 11)
+    model, _ = build(N, X, Y, kx, ky, T, upper=False)
+    crs = model.hamiltonian.m_crsSparseMatrix
+    rp, col, val = crs.to_host()
+    n = len(rp) - 1
+    A, ea = _fix_ints(val.view(np.float64))
+    rng = np.random.default_rng(7)
+    for x in (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n),
+              (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.exp(rng.uniform(-30, 3, n))):
+        Xq, ex = _fix_ints(x.view(np.float64))
+        ar, ai = A[0::2].tolist(), A[1::2].tolist()
+        xr, xi = Xq[0::2].tolist(), Xq[1::2].tolist()
+        sc = ea + ex - 2160
+        ref = np.empty(2 * n)
+        for i in range(n):
+            sre = sim = 0
+            for k in range(rp[i], rp[i + 1]):
+                c = col[k]
+                sre += ar[k] * xr[c] - ai[k] * xi[c]
+                sim += ar[k] * xi[c] + ai[k] * xr[c]
+            ref[2 * i], ref[2 * i + 1] = _round(sre, sc), _round(sim, sc)
+        xd = torch.from_numpy(x.view(np.float64).copy()).cuda()
+        y2, y1, y0 = torch.empty_like(xd), torch.empty_like(xd), torch.empty_like(xd)
+        crs.multiply(xd, y2, 2)
+        crs.multiply(xd, y1, 1)
+        model.hamiltonian.apply(xd, y0)
+        torch.cuda.synchronize()
+        assert np.array_equal(y2.cpu().numpy().view(np.uint64), ref.view(np.uint64))
+        assert torch.equal(y0, y2)                     # full storage uses the integer kernel
+        scale = np.abs(val).max() * np.abs(x).max() * 50
+        assert np.max(np.abs((y1 - y2).cpu().numpy())) <= 1e-13 * scale
+
+
+def test_fixed_point_complex_product_edges(cuda, oracle):
+    torch = cuda
+    T = tables(oracle, 3, 4, 11)
+    model, _ = build(5, 3, 4, 2, 3, T, upper=False)
+    crs = model.hamiltonian.m_crsSparseMatrix
+    n = crs.GetNbrRows()
+    x = np.random.default_rng(8).uniform(-1, 1, 2 * n)
+    x[5] = np.inf
+    xd = torch.from_numpy(x).cuda()
+    y = torch.zeros_like(xd)
+    crs.multiply(xd, y, 2)
+    torch.cuda.synchronize()
+    assert torch.isnan(y).all()                        # a non-finite entry of x: every entry NaN
+    up, _ = build(5, 3, 4, 2, 3, T, upper=True)
+    with pytest.raises(ed.EDError):
+        up.hamiltonian.m_crsSparseMatrix.multiply(xd, torch.empty_like(xd), 2)
