@@ -403,8 +403,8 @@ ed_status ed_crs_set_product_kernel(ed_crs* a, int kernel)
 {
     return guarded([&] {
         ED_NONNULL(a);
-        ED_REQUIRE(kernel >= 0 && kernel <= 7, ED_ERR_ARG, "kernel: 0 (chosen by shape) or 1-7 (ed_spmv_kernel)");
-        ED_REQUIRE(kernel == 0 || !a->upper, ED_ERR_ARG, "kernels 1-7 take full storage");
+        ED_REQUIRE(kernel >= 0 && kernel <= 8, ED_ERR_ARG, "kernel: 0 (chosen by shape) or 1-8 (ed_spmv_kernel)");
+        ED_REQUIRE(kernel == 0 || !a->upper, ED_ERR_ARG, "kernels 1-8 take full storage");
         a->product_kernel = kernel;
     });
 }

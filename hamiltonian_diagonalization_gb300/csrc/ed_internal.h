@@ -231,7 +231,12 @@ struct ed_sell {
 // after them, the vector's exponent bound.
 struct ed_fixq {
     int ea = 1;
-    edgb::DevBuf<int64_t> val;   // nnz + kCrsPad pairs (zero pairs after the last row)
+    // the values as limb pairs, each copy made when a kernel first needs it
+    // (state 0 not yet tried, 1 made, -1 declined for memory): val in the
+    // CRS order (nnz + kCrsPad pairs, zero pairs after the last row), sval in
+    // the sliced-ELL order (nnz_pad + kCrsPad)
+    edgb::DevBuf<int64_t> val, sval;
+    int val_state = 0, sval_state = 0;
     // the staged kernel's ring: stage capacity (elements) and stage count,
     // 0 when it does not fit; err counts its waits that ran out
     int stage_elems = 0, stages = 0;
@@ -330,7 +335,8 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st);
 void spmv_prepare(const ed_crs& a, cudaStream_t st);
 // kernel 0: as spmv; 1: row lanes k_spmv_full<8,4>; 2, 3: shared reduction k_spmv_rows<8,4,2>,
 // <8,2,2>; 4, 5: sliced ELL k_spmv_sell<16>, <8>; 6: fixed-point integer rows k_spmv_fix<8,8>;
-// 7: the same with the rows staged in shared memory by bulk copies, k_spmv_fix_staged (full storage)
+// 7: the same with the rows staged in shared memory by bulk copies, k_spmv_fix_staged; 8: fixed-point
+// sliced ELL k_spmv_sell_fix (full storage)
 void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st);
 // Throws when a staged product's wait ran out since the last call (reads a
 // device word: synchronises the stream).

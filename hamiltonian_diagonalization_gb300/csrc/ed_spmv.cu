@@ -663,6 +663,62 @@ __global__ void __launch_bounds__(256) k_spmv_sell(const int64_t* __restrict__ o
     }
 }
 
+// The sliced-ELL product on the fixed-point values (k_spmv_fix's exact
+// arithmetic, one lane a row): U elements' loads ahead, their products'
+// int64 partial sums flushed into the lane's 128-bit row sum every eight,
+// one rounding per row.  The row's sum is exact, so y is k_spmv_fix's to the
+// bit.
+template <int U, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_spmv_sell_fix(const int64_t* __restrict__ off,
+                                                            const int32_t* __restrict__ clen,
+                                                            const int32_t* __restrict__ row,
+                                                            const int32_t* __restrict__ scol,
+                                                            const int2* __restrict__ sq, const int2* __restrict__ xq,
+                                                            const int* __restrict__ xexp, int ea,
+                                                            double* __restrict__ y, int64_t nchunks)
+{
+    static_assert(U % 8 == 0, "whole groups of eight");
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int ex = __ldg(xexp);
+    const bool finite = ex < 2047;
+    const int sc = ea + ex - 2160;
+    for (int64_t c = warp; c < nchunks; c += nwarps) {
+        const int L = clen[c];
+        const int r = row[c * kSellC + lane];
+        const int2* vp = sq + off[c] + lane;
+        const int32_t* cp = scol + off[c] + lane;
+        __int128 acc = 0;
+        int j = 0;
+        for (; j + U <= L; j += U) {
+            int2 av[U];
+            int cc[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                av[u] = ld_stream(vp + (int64_t)(j + u) * kSellC);
+                cc[u] = ld_stream(cp + (int64_t)(j + u) * kSellC);
+            }
+            int2 xv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) xv[u] = __ldg(xq + cc[u]);
+#pragma unroll
+            for (int h = 0; h < U; h += 8) {
+                long long p2 = 0, p1 = 0, p0 = 0;
+#pragma unroll
+                for (int u = h; u < h + 8; ++u) fix_mac(av[u], xv[u], p2, p1, p0);
+                acc += fix_combine(p2, p1, p0);
+            }
+        }
+        for (; j < L; ++j) {
+            long long p2 = 0, p1 = 0, p0 = 0;
+            fix_mac(ld_stream(vp + (int64_t)j * kSellC), __ldg(xq + ld_stream(cp + (int64_t)j * kSellC)), p2, p1, p0);
+            acc += fix_combine(p2, p1, p0);
+        }
+        if (r >= 0) y[r] = finite ? round_i128(acc, sc) : __longlong_as_double(0x7FF8000000000000ll);
+    }
+}
+
 // Upper-triangle storage, the reference's layout: gather for the stored
 // part, scatter (atomic) for the transposed part.  y must be zero on entry.
 template <int G>
@@ -882,25 +938,21 @@ namespace {
 
 int fix_parts() { return sms() * kFixPartPerSm; }
 
-// The fixed-point copy of the values (declined when it would take more than
-// half of the free device memory, or when a value is not finite).
+// The fixed-point state of a matrix: the values' exponent bound (declined
+// for a non-finite value or a row longer than kFixMaxRow); the copies of the
+// values are made by fix_copy.
 void fix_build(const ed_crs& a, cudaStream_t st)
 {
-    size_t free_b = 0, total_b = 0;
-    ED_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t need = (size_t)(a.nnz + kCrsPad) * 8 + (size_t)a.n * 8;
-    if (need > free_b / 2 || a.max_row > kFixMaxRow) {
+    if (a.max_row > kFixMaxRow) {
         a.fix_state = -1;
         return;
     }
     auto fq = std::make_unique<ed_fixq>();
     const int P = fix_parts();
     DevBuf<int> part((size_t)P + 1);
-    fq->val.alloc((size_t)(a.nnz + kCrsPad));
-    ED_CUDA(cudaMemsetAsync(fq->val.p + a.nnz, 0, (size_t)kCrsPad * 8, st));
     k_fix_exp<<<P, 256, 0, st>>>(a.val.p, a.nnz, part.p);
     count_launch();
-    k_fix_conv<<<sms() * 8, 256, 0, st>>>(a.val.p, a.nnz, part.p, P, fq->val.p);
+    k_fix_conv<<<1, 256, 0, st>>>(a.val.p, 0, part.p, P, nullptr);   // the bound into part[P]
     count_launch();
     ED_CUDA(cudaGetLastError());
     int ea = 1;
@@ -949,17 +1001,49 @@ ed_fixq::Scratch* fix_scratch(const ed_crs& a, cudaStream_t st)
     return f.scratch.emplace(key, std::move(sc)).first->second.get();
 }
 
+// The values' limb pairs in the CRS order (sell false) or the sliced-ELL
+// order (sell true, after sell_build), made once outside a capture; false
+// when the copy is not there (declined when it would take more than half of
+// the free device memory).
+bool fix_copy(const ed_crs& a, bool sell, cudaStream_t st)
+{
+    ed_fixq& f = *a.fixq;
+    int& state = sell ? f.sval_state : f.val_state;
+    if (state != 0) return state == 1;
+    if (sell && a.sell_state != 1) return false;
+    if (stream_capturing(st)) return false;
+    const int64_t cnt = sell ? a.sell->nnz_pad : a.nnz;
+    size_t free_b = 0, total_b = 0;
+    ED_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if ((size_t)(cnt + kCrsPad) * 8 > free_b / 2) {
+        state = -1;
+        return false;
+    }
+    DevBuf<int64_t>& dst = sell ? f.sval : f.val;
+    dst.alloc((size_t)(cnt + kCrsPad));
+    ED_CUDA(cudaMemsetAsync(dst.p + cnt, 0, (size_t)kCrsPad * 8, st));
+    DevBuf<int> part(2);
+    ED_CUDA(cudaMemcpyAsync(part.p, &f.ea, sizeof(int), cudaMemcpyHostToDevice, st));
+    k_fix_conv<<<sms() * 8, 256, 0, st>>>(sell ? a.sell->val.p : a.val.p, cnt, part.p, 1, dst.p);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+    ED_CUDA(cudaStreamSynchronize(st));
+    state = 1;
+    return true;
+}
+
 bool fix_shape(const ed_crs& a)
 {
     return !a.upper && a.n > 0 && (double)a.nnz >= kSellMaxAvg * (double)a.n;
 }
 
-// The fixed-point copy and this stream's scratch, made when missing and not
-// capturing; false when either is not there.
-bool fix_ready(const ed_crs& a, cudaStream_t st)
+// The fixed-point state, the copy of the values in the wanted order and
+// this stream's scratch, made when missing and not capturing; false when one
+// of them is not there.
+bool fix_ready(const ed_crs& a, cudaStream_t st, bool sell = false)
 {
     if (a.fix_state == 0 && !stream_capturing(st)) fix_build(a, st);
-    return a.fix_state == 1 && fix_scratch(a, st) != nullptr;
+    return a.fix_state == 1 && fix_copy(a, sell, st) && fix_scratch(a, st) != nullptr;
 }
 
 // x's fixed-point copy into the stream's scratch; returns the scratch.
@@ -1006,41 +1090,55 @@ void fix_launch(const ed_crs& a, const double* x, double* y, cudaStream_t st)
     ED_CUDA(cudaGetLastError());
 }
 
+void fix_launch_sell(const ed_crs& a, const double* x, double* y, cudaStream_t st)
+{
+    const ed_fixq& f = *a.fixq;
+    const ed_sell& sl = *a.sell;
+    ed_fixq::Scratch& sc = fix_convert_x(a, x, st);
+    k_spmv_sell_fix<8, 4><<<sms() * 8, 256, 0, st>>>(sl.off.p, sl.len.p, sl.row.p, sl.col.p,
+                                                     reinterpret_cast<const int2*>(f.sval.p),
+                                                     reinterpret_cast<const int2*>(sc.xq.p), sc.part.p + fix_parts(),
+                                                     f.ea, y, sl.nchunks);
+    count_launch();
+    ED_CUDA(cudaGetLastError());
+}
+
 }  // namespace
 
 void spmv_prepare(const ed_crs& a, cudaStream_t st)
 {
-    if (a.n > 0 && !stream_capturing(st) &&
-        (a.product_kernel == 6 || (a.product_kernel == 0 && fix_shape(a)))) {
-        fix_ready(a, st);
+    if (a.n == 0 || stream_capturing(st)) return;
+    const int k = a.product_kernel;
+    if (k == 6 || k == 7 || (k == 0 && fix_shape(a))) fix_ready(a, st);
+    if ((k == 4 || k == 5 || k == 8) && a.sell_state == 0) sell_build(a, st);
+    if (k == 0 && a.sell_state == 0) {
+        // one-level sectors (96 and more elements a row) stay with the row lanes
+        if (a.upper || a.n < kSellMinRows || (double)a.nnz >= kSellMaxAvg * (double)a.n) a.sell_state = -1;
+        else sell_build(a, st);
     }
-    if ((a.product_kernel == 4 || a.product_kernel == 5) && a.sell_state == 0 && a.n > 0 &&
-        !stream_capturing(st)) {
-        sell_build(a, st);
-        return;
-    }
-    if (a.sell_state != 0) return;
-    // one-level sectors (96 and more elements a row) stay with the row lanes
-    if (a.upper || a.n < kSellMinRows || (double)a.nnz >= kSellMaxAvg * (double)a.n) {
-        a.sell_state = -1;
-        return;
-    }
-    if (stream_capturing(st)) return;
-    sell_build(a, st);
+    if ((k == 0 || k == 8) && a.sell_state == 1) fix_ready(a, st, true);
 }
 
 void spmv_kernel(const ed_crs& a, int kernel, const double* x, double* y, cudaStream_t st)
 {
     if (a.n == 0) return;
-    ED_REQUIRE(kernel >= 0 && kernel <= 7, ED_ERR_ARG,
+    ED_REQUIRE(kernel >= 0 && kernel <= 8, ED_ERR_ARG,
                "kernel: 0 (chosen by shape), 1 (row lanes 8x4), 2 / 3 (shared reduction 8x4x2 / 8x2x2), "
                "4 / 5 (sliced ELL, 16 / 8 loads ahead), 6 (fixed-point integer rows 8x8), 7 (the same, rows "
-               "staged in shared memory by bulk copies)");
+               "staged in shared memory by bulk copies), 8 (fixed-point sliced ELL)");
     if (kernel == 0) {
         spmv(a, x, y, st);
         return;
     }
     ED_REQUIRE(!a.upper, ED_ERR_ARG, "the row, sliced-ELL and fixed-point kernels take full storage");
+    if (kernel == 8) {
+        if (a.sell_state == 0 && !stream_capturing(st)) sell_build(a, st);   // any size here
+        ED_REQUIRE(a.sell_state == 1 && fix_ready(a, st, true), ED_ERR_RANGE,
+                   "no fixed-point sliced-ELL copy (a non-finite value, a row of more than 2048 elements, not "
+                   "enough free device memory, or a first product on this stream inside a capture)");
+        fix_launch_sell(a, x, y, st);
+        return;
+    }
     if (kernel == 6 || kernel == 7) {
         ED_REQUIRE(fix_ready(a, st), ED_ERR_RANGE,
                    "no fixed-point copy (a non-finite value, a row of more than 2048 elements, not enough free "
@@ -1101,6 +1199,12 @@ void spmv(const ed_crs& a, const double* x, double* y, cudaStream_t st)
     }
     if (a.sell_state == 0) spmv_prepare(a, st);   // waits for a solver's explicit call while capturing
     if (a.sell_state == 1) {
+        if (fix_ready(a, st, true)) {
+            // the fixed-point sliced ELL (two-level N=8, 2S=21: see
+            // k_spmv_sell_fix), else the FP64 kernel below
+            fix_launch_sell(a, x, y, st);
+            return;
+        }
         // rows of fewer than 96 elements (two-level sectors, small one-level
         // ones), measured on GB300 at two-level N=8, 2S=18 (2.03M rows of 59
         // on average) / 2S=21 (5.90M rows of 73): sliced ELL with 16 loads

@@ -300,7 +300,8 @@ class CrsSparseMatrix:
     def multiply(self, x, y, kernel: int = 0, stream=None):
         """y = A x on device vectors with a chosen product kernel (ed_spmv_kernel:
         0 by shape, 1 row lanes, 2-3 shared-reduction rows, 4-5 sliced ELL,
-        6 fixed-point integer rows, 7 the same with bulk-copy staging)."""
+        6 fixed-point integer rows, 7 the same with bulk-copy staging, 8
+        fixed-point sliced ELL)."""
         check(lib().ed_spmv_kernel(self._h, int(kernel), _dptr(x), _dptr(y), stream))
 
     def device_arrays(self):

@@ -61,7 +61,8 @@ def main():
     ap.add_argument("--products-only", action="store_true", help="two-level / complex: stop after the products")
     ap.add_argument("--kernel", type=int, default=0,
                     help="full-storage product kernel (ed_spmv_kernel): 0 by shape, 1 row lanes, "
-                         "2-3 shared-reduction rows, 4-5 sliced ELL, 6 fixed-point integer rows")
+                         "2-3 shared-reduction rows, 4-5 sliced ELL, 6 fixed-point integer rows, 7 the same "
+                         "with bulk-copy staging, 8 fixed-point sliced ELL")
     ap.add_argument("--fp64-rate", action="store_true", help="measure the FP64 FMA issue rate instead")
     args = ap.parse_args()
     import torch

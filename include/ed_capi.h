@@ -168,11 +168,13 @@ ed_status ed_ham_diagonal(const ed_basis* b, const ed_terms* t, double* diag_dev
 /* y = H x from a stored CRS (either storage).  Device vectors of n doubles.
  * Replaces MatrixVectorFunction::Simple (hamiltonians/matrix_vector_routines.hpp:94-104)
  * -> SymmetricMatrixVectorMultiply (utilities/mathematics/sparse_linear_algebra.hpp:78-168).
- * Full storage with 96 and more elements a row on average (the one-level
- * sectors) uses the fixed-point integer kernel (kernel 6 below): the first
- * product makes a fixed-point copy of the values (8 bytes an element) and,
- * per stream, an n-element scratch for x; products of one matrix on one
- * stream must not overlap (they share that stream's scratch). */
+ * Full storage uses the fixed-point integer kernels (kernel 6 below for 96
+ * and more elements a row on average, the one-level sectors; kernel 8 on
+ * the sliced-ELL copy for shorter rows from 4096 rows up, the two-level
+ * sectors): the first product makes a fixed-point copy of the values (8
+ * bytes an element) and, per stream, an n-element scratch for x; products of
+ * one matrix on one stream must not overlap (they share that stream's
+ * scratch). */
 ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream stream);
 
 /* The same product with a chosen kernel of the full storage, for measuring
@@ -188,9 +190,11 @@ ed_status ed_spmv(const ed_crs* a, const double* x_dev, double* y_dev, ed_stream
  * entry of x gives NaN in every entry of y; 7 the same arithmetic with the
  * rows' values and columns streamed into shared memory by bulk copies (a
  * producer warp and a ring of stages of 16 rows, one consumer warp a row;
- * the same bits as 6).  ED_ERR_ARG for 1-7 on upper-triangle storage;
- * ED_ERR_RANGE for 4-7 when the copy does not fit in half the free device
- * memory, for 6-7 also when a value is not finite, a row has more than 2048
+ * the same bits as 6); 8 the same arithmetic over the sliced-ELL copy (one
+ * lane a row; the same bits as 6; the default for rows shorter than 96
+ * elements on average).  ED_ERR_ARG for 1-8 on upper-triangle storage;
+ * ED_ERR_RANGE for 4-8 when the copy does not fit in half the free device
+ * memory, for 6-8 also when a value is not finite, a row has more than 2048
  * elements, or the stream's first product is inside a capture.  The values
  * must not change after the first product (the copies are made once). */
 ed_status ed_spmv_kernel(const ed_crs* a, int kernel, const double* x_dev, double* y_dev, ed_stream stream);

@@ -58,7 +58,7 @@ def test_row_kernels_match_oracle(cuda, oracle, case):
     scale = np.abs(uval).max() * np.abs(x).max() * 50
     H, _ = setup(N, norb, tlz, pp)
     xd = torch.from_numpy(x).cuda()
-    for kernel in range(1, 8):
+    for kernel in range(1, 9):
         yd = torch.full_like(xd, np.nan)
         H.m_crsSparseMatrix.multiply(xd, yd, kernel)
         torch.cuda.synchronize()
@@ -145,7 +145,7 @@ def test_fixed_point_product_is_exactly_rounded(cuda, case):
     for x in xs:
         xd = torch.from_numpy(x).cuda()
         ref = _fix_product(rp, col, val, x).view(np.uint64)
-        for kernel in (6, 7):          # registers, and rows staged in shared memory
+        for kernel in (6, 7, 8):       # rows in registers, staged in shared memory, sliced ELL
             yd = torch.full_like(xd, np.nan)
             H.m_crsSparseMatrix.multiply(xd, yd, kernel)
             torch.cuda.synchronize()

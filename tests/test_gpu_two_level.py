@@ -206,3 +206,27 @@ def test_diagonal_two_level_matrix_from_its_diagonal(cuda, oracle, upper):
         assert np.max(np.abs(H.m_eigenvalues - want)) <= 1e-12
         V = H.m_eigenvectors
         assert np.allclose(V @ V.T, np.eye(6)) and np.array_equal(np.abs(V).sum(axis=1), np.ones(6))
+
+
+def test_two_level_product_takes_the_fixed_point_sliced_ell(cuda, oracle):
+    # a two-level sector with short rows and more than 4096 of them: the
+    # default product is the fixed-point sliced ELL, bit-identical to the
+    # fixed-point row kernel (both round each row's exact sum once) and within
+    # 1e-13 of the FP64 kernels
+    torch = cuda
+    t0, t1 = tables(oracle, 11, 31)
+    H = build(6, 11, 0, t0, t1, upper=False)    # 6,902 states
+    crs = H.m_crsSparseMatrix
+    n = crs.GetNbrRows()
+    assert n >= 4096 and crs.GetNbrNonZeros() < 96 * n
+    x = np.random.default_rng(16).uniform(-1, 1, n)
+    xd = torch.from_numpy(x).cuda()
+    ys = {}
+    for kernel in (0, 4, 6, 8):
+        y = torch.full_like(xd, np.nan)
+        crs.multiply(xd, y, kernel)
+        torch.cuda.synchronize()
+        ys[kernel] = y
+    assert torch.equal(ys[0], ys[8]) and torch.equal(ys[6], ys[8])
+    _, _, val = crs.to_host()
+    assert torch.max(torch.abs(ys[4] - ys[8])).item() <= 1e-13 * np.abs(val).max() * 50
