@@ -5,20 +5,22 @@
 //   y[i] += a*x[c]; if (i != c) y[c] += a*x[i]   over the stored upper triangle.
 //
 // On GB300 the FP64 pipe issues about 0.53e12 FMA/s (ed_fp64_fma_rate), less
-// than streaming the CRS at HBM rate (12 bytes per element) demands, so the
-// products are FP64-bound before they are HBM-bound and spend FP64
-// instructions only where they must: one FMA per element, as few additions
-// as the reduction allows, and no FP64 instruction issued for lanes with no
-// element.  Full storage takes one of two layouts:
-//  - rows of 96 and more elements (the one-level sectors): k_spmv_rows, 8
-//    lanes on each of two consecutive rows, each lane one FMA chain over its
-//    share of the row, the two rows' sums reduce-scattered (12 additions a
-//    row instead of 24);
-//  - shorter rows (two-level sectors): k_spmv_sell over a sliced-ELL copy
+// than streaming the CRS at HBM rate (12 bytes per element) demands, so an
+// FP64 product is FP64-bound before it is HBM-bound.  The default products of
+// full storage therefore run on the integer pipes in exact fixed-point
+// arithmetic (ed_fixed.cuh: values and x in 58-bit fixed point, exact 128-bit
+// row sums, one rounding to FP64), in one of two layouts:
+//  - rows of 96 and more elements (the one-level sectors): k_spmv_fix, 8
+//    lanes a row, each lane's exact sum over its share of the row, the lanes'
+//    sums added exactly;
+//  - shorter rows (two-level sectors): k_spmv_sell_fix over a sliced-ELL copy
 //    (rows sorted by length within windows, chunks of 32 rows transposed), one
 //    lane a row, no reduction, and the lanes of a chunk finish together.
-// Column and value streams are read once with evict-first loads so that x
-// stays resident in L2.
+// Both give the same bits.  The FP64 kernels (k_spmv_full, k_spmv_rows,
+// k_spmv_sell) remain as selectable alternatives, spending FP64 instructions
+// only where they must: one FMA per element, as few additions as the
+// reduction allows, none for lanes with no element.  Column and value streams
+// are read once with evict-first loads so that x stays resident in L2.
 #include <algorithm>
 #include <cmath>
 #include <string>
